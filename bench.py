@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark: ms per 256^3 pressure-Poisson solve to 1e-10 relative residual,
+FP32-in-FP64 multigrid vs FP64 multigrid, on one GB300.
+
+Workload (one step = one pressure solve): the 256^3 rising-bubble projection
+case -- one sphere of radius 0.2 at (0.5, 0.5, 0.3) in [0,1]^3, density 1 in
+the bubble and 1000 outside through the smoothed Heaviside (half width 1.5 dx),
+b = div(u*)/dt with u* ~ N(0,1), dt = 1e-3, Neumann walls, zero-mean pressure.
+A step sets the operator from the level set (density, face coefficients,
+coarse levels, coarse inverse) and solves from a zero initial guess to
+||b - A p|| / ||b|| < 1e-10.
+
+Arms:
+  default            this repo's CUDA path (device-resident inputs; value = mixed
+                     precision ms per solve, FP64 beside it), plus the e2e run
+                     through the C ABI with pinned host buffers, a per-kernel
+                     profile pass for the roofline, and the CPU baseline (the
+                     oracle on the host cores).
+  --impl reference   the reference's own algorithm on the host cores: the FP64
+                     multigrid with lexicographic Gauss-Seidel in OpenMP subdomains
+                     (the oracle's restatement; the Fortran reference cannot be
+                     built here).
+
+Prints one JSON line (rank 0).  Under torchrun each rank solves its own copy
+(replicas, weak scaling); value = max-over-ranks time / (steps * ranks).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per 256³ Poisson solve to 1e-10 rel. residual: FP32-in-FP64 vs FP64 MG"
+TOL = 1e-10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1, help="synthetic case index (1 = 256^3 sphere)")
+    ap.add_argument("--scale", type=int, default=1, help="divide every axis by this (quick runs)")
+    ap.add_argument("--krylov", action="store_true", help="flexible CG around the V-cycle")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_desc(case):
+    nz, ny, nx = case.shape
+    return (f"{case.name}: {nx}x{ny}x{nz} cells, {len(case.radii)} bubble(s), density ratio "
+            f"{case.rho_pos / case.rho_neg:g}, eps=1.5dx, u*~N(0,1) seed {case.seed}, dt={case.dt:g}, "
+            f"tol {TOL:g} relative residual, zero initial guess")
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """dram bytes per fine cell per launch, per kernel class, from an ncu capture
+    summarised in profiles/ (None when no capture was made)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# algorithmic bytes per fine cell per launch of each kernel class (w = word size)
+def algorithmic_bytes_per_cell(cls, w):
+    return {
+        "smooth_fine": 3.0 * w,                 # half sweep of the 6w/cell sweep (p, b, bx, by, bz, p')
+        "restrict_fine": 5.0 * w + 2.0 * w / 8,  # p, b, bx, by, bz -> coarse b, sol
+        "prolong_fine": 2.0 * w + w / 8,         # p r/w + coarse e
+        "residual": 40.0 + (4.0 if w == 4 else 0.0),  # FP64 p, b, bx, by, bz (+ FP32 r)
+    }.get(cls)
+
+
+def run_reference(args):
+    """The reference's FP64 multigrid on the host cores (oracle restatement)."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from fortrancfd_gb300 import inputs
+    from oracle import oracle as orc
+
+    case = inputs.config(args.config, args.scale)
+    phi = inputs.level_set(case)
+    u, v, w = inputs.velocity(case)
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    blocks = _factor3(threads)
+    times, cycles = [], []
+
+    def step():
+        rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
+        coef = orc.face_coef(rho, case.spacing)
+        b = orc.divergence(u, v, w, case.dt, case.spacing)
+        t0 = time.perf_counter()
+        p, st = orc.mg_solve(coef, b, tol=TOL, smoother=1, blocks=blocks)
+        return (time.perf_counter() - t0) * 1e3, st
+
+    for _ in range(args.warmup):
+        step()
+    for _ in range(args.steps):
+        ms, st = step()
+        times.append(ms)
+        cycles.append(st["cycles"])
+    value = float(np.mean(times))
+    sample = (f"{args.steps} full FP64 solves of {case.name}, lexicographic Gauss-Seidel V(2,2) in "
+              f"{blocks[0]}x{blocks[1]}x{blocks[2]} OpenMP subdomains, {cycles[-1]} cycles each")
+    line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload_desc(case), "grid": list(case.shape[::-1]), "tol": TOL,
+                       "cycles": cycles[-1]},
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _factor3(n):
+    """Split n threads into a 3D subdomain grid (largest factors on z, then y)."""
+    best = (1, 1, n)
+    for a in range(1, n + 1):
+        if n % a:
+            continue
+        for b in range(a, n + 1):
+            if (n // a) % b:
+                continue
+            c = n // a // b
+            if c >= b and (c - a) < (best[2] - best[0]):
+                best = (a, b, c)
+    return best
+
+
+def cpu_baseline(case, phi, u, v, w, budget_s):
+    """The oracle's FP64 multigrid (red-black, all host threads), full solves
+    until the sample budget is spent (at least one)."""
+    from oracle import oracle as orc
+
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
+    coef = orc.face_coef(rho, case.spacing)
+    b = orc.divergence(u, v, w, case.dt, case.spacing)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        _, st = orc.mg_solve(coef, b, tol=TOL)
+        times.append((time.perf_counter() - t0) * 1e3)
+        if time.perf_counter() - t_start > budget_s * 0.5:
+            break
+    return {"value": float(np.mean(times)), "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full FP64 red-black V(2,2) solve(s) of the same case on "
+                      f"{threads} threads, {st['cycles']} cycles each (oracle restatement)"}
+
+
+def run_ours(args):
+    import torch
+
+    from fortrancfd_gb300 import PressurePoisson, inputs
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    case = inputs.config(args.config, args.scale)
+    phi_h = inputs.level_set(case)
+    u_h, v_h, w_h = inputs.velocity(case)
+    n = int(np.prod(case.shape))
+    stream = torch.cuda.Stream(device=dev)
+
+    def dev_t(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+    phi = dev_t(phi_h)
+    u, v, w = dev_t(u_h), dev_t(v_h), dev_t(w_h)
+    kw = dict(krylov=args.krylov, stream=stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(solver, steps, warmup, b, p, sample_clocks=False):
+        def step():
+            p.zero_()
+            solver.rho_mu(phi, case.eps, case.rho_pos, case.rho_neg)
+            _, st = solver.solve(b, p, tol=TOL)
+            return st
+
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                st = step()
+            barrier()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            launches0 = solver.kernel_launches
+            sampler = ClockSampler(dev.index if dev.index is not None else 0)
+            with (sampler if sample_clocks else _Null()):
+                e0.record(stream)
+                for _ in range(steps):
+                    st = step()
+                e1.record(stream)
+                torch.cuda.synchronize()
+            barrier()
+            ms = e0.elapsed_time(e1)
+            launches = solver.kernel_launches - launches0
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, st, launches, (sampler.summary() if sample_clocks else None)
+
+    with torch.cuda.stream(stream):
+        b = torch.empty(case.shape, dtype=torch.float64, device=dev)
+        p = torch.zeros_like(b)
+    mixed = PressurePoisson(case.shape, case.spacing, precision="mixed", **kw)
+    mixed.divergence(u, v, w, case.dt, out=b)
+    ms_mixed, st_mixed, launches, clocks = timed(mixed, args.steps, args.warmup, b, p,
+                                                 sample_clocks=True)
+    per_solve = ms_mixed / args.steps / world
+    p_mixed = p.clone()
+
+    fp64 = None
+    if not args.no_fp64:
+        s64 = PressurePoisson(case.shape, case.spacing, precision="fp64", **kw)
+        ms64, st64, _, _ = timed(s64, max(1, args.steps // 2), max(1, args.warmup // 2), b, p)
+        fp64 = {"ms_per_solve": ms64 / max(1, args.steps // 2) / world, "cycles": st64["cycles"],
+                "rel_residual": st64["rel_residual"],
+                "p_rel_diff_vs_mixed": float((p - p_mixed).norm() / p.norm())}
+        s64.close()
+
+    # per-kernel profile pass (eager launches bracketed by CUDA events)
+    roofline = None
+    prof = None
+    if not args.no_profile:
+        with torch.cuda.stream(stream):
+            mixed.set_profiling(True)
+            p.zero_()
+            mixed.rho_mu(phi, case.eps, case.rho_pos, case.rho_neg)
+            mixed.solve(b, p, tol=TOL)
+            prof = mixed.profile()
+            mixed.set_profiling(False)
+        total = sum(v[0] for v in prof.values())
+        ranked = sorted(((k, v) for k, v in prof.items() if algorithmic_bytes_per_cell(k, 4)),
+                        key=lambda kv: -kv[1][0])
+        cls, (ms_cls, cnt) = ranked[0]
+        per_launch_ms = ms_cls / max(cnt, 1)
+        alg = algorithmic_bytes_per_cell(cls, 4) * n
+        peak, peak_kind = measured_peaks()
+        achieved = alg / (per_launch_ms * 1e-3) / 1e9
+        tr = traffic_per_cell().get(cls)
+        roofline = {"kernel": cls, "bound": "hbm", "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                    "traffic": (tr * n if tr else None), "launch_ms": per_launch_ms,
+                    "share": ms_cls / total if total else None,
+                    "algorithmic_bytes_per_launch": alg}
+
+    e2e = None
+    if not args.no_e2e:
+        # through the C ABI with pinned host buffers: H2D of phi, b and the
+        # initial p, D2H of p, every step
+        phi_p = torch.from_numpy(np.ascontiguousarray(phi_h)).pin_memory()
+        b_p = b.cpu().pin_memory()
+        p_p = torch.zeros(case.shape, dtype=torch.float64).pin_memory()
+        with torch.cuda.stream(stream):
+            def e2e_step():
+                p_p.zero_()
+                mixed.rho_mu(phi_p, case.eps, case.rho_pos, case.rho_neg)
+                _, st = mixed.solve(b_p, p_p, tol=TOL)
+                return st
+            for _ in range(max(1, args.warmup)):
+                e2e_step()
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                st_e = e2e_step()
+            torch.cuda.synchronize()
+            barrier()
+            wall = (time.perf_counter() - t0) * 1e3
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([wall], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            wall = float(t.item())
+        e2e = {"value": wall / args.steps / world, "unit": "ms", "h2d_bytes_per_step": 3 * 8 * n,
+               "d2h_bytes_per_step": 8 * n, "timing": "host wall clock around synchronous C-ABI calls",
+               "rel_residual": st_e["rel_residual"]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
+
+    if rank == 0:
+        ws_gb = n * 8 * 9 / 1e9
+        line = {"metric": METRIC, "value": per_solve, "unit": "ms", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32-in-f64", "data": "synthetic",
+                "config": {"workload": workload_desc(case), "grid": list(case.shape[::-1]),
+                           "tol": TOL, "cycles": st_mixed["cycles"],
+                           "rel_residual": st_mixed["rel_residual"],
+                           "precision": "FP32 V(2,2) cycles inside FP64 defect correction",
+                           "krylov": bool(args.krylov),
+                           "fp64": fp64,
+                           "mixed_over_fp64": (per_solve / fp64["ms_per_solve"]) if fp64 else None,
+                           "l2": f"inputs larger than L2: working set ~{ws_gb:.2f} GB vs 0.129 GB L2, "
+                                 "each FP64 field alone exceeds it",
+                           "parallelism": f"replicas x{world}"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": launches}
+        if prof:
+            line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

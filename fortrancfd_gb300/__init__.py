@@ -1,0 +1,12 @@
+"""GB300-native pressure-Poisson multigrid for the two-phase solvers of
+ntu-d09525007/FortranCFD.
+
+The product is libgbmg.so (CUDA kernels for sm_103a + the C ABI of
+include/gbmg.h).  This package holds its sources (csrc/), the in-tree build
+recipe (build.py), the ctypes binding (_lib.py), the host-side mirror of the
+reference's pressure routine (ppe.py), the differentiable solve (autograd.py)
+and the seeded synthetic inputs (inputs.py).
+"""
+from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
+
+__all__ = ["PressurePoisson", "ConvergenceError", "GBMGError"]

@@ -1,0 +1,1023 @@
+// Host orchestration and C ABI of the GB300 pressure-Poisson multigrid.
+//
+// One handle owns the device hierarchy of one grid: FP64 face coefficients on
+// every level (plus 1/diagonal for the FP64 smoother), FP32 copies for the
+// mixed-precision cycle, cycle vectors, the dense coarsest-level inverse and
+// the reduction scratch.  A solve is a loop of cycles; each cycle (V-cycle,
+// FP64 residual and its norm, and the 8-byte copy of the norm to pinned host
+// memory) is captured once as a CUDA graph and replayed, and the host reads
+// one scalar per cycle to decide whether to stop.
+//
+// Reference call shape: ppe_sor_init; ppe_sor_solver(tol) -> ns_momentum_correction
+// ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-205"),
+// with the cycle of "DomainDecomposition/3D/src/others/multigrid_solver.f90"
+// and the outer loop of ppe_mg_solver
+// ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90:17-50").
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "gbmg.h"
+#include "gbmg_internal.h"
+
+using namespace gbmg;
+
+namespace {
+
+struct Level {
+  int nx = 0, ny = 0, nz = 0;
+  int fx = 1, fy = 1, fz = 1;
+  size_t n = 0;
+  double *cx = nullptr, *cy = nullptr, *cz = nullptr, *idiag = nullptr;
+  double *sol = nullptr, *src = nullptr;  // owned on levels >= 1
+  float *cx32 = nullptr, *cy32 = nullptr, *cz32 = nullptr;
+  float *sol32 = nullptr, *src32 = nullptr;
+};
+
+enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
+
+}  // namespace
+
+struct gbmg_handle {
+  gbmg_grid grid{};
+  gbmg_params prm{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int L = 0;
+  Level lv[kMaxLevels];
+  size_t n0 = 0;
+  bool mixed = false;
+  // fine-level buffers
+  double* b = nullptr;    // mean-free right-hand side
+  double* p = nullptr;    // pressure being solved for
+  double* rho = nullptr;  // cell density of the current operator
+  double* vel[3] = {nullptr, nullptr, nullptr};
+  size_t vel_n[3] = {0, 0, 0};
+  // flexible CG vectors (allocated when krylov = 1)
+  double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
+  // coarsest level
+  int nc = 0;
+  double *minv = nullptr, *adense = nullptr;
+  float *minv32 = nullptr, *adense32 = nullptr;
+  // reductions
+  ReduceScratch red{};
+  double* host_res = nullptr;  // pinned mirror of red.result
+  // graphs
+  cudaGraphExec_t graph = nullptr;
+  int graph_kind = kGraphNone;
+  int64_t graph_kernels = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int64_t launches = 0;
+  // profiling: event pairs around launches, summed per kernel class
+  bool prof = false;
+  cudaEvent_t pev[2 * 512] = {};
+  int pcls[512] = {};
+  int pused = 0;
+  double prof_ms[GBMG_PROF_CLASSES] = {};
+  int64_t prof_n[GBMG_PROF_CLASSES] = {};
+  bool coef_ready = false;
+  bool rho_ready = false;
+  std::string err;
+};
+
+namespace {
+
+#define GB_CUDA(h, call)                                                        \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return e_ == cudaErrorMemoryAllocation ? GBMG_OUT_OF_MEMORY : GBMG_CUDA_ERROR; \
+    }                                                                           \
+  } while (0)
+
+#define GB_TRY(expr)            \
+  do {                          \
+    int rc_ = (expr);           \
+    if (rc_ != GBMG_OK) return rc_; \
+  } while (0)
+
+int check_launch(gbmg_handle* h, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return GBMG_CUDA_ERROR;
+  }
+  return GBMG_OK;
+}
+
+// Sum the recorded event pairs into the per-class totals (syncs the stream).
+void prof_flush(gbmg_handle* h) {
+  if (!h->pused) return;
+  cudaStreamSynchronize(h->stream);
+  for (int i = 0; i < h->pused; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->pev[2 * i], h->pev[2 * i + 1]) == cudaSuccess) {
+      h->prof_ms[h->pcls[i]] += ms;
+      h->prof_n[h->pcls[i]] += 1;
+    }
+  }
+  h->pused = 0;
+}
+
+void prof_begin(gbmg_handle* h) {
+  if (!h->prof) return;
+  if (h->pused == 512) prof_flush(h);
+  cudaEvent_t& e = h->pev[2 * h->pused];
+  if (!e) cudaEventCreate(&e);
+  cudaEventRecord(e, h->stream);
+}
+
+void prof_end(gbmg_handle* h, int cls) {
+  h->launches += 1;
+  if (!h->prof) return;
+  cudaEvent_t& e = h->pev[2 * h->pused + 1];
+  if (!e) cudaEventCreate(&e);
+  cudaEventRecord(e, h->stream);
+  h->pcls[h->pused++] = cls;
+}
+
+// One kernel launch, counted and (when profiling) timed as class `cls`.
+#define LAUNCH(h, cls, stmt) \
+  do {                       \
+    prof_begin(h);           \
+    stmt;                    \
+    prof_end(h, cls);        \
+  } while (0)
+
+template <typename T>
+int dmalloc(gbmg_handle* h, T** ptr, size_t n) {
+  *ptr = nullptr;
+  GB_CUDA(h, cudaMalloc((void**)ptr, (n ? n : 1) * sizeof(T)));
+  return GBMG_OK;
+}
+
+template <typename T>
+void dfree(T*& ptr) {
+  if (ptr) cudaFree((void*)ptr);
+  ptr = nullptr;
+}
+
+// Level plan, the same rule as the oracle: every axis with more than one cell
+// halves per level; auto mode stops at <= coarse_max cells or when an axis is
+// odd; explicit levels require divisibility (manager_init,
+// "DomainDecomposition/3D/lib/data/branches.f90:172-216").
+int plan_levels(const gbmg_grid& g, int levels, int coarse_max, int dims[][3]) {
+  int n[3] = {g.nx, g.ny, g.nz};
+  int L = 1;
+  dims[0][0] = n[0]; dims[0][1] = n[1]; dims[0][2] = n[2];
+  for (;;) {
+    if (levels > 0 && L >= levels) break;
+    if (levels <= 0 && (long)n[0] * n[1] * n[2] <= coarse_max) break;
+    bool ok = true, any = false;
+    for (int a = 0; a < 3; ++a)
+      if (n[a] > 1) { any = true; if (n[a] % 2) ok = false; }
+    if (!ok || !any) {
+      if (levels > 0) return -1;
+      break;
+    }
+    for (int a = 0; a < 3; ++a)
+      if (n[a] > 1) n[a] /= 2;
+    if (L >= kMaxLevels) return -1;
+    dims[L][0] = n[0]; dims[L][1] = n[1]; dims[L][2] = n[2];
+    ++L;
+  }
+  return L;
+}
+
+LevelView<double> v64(const Level& l) {
+  return LevelView<double>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx, l.cy, l.cz, l.idiag, l.sol, l.src};
+}
+LevelView<float> v32(const Level& l) {
+  return LevelView<float>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
+                          l.sol32, l.src32};
+}
+template <typename T>
+LevelView<T> view(const Level& l);
+template <>
+LevelView<double> view<double>(const Level& l) { return v64(l); }
+template <>
+LevelView<float> view<float>(const Level& l) { return v32(l); }
+
+template <typename T> const T* minv_of(const gbmg_handle* h);
+template <> const double* minv_of<double>(const gbmg_handle* h) { return h->minv; }
+template <> const float* minv_of<float>(const gbmg_handle* h) { return h->minv32; }
+template <typename T> const T* adense_of(const gbmg_handle* h);
+template <> const double* adense_of<double>(const gbmg_handle* h) { return h->adense; }
+template <> const float* adense_of<float>(const gbmg_handle* h) { return h->adense32; }
+
+// One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
+// the post-smoothing colours black-first (symmetric preconditioner for CG).
+template <typename T>
+int enqueue_vcycle(gbmg_handle* h, bool reverse_post) {
+  const int L = h->L;
+  const cudaStream_t s = h->stream;
+  for (int l = 0; l < L - 1; ++l) {
+    const LevelView<T> V = view<T>(h->lv[l]);
+    const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
+    for (int it = 0; it < h->prm.nu1; ++it) {
+      LAUNCH(h, cs, launch_smooth<T>(s, V, 0));
+      LAUNCH(h, cs, launch_smooth<T>(s, V, 1));
+    }
+    LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
+           launch_restrict<T>(s, V, view<T>(h->lv[l + 1])));
+  }
+  const Level& c = h->lv[L - 1];
+  const LevelView<T> C = view<T>(c);
+  LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
+         launch_coarse_solve<T>(s, h->nc, minv_of<T>(h), adense_of<T>(h), C.src, C.sol));
+  for (int l = L - 2; l >= 0; --l) {
+    const LevelView<T> V = view<T>(h->lv[l]);
+    const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
+    LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
+           launch_prolong<T>(s, V, view<T>(h->lv[l + 1])));
+    for (int it = 0; it < h->prm.nu2; ++it) {
+      LAUNCH(h, cs, launch_smooth<T>(s, V, reverse_post ? 1 : 0));
+      LAUNCH(h, cs, launch_smooth<T>(s, V, reverse_post ? 0 : 1));
+    }
+  }
+  return check_launch(h, "v-cycle");
+}
+
+// Algorithmic HBM bytes of one V-cycle (each array touched once per kernel).
+double vcycle_bytes(const gbmg_handle* h, int w) {
+  double bytes = 0.0;
+  const bool idiag = (w == 8);
+  for (int l = 0; l < h->L - 1; ++l) {
+    const double n = (double)h->lv[l].n, nc = (double)h->lv[l + 1].n;
+    const double sweep = (idiag ? 7.0 : 6.0) * w * n;  // p r/w, b, cx, cy, cz (+ 1/diag)
+    bytes += (h->prm.nu1 + h->prm.nu2) * sweep;
+    bytes += 5.0 * w * n + 2.0 * w * nc;  // restrict: p, b, cx, cy, cz -> coarse b, sol
+    bytes += 2.0 * w * n + w * nc;        // prolong: p r/w, coarse e
+  }
+  bytes += 2.0 * w * h->nc + (double)w * h->nc * h->nc;
+  return bytes;
+}
+
+int reset_graph(gbmg_handle* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  h->graph = nullptr;
+  h->graph_kind = kGraphNone;
+  h->graph_kernels = 0;
+  return GBMG_OK;
+}
+
+int free_all(gbmg_handle* h) {
+  reset_graph(h);
+  for (int l = 0; l < h->L; ++l) {
+    Level& v = h->lv[l];
+    dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
+    if (l > 0) { dfree(v.sol); dfree(v.src); }
+    dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.src32);
+  }
+  dfree(h->b); dfree(h->p); dfree(h->rho);
+  for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
+  dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
+  dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32);
+  dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
+  if (h->host_res) cudaFreeHost(h->host_res);
+  h->host_res = nullptr;
+  for (int i = 0; i < 2 * 512; ++i)
+    if (h->pev[i]) cudaEventDestroy(h->pev[i]);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  h->ev0 = h->ev1 = nullptr;
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  h->stream = nullptr;
+  return GBMG_OK;
+}
+
+int allocate(gbmg_handle* h) {
+  int dims[kMaxLevels][3];
+  const int L = plan_levels(h->grid, h->prm.levels, h->prm.coarse_max, dims);
+  if (L < 1) {
+    h->err = "grid cannot be coarsened to the requested level count";
+    return GBMG_INVALID_ARG;
+  }
+  const int nc = dims[L - 1][0] * dims[L - 1][1] * dims[L - 1][2];
+  if (nc > kMaxCoarse) {
+    h->err = "coarsest level has " + std::to_string(nc) + " cells; the dense coarse solve takes at most " +
+             std::to_string(kMaxCoarse) + " (use more levels or a grid with more factors of 2)";
+    return GBMG_INVALID_ARG;
+  }
+  h->L = L;
+  h->nc = nc;
+  const bool need64 = !h->mixed || h->prm.krylov;
+  for (int l = 0; l < L; ++l) {
+    Level& v = h->lv[l];
+    v.nx = dims[l][0]; v.ny = dims[l][1]; v.nz = dims[l][2];
+    v.n = (size_t)v.nx * v.ny * v.nz;
+    if (l + 1 < L) {
+      v.fx = v.nx / dims[l + 1][0]; v.fy = v.ny / dims[l + 1][1]; v.fz = v.nz / dims[l + 1][2];
+    } else {
+      v.fx = v.fy = v.fz = 1;
+    }
+    GB_TRY(dmalloc(h, &v.cx, v.n));
+    GB_TRY(dmalloc(h, &v.cy, v.n));
+    GB_TRY(dmalloc(h, &v.cz, v.n));
+    if (!h->mixed) GB_TRY(dmalloc(h, &v.idiag, v.n));
+    if (l > 0 && !h->mixed) {
+      GB_TRY(dmalloc(h, &v.sol, v.n));
+      GB_TRY(dmalloc(h, &v.src, v.n));
+    }
+    if (h->mixed) {
+      GB_TRY(dmalloc(h, &v.cx32, v.n));
+      GB_TRY(dmalloc(h, &v.cy32, v.n));
+      GB_TRY(dmalloc(h, &v.cz32, v.n));
+      GB_TRY(dmalloc(h, &v.sol32, v.n));
+      GB_TRY(dmalloc(h, &v.src32, v.n));
+    }
+  }
+  (void)need64;
+  h->n0 = h->lv[0].n;
+  GB_TRY(dmalloc(h, &h->b, h->n0));
+  GB_TRY(dmalloc(h, &h->p, h->n0));
+  GB_TRY(dmalloc(h, &h->rho, h->n0));
+  if (h->prm.krylov) {
+    GB_TRY(dmalloc(h, &h->kr, h->n0));
+    GB_TRY(dmalloc(h, &h->kz, h->n0));
+    GB_TRY(dmalloc(h, &h->kzold, h->n0));
+    GB_TRY(dmalloc(h, &h->kd, h->n0));
+    GB_TRY(dmalloc(h, &h->kq, h->n0));
+  }
+  GB_TRY(dmalloc(h, &h->minv, (size_t)nc * nc));
+  GB_TRY(dmalloc(h, &h->adense, (size_t)nc * nc));
+  GB_TRY(dmalloc(h, &h->minv32, (size_t)nc * nc));
+  GB_TRY(dmalloc(h, &h->adense32, (size_t)nc * nc));
+  const size_t rows = (size_t)h->lv[0].ny * h->lv[0].nz;
+  const int mb = std::max(reduce_blocks_for(rows), reduce_blocks_for(h->n0));
+  h->red.max_blocks = mb;
+  GB_TRY(dmalloc(h, &h->red.partials, (size_t)kRedValues * mb));
+  GB_TRY(dmalloc(h, &h->red.counter, 1));
+  GB_TRY(dmalloc(h, &h->red.result, kRedSlots));
+  GB_CUDA(h, cudaMemsetAsync(h->red.counter, 0, sizeof(unsigned int), h->stream));
+  GB_CUDA(h, cudaMemsetAsync(h->red.result, 0, kRedSlots * sizeof(double), h->stream));
+  GB_CUDA(h, cudaMallocHost((void**)&h->host_res, kRedSlots * sizeof(double)));
+  GB_CUDA(h, cudaEventCreate(&h->ev0));
+  GB_CUDA(h, cudaEventCreate(&h->ev1));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+bool dense_cells(const gbmg_field& f, int nx, int ny) {
+  return f.sy == nx && f.sz == (int64_t)nx * ny;
+}
+
+// Copy a field of extent (ex, ey, ez) into a dense device buffer.
+int upload(gbmg_handle* h, const gbmg_field& f, int ex, int ey, int ez, int mem, double* dst) {
+  if (!f.data) {
+    h->err = "null field";
+    return GBMG_INVALID_ARG;
+  }
+  const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  if (dense_cells(f, ex, ey)) {
+    GB_CUDA(h, cudaMemcpyAsync(dst, f.data, (size_t)ex * ey * ez * sizeof(double), kind, h->stream));
+  } else if (mem == GBMG_MEM_DEVICE) {
+    launch_copy_in(h->stream, ex, ey, ez, Strided{f.data, f.sy, f.sz}, dst);
+    h->launches += 1;
+    GB_TRY(check_launch(h, "copy_in"));
+  } else {
+    for (int k = 0; k < ez; ++k)
+      GB_CUDA(h, cudaMemcpy2DAsync(dst + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
+                                   f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
+                                   (size_t)ex * sizeof(double), (size_t)ey, kind, h->stream));
+  }
+  return GBMG_OK;
+}
+
+int download(gbmg_handle* h, const double* src, int ex, int ey, int ez, int mem,
+             const gbmg_field& f) {
+  const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (dense_cells(f, ex, ey)) {
+    GB_CUDA(h, cudaMemcpyAsync(f.data, src, (size_t)ex * ey * ez * sizeof(double), kind, h->stream));
+  } else if (mem == GBMG_MEM_DEVICE) {
+    launch_copy_out(h->stream, ex, ey, ez, src, f.data, f.sy, f.sz);
+    h->launches += 1;
+    GB_TRY(check_launch(h, "copy_out"));
+  } else {
+    for (int k = 0; k < ez; ++k)
+      GB_CUDA(h, cudaMemcpy2DAsync(f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
+                                   src + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
+                                   (size_t)ex * sizeof(double), (size_t)ey, kind, h->stream));
+  }
+  return GBMG_OK;
+}
+
+// Coarse levels, 1/diagonal, FP32 copies and the coarse inverse from the
+// level-0 FP64 coefficients.
+int build_hierarchy(gbmg_handle* h) {
+  const cudaStream_t s = h->stream;
+  for (int l = 1; l < h->L; ++l) {
+    Level& c = h->lv[l];
+    LAUNCH(h, GBMG_PROF_SETUP, launch_coarsen(s, v64(h->lv[l - 1]), c.cx, c.cy, c.cz, c.nx, c.ny, c.nz));
+  }
+  for (int l = 0; l < h->L; ++l) {
+    Level& v = h->lv[l];
+    if (v.idiag) LAUNCH(h, GBMG_PROF_SETUP, launch_idiag(s, v64(v), v.idiag));
+    if (v.cx32) {
+      LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cx, v.cx32, v.n));
+      LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cy, v.cy32, v.n));
+      LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cz, v.cz32, v.n));
+    }
+  }
+  LAUNCH(h, GBMG_PROF_SETUP,
+         launch_coarse_invert(s, v64(h->lv[h->L - 1]), h->minv, h->adense, h->minv32, h->adense32));
+  GB_TRY(check_launch(h, "hierarchy"));
+  h->coef_ready = true;
+  return GBMG_OK;
+}
+
+int set_rho_device(gbmg_handle* h) {
+  const gbmg_grid& g = h->grid;
+  Level& f = h->lv[0];
+  LAUNCH(h, GBMG_PROF_SETUP,
+         launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
+                          h->rho, f.cx, f.cy, f.cz));
+  GB_TRY(check_launch(h, "face_coef"));
+  h->rho_ready = true;
+  return build_hierarchy(h);
+}
+
+// b -> h->b with the mean removed (when asked); result[kSlotSumB+1] = |b|^2.
+int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
+  const gbmg_grid& g = h->grid;
+  GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
+  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
+  if (h->prm.remove_rhs_mean)
+    LAUNCH(h, GBMG_PROF_VECTOR,
+           launch_shift_by_mean(h->stream, h->b, h->b, h->n0, h->red, kSlotSumB, kSlotSumB + 1));
+  GB_TRY(check_launch(h, "rhs"));
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  *bnorm = std::sqrt(h->host_res[kSlotSumB + 1]);
+  return GBMG_OK;
+}
+
+int read_result(gbmg_handle* h, int slot, double* v) {
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  *v = h->host_res[slot];
+  return GBMG_OK;
+}
+
+// Enqueue the body of one solver iteration for the given kind.
+int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
+  const cudaStream_t s = h->stream;
+  Level& f = h->lv[0];
+  const size_t n = h->n0;
+  const int V = GBMG_PROF_VECTOR, R = GBMG_PROF_RESIDUAL;
+  if (kind == kGraphFp64) {
+    f.sol = h->p; f.src = h->b;
+    GB_TRY(enqueue_vcycle<double>(h, false));
+    LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
+  } else if (kind == kGraphMixed) {
+    GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
+    GB_TRY(enqueue_vcycle<float>(h, false));
+    LAUNCH(h, V, launch_add_float(s, h->p, f.sol32, n));
+    f.sol = h->p; f.src = h->b;
+    LAUNCH(h, R, launch_residual_norm<float>(s, v64(f), f.src32, h->red, kSlotNorm));
+  } else {
+    // flexible CG: z = M r (one V-cycle from zero), mean-free
+    if (kind == kGraphPcg64) {
+      GB_CUDA(h, cudaMemsetAsync(h->kz, 0, n * sizeof(double), s));
+      f.sol = h->kz; f.src = h->kr;
+      GB_TRY(enqueue_vcycle<double>(h, true));
+    } else {
+      LAUNCH(h, V, launch_double_to_float(s, h->kr, f.src32, n));
+      GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
+      GB_TRY(enqueue_vcycle<float>(h, true));
+      LAUNCH(h, V, launch_float_to_double(s, f.sol32, h->kz, n));
+    }
+    LAUNCH(h, V, launch_sum(s, h->kz, n, h->red, kSlotSum));
+    LAUNCH(h, V, launch_shift_by_mean(s, h->kz, h->kz, n, h->red, kSlotSum, -1));
+    LAUNCH(h, V, launch_dot2(s, h->kr, h->kz, h->kzold, n, h->red, kSlotDot));
+    LAUNCH(h, V, launch_pcg_direction(s, h->kd, h->kzold, h->kz, n, h->red, first ? 1 : 0));
+    h->launches += 1;  // the one-thread rz bookkeeping kernel
+    f.sol = h->p; f.src = h->b;
+    LAUNCH(h, R, launch_apply_dot(s, v64(f), h->kd, h->kq, h->red, kSlotDot2));
+    LAUNCH(h, V, launch_pcg_step(s, h->p, h->kd, n, h->red));
+    LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
+  }
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  return check_launch(h, "iteration");
+}
+
+int run_iteration(gbmg_handle* h, int kind, bool first) {
+  if (!h->prm.use_graph || first || h->prof) {
+    GB_TRY(enqueue_iteration(h, kind, first));
+    return GBMG_OK;
+  }
+  if (h->graph_kind != kind) {
+    reset_graph(h);
+    cudaGraph_t g = nullptr;
+    const int64_t before = h->launches;
+    GB_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_iteration(h, kind, false);
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc != GBMG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ec != cudaSuccess) {
+      h->err = std::string("graph capture: ") + cudaGetErrorString(ec);
+      if (g) cudaGraphDestroy(g);
+      return GBMG_CUDA_ERROR;
+    }
+    h->graph_kernels = h->launches - before;
+    h->launches = before;
+    const cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      h->err = std::string("graph instantiate: ") + cudaGetErrorString(ei);
+      h->graph = nullptr;
+      return GBMG_CUDA_ERROR;
+    }
+    h->graph_kind = kind;
+  }
+  GB_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+  h->launches += h->graph_kernels;
+  return GBMG_OK;
+}
+
+// The solve loop on the internal (b, p).  Leaves p mean-free.
+int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
+  const cudaStream_t s = h->stream;
+  Level& f = h->lv[0];
+  const size_t n = h->n0;
+  const bool pcg = h->prm.krylov != 0;
+  const int kind = pcg ? (h->mixed ? kGraphPcgMixed : kGraphPcg64) : (h->mixed ? kGraphMixed : kGraphFp64);
+  const double scale = bnorm > 0.0 ? bnorm : 1.0;
+  // initial residual
+  f.sol = h->p; f.src = h->b;
+  if (pcg) {
+    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
+    GB_CUDA(h, cudaMemsetAsync(h->kzold, 0, n * sizeof(double), s));
+  } else if (h->mixed) {
+    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<float>(s, v64(f), f.src32, h->red, kSlotNorm));
+  } else {
+    LAUNCH(h, GBMG_PROF_RESIDUAL,
+           launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
+  }
+  GB_TRY(check_launch(h, "residual"));
+  double r2 = 0.0;
+  GB_TRY(read_result(h, kSlotNorm, &r2));
+  double rel = std::sqrt(r2) / scale;
+  st->res0 = rel;
+  int status = GBMG_NOT_CONVERGED;
+  int cyc = 0;
+  if (rel < tol) {
+    status = GBMG_OK;
+  } else {
+    for (cyc = 1; cyc <= h->prm.max_cycles; ++cyc) {
+      GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
+      GB_CUDA(h, cudaStreamSynchronize(s));
+      prof_flush(h);
+      r2 = h->host_res[kSlotNorm];
+      rel = std::sqrt(r2) / scale;
+      if (!std::isfinite(rel) || rel > 1e3) { status = GBMG_DIVERGED; break; }
+      if (rel < tol) { status = GBMG_OK; break; }
+    }
+    if (cyc > h->prm.max_cycles) cyc = h->prm.max_cycles;
+  }
+  // mean projection of p (compatibility_sol on the finest level)
+  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+  LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
+  GB_TRY(check_launch(h, "mean"));
+  st->status = status;
+  st->cycles = cyc;
+  st->levels = h->L;
+  st->coarse_n = h->nc;
+  st->rel_residual = rel;
+  st->rms_residual = std::sqrt(r2 / (double)n);
+  // algorithmic bytes: per cycle V-cycle + FP64 residual (p, b, cx, cy, cz)
+  const int w = h->mixed ? 4 : 8;
+  double per = vcycle_bytes(h, w) + 40.0 * n;
+  if (h->mixed) per += 4.0 * n + 20.0 * n + 4.0 * n;  // r32 write, p += e, zero e
+  if (pcg) per += (h->mixed ? 24.0 : 8.0) * n + 16.0 * n + 32.0 * n + 48.0 * n + 24.0 * n + 8.0 * n;
+  st->bytes = per * cyc + 40.0 * n + 32.0 * n;
+  return status;
+}
+
+int validate_field(gbmg_handle* h, const gbmg_field& f, const char* name) {
+  if (!f.data || f.sy < 1 || f.sz < 1) {
+    h->err = std::string("invalid field ") + name;
+    return GBMG_INVALID_ARG;
+  }
+  return GBMG_OK;
+}
+
+int begin(gbmg_handle* h) {
+  if (!h) return GBMG_INVALID_ARG;
+  h->err.clear();
+  GB_CUDA(h, cudaSetDevice(h->device));
+  return GBMG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void gbmg_default_params(gbmg_params* prm) {
+  if (!prm) return;
+  std::memset(prm, 0, sizeof(*prm));
+  prm->precision = GBMG_PREC_FP64;
+  prm->nu1 = 2;
+  prm->nu2 = 2;
+  prm->levels = 0;
+  prm->coarse_max = 64;
+  prm->max_cycles = 100;
+  prm->krylov = 0;
+  prm->use_graph = 1;
+  prm->remove_rhs_mean = 1;
+  prm->device = -1;
+  prm->stream = nullptr;
+}
+
+int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out) {
+  if (!grid || !out) return GBMG_INVALID_ARG;
+  *out = nullptr;
+  if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0) || !(grid->dy > 0) ||
+      (grid->nz > 1 && !(grid->dz > 0)))
+    return GBMG_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return GBMG_NO_DEVICE;
+  }
+  gbmg_handle* h = new gbmg_handle();
+  h->grid = *grid;
+  if (h->grid.nz == 1 && !(h->grid.dz > 0)) h->grid.dz = 1.0;
+  if (prm) h->prm = *prm; else gbmg_default_params(&h->prm);
+  if (h->prm.nu1 < 0 || h->prm.nu2 < 0 || h->prm.max_cycles < 1 || h->prm.coarse_max < 1 ||
+      h->prm.coarse_max > kMaxCoarse || (h->prm.precision != GBMG_PREC_FP64 &&
+                                         h->prm.precision != GBMG_PREC_MIXED)) {
+    delete h;
+    return GBMG_INVALID_ARG;
+  }
+  h->mixed = h->prm.precision == GBMG_PREC_MIXED;
+  if (h->prm.device >= 0) {
+    if (h->prm.device >= ndev) { delete h; return GBMG_INVALID_ARG; }
+    h->device = h->prm.device;
+  } else {
+    cudaGetDevice(&h->device);
+  }
+  if (cudaSetDevice(h->device) != cudaSuccess) { delete h; return GBMG_CUDA_ERROR; }
+  if (h->prm.stream) {
+    h->stream = (cudaStream_t)h->prm.stream;
+    h->own_stream = false;
+  } else {
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete h;
+      return GBMG_CUDA_ERROR;
+    }
+    h->own_stream = true;
+  }
+  const int rc = allocate(h);
+  if (rc != GBMG_OK) {
+    std::fprintf(stderr, "gbmg_create: %s\n", h->err.c_str());
+    free_all(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return GBMG_OK;
+}
+
+int gbmg_destroy(gbmg_handle* h) {
+  if (!h) return GBMG_INVALID_ARG;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+  return GBMG_OK;
+}
+
+int gbmg_set_rho(gbmg_handle* h, gbmg_field rho, int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, rho, "rho"));
+  const gbmg_grid& g = h->grid;
+  GB_TRY(upload(h, rho, g.nx, g.ny, g.nz, mem, h->rho));
+  GB_TRY(set_rho_device(h));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_set_phi(gbmg_handle* h, gbmg_field phi, double eps, double rho_pos, double rho_neg,
+                 int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, phi, "phi"));
+  if (!(eps > 0)) { h->err = "eps must be > 0"; return GBMG_INVALID_ARG; }
+  const gbmg_grid& g = h->grid;
+  const double* src = phi.data;
+  Strided sp{phi.data, phi.sy, phi.sz};
+  if (mem == GBMG_MEM_HOST) {
+    GB_TRY(upload(h, phi, g.nx, g.ny, g.nz, mem, h->p));  // p as staging
+    sp = Strided{h->p, g.nx, (int64_t)g.nx * g.ny};
+  }
+  (void)src;
+  launch_rho_from_phi(h->stream, g.nx, g.ny, g.nz, sp, eps, rho_pos, rho_neg, h->rho);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "rho_from_phi"));
+  GB_TRY(set_rho_device(h));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_set_coef(gbmg_handle* h, gbmg_field cx, gbmg_field cy, gbmg_field cz, int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, cx, "cx"));
+  GB_TRY(validate_field(h, cy, "cy"));
+  GB_TRY(validate_field(h, cz, "cz"));
+  const gbmg_grid& g = h->grid;
+  Level& f = h->lv[0];
+  GB_TRY(upload(h, cx, g.nx, g.ny, g.nz, mem, f.cx));
+  GB_TRY(upload(h, cy, g.nx, g.ny, g.nz, mem, f.cy));
+  GB_TRY(upload(h, cz, g.nx, g.ny, g.nz, mem, f.cz));
+  // the wall entries are taken as walls whatever the caller stored there
+  for (int k = 0; k < g.nz; ++k) {
+    GB_CUDA(h, cudaMemset2DAsync(f.cx + (size_t)k * g.nx * g.ny, (size_t)g.nx * sizeof(double), 0,
+                                 sizeof(double), (size_t)g.ny, h->stream));
+  }
+  GB_CUDA(h, cudaMemsetAsync(f.cz, 0, (size_t)g.nx * g.ny * sizeof(double), h->stream));
+  for (int k = 0; k < g.nz; ++k)
+    GB_CUDA(h, cudaMemsetAsync(f.cy + (size_t)k * g.nx * g.ny, 0, (size_t)g.nx * sizeof(double),
+                               h->stream));
+  h->rho_ready = false;
+  GB_TRY(build_hierarchy(h));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
+               gbmg_stats* stats) {
+  GB_TRY(begin(h));
+  gbmg_stats local{};
+  gbmg_stats* st = stats ? stats : &local;
+  std::memset(st, 0, sizeof(*st));
+  if (!h->coef_ready) { h->err = "no coefficients: call gbmg_set_rho/phi/coef first"; return GBMG_STATE_ERROR; }
+  GB_TRY(validate_field(h, b, "b"));
+  GB_TRY(validate_field(h, p, "p"));
+  if (!(tol > 0)) { h->err = "tol must be > 0"; return GBMG_INVALID_ARG; }
+  const gbmg_grid& g = h->grid;
+  GB_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+  double bnorm = 0.0;
+  GB_TRY(prepare_rhs(h, b, mem, &bnorm));
+  GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  const int status = solve_internal(h, tol, bnorm, st);
+  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
+  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
+  GB_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+  GB_CUDA(h, cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st->ms = ms;
+  st->bytes += 16.0 * h->n0;
+  return status;
+}
+
+int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_field p,
+                 double dt, double tol, int mem, gbmg_stats* stats) {
+  GB_TRY(begin(h));
+  gbmg_stats local{};
+  gbmg_stats* st = stats ? stats : &local;
+  std::memset(st, 0, sizeof(*st));
+  if (!h->coef_ready || !h->rho_ready) {
+    h->err = "the projection needs the density: call gbmg_set_rho or gbmg_set_phi first";
+    return GBMG_STATE_ERROR;
+  }
+  GB_TRY(validate_field(h, u, "u"));
+  GB_TRY(validate_field(h, v, "v"));
+  GB_TRY(validate_field(h, p, "p"));
+  const bool has_w = w.data != nullptr && h->grid.nz > 1;
+  if (has_w) GB_TRY(validate_field(h, w, "w"));
+  if (!(dt > 0) || !(tol > 0)) { h->err = "dt and tol must be > 0"; return GBMG_INVALID_ARG; }
+  const gbmg_grid& g = h->grid;
+  const cudaStream_t s = h->stream;
+  GB_CUDA(h, cudaEventRecord(h->ev0, s));
+  const int ext[3][3] = {{g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz}, {g.nx, g.ny, g.nz + 1}};
+  const gbmg_field* fv[3] = {&u, &v, &w};
+  double* dv[3] = {nullptr, nullptr, nullptr};
+  gbmg_field dfield[3];
+  for (int a = 0; a < 3; ++a) {
+    if (a == 2 && !has_w) continue;
+    const size_t n = (size_t)ext[a][0] * ext[a][1] * ext[a][2];
+    const bool direct = mem == GBMG_MEM_DEVICE;
+    if (direct) {
+      dv[a] = fv[a]->data;
+      dfield[a] = *fv[a];
+    } else {
+      if (h->vel_n[a] < n) {
+        dfree(h->vel[a]);
+        GB_TRY(dmalloc(h, &h->vel[a], n));
+        h->vel_n[a] = n;
+      }
+      GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
+      dv[a] = h->vel[a];
+      dfield[a] = gbmg_field{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
+    }
+  }
+  // b = div(u*)/dt into h->b (the RHS of ppe_sor_solver)
+  Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
+  Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
+  launch_divergence(s, g.nx, g.ny, g.nz, su, sv, sw, g.dx, g.dy, g.dz, dt, h->b);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "divergence"));
+  // mean projection + norm of b in place
+  launch_sum(s, h->b, h->n0, h->red, kSlotSumB);
+  launch_shift_by_mean(s, h->b, h->b, h->n0, h->red, kSlotSumB, kSlotSumB + 1);
+  h->launches += 2;
+  double bn2 = 0.0;
+  GB_TRY(read_result(h, kSlotSumB + 1, &bn2));
+  GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  const int status = solve_internal(h, tol, std::sqrt(bn2), st);
+  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
+  // u -= dt beta grad p (ns_momentum_correction)
+  launch_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, g.dx, g.dy, g.dz, dt, dv[0], dfield[0].sy,
+                 dfield[0].sz, dv[1], dfield[1].sy, dfield[1].sz, has_w ? dv[2] : nullptr,
+                 has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "correct"));
+  if (mem == GBMG_MEM_HOST)
+    for (int a = 0; a < 3; ++a) {
+      if (a == 2 && !has_w) continue;
+      GB_TRY(download(h, dv[a], ext[a][0], ext[a][1], ext[a][2], mem, *fv[a]));
+    }
+  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
+  GB_CUDA(h, cudaEventRecord(h->ev1, s));
+  GB_CUDA(h, cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st->ms = ms;
+  return status;
+}
+
+int gbmg_divergence(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double dt,
+                    gbmg_field b, int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, u, "u"));
+  GB_TRY(validate_field(h, v, "v"));
+  GB_TRY(validate_field(h, b, "b"));
+  const gbmg_grid& g = h->grid;
+  const bool has_w = w.data != nullptr && g.nz > 1;
+  const int ext[3][3] = {{g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz}, {g.nx, g.ny, g.nz + 1}};
+  const gbmg_field* fv[3] = {&u, &v, &w};
+  Strided sd[3] = {{nullptr, 0, 0}, {nullptr, 0, 0}, {nullptr, 0, 0}};
+  for (int a = 0; a < 3; ++a) {
+    if (a == 2 && !has_w) continue;
+    if (mem == GBMG_MEM_DEVICE) {
+      sd[a] = Strided{fv[a]->data, fv[a]->sy, fv[a]->sz};
+    } else {
+      const size_t n = (size_t)ext[a][0] * ext[a][1] * ext[a][2];
+      if (h->vel_n[a] < n) {
+        dfree(h->vel[a]);
+        GB_TRY(dmalloc(h, &h->vel[a], n));
+        h->vel_n[a] = n;
+      }
+      GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
+      sd[a] = Strided{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
+    }
+  }
+  launch_divergence(h->stream, g.nx, g.ny, g.nz, sd[0], sd[1], sd[2], g.dx, g.dy, g.dz, dt, h->b);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "divergence"));
+  GB_TRY(download(h, h->b, g.nx, g.ny, g.nz, mem, b));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_residual(gbmg_handle* h, gbmg_field b, gbmg_field p, gbmg_field r, double* norm2,
+                  int mem) {
+  GB_TRY(begin(h));
+  if (!h->coef_ready) { h->err = "no coefficients"; return GBMG_STATE_ERROR; }
+  GB_TRY(validate_field(h, b, "b"));
+  GB_TRY(validate_field(h, p, "p"));
+  const gbmg_grid& g = h->grid;
+  GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
+  GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  Level& f = h->lv[0];
+  f.sol = h->p; f.src = h->b;
+  // the residual overwrites the staging copy of b (not the caller's array)
+  launch_residual_norm<double>(h->stream, v64(f), r.data ? h->b : nullptr, h->red, kSlotNorm);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "residual"));
+  double s2 = 0.0;
+  GB_TRY(read_result(h, kSlotNorm, &s2));
+  if (norm2) *norm2 = s2;
+  if (r.data) {
+    GB_TRY(download(h, h->b, g.nx, g.ny, g.nz, mem, r));
+    GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return GBMG_OK;
+}
+
+int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double* max_div,
+                   double* mean_div, int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, u, "u"));
+  GB_TRY(validate_field(h, v, "v"));
+  const gbmg_grid& g = h->grid;
+  const bool has_w = w.data != nullptr && g.nz > 1;
+  const int ext[3][3] = {{g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz}, {g.nx, g.ny, g.nz + 1}};
+  const gbmg_field* fv[3] = {&u, &v, &w};
+  Strided sd[3] = {{nullptr, 0, 0}, {nullptr, 0, 0}, {nullptr, 0, 0}};
+  for (int a = 0; a < 3; ++a) {
+    if (a == 2 && !has_w) continue;
+    if (mem == GBMG_MEM_DEVICE) {
+      sd[a] = Strided{fv[a]->data, fv[a]->sy, fv[a]->sz};
+    } else {
+      const size_t n = (size_t)ext[a][0] * ext[a][1] * ext[a][2];
+      if (h->vel_n[a] < n) {
+        dfree(h->vel[a]);
+        GB_TRY(dmalloc(h, &h->vel[a], n));
+        h->vel_n[a] = n;
+      }
+      GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
+      sd[a] = Strided{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
+    }
+  }
+  launch_div_stats(h->stream, g.nx, g.ny, g.nz, sd[0], sd[1], sd[2], g.dx, g.dy, g.dz, h->red);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "div_stats"));
+  double sum = 0.0;
+  GB_TRY(read_result(h, kSlotSum, &sum));
+  if (max_div) *max_div = h->host_res[kSlotMax];
+  if (mean_div) *mean_div = sum / (double)h->n0;
+  return GBMG_OK;
+}
+
+int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,
+                    int mem) {
+  GB_TRY(begin(h));
+  if (!h->coef_ready) { h->err = "no coefficients"; return GBMG_STATE_ERROR; }
+  if (level < 0 || level >= h->L) return GBMG_INVALID_ARG;
+  const Level& v = h->lv[level];
+  GB_TRY(download(h, v.cx, v.nx, v.ny, v.nz, mem, cx));
+  GB_TRY(download(h, v.cy, v.nx, v.ny, v.nz, mem, cy));
+  GB_TRY(download(h, v.cz, v.nx, v.ny, v.nz, mem, cz));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_level_dims(gbmg_handle* h, int32_t* levels, int32_t* dims, int32_t max_levels) {
+  if (!h) return GBMG_INVALID_ARG;
+  if (levels) *levels = h->L;
+  if (dims)
+    for (int l = 0; l < h->L && l < max_levels; ++l) {
+      dims[3 * l] = h->lv[l].nx;
+      dims[3 * l + 1] = h->lv[l].ny;
+      dims[3 * l + 2] = h->lv[l].nz;
+    }
+  return GBMG_OK;
+}
+
+int64_t gbmg_kernel_launches(gbmg_handle* h) { return h ? h->launches : 0; }
+
+int gbmg_set_profiling(gbmg_handle* h, int on) {
+  GB_TRY(begin(h));
+  prof_flush(h);
+  h->prof = on != 0;
+  for (int c = 0; c < GBMG_PROF_CLASSES; ++c) {
+    h->prof_ms[c] = 0.0;
+    h->prof_n[c] = 0;
+  }
+  return GBMG_OK;
+}
+
+int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n) {
+  GB_TRY(begin(h));
+  prof_flush(h);
+  for (int c = 0; c < GBMG_PROF_CLASSES && c < n; ++c) {
+    if (ms) ms[c] = h->prof_ms[c];
+    if (launches) launches[c] = h->prof_n[c];
+  }
+  return GBMG_OK;
+}
+
+const char* gbmg_strerror(int status) {
+  switch (status) {
+    case GBMG_OK: return "ok";
+    case GBMG_NOT_CONVERGED: return "not converged within max_cycles";
+    case GBMG_DIVERGED: return "diverged (residual not finite or grew above 1e3)";
+    case GBMG_INVALID_ARG: return "invalid argument";
+    case GBMG_CUDA_ERROR: return "CUDA error";
+    case GBMG_NO_DEVICE: return "no CUDA device";
+    case GBMG_OUT_OF_MEMORY: return "out of device memory";
+    case GBMG_STATE_ERROR: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+const char* gbmg_last_error(gbmg_handle* h) { return h ? h->err.c_str() : ""; }
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// Internal declarations shared by the CUDA translation units of libgbmg.
+//
+// Device layout: every level stores dense cell arrays in C order (z, y, x),
+// x fastest, with strides sy = nx and sz = nx*ny.  Face coefficients are
+// cell-shaped low-face arrays (cx[q] couples cells q-1 and q along x; the low
+// wall entries are 0 and the high wall is implicit), so every array of a level
+// has the same index map and alignment.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace gbmg {
+
+constexpr int kMaxCoarse = 64;    // largest coarsest level solved by the dense inverse
+constexpr int kMaxLevels = 24;
+
+// One multigrid level seen by the kernels, in arithmetic type T.
+template <typename T>
+struct LevelView {
+  int nx, ny, nz;
+  int fx, fy, fz;        // coarsening factor to the next level per axis (1 or 2)
+  const T* cx;
+  const T* cy;
+  const T* cz;
+  const T* idiag;        // 1/diagonal, or nullptr (computed on the fly)
+  T* sol;
+  T* src;
+};
+
+// Deterministic single-pass grid reduction scratch: per-block partial sums,
+// a completion counter and result slots (see reduce.cuh).
+struct ReduceScratch {
+  double* partials;      // kRedValues * max_blocks
+  unsigned int* counter; // 1 word, returns to 0 after each reduction
+  double* result;        // result slots
+  int max_blocks;
+};
+
+constexpr int kRedValues = 2;   // values reduced together per launch
+constexpr int kRedSlots = 16;   // result slots
+
+// Result slot assignment.
+enum : int {
+  kSlotNorm = 0,     // sum r^2 of the last residual
+  kSlotSumB = 2,     // sum b, sum (b - mean)^2
+  kSlotSum = 4,      // generic sum / sum of squares
+  kSlotMax = 6,      // max |div| (bit pattern, atomicMax)
+  kSlotDot = 8,      // Krylov dot products (2 values)
+  kSlotDot2 = 10,
+};
+
+// ---- launchers (kernels_mg.cu) ---------------------------------------------
+template <typename T>
+void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color);
+template <typename T>
+void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
+template <typename T>
+void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
+// r = src - A sol on a level; writes r (type TO, may be null) and sum r^2 into slot.
+template <typename TO>
+void launch_residual_norm(cudaStream_t s, const LevelView<double>& L, TO* r,
+                          const ReduceScratch& R, int slot);
+template <typename T>
+void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, const T* b, T* x);
+void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
+                          double* adense, float* minv32, float* adense32);
+void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,
+                    double* cz, int cnx, int cny, int cnz);
+void launch_idiag(cudaStream_t s, const LevelView<double>& L, double* idiag);
+void launch_to_float(cudaStream_t s, const double* a, float* b, size_t n);
+
+// ---- launchers (kernels_flow.cu) -------------------------------------------
+struct Strided {
+  const double* data;
+  int64_t sy, sz;
+};
+void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, double eps,
+                         double rho_pos, double rho_neg, double* rho);
+void launch_copy_in(cudaStream_t s, int nx, int ny, int nz, Strided src, double* dst);
+void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, double* dst,
+                     int64_t sy, int64_t sz);
+void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
+                      const double* rho, double* cx, double* cy, double* cz);
+void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
+                       double dx, double dy, double dz, double dt, double* b);
+void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,
+                    double dx, double dy, double dz, double dt, double* u, int64_t usy,
+                    int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w, int64_t wsy,
+                    int64_t wsz);
+void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
+                      double dx, double dy, double dz, const ReduceScratch& R);
+// slot <- sum x, slot+1 <- sum x^2
+void launch_sum(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot);
+// y = x - result[slot]/n ; result[slot2] <- sum y^2 (slot2 < 0: no norm)
+void launch_shift_by_mean(cudaStream_t s, const double* x, double* y, size_t n,
+                          const ReduceScratch& R, int slot, int slot2);
+void launch_add_float(cudaStream_t s, double* p, const float* e, size_t n);
+// Flexible-CG helpers.  Slots: kSlotDot = r.z, kSlotDot+1 = r.z_old,
+// kSlotDot2 = d.(A d), kSlotDot2+1 = r.z of the previous iteration.
+void launch_dot2(cudaStream_t s, const double* a, const double* b, const double* c, size_t n,
+                 const ReduceScratch& R, int slot);
+void launch_pcg_direction(cudaStream_t s, double* d, double* zold, const double* z, size_t n,
+                          const ReduceScratch& R, int first);
+void launch_pcg_step(cudaStream_t s, double* x, const double* d, size_t n, const ReduceScratch& R);
+// q = A d on a level and d.q into slot (kernels_mg.cu)
+void launch_apply_dot(cudaStream_t s, const LevelView<double>& L, const double* d, double* q,
+                      const ReduceScratch& R, int slot);
+void launch_float_to_double(cudaStream_t s, const float* a, double* b, size_t n);
+void launch_double_to_float(cudaStream_t s, const double* a, float* b, size_t n);
+
+int reduce_blocks_for(size_t n);
+
+}  // namespace gbmg

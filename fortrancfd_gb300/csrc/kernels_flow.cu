@@ -1,0 +1,331 @@
+// Projection-step kernels for sm_103a: level set -> density, density -> face
+// coefficients, MAC divergence, pressure-gradient correction, divergence
+// statistics, and the FP64 vector kernels of the solve loop (mean projection,
+// mixed-precision update, flexible-CG steps).
+//
+// Reference loops: rho_mu / ls_funs ("Two phase flows/newOpenMP/2D/src/
+// interface_solver/others.f90:1-61"), ppe_sor_init and ppe_sor_solver's RHS
+// ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-65,
+// 77-89"), ns_momentum_correction (same file :174-205) and
+// ns_check_convergence_div ("Two phase flows/newOpenMP/2D/src/ns_solver/
+// ns_solvers.f90:55-83").
+#include <algorithm>
+
+#include "gbmg_internal.h"
+#include "reduce.cuh"
+
+namespace gbmg {
+
+namespace {
+
+inline unsigned cdiv(size_t a, unsigned b) { return (unsigned)((a + b - 1) / b); }
+
+inline unsigned stride_blocks(size_t n) {
+  const size_t b = cdiv(n, kRedThreads);
+  return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 152 * 8));
+}
+
+// Smoothed Heaviside H(phi/eps) = (1 + x + sin(pi x)/pi)/2 on |x| < 1, then
+// rho = rho_pos H + rho_neg (1 - H).
+__global__ void __launch_bounds__(256) k_rho_from_phi(int nx, int ny, int nz, Strided phi,
+                                                      double eps, double rho_pos,
+                                                      double rho_neg, double* rho) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const double pi = 3.141592653589793;
+  const double x = phi.data[i + j * phi.sy + k * phi.sz] / eps;
+  double h;
+  if (x > 1.0 - 1e-12) h = 1.0;
+  else if (x < -1.0 + 1e-12) h = 0.0;
+  else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+  h = fmax(fmin(h, 1.0), 0.0);
+  rho[((size_t)k * ny + j) * nx + i] = rho_pos * h + rho_neg * (1.0 - h);
+}
+
+__global__ void __launch_bounds__(256) k_copy_in(int nx, int ny, int nz, Strided src, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  dst[((size_t)k * ny + j) * nx + i] = src.data[i + j * src.sy + k * src.sz];
+}
+
+__global__ void __launch_bounds__(256) k_copy_out(int nx, int ny, int nz, const double* src,
+                                                  double* dst, int64_t sy, int64_t sz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  dst[i + j * sy + k * sz] = src[((size_t)k * ny + j) * nx + i];
+}
+
+// coe = 2/(rho_i + rho_nb)/h^2 on the low face of every cell, 0 on the walls
+// (the reference's arithmetic, ns_ppe_solver.f90:12-24, so the operator is
+// bit-identical to the oracle's).
+__global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, double dx2,
+                                                   double dy2, double dz2,
+                                                   const double* __restrict__ rho, double* cx,
+                                                   double* cy, double* cz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const size_t q = ((size_t)k * ny + j) * nx + i;
+  const double r = rho[q];
+  cx[q] = i > 0 ? 2.0 / (r + rho[q - 1]) / dx2 : 0.0;
+  cy[q] = j > 0 ? 2.0 / (r + rho[q - nx]) / dy2 : 0.0;
+  cz[q] = k > 0 ? 2.0 / (r + rho[q - (size_t)nx * ny]) / dz2 : 0.0;
+}
+
+// b = div(u)/dt with MAC faces: u(f,j,k) on the x-face at f*dx, f = 0..nx.
+__global__ void __launch_bounds__(256) k_divergence(int nx, int ny, int nz, Strided u, Strided v,
+                                                    Strided w, double dx, double dy,
+                                                    double dz, double dt, double* b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const int64_t qu = i + j * u.sy + k * u.sz;
+  const int64_t qv = i + j * v.sy + k * v.sz;
+  double d = (u.data[qu + 1] - u.data[qu]) / dx + (v.data[qv + v.sy] - v.data[qv]) / dy;
+  if (w.data) {
+    const int64_t qw = i + j * w.sy + k * w.sz;
+    d += (w.data[qw + w.sz] - w.data[qw]) / dz;
+  }
+  b[((size_t)k * ny + j) * nx + i] = d / dt;
+}
+
+// u_f -= dt (p_i - p_{i-1})/dx / ((rho_i + rho_{i-1})/2) on every interior
+// face; each cell corrects its low faces.
+__global__ void __launch_bounds__(256) k_correct(int nx, int ny, int nz,
+                                                 const double* __restrict__ rho,
+                                                 const double* __restrict__ p, double dx,
+                                                 double dy, double dz, double dt, double* u,
+                                                 int64_t usy, int64_t usz, double* v, int64_t vsy,
+                                                 int64_t vsz, double* w, int64_t wsy, int64_t wsz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const size_t q = ((size_t)k * ny + j) * nx + i;
+  if (i > 0) {
+    const double rf = (rho[q] + rho[q - 1]) / 2.0;
+    const double px = (p[q] - p[q - 1]) / dx;
+    u[i + j * usy + k * usz] -= dt * px / rf;
+  }
+  if (j > 0) {
+    const double rf = (rho[q] + rho[q - nx]) / 2.0;
+    const double py = (p[q] - p[q - nx]) / dy;
+    v[i + j * vsy + k * vsz] -= dt * py / rf;
+  }
+  if (k > 0 && w) {
+    const size_t sz = (size_t)nx * ny;
+    const double rf = (rho[q] + rho[q - sz]) / 2.0;
+    const double pz = (p[q] - p[q - sz]) / dz;
+    w[i + j * wsy + k * wsz] -= dt * pz / rf;
+  }
+}
+
+// max |div u| by atomicMax on the bit pattern (non-negative doubles order as
+// unsigned integers) and sum |div u| through the deterministic reducer.
+__global__ void __launch_bounds__(kRedThreads) k_div_stats(int nx, int ny, int nz, Strided u,
+                                                           Strided v, Strided w, double dx,
+                                                           double dy, double dz,
+                                                           ReduceScratch R) {
+  double acc[1] = {0.0};
+  double mx = 0.0;
+  const int rows = ny * nz;
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int j = row % ny, k = row / ny;
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+      const int64_t qu = i + j * u.sy + k * u.sz;
+      const int64_t qv = i + j * v.sy + k * v.sz;
+      double d = (u.data[qu + 1] - u.data[qu]) / dx + (v.data[qv + v.sy] - v.data[qv]) / dy;
+      if (w.data) {
+        const int64_t qw = i + j * w.sy + k * w.sz;
+        d += (w.data[qw + w.sz] - w.data[qw]) / dz;
+      }
+      d = fabs(d);
+      mx = fmax(mx, d);
+      acc[0] += d;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(reinterpret_cast<unsigned long long*>(R.result + kSlotMax),
+              (unsigned long long)__double_as_longlong(mx));
+  grid_sum_finish<1>(acc, R, kSlotSum);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_sum(const double* __restrict__ x, size_t n,
+                                                     ReduceScratch R, int slot) {
+  double acc[2] = {0.0, 0.0};
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const double a = x[q];
+    acc[0] += a;
+    acc[1] += a * a;
+  }
+  grid_sum_finish<2>(acc, R, slot);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_shift_by_mean(const double* __restrict__ x,
+                                                               double* y, size_t n,
+                                                               ReduceScratch R, int slot,
+                                                               int slot2) {
+  const double m = R.result[slot] / (double)n;
+  double acc[1] = {0.0};
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const double a = x[q] - m;
+    y[q] = a;
+    acc[0] += a * a;
+  }
+  if (slot2 >= 0) grid_sum_finish<1>(acc, R, slot2);
+}
+
+__global__ void k_add_float(double* p, const float* __restrict__ e, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    p[q] += (double)e[q];
+}
+
+__global__ void k_f2d(const float* __restrict__ a, double* b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    b[q] = (double)a[q];
+}
+
+__global__ void k_d2f(const double* __restrict__ a, float* b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    b[q] = (float)a[q];
+}
+
+// slot <- a.b, slot+1 <- a.c (c may be null)
+__global__ void __launch_bounds__(kRedThreads) k_dot2(const double* __restrict__ a,
+                                                      const double* __restrict__ b,
+                                                      const double* __restrict__ c, size_t n,
+                                                      ReduceScratch R, int slot) {
+  double acc[2] = {0.0, 0.0};
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    acc[0] += a[q] * b[q];
+    if (c) acc[1] += a[q] * c[q];
+  }
+  grid_sum_finish<2>(acc, R, slot);
+}
+
+// Flexible-CG direction: beta = (r.z - r.z_old)/rz_old (0 on the first
+// iteration), d = z + beta d, z_old = z.  rz_old lives in result[kSlotDot2+1].
+__global__ void k_pcg_direction(double* d, double* zold, const double* __restrict__ z, size_t n,
+                                ReduceScratch R, int first) {
+  const double rz = R.result[kSlotDot], rzo = R.result[kSlotDot + 1];
+  const double beta = first ? 0.0 : (rz - rzo) / R.result[kSlotDot2 + 1];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    d[q] = first ? z[q] : z[q] + beta * d[q];
+    zold[q] = z[q];
+  }
+}
+
+__global__ void k_pcg_keep_rz(ReduceScratch R) { R.result[kSlotDot2 + 1] = R.result[kSlotDot]; }
+
+// x += alpha d with alpha = (r.z)/(d.q)
+__global__ void k_pcg_step(double* x, const double* __restrict__ d, size_t n, ReduceScratch R) {
+  const double alpha = R.result[kSlotDot] / R.result[kSlotDot2];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    x[q] += alpha * d[q];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static inline dim3 grid3(int nx, int ny, int nz) {
+  return dim3(cdiv((size_t)nx, 32), cdiv((size_t)ny, 8), (unsigned)nz);
+}
+
+void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, double eps,
+                         double rho_pos, double rho_neg, double* rho) {
+  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, phi, eps, rho_pos, rho_neg,
+                                                          rho);
+}
+
+void launch_copy_in(cudaStream_t s, int nx, int ny, int nz, Strided src, double* dst) {
+  k_copy_in<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, src, dst);
+}
+
+void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, double* dst,
+                     int64_t sy, int64_t sz) {
+  k_copy_out<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, src, dst, sy, sz);
+}
+
+void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
+                      const double* rho, double* cx, double* cy, double* cz) {
+  k_face_coef<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, dx2, dy2, dz2, rho, cx, cy, cz);
+}
+
+void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
+                       double dx, double dy, double dz, double dt, double* b) {
+  k_divergence<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, dt, b);
+}
+
+void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,
+                    double dx, double dy, double dz, double dt, double* u, int64_t usy,
+                    int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w, int64_t wsy,
+                    int64_t wsz) {
+  k_correct<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, rho, p, dx, dy, dz, dt, u, usy,
+                                                     usz, v, vsy, vsz, w, wsy, wsz);
+}
+
+void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
+                      double dx, double dy, double dz, const ReduceScratch& R) {
+  cudaMemsetAsync(R.result + kSlotMax, 0, sizeof(double), s);
+  const int blocks = std::min(reduce_blocks_for((size_t)ny * nz), R.max_blocks);
+  k_div_stats<<<blocks, kRedThreads, 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, R);
+}
+
+void launch_sum(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot) {
+  const unsigned b = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_sum<<<b, kRedThreads, 0, s>>>(x, n, R, slot);
+}
+
+void launch_shift_by_mean(cudaStream_t s, const double* x, double* y, size_t n,
+                          const ReduceScratch& R, int slot, int slot2) {
+  const unsigned b = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_shift_by_mean<<<b, kRedThreads, 0, s>>>(x, y, n, R, slot, slot2);
+}
+
+void launch_add_float(cudaStream_t s, double* p, const float* e, size_t n) {
+  k_add_float<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(p, e, n);
+}
+
+void launch_float_to_double(cudaStream_t s, const float* a, double* b, size_t n) {
+  k_f2d<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(a, b, n);
+}
+
+void launch_double_to_float(cudaStream_t s, const double* a, float* b, size_t n) {
+  k_d2f<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(a, b, n);
+}
+
+void launch_dot2(cudaStream_t s, const double* a, const double* b, const double* c, size_t n,
+                 const ReduceScratch& R, int slot) {
+  const unsigned bl = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_dot2<<<bl, kRedThreads, 0, s>>>(a, b, c, n, R, slot);
+}
+
+void launch_pcg_direction(cudaStream_t s, double* d, double* zold, const double* z, size_t n,
+                          const ReduceScratch& R, int first) {
+  k_pcg_direction<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(d, zold, z, n, R, first);
+  k_pcg_keep_rz<<<1, 1, 0, s>>>(R);
+}
+
+void launch_pcg_step(cudaStream_t s, double* x, const double* d, size_t n, const ReduceScratch& R) {
+  k_pcg_step<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(x, d, n, R);
+}
+
+}  // namespace gbmg

@@ -1,0 +1,445 @@
+// Multigrid kernels for sm_103a: red-black Gauss-Seidel smoother, fused
+// residual + restriction, central-slope prolongation, fine-level residual
+// norm, coarse-operator construction and the dense coarsest-level solve.
+//
+// The cycle restated here is the reference's ("DomainDecomposition/3D/src/
+// others/multigrid_solver.f90": multigrid_relax :1-49, multigrid_restriction
+// :51-90, multigrid_final_exact :92-104, multigrid_prolongation :106-160,
+// multigrid_residual :162-222) applied to the variable-coefficient operator of
+// ppe_sor_init ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/
+// ns_ppe_solver.f90:1-65").  Operator: (A p)_i = sum_f coe_f (p_nb - p_i), with
+// zero coefficients on walls.
+#include <algorithm>
+#include <cstdio>
+
+#include "gbmg_internal.h"
+#include "reduce.cuh"
+
+namespace gbmg {
+
+namespace {
+
+inline unsigned cdiv(size_t a, unsigned b) { return (unsigned)((a + b - 1) / b); }
+
+// Neighbour sum s = sum_f coe_f p_nb and diagonal d = sum_f coe_f of cell
+// (i,j,k), accumulated in the order x-, x+, y-, y+, z-, z+.
+template <typename T>
+__device__ __forceinline__ void stencil(const LevelView<T>& L, const T* __restrict__ p, int i,
+                                        int j, int k, size_t q, T& s, T& d) {
+  const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+  T c;
+  s = T(0);
+  d = T(0);
+  if (i > 0) { c = L.cx[q]; s += c * p[q - 1]; d += c; }
+  if (i < L.nx - 1) { c = L.cx[q + 1]; s += c * p[q + 1]; d += c; }
+  if (j > 0) { c = L.cy[q]; s += c * p[q - sy]; d += c; }
+  if (j < L.ny - 1) { c = L.cy[q + sy]; s += c * p[q + sy]; d += c; }
+  if (k > 0) { c = L.cz[q]; s += c * p[q - sz]; d += c; }
+  if (k < L.nz - 1) { c = L.cz[q + sz]; s += c * p[q + sz]; d += c; }
+}
+
+// One colour of a red-black Gauss-Seidel sweep: cells with (i+j+k)%2 == color
+// get p_i = (s - b_i)/d (the reference's p_i = (src - sum coe p_nb)/c with
+// c = -d).  One thread per cell of the colour.
+template <typename T, bool kIdiag>
+__global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (j >= L.ny) return;
+  const int i = 2 * (blockIdx.x * blockDim.x + threadIdx.x) + ((j + k + color) & 1);
+  if (i >= L.nx) return;
+  const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
+  T s, d;
+  stencil(L, L.sol, i, j, k, q, s, d);
+  const T v = s - L.src[q];
+  if (kIdiag) L.sol[q] = v * L.idiag[q];
+  else L.sol[q] = v / d;
+}
+
+// Fused residual + restriction: coarse src = mean over the children of
+// (src - A sol) on the fine level; coarse sol = 0.  One thread per coarse cell.
+template <typename T>
+__global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= C.nx || J >= C.ny) return;
+  T acc = T(0);
+  for (int dz = 0; dz < F.fz; ++dz)
+    for (int dy = 0; dy < F.fy; ++dy)
+      for (int dx = 0; dx < F.fx; ++dx) {
+        const int i = F.fx * I + dx, j = F.fy * J + dy, k = F.fz * K + dz;
+        const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
+        T s, d;
+        stencil(F, F.sol, i, j, k, q, s, d);
+        acc += F.src[q] - (s - d * F.sol[q]);
+      }
+  const size_t cq = ((size_t)K * C.ny + J) * C.nx + I;
+  C.src[cq] = acc * (T(1) / T(F.fx * F.fy * F.fz));
+  C.sol[cq] = T(0);
+}
+
+// Prolongation + correction: fine sol += e_c +/- m/4 per coarsened axis, with
+// central slopes m = (e_{c+1} - e_{c-1})/2 and zero-gradient ghosts at walls.
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> C) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= F.nx || j >= F.ny) return;
+  const int I = i / F.fx, J = j / F.fy, K = k / F.fz;
+  const size_t csy = (size_t)C.nx, csz = (size_t)C.nx * C.ny;
+  const size_t cq = (size_t)K * csz + (size_t)J * csy + I;
+  const T* e = C.sol;
+  const T ec = e[cq];
+  T val = ec;
+  if (F.fx == 2) {
+    const T em = I > 0 ? e[cq - 1] : ec, ep = I < C.nx - 1 ? e[cq + 1] : ec;
+    const T m = T(0.5) * (ep - em);
+    val += (i & 1) ? T(0.25) * m : -(T(0.25) * m);
+  }
+  if (F.fy == 2) {
+    const T em = J > 0 ? e[cq - csy] : ec, ep = J < C.ny - 1 ? e[cq + csy] : ec;
+    const T m = T(0.5) * (ep - em);
+    val += (j & 1) ? T(0.25) * m : -(T(0.25) * m);
+  }
+  if (F.fz == 2) {
+    const T em = K > 0 ? e[cq - csz] : ec, ep = K < C.nz - 1 ? e[cq + csz] : ec;
+    const T m = T(0.5) * (ep - em);
+    val += (k & 1) ? T(0.25) * m : -(T(0.25) * m);
+  }
+  const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
+  F.sol[q] += val;
+}
+
+// FP64 residual r = src - A sol with sum r^2.  Blocks stride over (y, z) rows,
+// threads over x; r is stored as TO (double, or float for the FP32 cycle).
+template <typename TO>
+__global__ void __launch_bounds__(kRedThreads) k_residual_norm(LevelView<double> L, TO* r,
+                                                               ReduceScratch R, int slot) {
+  double acc[1] = {0.0};
+  const int rows = L.ny * L.nz;
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int j = row % L.ny, k = row / L.ny;
+    for (int i = threadIdx.x; i < L.nx; i += blockDim.x) {
+      const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
+      double s, d;
+      stencil(L, L.sol, i, j, k, q, s, d);
+      const double rr = L.src[q] - (s - d * L.sol[q]);
+      if (r) r[q] = (TO)rr;
+      acc[0] += rr * rr;
+    }
+  }
+  grid_sum_finish<1>(acc, R, slot);
+}
+
+// q = A d and sum d.q (the flexible-CG matrix product), rows as k_residual_norm.
+__global__ void __launch_bounds__(kRedThreads) k_apply_dot(LevelView<double> L,
+                                                           const double* __restrict__ dvec,
+                                                           double* qvec, ReduceScratch R,
+                                                           int slot) {
+  double acc[1] = {0.0};
+  const int rows = L.ny * L.nz;
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int j = row % L.ny, k = row / L.ny;
+    for (int i = threadIdx.x; i < L.nx; i += blockDim.x) {
+      const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
+      double s, d;
+      stencil(L, dvec, i, j, k, q, s, d);
+      const double a = s - d * dvec[q];
+      qvec[q] = a;
+      acc[0] += dvec[q] * a;
+    }
+  }
+  grid_sum_finish<1>(acc, R, slot);
+}
+
+// Dense solve of the coarsest level, one block: x = Minv b; one refinement
+// step when max|b - A x| > 1e-10 (mg_find_error / mg_solve_correct,
+// "DomainDecomposition/3D/lib/data/tree_multigrid.f90:175-238"); mean projection
+// (multigrid_final_exact's compatibility_sol, multigrid_solver.f90:100).
+template <typename T>
+__global__ void __launch_bounds__(kMaxCoarse) k_coarse_solve(int n, const T* __restrict__ minv,
+                                                             const T* __restrict__ a,
+                                                             const T* __restrict__ b, T* x) {
+  __shared__ T sb[kMaxCoarse], sx[kMaxCoarse], se[kMaxCoarse];
+  __shared__ T red[kMaxCoarse];
+  __shared__ int refine;
+  const int t = threadIdx.x;
+  if (t == 0) refine = 0;
+  if (t < n) sb[t] = b[t];
+  __syncthreads();
+  if (t < n) {
+    T acc = T(0);
+    for (int q = 0; q < n; ++q) acc += minv[t * n + q] * sb[q];
+    sx[t] = acc;
+  }
+  __syncthreads();
+  if (t < n) {
+    T e = sb[t];
+    for (int q = 0; q < n; ++q) e -= a[t * n + q] * sx[q];
+    se[t] = e;
+    if (fabs((double)e) > 1e-10) atomicOr(&refine, 1);
+  }
+  __syncthreads();
+  if (refine && t < n) {
+    T acc = T(0);
+    for (int q = 0; q < n; ++q) acc += minv[t * n + q] * se[q];
+    sx[t] += acc;
+  }
+  __syncthreads();
+  // mean projection, summed in index order by thread 0 (n <= 64)
+  if (t == 0) {
+    T s = T(0);
+    for (int q = 0; q < n; ++q) s += sx[q];
+    red[0] = s / T(n);
+  }
+  __syncthreads();
+  if (t < n) x[t] = sx[t] - red[0];
+}
+
+// Coarsest-level operator and its inverse, one block, FP64.  The dense
+// Neumann matrix A is singular (constant null space); M = A - s 11^T/n with s
+// the mean diagonal is not, and M^{-1} b is the mean-free solution for a
+// mean-free b.  Gauss-Jordan with partial pivoting in shared memory.  The
+// reference LU-factors the singular matrix with LAPACK dgesv instead
+// ("DomainDecomposition/3D/lib/data/tree_multigrid.f90:134-173").
+__global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, double* minv,
+                                                       double* adense, float* minv32,
+                                                       float* adense32) {
+  extern __shared__ double smem[];
+  const int n = C.nx * C.ny * C.nz;
+  const int w = 2 * n;
+  double* M = smem;                  // n x 2n augmented matrix
+  double* f = smem + (size_t)n * w;  // column factors
+  __shared__ double dsum_sh;
+  __shared__ int piv_sh;
+  const int t = threadIdx.x, nt = blockDim.x;
+  for (int e = t; e < n * n; e += nt) adense[e] = 0.0;
+  __syncthreads();
+  if (t == 0) {
+    // assemble in the oracle's order (serial, n <= 64)
+    double dsum = 0.0;
+    for (int k = 0; k < C.nz; ++k)
+      for (int j = 0; j < C.ny; ++j)
+        for (int i = 0; i < C.nx; ++i) {
+          const int q = (k * C.ny + j) * C.nx + i;
+          double d = 0.0, c;
+          if (i > 0) { c = C.cx[q]; adense[q * n + q - 1] += c; d += c; }
+          if (i < C.nx - 1) { c = C.cx[q + 1]; adense[q * n + q + 1] += c; d += c; }
+          if (j > 0) { c = C.cy[q]; adense[q * n + q - C.nx] += c; d += c; }
+          if (j < C.ny - 1) { c = C.cy[q + C.nx]; adense[q * n + q + C.nx] += c; d += c; }
+          if (k > 0) { c = C.cz[q]; adense[q * n + q - C.nx * C.ny] += c; d += c; }
+          if (k < C.nz - 1) { c = C.cz[q + C.nx * C.ny]; adense[q * n + q + C.nx * C.ny] += c; d += c; }
+          adense[q * n + q] -= d;
+          dsum += d;
+        }
+    double s = n > 0 ? dsum / n : 1.0;
+    if (s <= 0.0) s = 1.0;
+    dsum_sh = s;
+  }
+  __syncthreads();
+  const double s = dsum_sh;
+  for (int e = t; e < n * w; e += nt) {
+    const int r = e / w, q = e % w;
+    M[e] = q < n ? adense[r * n + q] - s / n : (q - n == r ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  for (int col = 0; col < n; ++col) {
+    if (t == 0) {
+      int piv = col;
+      double best = fabs(M[col * w + col]);
+      for (int r = col + 1; r < n; ++r) {
+        const double v = fabs(M[r * w + col]);
+        if (v > best) { best = v; piv = r; }
+      }
+      piv_sh = piv;
+    }
+    __syncthreads();
+    const int piv = piv_sh;
+    if (piv != col)
+      for (int q = t; q < w; q += nt) {
+        const double tmp = M[col * w + q];
+        M[col * w + q] = M[piv * w + q];
+        M[piv * w + q] = tmp;
+      }
+    __syncthreads();
+    const double inv = 1.0 / M[col * w + col];
+    __syncthreads();
+    for (int q = t; q < w; q += nt) M[col * w + q] *= inv;
+    __syncthreads();
+    for (int r = t; r < n; r += nt) f[r] = M[r * w + col];
+    __syncthreads();
+    for (int e = t; e < n * w; e += nt) {
+      const int r = e / w, q = e % w;
+      if (r != col) M[e] -= f[r] * M[col * w + q];
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < n * n; e += nt) {
+    const int r = e / n, q = e % n;
+    const double v = M[r * w + n + q];
+    minv[e] = v;
+    if (minv32) minv32[e] = (float)v;
+    if (adense32) adense32[e] = (float)adense[e];
+  }
+}
+
+// Coarse face coefficients, rediscretised on spacing 2h from the mean of the
+// fine face coefficients covering each coarse face: coe_c = mean(coe_f)/f^2
+// along a coarsened axis (beta_c = mean beta_f).  The reference multigrid is
+// constant-coefficient and has no counterpart.
+__global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx, double* cy,
+                                                 double* cz, int cnx, int cny, int cnz) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= cnx || J >= cny) return;
+  const size_t cq = ((size_t)K * cny + J) * cnx + I;
+  const double tang = 1.0 / (double)(F.fx * F.fy * F.fz);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double* fc = a == 0 ? F.cx : (a == 1 ? F.cy : F.cz);
+    double* cc = a == 0 ? cx : (a == 1 ? cy : cz);
+    const int idx = a == 0 ? I : (a == 1 ? J : K);
+    const int fa = a == 0 ? F.fx : (a == 1 ? F.fy : F.fz);
+    if (idx == 0 || fa == 1) { cc[cq] = 0.0; continue; }
+    double acc = 0.0;
+    for (int dz = 0; dz < F.fz; ++dz)
+      for (int dy = 0; dy < F.fy; ++dy)
+        for (int dx = 0; dx < F.fx; ++dx) {
+          if ((a == 0 && dx) || (a == 1 && dy) || (a == 2 && dz)) continue;
+          const size_t fq = ((size_t)(F.fz * K + dz) * F.ny + (F.fy * J + dy)) * F.nx + (F.fx * I + dx);
+          acc += fc[fq];
+        }
+    acc *= tang * fa;
+    cc[cq] = acc / (double)(fa * fa);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_idiag(LevelView<double> L, double* idiag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= L.nx || j >= L.ny) return;
+  const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+  const size_t q = (size_t)k * sz + (size_t)j * sy + i;
+  double d = 0.0;
+  if (i > 0) d += L.cx[q];
+  if (i < L.nx - 1) d += L.cx[q + 1];
+  if (j > 0) d += L.cy[q];
+  if (j < L.ny - 1) d += L.cy[q + sy];
+  if (k > 0) d += L.cz[q];
+  if (k < L.nz - 1) d += L.cz[q + sz];
+  idiag[q] = d > 0.0 ? 1.0 / d : 0.0;
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    b[q] = (float)a[q];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+template <typename T>
+void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd(cdiv((size_t)(L.nx + 1) / 2, 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
+  if (L.idiag) k_smooth<T, true><<<grd, blk, 0, s>>>(L, color);
+  else k_smooth<T, false><<<grd, blk, 0, s>>>(L, color);
+}
+
+template <typename T>
+void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+  k_restrict<T><<<grd, blk, 0, s>>>(F, C);
+}
+
+template <typename T>
+void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd(cdiv((size_t)F.nx, 32), cdiv((size_t)F.ny, 8), (unsigned)F.nz);
+  k_prolong<T><<<grd, blk, 0, s>>>(F, C);
+}
+
+// Blocks for a grid-stride reduction: 8 per SM, at most one per row.  The SM
+// count is read once per process (every GPU of the target has the same).
+int reduce_blocks_for(size_t rows) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, v = 152;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) v = 152;
+    sms = v;
+  }
+  const size_t cap = (size_t)sms * 8;
+  return (int)(rows < cap ? (rows > 0 ? rows : 1) : cap);
+}
+
+template <typename TO>
+void launch_residual_norm(cudaStream_t s, const LevelView<double>& L, TO* r,
+                          const ReduceScratch& R, int slot) {
+  const int blocks = std::min(reduce_blocks_for((size_t)L.ny * L.nz), R.max_blocks);
+  k_residual_norm<TO><<<blocks, kRedThreads, 0, s>>>(L, r, R, slot);
+}
+
+void launch_apply_dot(cudaStream_t s, const LevelView<double>& L, const double* d, double* q,
+                      const ReduceScratch& R, int slot) {
+  const int blocks = std::min(reduce_blocks_for((size_t)L.ny * L.nz), R.max_blocks);
+  k_apply_dot<<<blocks, kRedThreads, 0, s>>>(L, d, q, R, slot);
+}
+
+template <typename T>
+void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, const T* b, T* x) {
+  k_coarse_solve<T><<<1, kMaxCoarse, 0, s>>>(n, minv, adense, b, x);
+}
+
+void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
+                          double* adense, float* minv32, float* adense32) {
+  const int n = C.nx * C.ny * C.nz;
+  const size_t shm = ((size_t)n * 2 * n + n) * sizeof(double);
+  cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_coarse_invert<<<1, 256, shm, s>>>(C, minv, adense, minv32, adense32);
+}
+
+void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,
+                    double* cz, int cnx, int cny, int cnz) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd(cdiv((size_t)cnx, 32), cdiv((size_t)cny, 8), (unsigned)cnz);
+  k_coarsen<<<grd, blk, 0, s>>>(F, cx, cy, cz, cnx, cny, cnz);
+}
+
+void launch_idiag(cudaStream_t s, const LevelView<double>& L, double* idiag) {
+  const dim3 blk(32, 8, 1);
+  const dim3 grd(cdiv((size_t)L.nx, 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
+  k_idiag<<<grd, blk, 0, s>>>(L, idiag);
+}
+
+void launch_to_float(cudaStream_t s, const double* a, float* b, size_t n) {
+  const unsigned blocks = (unsigned)std::min<size_t>(cdiv(n, 256), 152 * 16);
+  k_to_float<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(a, b, n);
+}
+
+template void launch_smooth<double>(cudaStream_t, const LevelView<double>&, int);
+template void launch_smooth<float>(cudaStream_t, const LevelView<float>&, int);
+template void launch_restrict<double>(cudaStream_t, const LevelView<double>&,
+                                      const LevelView<double>&);
+template void launch_restrict<float>(cudaStream_t, const LevelView<float>&,
+                                     const LevelView<float>&);
+template void launch_prolong<double>(cudaStream_t, const LevelView<double>&,
+                                     const LevelView<double>&);
+template void launch_prolong<float>(cudaStream_t, const LevelView<float>&,
+                                    const LevelView<float>&);
+template void launch_residual_norm<double>(cudaStream_t, const LevelView<double>&, double*,
+                                           const ReduceScratch&, int);
+template void launch_residual_norm<float>(cudaStream_t, const LevelView<double>&, float*,
+                                          const ReduceScratch&, int);
+template void launch_coarse_solve<double>(cudaStream_t, int, const double*, const double*,
+                                          const double*, double*);
+template void launch_coarse_solve<float>(cudaStream_t, int, const float*, const float*,
+                                         const float*, float*);
+
+}  // namespace gbmg

@@ -1,0 +1,300 @@
+"""Host-side mirror of the reference's pressure routine, over libgbmg's C ABI.
+
+The reference ("Two phase flows/newOpenMP/{2D,3D+IBM}/src/ns_solver/
+ns_ppe_solver.f90") calls, once per Adams-Bashforth sub-iteration,
+
+    call ppe_sor_init                 ! face coefficients 2/(rho_i+rho_nb)/h^2
+    call ppe_sor_solver(p%glb%p_tol)  ! b = div(u*)/dt, iterate, then
+                                      ! ns_momentum_correction: u -= dt grad(p)/rho_f
+
+PressurePoisson keeps those names and meanings: ppe_init(rho) is
+ppe_sor_init, ppe_solver(u, v, w, dt, tol, p) is ppe_sor_solver including the
+momentum correction, rho_mu(phi, ...) is the density chain of
+interface_solver/others.f90.  Where the reference STOPs the program
+(non-convergence, ns_ppe_solver.f90:154-157) this raises ConvergenceError.
+
+Arrays: numpy float64 arrays live in host memory; torch float64 CUDA tensors
+are used in place on the device.  Cell arrays have shape (nz, ny, nx) (or
+(ny, nx) in 2D); face velocities (nz, ny, nx+1), (nz, ny+1, nx),
+(nz+1, ny, nx).  x must be contiguous; y and z strides are free, so views of
+ghost-padded arrays work.  All work runs on the handle's own CUDA stream;
+every call returns after its work finished.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+try:  # torch is optional for host-memory use
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+
+class GBMGError(RuntimeError):
+    """A libgbmg call failed (invalid argument, CUDA error, wrong call order)."""
+
+
+class ConvergenceError(RuntimeError):
+    """The solve did not reach the tolerance (the reference STOPs here)."""
+
+    def __init__(self, msg, stats):
+        super().__init__(msg)
+        self.stats = stats
+
+
+def _is_torch(a):
+    return torch is not None and isinstance(a, torch.Tensor)
+
+
+def _as3(a):
+    if a is None:
+        return None
+    if a.ndim == 2:
+        return a.reshape((1,) + tuple(a.shape)) if not _is_torch(a) else a.unsqueeze(0)
+    if a.ndim != 3:
+        raise ValueError(f"expected a 2D or 3D array, got shape {tuple(a.shape)}")
+    return a
+
+
+def _field(a, shape):
+    """gbmg_field of an array whose logical extent is `shape` (nz, ny, nx)."""
+    if a is None:
+        return _lib.Field(None, 0, 0), None
+    a = _as3(a)
+    if tuple(a.shape) != tuple(shape):
+        raise ValueError(f"expected shape {tuple(shape)}, got {tuple(a.shape)}")
+    if _is_torch(a):
+        if a.dtype != torch.float64:
+            raise TypeError("tensors must be float64")
+        if not a.is_cuda:
+            a = a.contiguous().numpy()
+        else:
+            if a.stride(2) != 1:
+                raise ValueError("x must be contiguous")
+            return _lib.Field(a.data_ptr(), a.stride(1), a.stride(0)), _lib.GBMG_MEM_DEVICE
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64:
+        raise TypeError("arrays must be float64 numpy arrays or torch tensors")
+    if a.strides[2] != 8:
+        raise ValueError("x must be contiguous")
+    return _lib.Field(a.ctypes.data, a.strides[1] // 8, a.strides[0] // 8), _lib.GBMG_MEM_HOST
+
+
+def _mem_of(*pairs):
+    mems = {m for _, m in pairs if m is not None}
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must be in the same memory (host or CUDA)")
+    return mems.pop()
+
+
+class PressurePoisson:
+    """Variable-coefficient pressure-Poisson multigrid on one GB300.
+
+    shape: (nz, ny, nx) cells (nz = 1 for 2D); spacing: (dx, dy, dz).
+    precision: "fp64" (FP64 V-cycles) or "mixed" (FP32 V-cycles inside FP64
+    defect correction).  krylov=True wraps one V-cycle per iteration in
+    flexible CG.
+    """
+
+    def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
+                 max_cycles=100, krylov=False, use_graph=True, remove_rhs_mean=True, device=None,
+                 stream=None):
+        if len(shape) == 2:
+            shape = (1,) + tuple(shape)
+        self.shape = tuple(int(s) for s in shape)
+        nz, ny, nx = self.shape
+        if len(spacing) == 2:
+            spacing = tuple(spacing) + (1.0,)
+        self.spacing = tuple(float(s) for s in spacing)
+        self.precision = precision
+        L = _lib.load()
+        self._L = L
+        prm = _lib.Params()
+        L.gbmg_default_params(C.byref(prm))
+        prm.precision = {"fp64": _lib.GBMG_PREC_FP64, "mixed": _lib.GBMG_PREC_MIXED}[precision]
+        prm.nu1, prm.nu2 = nu1, nu2
+        prm.levels, prm.coarse_max, prm.max_cycles = levels, coarse_max, max_cycles
+        prm.krylov = int(bool(krylov))
+        prm.use_graph = int(bool(use_graph))
+        prm.remove_rhs_mean = int(bool(remove_rhs_mean))
+        prm.device = -1 if device is None else int(device)
+        # a torch.cuda.Stream, or a raw cudaStream_t handle; None = the handle's own stream
+        prm.stream = getattr(stream, "cuda_stream", stream) or None
+        if device is not None and torch is not None:
+            torch.cuda.set_device(int(device))
+        g = _lib.Grid(nx, ny, nz, *self.spacing)
+        h = C.c_void_p()
+        rc = L.gbmg_create(C.byref(g), C.byref(prm), C.byref(h))
+        if rc != _lib.GBMG_OK:
+            raise GBMGError(f"gbmg_create: {L.gbmg_strerror(rc).decode()}")
+        self._h = h
+
+    # -- lifetime --------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gbmg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- helpers ---------------------------------------------------------------
+    def _check(self, rc, what):
+        if rc != _lib.GBMG_OK:
+            msg = self._L.gbmg_last_error(self._h).decode()
+            raise GBMGError(f"{what}: {self._L.gbmg_strerror(rc).decode()} {msg}".strip())
+
+    @staticmethod
+    def _sync_torch(*arrays):
+        if torch is not None and any(_is_torch(a) and a.is_cuda for a in arrays if a is not None):
+            torch.cuda.current_stream().synchronize()
+
+    def _faces(self):
+        nz, ny, nx = self.shape
+        return (nz, ny, nx + 1), (nz, ny + 1, nx), (nz + 1, ny, nx)
+
+    # -- coefficients (ppe_sor_init, rho_mu) -------------------------------------
+    def ppe_init(self, rho):
+        """ppe_sor_init: face coefficients 2/(rho_i + rho_nb)/h^2 from cell density."""
+        f, m = _field(rho, self.shape)
+        self._sync_torch(rho)
+        self._check(self._L.gbmg_set_rho(self._h, f, m), "ppe_init")
+
+    def rho_mu(self, phi, eps, rho_pos=1.0, rho_neg=1e-3):
+        """rho_mu + ppe_sor_init: rho = rho_pos H(phi) + rho_neg (1 - H(phi))."""
+        f, m = _field(phi, self.shape)
+        self._sync_torch(phi)
+        self._check(self._L.gbmg_set_phi(self._h, f, eps, rho_pos, rho_neg, m), "rho_mu")
+
+    def set_coef(self, cx, cy, cz):
+        """Face coefficients given directly (cell-shaped low-face arrays)."""
+        fx, m1 = _field(cx, self.shape)
+        fy, m2 = _field(cy, self.shape)
+        fz, m3 = _field(cz, self.shape)
+        m = _mem_of((fx, m1), (fy, m2), (fz, m3))
+        self._sync_torch(cx, cy, cz)
+        self._check(self._L.gbmg_set_coef(self._h, fx, fy, fz, m), "set_coef")
+
+    # -- solves ------------------------------------------------------------------
+    def solve(self, b, p=None, tol=1e-10, check=True):
+        """Solve A p = b (p: initial guess, overwritten with the mean-free
+        solution).  Returns (p, stats)."""
+        if p is None:
+            p = torch.zeros_like(b) if _is_torch(b) else np.zeros_like(b)
+        fb, m1 = _field(b, self.shape)
+        fp, m2 = _field(p, self.shape)
+        m = _mem_of((fb, m1), (fp, m2))
+        self._sync_torch(b, p)
+        st = _lib.Stats()
+        rc = self._L.gbmg_solve(self._h, fb, fp, float(tol), m, C.byref(st))
+        stats = st.as_dict()
+        self._finish(rc, stats, check, "solve")
+        return p, stats
+
+    def ppe_solver(self, u, v, w, dt, tol=1e-10, p=None, check=True):
+        """ppe_sor_solver + ns_momentum_correction: b = div(u*)/dt, solve, and
+        correct u, v, w in place.  Returns (p, stats)."""
+        if p is None:
+            p = torch.zeros(self.shape, dtype=torch.float64, device=u.device) if _is_torch(u) \
+                else np.zeros(self.shape)
+        su, sv, sw = self._faces()
+        fu, m1 = _field(u, su)
+        fv, m2 = _field(v, sv)
+        fw, m3 = _field(w if self.shape[0] > 1 else None, sw)
+        fp, m4 = _field(p, self.shape)
+        m = _mem_of((fu, m1), (fv, m2), (fp, m4), *(((fw, m3),) if m3 is not None else ()))
+        self._sync_torch(u, v, w, p)
+        st = _lib.Stats()
+        rc = self._L.gbmg_project(self._h, fu, fv, fw, fp, float(dt), float(tol), m, C.byref(st))
+        stats = st.as_dict()
+        self._finish(rc, stats, check, "ppe_solver")
+        return p, stats
+
+    def _finish(self, rc, stats, check, what):
+        if rc in (_lib.GBMG_OK,):
+            return
+        if rc in (_lib.GBMG_NOT_CONVERGED, _lib.GBMG_DIVERGED):
+            if check:
+                raise ConvergenceError(
+                    f"{what}: {self._L.gbmg_strerror(rc).decode()} after {stats['cycles']} cycles, "
+                    f"relative residual {stats['rel_residual']:.3e}", stats)
+            return
+        self._check(rc, what)
+
+    # -- diagnostics ------------------------------------------------------------
+    def divergence(self, u, v, w, dt, out=None):
+        su, sv, sw = self._faces()
+        fu, m1 = _field(u, su)
+        fv, m2 = _field(v, sv)
+        fw, m3 = _field(w if self.shape[0] > 1 else None, sw)
+        if out is None:
+            out = torch.empty(self.shape, dtype=torch.float64, device=u.device) if _is_torch(u) \
+                else np.empty(self.shape)
+        fb, m4 = _field(out, self.shape)
+        m = _mem_of((fu, m1), (fv, m2), (fb, m4), *(((fw, m3),) if m3 is not None else ()))
+        self._sync_torch(u, v, w)
+        self._check(self._L.gbmg_divergence(self._h, fu, fv, fw, float(dt), fb, m), "divergence")
+        return out
+
+    def residual(self, b, p, out=None, want_r=True):
+        fb, m1 = _field(b, self.shape)
+        fp, m2 = _field(p, self.shape)
+        if want_r and out is None:
+            out = torch.empty_like(b) if _is_torch(b) else np.empty(self.shape)
+        fr, _ = _field(out, self.shape) if want_r else (_lib.Field(None, 0, 0), None)
+        m = _mem_of((fb, m1), (fp, m2))
+        n2 = C.c_double()
+        self._sync_torch(b, p)
+        self._check(self._L.gbmg_residual(self._h, fb, fp, fr, C.byref(n2), m), "residual")
+        return out, n2.value
+
+    def div_stats(self, u, v, w):
+        su, sv, sw = self._faces()
+        fu, m1 = _field(u, su)
+        fv, m2 = _field(v, sv)
+        fw, m3 = _field(w if self.shape[0] > 1 else None, sw)
+        m = _mem_of((fu, m1), (fv, m2), *(((fw, m3),) if m3 is not None else ()))
+        mx, mean = C.c_double(), C.c_double()
+        self._sync_torch(u, v, w)
+        self._check(self._L.gbmg_div_stats(self._h, fu, fv, fw, C.byref(mx), C.byref(mean), m),
+                    "div_stats")
+        return mx.value, mean.value
+
+    def level_dims(self):
+        n = C.c_int32()
+        dims = (C.c_int32 * 96)()
+        self._L.gbmg_level_dims(self._h, C.byref(n), dims, 32)
+        return [(dims[3 * l + 2], dims[3 * l + 1], dims[3 * l]) for l in range(n.value)]
+
+    def level_coef(self, level):
+        shape = self.level_dims()[level]
+        out = [np.empty(shape) for _ in range(3)]
+        f = [_field(a, shape)[0] for a in out]
+        self._check(self._L.gbmg_level_coef(self._h, level, *f, _lib.GBMG_MEM_HOST), "level_coef")
+        return out
+
+    @property
+    def kernel_launches(self):
+        return int(self._L.gbmg_kernel_launches(self._h))
+
+    def set_profiling(self, on=True):
+        """Time every launch with CUDA events, per kernel class (graphs off)."""
+        self._check(self._L.gbmg_set_profiling(self._h, int(bool(on))), "set_profiling")
+
+    def profile(self):
+        """{class: (total ms, launches)} since profiling was switched on."""
+        n = len(_lib.PROF_CLASSES)
+        ms = (C.c_double * n)()
+        cnt = (C.c_int64 * n)()
+        self._check(self._L.gbmg_profile(self._h, ms, cnt, n), "profile")
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(_lib.PROF_CLASSES)}

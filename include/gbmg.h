@@ -1,0 +1,199 @@
+/*
+ * gbmg.h -- C ABI of the GB300 pressure-Poisson multigrid.
+ *
+ * Drop-in for the pressure routine of the reference's two-phase solvers
+ * (ntu-d09525007/FortranCFD).  The reference has no C interface: its pressure
+ * step is a set of Fortran subroutines over module state, called as
+ *     call ppe_sor_init                      ("Two phase flows/newOpenMP/3D+IBM/
+ *     call ppe_sor_solver(p%glb%p_tol)         src/ns_solver/admas_bashforth_solver.f90:50,62")
+ * with ppe_sor_solver ending in ns_momentum_correction
+ * ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-205"),
+ * or as CALL SOLVE_PRESSURE_POISSON() ("MPLS_RisingBubble/20190612/SOLVE_NS.F90:35").
+ * Each entry point below names the routine it replaces.  Plain pointers and
+ * sizes only; a Fortran host binds them with ISO_C_BINDING.
+ *
+ * Arrays.  Every array is a gbmg_field: the address of element (0,0,0) plus
+ * the element strides of y and z; x is contiguous.  Cell arrays hold
+ * nx*ny*nz interior cells.  Face velocities follow the reference's MAC layout:
+ * u(f, j, k) is the x-face at x = f*dx for f = 0..nx (the reference's
+ * u(i,j,k) on face i+1/2 with 1-based cells), v(i, f, k) with f = 0..ny,
+ * w(i, j, f) with f = 0..nz.  A Fortran caller with ghost width g passes
+ * c_loc(p(1,1,1)) with sy = nx+2g, sz = (nx+2g)*(ny+2g), and c_loc(u(0,1,1))
+ * with the same strides.  Memory is host or device memory (GBMG_MEM_*).
+ *
+ * Operator: (A p)_i = sum over faces f of coe_f (p_nb - p_i), coe_f =
+ * 2/(rho_i + rho_nb)/h^2, zero on walls (homogeneous Neumann, folded as in
+ * ppe_sor_init).  The solve finds the mean-free p with A p = b to a relative
+ * residual ||b - A p||_2/||b||_2 < tol.
+ *
+ * Errors never abort: every call returns a gbmg_status.  A solve that reaches
+ * max_cycles returns GBMG_NOT_CONVERGED with the best iterate in p (the
+ * reference STOPs the program instead, ns_ppe_solver.f90:154-157).
+ * Threading: a handle is not re-entrant; use one handle per host thread.  All
+ * work runs on the handle's stream and every call returns after it finished.
+ */
+#ifndef GBMG_H
+#define GBMG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GBMG_OK = 0,
+  GBMG_NOT_CONVERGED = 1,
+  GBMG_DIVERGED = 2,
+  GBMG_INVALID_ARG = 3,
+  GBMG_CUDA_ERROR = 4,
+  GBMG_NO_DEVICE = 5,
+  GBMG_OUT_OF_MEMORY = 6,
+  GBMG_STATE_ERROR = 7
+} gbmg_status;
+
+enum { GBMG_PREC_FP64 = 0, GBMG_PREC_MIXED = 1 };
+enum { GBMG_MEM_HOST = 0, GBMG_MEM_DEVICE = 1 };
+
+typedef struct {
+  int32_t nx, ny, nz; /* interior cells; nz = 1 for a 2D problem */
+  double dx, dy, dz;  /* cell sizes (dz ignored when nz = 1) */
+} gbmg_grid;
+
+typedef struct {
+  int32_t precision;       /* GBMG_PREC_FP64: FP64 V-cycles; GBMG_PREC_MIXED: FP32 V-cycles
+                              inside FP64 defect correction */
+  int32_t nu1, nu2;        /* red-black Gauss-Seidel sweeps before/after the coarse correction */
+  int32_t levels;          /* 0 = automatic; else the reference's "Multigrid level" count */
+  int32_t coarse_max;      /* automatic levels: coarsen until at most this many cells (<= 64) */
+  int32_t max_cycles;      /* cycle (or Krylov iteration) limit */
+  int32_t krylov;          /* 0: stationary V-cycles; 1: flexible CG, one V-cycle as preconditioner */
+  int32_t use_graph;       /* 1: replay each cycle as a captured CUDA graph */
+  int32_t remove_rhs_mean; /* 1: project the mean out of b before solving (compatibility) */
+  int32_t device;          /* CUDA device ordinal; -1 = the current device */
+  void* stream;            /* cudaStream_t to run on; NULL = the handle creates its own */
+} gbmg_params;
+
+typedef struct {
+  int32_t status;       /* gbmg_status of the solve */
+  int32_t cycles;       /* V-cycles (or Krylov iterations) done */
+  int32_t levels;       /* multigrid levels used */
+  int32_t coarse_n;     /* cells on the coarsest level (solved directly) */
+  double rel_residual;  /* ||b - A p||_2 / ||b||_2 at exit (FP64) */
+  double rms_residual;  /* sqrt(sum r^2 / n): the reference's multigrid norm */
+  double res0;          /* relative residual of the initial guess */
+  double ms;            /* device time of the call (CUDA events on the handle's stream) */
+  double bytes;         /* algorithmic HBM bytes of the call (model in the design doc) */
+} gbmg_stats;
+
+typedef struct {
+  double* data; /* address of element (0,0,0) */
+  int64_t sy;   /* element stride between y rows */
+  int64_t sz;   /* element stride between z planes */
+} gbmg_field;
+
+typedef struct gbmg_handle gbmg_handle;
+
+/* Defaults: FP64, V(2,2), automatic levels, coarse_max 64, 100 cycles,
+ * stationary cycles, graphs on, mean projection of b on, current device. */
+void gbmg_default_params(gbmg_params* prm);
+
+/* Allocates the device hierarchy for one grid.  Replaces the level set-up of
+ * manager_init ("DomainDecomposition/3D/lib/data/branches.f90:172-216").
+ * Returns GBMG_INVALID_ARG for a grid the hierarchy cannot coarsen as asked. */
+int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out);
+
+int gbmg_destroy(gbmg_handle* h);
+
+/* Face coefficients from the cell density rho: ppe_sor_init
+ * ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-65";
+ * 2D "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ppe_solver.f90:1-48").
+ * Also builds every coarse level and the coarse-level inverse. */
+int gbmg_set_rho(gbmg_handle* h, gbmg_field rho, int mem);
+
+/* Density from the level set, then as gbmg_set_rho: rho_mu + ls_funs
+ * ("Two phase flows/newOpenMP/2D/src/interface_solver/others.f90:1-61"):
+ * rho = rho_pos*H + rho_neg*(1-H), H the smoothed Heaviside of half width eps.
+ * The reference is rho_pos = 1, rho_neg = rho_12. */
+int gbmg_set_phi(gbmg_handle* h, gbmg_field phi, double eps, double rho_pos, double rho_neg,
+                 int mem);
+
+/* Face coefficients given directly as cell-shaped low-face arrays (cx(i,j,k)
+ * couples cells i-1 and i; cx(0,j,k) is ignored and taken as the wall). */
+int gbmg_set_coef(gbmg_handle* h, gbmg_field cx, gbmg_field cy, gbmg_field cz, int mem);
+
+/* Solve A p = b.  p is the initial guess on entry (the reference warm-starts
+ * from the previous pressure) and the mean-free solution on exit.  Replaces
+ * the iteration of ppe_sor_solver (ns_ppe_solver.f90:93-163) and of
+ * ppe_mg_solver ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90:1-60"). */
+int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
+               gbmg_stats* stats);
+
+/* The whole projection, ppe_sor_solver + ns_momentum_correction
+ * (ns_ppe_solver.f90:67-205): b = div(u*)/dt, solve, then
+ * u_f -= dt (p_nb - p_i)/h / rho_f with rho_f the face average of rho (from the
+ * last gbmg_set_rho / gbmg_set_phi).  u, v, w are corrected in place; wall
+ * faces are left as given. */
+int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_field p,
+                 double dt, double tol, int mem, gbmg_stats* stats);
+
+/* b = div(u)/dt (the right-hand side of ppe_sor_solver, ns_ppe_solver.f90:77-89),
+ * without mean removal. */
+int gbmg_divergence(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double dt,
+                    gbmg_field b, int mem);
+
+/* r = b - A p with the current coefficients; *norm2 = sum r^2 (FP64).  r may
+ * have data == NULL (norm only).  The residual of multigrid_residual
+ * ("DomainDecomposition/3D/src/others/multigrid_solver.f90:162-222"). */
+int gbmg_residual(gbmg_handle* h, gbmg_field b, gbmg_field p, gbmg_field r, double* norm2,
+                  int mem);
+
+/* max and mean |div u| over the cells: ns_check_convergence_div
+ * ("Two phase flows/newOpenMP/2D/src/ns_solver/ns_solvers.f90:55-83"). */
+int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double* max_div,
+                   double* mean_div, int mem);
+
+/* Copies level `level`'s face coefficients (FP64) into cell-shaped arrays of
+ * that level's size (gbmg_level_dims).  For tests of the coarsening rule. */
+int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,
+                    int mem);
+
+/* Level count and per-level sizes (dims[3*l+0..2] = nx, ny, nz). */
+int gbmg_level_dims(gbmg_handle* h, int32_t* levels, int32_t* dims, int32_t max_levels);
+
+/* Number of kernels this handle launched since creation (graph replays count
+ * every kernel node). */
+int64_t gbmg_kernel_launches(gbmg_handle* h);
+
+/* Per-kernel-class timing (no reference counterpart; the reference only
+ * accumulates the wall time of the whole pressure step, ns_ppe_solver.f90:
+ * 75,167-168).  With profiling on, graphs are bypassed and every launch is
+ * bracketed by CUDA events on the handle's stream.  Classes: GBMG_PROF_*. */
+enum {
+  GBMG_PROF_SMOOTH_FINE = 0,   /* smoother on the finest level */
+  GBMG_PROF_SMOOTH_COARSE = 1, /* smoother on the other levels */
+  GBMG_PROF_RESTRICT_FINE = 2, /* residual + restriction out of the finest level */
+  GBMG_PROF_RESTRICT_COARSE = 3,
+  GBMG_PROF_PROLONG_FINE = 4,  /* prolongation + correction into the finest level */
+  GBMG_PROF_PROLONG_COARSE = 5,
+  GBMG_PROF_COARSE_SOLVE = 6,
+  GBMG_PROF_RESIDUAL = 7,      /* FP64 residual + norm on the finest level */
+  GBMG_PROF_VECTOR = 8,        /* mean projection, p += e, Krylov vector kernels */
+  GBMG_PROF_SETUP = 9,         /* coefficients, coarse operators, coarse inverse */
+  GBMG_PROF_CLASSES = 10
+};
+int gbmg_set_profiling(gbmg_handle* h, int on);
+/* ms[c] = summed device time, launches[c] = launch count of class c since
+ * profiling was switched on (arrays of n >= GBMG_PROF_CLASSES entries). */
+int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n);
+
+const char* gbmg_strerror(int status);
+
+/* Text of the last error on this handle ("" if none). */
+const char* gbmg_last_error(gbmg_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBMG_H */

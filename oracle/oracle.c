@@ -1,0 +1,881 @@
+/*
+ * oracle.c -- CPU restatement (FP64, C11 + OpenMP) of the pressure-Poisson
+ * path of ntu-d09525007/FortranCFD.  TEST INFRASTRUCTURE ONLY: the product
+ * (fortrancfd_gb300/) never links, loads or calls this file; it is used by
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, as
+ * the checker and the timed CPU reference.
+ *
+ * PARITY UNPINNED: the reference ships no tests, golden vectors or fixtures
+ * for this path, and it cannot be built here (Fortran + Intel MKL only).  The
+ * restatement is pinned instead by known-answer properties (manufactured
+ * solutions, operator symmetry and null space, convergence of the multigrid to
+ * the fully converged point-relaxation fixed point) in tests/.
+ *
+ * Every function cites the reference loop it follows.  Paths are relative to
+ * the reference project:
+ *   NO2 = "Two phase flows/newOpenMP/2D", NO3 = "Two phase flows/newOpenMP/3D+IBM"
+ *   MP3 = "MPLS_RisingBubble/20190612",  DD3 = "DomainDecomposition/3D"
+ *
+ * Layout (shared with the CUDA path): every cell array is dense, C order
+ * (z, y, x) with x fastest, which is the Fortran column-major (i, j, k) order
+ * of the reference without its ghost cells.  Face coefficients are stored in
+ * cell-shaped "low face" arrays: cx[k][j][i] couples cell (i-1,j,k) and
+ * (i,j,k); cx[..][..][0] is the x=0 wall and is 0.  The high wall of the last
+ * cell has no entry and is implicitly 0.  Zero wall coefficients are the
+ * Neumann folding of ppe_sor_init (NO3/src/ns_solver/ns_ppe_solver.f90:30-58):
+ * the wall term moves into the diagonal and vanishes from the sum, which is
+ * the same as a zero-gradient ghost (NO2/src/others/bcs.f90:1-26).
+ *
+ * Build: gcc -O3 -fopenmp -ffp-contract=off -fPIC -shared (see oracle/build.py);
+ * -ffp-contract=off keeps results bit-identical on x86_64 and aarch64.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+  int32_t nx, ny, nz;
+  double dx, dy, dz;
+} or_grid;
+
+/* Multigrid parameters.  Defaults in or_mg_default(). */
+typedef struct {
+  int32_t nu1, nu2;          /* pre/post sweeps per level: DD3 multigrid_solver.f90:57,158 use 2,2 */
+  int32_t levels;            /* 0 = auto (coarsen until <= coarse_max cells) */
+  int32_t coarse_max;        /* auto mode: stop coarsening at or below this many cells */
+  int32_t max_cycles;        /* DD3 ns_ppe_mg_solver.f90:17 uses 100 */
+  int32_t smoother;          /* 0 = red-black GS, 1 = lexicographic GS in blocks (DD3 relax) */
+  int32_t blocks[3];         /* lexicographic mode: subdomain grid (DD3 input/default.txt:5-6) */
+  int32_t mean_every_sweep;  /* 1 = compatibility_sol after every sweep (DD3 :43) */
+  int32_t coarse_op;         /* 0 = arithmetic face average, 1 = series-harmonic along the normal */
+  int32_t record_history;    /* fill stats->history with the per-cycle relative residual */
+  int32_t krylov;            /* 0 = stationary V-cycles (the reference's loop), 1 = flexible PCG
+                                with one V-cycle as the preconditioner */
+  int32_t prolong;           /* 0 = central-slope linear (DD3 :106-160), 1 = piecewise constant */
+  double coarse_scale;       /* multiplies the coarse correction before it is added */
+} or_mg_params;
+
+typedef struct {
+  int32_t cycles;
+  int32_t levels;
+  int32_t status;            /* 0 ok, 1 not converged, 2 diverged, 3 bad argument */
+  int32_t coarse_n;
+  double rel_residual;       /* ||b - A p||_2 / ||b||_2 */
+  double rms_residual;       /* sqrt(sum r^2 / n), the reference's l2norm (DD3 :204) */
+  double history[256];
+} or_mg_stats;
+
+#define OR_OK 0
+#define OR_NOT_CONVERGED 1
+#define OR_DIVERGED 2
+#define OR_BAD_ARG 3
+
+static inline size_t cells_of(int nx, int ny, int nz) { return (size_t)nx * ny * nz; }
+
+/* ------------------------------------------------------------------------- */
+/* a1: smoothed Heaviside and density.                                        */
+/* ls_funs / rho_mu, NO2/src/interface_solver/others.f90:1-37,39-61:          */
+/*   x = phi/eps; H = 1 if x > 1-1e-12, 0 if x < -1+1e-12,                    */
+/*   else 0.5(1 + x + sin(pi x)/pi); H clipped to [0,1];                      */
+/*   rho = H + rho_12 (1 - H)  (heavy fluid where phi > 0).                   */
+/* Generalised here to rho = rho_pos H + rho_neg (1 - H); the reference is     */
+/* rho_pos = 1, rho_neg = rho_12.                                             */
+/* ------------------------------------------------------------------------- */
+void or_heaviside(const double* phi, int64_t n, double eps, double* H) {
+  const double pi = acos(-1.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < n; ++q) {
+    double x = phi[q] / eps, h;
+    if (x > 1.0 - 1e-12) h = 1.0;
+    else if (x < -1.0 + 1e-12) h = 0.0;
+    else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+    H[q] = fmax(fmin(h, 1.0), 0.0);
+  }
+}
+
+/* Derivative of the smoothed Heaviside (others.f90:24: hp = (1+cos(pi x))/(2 eps)). */
+void or_heaviside_deriv(const double* phi, int64_t n, double eps, double* dH) {
+  const double pi = acos(-1.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < n; ++q) {
+    double x = phi[q] / eps;
+    dH[q] = (x > 1.0 - 1e-12 || x < -1.0 + 1e-12) ? 0.0 : 0.5 * (1.0 + cos(pi * x)) / eps;
+  }
+}
+
+void or_rho_from_phi(const double* phi, int64_t n, double eps, double rho_pos, double rho_neg,
+                     double* rho) {
+  or_heaviside(phi, n, eps, rho);
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < n; ++q) rho[q] = rho_pos * rho[q] + rho_neg * (1.0 - rho[q]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* a2: face coefficients, ppe_sor_init (NO3/src/ns_solver/ns_ppe_solver.f90:1-65; */
+/* 2D NO2 :1-48): coe_f = 2/(rho_i + rho_nb)/h^2, walls folded to 0.           */
+/* ------------------------------------------------------------------------- */
+void or_face_coef(const or_grid* g, const double* rho, double* cx, double* cy, double* cz) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const double dx2 = g->dx * g->dx, dy2 = g->dy * g->dy, dz2 = g->dz * g->dz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        cx[q] = (i > 0) ? 2.0 / (rho[q] + rho[q - 1]) / dx2 : 0.0;
+        cy[q] = (j > 0) ? 2.0 / (rho[q] + rho[q - nx]) / dy2 : 0.0;
+        cz[q] = (k > 0) ? 2.0 / (rho[q] + rho[q - (size_t)nx * ny]) / dz2 : 0.0;
+      }
+}
+
+/* ------------------------------------------------------------------------- */
+/* a3: RHS b = div(u*)/dt (NO3 ns_ppe_solver.f90:77-89; NO2 :60-69).          */
+/* Face velocities: u has shape (nz, ny, nx+1), u[.][.][f] on the x-face at    */
+/* x = f dx (reference u(f) with cells 1-based); v (nz, ny+1, nx); w (nz+1,    */
+/* ny, nx).  remove_mean subtracts the mean of b (the synthetic configs ask    */
+/* for a mean-free b; the reference relies on zero wall fluxes instead).       */
+/* ------------------------------------------------------------------------- */
+void or_divergence(const or_grid* g, const double* u, const double* v, const double* w, double dt,
+                   int remove_mean, double* b) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  double s = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        size_t qu = ((size_t)k * ny + j) * (nx + 1) + i;
+        size_t qv = ((size_t)k * (ny + 1) + j) * nx + i;
+        size_t qw = ((size_t)k * ny + j) * nx + i;
+        double d = (u[qu + 1] - u[qu]) / g->dx + (v[qv + nx] - v[qv]) / g->dy;
+        if (nz > 1 || w) d += (w[qw + (size_t)nx * ny] - w[qw]) / g->dz;
+        b[q] = d / dt;
+        s += b[q];
+      }
+  if (remove_mean) {
+    size_t n = cells_of(nx, ny, nz);
+    s /= (double)n;
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < n; ++q) b[q] -= s;
+  }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Operator: (A p)_i = sum_f coe_f (p_nb - p_i), the sign convention of every  */
+/* reference PPE (NO3 ns_ppe_solver.f90:104-111 solves p_i = (src - sum coe    */
+/* p_nb)/c with c = -sum coe).                                                */
+/* ------------------------------------------------------------------------- */
+static inline double stencil_sum(int nx, int ny, int nz, const double* cx, const double* cy,
+                                 const double* cz, const double* p, int i, int j, int k,
+                                 double* diag) {
+  size_t q = ((size_t)k * ny + j) * nx + i;
+  size_t sy = nx, sz = (size_t)nx * ny;
+  double s = 0.0, d = 0.0, c;
+  if (i > 0) { c = cx[q]; s += c * p[q - 1]; d += c; }
+  if (i < nx - 1) { c = cx[q + 1]; s += c * p[q + 1]; d += c; }
+  if (j > 0) { c = cy[q]; s += c * p[q - sy]; d += c; }
+  if (j < ny - 1) { c = cy[q + sy]; s += c * p[q + sy]; d += c; }
+  if (k > 0) { c = cz[q]; s += c * p[q - sz]; d += c; }
+  if (k < nz - 1) { c = cz[q + sz]; s += c * p[q + sz]; d += c; }
+  *diag = d;
+  return s;
+}
+
+void or_apply(const or_grid* g, const double* cx, const double* cy, const double* cz,
+              const double* p, double* Ap) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double d, s = stencil_sum(nx, ny, nz, cx, cy, cz, p, i, j, k, &d);
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        Ap[q] = s - d * p[q];
+      }
+}
+
+/* r = b - A p; returns sum r^2 (multigrid_residual, DD3 multigrid_solver.f90:162-222). */
+double or_residual(const or_grid* g, const double* cx, const double* cy, const double* cz,
+                   const double* p, const double* b, double* r) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  double s2 = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s2)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        double d, s = stencil_sum(nx, ny, nz, cx, cy, cz, p, i, j, k, &d);
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        double rr = b[q] - (s - d * p[q]);
+        if (r) r[q] = rr;
+        s2 += rr * rr;
+      }
+  return s2;
+}
+
+static double sum_of(const double* a, size_t n) {
+  double s = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s)
+  for (size_t q = 0; q < n; ++q) s += a[q];
+  return s;
+}
+
+/* compatibility_sol / compatibility_src (DD3 multigrid_solver.f90:224-308): a -= mean(a). */
+void or_remove_mean(double* a, int64_t n) {
+  double m = sum_of(a, (size_t)n) / (double)n;
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < n; ++q) a[q] -= m;
+}
+
+/* ------------------------------------------------------------------------- */
+/* a12: projection, ns_momentum_correction (NO3 ns_ppe_solver.f90:174-205):   */
+/* u_f -= dt (p_nb - p_i)/h / rho_f with rho_f = (rho_i + rho_nb)/2.  Wall     */
+/* faces are left untouched (velbc keeps them 0).  Face layout as in           */
+/* or_divergence.                                                             */
+/* ------------------------------------------------------------------------- */
+void or_correct(const or_grid* g, const double* rho, const double* p, double dt, double* u,
+                double* v, double* w) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        if (i > 0) {
+          double rf = (rho[q] + rho[q - 1]) / 2.0;
+          double px = (p[q] - p[q - 1]) / g->dx;
+          u[((size_t)k * ny + j) * (nx + 1) + i] -= dt * px / rf;
+        }
+        if (j > 0) {
+          double rf = (rho[q] + rho[q - nx]) / 2.0;
+          double py = (p[q] - p[q - nx]) / g->dy;
+          v[((size_t)k * (ny + 1) + j) * nx + i] -= dt * py / rf;
+        }
+        if (k > 0 && w) {
+          size_t sz = (size_t)nx * ny;
+          double rf = (rho[q] + rho[q - sz]) / 2.0;
+          double pz = (p[q] - p[q - sz]) / g->dz;
+          w[q] -= dt * pz / rf;
+        }
+      }
+}
+
+/* a13: max and mean |div u| (ns_check_convergence_div, NO2/src/ns_solver/ns_solvers.f90:55-83). */
+void or_div_stats(const or_grid* g, const double* u, const double* v, const double* w,
+                  double* out_max, double* out_mean) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  double mx = 0.0, sm = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : mx) reduction(+ : sm)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t qu = ((size_t)k * ny + j) * (nx + 1) + i;
+        size_t qv = ((size_t)k * (ny + 1) + j) * nx + i;
+        size_t qw = ((size_t)k * ny + j) * nx + i;
+        double d = (u[qu + 1] - u[qu]) / g->dx + (v[qv + nx] - v[qv]) / g->dy;
+        if (w) d += (w[qw + (size_t)nx * ny] - w[qw]) / g->dz;
+        d = fabs(d);
+        mx = d > mx ? d : mx;
+        sm += d;
+      }
+  *out_max = mx;
+  *out_mean = sm / (double)cells_of(nx, ny, nz);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Faithful point relaxation, ppe_sor_solver (NO2 ns_ppe_solver.f90:73-135;   */
+/* NO3 :93-163).  The reference sweeps in place under OpenMP (a data race);    */
+/* this serial restatement sweeps lexicographically.  Per iteration:           */
+/*   tmp = p; p_i = (src - sum coe p_nb)/c in place; p -= mean(p);             */
+/*   p = w p + (1-w) tmp; err = max|p - tmp|; stop when err < tol.             */
+/* max_iter replaces the reference's STOP (err > 10 after 1e5 sweeps).         */
+/* Returns the sweep count (negative if max_iter was reached).                 */
+/* ------------------------------------------------------------------------- */
+int64_t or_sor_solve(const or_grid* g, const double* cx, const double* cy, const double* cz,
+                     const double* b, double* p, double w, double tol, int64_t max_iter,
+                     double* out_err) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t n = cells_of(nx, ny, nz);
+  double* tmp = (double*)malloc(n * sizeof(double));
+  int64_t it = 0;
+  double err = 0.0;
+  for (;;) {
+    ++it;
+    memcpy(tmp, p, n * sizeof(double));
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          double d, s = stencil_sum(nx, ny, nz, cx, cy, cz, p, i, j, k, &d);
+          size_t q = ((size_t)k * ny + j) * nx + i;
+          p[q] = (b[q] - s) / (-d);
+        }
+    double m = sum_of(p, n) / (double)n;
+    err = 0.0;
+    for (size_t q = 0; q < n; ++q) {
+      p[q] -= m;
+      p[q] = w * p[q] + (1.0 - w) * tmp[q];
+      double e = fabs(p[q] - tmp[q]);
+      err = e > err ? e : err;
+    }
+    if (err < tol) break;
+    if (it >= max_iter) { it = -it; break; }
+  }
+  free(tmp);
+  if (out_err) *out_err = err;
+  return it;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Multigrid: the cycle of DD3 (multigrid_solver.f90:1-326, tree_multigrid.f90) */
+/* applied to the variable-coefficient operator of ppe_sor_init.              */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int nx, ny, nz;
+  int fx, fy, fz; /* coarsening factor from this level to the next (1 or 2) */
+  double *cx, *cy, *cz;
+  double *sol, *src, *res, *snap;
+} or_level;
+
+typedef struct {
+  int L;
+  or_level lv[32];
+  int nc;          /* coarsest cell count */
+  double* Minv;    /* nc x nc inverse of the mean-constrained coarsest operator */
+  double* Adense;  /* nc x nc coarsest operator (for the refinement step) */
+} or_mg;
+
+void or_mg_default(or_mg_params* prm) {
+  memset(prm, 0, sizeof(*prm));
+  prm->nu1 = 2;
+  prm->nu2 = 2;
+  prm->levels = 0;
+  prm->coarse_max = 64;
+  prm->max_cycles = 100;
+  prm->smoother = 0;
+  prm->blocks[0] = prm->blocks[1] = prm->blocks[2] = 1;
+  prm->mean_every_sweep = 1;
+  prm->coarse_op = 0;
+  prm->record_history = 1;
+  prm->krylov = 0;
+  prm->prolong = 0;
+  prm->coarse_scale = 1.0;
+}
+
+/* Level plan.  Each axis with more than one cell is halved per level; an axis
+ * of one cell (nz = 1 in 2D) is never coarsened.  Explicit levels require
+ * divisibility as manager_init does (DD3/lib/data/branches.f90:172-216);
+ * auto mode stops when the next halving is impossible or the level already
+ * has <= coarse_max cells.  Returns the level count or -1. */
+int or_mg_plan(int nx, int ny, int nz, int levels, int coarse_max, int32_t* dims_out) {
+  int L = 1;
+  int n[3] = {nx, ny, nz};
+  if (nx < 1 || ny < 1 || nz < 1) return -1;
+  if (dims_out) { dims_out[0] = nx; dims_out[1] = ny; dims_out[2] = nz; }
+  for (;;) {
+    if (levels > 0 && L >= levels) break;
+    if (levels <= 0 && (long)n[0] * n[1] * n[2] <= coarse_max) break;
+    int ok = 1, any = 0;
+    for (int a = 0; a < 3; ++a)
+      if (n[a] > 1) { any = 1; if (n[a] % 2) ok = 0; }
+    if (!ok || !any) {
+      if (levels > 0) return -1;
+      break;
+    }
+    for (int a = 0; a < 3; ++a)
+      if (n[a] > 1) n[a] /= 2;
+    if (dims_out) { dims_out[3 * L] = n[0]; dims_out[3 * L + 1] = n[1]; dims_out[3 * L + 2] = n[2]; }
+    ++L;
+    if (L >= 32) return -1;
+  }
+  return L;
+}
+
+/* Coarse face coefficients from the fine ones.  No reference counterpart (its
+ * multigrid is constant-coefficient, DD3 multigrid_solver.f90:12); the coarse
+ * operator is rediscretised with spacing 2h:
+ *   coarse_op 0: beta_c = mean of the fine face betas covering the coarse face;
+ *   coarse_op 1: along the normal, the fine links between the two coarse
+ *     centres in series (half, full, half link), averaged over the tangential
+ *     children: coe_c = mean_t 1/(1/c_{2I-1} + 2/c_{2I} + 1/c_{2I+1}).
+ * Both reduce to coe_c = coe/4 for constant coefficients. */
+static void coarsen_coef(const or_level* f, or_level* c, int op) {
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const int fx = f->fx, fy = f->fy, fz = f->fz;
+  const int fnx = f->nx, fny = f->ny;
+  const double tang = 1.0 / (double)(fx * fy * fz);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        size_t q = ((size_t)k * ny + j) * nx + i;
+        for (int a = 0; a < 3; ++a) {
+          const double* fc = a == 0 ? f->cx : (a == 1 ? f->cy : f->cz);
+          double* cc = a == 0 ? c->cx : (a == 1 ? c->cy : c->cz);
+          int idx = a == 0 ? i : (a == 1 ? j : k);
+          int fa = a == 0 ? fx : (a == 1 ? fy : fz);
+          if (idx == 0 || fa == 1) { cc[q] = 0.0; continue; }
+          size_t fs = a == 0 ? 1 : (a == 1 ? (size_t)fnx : (size_t)fnx * fny);
+          double acc = 0.0;
+          for (int dz = 0; dz < fz; ++dz)
+            for (int dy = 0; dy < fy; ++dy)
+              for (int dx = 0; dx < fx; ++dx) {
+                /* children that touch the coarse low face along axis a only */
+                if ((a == 0 && dx) || (a == 1 && dy) || (a == 2 && dz)) continue;
+                size_t fq = ((size_t)(fz * k + dz) * fny + (fy * j + dy)) * fnx + (fx * i + dx);
+                if (op == 0 || op == 2) {
+                  acc += fc[fq];
+                } else {
+                  double c1 = fc[fq - fs], c2 = fc[fq], c3 = fc[fq + fs];
+                  acc += (c1 > 0.0 && c2 > 0.0 && c3 > 0.0) ? 1.0 / (1.0 / c1 + 2.0 / c2 + 1.0 / c3) : 0.0;
+                }
+              }
+          /* fa children along the normal were skipped: the count is fx*fy*fz/fa */
+          acc *= tang * fa;
+          /* op 2: Galerkin R A P with piecewise-constant P and averaging R:
+           * sum of the crossing fine coefficients / 2^d = mean / fa */
+          cc[q] = op == 0 ? acc / (double)(fa * fa) : (op == 2 ? acc / (double)fa : acc);
+        }
+      }
+}
+
+static double* dalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+/* Dense solve of the coarsest level (manager_mg_setup / manager_mg_solve_exact /
+ * mg_find_error / mg_solve_correct, DD3 tree_multigrid.f90:1-238).  The
+ * reference LU-factors the singular Neumann matrix with dgesv; here the null
+ * space is removed first: M = A - s 11^T/n (s = mean diagonal), which is
+ * non-singular and gives the mean-free solution for a mean-free right-hand
+ * side.  M is inverted once per operator by Gauss-Jordan with partial
+ * pivoting; each cycle applies the inverse, does the reference's one
+ * refinement step when max|b - A x| > 1e-10, and projects the mean. */
+static int build_coarse(or_mg* mg) {
+  or_level* c = &mg->lv[mg->L - 1];
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const int n = nx * ny * nz;
+  mg->nc = n;
+  double* A = dalloc((size_t)n * n);
+  double* M = dalloc((size_t)n * 2 * n);
+  mg->Minv = dalloc((size_t)n * n);
+  mg->Adense = A;
+  double dsum = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        int q = (k * ny + j) * nx + i;
+        double d = 0.0, cc;
+        if (i > 0) { cc = c->cx[q]; A[(size_t)q * n + q - 1] += cc; d += cc; }
+        if (i < nx - 1) { cc = c->cx[q + 1]; A[(size_t)q * n + q + 1] += cc; d += cc; }
+        if (j > 0) { cc = c->cy[q]; A[(size_t)q * n + q - nx] += cc; d += cc; }
+        if (j < ny - 1) { cc = c->cy[q + nx]; A[(size_t)q * n + q + nx] += cc; d += cc; }
+        if (k > 0) { cc = c->cz[q]; A[(size_t)q * n + q - nx * ny] += cc; d += cc; }
+        if (k < nz - 1) { cc = c->cz[q + nx * ny]; A[(size_t)q * n + q + nx * ny] += cc; d += cc; }
+        A[(size_t)q * n + q] -= d;
+        dsum += d;
+      }
+  double s = (n > 0 ? dsum / n : 1.0);
+  if (s <= 0.0) s = 1.0;
+  for (int r = 0; r < n; ++r) {
+    for (int q = 0; q < n; ++q) M[(size_t)r * 2 * n + q] = A[(size_t)r * n + q] - s / n;
+    M[(size_t)r * 2 * n + n + r] = 1.0;
+  }
+  for (int col = 0; col < n; ++col) {
+    int piv = col;
+    double best = fabs(M[(size_t)col * 2 * n + col]);
+    for (int r = col + 1; r < n; ++r) {
+      double v = fabs(M[(size_t)r * 2 * n + col]);
+      if (v > best) { best = v; piv = r; }
+    }
+    if (best == 0.0) { free(M); return OR_BAD_ARG; }
+    if (piv != col)
+      for (int q = 0; q < 2 * n; ++q) {
+        double t = M[(size_t)col * 2 * n + q];
+        M[(size_t)col * 2 * n + q] = M[(size_t)piv * 2 * n + q];
+        M[(size_t)piv * 2 * n + q] = t;
+      }
+    double inv = 1.0 / M[(size_t)col * 2 * n + col];
+    for (int q = 0; q < 2 * n; ++q) M[(size_t)col * 2 * n + q] *= inv;
+    for (int r = 0; r < n; ++r) {
+      if (r == col) continue;
+      double f = M[(size_t)r * 2 * n + col];
+      if (f == 0.0) continue;
+      for (int q = 0; q < 2 * n; ++q) M[(size_t)r * 2 * n + q] -= f * M[(size_t)col * 2 * n + q];
+    }
+  }
+  for (int r = 0; r < n; ++r)
+    for (int q = 0; q < n; ++q) mg->Minv[(size_t)r * n + q] = M[(size_t)r * 2 * n + n + q];
+  free(M);
+  return OR_OK;
+}
+
+static void v_cycle(or_mg* mg, const or_mg_params* prm);
+static void coarse_solve(or_mg* mg) {
+  or_level* c = &mg->lv[mg->L - 1];
+  const int n = mg->nc;
+  double* x = c->sol;
+  const double* b = c->src;
+  double* e = dalloc(n);
+  for (int r = 0; r < n; ++r) {
+    double a = 0.0;
+    for (int q = 0; q < n; ++q) a += mg->Minv[(size_t)r * n + q] * b[q];
+    x[r] = a;
+  }
+  /* mg_find_error: error = b - A x; refine once when max|error| > 1e-10 */
+  double emax = 0.0;
+  for (int r = 0; r < n; ++r) {
+    double a = b[r];
+    for (int q = 0; q < n; ++q) a -= mg->Adense[(size_t)r * n + q] * x[q];
+    e[r] = a;
+    emax = fabs(a) > emax ? fabs(a) : emax;
+  }
+  if (emax > 1e-10) {
+    for (int r = 0; r < n; ++r) {
+      double a = 0.0;
+      for (int q = 0; q < n; ++q) a += mg->Minv[(size_t)r * n + q] * e[q];
+      x[r] += a;
+    }
+  }
+  free(e);
+  or_remove_mean(x, n); /* multigrid_final_exact: compatibility_sol (DD3 :100) */
+}
+
+static int mg_setup(or_mg* mg, const or_grid* g, const double* cx, const double* cy,
+                    const double* cz, const or_mg_params* prm) {
+  int32_t dims[96];
+  int L = or_mg_plan(g->nx, g->ny, g->nz, prm->levels, prm->coarse_max, dims);
+  if (L < 1) return OR_BAD_ARG;
+  memset(mg, 0, sizeof(*mg));
+  mg->L = L;
+  for (int l = 0; l < L; ++l) {
+    or_level* v = &mg->lv[l];
+    v->nx = dims[3 * l];
+    v->ny = dims[3 * l + 1];
+    v->nz = dims[3 * l + 2];
+    size_t n = cells_of(v->nx, v->ny, v->nz);
+    if (l + 1 < L) {
+      v->fx = v->nx / dims[3 * l + 3];
+      v->fy = v->ny / dims[3 * l + 4];
+      v->fz = v->nz / dims[3 * l + 5];
+    } else {
+      v->fx = v->fy = v->fz = 1;
+    }
+    if (l == 0) {
+      v->cx = (double*)cx; v->cy = (double*)cy; v->cz = (double*)cz;
+      v->src = NULL; v->sol = NULL;
+    } else {
+      v->cx = dalloc(n); v->cy = dalloc(n); v->cz = dalloc(n);
+      v->src = dalloc(n); v->sol = dalloc(n);
+    }
+    v->res = dalloc(n);
+    v->snap = dalloc(n);
+  }
+  for (int l = 1; l < L; ++l) coarsen_coef(&mg->lv[l - 1], &mg->lv[l], prm->coarse_op);
+  return build_coarse(mg);
+}
+
+static void mg_free(or_mg* mg) {
+  for (int l = 0; l < mg->L; ++l) {
+    or_level* v = &mg->lv[l];
+    if (l > 0) { free(v->cx); free(v->cy); free(v->cz); free(v->src); free(v->sol); }
+    free(v->res);
+    free(v->snap);
+  }
+  free(mg->Minv);
+  free(mg->Adense);
+}
+
+/* One smoothing sweep.  Red-black: all cells with (i+j+k) even, then odd,
+ * each colour from the latest values (deterministic, order-free).  Blocked
+ * lexicographic: the reference's multigrid_relax (DD3 multigrid_solver.f90:1-49)
+ * runs an in-place lexicographic Gauss-Seidel inside each OpenMP subdomain and
+ * reads neighbouring subdomains through halos refreshed only before the sweep
+ * (ptrmgpart_sync, DD3/lib/pointer/ptr_roots.f90:437-606); blocks = 1x1x1 is a
+ * plain serial lexicographic sweep. */
+static void smooth_sweep(or_level* v, const or_mg_params* prm, int reverse) {
+  const int nx = v->nx, ny = v->ny, nz = v->nz;
+  double* p = v->sol;
+  const double* b = v->src;
+  if (prm->smoother == 0) {
+    for (int cc = 0; cc < 2; ++cc) {
+      const int color = reverse ? 1 - cc : cc;
+#pragma omp parallel for schedule(static)
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = (j + k + color) & 1; i < nx; i += 2) {
+            double d, s = stencil_sum(nx, ny, nz, v->cx, v->cy, v->cz, p, i, j, k, &d);
+            size_t q = ((size_t)k * ny + j) * nx + i;
+            p[q] = (s - b[q]) / d;
+          }
+    }
+  } else {
+    const size_t n = cells_of(nx, ny, nz);
+    memcpy(v->snap, p, n * sizeof(double));
+    const int bx = prm->blocks[0] > 0 ? prm->blocks[0] : 1;
+    const int by = prm->blocks[1] > 0 ? prm->blocks[1] : 1;
+    const int bz = prm->blocks[2] > 0 ? prm->blocks[2] : 1;
+    const int nb = bx * by * bz;
+#pragma omp parallel for schedule(static)
+    for (int id = 0; id < nb; ++id) {
+      int ib = id % bx, jb = (id / bx) % by, kb = id / (bx * by);
+      int i0 = (int)((long)nx * ib / bx), i1 = (int)((long)nx * (ib + 1) / bx);
+      int j0 = (int)((long)ny * jb / by), j1 = (int)((long)ny * (jb + 1) / by);
+      int k0 = (int)((long)nz * kb / bz), k1 = (int)((long)nz * (kb + 1) / bz);
+      const size_t sy = nx, sz = (size_t)nx * ny;
+      for (int k = k0; k < k1; ++k)
+        for (int j = j0; j < j1; ++j)
+          for (int i = i0; i < i1; ++i) {
+            size_t q = ((size_t)k * ny + j) * nx + i;
+            double s = 0.0, d = 0.0, c;
+            /* neighbours inside the block: latest values; outside: the halo snapshot */
+            if (i > 0) { c = v->cx[q]; s += c * (i - 1 >= i0 ? p[q - 1] : v->snap[q - 1]); d += c; }
+            if (i < nx - 1) { c = v->cx[q + 1]; s += c * (i + 1 < i1 ? p[q + 1] : v->snap[q + 1]); d += c; }
+            if (j > 0) { c = v->cy[q]; s += c * (j - 1 >= j0 ? p[q - sy] : v->snap[q - sy]); d += c; }
+            if (j < ny - 1) { c = v->cy[q + sy]; s += c * (j + 1 < j1 ? p[q + sy] : v->snap[q + sy]); d += c; }
+            if (k > 0) { c = v->cz[q]; s += c * (k - 1 >= k0 ? p[q - sz] : v->snap[q - sz]); d += c; }
+            if (k < nz - 1) { c = v->cz[q + sz]; s += c * (k + 1 < k1 ? p[q + sz] : v->snap[q + sz]); d += c; }
+            p[q] = (s - b[q]) / d;
+          }
+    }
+  }
+}
+
+/* multigrid_relax (DD3 :1-49): num sweeps, each followed by compatibility_sol.
+ * reverse = 1 runs the red-black colours black-first (post-smoothing of the
+ * symmetric V-cycle used as a Krylov preconditioner). */
+static void relax(or_level* v, int num, const or_mg_params* prm, int reverse) {
+  const size_t n = cells_of(v->nx, v->ny, v->nz);
+  for (int s = 0; s < num; ++s) {
+    smooth_sweep(v, prm, reverse);
+    if (prm->mean_every_sweep) or_remove_mean(v->sol, (int64_t)n);
+  }
+}
+
+static double level_residual(or_level* v) {
+  or_grid g = {v->nx, v->ny, v->nz, 1, 1, 1};
+  return or_residual(&g, v->cx, v->cy, v->cz, v->sol, v->src, v->res);
+}
+
+/* multigrid_restriction (DD3 :51-90): relax, residual, coarse src = mean of the
+ * children's residuals, coarse sol = 0, compatibility_src. */
+static void restrict_level(or_mg* mg, int l, const or_mg_params* prm) {
+  or_level* f = &mg->lv[l];
+  or_level* c = &mg->lv[l + 1];
+  relax(f, prm->nu1, prm, 0);
+  level_residual(f);
+  const int fx = f->fx, fy = f->fy, fz = f->fz, fnx = f->nx, fny = f->ny;
+  const double w = 1.0 / (double)(fx * fy * fz);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < c->nz; ++k)
+    for (int j = 0; j < c->ny; ++j)
+      for (int i = 0; i < c->nx; ++i) {
+        double s = 0.0;
+        for (int dz = 0; dz < fz; ++dz)
+          for (int dy = 0; dy < fy; ++dy)
+            for (int dx = 0; dx < fx; ++dx)
+              s += f->res[((size_t)(fz * k + dz) * fny + (fy * j + dy)) * fnx + (fx * i + dx)];
+        size_t q = ((size_t)k * c->ny + j) * c->nx + i;
+        c->src[q] = s * w;
+        c->sol[q] = 0.0;
+      }
+  or_remove_mean(c->src, (int64_t)cells_of(c->nx, c->ny, c->nz));
+}
+
+/* multigrid_prolongation (DD3 :106-160): central slopes of the coarse solution
+ * with zero-gradient ghosts (ptrmgpart_sync copies the first interior cell into
+ * the wall ghost), child = e_c +/- m_x/4 +/- m_y/4 +/- m_z/4 on coarsened axes,
+ * sol += child value, then relax. */
+static void prolong_level(or_mg* mg, int l, const or_mg_params* prm) {
+  or_level* f = &mg->lv[l];
+  or_level* c = &mg->lv[l + 1];
+  const int cnx = c->nx, cny = c->ny, cnz = c->nz;
+  const size_t csy = cnx, csz = (size_t)cnx * cny;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < f->nz; ++k)
+    for (int j = 0; j < f->ny; ++j)
+      for (int i = 0; i < f->nx; ++i) {
+        int I = i / f->fx, J = j / f->fy, K = k / f->fz;
+        size_t cq = ((size_t)K * cny + J) * cnx + I;
+        const double* e = c->sol;
+        double ec = e[cq], val = ec;
+        if (prm->prolong == 1) {
+          f->sol[((size_t)k * f->ny + j) * f->nx + i] += prm->coarse_scale * val;
+          continue;
+        }
+        if (f->fx == 2) {
+          double em = I > 0 ? e[cq - 1] : ec, ep = I < cnx - 1 ? e[cq + 1] : ec;
+          double m = 0.5 * (ep - em);
+          val += (i & 1) ? 0.25 * m : -0.25 * m;
+        }
+        if (f->fy == 2) {
+          double em = J > 0 ? e[cq - csy] : ec, ep = J < cny - 1 ? e[cq + csy] : ec;
+          double m = 0.5 * (ep - em);
+          val += (j & 1) ? 0.25 * m : -0.25 * m;
+        }
+        if (f->fz == 2) {
+          double em = K > 0 ? e[cq - csz] : ec, ep = K < cnz - 1 ? e[cq + csz] : ec;
+          double m = 0.5 * (ep - em);
+          val += (k & 1) ? 0.25 * m : -0.25 * m;
+        }
+        f->sol[((size_t)k * f->ny + j) * f->nx + i] += prm->coarse_scale == 1.0 ? val : prm->coarse_scale * val;
+      }
+  relax(f, prm->nu2, prm, prm->krylov ? 1 : 0);
+}
+
+/* multigrid_v_cycle (DD3 :310-326). */
+static void v_cycle(or_mg* mg, const or_mg_params* prm) {
+  for (int l = 0; l < mg->L - 1; ++l) restrict_level(mg, l, prm);
+  coarse_solve(mg);
+  for (int l = mg->L - 2; l >= 0; --l) prolong_level(mg, l, prm);
+}
+
+static double dot(const double* a, const double* b, size_t n) {
+  double s = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : s)
+  for (size_t q = 0; q < n; ++q) s += a[q] * b[q];
+  return s;
+}
+
+/* Flexible preconditioned CG (Polak-Ribiere beta), preconditioner = one V-cycle
+ * from a zero initial guess on the residual.  No reference counterpart: an
+ * optional acceleration for many-bubble cases where the stationary cycle
+ * stalls on the near-null modes of isolated light bubbles.  A and the V-cycle
+ * are both negative (semi)definite; the signs cancel in alpha and beta. */
+static int pcg_loop(or_mg* mg, const or_mg_params* prm, const or_grid* g, double* p,
+                    const double* b, double bnorm, double tol, or_mg_stats* st, int* cyc_out,
+                    double* rel_out, double* r2_out) {
+  const size_t n = cells_of(g->nx, g->ny, g->nz);
+  or_level* f = &mg->lv[0];
+  double* r = dalloc(n);
+  double* z = dalloc(n);
+  double* zold = dalloc(n);
+  double* d = dalloc(n);
+  double* q = dalloc(n);
+  double* x = f->sol; /* == p */
+  double r2 = or_residual(g, f->cx, f->cy, f->cz, x, b, r);
+  double rel = sqrt(r2) / (bnorm > 0 ? bnorm : 1.0);
+  int status = OR_NOT_CONVERGED, it;
+  double rz = 0.0;
+  /* the V-cycle works on level 0's (sol, src) = (z, r) */
+  f->src = r;
+  for (it = 1; it <= prm->max_cycles; ++it) {
+    memset(z, 0, n * sizeof(double));
+    f->sol = z;
+    v_cycle(mg, prm);
+    or_remove_mean(z, (int64_t)n);
+    double rz_new = dot(r, z, n);
+    if (it == 1) {
+      memcpy(d, z, n * sizeof(double));
+    } else {
+      double beta = (rz_new - dot(r, zold, n)) / rz;
+#pragma omp parallel for schedule(static)
+      for (size_t k = 0; k < n; ++k) d[k] = z[k] + beta * d[k];
+    }
+    rz = rz_new;
+    memcpy(zold, z, n * sizeof(double));
+    or_apply(g, f->cx, f->cy, f->cz, d, q);
+    double alpha = rz / dot(d, q, n);
+#pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n; ++k) { x[k] += alpha * d[k]; r[k] -= alpha * q[k]; }
+    /* true residual for the stopping test, as the stationary loop does */
+    r2 = or_residual(g, f->cx, f->cy, f->cz, x, b, r);
+    rel = sqrt(r2) / (bnorm > 0 ? bnorm : 1.0);
+    if (prm->record_history && it <= 256) st->history[it - 1] = rel;
+    if (!isfinite(rel) || rel > 1e3) { status = OR_DIVERGED; break; }
+    if (rel < tol) { status = OR_OK; break; }
+  }
+  if (it > prm->max_cycles) it = prm->max_cycles;
+  f->sol = p;
+  f->src = (double*)b;
+  free(r); free(z); free(zold); free(d); free(q);
+  *cyc_out = it;
+  *rel_out = rel;
+  *r2_out = r2;
+  return status;
+}
+
+/* The solve.  Outer loop as ppe_mg_solver (DD3/src/ns_solver/ns_ppe_mg_solver.f90:
+ * 17-50): V-cycles until the relative residual ||b - A p||_2/||b||_2 < tol, at
+ * most max_cycles.  p is the initial guess on entry (warm start) and the
+ * mean-free solution on exit.  b must be mean-free (compatible). */
+int or_mg_solve(const or_grid* g, const double* cx, const double* cy, const double* cz,
+                const double* b, double* p, double tol, const or_mg_params* prm_in,
+                or_mg_stats* st) {
+  or_mg_params prm;
+  if (prm_in) prm = *prm_in; else or_mg_default(&prm);
+  or_mg mg;
+  or_mg_stats local;
+  if (!st) st = &local;
+  memset(st, 0, sizeof(*st));
+  int rc = mg_setup(&mg, g, cx, cy, cz, &prm);
+  if (rc) { st->status = OR_BAD_ARG; return OR_BAD_ARG; }
+  st->levels = mg.L;
+  st->coarse_n = mg.nc;
+  or_level* f = &mg.lv[0];
+  f->sol = p;
+  f->src = (double*)b;
+  const size_t n = cells_of(g->nx, g->ny, g->nz);
+  double b2 = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : b2)
+  for (size_t q = 0; q < n; ++q) b2 += b[q] * b[q];
+  const double bnorm = sqrt(b2);
+  double r2 = level_residual(f);
+  double rel = bnorm > 0 ? sqrt(r2) / bnorm : sqrt(r2);
+  int status = OR_NOT_CONVERGED;
+  int cyc = 0;
+  if (prm.krylov && !(rel < tol)) {
+    status = pcg_loop(&mg, &prm, g, p, b, bnorm, tol, st, &cyc, &rel, &r2);
+  } else if (!(rel < tol)) {
+    for (cyc = 1; cyc <= prm.max_cycles; ++cyc) {
+      v_cycle(&mg, &prm);
+      r2 = level_residual(f);
+      rel = bnorm > 0 ? sqrt(r2) / bnorm : sqrt(r2);
+      if (prm.record_history && cyc <= 256) st->history[cyc - 1] = rel;
+      if (!isfinite(rel) || rel > 1e3) { status = OR_DIVERGED; break; }
+      if (rel < tol) { status = OR_OK; break; }
+    }
+    if (cyc > prm.max_cycles) cyc = prm.max_cycles;
+  } else {
+    status = OR_OK;
+  }
+  or_remove_mean(p, (int64_t)n);
+  st->cycles = cyc;
+  st->status = status;
+  st->rel_residual = rel;
+  st->rms_residual = sqrt(r2 / (double)n);
+  mg_free(&mg);
+  return status;
+}
+
+/* Coarse-level coefficients (for tests of the coarsening rule): writes level
+ * `level`'s cx, cy, cz into the caller's arrays sized by or_mg_plan. */
+int or_mg_level_coef(const or_grid* g, const double* cx, const double* cy, const double* cz,
+                     const or_mg_params* prm, int level, double* ocx, double* ocy, double* ocz) {
+  or_mg mg;
+  if (mg_setup(&mg, g, cx, cy, cz, prm)) return OR_BAD_ARG;
+  if (level < 0 || level >= mg.L) { mg_free(&mg); return OR_BAD_ARG; }
+  or_level* v = &mg.lv[level];
+  size_t n = cells_of(v->nx, v->ny, v->nz);
+  memcpy(ocx, v->cx, n * sizeof(double));
+  memcpy(ocy, v->cy, n * sizeof(double));
+  memcpy(ocz, v->cz, n * sizeof(double));
+  mg_free(&mg);
+  return OR_OK;
+}
+
+int or_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}

@@ -1,0 +1,221 @@
+"""ctypes front end of the CPU oracle (oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker.  The product package never
+imports it.  Parity unpinned: the reference has no tests or fixtures for this
+path and cannot be built here (see oracle.c).
+
+Arrays are numpy float64, C order (z, y, x).  Face velocities: u (nz, ny, nx+1),
+v (nz, ny+1, nx), w (nz+1, ny, nx).  Face coefficients: cell-shaped low-face
+arrays cx, cy, cz (0 on the low walls).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class Grid(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+
+
+class MGParams(C.Structure):
+    _fields_ = [("nu1", C.c_int32), ("nu2", C.c_int32), ("levels", C.c_int32),
+                ("coarse_max", C.c_int32), ("max_cycles", C.c_int32), ("smoother", C.c_int32),
+                ("blocks", C.c_int32 * 3), ("mean_every_sweep", C.c_int32),
+                ("coarse_op", C.c_int32), ("record_history", C.c_int32),
+                ("krylov", C.c_int32), ("prolong", C.c_int32), ("coarse_scale", C.c_double)]
+
+
+class MGStats(C.Structure):
+    _fields_ = [("cycles", C.c_int32), ("levels", C.c_int32), ("status", C.c_int32),
+                ("coarse_n", C.c_int32), ("rel_residual", C.c_double),
+                ("rms_residual", C.c_double), ("history", C.c_double * 256)]
+
+
+_D = C.POINTER(C.c_double)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        so = _build.build()
+        L = C.CDLL(so)
+        L.or_heaviside.argtypes = [_D, C.c_int64, C.c_double, _D]
+        L.or_heaviside_deriv.argtypes = [_D, C.c_int64, C.c_double, _D]
+        L.or_rho_from_phi.argtypes = [_D, C.c_int64, C.c_double, C.c_double, C.c_double, _D]
+        L.or_face_coef.argtypes = [C.POINTER(Grid), _D, _D, _D, _D]
+        L.or_divergence.argtypes = [C.POINTER(Grid), _D, _D, _D, C.c_double, C.c_int, _D]
+        L.or_apply.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D]
+        L.or_residual.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D, _D]
+        L.or_residual.restype = C.c_double
+        L.or_remove_mean.argtypes = [_D, C.c_int64]
+        L.or_correct.argtypes = [C.POINTER(Grid), _D, _D, C.c_double, _D, _D, _D]
+        L.or_div_stats.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D]
+        L.or_sor_solve.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D, C.c_double, C.c_double,
+                                   C.c_int64, _D]
+        L.or_sor_solve.restype = C.c_int64
+        L.or_mg_default.argtypes = [C.POINTER(MGParams)]
+        L.or_mg_plan.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32)]
+        L.or_mg_plan.restype = C.c_int
+        L.or_mg_solve.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D, C.c_double,
+                                  C.POINTER(MGParams), C.POINTER(MGStats)]
+        L.or_mg_solve.restype = C.c_int
+        L.or_mg_level_coef.argtypes = [C.POINTER(Grid), _D, _D, _D, C.POINTER(MGParams), C.c_int,
+                                       _D, _D, _D]
+        L.or_mg_level_coef.restype = C.c_int
+        L.or_num_threads.restype = C.c_int
+        L.or_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(_D)
+
+
+def grid(shape, spacing):
+    nz, ny, nx = shape
+    dx, dy, dz = spacing
+    return Grid(nx, ny, nz, dx, dy, dz)
+
+
+def heaviside(phi, eps):
+    phi = np.ascontiguousarray(phi, np.float64)
+    out = np.empty_like(phi)
+    lib().or_heaviside(_p(phi), phi.size, eps, _p(out))
+    return out
+
+
+def heaviside_deriv(phi, eps):
+    phi = np.ascontiguousarray(phi, np.float64)
+    out = np.empty_like(phi)
+    lib().or_heaviside_deriv(_p(phi), phi.size, eps, _p(out))
+    return out
+
+
+def rho_from_phi(phi, eps, rho_pos, rho_neg):
+    phi = np.ascontiguousarray(phi, np.float64)
+    out = np.empty_like(phi)
+    lib().or_rho_from_phi(_p(phi), phi.size, eps, rho_pos, rho_neg, _p(out))
+    return out
+
+
+def face_coef(rho, spacing):
+    rho = np.ascontiguousarray(rho, np.float64)
+    g = grid(rho.shape, spacing)
+    cx, cy, cz = (np.empty_like(rho) for _ in range(3))
+    lib().or_face_coef(C.byref(g), _p(rho), _p(cx), _p(cy), _p(cz))
+    return cx, cy, cz
+
+
+def divergence(u, v, w, dt, spacing, remove_mean=True):
+    nz, ny, nx1 = u.shape
+    shape = (nz, ny, nx1 - 1)
+    g = grid(shape, spacing)
+    b = np.empty(shape)
+    lib().or_divergence(C.byref(g), _p(u), _p(v), _p(w), dt, int(remove_mean), _p(b))
+    return b
+
+
+def apply(coef, p, spacing=(1.0, 1.0, 1.0)):
+    cx, cy, cz = coef
+    g = grid(p.shape, spacing)
+    out = np.empty_like(p)
+    lib().or_apply(C.byref(g), _p(cx), _p(cy), _p(cz), _p(p), _p(out))
+    return out
+
+
+def residual(coef, p, b):
+    cx, cy, cz = coef
+    g = grid(p.shape, (1.0, 1.0, 1.0))
+    r = np.empty_like(p)
+    s2 = lib().or_residual(C.byref(g), _p(cx), _p(cy), _p(cz), _p(p), _p(b), _p(r))
+    return r, s2
+
+
+def correct(rho, p, dt, u, v, w, spacing):
+    g = grid(p.shape, spacing)
+    u, v, w = (np.array(a, np.float64, copy=True) for a in (u, v, w))
+    lib().or_correct(C.byref(g), _p(rho), _p(p), dt, _p(u), _p(v), _p(w))
+    return u, v, w
+
+
+def div_stats(u, v, w, spacing):
+    nz, ny, nx1 = u.shape
+    g = grid((nz, ny, nx1 - 1), spacing)
+    mx, mean = C.c_double(), C.c_double()
+    lib().or_div_stats(C.byref(g), _p(u), _p(v), _p(w), C.byref(mx), C.byref(mean))
+    return mx.value, mean.value
+
+
+def sor_solve(coef, b, p0=None, w=1.5, tol=1e-10, max_iter=10**6):
+    cx, cy, cz = coef
+    p = np.zeros_like(b) if p0 is None else np.array(p0, np.float64, copy=True)
+    g = grid(b.shape, (1.0, 1.0, 1.0))
+    err = C.c_double()
+    it = lib().or_sor_solve(C.byref(g), _p(cx), _p(cy), _p(cz), _p(b), _p(p), w, tol, max_iter,
+                            C.byref(err))
+    return p, it, err.value
+
+
+def mg_params(**kw):
+    prm = MGParams()
+    lib().or_mg_default(C.byref(prm))
+    for k, v in kw.items():
+        if k == "blocks":
+            prm.blocks[:] = list(v)
+        else:
+            setattr(prm, k, v)
+    return prm
+
+
+def mg_plan(shape, levels=0, coarse_max=64):
+    nz, ny, nx = shape
+    dims = (C.c_int32 * 96)()
+    L = lib().or_mg_plan(nx, ny, nz, levels, coarse_max, dims)
+    if L < 1:
+        return []
+    return [(dims[3 * l + 2], dims[3 * l + 1], dims[3 * l]) for l in range(L)]
+
+
+def mg_solve(coef, b, p0=None, tol=1e-10, **kw):
+    """Returns (p, stats dict).  p is mean-free."""
+    cx, cy, cz = coef
+    p = np.zeros_like(b) if p0 is None else np.array(p0, np.float64, copy=True)
+    g = grid(b.shape, (1.0, 1.0, 1.0))
+    prm = mg_params(**kw)
+    st = MGStats()
+    lib().or_mg_solve(C.byref(g), _p(cx), _p(cy), _p(cz), _p(b), _p(p), tol, C.byref(prm),
+                      C.byref(st))
+    hist = [st.history[i] for i in range(min(st.cycles, 256))]
+    return p, dict(cycles=st.cycles, levels=st.levels, status=st.status, coarse_n=st.coarse_n,
+                   rel_residual=st.rel_residual, rms_residual=st.rms_residual, history=hist)
+
+
+def mg_level_coef(coef, level, **kw):
+    cx, cy, cz = coef
+    shape = cx.shape
+    plan = mg_plan(shape, kw.get("levels", 0), kw.get("coarse_max", 64))
+    g = grid(shape, (1.0, 1.0, 1.0))
+    prm = mg_params(**kw)
+    out = [np.empty(plan[level]) for _ in range(3)]
+    rc = lib().or_mg_level_coef(C.byref(g), _p(cx), _p(cy), _p(cz), C.byref(prm), level,
+                                *(_p(a) for a in out))
+    assert rc == 0
+    return out
+
+
+def set_threads(n):
+    lib().or_set_threads(int(n))
+
+
+def num_threads():
+    return lib().or_num_threads()

@@ -1,0 +1,356 @@
+"""Plain-Python transliterations of the reference's loops, for small cases only.
+
+Test infrastructure: used to pin the C oracle (oracle/oracle.c) against a
+second, independent restatement written line by line from the reference's
+Fortran, with its 1-based, ghost-padded indexing kept (numpy index = Fortran
+index, arrays allocated 0..n+1 on every axis).  Nothing here is fast.
+
+Sources (paths in the reference project):
+  ppe_sor_init / ppe_sor_solver / ns_momentum_correction:
+      "Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-205"
+      (2D: "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ppe_solver.f90:1-171")
+  bc (zero-gradient ghost copy): "Two phase flows/newOpenMP/2D/src/others/bcs.f90:1-26"
+  ls_funs / rho_mu: "Two phase flows/newOpenMP/2D/src/interface_solver/others.f90:1-61"
+  multigrid cycle: "DomainDecomposition/3D/src/others/multigrid_solver.f90:1-326"
+      (2D: "DomainDecomposition/2D/src/others/multigrid_solver.f90")
+  coarse solve: "DomainDecomposition/3D/lib/data/tree_multigrid.f90:1-238"
+  outer loop: "DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90:17-50"
+"""
+import math
+
+import numpy as np
+
+
+def ls_funs_rho(phi, ls_wid, rho_12):
+    """rho = heavy + rho_12 (1 - heavy), others.f90:14-27,54 (one value)."""
+    eps = 1.0e-12
+    x = phi / ls_wid
+    if x > 1.0 - eps:
+        heavy = 1.0
+    elif x < -1.0 + eps:
+        heavy = 0.0
+    else:
+        heavy = 0.5 * (1.0 + x + math.sin(math.pi * x) / math.pi)
+    heavy = max(min(heavy, 1.0), 0.0)
+    return heavy + rho_12 * (1.0 - heavy)
+
+
+def pad(a):
+    """(nz, ny, nx) numpy -> Fortran-indexed (0..nx+1, 0..ny+1, 0..nz+1) with
+    zero-gradient ghosts (bc)."""
+    nz, ny, nx = a.shape
+    g = np.zeros((nx + 2, ny + 2, nz + 2))
+    g[1:nx + 1, 1:ny + 1, 1:nz + 1] = a.transpose(2, 1, 0)
+    bc(g)
+    return g
+
+
+def unpad(g):
+    return np.ascontiguousarray(g[1:-1, 1:-1, 1:-1].transpose(2, 1, 0))
+
+
+def bc(g):
+    """Zero-gradient ghost copy on every wall (bcs.f90:1-26; job_bc order 0)."""
+    g[0, :, :] = g[1, :, :]
+    g[-1, :, :] = g[-2, :, :]
+    g[:, 0, :] = g[:, 1, :]
+    g[:, -1, :] = g[:, -2, :]
+    g[:, :, 0] = g[:, :, 1]
+    g[:, :, -1] = g[:, :, -2]
+
+
+def ppe_sor_init(rho_g, nx, ny, nz, dx, dy, dz):
+    """ns_ppe_solver.f90:1-65: the seven coefficient arrays r,l,f,b,u,d,c."""
+    shp = rho_g.shape
+    r, l, f, b, u, d, c = (np.zeros(shp) for _ in range(7))
+    three_d = nz > 1
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                R = rho_g
+                r[i, j, k] = 2.0 / (R[i, j, k] + R[i + 1, j, k]) / dx ** 2.0
+                l[i, j, k] = 2.0 / (R[i, j, k] + R[i - 1, j, k]) / dx ** 2.0
+                f[i, j, k] = 2.0 / (R[i, j, k] + R[i, j + 1, k]) / dy ** 2.0
+                b[i, j, k] = 2.0 / (R[i, j, k] + R[i, j - 1, k]) / dy ** 2.0
+                if three_d:
+                    u[i, j, k] = 2.0 / (R[i, j, k] + R[i, j, k + 1]) / dz ** 2.0
+                    d[i, j, k] = 2.0 / (R[i, j, k] + R[i, j, k - 1]) / dz ** 2.0
+                c[i, j, k] = -(r[i, j, k] + l[i, j, k] + f[i, j, k] + b[i, j, k] + u[i, j, k]
+                               + d[i, j, k])
+                if i == 1:
+                    c[i, j, k] += l[i, j, k]; l[i, j, k] = 0.0
+                if i == nx:
+                    c[i, j, k] += r[i, j, k]; r[i, j, k] = 0.0
+                if j == 1:
+                    c[i, j, k] += b[i, j, k]; b[i, j, k] = 0.0
+                if j == ny:
+                    c[i, j, k] += f[i, j, k]; f[i, j, k] = 0.0
+                if three_d:
+                    if k == 1:
+                        c[i, j, k] += d[i, j, k]; d[i, j, k] = 0.0
+                    if k == nz:
+                        c[i, j, k] += u[i, j, k]; u[i, j, k] = 0.0
+    return r, l, f, b, u, d, c
+
+
+def ppe_apply(coe, p_g, nx, ny, nz):
+    """sum coe p_nb + c p_i, the operator ppe_sor_solver relaxes."""
+    r, l, f, b, u, d, c = coe
+    out = np.zeros((nz, ny, nx))
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                P = p_g
+                v = (r[i, j, k] * P[i + 1, j, k] + l[i, j, k] * P[i - 1, j, k]
+                     + f[i, j, k] * P[i, j + 1, k] + b[i, j, k] * P[i, j - 1, k]
+                     + c[i, j, k] * P[i, j, k])
+                if nz > 1:
+                    v += u[i, j, k] * P[i, j, k + 1] + d[i, j, k] * P[i, j, k - 1]
+                out[k - 1, j - 1, i - 1] = v
+    return out
+
+
+def ppe_sor_solver(coe, src, p0, w, tol, max_iter):
+    """ns_ppe_solver.f90:93-163 run serially (lexicographic k, j, i): returns
+    (p, iterations, err)."""
+    nz, ny, nx = src.shape
+    r, l, f, b, u, d, c = coe
+    P = pad(p0)
+    S = pad(src)
+    it = 0
+    while True:
+        it += 1
+        tmp = P.copy()
+        for k in range(1, nz + 1):
+            for j in range(1, ny + 1):
+                for i in range(1, nx + 1):
+                    v = (S[i, j, k] - r[i, j, k] * P[i + 1, j, k] - l[i, j, k] * P[i - 1, j, k]
+                         - f[i, j, k] * P[i, j + 1, k] - b[i, j, k] * P[i, j - 1, k])
+                    if nz > 1:
+                        v = v - u[i, j, k] * P[i, j, k + 1] - d[i, j, k] * P[i, j, k - 1]
+                    P[i, j, k] = v / c[i, j, k]
+        inner = P[1:nx + 1, 1:ny + 1, 1:nz + 1]
+        sump = inner.sum() / (nx * ny * nz)
+        inner -= sump
+        inner[...] = w * inner + (1.0 - w) * tmp[1:nx + 1, 1:ny + 1, 1:nz + 1]
+        err = np.abs(inner - tmp[1:nx + 1, 1:ny + 1, 1:nz + 1]).max()
+        bc(P)
+        if err < tol or it >= max_iter:
+            break
+    return unpad(P), it, err
+
+
+def momentum_correction(rho, p, u, v, w, dt, dx, dy, dz):
+    """ns_momentum_correction (ns_ppe_solver.f90:174-205) on interior faces;
+    face arrays in the (nz, ny, nx+1) / (nz, ny+1, nx) / (nz+1, ny, nx) layout."""
+    nz, ny, nx = p.shape
+    u, v, w = u.copy(), v.copy(), w.copy()
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                if i + 1 < nx:
+                    rf = (rho[k, j, i] + rho[k, j, i + 1]) / 2.0
+                    px = (p[k, j, i + 1] - p[k, j, i]) / dx
+                    u[k, j, i + 1] = u[k, j, i + 1] - dt * px / rf
+                if j + 1 < ny:
+                    rf = (rho[k, j, i] + rho[k, j + 1, i]) / 2.0
+                    py = (p[k, j + 1, i] - p[k, j, i]) / dy
+                    v[k, j + 1, i] = v[k, j + 1, i] - dt * py / rf
+                if k + 1 < nz:
+                    rf = (rho[k, j, i] + rho[k + 1, j, i]) / 2.0
+                    pz = (p[k + 1, j, i] - p[k, j, i]) / dz
+                    w[k + 1, j, i] = w[k + 1, j, i] - dt * pz / rf
+    return u, v, w
+
+
+# ---------------------------------------------------------------------------
+# DomainDecomposition multigrid, one subdomain, constant coefficient.
+# wall="ghost": multigrid_relax as written (the wall neighbour is the ghost
+#   copied by the sync before the sweep, the diagonal a counts every face);
+# wall="folded": the wall term folded into the diagonal as ppe_sor_init does
+#   (the form the variable-coefficient solver uses).
+# ---------------------------------------------------------------------------
+class DDLevel:
+    def __init__(self, nx, ny, nz, dx, dy, dz):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.dx, self.dy, self.dz = dx, dy, dz
+        shp = (nx + 2, ny + 2, nz + 2)
+        self.sol = np.zeros(shp)
+        self.src = np.zeros(shp)
+        self.res = np.zeros(shp)
+        self.pol = np.zeros(shp)
+
+
+class DDMultigrid:
+    def __init__(self, nx, ny, nz, dx, dy, dz, levels, wall="folded"):
+        self.three_d = nz > 1
+        self.lv = []
+        for lev in range(levels):
+            f = 2 ** lev
+            self.lv.append(DDLevel(nx // f, ny // f, nz // f if nz > 1 else 1, dx * f, dy * f,
+                                   dz * f))
+        self.wall = wall
+        self._setup_coarse()
+
+    def sync(self, a):
+        bc(a)
+
+    def relax(self, L, num):
+        v = self.lv[L]
+        dx2, dy2, dz2 = v.dx ** 2.0, v.dy ** 2.0, v.dz ** 2.0
+        for _ in range(num):
+            self.sync(v.sol)
+            S, B = v.sol, v.src
+            for k in range(1, v.nz + 1):
+                for j in range(1, v.ny + 1):
+                    for i in range(1, v.nx + 1):
+                        if self.wall == "ghost":
+                            a = -2.0 / dx2 - 2.0 / dy2 - (2.0 / dz2 if self.three_d else 0.0)
+                            t = (B[i, j, k] - (S[i + 1, j, k] + S[i - 1, j, k]) / dx2
+                                 - (S[i, j + 1, k] + S[i, j - 1, k]) / dy2)
+                            if self.three_d:
+                                t -= (S[i, j, k + 1] + S[i, j, k - 1]) / dz2
+                            S[i, j, k] = t / a
+                        else:
+                            s, dsum = 0.0, 0.0
+                            nb = [(i - 1, j, k, 1 / dx2, i > 1), (i + 1, j, k, 1 / dx2, i < v.nx),
+                                  (i, j - 1, k, 1 / dy2, j > 1), (i, j + 1, k, 1 / dy2, j < v.ny)]
+                            if self.three_d:
+                                nb += [(i, j, k - 1, 1 / dz2, k > 1), (i, j, k + 1, 1 / dz2, k < v.nz)]
+                            for (ii, jj, kk, cc, inside) in nb:
+                                if inside:
+                                    s += cc * S[ii, jj, kk]
+                                    dsum += cc
+                            S[i, j, k] = (s - B[i, j, k]) / dsum
+            self.compat(v.sol, v)
+        self.sync(v.sol)
+
+    def compat(self, a, v):
+        inner = a[1:v.nx + 1, 1:v.ny + 1, 1:v.nz + 1]
+        inner -= inner.sum() / (v.nx * v.ny * v.nz)
+
+    def residual(self, L):
+        v = self.lv[L]
+        self.sync(v.sol)
+        S = v.sol
+        tot = 0.0
+        for k in range(1, v.nz + 1):
+            for j in range(1, v.ny + 1):
+                for i in range(1, v.nx + 1):
+                    r = (v.src[i, j, k]
+                         - (S[i + 1, j, k] - 2.0 * S[i, j, k] + S[i - 1, j, k]) / v.dx ** 2.0
+                         - (S[i, j + 1, k] - 2.0 * S[i, j, k] + S[i, j - 1, k]) / v.dy ** 2.0)
+                    if self.three_d:
+                        r -= (S[i, j, k + 1] - 2.0 * S[i, j, k] + S[i, j, k - 1]) / v.dz ** 2.0
+                    v.res[i, j, k] = r
+                    tot += r ** 2.0
+        return math.sqrt(tot / (v.nx * v.ny * v.nz))
+
+    def restriction(self, L):
+        self.relax(L, 2)
+        self.residual(L)
+        f, c = self.lv[L], self.lv[L + 1]
+        for k in range(1, c.nz + 1):
+            for j in range(1, c.ny + 1):
+                for i in range(1, c.nx + 1):
+                    R = f.res
+                    if self.three_d:
+                        s = (R[2 * i - 1, 2 * j - 1, 2 * k - 1] + R[2 * i, 2 * j - 1, 2 * k - 1]
+                             + R[2 * i - 1, 2 * j, 2 * k - 1] + R[2 * i, 2 * j, 2 * k - 1]
+                             + R[2 * i - 1, 2 * j - 1, 2 * k] + R[2 * i, 2 * j - 1, 2 * k]
+                             + R[2 * i - 1, 2 * j, 2 * k] + R[2 * i, 2 * j, 2 * k]) / 8.0
+                    else:
+                        s = (R[2 * i - 1, 2 * j - 1, 1] + R[2 * i, 2 * j - 1, 1]
+                             + R[2 * i - 1, 2 * j, 1] + R[2 * i, 2 * j, 1]) / 4.0
+                    c.src[i, j, k] = s
+                    c.sol[i, j, k] = 0.0
+        self.compat(c.src, c)
+
+    def _setup_coarse(self):
+        """manager_mg_setup (tree_multigrid.f90:1-132), single subdomain."""
+        v = self.lv[-1]
+        n = v.nx * v.ny * v.nz
+        A = np.zeros((n, n))
+        node = lambda i, j, k: (k - 1) * v.nx * v.ny + (j - 1) * v.nx + (i - 1)  # noqa: E731
+        for k in range(1, v.nz + 1):
+            for j in range(1, v.ny + 1):
+                for i in range(1, v.nx + 1):
+                    q = node(i, j, k)
+                    A[q, q] = -2.0 / v.dx ** 2.0 - 2.0 / v.dy ** 2.0
+                    if self.three_d:
+                        A[q, q] += -2.0 / v.dz ** 2.0
+                    for (ii, jj, kk, h, inside) in [
+                            (i - 1, j, k, v.dx, i > 1), (i + 1, j, k, v.dx, i < v.nx),
+                            (i, j - 1, k, v.dy, j > 1), (i, j + 1, k, v.dy, j < v.ny)] + (
+                            [(i, j, k - 1, v.dz, k > 1), (i, j, k + 1, v.dz, k < v.nz)]
+                            if self.three_d else []):
+                        if inside:
+                            A[q, node(ii, jj, kk)] = 1.0 / h ** 2.0
+                        else:
+                            A[q, q] += 1.0 / h ** 2.0
+        self.A = A
+        self.node = node
+
+    def final_exact(self):
+        """manager_mg_solve_exact + mg_find_error + compatibility_sol.  The
+        singular dgesv is replaced by the least-squares (minimum-norm, hence
+        mean-free) solution."""
+        v = self.lv[-1]
+        n = v.nx * v.ny * v.nz
+        B = np.zeros(n)
+        for k in range(1, v.nz + 1):
+            for j in range(1, v.ny + 1):
+                for i in range(1, v.nx + 1):
+                    B[self.node(i, j, k)] = v.src[i, j, k]
+        x = np.linalg.lstsq(self.A, B, rcond=None)[0]
+        err = B - self.A @ x
+        if np.abs(err).max() > 1e-10:
+            x = x + np.linalg.lstsq(self.A, err, rcond=None)[0]
+        for k in range(1, v.nz + 1):
+            for j in range(1, v.ny + 1):
+                for i in range(1, v.nx + 1):
+                    v.sol[i, j, k] = x[self.node(i, j, k)]
+        self.compat(v.sol, v)
+
+    def prolongation(self, L):
+        f, c = self.lv[L], self.lv[L + 1]
+        self.sync(c.sol)
+        E = c.sol
+        for k in range(1, c.nz + 1):
+            for j in range(1, c.ny + 1):
+                for i in range(1, c.nx + 1):
+                    mx = 0.5 * (E[i + 1, j, k] - E[i - 1, j, k])
+                    my = 0.5 * (E[i, j + 1, k] - E[i, j - 1, k])
+                    if self.three_d:
+                        mz = 0.5 * (E[i, j, k + 1] - E[i, j, k - 1])
+                        for dk, sz in ((0, -1), (1, 1)):
+                            for dj, sy in ((0, -1), (1, 1)):
+                                for di, sx in ((0, -1), (1, 1)):
+                                    f.pol[2 * i - 1 + di, 2 * j - 1 + dj, 2 * k - 1 + dk] = (
+                                        E[i, j, k] + sx * 0.25 * mx + sy * 0.25 * my + sz * 0.25 * mz)
+                    else:
+                        for dj, sy in ((0, -1), (1, 1)):
+                            for di, sx in ((0, -1), (1, 1)):
+                                f.pol[2 * i - 1 + di, 2 * j - 1 + dj, 1] = (
+                                    E[i, j, k] + sx * 0.25 * mx + sy * 0.25 * my)
+        f.sol[1:f.nx + 1, 1:f.ny + 1, 1:f.nz + 1] += f.pol[1:f.nx + 1, 1:f.ny + 1, 1:f.nz + 1]
+        self.relax(L, 2)
+
+    def v_cycle(self):
+        for L in range(len(self.lv) - 1):
+            self.restriction(L)
+        self.final_exact()
+        for L in range(len(self.lv) - 2, -1, -1):
+            self.prolongation(L)
+
+    def solve(self, b, p0, cycles):
+        """ppe_mg_solver's loop for a fixed number of cycles; returns p after
+        each cycle (mean-free)."""
+        f = self.lv[0]
+        f.src = pad(b)
+        f.sol = pad(p0)
+        out = []
+        for _ in range(cycles):
+            self.v_cycle()
+            out.append(unpad(f.sol).copy())
+        return out

@@ -1,0 +1,68 @@
+"""CPU tests of the C ABI boundary: libgbmg.so builds, loads, and exports every
+function include/gbmg.h declares; calls that need no GPU behave.  No kernel is
+launched here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from fortrancfd_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "gbmg.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbmg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declarations_are_the_binding_exports():
+    assert header_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    for name in header_functions():
+        assert hasattr(L, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.library_path()],
+                         capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (gbmg_\w+)", out))
+    assert set(header_functions()) <= exported
+
+
+def test_default_params_and_strerror():
+    L = _lib.load()
+    prm = _lib.Params()
+    L.gbmg_default_params(C.byref(prm))
+    assert (prm.precision, prm.nu1, prm.nu2, prm.max_cycles, prm.coarse_max) == (0, 2, 2, 100, 64)
+    assert prm.use_graph == 1 and prm.remove_rhs_mean == 1 and prm.device == -1
+    for code in range(8):
+        assert L.gbmg_strerror(code)
+    assert L.gbmg_strerror(1).decode().startswith("not converged")
+
+
+def test_null_and_invalid_arguments_return_codes():
+    L = _lib.load()
+    h = C.c_void_p()
+    assert L.gbmg_create(None, None, C.byref(h)) == _lib.GBMG_INVALID_ARG
+    g = _lib.Grid(0, 4, 4, 1.0, 1.0, 1.0)
+    assert L.gbmg_create(C.byref(g), None, C.byref(h)) == _lib.GBMG_INVALID_ARG
+    assert L.gbmg_destroy(None) == _lib.GBMG_INVALID_ARG
+    assert L.gbmg_kernel_launches(None) == 0
+
+
+def test_create_without_device_reports_no_device():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    L = _lib.load()
+    h = C.c_void_p()
+    g = _lib.Grid(8, 8, 8, 0.125, 0.125, 0.125)
+    assert L.gbmg_create(C.byref(g), None, C.byref(h)) == _lib.GBMG_NO_DEVICE
+    assert not h.value

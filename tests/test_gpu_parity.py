@@ -1,0 +1,257 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle on
+the same seeded inputs.
+
+Tolerances (floating point):
+  * set-up kernels (face coefficients, coarse coefficients, divergence,
+    correction formulas) do the oracle's arithmetic in the same order and are
+    compared bit for bit, except rho(phi) (CUDA's sin vs the C library's, 1e-14);
+  * the residual differs by FMA contraction: 1e-12 relative to max|b|;
+  * plain FP64 solve: mean-free pressure within 1e-9 relative L2 of the
+    oracle's and the same cycle count +/- 1;
+  * mixed precision (FP32 cycles inside FP64 defect correction): the same
+    1e-10 relative residual in FP64, pressure within 1e-8 relative L2 of the
+    FP64 oracle solution.
+"""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import ConvergenceError, GBMGError, PressurePoisson, inputs
+from oracle import oracle as orc
+from tests import cases
+from tests.cases import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def solver(built, **kw):
+    return PressurePoisson(built.shape, built.spacing, **kw)
+
+
+# --- set-up kernels ----------------------------------------------------------------
+@pytest.mark.parametrize("idx,scale", [(0, 1), (1, 8), (4, 8)])
+def test_face_coefficients_bitwise(cuda, idx, scale):
+    c = cases.config(idx, scale)
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        got = s.level_coef(0)
+        for a, b in zip(got, c.coef):
+            np.testing.assert_array_equal(a, b)
+        for lev, dims in enumerate(s.level_dims()):
+            want = orc.mg_level_coef(c.coef, lev)
+            got = s.level_coef(lev)
+            assert got[0].shape == dims
+            for a, b in zip(got, want):
+                np.testing.assert_array_equal(a, b)
+        assert s.level_dims() == orc.mg_plan(c.shape)
+
+
+def test_rho_from_phi(cuda):
+    c = cases.config(1, 8)
+    with solver(c) as s:
+        s.rho_mu(c.phi, c.case.eps, c.case.rho_pos, c.case.rho_neg)
+        got = s.level_coef(0)
+        for a, b in zip(got, c.coef):
+            np.testing.assert_allclose(a, b, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("idx,scale", [(0, 2), (1, 8)])
+def test_divergence_bitwise(cuda, idx, scale):
+    c = cases.config(idx, scale)
+    with solver(c) as s:
+        got = s.divergence(c.u, c.v, c.w, c.case.dt)
+    want = orc.divergence(c.u, c.v, c.w, c.case.dt, c.spacing, remove_mean=False)
+    np.testing.assert_array_equal(got, want)
+
+
+def test_residual(cuda):
+    c = cases.config(1, 8)
+    p = np.random.default_rng(7).standard_normal(c.shape)
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        r, n2 = s.residual(c.b, p)
+    r_or, n2_or = orc.residual(c.coef, p, c.b)
+    np.testing.assert_allclose(r, r_or, rtol=0, atol=1e-12 * np.abs(c.b).max())
+    assert n2 == pytest.approx(n2_or, rel=1e-12)
+
+
+# --- solves -------------------------------------------------------------------------
+@pytest.mark.parametrize("idx,scale", [(0, 1), (1, 4), (1, 2)])
+def test_fp64_solve_matches_oracle(cuda, idx, scale):
+    c = cases.config(idx, scale)
+    p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-10)
+    assert st_or["status"] == 0
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == 0 and st["rel_residual"] < 1e-10
+    assert abs(st["cycles"] - st_or["cycles"]) <= 1, (st["cycles"], st_or["cycles"])
+    assert rel_l2(p, p_or) <= 1e-9
+    assert abs(p.mean()) <= 1e-12 * np.abs(p).max()
+
+
+@pytest.mark.parametrize("idx,scale", [(0, 1), (1, 4), (1, 2)])
+def test_mixed_solve_reaches_fp64_accuracy(cuda, idx, scale):
+    c = cases.config(idx, scale)
+    p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-10)
+    with solver(c, precision="mixed") as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == 0 and st["rel_residual"] < 1e-10
+    # the true FP64 residual, recomputed by the oracle
+    _, r2 = orc.residual(c.coef, p, c.b)
+    assert np.sqrt(r2) / np.linalg.norm(c.b) < 1e-10
+    assert rel_l2(p, p_or) <= 1e-8
+    assert st["cycles"] <= st_or["cycles"] + 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_krylov_matches_oracle(cuda, precision):
+    c = cases.config(2, 8)
+    p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-10, krylov=1)
+    assert st_or["status"] == 0
+    with solver(c, precision=precision, krylov=True) as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == 0 and st["rel_residual"] < 1e-10
+    if precision == "fp64":
+        assert abs(st["cycles"] - st_or["cycles"]) <= 1, (st["cycles"], st_or["cycles"])
+    else:
+        assert st["cycles"] <= st_or["cycles"] + 3
+    assert rel_l2(p, p_or) <= 1e-8
+
+
+def test_projection_matches_oracle(cuda):
+    c = cases.config(1, 8)
+    p_or, _ = orc.mg_solve(c.coef, c.b, tol=1e-12, max_cycles=200)
+    u_or, v_or, w_or = orc.correct(c.rho, p_or, c.case.dt, c.u, c.v, c.w, c.spacing)
+    u, v, w = c.u.copy(), c.v.copy(), c.w.copy()
+    with solver(c, max_cycles=200) as s:
+        s.ppe_init(c.rho)
+        p, st = s.ppe_solver(u, v, w, c.case.dt, tol=1e-12)
+        mx, mean = s.div_stats(u, v, w)
+    assert st["status"] == 0
+    assert rel_l2(p, p_or) <= 1e-9
+    scale = np.abs(c.u).max()
+    for a, b in ((u, u_or), (v, v_or), (w, w_or)):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-9 * scale)
+    mx0, _ = orc.div_stats(c.u, c.v, c.w, c.spacing)
+    assert mx < 1e-9 * mx0
+    mx_or, mean_or = orc.div_stats(u, v, w, c.spacing)
+    assert mx == pytest.approx(mx_or, rel=1e-12, abs=1e-12 * mx0)
+
+
+# --- interfaces, layouts, edge cases -------------------------------------------------
+def test_ghost_padded_host_arrays(cuda):
+    """Fortran-style arrays with 3 ghost cells per side (c_loc(p(1,1,1)) and
+    padded strides) give the same answer as dense arrays."""
+    c = cases.config(1, 8)
+    g = 3
+    nz, ny, nx = c.shape
+
+    def padded(a, extra=(0, 0, 0)):
+        big = np.full((nz + extra[0] + 2 * g, ny + extra[1] + 2 * g, nx + extra[2] + 2 * g), np.nan)
+        view = big[g:g + a.shape[0], g:g + a.shape[1], g:g + a.shape[2]]
+        view[...] = a
+        return big, view
+
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        p_dense, _ = s.solve(c.b, tol=1e-10)
+        _, rho_v = padded(c.rho)
+        _, b_v = padded(c.b)
+        pbig, p_v = padded(np.zeros(c.shape))
+        s.ppe_init(rho_v)
+        s.solve(b_v, p_v, tol=1e-10)
+    np.testing.assert_array_equal(p_v, p_dense)
+    assert np.isnan(pbig[0]).all()  # ghosts untouched
+
+
+def test_device_tensors_in_place(cuda):
+    import torch
+    c = cases.config(1, 8)
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        p_host, _ = s.solve(c.b, tol=1e-10)
+        rho = torch.from_numpy(c.rho).to(cuda)
+        b = torch.from_numpy(c.b).to(cuda)
+        p = torch.zeros_like(b)
+        s.ppe_init(rho)
+        out, st = s.solve(b, p, tol=1e-10)
+        assert out is p
+    np.testing.assert_array_equal(p.cpu().numpy(), p_host)
+
+
+def test_deterministic(cuda):
+    c = cases.config(1, 4)
+    with solver(c, precision="mixed") as s:
+        s.ppe_init(c.rho)
+        p1, s1 = s.solve(c.b, tol=1e-10)
+        p2, s2 = s.solve(c.b, tol=1e-10)
+    np.testing.assert_array_equal(p1, p2)
+    assert s1["cycles"] == s2["cycles"]
+
+
+def test_graph_and_eager_paths_agree(cuda):
+    c = cases.config(0, 1)
+    out = []
+    for g in (True, False):
+        with solver(c, use_graph=g) as s:
+            s.ppe_init(c.rho)
+            out.append(s.solve(c.b, tol=1e-10)[0])
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4), (1, 12, 20), (6, 10, 8), (1, 1, 2)])
+def test_small_and_ragged_grids(cuda, shape):
+    case = inputs.custom(shape, centers=((0.5, 0.4, 0.5),), radii=(0.3,), seed=3)
+    c = cases.Built(case)
+    p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-10)
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        assert s.level_dims() == orc.mg_plan(shape)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == st_or["status"] == 0
+    assert abs(st["cycles"] - st_or["cycles"]) <= 1
+    assert rel_l2(p, p_or) <= 1e-9
+
+
+def test_zero_rhs_returns_zero(cuda):
+    c = cases.config(1, 8)
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(np.zeros(c.shape), tol=1e-10)
+    assert st["status"] == 0 and st["cycles"] == 0
+    assert not p.any()
+
+
+def test_status_codes(cuda):
+    c = cases.config(1, 8)
+    with solver(c, max_cycles=1) as s:
+        s.ppe_init(c.rho)
+        with pytest.raises(ConvergenceError) as e:
+            s.solve(c.b, tol=1e-12)
+        assert e.value.stats["status"] == 1 and e.value.stats["cycles"] == 1
+        _, st = s.solve(c.b, tol=1e-12, check=False)
+        assert st["status"] == 1
+    with solver(c) as s:
+        bad = [a.copy() for a in c.coef]
+        bad[0][2, 2, 2] = np.nan
+        s.set_coef(*bad)
+        _, st = s.solve(c.b, tol=1e-10, check=False)
+        assert st["status"] == 2
+    with pytest.raises(GBMGError):
+        PressurePoisson((10, 14, 18), (0.1, 0.1, 0.1))  # coarsest level 5x7x9 > 64 cells
+    with pytest.raises(GBMGError):
+        PressurePoisson((8, 8, 8), (0.1, 0.1, 0.1), levels=5)  # not divisible (the reference STOPs)
+    with solver(c) as s:
+        with pytest.raises(GBMGError):
+            s.solve(c.b)  # no coefficients yet
+
+
+def test_kernels_are_launched(cuda):
+    c = cases.config(1, 8)
+    with solver(c) as s:
+        n0 = s.kernel_launches
+        s.ppe_init(c.rho)
+        s.solve(c.b, tol=1e-10)
+        assert s.kernel_launches > n0 + 20

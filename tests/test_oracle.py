@@ -1,0 +1,266 @@
+"""CPU tests of the oracle (oracle/oracle.c): known-answer properties and
+agreement with the line-by-line transliteration of the reference's loops
+(tests/refloops.py).  No GPU."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from fortrancfd_gb300 import inputs
+from tests import refloops as ref
+
+
+def _small_case(shape, seed=0, ratio=1000.0):
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = shape
+    case = inputs.custom(shape, centers=((0.45, 0.55, 0.5),), radii=(0.3,), seed=seed)
+    phi = inputs.level_set(case)
+    rho = orc.rho_from_phi(phi, case.eps, ratio, 1.0)
+    coef = orc.face_coef(rho, case.spacing)
+    u, v, w = inputs.velocity(case)
+    b = orc.divergence(u, v, w, case.dt, case.spacing)
+    return case, rho, coef, (u, v, w), b, rng
+
+
+# --- a1: smoothed Heaviside / density (others.f90:1-61) ---------------------
+def test_heaviside_matches_reference_formula():
+    phi = np.linspace(-2.0, 2.0, 401)
+    eps = 0.37
+    H = orc.heaviside(phi, eps)
+    rho = orc.rho_from_phi(phi, eps, 1.0, 1e-3)
+    for x, h, r in zip(phi, H, rho):
+        assert r == ref.ls_funs_rho(x, eps, 1e-3)
+        assert 0.0 <= h <= 1.0
+    assert H[0] == 0.0 and H[-1] == 1.0
+    assert H[200] == pytest.approx(0.5, abs=1e-15)
+
+
+def test_heaviside_derivative_by_differences():
+    phi = np.linspace(-0.9, 0.9, 37)
+    eps = 1.0
+    d = orc.heaviside_deriv(phi, eps)
+    h = 1e-6
+    fd = (orc.heaviside(phi + h, eps) - orc.heaviside(phi - h, eps)) / (2 * h)
+    np.testing.assert_allclose(d, fd, rtol=1e-7, atol=1e-9)
+
+
+# --- a2: ppe_sor_init ------------------------------------------------------------
+@pytest.mark.parametrize("shape", [(1, 7, 9), (5, 4, 6)])
+def test_face_coef_matches_ppe_sor_init(shape):
+    nz, ny, nx = shape
+    rng = np.random.default_rng(1)
+    rho = rng.uniform(1.0, 1000.0, shape)
+    spacing = (0.1, 0.2, 0.3)
+    coef = orc.face_coef(rho, spacing)
+    coe7 = ref.ppe_sor_init(ref.pad(rho), nx, ny, nz, *spacing)
+    p = rng.standard_normal(shape)
+    a_ref = ref.ppe_apply(coe7, ref.pad(p), nx, ny, nz)
+    a_or = orc.apply(coef, p)
+    np.testing.assert_allclose(a_or, a_ref, rtol=0, atol=1e-12 * np.abs(a_ref).max())
+    # interior coefficients are bit-identical to r(i-1) / l(i) of the reference
+    r, l = coe7[0], coe7[1]
+    cx = coef[0]
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(1, nx):
+                assert cx[k, j, i] == l[i + 1, j + 1, k + 1]
+                assert cx[k, j, i] == r[i, j + 1, k + 1]
+            assert cx[k, j, 0] == 0.0
+
+
+def test_operator_symmetric_with_constant_null_space():
+    case, rho, coef, _, _, rng = _small_case((6, 8, 10))
+    x = rng.standard_normal(rho.shape)
+    y = rng.standard_normal(rho.shape)
+    Ax, Ay = orc.apply(coef, x), orc.apply(coef, y)
+    lhs, rhs = np.vdot(Ax, y), np.vdot(x, Ay)
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    A1 = orc.apply(coef, np.ones_like(x))
+    assert np.abs(A1).max() <= 1e-15 * np.abs(coef[0]).max()
+    assert abs(Ax.sum()) <= 1e-12 * np.abs(Ax).sum()  # 1^T A = 0 (compatibility)
+    assert np.vdot(x - x.mean(), orc.apply(coef, x - x.mean())) < 0  # negative definite off 1
+
+
+def test_manufactured_solution_second_order():
+    """-div(beta grad p) with smooth beta: O(h^2) error of the discrete solve."""
+    errs = []
+    for n in (16, 32, 64):
+        h = 1.0 / n
+        xc = (np.arange(n) + 0.5) * h
+        X, Y = np.meshgrid(xc, xc, indexing="xy")
+        rho = (1.0 + 0.5 * np.sin(np.pi * X) * np.sin(np.pi * Y))[None]
+        p_ex = np.cos(np.pi * X) * np.cos(2 * np.pi * Y)
+        # continuous A p = div(beta grad p), beta = 1/rho, by symbolic derivatives
+        beta = 1.0 / rho[0]
+        px = -np.pi * np.sin(np.pi * X) * np.cos(2 * np.pi * Y)
+        py = -2 * np.pi * np.cos(np.pi * X) * np.sin(2 * np.pi * Y)
+        lap = -(np.pi ** 2 + 4 * np.pi ** 2) * p_ex
+        drho_x = 0.5 * np.pi * np.cos(np.pi * X) * np.sin(np.pi * Y)
+        drho_y = 0.5 * np.pi * np.sin(np.pi * X) * np.cos(np.pi * Y)
+        bx, by = -drho_x * beta ** 2, -drho_y * beta ** 2
+        f = beta * lap + bx * px + by * py
+        coef = orc.face_coef(rho, (h, h, 1.0))
+        b = f[None] - f.mean()
+        p, st = orc.mg_solve(coef, b, tol=1e-12, max_cycles=200)
+        assert st["status"] == 0
+        pe = p_ex - p_ex.mean()
+        errs.append(np.abs(p[0] - pe).max())
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert all(r > 1.8 for r in rates), (errs, rates)
+
+
+# --- a3 / a12 / a13: divergence, correction, divergence check -------------------
+def test_divergence_and_correction_match_reference_loops():
+    case, rho, coef, (u, v, w), b, _ = _small_case((4, 6, 5))
+    dx, dy, dz = case.spacing
+    b_raw = orc.divergence(u, v, w, case.dt, case.spacing, remove_mean=False)
+    nz, ny, nx = rho.shape
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                dref = ((u[k, j, i + 1] - u[k, j, i]) / dx + (v[k, j + 1, i] - v[k, j, i]) / dy
+                        + (w[k + 1, j, i] - w[k, j, i]) / dz) / case.dt
+                assert b_raw[k, j, i] == dref
+    # zero wall fluxes: the divergence is compatible up to rounding
+    assert abs(b_raw.sum()) <= 1e-10 * np.abs(b_raw).sum()
+    p = np.random.default_rng(5).standard_normal(rho.shape)
+    uo, vo, wo = orc.correct(rho, p, case.dt, u, v, w, case.spacing)
+    ur, vr, wr = ref.momentum_correction(rho, p, u, v, w, case.dt, dx, dy, dz)
+    np.testing.assert_array_equal(uo, ur)
+    np.testing.assert_array_equal(vo, vr)
+    np.testing.assert_array_equal(wo, wr)
+
+
+def test_projection_removes_divergence():
+    case, rho, coef, (u, v, w), b, _ = _small_case((8, 8, 8))
+    p, st = orc.mg_solve(coef, b, tol=1e-12, max_cycles=200)
+    assert st["status"] == 0
+    uo, vo, wo = orc.correct(rho, p, case.dt, u, v, w, case.spacing)
+    mx0, _ = orc.div_stats(u, v, w, case.spacing)
+    mx, mean = orc.div_stats(uo, vo, wo, case.spacing)
+    assert mx < 1e-9 * mx0
+
+
+# --- point relaxation (ppe_sor_solver) ----------------------------------------------
+def test_sor_matches_reference_loop():
+    case, rho, coef, _, b, _ = _small_case((1, 10, 12))
+    nz, ny, nx = rho.shape
+    coe7 = ref.ppe_sor_init(ref.pad(rho), nx, ny, nz, *case.spacing)
+    p_ref, it_ref, _ = ref.ppe_sor_solver(coe7, b, np.zeros_like(b), 1.5, 0.0, 25)
+    p_or, it_or, _ = orc.sor_solve(coef, b, w=1.5, tol=0.0, max_iter=25)
+    assert it_ref == 25 and it_or == -25
+    np.testing.assert_allclose(p_or, p_ref, rtol=0, atol=1e-11 * np.abs(p_ref).max())
+
+
+def test_multigrid_reaches_the_point_relaxation_fixed_point():
+    case, rho, coef, _, b, _ = _small_case((1, 16, 16), ratio=10.0)
+    p_sor, it, err = orc.sor_solve(coef, b, w=1.0, tol=1e-13, max_iter=200000)
+    assert it > 0
+    p_mg, st = orc.mg_solve(coef, b, tol=1e-13)
+    assert st["status"] == 0
+    p_sor = p_sor - p_sor.mean()
+    assert np.linalg.norm(p_mg - p_sor) <= 1e-9 * np.linalg.norm(p_sor)
+
+
+# --- the cycle (DomainDecomposition multigrid) -------------------------------------
+@pytest.mark.parametrize("shape,levels", [((1, 16, 16), 3), ((8, 8, 8), 3)])
+def test_cycle_matches_domain_decomposition_multigrid(shape, levels):
+    """Constant coefficients, one subdomain, lexicographic GS with the folded
+    wall closure: the oracle's cycle equals the transliterated reference cycle
+    iterate by iterate."""
+    nz, ny, nx = shape
+    h = 1.0 / nx
+    rho = np.ones(shape)
+    coef = orc.face_coef(rho, (h, h, h))
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(shape)
+    b -= b.mean()
+    dd = ref.DDMultigrid(nx, ny, nz, h, h, h, levels, wall="folded")
+    iters = dd.solve(b, np.zeros(shape), 3)
+    for k, p_ref in enumerate(iters, start=1):
+        p_or, st = orc.mg_solve(coef, b, tol=1e-300, max_cycles=k, levels=levels, smoother=1,
+                                record_history=0)
+        assert st["cycles"] == k
+        np.testing.assert_allclose(p_or, p_ref, rtol=0, atol=1e-11 * np.abs(p_ref).max())
+
+
+def test_ghost_wall_closure_converges_like_folded():
+    """multigrid_relax as written (wall ghost lagged one sweep) and the folded
+    closure reach the same solution at a similar rate."""
+    shape, levels = (1, 16, 16), 3
+    h = 1.0 / 16
+    rng = np.random.default_rng(4)
+    b = rng.standard_normal(shape)
+    b -= b.mean()
+    res = {}
+    for wall in ("ghost", "folded"):
+        dd = ref.DDMultigrid(16, 16, 1, h, h, h, levels, wall=wall)
+        res[wall] = dd.solve(b, np.zeros(shape), 12)[-1]
+    np.testing.assert_allclose(res["ghost"], res["folded"], atol=1e-8 * np.abs(res["folded"]).max())
+
+
+def test_red_black_and_lexicographic_agree_at_convergence():
+    case, rho, coef, _, b, _ = _small_case((16, 16, 16))
+    p_rb, s_rb = orc.mg_solve(coef, b, tol=1e-11)
+    p_lx, s_lx = orc.mg_solve(coef, b, tol=1e-11, smoother=1, blocks=(2, 2, 2))
+    assert s_rb["status"] == 0 and s_lx["status"] == 0
+    assert abs(s_rb["cycles"] - s_lx["cycles"]) <= 3
+    assert np.linalg.norm(p_rb - p_lx) <= 1e-8 * np.linalg.norm(p_rb)
+
+
+def test_mean_projection_per_sweep_is_shift_equivariant():
+    """The cycle commutes with adding constants, so projecting the mean after
+    every sweep (the reference) or once at the end gives the same iterates up
+    to rounding -- the GPU path projects once per solve."""
+    case, rho, coef, _, b, _ = _small_case((16, 16, 16))
+    p1, s1 = orc.mg_solve(coef, b, tol=1e-10, mean_every_sweep=1)
+    p0, s0 = orc.mg_solve(coef, b, tol=1e-10, mean_every_sweep=0)
+    assert s1["cycles"] == s0["cycles"]
+    assert np.linalg.norm(p1 - p0) <= 1e-11 * np.linalg.norm(p1)
+    # residuals near 1e-10 of |b| carry relative rounding noise of ~1e-6
+    np.testing.assert_allclose(s1["history"], s0["history"], rtol=1e-3)
+
+
+def test_krylov_mode_reaches_same_solution():
+    case = inputs.config(2, 8)
+    phi = inputs.level_set(case)
+    rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
+    coef = orc.face_coef(rho, case.spacing)
+    b = orc.divergence(*inputs.velocity(case), case.dt, case.spacing)
+    p_k, s_k = orc.mg_solve(coef, b, tol=1e-10, krylov=1)
+    assert s_k["status"] == 0
+    p_v, s_v = orc.mg_solve(coef, b, tol=1e-10, max_cycles=400)
+    assert s_v["status"] == 0 and s_v["cycles"] > s_k["cycles"]
+    assert np.linalg.norm(p_k - p_v) <= 1e-8 * np.linalg.norm(p_v)
+
+
+# --- levels ---------------------------------------------------------------------
+def test_level_plan():
+    assert orc.mg_plan((256, 256, 256)) == [(256 >> l,) * 3 for l in range(7)]
+    assert orc.mg_plan((1, 128, 128)) == [(1, 128 >> l, 128 >> l) for l in range(5)]
+    assert orc.mg_plan((256, 128, 128))[-1] == (4, 2, 2)
+    assert orc.mg_plan((1, 12, 20)) == [(1, 12, 20), (1, 6, 10)]
+    assert orc.mg_plan((1, 12, 20), coarse_max=1) == [(1, 12, 20), (1, 6, 10), (1, 3, 5)]
+    assert orc.mg_plan((8, 8, 8), levels=3) == [(8, 8, 8), (4, 4, 4), (2, 2, 2)]
+    assert orc.mg_plan((8, 8, 8), levels=5) == []   # the reference STOPs (branches.f90:190-210)
+    assert orc.mg_plan((1, 1, 1)) == [(1, 1, 1)]
+
+
+def test_coarse_coefficients_constant_case():
+    rho = np.full((8, 8, 8), 2.0)
+    coef = orc.face_coef(rho, (0.1, 0.1, 0.1))
+    c1 = orc.mg_level_coef(coef, 1, coarse_max=1)
+    interior = c1[0][:, :, 1:]
+    np.testing.assert_allclose(interior, 1.0 / 2.0 / 0.2 ** 2, rtol=1e-14)
+    assert (c1[0][:, :, 0] == 0).all() and (c1[1][:, 0, :] == 0).all() and (c1[2][0] == 0).all()
+
+
+def test_status_codes():
+    case, rho, coef, _, b, _ = _small_case((8, 8, 8))
+    _, st = orc.mg_solve(coef, b, tol=1e-14, max_cycles=1)
+    assert st["status"] == 1 and st["cycles"] == 1
+    bad = [c.copy() for c in coef]
+    bad[0][3, 3, 3] = np.nan
+    _, st = orc.mg_solve(tuple(bad), b, tol=1e-10)
+    assert st["status"] == 2
