@@ -36,6 +36,7 @@ struct Level {
   double *sol = nullptr, *src = nullptr;  // owned on levels >= 1
   float *cx32 = nullptr, *cy32 = nullptr, *cz32 = nullptr;
   float *sol32 = nullptr, *src32 = nullptr;
+  float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -211,6 +212,30 @@ template <typename T> const T* adense_of(const gbmg_handle* h);
 template <> const double* adense_of<double>(const gbmg_handle* h) { return h->adense; }
 template <> const float* adense_of<float>(const gbmg_handle* h) { return h->adense32; }
 
+// One red-black sweep of level l.  FP64: two colour launches in place.
+// FP32: one fused launch out of place, after which the level's solution lives
+// in the other buffer (the host swaps the pointers; graph capture records the
+// resulting sequence, which replays identically).
+template <typename T>
+void sweep(gbmg_handle* h, int l, int first_color);
+
+template <>
+void sweep<double>(gbmg_handle* h, int l, int first_color) {
+  const LevelView<double> V = v64(h->lv[l]);
+  const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
+  LAUNCH(h, cs, launch_smooth<double>(h->stream, V, first_color));
+  LAUNCH(h, cs, launch_smooth<double>(h->stream, V, 1 - first_color));
+}
+
+template <>
+void sweep<float>(gbmg_handle* h, int l, int first_color) {
+  Level& lv = h->lv[l];
+  const LevelView<float> V = v32(lv);
+  const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
+  LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
+  std::swap(lv.sol32, lv.alt32);
+}
+
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
 // the post-smoothing colours black-first (symmetric preconditioner for CG).
 template <typename T>
@@ -218,28 +243,18 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post) {
   const int L = h->L;
   const cudaStream_t s = h->stream;
   for (int l = 0; l < L - 1; ++l) {
-    const LevelView<T> V = view<T>(h->lv[l]);
-    const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-    for (int it = 0; it < h->prm.nu1; ++it) {
-      LAUNCH(h, cs, launch_smooth<T>(s, V, 0));
-      LAUNCH(h, cs, launch_smooth<T>(s, V, 1));
-    }
+    for (int it = 0; it < h->prm.nu1; ++it) sweep<T>(h, l, 0);
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
-           launch_restrict<T>(s, V, view<T>(h->lv[l + 1])));
+           launch_restrict<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
   }
   const Level& c = h->lv[L - 1];
   const LevelView<T> C = view<T>(c);
   LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
          launch_coarse_solve<T>(s, h->nc, minv_of<T>(h), adense_of<T>(h), C.src, C.sol));
   for (int l = L - 2; l >= 0; --l) {
-    const LevelView<T> V = view<T>(h->lv[l]);
-    const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
     LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
-           launch_prolong<T>(s, V, view<T>(h->lv[l + 1])));
-    for (int it = 0; it < h->prm.nu2; ++it) {
-      LAUNCH(h, cs, launch_smooth<T>(s, V, reverse_post ? 1 : 0));
-      LAUNCH(h, cs, launch_smooth<T>(s, V, reverse_post ? 0 : 1));
-    }
+           launch_prolong<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
+    for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0);
   }
   return check_launch(h, "v-cycle");
 }
@@ -273,7 +288,7 @@ int free_all(gbmg_handle* h) {
     Level& v = h->lv[l];
     dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
     if (l > 0) { dfree(v.sol); dfree(v.src); }
-    dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.src32);
+    dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.alt32); dfree(v.src32);
   }
   dfree(h->b); dfree(h->p); dfree(h->rho);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
@@ -330,6 +345,7 @@ int allocate(gbmg_handle* h) {
       GB_TRY(dmalloc(h, &v.cy32, v.n));
       GB_TRY(dmalloc(h, &v.cz32, v.n));
       GB_TRY(dmalloc(h, &v.sol32, v.n));
+      GB_TRY(dmalloc(h, &v.alt32, v.n));
       GB_TRY(dmalloc(h, &v.src32, v.n));
     }
   }

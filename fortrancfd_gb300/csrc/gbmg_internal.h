@@ -55,6 +55,11 @@ enum : int {
 // ---- launchers (kernels_mg.cu) ---------------------------------------------
 template <typename T>
 void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color);
+// One whole red-black sweep, out of place (smooth_fused.cu); first_color 0 =
+// red first.  Instantiated for float.
+template <typename T>
+void launch_smooth_fused(cudaStream_t s, const LevelView<T>& L, const T* pin, T* pout,
+                         int first_color);
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
 template <typename T>
