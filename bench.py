@@ -151,13 +151,15 @@ def traffic_per_cell():
         return {}
 
 
-# algorithmic bytes per fine cell per launch of each kernel class (w = word size)
-def algorithmic_bytes_per_cell(cls, w):
+# algorithmic bytes per fine cell per launch of each kernel class, mixed solve:
+# FP32 cycle arrays (w = 4) and the double-word defect kernel
+def algorithmic_bytes_per_cell(cls, w=4):
     return {
-        "smooth_fine": 3.0 * w,                 # half sweep of the 6w/cell sweep (p, b, bx, by, bz, p')
+        "smooth_fine": 6.0 * w,                  # one fused sweep: p, b, bx, by, bz read, p' write
         "restrict_fine": 5.0 * w + 2.0 * w / 8,  # p, b, bx, by, bz -> coarse b, sol
         "prolong_fine": 2.0 * w + w / 8,         # p r/w + coarse e
-        "residual": 40.0 + (4.0 if w == 4 else 0.0),  # FP64 p, b, bx, by, bz (+ FP32 r)
+        "residual": 56.0,                        # defect: p(8) + e(4) + b(8) + 3 coefs(24) in,
+                                                 # p(8) + r32(4) out
     }.get(cls)
 
 
@@ -177,11 +179,13 @@ def run_reference(args):
     blocks = _factor3(threads)
     times, cycles = [], []
 
+    b = orc.divergence(u, v, w, case.dt, case.spacing)
+
     def step():
+        # the same step as the GPU arm: operator from the level set, then the solve
+        t0 = time.perf_counter()
         rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
         coef = orc.face_coef(rho, case.spacing)
-        b = orc.divergence(u, v, w, case.dt, case.spacing)
-        t0 = time.perf_counter()
         p, st = orc.mg_solve(coef, b, tol=TOL, smoother=1, blocks=blocks)
         return (time.perf_counter() - t0) * 1e3, st
 
@@ -229,13 +233,13 @@ def cpu_baseline(case, phi, u, v, w, budget_s):
 
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
-    rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
-    coef = orc.face_coef(rho, case.spacing)
     b = orc.divergence(u, v, w, case.dt, case.spacing)
     times = []
     t_start = time.perf_counter()
     while True:
         t0 = time.perf_counter()
+        rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
+        coef = orc.face_coef(rho, case.spacing)
         _, st = orc.mg_solve(coef, b, tol=TOL)
         times.append((time.perf_counter() - t0) * 1e3)
         if time.perf_counter() - t_start > budget_s * 0.5:

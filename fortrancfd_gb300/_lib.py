@@ -33,7 +33,8 @@ EXPORTS = (
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
-                "prolong_fine", "prolong_coarse", "coarse_solve", "residual", "vector", "setup")
+                "prolong_fine", "prolong_coarse", "coarse_solve", "residual", "vector", "setup",
+                "certify")
 
 
 class Grid(C.Structure):
@@ -45,7 +46,7 @@ class Params(C.Structure):
     _fields_ = [("precision", C.c_int32), ("nu1", C.c_int32), ("nu2", C.c_int32),
                 ("levels", C.c_int32), ("coarse_max", C.c_int32), ("max_cycles", C.c_int32),
                 ("krylov", C.c_int32), ("use_graph", C.c_int32), ("remove_rhs_mean", C.c_int32),
-                ("device", C.c_int32), ("stream", C.c_void_p)]
+                ("certify", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p)]
 
 
 class Stats(C.Structure):

@@ -68,10 +68,14 @@ struct gbmg_handle {
   // reductions
   ReduceScratch red{};
   double* host_res = nullptr;  // pinned mirror of red.result
-  // graphs
-  cudaGraphExec_t graph = nullptr;
-  int graph_kind = kGraphNone;
-  int64_t graph_kernels = 0;
+  // double-word finest level of the mixed solve: p (ping-pong), b, coefficients
+  float2* pw[2] = {nullptr, nullptr};
+  float2* bw = nullptr;
+  float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
+  int pcur = 0;  // which pw holds the current pressure
+  // captured iterations, per kind and per parity of pcur
+  cudaGraphExec_t graph[4][2] = {};
+  int64_t graph_kernels[4][2] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int64_t launches = 0;
   // profiling: event pairs around launches, summed per kernel class
@@ -274,16 +278,23 @@ double vcycle_bytes(const gbmg_handle* h, int w) {
   return bytes;
 }
 
-int reset_graph(gbmg_handle* h) {
-  if (h->graph) cudaGraphExecDestroy(h->graph);
-  h->graph = nullptr;
-  h->graph_kind = kGraphNone;
-  h->graph_kernels = 0;
+int reset_graphs(gbmg_handle* h) {
+  for (int k = 0; k < 4; ++k)
+    for (int par = 0; par < 2; ++par) {
+      if (h->graph[k][par]) cudaGraphExecDestroy(h->graph[k][par]);
+      h->graph[k][par] = nullptr;
+      h->graph_kernels[k][par] = 0;
+    }
   return GBMG_OK;
 }
 
+DwOperator dw_op(const gbmg_handle* h) {
+  const Level& f = h->lv[0];
+  return DwOperator{f.nx, f.ny, f.nz, h->cxw, h->cyw, h->czw, h->bw};
+}
+
 int free_all(gbmg_handle* h) {
-  reset_graph(h);
+  reset_graphs(h);
   for (int l = 0; l < h->L; ++l) {
     Level& v = h->lv[l];
     dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
@@ -291,6 +302,7 @@ int free_all(gbmg_handle* h) {
     dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.alt32); dfree(v.src32);
   }
   dfree(h->b); dfree(h->p); dfree(h->rho);
+  dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
   dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32);
@@ -354,6 +366,14 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->b, h->n0));
   GB_TRY(dmalloc(h, &h->p, h->n0));
   GB_TRY(dmalloc(h, &h->rho, h->n0));
+  if (h->mixed) {
+    GB_TRY(dmalloc(h, &h->pw[0], h->n0));
+    GB_TRY(dmalloc(h, &h->pw[1], h->n0));
+    GB_TRY(dmalloc(h, &h->bw, h->n0));
+    GB_TRY(dmalloc(h, &h->cxw, h->n0));
+    GB_TRY(dmalloc(h, &h->cyw, h->n0));
+    GB_TRY(dmalloc(h, &h->czw, h->n0));
+  }
   if (h->prm.krylov) {
     GB_TRY(dmalloc(h, &h->kr, h->n0));
     GB_TRY(dmalloc(h, &h->kz, h->n0));
@@ -366,7 +386,9 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->minv32, (size_t)nc * nc));
   GB_TRY(dmalloc(h, &h->adense32, (size_t)nc * nc));
   const size_t rows = (size_t)h->lv[0].ny * h->lv[0].nz;
-  const int mb = std::max(reduce_blocks_for(rows), reduce_blocks_for(h->n0));
+  const dim3 dg = defect_grid(h->lv[0].nx, h->lv[0].ny, h->lv[0].nz);
+  const int mb = std::max({reduce_blocks_for(rows), reduce_blocks_for(h->n0),
+                           (int)(dg.x * dg.y * dg.z)});
   h->red.max_blocks = mb;
   GB_TRY(dmalloc(h, &h->red.partials, (size_t)kRedValues * mb));
   GB_TRY(dmalloc(h, &h->red.counter, 1));
@@ -443,6 +465,12 @@ int build_hierarchy(gbmg_handle* h) {
   }
   LAUNCH(h, GBMG_PROF_SETUP,
          launch_coarse_invert(s, v64(h->lv[h->L - 1]), h->minv, h->adense, h->minv32, h->adense32));
+  if (h->mixed) {
+    const Level& f = h->lv[0];
+    LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cx, h->cxw, f.n));
+    LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cy, h->cyw, f.n));
+    LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cz, h->czw, f.n));
+  }
   GB_TRY(check_launch(h, "hierarchy"));
   h->coef_ready = true;
   return GBMG_OK;
@@ -467,6 +495,7 @@ int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
   if (h->prm.remove_rhs_mean)
     LAUNCH(h, GBMG_PROF_VECTOR,
            launch_shift_by_mean(h->stream, h->b, h->b, h->n0, h->red, kSlotSumB, kSlotSumB + 1));
+  if (h->mixed) LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(h->stream, h->b, h->bw, h->n0));
   GB_TRY(check_launch(h, "rhs"));
   GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
                              cudaMemcpyDeviceToHost, h->stream));
@@ -494,11 +523,12 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
     GB_TRY(enqueue_vcycle<double>(h, false));
     LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
   } else if (kind == kGraphMixed) {
+    // e = V-cycle(r) in FP32; p += e and r = b - A p in double-word
     GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
     GB_TRY(enqueue_vcycle<float>(h, false));
-    LAUNCH(h, V, launch_add_float(s, h->p, f.sol32, n));
-    f.sol = h->p; f.src = h->b;
-    LAUNCH(h, R, launch_residual_norm<float>(s, v64(f), f.src32, h->red, kSlotNorm));
+    const int c = h->pcur;
+    LAUNCH(h, R, launch_defect(s, dw_op(h), h->pw[c], h->pw[1 - c], f.sol32, f.src32, h->red,
+                               kSlotNorm));
   } else {
     // flexible CG: z = M r (one V-cycle from zero), mean-free
     if (kind == kGraphPcg64) {
@@ -531,8 +561,9 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
     GB_TRY(enqueue_iteration(h, kind, first));
     return GBMG_OK;
   }
-  if (h->graph_kind != kind) {
-    reset_graph(h);
+  const int par = kind == kGraphMixed ? h->pcur : 0;
+  cudaGraphExec_t& gx = h->graph[kind][par];
+  if (!gx) {
     cudaGraph_t g = nullptr;
     const int64_t before = h->launches;
     GB_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -547,19 +578,18 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
       if (g) cudaGraphDestroy(g);
       return GBMG_CUDA_ERROR;
     }
-    h->graph_kernels = h->launches - before;
+    h->graph_kernels[kind][par] = h->launches - before;
     h->launches = before;
-    const cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+    const cudaError_t ei = cudaGraphInstantiate(&gx, g, 0);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
       h->err = std::string("graph instantiate: ") + cudaGetErrorString(ei);
-      h->graph = nullptr;
+      gx = nullptr;
       return GBMG_CUDA_ERROR;
     }
-    h->graph_kind = kind;
   }
-  GB_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
-  h->launches += h->graph_kernels;
+  GB_CUDA(h, cudaGraphLaunch(gx, h->stream));
+  h->launches += h->graph_kernels[kind][par];
   return GBMG_OK;
 }
 
@@ -577,7 +607,11 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
     GB_CUDA(h, cudaMemsetAsync(h->kzold, 0, n * sizeof(double), s));
   } else if (h->mixed) {
-    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<float>(s, v64(f), f.src32, h->red, kSlotNorm));
+    // p into double-word, then the first residual (no correction yet)
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
+    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_defect(s, dw_op(h), h->pw[0], h->pw[1], nullptr, f.src32,
+                                                h->red, kSlotNorm));
+    h->pcur = 1;
   } else {
     LAUNCH(h, GBMG_PROF_RESIDUAL,
            launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
@@ -594,6 +628,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   } else {
     for (cyc = 1; cyc <= h->prm.max_cycles; ++cyc) {
       GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
+      if (kind == kGraphMixed) h->pcur ^= 1;
       GB_CUDA(h, cudaStreamSynchronize(s));
       prof_flush(h);
       r2 = h->host_res[kSlotNorm];
@@ -604,9 +639,24 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     if (cyc > h->prm.max_cycles) cyc = h->prm.max_cycles;
   }
   // mean projection of p (compatibility_sol on the finest level)
-  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
-  LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
+  if (kind == kGraphMixed) {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_sum(s, h->pw[h->pcur], n, h->red, kSlotSum));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_out(s, h->pw[h->pcur], h->p, n, h->red, kSlotSum));
+  } else {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
+  }
   GB_TRY(check_launch(h, "mean"));
+  if (kind == kGraphMixed && h->prm.certify) {
+    // the loop tracked the residual in double-word; restate it in native FP64
+    f.sol = h->p; f.src = h->b;
+    LAUNCH(h, GBMG_PROF_CERTIFY,
+           launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
+    GB_TRY(check_launch(h, "certify"));
+    GB_TRY(read_result(h, kSlotNorm, &r2));
+    rel = std::sqrt(r2) / scale;
+    if (status == GBMG_OK && !(rel < tol)) status = GBMG_NOT_CONVERGED;
+  }
   st->status = status;
   st->cycles = cyc;
   st->levels = h->L;
@@ -616,7 +666,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   // algorithmic bytes: per cycle V-cycle + FP64 residual (p, b, cx, cy, cz)
   const int w = h->mixed ? 4 : 8;
   double per = vcycle_bytes(h, w) + 40.0 * n;
-  if (h->mixed) per += 4.0 * n + 20.0 * n + 4.0 * n;  // r32 write, p += e, zero e
+  if (h->mixed) per += 16.0 * n + 4.0 * n;  // defect: + e read, p write, r32 write; zero e
   if (pcg) per += (h->mixed ? 24.0 : 8.0) * n + 16.0 * n + 32.0 * n + 48.0 * n + 24.0 * n + 8.0 * n;
   st->bytes = per * cyc + 40.0 * n + 32.0 * n;
   return status;
@@ -656,6 +706,7 @@ void gbmg_default_params(gbmg_params* prm) {
   prm->krylov = 0;
   prm->use_graph = 1;
   prm->remove_rhs_mean = 1;
+  prm->certify = 1;
   prm->device = -1;
   prm->stream = nullptr;
 }

@@ -118,4 +118,22 @@ void launch_double_to_float(cudaStream_t s, const double* a, float* b, size_t n)
 
 int reduce_blocks_for(size_t n);
 
+// ---- double-word (float-float) operator of the finest level (kernels_dw.cu) ----
+struct DwOperator {
+  int nx, ny, nz;
+  const float2* cx;
+  const float2* cy;
+  const float2* cz;
+  const float2* b;
+};
+dim3 defect_grid(int nx, int ny, int nz);
+// p_out = p_in + e (e may be null), r32 = float(b - A p_out), slot <- sum r^2
+void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
+                   const float* e, float* r32, const ReduceScratch& R, int slot);
+void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
+void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
+// out = double(p) - result[slot]/n
+void launch_dw_out(cudaStream_t s, const float2* p, double* out, size_t n, const ReduceScratch& R,
+                   int slot);
+
 }  // namespace gbmg

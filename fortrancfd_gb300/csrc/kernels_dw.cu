@@ -1,0 +1,163 @@
+// Double-word kernels of the mixed-precision solve (sm_103a).
+//
+// k_defect is the FP64-accuracy half of one defect-correction step:
+//     p_out = p_in + e          (e: the FP32 V-cycle's correction)
+//     r     = b - A p_out       (the operator of ppe_sor_init, double-word)
+//     r32   = float(r), and sum r^2 for the stopping test
+// in one pass.  Blocks own 32 x 8 tiles of the x-y plane and march up a chunk
+// of z planes with a 3-plane ring of p_out (tile + 1-cell halo) in shared
+// memory; halo cells are updated redundantly and only the owner stores them.
+// It runs out of place (p_in -> p_out) so that no block ever reads a value
+// another block already advanced.  Per cell: read p (8 B), e (4), b (8), three
+// coefficients (24); write p (8), r32 (4): 56 bytes.
+//
+// The residual is sum_f coe_f (p_nb - p_i) as in multigrid_residual
+// ("DomainDecomposition/3D/src/others/multigrid_solver.f90:162-222") with the
+// coefficients of ppe_sor_init ("Two phase flows/newOpenMP/3D+IBM/src/
+// ns_solver/ns_ppe_solver.f90:1-65"): differences first, so each term's
+// rounding is relative to a flux, not to |p|.
+#include <algorithm>
+
+#include "dword.cuh"
+#include "gbmg_internal.h"
+#include "reduce.cuh"
+
+namespace gbmg {
+
+namespace {
+
+constexpr int kDTX = 32, kDTY = 8, kDZ = 32;
+constexpr int kDSX = kDTX + 2, kDSY = kDTY + 2;
+
+struct DefectRing {
+  float2 p[3][kDSY][kDSX];
+};
+
+__device__ __forceinline__ void defect_load(const DwOperator& A, const float2* __restrict__ pin,
+                                            float2* __restrict__ pout, const float* __restrict__ e,
+                                            DefectRing& R, int k, int x0, int y0, int z0, int z1,
+                                            int tid) {
+  const int slot = k % 3;
+  const size_t sz = (size_t)A.nx * A.ny;
+  for (int t = tid; t < kDSX * kDSY; t += kDTX * kDTY) {
+    const int lx = t % kDSX, ly = t / kDSX;
+    const int x = x0 - 1 + lx, y = y0 - 1 + ly;
+    float2 v = make_float2(0.f, 0.f);
+    if (x >= 0 && x < A.nx && y >= 0 && y < A.ny) {
+      const size_t q = (size_t)k * sz + (size_t)y * A.nx + x;
+      dw a = dw_ldg(pin + q);
+      if (e) a = dw_add_f(a, __ldg(e + q));
+      v = make_float2(a.hi, a.lo);
+      if (lx >= 1 && lx <= kDTX && ly >= 1 && ly <= kDTY && k >= z0 && k < z1) pout[q] = v;
+    }
+    R.p[slot][ly][lx] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const float2* __restrict__ pin,
+                                                        float2* __restrict__ pout,
+                                                        const float* __restrict__ e,
+                                                        float* __restrict__ r32, ReduceScratch R,
+                                                        int slot) {
+  __shared__ DefectRing ring;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
+  const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
+  const int z0 = blockIdx.z * kDZ, z1 = min(z0 + kDZ, A.nz);
+  const int x = x0 + tx, y = y0 + ty;
+  const bool mine = x < A.nx && y < A.ny;
+  const size_t sy = (size_t)A.nx, sz = (size_t)A.nx * A.ny;
+  float s2 = 0.f;
+  if (z0 > 0) defect_load(A, pin, pout, e, ring, z0 - 1, x0, y0, z0, z1, tid);
+  defect_load(A, pin, pout, e, ring, z0, x0, y0, z0, z1, tid);
+  for (int k = z0; k < z1; ++k) {
+    if (k + 1 < A.nz) defect_load(A, pin, pout, e, ring, k + 1, x0, y0, z0, z1, tid);
+    __syncthreads();
+    if (mine) {
+      const int s0 = k % 3, sm = (k + 2) % 3, sp = (k + 1) % 3;
+      const size_t q = (size_t)k * sz + (size_t)y * sy + x;
+      const float2 c2 = ring.p[s0][ty + 1][tx + 1];
+      const dw pc{c2.x, c2.y};
+      dw acc{0.f, 0.f};
+#define DW_TERM(cond, cptr, nbv)                                   \
+      if (cond) {                                                  \
+        const float2 nb = nbv;                                     \
+        const dw d = dw_sub(dw{nb.x, nb.y}, pc);                    \
+        acc = dw_add(acc, dw_mul(dw_ldg(cptr), d));                 \
+      }
+      DW_TERM(x > 0, A.cx + q, ring.p[s0][ty + 1][tx])
+      DW_TERM(x < A.nx - 1, A.cx + q + 1, ring.p[s0][ty + 1][tx + 2])
+      DW_TERM(y > 0, A.cy + q, ring.p[s0][ty][tx + 1])
+      DW_TERM(y < A.ny - 1, A.cy + q + sy, ring.p[s0][ty + 2][tx + 1])
+      DW_TERM(k > 0, A.cz + q, ring.p[sm][ty + 1][tx + 1])
+      DW_TERM(k < A.nz - 1, A.cz + q + sz, ring.p[sp][ty + 1][tx + 1])
+#undef DW_TERM
+      const dw r = dw_sub(dw_ldg(A.b + q), acc);
+      const float rf = dw_to_float(r);
+      r32[q] = rf;
+      s2 = fmaf(rf, rf, s2);
+    }
+    __syncthreads();
+  }
+  double v[1] = {(double)s2};
+  grid_sum_finish<1>(v, R, slot);
+}
+
+__global__ void k_to_dw(const double* __restrict__ a, float2* __restrict__ out, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const dw v = dw_from_double(a[q]);
+    out[q] = make_float2(v.hi, v.lo);
+  }
+}
+
+// slot <- sum of the double values of p (for the final mean projection)
+__global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict__ p, size_t n,
+                                                        ReduceScratch R, int slot) {
+  double acc[1] = {0.0};
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    acc[0] += dw_to_double(dw_ldg(p + q));
+  grid_sum_finish<1>(acc, R, slot);
+}
+
+// out = double(p) - result[slot]/n
+__global__ void k_dw_out(const float2* __restrict__ p, double* __restrict__ out, size_t n,
+                         ReduceScratch R, int slot) {
+  const double m = R.result[slot] / (double)n;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    out[q] = dw_to_double(dw_ldg(p + q)) - m;
+}
+
+inline unsigned stride_blocks(size_t n) {
+  const size_t b = (n + kRedThreads - 1) / kRedThreads;
+  return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 152 * 8));
+}
+
+}  // namespace
+
+dim3 defect_grid(int nx, int ny, int nz) {
+  return dim3((unsigned)((nx + kDTX - 1) / kDTX), (unsigned)((ny + kDTY - 1) / kDTY),
+              (unsigned)((nz + kDZ - 1) / kDZ));
+}
+
+void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
+                   const float* e, float* r32, const ReduceScratch& R, int slot) {
+  k_defect<<<defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s>>>(A, pin, pout, e, r32, R, slot);
+}
+
+void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {
+  k_to_dw<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(a, out, n);
+}
+
+void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot) {
+  const unsigned b = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_dw_sum<<<b, kRedThreads, 0, s>>>(p, n, R, slot);
+}
+
+void launch_dw_out(cudaStream_t s, const float2* p, double* out, size_t n, const ReduceScratch& R,
+                   int slot) {
+  k_dw_out<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(p, out, n, R, slot);
+}
+
+}  // namespace gbmg

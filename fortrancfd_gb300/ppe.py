@@ -98,8 +98,8 @@ class PressurePoisson:
     """
 
     def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
-                 max_cycles=100, krylov=False, use_graph=True, remove_rhs_mean=True, device=None,
-                 stream=None):
+                 max_cycles=100, krylov=False, use_graph=True, remove_rhs_mean=True, certify=True,
+                 device=None, stream=None):
         if len(shape) == 2:
             shape = (1,) + tuple(shape)
         self.shape = tuple(int(s) for s in shape)
@@ -118,6 +118,7 @@ class PressurePoisson:
         prm.krylov = int(bool(krylov))
         prm.use_graph = int(bool(use_graph))
         prm.remove_rhs_mean = int(bool(remove_rhs_mean))
+        prm.certify = int(bool(certify))
         prm.device = -1 if device is None else int(device)
         # a torch.cuda.Stream, or a raw cudaStream_t handle; None = the handle's own stream
         prm.stream = getattr(stream, "cuda_stream", stream) or None

@@ -70,6 +70,8 @@ typedef struct {
   int32_t krylov;          /* 0: stationary V-cycles; 1: flexible CG, one V-cycle as preconditioner */
   int32_t use_graph;       /* 1: replay each cycle as a captured CUDA graph */
   int32_t remove_rhs_mean; /* 1: project the mean out of b before solving (compatibility) */
+  int32_t certify;         /* mixed precision: 1 = recompute the final residual in native FP64
+                              (the cycle loop tracks it in double-word FP32 pairs) */
   int32_t device;          /* CUDA device ordinal; -1 = the current device */
   void* stream;            /* cudaStream_t to run on; NULL = the handle creates its own */
 } gbmg_params;
@@ -95,7 +97,8 @@ typedef struct {
 typedef struct gbmg_handle gbmg_handle;
 
 /* Defaults: FP64, V(2,2), automatic levels, coarse_max 64, 100 cycles,
- * stationary cycles, graphs on, mean projection of b on, current device. */
+ * stationary cycles, graphs on, mean projection of b on, FP64 certification
+ * on, current device. */
 void gbmg_default_params(gbmg_params* prm);
 
 /* Allocates the device hierarchy for one grid.  Replaces the level set-up of
@@ -177,10 +180,11 @@ enum {
   GBMG_PROF_PROLONG_FINE = 4,  /* prolongation + correction into the finest level */
   GBMG_PROF_PROLONG_COARSE = 5,
   GBMG_PROF_COARSE_SOLVE = 6,
-  GBMG_PROF_RESIDUAL = 7,      /* FP64 residual + norm on the finest level */
+  GBMG_PROF_RESIDUAL = 7,      /* FP64 (or double-word) residual + norm on the finest level */
   GBMG_PROF_VECTOR = 8,        /* mean projection, p += e, Krylov vector kernels */
   GBMG_PROF_SETUP = 9,         /* coefficients, coarse operators, coarse inverse */
-  GBMG_PROF_CLASSES = 10
+  GBMG_PROF_CERTIFY = 10,      /* native FP64 residual after a mixed-precision solve */
+  GBMG_PROF_CLASSES = 11
 };
 int gbmg_set_profiling(gbmg_handle* h, int on);
 /* ms[c] = summed device time, launches[c] = launch count of class c since

@@ -39,6 +39,7 @@ def test_default_params_and_strerror():
     L.gbmg_default_params(C.byref(prm))
     assert (prm.precision, prm.nu1, prm.nu2, prm.max_cycles, prm.coarse_max) == (0, 2, 2, 100, 64)
     assert prm.use_graph == 1 and prm.remove_rhs_mean == 1 and prm.device == -1
+    assert prm.certify == 1 and prm.stream is None
     for code in range(8):
         assert L.gbmg_strerror(code)
     assert L.gbmg_strerror(1).decode().startswith("not converged")
