@@ -488,9 +488,9 @@ int set_rho_device(gbmg_handle* h) {
 }
 
 // b -> h->b with the mean removed (when asked); result[kSlotSumB+1] = |b|^2.
-int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
-  const gbmg_grid& g = h->grid;
-  GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
+// h->b holds the right-hand side: project its mean out (when asked), make the
+// double-word copy of the mixed solve, and return |b|.
+int finish_rhs(gbmg_handle* h, double* bnorm) {
   LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
   if (h->prm.remove_rhs_mean)
     LAUNCH(h, GBMG_PROF_VECTOR,
@@ -502,6 +502,12 @@ int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   *bnorm = std::sqrt(h->host_res[kSlotSumB + 1]);
   return GBMG_OK;
+}
+
+int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
+  const gbmg_grid& g = h->grid;
+  GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
+  return finish_rhs(h, bnorm);
 }
 
 int read_result(gbmg_handle* h, int slot, double* v) {
@@ -901,13 +907,10 @@ int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_
   h->launches += 1;
   GB_TRY(check_launch(h, "divergence"));
   // mean projection + norm of b in place
-  launch_sum(s, h->b, h->n0, h->red, kSlotSumB);
-  launch_shift_by_mean(s, h->b, h->b, h->n0, h->red, kSlotSumB, kSlotSumB + 1);
-  h->launches += 2;
-  double bn2 = 0.0;
-  GB_TRY(read_result(h, kSlotSumB + 1, &bn2));
+  double bnorm = 0.0;
+  GB_TRY(finish_rhs(h, &bnorm));
   GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
-  const int status = solve_internal(h, tol, std::sqrt(bn2), st);
+  const int status = solve_internal(h, tol, bnorm, st);
   if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
   // u -= dt beta grad p (ns_momentum_correction)
   launch_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, g.dx, g.dy, g.dz, dt, dv[0], dfield[0].sy,
