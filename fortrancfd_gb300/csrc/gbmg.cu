@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -37,6 +38,8 @@ struct Level {
   float *cx32 = nullptr, *cy32 = nullptr, *cz32 = nullptr;
   float *sol32 = nullptr, *src32 = nullptr;
   float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
+  float* buf_a = nullptr;  // the buffer sol32 pointed to at allocation
+  SweepMaps* tmaps = nullptr;  // TMA maps with p = buffer A and p = buffer B (host memory)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -73,6 +76,8 @@ struct gbmg_handle {
   float2* bw = nullptr;
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
+  int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
+  int* derr = nullptr;   // device error flags (TMA wait timeouts)
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
@@ -236,8 +241,17 @@ void sweep<float>(gbmg_handle* h, int l, int first_color) {
   Level& lv = h->lv[l];
   const LevelView<float> V = v32(lv);
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-  LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
-  std::swap(lv.sol32, lv.alt32);
+  if (lv.tmaps) {
+    const SweepMaps& m = lv.tmaps[lv.sol32 == lv.buf_a ? 0 : 1];
+    LAUNCH(h, cs, launch_smooth_tma(h->stream, m, lv.nx, lv.ny, lv.nz, lv.alt32, first_color, h->derr));
+    std::swap(lv.sol32, lv.alt32);
+  } else if (h->fused_levels > l) {
+    LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
+    std::swap(lv.sol32, lv.alt32);
+  } else {
+    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, first_color));
+    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, 1 - first_color));
+  }
 }
 
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
@@ -300,12 +314,14 @@ int free_all(gbmg_handle* h) {
     dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
     if (l > 0) { dfree(v.sol); dfree(v.src); }
     dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.alt32); dfree(v.src32);
+    delete[] v.tmaps;
+    v.tmaps = nullptr;
   }
   dfree(h->b); dfree(h->p); dfree(h->rho);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
-  dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32);
+  dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
   if (h->host_res) cudaFreeHost(h->host_res);
   h->host_res = nullptr;
@@ -316,6 +332,29 @@ int free_all(gbmg_handle* h) {
   h->ev0 = h->ev1 = nullptr;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   h->stream = nullptr;
+  return GBMG_OK;
+}
+
+// TMA-fed sweeps on the FP32 levels with at least 2^15 cells and rows a
+// multiple of 16 bytes (GBMG_TMA_LEVELS overrides how many finest levels).
+int setup_tma(gbmg_handle* h) {
+  int want = h->L;
+  if (const char* e = std::getenv("GBMG_TMA_LEVELS")) want = std::atoi(e);
+  if (smooth_tma_init() != 0) return GBMG_OK;  // keep the two-colour sweeps
+  for (int l = 0; l < h->L && l < want; ++l) {
+    Level& v = h->lv[l];
+    if (v.nx % 4 != 0 || v.n < (size_t(1) << 15)) continue;
+    SweepMaps* m = new SweepMaps[2];
+    v.buf_a = v.sol32;
+    const bool ok =
+        make_sweep_maps(&m[0], v.sol32, v.src32, v.cx32, v.cy32, v.cz32, v.nx, v.ny, v.nz) &&
+        make_sweep_maps(&m[1], v.alt32, v.src32, v.cx32, v.cy32, v.cz32, v.nx, v.ny, v.nz);
+    if (!ok) {
+      delete[] m;
+      continue;
+    }
+    v.tmaps = m;
+  }
   return GBMG_OK;
 }
 
@@ -396,6 +435,9 @@ int allocate(gbmg_handle* h) {
   GB_CUDA(h, cudaMemsetAsync(h->red.counter, 0, sizeof(unsigned int), h->stream));
   GB_CUDA(h, cudaMemsetAsync(h->red.result, 0, kRedSlots * sizeof(double), h->stream));
   GB_CUDA(h, cudaMallocHost((void**)&h->host_res, kRedSlots * sizeof(double)));
+  GB_TRY(dmalloc(h, &h->derr, 4));
+  GB_CUDA(h, cudaMemsetAsync(h->derr, 0, 4 * sizeof(int), h->stream));
+  if (h->mixed) GB_TRY(setup_tma(h));
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -662,6 +704,16 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     GB_TRY(read_result(h, kSlotNorm, &r2));
     rel = std::sqrt(r2) / scale;
     if (status == GBMG_OK && !(rel < tol)) status = GBMG_NOT_CONVERGED;
+  }
+  {
+    int flags = 0;
+    GB_CUDA(h, cudaMemcpyAsync(&flags, h->derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(h, cudaStreamSynchronize(s));
+    if (flags) {
+      h->err = "a TMA wait timed out inside the sweep kernel";
+      cudaMemsetAsync(h->derr, 0, sizeof(int), s);
+      return GBMG_CUDA_ERROR;
+    }
   }
   st->status = status;
   st->cycles = cyc;

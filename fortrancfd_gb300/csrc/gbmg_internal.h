@@ -7,6 +7,7 @@
 // has the same index map and alignment.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -55,6 +56,17 @@ enum : int {
 // ---- launchers (kernels_mg.cu) ---------------------------------------------
 template <typename T>
 void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color);
+// TMA descriptors of one FP32 level for the TMA-fed sweep (smooth_tma.cu).
+struct SweepMaps {
+  CUtensorMap p, b, cx, cy, cz;
+};
+bool make_sweep_maps(SweepMaps* m, const float* p, const float* b, const float* cx,
+                     const float* cy, const float* cz, int nx, int ny, int nz);
+int smooth_tma_init();
+// One whole red-black sweep, p (from maps.p) -> pout; *err |= 1 on a TMA wait timeout.
+void launch_smooth_tma(cudaStream_t s, const SweepMaps& maps, int nx, int ny, int nz, float* pout,
+                       int first_color, int* err);
+
 // One whole red-black sweep, out of place (smooth_fused.cu); first_color 0 =
 // red first.  Instantiated for float.
 template <typename T>

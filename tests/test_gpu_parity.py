@@ -255,3 +255,19 @@ def test_kernels_are_launched(cuda):
         s.ppe_init(c.rho)
         s.solve(c.b, tol=1e-10)
         assert s.kernel_launches > n0 + 20
+
+
+@pytest.mark.parametrize("idx,scale", [(1, 4), (4, 4)])
+def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale):
+    """The TMA-fed out-of-place sweep computes the same red-black sweep as the
+    two colour launches (GBMG_TMA_LEVELS=0 switches it off at handle creation)."""
+    c = cases.config(idx, scale)
+    out = {}
+    for levels in ("0", "99"):
+        monkeypatch.setenv("GBMG_TMA_LEVELS", levels)
+        with solver(c, precision="mixed") as s:
+            s.ppe_init(c.rho)
+            out[levels] = s.solve(c.b, tol=1e-10)
+    (p0, s0), (p1, s1) = out["0"], out["99"]
+    assert s0["cycles"] == s1["cycles"]
+    assert rel_l2(p1, p0) <= 1e-12
