@@ -257,15 +257,16 @@ def test_kernels_are_launched(cuda):
         assert s.kernel_launches > n0 + 20
 
 
-@pytest.mark.parametrize("idx,scale", [(1, 4), (4, 4)])
-def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale):
+@pytest.mark.parametrize("idx,scale,krylov", [(1, 4, False), (1, 2, False), (4, 4, True)])
+def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale, krylov):
     """The TMA-fed out-of-place sweep computes the same red-black sweep as the
-    two colour launches (GBMG_TMA_LEVELS=0 switches it off at handle creation)."""
+    two colour launches (GBMG_TMA_LEVELS=0 switches it off at handle creation);
+    the Krylov case runs its post-smoother black-first."""
     c = cases.config(idx, scale)
     out = {}
     for levels in ("0", "99"):
         monkeypatch.setenv("GBMG_TMA_LEVELS", levels)
-        with solver(c, precision="mixed") as s:
+        with solver(c, precision="mixed", krylov=krylov) as s:
             s.ppe_init(c.rho)
             out[levels] = s.solve(c.b, tol=1e-10)
     (p0, s0), (p1, s1) = out["0"], out["99"]
