@@ -78,6 +78,7 @@ struct gbmg_handle {
   int pcur = 0;  // which pw holds the current pressure
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
   int* derr = nullptr;   // device error flags (TMA wait timeouts)
+  DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B]
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
@@ -307,6 +308,18 @@ DwOperator dw_op(const gbmg_handle* h) {
   return DwOperator{f.nx, f.ny, f.nz, h->cxw, h->cyw, h->czw, h->bw};
 }
 
+// p_out = p_in + e, r32 = b - A p_out (double-word), |r|^2 -> slot; pc = p_in buffer.
+void enqueue_defect(gbmg_handle* h, int pc, const float* e, float* r32, int slot) {
+  const Level& f = h->lv[0];
+  if (h->dmaps) {
+    const int ei = e == nullptr ? 0 : (e == f.buf_a ? 1 : 2);
+    launch_defect_tma(h->stream, h->dmaps[pc * 3 + ei], f.nx, f.ny, f.nz, e != nullptr,
+                      h->pw[1 - pc], r32, h->red, slot, h->derr);
+  } else {
+    launch_defect(h->stream, dw_op(h), h->pw[pc], h->pw[1 - pc], e, r32, h->red, slot);
+  }
+}
+
 int free_all(gbmg_handle* h) {
   reset_graphs(h);
   for (int l = 0; l < h->L; ++l) {
@@ -322,6 +335,8 @@ int free_all(gbmg_handle* h) {
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
   dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
+  delete[] h->dmaps;
+  h->dmaps = nullptr;
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
   if (h->host_res) cudaFreeHost(h->host_res);
   h->host_res = nullptr;
@@ -338,8 +353,25 @@ int free_all(gbmg_handle* h) {
 // TMA-fed sweeps on the FP32 levels with at least 2^15 cells and rows a
 // multiple of 16 bytes (GBMG_TMA_LEVELS overrides how many finest levels).
 int setup_tma(gbmg_handle* h) {
-  int want = h->L;
+  // the two-colour FP32 sweep measured faster than the TMA-fed one on GB300
+  // (132 vs 143 us per 256^3 sweep), so the TMA sweep is opt-in
+  int want = 0;
   if (const char* e = std::getenv("GBMG_TMA_LEVELS")) want = std::atoi(e);
+  Level& f = h->lv[0];
+  f.buf_a = f.sol32;
+  const char* ed = std::getenv("GBMG_TMA_DEFECT");
+  if (f.nx % 4 == 0 && !(ed && std::atoi(ed) == 0) && defect_tma_init() == 0) {
+    DefectMaps* m = new DefectMaps[6];
+    bool ok = true;
+    for (int pc = 0; pc < 2; ++pc)
+      for (int ei = 0; ei < 3; ++ei) {
+        const float* e = ei == 0 ? nullptr : (ei == 1 ? f.sol32 : f.alt32);
+        ok = ok && make_defect_maps(&m[pc * 3 + ei], h->pw[pc], e, h->bw, h->cxw, h->cyw, h->czw,
+                                    f.nx, f.ny, f.nz);
+      }
+    if (ok) h->dmaps = m;
+    else delete[] m;
+  }
   if (smooth_tma_init() != 0) return GBMG_OK;  // keep the two-colour sweeps
   for (int l = 0; l < h->L && l < want; ++l) {
     Level& v = h->lv[l];
@@ -574,9 +606,7 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
     // e = V-cycle(r) in FP32; p += e and r = b - A p in double-word
     GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
     GB_TRY(enqueue_vcycle<float>(h, false));
-    const int c = h->pcur;
-    LAUNCH(h, R, launch_defect(s, dw_op(h), h->pw[c], h->pw[1 - c], f.sol32, f.src32, h->red,
-                               kSlotNorm));
+    LAUNCH(h, R, enqueue_defect(h, h->pcur, f.sol32, f.src32, kSlotNorm));
   } else {
     // flexible CG: z = M r (one V-cycle from zero), mean-free
     if (kind == kGraphPcg64) {
@@ -657,8 +687,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   } else if (h->mixed) {
     // p into double-word, then the first residual (no correction yet)
     LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
-    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_defect(s, dw_op(h), h->pw[0], h->pw[1], nullptr, f.src32,
-                                                h->red, kSlotNorm));
+    LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
     h->pcur = 1;
   } else {
     LAUNCH(h, GBMG_PROF_RESIDUAL,

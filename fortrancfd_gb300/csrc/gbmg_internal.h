@@ -142,6 +142,16 @@ dim3 defect_grid(int nx, int ny, int nz);
 // p_out = p_in + e (e may be null), r32 = float(b - A p_out), slot <- sum r^2
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
                    const float* e, float* r32, const ReduceScratch& R, int slot);
+// TMA-fed k_defect (finest level with nx % 4 == 0): maps of p, e, b, cx, cy, cz.
+struct DefectMaps {
+  CUtensorMap p, e, b, cx, cy, cz;
+};
+bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
+                      const float2* cx, const float2* cy, const float2* cz, int nx, int ny,
+                      int nz);
+int defect_tma_init();
+void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
+                       float2* pout, float* r32, const ReduceScratch& R, int slot, int* err);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
 // out = double(p) - result[slot]/n

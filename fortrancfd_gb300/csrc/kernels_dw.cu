@@ -21,6 +21,7 @@
 #include "dword.cuh"
 #include "gbmg_internal.h"
 #include "reduce.cuh"
+#include "tma.cuh"
 
 namespace gbmg {
 
@@ -102,6 +103,123 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
   grid_sum_finish<1>(v, R, slot);
 }
 
+// ---- TMA-fed defect ------------------------------------------------------------
+// Same arithmetic as k_defect; each plane's boxes (tile + 1-cell halo) of p, b,
+// cx, cy, cz (float pairs, through FP32 maps of doubled x extent, box from
+// x0-2) and e (FP32, box from x0-4) stream into a 4-slot ring two planes ahead
+// of the compute.  Wall coefficients are stored as zeros and TMA zero-fills
+// out-of-range box cells, so x and y walls add exact zeros.
+constexpr int kQBX = kDTX + 4;         // float-pair box width, from x0 - 2
+constexpr int kQBY = kDTY + 2;         // box height, from y0 - 1
+constexpr int kQEX = kDTX + 8;         // e box width, from x0 - 4
+constexpr int kQSlots = 4;
+constexpr int kQTile = kQBX * kQBY;    // float pairs per box (2880 bytes)
+constexpr int kQTileBytes = 2944;      // padded to a multiple of 128
+constexpr int kQEBytes = 1664;         // e box (1600 bytes) padded
+constexpr int kQSlotBytes = 5 * kQTileBytes + kQEBytes;  // 16384
+constexpr uint32_t kQPairBytes = kQTile * 8;
+constexpr uint32_t kQEBoxBytes = kQEX * kQBY * 4;
+constexpr size_t kQSmem = (size_t)kQSlots * kQSlotBytes + 128 + kQSlots * sizeof(uint64_t);
+
+__device__ __forceinline__ float2* qtile(unsigned char* base, int slot, int a) {
+  return reinterpret_cast<float2*>(base + (size_t)slot * kQSlotBytes + (size_t)a * kQTileBytes);
+}
+__device__ __forceinline__ float* qtile_e(unsigned char* base, int slot) {
+  return reinterpret_cast<float*>(base + (size_t)slot * kQSlotBytes + 5 * kQTileBytes);
+}
+
+__global__ void __launch_bounds__(kDTX * kDTY, 3)
+    k_defect_tma(const __grid_constant__ DefectMaps maps, int nx, int ny, int nz, int use_e,
+                 float2* __restrict__ pout, float* __restrict__ r32, ReduceScratch R, int slot,
+                 int* err) {
+  extern __shared__ unsigned char dsm_raw[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(dsm_raw) + 127) & ~uintptr_t(127));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)kQSlots * kQSlotBytes);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
+  const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
+  const int z0 = blockIdx.z * kDZ, z1 = min(z0 + kDZ, nz);
+  const int plo = max(z0 - 1, 0), phi = min(z1, nz - 1);
+  if (tid == 0) {
+    for (int s = 0; s < kQSlots; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  auto issue = [&](int k) {  // thread 0
+    const int s = k % kQSlots;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(&bar[s], 5 * kQPairBytes + (use_e ? kQEBoxBytes : 0));
+    const int xq = 2 * (x0 - 2), yq = y0 - 1;
+    tma_load_3d(qtile(base, s, 0), &maps.p, xq, yq, k, &bar[s]);
+    tma_load_3d(qtile(base, s, 1), &maps.b, xq, yq, k, &bar[s]);
+    tma_load_3d(qtile(base, s, 2), &maps.cx, xq, yq, k, &bar[s]);
+    tma_load_3d(qtile(base, s, 3), &maps.cy, xq, yq, k, &bar[s]);
+    tma_load_3d(qtile(base, s, 4), &maps.cz, xq, yq, k, &bar[s]);
+    if (use_e) tma_load_3d(qtile_e(base, s), &maps.e, x0 - 4, yq, k, &bar[s]);
+  };
+  uint32_t parity = 0;
+  const int pre_end = min(z0 + 1, phi);
+  if (tid == 0)
+    for (int k = plo; k <= pre_end; ++k) issue(k);
+  int issued = pre_end, waited = plo - 1;
+  float s2 = 0.f;
+  for (int k = z0; k < z1; ++k) {
+    if (k + 2 <= phi && k + 2 > issued) {
+      if (tid == 0) issue(k + 2);
+      issued = k + 2;
+    }
+    const int need = min(k + 1, phi);
+    while (waited < need) {
+      ++waited;
+      const int s = waited % kQSlots;
+      mbar_wait(&bar[s], (parity >> s) & 1u, err);
+      parity ^= 1u << s;
+      if (use_e) {  // p + e on the whole box
+        float2* P = qtile(base, s, 0);
+        const float* E = qtile_e(base, s);
+        for (int t = tid; t < kQTile; t += kDTX * kDTY) {
+          const int row = t / kQBX, col = t % kQBX;
+          const dw a = dw_add_f(dw{P[t].x, P[t].y}, E[row * kQEX + col + 2]);
+          P[t] = make_float2(a.hi, a.lo);
+        }
+      }
+      __syncthreads();
+    }
+    const int x = x0 + tx, y = y0 + ty;
+    if (x < nx && y < ny) {
+      const int s0 = k % kQSlots, sm = (k + kQSlots - 1) % kQSlots, sp = (k + 1) % kQSlots;
+      const int t = (ty + 1) * kQBX + (tx + 2);
+      const float2* P = qtile(base, s0, 0);
+      const float2* CX = qtile(base, s0, 2);
+      const float2* CY = qtile(base, s0, 3);
+      const dw pc{P[t].x, P[t].y};
+      dw acc{0.f, 0.f};
+#define DWQ_TERM(cv, nbv)                                              \
+      {                                                                \
+        const float2 c2 = cv, n2 = nbv;                                \
+        acc = dw_add(acc, dw_mul(dw{c2.x, c2.y}, dw_sub(dw{n2.x, n2.y}, pc))); \
+      }
+      DWQ_TERM(CX[t], P[t - 1])
+      DWQ_TERM(CX[t + 1], P[t + 1])
+      DWQ_TERM(CY[t], P[t - kQBX])
+      DWQ_TERM(CY[t + kQBX], P[t + kQBX])
+      if (k > 0) DWQ_TERM(qtile(base, s0, 4)[t], qtile(base, sm, 0)[t])
+      if (k < nz - 1) DWQ_TERM(qtile(base, sp, 4)[t], qtile(base, sp, 0)[t])
+#undef DWQ_TERM
+      const float2 b2 = qtile(base, s0, 1)[t];
+      const dw r = dw_sub(dw{b2.x, b2.y}, acc);
+      const size_t q = ((size_t)k * ny + y) * nx + x;
+      const float rf = dw_to_float(r);
+      r32[q] = rf;
+      pout[q] = P[t];
+      s2 = fmaf(rf, rf, s2);
+    }
+    __syncthreads();
+  }
+  double v[1] = {(double)s2};
+  grid_sum_finish<1>(v, R, slot);
+}
+
 __global__ void k_to_dw(const double* __restrict__ a, float2* __restrict__ out, size_t n) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
        q += (size_t)gridDim.x * blockDim.x) {
@@ -144,6 +262,34 @@ dim3 defect_grid(int nx, int ny, int nz) {
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
                    const float* e, float* r32, const ReduceScratch& R, int slot) {
   k_defect<<<defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s>>>(A, pin, pout, e, r32, R, slot);
+}
+
+bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
+                      const float2* cx, const float2* cy, const float2* cz, int nx, int ny,
+                      int nz) {
+  const CUtensorMapDataType f32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  const int nx2 = 2 * nx, bx2 = 2 * kQBX;
+  bool ok = make_tensor_map_3d(&m->p, p, f32, 4, nx2, ny, nz, bx2, kQBY) &&
+            make_tensor_map_3d(&m->b, b, f32, 4, nx2, ny, nz, bx2, kQBY) &&
+            make_tensor_map_3d(&m->cx, cx, f32, 4, nx2, ny, nz, bx2, kQBY) &&
+            make_tensor_map_3d(&m->cy, cy, f32, 4, nx2, ny, nz, bx2, kQBY) &&
+            make_tensor_map_3d(&m->cz, cz, f32, 4, nx2, ny, nz, bx2, kQBY);
+  if (e) ok = ok && make_tensor_map_3d(&m->e, e, f32, 4, nx, ny, nz, kQEX, kQBY);
+  else m->e = m->p;
+  return ok;
+}
+
+int defect_tma_init() {
+  return cudaFuncSetAttribute(k_defect_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kQSmem) == cudaSuccess
+             ? 0
+             : -1;
+}
+
+void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
+                       float2* pout, float* r32, const ReduceScratch& R, int slot, int* err) {
+  k_defect_tma<<<defect_grid(nx, ny, nz), dim3(kDTX, kDTY), kQSmem, s>>>(
+      maps, nx, ny, nz, use_e ? 1 : 0, pout, r32, R, slot, err);
 }
 
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {

@@ -21,6 +21,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "gbmg_internal.h"
 #include "tma.cuh"
@@ -62,14 +63,14 @@ __device__ __forceinline__ float relax(float* base, int s, int sm, int sp, bool 
 }
 
 __global__ void __launch_bounds__(kThreads, 2)
-    k_smooth_tma(const __grid_constant__ SweepMaps maps, int nx, int ny, int nz,
+    k_smooth_tma(const __grid_constant__ SweepMaps maps, int nx, int ny, int nz, int zc,
                  float* __restrict__ pout, int c0, int* err) {
   extern __shared__ unsigned char smem_raw[];
   float* base = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)kSlots * kArrays * kTile);
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * kTX, y0 = blockIdx.y * kTY;
-  const int z0 = blockIdx.z * kZC, z1 = min(z0 + kZC, nz);
+  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, nz);
   const int kstart = z0 > 0 ? z0 - 1 : z0;  // first plane whose first colour is computed
   const int kfirst_end = min(z1, nz - 1);   // last plane whose first colour is computed
   const int plo = max(kstart - 1, 0), phi = min(kfirst_end + 1, nz - 1);  // planes loaded
@@ -195,9 +196,14 @@ int smooth_tma_init() {
 
 void launch_smooth_tma(cudaStream_t s, const SweepMaps& maps, int nx, int ny, int nz, float* pout,
                        int first_color, int* err) {
+  static int zc = 0;
+  if (zc == 0) {
+    const char* e = std::getenv("GBMG_TMA_ZC");
+    zc = e ? std::max(1, std::atoi(e)) : kZC;
+  }
   const dim3 grd((unsigned)((nx + kTX - 1) / kTX), (unsigned)((ny + kTY - 1) / kTY),
-                 (unsigned)((nz + kZC - 1) / kZC));
-  k_smooth_tma<<<grd, kThreads, kSmemBytes, s>>>(maps, nx, ny, nz, pout, first_color, err);
+                 (unsigned)((nz + zc - 1) / zc));
+  k_smooth_tma<<<grd, kThreads, kSmemBytes, s>>>(maps, nx, ny, nz, zc, pout, first_color, err);
 }
 
 }  // namespace gbmg

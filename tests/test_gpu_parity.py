@@ -259,13 +259,15 @@ def test_kernels_are_launched(cuda):
 
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 4, False), (1, 2, False), (4, 4, True)])
 def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale, krylov):
-    """The TMA-fed out-of-place sweep computes the same red-black sweep as the
-    two colour launches (GBMG_TMA_LEVELS=0 switches it off at handle creation);
-    the Krylov case runs its post-smoother black-first."""
+    """The TMA-fed out-of-place sweep and defect kernels compute what the
+    two-colour launches and the plain defect kernel compute (GBMG_TMA_LEVELS=0
+    and GBMG_TMA_DEFECT=0 switch them off at handle creation); the Krylov case
+    runs its post-smoother black-first."""
     c = cases.config(idx, scale)
     out = {}
     for levels in ("0", "99"):
         monkeypatch.setenv("GBMG_TMA_LEVELS", levels)
+        monkeypatch.setenv("GBMG_TMA_DEFECT", "0" if levels == "0" else "1")
         with solver(c, precision="mixed", krylov=krylov) as s:
             s.ppe_init(c.rho)
             out[levels] = s.solve(c.b, tol=1e-10)
