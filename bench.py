@@ -66,6 +66,18 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value, device=None):
+    """Max of a float over all ranks (the job's time is its slowest rank's);
+    the value itself when not distributed."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_desc(case):
     nz, ny, nx = case.shape
     return (f"{case.name}: {nx}x{ny}x{nz} cells, {len(case.radii)} bubble(s), density ratio "
@@ -304,11 +316,7 @@ def run_ours(args):
             barrier()
             ms = e0.elapsed_time(e1)
             launches = solver.kernel_launches - launches0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         return ms, st, launches, (sampler.summary() if sample_clocks else None)
 
     with torch.cuda.stream(stream):
@@ -379,11 +387,7 @@ def run_ours(args):
             torch.cuda.synchronize()
             barrier()
             wall = (time.perf_counter() - t0) * 1e3
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([wall], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            wall = float(t.item())
+        wall = max_over_ranks(wall, dev)
         e2e = {"value": wall / args.steps / world, "unit": "ms", "h2d_bytes_per_step": 3 * 8 * n,
                "d2h_bytes_per_step": 8 * n, "timing": "host wall clock around synchronous C-ABI calls",
                "rel_residual": st_e["rel_residual"]}

@@ -66,6 +66,30 @@ __device__ __forceinline__ dw dw_from_double(double x) {
 
 __device__ __forceinline__ double dw_to_double(dw a) { return (double)a.hi + (double)a.lo; }
 
+// Accumulator of sum_f c_f (p_nb - p_c) with cascaded summation: the high
+// parts are added error-free with TwoSum, everything of order u|term| goes
+// into one float.  Absolute error O(u^2 sum |c_f (p_nb - p_c)|), the bound the
+// residual needs; about 19 FP32 operations per term instead of ~30 with the
+// normalised double-word operations.
+struct flux_acc {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add_term(dw c, dw nb, dw pc) {
+    // d = nb - pc: TwoSum of the high parts plus the low parts, unnormalised
+    const dw s = two_sum(nb.hi, -pc.hi);
+    const float dlo = s.lo + (nb.lo - pc.lo);
+    // t = c * d: TwoProd of the high parts plus the cross terms
+    const float th = c.hi * s.hi;
+    float tl = fmaf(c.hi, s.hi, -th);
+    tl = fmaf(c.hi, dlo, tl);
+    tl = fmaf(c.lo, s.hi, tl);
+    // acc += t
+    const dw a = two_sum(hi, th);
+    hi = a.hi;
+    lo += a.lo + tl;
+  }
+  __device__ __forceinline__ dw value() const { return fast_two_sum(hi, lo); }
+};
+
 __device__ __forceinline__ dw dw_load(const float2* p) {
   const float2 v = *p;
   return dw{v.x, v.y};

@@ -92,6 +92,7 @@ struct gbmg_handle {
   double prof_ms[GBMG_PROF_CLASSES] = {};
   int64_t prof_n[GBMG_PROF_CLASSES] = {};
   bool coef_ready = false;
+  bool fine_copies = false;  // finest FP32 / double-word coefficients already written
   bool rho_ready = false;
   std::string err;
 };
@@ -531,7 +532,7 @@ int build_hierarchy(gbmg_handle* h) {
   for (int l = 0; l < h->L; ++l) {
     Level& v = h->lv[l];
     if (v.idiag) LAUNCH(h, GBMG_PROF_SETUP, launch_idiag(s, v64(v), v.idiag));
-    if (v.cx32) {
+    if (v.cx32 && !(l == 0 && h->fine_copies)) {
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cx, v.cx32, v.n));
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cy, v.cy32, v.n));
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cz, v.cz32, v.n));
@@ -539,7 +540,7 @@ int build_hierarchy(gbmg_handle* h) {
   }
   LAUNCH(h, GBMG_PROF_SETUP,
          launch_coarse_invert(s, v64(h->lv[h->L - 1]), h->minv, h->adense, h->minv32, h->adense32));
-  if (h->mixed) {
+  if (h->mixed && !h->fine_copies) {
     const Level& f = h->lv[0];
     LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cx, h->cxw, f.n));
     LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cy, h->cyw, f.n));
@@ -553,9 +554,13 @@ int build_hierarchy(gbmg_handle* h) {
 int set_rho_device(gbmg_handle* h) {
   const gbmg_grid& g = h->grid;
   Level& f = h->lv[0];
+  float* c32[3] = {f.cx32, f.cy32, f.cz32};
+  float2* cw[3] = {h->cxw, h->cyw, h->czw};
   LAUNCH(h, GBMG_PROF_SETUP,
          launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
-                          h->rho, f.cx, f.cy, f.cz));
+                          h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
+                          h->mixed ? cw : nullptr));
+  h->fine_copies = h->mixed;
   GB_TRY(check_launch(h, "face_coef"));
   h->rho_ready = true;
   return build_hierarchy(h);
@@ -908,6 +913,7 @@ int gbmg_set_coef(gbmg_handle* h, gbmg_field cx, gbmg_field cy, gbmg_field cz, i
     GB_CUDA(h, cudaMemsetAsync(f.cy + (size_t)k * g.nx * g.ny, 0, (size_t)g.nx * sizeof(double),
                                h->stream));
   h->rho_ready = false;
+  h->fine_copies = false;
   GB_TRY(build_hierarchy(h));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;

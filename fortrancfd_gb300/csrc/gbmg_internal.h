@@ -99,8 +99,11 @@ void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, do
 void launch_copy_in(cudaStream_t s, int nx, int ny, int nz, Strided src, double* dst);
 void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, double* dst,
                      int64_t sy, int64_t sz);
+// c32 / cw: optional arrays of 3 pointers (x, y, z) for the FP32 and
+// double-word copies, written in the same pass.
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
-                      const double* rho, double* cx, double* cy, double* cz);
+                      const double* rho, double* cx, double* cy, double* cz, float* const* c32,
+                      float2* const* cw);
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                        double dx, double dy, double dz, double dt, double* b);
 void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,

@@ -78,12 +78,11 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
       const size_t q = (size_t)k * sz + (size_t)y * sy + x;
       const float2 c2 = ring.p[s0][ty + 1][tx + 1];
       const dw pc{c2.x, c2.y};
-      dw acc{0.f, 0.f};
+      flux_acc acc;
 #define DW_TERM(cond, cptr, nbv)                                   \
       if (cond) {                                                  \
         const float2 nb = nbv;                                     \
-        const dw d = dw_sub(dw{nb.x, nb.y}, pc);                    \
-        acc = dw_add(acc, dw_mul(dw_ldg(cptr), d));                 \
+        acc.add_term(dw_ldg(cptr), dw{nb.x, nb.y}, pc);            \
       }
       DW_TERM(x > 0, A.cx + q, ring.p[s0][ty + 1][tx])
       DW_TERM(x < A.nx - 1, A.cx + q + 1, ring.p[s0][ty + 1][tx + 2])
@@ -92,7 +91,7 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
       DW_TERM(k > 0, A.cz + q, ring.p[sm][ty + 1][tx + 1])
       DW_TERM(k < A.nz - 1, A.cz + q + sz, ring.p[sp][ty + 1][tx + 1])
 #undef DW_TERM
-      const dw r = dw_sub(dw_ldg(A.b + q), acc);
+      const dw r = dw_sub(dw_ldg(A.b + q), acc.value());
       const float rf = dw_to_float(r);
       r32[q] = rf;
       s2 = fmaf(rf, rf, s2);
@@ -193,11 +192,11 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       const float2* CX = qtile(base, s0, 2);
       const float2* CY = qtile(base, s0, 3);
       const dw pc{P[t].x, P[t].y};
-      dw acc{0.f, 0.f};
+      flux_acc acc;
 #define DWQ_TERM(cv, nbv)                                              \
       {                                                                \
         const float2 c2 = cv, n2 = nbv;                                \
-        acc = dw_add(acc, dw_mul(dw{c2.x, c2.y}, dw_sub(dw{n2.x, n2.y}, pc))); \
+        acc.add_term(dw{c2.x, c2.y}, dw{n2.x, n2.y}, pc);              \
       }
       DWQ_TERM(CX[t], P[t - 1])
       DWQ_TERM(CX[t + 1], P[t + 1])
@@ -207,7 +206,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       if (k < nz - 1) DWQ_TERM(qtile(base, sp, 4)[t], qtile(base, sp, 0)[t])
 #undef DWQ_TERM
       const float2 b2 = qtile(base, s0, 1)[t];
-      const dw r = dw_sub(dw{b2.x, b2.y}, acc);
+      const dw r = dw_sub(dw{b2.x, b2.y}, acc.value());
       const size_t q = ((size_t)k * ny + y) * nx + x;
       const float rf = dw_to_float(r);
       r32[q] = rf;

@@ -10,6 +10,7 @@
 // ns_check_convergence_div ("Two phase flows/newOpenMP/2D/src/ns_solver/
 // ns_solvers.f90:55-83").
 #include <algorithm>
+#include <cmath>
 
 #include "gbmg_internal.h"
 #include "reduce.cuh"
@@ -63,20 +64,47 @@ __global__ void __launch_bounds__(256) k_copy_out(int nx, int ny, int nz, const 
 
 // coe = 2/(rho_i + rho_nb)/h^2 on the low face of every cell, 0 on the walls
 // (the reference's arithmetic, ns_ppe_solver.f90:12-24, so the operator is
-// bit-identical to the oracle's).
-__global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, double dx2,
-                                                   double dy2, double dz2,
-                                                   const double* __restrict__ rho, double* cx,
-                                                   double* cy, double* cz) {
+// bit-identical to the oracle's).  When h^2 is a power of two the division by
+// it is an exact scaling and is done as a multiplication by 1/h^2 (same
+// result, one FP64 division instead of two).  Optionally also writes the
+// FP32 copies of the cycle and the double-word copies of the defect kernel.
+struct FaceOut {
+  double* c;
+  float* c32;
+  float2* cw;
+};
+
+__device__ __forceinline__ void face_store(const FaceOut& o, size_t q, double v) {
+  o.c[q] = v;
+  if (o.c32) o.c32[q] = (float)v;
+  if (o.cw) {
+    const float hi = __double2float_rn(v);
+    o.cw[q] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, double3 h2, double3 ih2,
+                                                   int pow2, const double* __restrict__ rho,
+                                                   FaceOut ox, FaceOut oy, FaceOut oz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
   const double r = rho[q];
-  cx[q] = i > 0 ? 2.0 / (r + rho[q - 1]) / dx2 : 0.0;
-  cy[q] = j > 0 ? 2.0 / (r + rho[q - nx]) / dy2 : 0.0;
-  cz[q] = k > 0 ? 2.0 / (r + rho[q - (size_t)nx * ny]) / dz2 : 0.0;
+  double c;
+  c = 0.0;
+  if (i > 0) { const double t = 2.0 / (r + rho[q - 1]); c = (pow2 & 1) ? t * ih2.x : t / h2.x; }
+  face_store(ox, q, c);
+  c = 0.0;
+  if (j > 0) { const double t = 2.0 / (r + rho[q - nx]); c = (pow2 & 2) ? t * ih2.y : t / h2.y; }
+  face_store(oy, q, c);
+  c = 0.0;
+  if (k > 0) {
+    const double t = 2.0 / (r + rho[q - (size_t)nx * ny]);
+    c = (pow2 & 4) ? t * ih2.z : t / h2.z;
+  }
+  face_store(oz, q, c);
 }
 
 // b = div(u)/dt with MAC faces: u(f,j,k) on the x-face at f*dx, f = 0..nx.
@@ -264,9 +292,21 @@ void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, 
   k_copy_out<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, src, dst, sy, sz);
 }
 
+static bool is_pow2(double v) {
+  int e;
+  return v > 0.0 && std::frexp(v, &e) == 0.5;
+}
+
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
-                      const double* rho, double* cx, double* cy, double* cz) {
-  k_face_coef<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, dx2, dy2, dz2, rho, cx, cy, cz);
+                      const double* rho, double* cx, double* cy, double* cz, float* const* c32,
+                      float2* const* cw) {
+  const int pow2 = (is_pow2(dx2) ? 1 : 0) | (is_pow2(dy2) ? 2 : 0) | (is_pow2(dz2) ? 4 : 0);
+  const FaceOut ox{cx, c32 ? c32[0] : nullptr, cw ? cw[0] : nullptr};
+  const FaceOut oy{cy, c32 ? c32[1] : nullptr, cw ? cw[1] : nullptr};
+  const FaceOut oz{cz, c32 ? c32[2] : nullptr, cw ? cw[2] : nullptr};
+  k_face_coef<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
+      nx, ny, nz, make_double3(dx2, dy2, dz2), make_double3(1.0 / dx2, 1.0 / dy2, 1.0 / dz2), pow2,
+      rho, ox, oy, oz);
 }
 
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,

@@ -199,26 +199,26 @@ __global__ void __launch_bounds__(kMaxCoarse) k_coarse_solve(int n, const T* __r
 }
 
 // Coarsest-level operator and its inverse, one block, FP64.  The dense
-// Neumann matrix A is singular (constant null space); M = A - s 11^T/n with s
-// the mean diagonal is not, and M^{-1} b is the mean-free solution for a
-// mean-free b.  Gauss-Jordan with partial pivoting in shared memory.  The
-// reference LU-factors the singular matrix with LAPACK dgesv instead
-// ("DomainDecomposition/3D/lib/data/tree_multigrid.f90:134-173").
+// Neumann matrix A is singular (constant null space) and negative
+// semi-definite; M = s 11^T/n - A (s = mean diagonal) is symmetric positive
+// definite, and -M^{-1} b is the mean-free solution of A x = b for a
+// mean-free b.  M = L L^T by Cholesky in shared memory, W = L^{-1} column by
+// column, M^{-1} = W^T W: about n^3/2 multiply-adds instead of Gauss-Jordan's
+// 2n^3.  The reference LU-factors the singular matrix with LAPACK dgesv
+// instead ("DomainDecomposition/3D/lib/data/tree_multigrid.f90:134-173").
 __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, double* minv,
                                                        double* adense, float* minv32,
                                                        float* adense32) {
   extern __shared__ double smem[];
   const int n = C.nx * C.ny * C.nz;
-  const int w = 2 * n;
-  double* M = smem;                  // n x 2n augmented matrix
-  double* f = smem + (size_t)n * w;  // column factors
+  double* M = smem;                   // n x n, becomes L (lower triangle)
+  double* W = smem + (size_t)n * n;   // n x n, becomes L^{-1} (lower triangle)
   __shared__ double dsum_sh;
-  __shared__ int piv_sh;
   const int t = threadIdx.x, nt = blockDim.x;
   for (int e = t; e < n * n; e += nt) adense[e] = 0.0;
   __syncthreads();
   if (t == 0) {
-    // assemble in the oracle's order (serial, n <= 64)
+    // assemble A in the oracle's order (serial, n <= 64)
     double dsum = 0.0;
     for (int k = 0; k < C.nz; ++k)
       for (int j = 0; j < C.ny; ++j)
@@ -239,48 +239,43 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
     dsum_sh = s;
   }
   __syncthreads();
-  const double s = dsum_sh;
-  for (int e = t; e < n * w; e += nt) {
-    const int r = e / w, q = e % w;
-    M[e] = q < n ? adense[r * n + q] - s / n : (q - n == r ? 1.0 : 0.0);
+  const double sn = dsum_sh / n;
+  for (int e = t; e < n * n; e += nt) {
+    M[e] = sn - adense[e];
+    W[e] = 0.0;
   }
   __syncthreads();
-  for (int col = 0; col < n; ++col) {
-    if (t == 0) {
-      int piv = col;
-      double best = fabs(M[col * w + col]);
-      for (int r = col + 1; r < n; ++r) {
-        const double v = fabs(M[r * w + col]);
-        if (v > best) { best = v; piv = r; }
-      }
-      piv_sh = piv;
-    }
+  // right-looking Cholesky, lower triangle in place
+  for (int j = 0; j < n; ++j) {
+    if (t == 0) M[j * n + j] = sqrt(M[j * n + j]);
     __syncthreads();
-    const int piv = piv_sh;
-    if (piv != col)
-      for (int q = t; q < w; q += nt) {
-        const double tmp = M[col * w + q];
-        M[col * w + q] = M[piv * w + q];
-        M[piv * w + q] = tmp;
-      }
+    const double djj = M[j * n + j];
+    for (int i = j + 1 + t; i < n; i += nt) M[i * n + j] /= djj;
     __syncthreads();
-    const double inv = 1.0 / M[col * w + col];
-    __syncthreads();
-    for (int q = t; q < w; q += nt) M[col * w + q] *= inv;
-    __syncthreads();
-    for (int r = t; r < n; r += nt) f[r] = M[r * w + col];
-    __syncthreads();
-    for (int e = t; e < n * w; e += nt) {
-      const int r = e / w, q = e % w;
-      if (r != col) M[e] -= f[r] * M[col * w + q];
+    const int m = n - j - 1;  // trailing block (j+1..n-1)^2, lower part
+    for (int e = t; e < m * m; e += nt) {
+      const int i = j + 1 + e / m, k = j + 1 + e % m;
+      if (k <= i) M[i * n + k] -= M[i * n + j] * M[k * n + j];
     }
     __syncthreads();
   }
+  // W = L^{-1}: forward substitution, one column per thread
+  for (int c = t; c < n; c += nt) {
+    W[c * n + c] = 1.0 / M[c * n + c];
+    for (int i = c + 1; i < n; ++i) {
+      double acc = 0.0;
+      for (int k = c; k < i; ++k) acc += M[i * n + k] * W[k * n + c];
+      W[i * n + c] = -acc / M[i * n + i];
+    }
+  }
+  __syncthreads();
+  // (A - s 11^T/n)^{-1} = -M^{-1} = -W^T W
   for (int e = t; e < n * n; e += nt) {
     const int r = e / n, q = e % n;
-    const double v = M[r * w + n + q];
-    minv[e] = v;
-    if (minv32) minv32[e] = (float)v;
+    double acc = 0.0;
+    for (int k = max(r, q); k < n; ++k) acc += W[k * n + r] * W[k * n + q];
+    minv[e] = -acc;
+    if (minv32) minv32[e] = (float)(-acc);
     if (adense32) adense32[e] = (float)adense[e];
   }
 }
@@ -400,7 +395,7 @@ void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, 
 void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
                           double* adense, float* minv32, float* adense32) {
   const int n = C.nx * C.ny * C.nz;
-  const size_t shm = ((size_t)n * 2 * n + n) * sizeof(double);
+  const size_t shm = (size_t)2 * n * n * sizeof(double);
   cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   k_coarse_invert<<<1, 256, shm, s>>>(C, minv, adense, minv32, adense32);
 }
