@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -261,6 +262,66 @@ def cpu_baseline(case, phi, u, v, w, budget_s):
                       f"{threads} threads, {st['cycles']} cycles each (oracle restatement)"}
 
 
+def adjoint_section(dev, stream, reps=5, scale=1):
+    """The differentiable solve on the 1024^2 eight-circle case: forward
+    (operator from phi + mixed-precision solve) and backward (operator rebuild,
+    adjoint solve, adjoint kernel) device times, and central differences of
+    J = |p - p_t|^2/2 with FP64 solves (step 1e-6, 4 random unit directions of
+    phi) against the mixed-precision gradient."""
+    import torch
+
+    from fortrancfd_gb300 import PressurePoisson, inputs
+    from fortrancfd_gb300.autograd import pressure_solve
+
+    case = inputs.config(3, scale)
+    kw = dict(eps=case.eps, rho_pos=case.rho_pos, rho_neg=case.rho_neg)
+    phi = torch.from_numpy(inputs.level_set(case)).to(dev)
+    with torch.cuda.stream(stream):
+        s = PressurePoisson(case.shape, case.spacing, precision="mixed", krylov=True,
+                            max_cycles=400, stream=stream)
+        s64 = PressurePoisson(case.shape, case.spacing, krylov=True, max_cycles=600, stream=stream)
+        tv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        b = s.divergence(*[tv(a) for a in inputs.velocity(case)], case.dt)
+        bt = s.divergence(*[tv(a) for a in inputs.velocity(case, seed=case.extra["target_seed"])],
+                          case.dt)
+        p_t = pressure_solve(phi, bt, s, tol=1e-10, **kw).detach()
+        fw, bw = [], []
+        for it in range(reps + 1):
+            x = phi.clone().requires_grad_(True)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            p = pressure_solve(x, b, s, tol=1e-10, **kw)
+            e1.record(stream)
+            loss = 0.5 * ((p - p_t) ** 2).sum()
+            loss.backward()
+            e2.record(stream)
+            torch.cuda.synchronize()
+            if it:
+                fw.append(e0.elapsed_time(e1))
+                bw.append(e1.elapsed_time(e2))
+        g = x.grad
+
+        def J(ph):
+            q = pressure_solve(ph, b, s64, tol=1e-14, **kw)
+            return 0.5 * ((q - p_t) ** 2).sum()
+
+        rng = np.random.default_rng(7)
+        errs = []
+        with torch.no_grad():
+            for _ in range(4):
+                v = torch.from_numpy(rng.standard_normal(case.shape)).to(dev)
+                v /= v.norm()
+                fd = float((J(phi + 1e-6 * v) - J(phi - 1e-6 * v)) / 2e-6)
+                errs.append(abs(fd - float((g * v).sum())) / abs(fd))
+        s.close()
+        s64.close()
+    f, bk = float(np.median(fw)), float(np.median(bw))
+    return {"workload": f"{case.name}: {case.shape[2]}x{case.shape[1]} cells, 8 circles, mixed "
+                        "precision, flexible CG, tol 1e-10",
+            "forward_ms": f, "backward_ms": bk, "backward_over_forward": bk / f,
+            "fd_max_rel_err": max(errs), "fd_directions": len(errs)}
+
+
 def run_ours(args):
     import torch
 
@@ -392,6 +453,10 @@ def run_ours(args):
                "d2h_bytes_per_step": 8 * n, "timing": "host wall clock around synchronous C-ABI calls",
                "rel_residual": st_e["rel_residual"]}
 
+    adj = None
+    if not args.no_adjoint:
+        adj = adjoint_section(dev, stream, scale=max(1, args.scale))
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
@@ -413,7 +478,7 @@ def run_ours(args):
                                  "each FP64 field alone exceeds it",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches}
+                "gpu_launches": launches, "adjoint": adj}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
         print(json.dumps(line), flush=True)

@@ -29,7 +29,7 @@ EXPORTS = (
     "gbmg_default_params", "gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
     "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence", "gbmg_residual",
     "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims", "gbmg_kernel_launches",
-    "gbmg_strerror", "gbmg_last_error", "gbmg_set_profiling", "gbmg_profile",
+    "gbmg_strerror", "gbmg_last_error", "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -107,11 +107,13 @@ def load(build_if_missing: bool = True):
         L.gbmg_last_error.argtypes = [H]
         L.gbmg_last_error.restype = C.c_char_p
         L.gbmg_set_profiling.argtypes = [H, C.c_int]
+        L.gbmg_adjoint.argtypes = [H, Field, Field, Field, C.c_double, C.c_double, C.c_double,
+                                   Field, Field, C.c_int]
         L.gbmg_profile.argtypes = [H, P(C.c_double), P(C.c_int64), C.c_int32]
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",
                      "gbmg_residual", "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims",
-                     "gbmg_set_profiling", "gbmg_profile"):
+                     "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint"):
             getattr(L, name).restype = C.c_int
         _lib = L
         return _lib

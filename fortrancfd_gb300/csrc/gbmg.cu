@@ -62,6 +62,7 @@ struct gbmg_handle {
   double* rho = nullptr;  // cell density of the current operator
   double* vel[3] = {nullptr, nullptr, nullptr};
   size_t vel_n[3] = {0, 0, 0};
+  double* aux[2] = {nullptr, nullptr};  // adjoint outputs / staging, allocated on first use
   // flexible CG vectors (allocated when krylov = 1)
   double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
   // coarsest level
@@ -334,6 +335,7 @@ int free_all(gbmg_handle* h) {
   dfree(h->b); dfree(h->p); dfree(h->rho);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
+  dfree(h->aux[0]); dfree(h->aux[1]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
   dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   delete[] h->dmaps;
@@ -1110,6 +1112,47 @@ int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, dou
   GB_TRY(read_result(h, kSlotSum, &sum));
   if (max_div) *max_div = h->host_res[kSlotMax];
   if (mean_div) *mean_div = sum / (double)h->n0;
+  return GBMG_OK;
+}
+
+int gbmg_adjoint(gbmg_handle* h, gbmg_field p, gbmg_field lam, gbmg_field phi, double eps,
+                 double rho_pos, double rho_neg, gbmg_field grad_rho, gbmg_field grad_phi,
+                 int mem) {
+  GB_TRY(begin(h));
+  if (!h->rho_ready) { h->err = "the adjoint needs the density: call gbmg_set_rho/phi first"; return GBMG_STATE_ERROR; }
+  GB_TRY(validate_field(h, p, "p"));
+  GB_TRY(validate_field(h, lam, "lam"));
+  GB_TRY(validate_field(h, grad_rho, "grad_rho"));
+  const bool want_phi = phi.data != nullptr;
+  if (want_phi) {
+    GB_TRY(validate_field(h, grad_phi, "grad_phi"));
+    if (!(eps > 0)) { h->err = "eps must be > 0"; return GBMG_INVALID_ARG; }
+  }
+  const gbmg_grid& g = h->grid;
+  for (int a = 0; a < 2; ++a)
+    if (!h->aux[a]) GB_TRY(dmalloc(h, &h->aux[a], h->n0));
+  // p -> h->p, lam -> h->b (both staging copies), phi -> aux[1] if in host memory
+  GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  GB_TRY(upload(h, lam, g.nx, g.ny, g.nz, mem, h->b));
+  Strided sp{nullptr, 0, 0};
+  if (want_phi) {
+    if (mem == GBMG_MEM_HOST) {
+      GB_TRY(upload(h, phi, g.nx, g.ny, g.nz, mem, h->aux[1]));
+      sp = Strided{h->aux[1], g.nx, (int64_t)g.nx * g.ny};
+    } else {
+      sp = Strided{phi.data, phi.sy, phi.sz};
+    }
+  }
+  double* gphi = want_phi ? h->aux[1] : nullptr;
+  // when phi lives in aux[1] (host input), the kernel reads and writes the same
+  // cell only, so grad_phi may overwrite it in place
+  LAUNCH(h, GBMG_PROF_VECTOR,
+         launch_adjoint(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz, h->rho,
+                        h->p, h->b, sp, eps, rho_pos, rho_neg, h->aux[0], gphi));
+  GB_TRY(check_launch(h, "adjoint"));
+  GB_TRY(download(h, h->aux[0], g.nx, g.ny, g.nz, mem, grad_rho));
+  if (want_phi) GB_TRY(download(h, h->aux[1], g.nx, g.ny, g.nz, mem, grad_phi));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
 }
 

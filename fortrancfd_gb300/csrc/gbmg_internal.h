@@ -110,6 +110,10 @@ void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, c
                     double dx, double dy, double dz, double dt, double* u, int64_t usy,
                     int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w, int64_t wsy,
                     int64_t wsz);
+// dJ/drho (and dJ/dphi when grad_phi != nullptr) from p and the adjoint lam.
+void launch_adjoint(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
+                    const double* rho, const double* p, const double* lam, Strided phi,
+                    double eps, double rpos, double rneg, double* grad_rho, double* grad_phi);
 void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                       double dx, double dy, double dz, const ReduceScratch& R);
 // slot <- sum x, slot+1 <- sum x^2

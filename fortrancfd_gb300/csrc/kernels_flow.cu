@@ -156,6 +156,44 @@ __global__ void __launch_bounds__(256) k_correct(int nx, int ny, int nz,
   }
 }
 
+// Adjoint of the solve with respect to the density (and the level set):
+// dJ/drho_i = sum over the faces of cell i of (lam_nb - lam_i)(p_nb - p_i)
+// * (-2/(rho_i + rho_nb)^2/h^2); with phi, dJ/dphi = dJ/drho (rho_pos -
+// rho_neg) H'(phi), H' = (1 + cos(pi phi/eps))/(2 eps) inside the band.
+__global__ void __launch_bounds__(256) k_adjoint(int nx, int ny, int nz, double3 h2,
+                                                 const double* __restrict__ rho,
+                                                 const double* __restrict__ p,
+                                                 const double* __restrict__ lam, Strided phi,
+                                                 double eps, double rpos, double rneg,
+                                                 double* grad_rho, double* grad_phi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= nx || j >= ny) return;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const size_t q = (size_t)k * sz + (size_t)j * sy + i;
+  const bool has[6] = {i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1};
+  const long long off[6] = {-1, 1, -(long long)sy, (long long)sy, -(long long)sz, (long long)sz};
+  const double hh[3] = {h2.x, h2.y, h2.z};
+  double acc = 0.0;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    if (!has[f]) continue;
+    const size_t n = (size_t)((long long)q + off[f]);
+    const double s = rho[q] + rho[n];
+    const double dcoe = -2.0 / (s * s) / hh[f / 2];
+    acc += (lam[n] - lam[q]) * (p[n] - p[q]) * dcoe;
+  }
+  grad_rho[q] = acc;
+  if (grad_phi) {
+    const double pi = 3.141592653589793;
+    const double x = phi.data[i + j * phi.sy + k * phi.sz] / eps;
+    const double hp =
+        (x > 1.0 - 1e-12 || x < -1.0 + 1e-12) ? 0.0 : 0.5 * (1.0 + cos(pi * x)) / eps;
+    grad_phi[q] = acc * (rpos - rneg) * hp;
+  }
+}
+
 // max |div u| by atomicMax on the bit pattern (non-negative doubles order as
 // unsigned integers) and sum |div u| through the deterministic reducer.
 __global__ void __launch_bounds__(kRedThreads) k_div_stats(int nx, int ny, int nz, Strided u,
@@ -320,6 +358,14 @@ void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, c
                     int64_t wsz) {
   k_correct<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, rho, p, dx, dy, dz, dt, u, usy,
                                                      usz, v, vsy, vsz, w, wsy, wsz);
+}
+
+void launch_adjoint(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
+                    const double* rho, const double* p, const double* lam, Strided phi,
+                    double eps, double rpos, double rneg, double* grad_rho, double* grad_phi) {
+  k_adjoint<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, make_double3(dx2, dy2, dz2), rho,
+                                                     p, lam, phi, eps, rpos, rneg, grad_rho,
+                                                     grad_phi);
 }
 
 void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,

@@ -232,6 +232,29 @@ class PressurePoisson:
             return
         self._check(rc, what)
 
+    def adjoint(self, p, lam, phi=None, eps=1.0, rho_pos=1.0, rho_neg=1e-3):
+        """dJ/drho (and dJ/dphi when phi is given) from the solution p and the
+        adjoint lam of A lam = dJ/dp, for the current density.  Returns
+        (grad_rho, grad_phi or None)."""
+        fp, m1 = _field(p, self.shape)
+        fl, m2 = _field(lam, self.shape)
+        like = (lambda: torch.empty_like(p)) if _is_torch(p) else (lambda: np.empty(self.shape))
+        grad_rho = like()
+        fr, _ = _field(grad_rho, self.shape)
+        grad_phi = None
+        fphi, fgp = _lib.Field(None, 0, 0), _lib.Field(None, 0, 0)
+        pairs = [(fp, m1), (fl, m2)]
+        if phi is not None:
+            grad_phi = like()
+            fphi, m3 = _field(phi, self.shape)
+            fgp, _ = _field(grad_phi, self.shape)
+            pairs.append((fphi, m3))
+        m = _mem_of(*pairs)
+        self._sync_torch(p, lam, phi)
+        self._check(self._L.gbmg_adjoint(self._h, fp, fl, fphi, float(eps), float(rho_pos),
+                                         float(rho_neg), fr, fgp, m), "adjoint")
+        return grad_rho, grad_phi
+
     # -- diagnostics ------------------------------------------------------------
     def divergence(self, u, v, w, dt, out=None):
         su, sv, sw = self._faces()

@@ -156,6 +156,17 @@ int gbmg_residual(gbmg_handle* h, gbmg_field b, gbmg_field p, gbmg_field r, doub
 int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double* max_div,
                    double* mean_div, int mem);
 
+/* Adjoint of the solve (no reference counterpart: the differentiable
+ * projection of this library).  Given the solution p of A p = b and the
+ * adjoint lam of A lam = dJ/dp (both from gbmg_solve with the current
+ * operator), writes dJ/drho_i = sum over the faces of cell i of
+ * (lam_nb - lam_i)(p_nb - p_i) * (-2/(rho_i + rho_nb)^2/h^2) into grad_rho,
+ * and, when phi.data is not NULL, dJ/dphi = dJ/drho (rho_pos - rho_neg) H'(phi)
+ * into grad_phi.  dJ/db is lam itself.  Uses the density of the last
+ * gbmg_set_rho / gbmg_set_phi. */
+int gbmg_adjoint(gbmg_handle* h, gbmg_field p, gbmg_field lam, gbmg_field phi, double eps,
+                 double rho_pos, double rho_neg, gbmg_field grad_rho, gbmg_field grad_phi, int mem);
+
 /* Copies level `level`'s face coefficients (FP64) into cell-shaped arrays of
  * that level's size (gbmg_level_dims).  For tests of the coarsening rule. */
 int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,

@@ -864,6 +864,48 @@ int or_mg_level_coef(const or_grid* g, const double* cx, const double* cy, const
   return OR_OK;
 }
 
+/* ------------------------------------------------------------------------- */
+/* Adjoint of the solve (no reference counterpart; the FP64 host reference of  */
+/* the differentiable solve).  With (A p)_i = sum_f coe_f (p_nb - p_i) and the */
+/* adjoint lam solving A lam = dJ/dp (mean-free):                              */
+/*   dJ/dcoe_f   = (lam_nb - lam_i)(p_nb - p_i)                                */
+/*   dcoe_f/drho = -2/(rho_i + rho_nb)^2/h^2 for both cells of the face        */
+/*   dJ/drho_i   = sum over the faces of cell i of the two products            */
+/* and through rho = rho_pos H(phi/eps) + rho_neg (1 - H):                      */
+/*   dJ/dphi_i   = dJ/drho_i (rho_pos - rho_neg) H'(phi_i)                      */
+/* phi may be NULL (grad_phi then not written).                                */
+/* ------------------------------------------------------------------------- */
+void or_adjoint(const or_grid* g, const double* rho, const double* p, const double* lam,
+                const double* phi, double eps, double rho_pos, double rho_neg, double* grad_rho,
+                double* grad_phi) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t sy = nx, sz = (size_t)nx * ny;
+  const double h2[3] = {g->dx * g->dx, g->dy * g->dy, g->dz * g->dz};
+  const double pi = acos(-1.0);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t q = (size_t)k * sz + (size_t)j * sy + i;
+        double acc = 0.0;
+        const int has[6] = {i > 0, i < nx - 1, j > 0, j < ny - 1, k > 0, k < nz - 1};
+        const long off[6] = {-1, 1, -(long)sy, (long)sy, -(long)sz, (long)sz};
+        for (int f = 0; f < 6; ++f) {
+          if (!has[f]) continue;
+          const size_t n = (size_t)((long)q + off[f]);
+          const double s = rho[q] + rho[n];
+          const double dcoe = -2.0 / (s * s) / h2[f / 2];
+          acc += (lam[n] - lam[q]) * (p[n] - p[q]) * dcoe;
+        }
+        grad_rho[q] = acc;
+        if (phi && grad_phi) {
+          const double x = phi[q] / eps;
+          const double hp = (x > 1.0 - 1e-12 || x < -1.0 + 1e-12) ? 0.0 : 0.5 * (1.0 + cos(pi * x)) / eps;
+          grad_phi[q] = acc * (rho_pos - rho_neg) * hp;
+        }
+      }
+}
+
 int or_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -68,6 +68,8 @@ def lib():
         L.or_mg_level_coef.argtypes = [C.POINTER(Grid), _D, _D, _D, C.POINTER(MGParams), C.c_int,
                                        _D, _D, _D]
         L.or_mg_level_coef.restype = C.c_int
+        L.or_adjoint.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, C.c_double, C.c_double,
+                                 C.c_double, _D, _D]
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -211,6 +213,17 @@ def mg_level_coef(coef, level, **kw):
                                 *(_p(a) for a in out))
     assert rc == 0
     return out
+
+
+def adjoint(rho, p, lam, spacing, phi=None, eps=1.0, rho_pos=1.0, rho_neg=1.0):
+    """(dJ/drho, dJ/dphi or None) from the solution p and the adjoint lam."""
+    g = grid(p.shape, spacing)
+    grad_rho = np.empty_like(p)
+    grad_phi = np.empty_like(p) if phi is not None else None
+    ph = np.ascontiguousarray(phi, np.float64) if phi is not None else None
+    lib().or_adjoint(C.byref(g), _p(rho), _p(p), _p(lam), _p(ph), eps, rho_pos, rho_neg,
+                     _p(grad_rho), _p(grad_phi))
+    return grad_rho, grad_phi
 
 
 def set_threads(n):
