@@ -228,22 +228,27 @@ template <> const float* adense_of<float>(const gbmg_handle* h) { return h->aden
 // FP32: one fused launch out of place, after which the level's solution lives
 // in the other buffer (the host swaps the pointers; graph capture records the
 // resulting sequence, which replays identically).
+// zero_guess: the level's values are taken as zero (its first sweep after the
+// coarse unknown was started at zero, or the finest level of a correction
+// cycle), so no memset is needed and the first colour does not read p.
 template <typename T>
-void sweep(gbmg_handle* h, int l, int first_color);
+void sweep(gbmg_handle* h, int l, int first_color, bool zero_guess);
 
 template <>
-void sweep<double>(gbmg_handle* h, int l, int first_color) {
+void sweep<double>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   const LevelView<double> V = v64(h->lv[l]);
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-  LAUNCH(h, cs, launch_smooth<double>(h->stream, V, first_color));
+  LAUNCH(h, cs, launch_smooth<double>(h->stream, V, first_color, zero_guess));
   LAUNCH(h, cs, launch_smooth<double>(h->stream, V, 1 - first_color));
 }
 
 template <>
-void sweep<float>(gbmg_handle* h, int l, int first_color) {
+void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   Level& lv = h->lv[l];
   const LevelView<float> V = v32(lv);
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
+  if (zero_guess && (lv.tmaps || h->fused_levels > l))  // out-of-place sweeps read p
+    cudaMemsetAsync(lv.sol32, 0, lv.n * sizeof(float), h->stream);
   if (lv.tmaps) {
     const SweepMaps& m = lv.tmaps[lv.sol32 == lv.buf_a ? 0 : 1];
     LAUNCH(h, cs, launch_smooth_tma(h->stream, m, lv.nx, lv.ny, lv.nz, lv.alt32, first_color, h->derr));
@@ -252,21 +257,25 @@ void sweep<float>(gbmg_handle* h, int l, int first_color) {
     LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
     std::swap(lv.sol32, lv.alt32);
   } else {
-    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, first_color));
+    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, first_color, zero_guess));
     LAUNCH(h, cs, launch_smooth<float>(h->stream, V, 1 - first_color));
   }
 }
 
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
 // the post-smoothing colours black-first (symmetric preconditioner for CG).
+// zero_fine: the level-0 unknown starts at zero (correction and Krylov
+// cycles); requires nu1 > 0, otherwise the caller zeroes it.
 template <typename T>
-int enqueue_vcycle(gbmg_handle* h, bool reverse_post) {
+int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
   const int L = h->L;
   const cudaStream_t s = h->stream;
+  const bool pre = h->prm.nu1 > 0;
   for (int l = 0; l < L - 1; ++l) {
-    for (int it = 0; it < h->prm.nu1; ++it) sweep<T>(h, l, 0);
+    for (int it = 0; it < h->prm.nu1; ++it)
+      sweep<T>(h, l, 0, it == 0 && (l > 0 || zero_fine));
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
-           launch_restrict<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
+           launch_restrict<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
   }
   const Level& c = h->lv[L - 1];
   const LevelView<T> C = view<T>(c);
@@ -275,7 +284,7 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post) {
   for (int l = L - 2; l >= 0; --l) {
     LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
            launch_prolong<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
-    for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0);
+    for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0, false);
   }
   return check_launch(h, "v-cycle");
 }
@@ -605,25 +614,26 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
   Level& f = h->lv[0];
   const size_t n = h->n0;
   const int V = GBMG_PROF_VECTOR, R = GBMG_PROF_RESIDUAL;
+  const bool zg = h->prm.nu1 > 0;  // zero initial guess handled by the first sweep
   if (kind == kGraphFp64) {
     f.sol = h->p; f.src = h->b;
-    GB_TRY(enqueue_vcycle<double>(h, false));
+    GB_TRY(enqueue_vcycle<double>(h, false, false));
     LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
   } else if (kind == kGraphMixed) {
     // e = V-cycle(r) in FP32; p += e and r = b - A p in double-word
-    GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
-    GB_TRY(enqueue_vcycle<float>(h, false));
+    if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
+    GB_TRY(enqueue_vcycle<float>(h, false, zg));
     LAUNCH(h, R, enqueue_defect(h, h->pcur, f.sol32, f.src32, kSlotNorm));
   } else {
     // flexible CG: z = M r (one V-cycle from zero), mean-free
     if (kind == kGraphPcg64) {
-      GB_CUDA(h, cudaMemsetAsync(h->kz, 0, n * sizeof(double), s));
+      if (!zg) GB_CUDA(h, cudaMemsetAsync(h->kz, 0, n * sizeof(double), s));
       f.sol = h->kz; f.src = h->kr;
-      GB_TRY(enqueue_vcycle<double>(h, true));
+      GB_TRY(enqueue_vcycle<double>(h, true, zg));
     } else {
       LAUNCH(h, V, launch_double_to_float(s, h->kr, f.src32, n));
-      GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
-      GB_TRY(enqueue_vcycle<float>(h, true));
+      if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
+      GB_TRY(enqueue_vcycle<float>(h, true, zg));
       LAUNCH(h, V, launch_float_to_double(s, f.sol32, h->kz, n));
     }
     LAUNCH(h, V, launch_sum(s, h->kz, n, h->red, kSlotSum));

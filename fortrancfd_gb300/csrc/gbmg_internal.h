@@ -54,8 +54,10 @@ enum : int {
 };
 
 // ---- launchers (kernels_mg.cu) ---------------------------------------------
+// zero_guess: the level's current values are taken as zero (first colour of
+// the first sweep after the coarse unknown was started at zero)
 template <typename T>
-void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color);
+void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_guess = false);
 // TMA descriptors of one FP32 level for the TMA-fed sweep (smooth_tma.cu).
 struct SweepMaps {
   CUtensorMap p, b, cx, cy, cz;
@@ -72,8 +74,10 @@ void launch_smooth_tma(cudaStream_t s, const SweepMaps& maps, int nx, int ny, in
 template <typename T>
 void launch_smooth_fused(cudaStream_t s, const LevelView<T>& L, const T* pin, T* pout,
                          int first_color);
+// zero_sol: also set the coarse unknown to zero (not needed when its first
+// sweep starts from a zero guess)
 template <typename T>
-void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
+void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, bool zero_sol);
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
 // r = src - A sol on a level; writes r (type TO, may be null) and sum r^2 into slot.

@@ -20,6 +20,7 @@
 
 #include "dword.cuh"
 #include "gbmg_internal.h"
+#include "pdl.cuh"
 #include "reduce.cuh"
 #include "tma.cuh"
 
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
                                                         const float* __restrict__ e,
                                                         float* __restrict__ r32, ReduceScratch R,
                                                         int slot) {
+  pdl_enter();
   __shared__ DefectRing ring;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
   const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
     k_defect_tma(const __grid_constant__ DefectMaps maps, int nx, int ny, int nz, int use_e,
                  float2* __restrict__ pout, float* __restrict__ r32, ReduceScratch R, int slot,
                  int* err) {
+  pdl_enter();
   extern __shared__ unsigned char dsm_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(dsm_raw) + 127) & ~uintptr_t(127));
@@ -260,7 +263,8 @@ dim3 defect_grid(int nx, int ny, int nz) {
 
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
                    const float* e, float* r32, const ReduceScratch& R, int slot) {
-  k_defect<<<defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s>>>(A, pin, pout, e, r32, R, slot);
+  launch_pdl(k_defect, defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s, A, pin, pout, e,
+             r32, R, slot);
 }
 
 bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
@@ -287,8 +291,8 @@ int defect_tma_init() {
 
 void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err) {
-  k_defect_tma<<<defect_grid(nx, ny, nz), dim3(kDTX, kDTY), kQSmem, s>>>(
-      maps, nx, ny, nz, use_e ? 1 : 0, pout, r32, R, slot, err);
+  launch_pdl(k_defect_tma, defect_grid(nx, ny, nz), dim3(kDTX, kDTY), kQSmem, s, maps, nx, ny, nz,
+             use_e ? 1 : 0, pout, r32, R, slot, err);
 }
 
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {

@@ -13,6 +13,7 @@
 #include <cstdio>
 
 #include "gbmg_internal.h"
+#include "pdl.cuh"
 #include "reduce.cuh"
 
 namespace gbmg {
@@ -41,8 +42,11 @@ __device__ __forceinline__ void stencil(const LevelView<T>& L, const T* __restri
 // One colour of a red-black Gauss-Seidel sweep: cells with (i+j+k)%2 == color
 // get p_i = (s - b_i)/d (the reference's p_i = (src - sum coe p_nb)/c with
 // c = -d).  One thread per cell of the colour.
-template <typename T, bool kIdiag>
+// kZero: the level's current values are taken as zero (the first colour of
+// the first sweep from a zero initial guess), so p_i = -b_i/d and p is not read.
+template <typename T, bool kIdiag, bool kZero>
 __global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
+  pdl_enter();
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (j >= L.ny) return;
@@ -50,66 +54,145 @@ __global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
   if (i >= L.nx) return;
   const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
   T s, d;
-  stencil(L, L.sol, i, j, k, q, s, d);
+  if (kZero) {
+    const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+    s = T(0);
+    d = T(0);
+    if (i > 0) d += L.cx[q];
+    if (i < L.nx - 1) d += L.cx[q + 1];
+    if (j > 0) d += L.cy[q];
+    if (j < L.ny - 1) d += L.cy[q + sy];
+    if (k > 0) d += L.cz[q];
+    if (k < L.nz - 1) d += L.cz[q + sz];
+  } else {
+    stencil(L, L.sol, i, j, k, q, s, d);
+  }
   const T v = s - L.src[q];
   if (kIdiag) L.sol[q] = v * L.idiag[q];
   else L.sol[q] = v / d;
 }
 
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
 // Fused residual + restriction: coarse src = mean over the children of
-// (src - A sol) on the fine level; coarse sol = 0.  One thread per coarse cell.
+// (src - A sol) on the fine level; coarse sol = 0.  One thread per coarse
+// cell; the children are summed in the order z, y, x (the oracle's).
 template <typename T>
-__global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C) {
+__global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C, int zero_sol) {
+  pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int K = blockIdx.z;
   if (I >= C.nx || J >= C.ny) return;
   T acc = T(0);
-  for (int dz = 0; dz < F.fz; ++dz)
-    for (int dy = 0; dy < F.fy; ++dy)
-      for (int dx = 0; dx < F.fx; ++dx) {
-        const int i = F.fx * I + dx, j = F.fy * J + dy, k = F.fz * K + dz;
-        const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
-        T s, d;
-        stencil(F, F.sol, i, j, k, q, s, d);
-        acc += F.src[q] - (s - d * F.sol[q]);
+  if (F.fx == 2) {
+    // the two x-children of each child row as vector loads
+    using V2 = typename Vec2<T>::type;
+    const size_t sy = (size_t)F.nx, sz = (size_t)F.nx * F.ny;
+    const int i0 = 2 * I;
+    const V2 zero2{T(0), T(0)};
+    for (int dz = 0; dz < F.fz; ++dz)
+      for (int dy = 0; dy < F.fy; ++dy) {
+        const int j = F.fy * J + dy, k = F.fz * K + dz;
+        const size_t q = ((size_t)k * F.ny + j) * F.nx + i0;
+        const V2 p = *reinterpret_cast<const V2*>(F.sol + q);
+        const V2 b = *reinterpret_cast<const V2*>(F.src + q);
+        const V2 cxp = *reinterpret_cast<const V2*>(F.cx + q);
+        const bool xl = i0 > 0, xr = i0 + 2 < F.nx;
+        const bool yl = j > 0, yr = j < F.ny - 1, zl = k > 0, zr = k < F.nz - 1;
+        const T pl = xl ? F.sol[q - 1] : T(0), pr = xr ? F.sol[q + 2] : T(0);
+        const T cxr = xr ? F.cx[q + 2] : T(0);
+        const V2 pym = yl ? *reinterpret_cast<const V2*>(F.sol + q - sy) : zero2;
+        const V2 pyp = yr ? *reinterpret_cast<const V2*>(F.sol + q + sy) : zero2;
+        const V2 pzm = zl ? *reinterpret_cast<const V2*>(F.sol + q - sz) : zero2;
+        const V2 pzp = zr ? *reinterpret_cast<const V2*>(F.sol + q + sz) : zero2;
+        const V2 cym = *reinterpret_cast<const V2*>(F.cy + q);
+        const V2 cyp = yr ? *reinterpret_cast<const V2*>(F.cy + q + sy) : zero2;
+        const V2 czm = *reinterpret_cast<const V2*>(F.cz + q);
+        const V2 czp = zr ? *reinterpret_cast<const V2*>(F.cz + q + sz) : zero2;
+        // child x = i0: neighbours x- (pl, cx[i0]), x+ (p.y, cx[i0+1]); same order as stencil()
+        {
+          T s = T(0), d = T(0), c;
+          if (xl) { c = cxp.x; s += c * pl; d += c; }
+          c = cxp.y; s += c * p.y; d += c;
+          if (yl) { c = cym.x; s += c * pym.x; d += c; }
+          if (yr) { c = cyp.x; s += c * pyp.x; d += c; }
+          if (zl) { c = czm.x; s += c * pzm.x; d += c; }
+          if (zr) { c = czp.x; s += c * pzp.x; d += c; }
+          acc += b.x - (s - d * p.x);
+        }
+        {
+          T s = T(0), d = T(0), c;
+          c = cxp.y; s += c * p.x; d += c;
+          if (xr) { c = cxr; s += c * pr; d += c; }
+          if (yl) { c = cym.y; s += c * pym.y; d += c; }
+          if (yr) { c = cyp.y; s += c * pyp.y; d += c; }
+          if (zl) { c = czm.y; s += c * pzm.y; d += c; }
+          if (zr) { c = czp.y; s += c * pzp.y; d += c; }
+          acc += b.y - (s - d * p.y);
+        }
       }
+  } else {
+    for (int dz = 0; dz < F.fz; ++dz)
+      for (int dy = 0; dy < F.fy; ++dy)
+        for (int dx = 0; dx < F.fx; ++dx) {
+          const int i = F.fx * I + dx, j = F.fy * J + dy, k = F.fz * K + dz;
+          const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
+          T s, d;
+          stencil(F, F.sol, i, j, k, q, s, d);
+          acc += F.src[q] - (s - d * F.sol[q]);
+        }
+  }
   const size_t cq = ((size_t)K * C.ny + J) * C.nx + I;
   C.src[cq] = acc * (T(1) / T(F.fx * F.fy * F.fz));
-  C.sol[cq] = T(0);
+  if (zero_sol) C.sol[cq] = T(0);
 }
 
 // Prolongation + correction: fine sol += e_c +/- m/4 per coarsened axis, with
 // central slopes m = (e_{c+1} - e_{c-1})/2 and zero-gradient ghosts at walls.
+// One thread per coarse cell updates its children; with fx = 2 the two
+// x-children are one vector load and store.  Per child the terms are added in
+// the order x, y, z, as the oracle does.
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> C) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= F.nx || j >= F.ny) return;
-  const int I = i / F.fx, J = j / F.fy, K = k / F.fz;
+  pdl_enter();
+  using V2 = typename Vec2<T>::type;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I >= C.nx || J >= C.ny) return;
   const size_t csy = (size_t)C.nx, csz = (size_t)C.nx * C.ny;
   const size_t cq = (size_t)K * csz + (size_t)J * csy + I;
   const T* e = C.sol;
   const T ec = e[cq];
-  T val = ec;
-  if (F.fx == 2) {
-    const T em = I > 0 ? e[cq - 1] : ec, ep = I < C.nx - 1 ? e[cq + 1] : ec;
-    const T m = T(0.5) * (ep - em);
-    val += (i & 1) ? T(0.25) * m : -(T(0.25) * m);
-  }
-  if (F.fy == 2) {
-    const T em = J > 0 ? e[cq - csy] : ec, ep = J < C.ny - 1 ? e[cq + csy] : ec;
-    const T m = T(0.5) * (ep - em);
-    val += (j & 1) ? T(0.25) * m : -(T(0.25) * m);
-  }
-  if (F.fz == 2) {
-    const T em = K > 0 ? e[cq - csz] : ec, ep = K < C.nz - 1 ? e[cq + csz] : ec;
-    const T m = T(0.5) * (ep - em);
-    val += (k & 1) ? T(0.25) * m : -(T(0.25) * m);
-  }
-  const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
-  F.sol[q] += val;
+  T mx = T(0), my = T(0), mz = T(0);
+  if (F.fx == 2) mx = T(0.5) * ((I < C.nx - 1 ? e[cq + 1] : ec) - (I > 0 ? e[cq - 1] : ec));
+  if (F.fy == 2) my = T(0.5) * ((J < C.ny - 1 ? e[cq + csy] : ec) - (J > 0 ? e[cq - csy] : ec));
+  if (F.fz == 2) mz = T(0.5) * ((K < C.nz - 1 ? e[cq + csz] : ec) - (K > 0 ? e[cq - csz] : ec));
+  for (int dz = 0; dz < F.fz; ++dz)
+    for (int dy = 0; dy < F.fy; ++dy) {
+      const int j = F.fy * J + dy, k = F.fz * K + dz;
+      T* row = F.sol + ((size_t)k * F.ny + j) * F.nx;
+      const T ty = dy ? T(0.25) * my : -(T(0.25) * my);
+      const T tz = dz ? T(0.25) * mz : -(T(0.25) * mz);
+      if (F.fx == 2) {
+        T v0 = ec + -(T(0.25) * mx), v1 = ec + T(0.25) * mx;
+        if (F.fy == 2) { v0 += ty; v1 += ty; }
+        if (F.fz == 2) { v0 += tz; v1 += tz; }
+        V2* pr = reinterpret_cast<V2*>(row) + I;
+        V2 cur = *pr;
+        cur.x += v0;
+        cur.y += v1;
+        *pr = cur;
+      } else {
+        T v = ec;
+        if (F.fy == 2) v += ty;
+        if (F.fz == 2) v += tz;
+        row[I] += v;
+      }
+    }
 }
 
 // FP64 residual r = src - A sol with sum r^2.  Blocks stride over (y, z) rows,
@@ -117,6 +200,7 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> C)
 template <typename TO>
 __global__ void __launch_bounds__(kRedThreads) k_residual_norm(LevelView<double> L, TO* r,
                                                                ReduceScratch R, int slot) {
+  pdl_enter();
   double acc[1] = {0.0};
   const int rows = L.ny * L.nz;
   for (int row = blockIdx.x; row < rows; row += gridDim.x) {
@@ -162,6 +246,7 @@ template <typename T>
 __global__ void __launch_bounds__(kMaxCoarse) k_coarse_solve(int n, const T* __restrict__ minv,
                                                              const T* __restrict__ a,
                                                              const T* __restrict__ b, T* x) {
+  pdl_enter();
   __shared__ T sb[kMaxCoarse], sx[kMaxCoarse], se[kMaxCoarse];
   __shared__ T red[kMaxCoarse];
   __shared__ int refine;
@@ -339,25 +424,30 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
 
 // ---------------------------------------------------------------------------
 template <typename T>
-void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color) {
+void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_guess) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)(L.nx + 1) / 2, 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
-  if (L.idiag) k_smooth<T, true><<<grd, blk, 0, s>>>(L, color);
-  else k_smooth<T, false><<<grd, blk, 0, s>>>(L, color);
+  if (L.idiag) {
+    if (zero_guess) launch_pdl(k_smooth<T, true, true>, grd, blk, 0, s, L, color);
+    else launch_pdl(k_smooth<T, true, false>, grd, blk, 0, s, L, color);
+  } else {
+    if (zero_guess) launch_pdl(k_smooth<T, false, true>, grd, blk, 0, s, L, color);
+    else launch_pdl(k_smooth<T, false, false>, grd, blk, 0, s, L, color);
+  }
 }
 
 template <typename T>
-void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
+void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, bool zero_sol) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-  k_restrict<T><<<grd, blk, 0, s>>>(F, C);
+  launch_pdl(k_restrict<T>, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
 }
 
 template <typename T>
 void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
   const dim3 blk(32, 8, 1);
-  const dim3 grd(cdiv((size_t)F.nx, 32), cdiv((size_t)F.ny, 8), (unsigned)F.nz);
-  k_prolong<T><<<grd, blk, 0, s>>>(F, C);
+  const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+  launch_pdl(k_prolong<T>, grd, blk, 0, s, F, C);
 }
 
 // Blocks for a grid-stride reduction: 8 per SM, at most one per row.  The SM
@@ -378,7 +468,7 @@ template <typename TO>
 void launch_residual_norm(cudaStream_t s, const LevelView<double>& L, TO* r,
                           const ReduceScratch& R, int slot) {
   const int blocks = std::min(reduce_blocks_for((size_t)L.ny * L.nz), R.max_blocks);
-  k_residual_norm<TO><<<blocks, kRedThreads, 0, s>>>(L, r, R, slot);
+  launch_pdl(k_residual_norm<TO>, dim3(blocks), dim3(kRedThreads), 0, s, L, r, R, slot);
 }
 
 void launch_apply_dot(cudaStream_t s, const LevelView<double>& L, const double* d, double* q,
@@ -389,7 +479,7 @@ void launch_apply_dot(cudaStream_t s, const LevelView<double>& L, const double* 
 
 template <typename T>
 void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, const T* b, T* x) {
-  k_coarse_solve<T><<<1, kMaxCoarse, 0, s>>>(n, minv, adense, b, x);
+  launch_pdl(k_coarse_solve<T>, dim3(1), dim3(kMaxCoarse), 0, s, n, minv, adense, b, x);
 }
 
 void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
@@ -418,12 +508,12 @@ void launch_to_float(cudaStream_t s, const double* a, float* b, size_t n) {
   k_to_float<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(a, b, n);
 }
 
-template void launch_smooth<double>(cudaStream_t, const LevelView<double>&, int);
-template void launch_smooth<float>(cudaStream_t, const LevelView<float>&, int);
+template void launch_smooth<double>(cudaStream_t, const LevelView<double>&, int, bool);
+template void launch_smooth<float>(cudaStream_t, const LevelView<float>&, int, bool);
 template void launch_restrict<double>(cudaStream_t, const LevelView<double>&,
-                                      const LevelView<double>&);
+                                      const LevelView<double>&, bool);
 template void launch_restrict<float>(cudaStream_t, const LevelView<float>&,
-                                     const LevelView<float>&);
+                                     const LevelView<float>&, bool);
 template void launch_prolong<double>(cudaStream_t, const LevelView<double>&,
                                      const LevelView<double>&);
 template void launch_prolong<float>(cudaStream_t, const LevelView<float>&,
