@@ -78,6 +78,7 @@ struct gbmg_handle {
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
+  int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   int* derr = nullptr;   // device error flags (TMA wait timeouts)
   DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B]
   // captured iterations, per kind and per parity of pcur
@@ -262,6 +263,32 @@ void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   }
 }
 
+// Levels [h->sub_lc, L) as one single-block launch.
+template <typename T>
+SubCycle<T> make_subcycle(gbmg_handle* h, bool reverse) {
+  SubCycle<T> S{};
+  const int lc = h->sub_lc;
+  S.nlev = h->L - lc;
+  S.nu1 = h->prm.nu1;
+  S.nu2 = h->prm.nu2;
+  S.reverse = reverse ? 1 : 0;
+  S.n_coarse = h->nc;
+  int off = 0;
+  for (int i = 0; i < S.nlev; ++i) {
+    const LevelView<T> V = view<T>(h->lv[lc + i]);
+    S.lv[i] = SubLevel<T>{V.nx, V.ny, V.nz, V.fx, V.fy, V.fz, V.cx, V.cy, V.cz};
+    S.off[i] = off;
+    off += 2 * V.nx * V.ny * V.nz;
+  }
+  S.off[S.nlev] = off;
+  const LevelView<T> V0 = view<T>(h->lv[lc]);
+  S.src_in = V0.src;
+  S.sol_out = V0.sol;
+  S.minv = minv_of<T>(h);
+  S.adense = adense_of<T>(h);
+  return S;
+}
+
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
 // the post-smoothing colours black-first (symmetric preconditioner for CG).
 // zero_fine: the level-0 unknown starts at zero (correction and Krylov
@@ -271,17 +298,21 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
   const int L = h->L;
   const cudaStream_t s = h->stream;
   const bool pre = h->prm.nu1 > 0;
-  for (int l = 0; l < L - 1; ++l) {
+  const int top = std::min(h->sub_lc, L - 1);  // levels above the bottom block
+  for (int l = 0; l < top; ++l) {
     for (int it = 0; it < h->prm.nu1; ++it)
       sweep<T>(h, l, 0, it == 0 && (l > 0 || zero_fine));
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
            launch_restrict<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
   }
-  const Level& c = h->lv[L - 1];
-  const LevelView<T> C = view<T>(c);
-  LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
-         launch_coarse_solve<T>(s, h->nc, minv_of<T>(h), adense_of<T>(h), C.src, C.sol));
-  for (int l = L - 2; l >= 0; --l) {
+  if (h->sub_lc < L) {
+    LAUNCH(h, GBMG_PROF_COARSE_SOLVE, launch_subcycle<T>(s, make_subcycle<T>(h, reverse_post)));
+  } else {
+    const LevelView<T> C = view<T>(h->lv[L - 1]);
+    LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
+           launch_coarse_solve<T>(s, h->nc, minv_of<T>(h), adense_of<T>(h), C.src, C.sol));
+  }
+  for (int l = top - 1; l >= 0; --l) {
     LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
            launch_prolong<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
     for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0, false);
@@ -364,6 +395,24 @@ int free_all(gbmg_handle* h) {
 
 // TMA-fed sweeps on the FP32 levels with at least 2^15 cells and rows a
 // multiple of 16 bytes (GBMG_TMA_LEVELS overrides how many finest levels).
+// The one-block bottom of the cycle: the first level >= 1 with at most
+// kSubMaxCells cells and at least one coarser level below it.
+template <typename T>
+void setup_subcycle(gbmg_handle* h) {
+  h->sub_lc = h->L;
+  if (const char* e = std::getenv("GBMG_SUBCYCLE"))
+    if (std::atoi(e) == 0) return;
+  for (int l = 1; l + 1 < h->L; ++l)
+    if (h->lv[l].n <= (size_t)kSubMaxCells && h->L - l <= kSubMaxLevels) {
+      h->sub_lc = l;
+      break;
+    }
+  if (h->sub_lc >= h->L) return;
+  const SubCycle<T> S = make_subcycle<T>(h, false);
+  const size_t smem = subcycle_smem<T>(S);
+  if (smem > 200 * 1024 || subcycle_init<T>(smem) != 0) h->sub_lc = h->L;
+}
+
 int setup_tma(gbmg_handle* h) {
   // the two-colour FP32 sweep measured faster than the TMA-fed one on GB300
   // (132 vs 143 us per 256^3 sweep), so the TMA sweep is opt-in
@@ -482,6 +531,8 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->derr, 4));
   GB_CUDA(h, cudaMemsetAsync(h->derr, 0, 4 * sizeof(int), h->stream));
   if (h->mixed) GB_TRY(setup_tma(h));
+  if (h->mixed) setup_subcycle<float>(h);
+  else setup_subcycle<double>(h);
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -562,7 +613,7 @@ int build_hierarchy(gbmg_handle* h) {
   return GBMG_OK;
 }
 
-int set_rho_device(gbmg_handle* h) {
+int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   const gbmg_grid& g = h->grid;
   Level& f = h->lv[0];
   float* c32[3] = {f.cx32, f.cy32, f.cz32};
@@ -570,7 +621,7 @@ int set_rho_device(gbmg_handle* h) {
   LAUNCH(h, GBMG_PROF_SETUP,
          launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
                           h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
-                          h->mixed ? cw : nullptr));
+                          h->mixed ? cw : nullptr, bulk_rho));
   h->fine_copies = h->mixed;
   GB_TRY(check_launch(h, "face_coef"));
   h->rho_ready = true;
@@ -879,7 +930,7 @@ int gbmg_set_rho(gbmg_handle* h, gbmg_field rho, int mem) {
   GB_TRY(validate_field(h, rho, "rho"));
   const gbmg_grid& g = h->grid;
   GB_TRY(upload(h, rho, g.nx, g.ny, g.nz, mem, h->rho));
-  GB_TRY(set_rho_device(h));
+  GB_TRY(set_rho_device(h, nullptr));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
 }
@@ -900,7 +951,9 @@ int gbmg_set_phi(gbmg_handle* h, gbmg_field phi, double eps, double rho_pos, dou
   launch_rho_from_phi(h->stream, g.nx, g.ny, g.nz, sp, eps, rho_pos, rho_neg, h->rho);
   h->launches += 1;
   GB_TRY(check_launch(h, "rho_from_phi"));
-  GB_TRY(set_rho_device(h));
+  // away from the interface rho is exactly rho_pos*1 + rho_neg*0 or rho_pos*0 + rho_neg*1
+  const double bulk[2] = {rho_pos * 1.0 + rho_neg * (1.0 - 1.0), rho_pos * 0.0 + rho_neg * (1.0 - 0.0)};
+  GB_TRY(set_rho_device(h, bulk));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
 }

@@ -53,6 +53,34 @@ enum : int {
   kSlotDot2 = 10,
 };
 
+// ---- the bottom of the cycle in one block (subcycle.cu) ----------------------
+constexpr int kSubMaxCells = 4096;  // levels this small run inside one block
+constexpr int kSubMaxLevels = 8;
+template <typename T>
+struct SubLevel {
+  int nx, ny, nz;
+  int fx, fy, fz;
+  const T* cx;
+  const T* cy;
+  const T* cz;
+};
+template <typename T>
+struct SubCycle {
+  int nlev, nu1, nu2, reverse, n_coarse;
+  SubLevel<T> lv[kSubMaxLevels];   // the levels from the first small one down
+  int off[kSubMaxLevels + 1];      // shared-memory offsets (elements): sol, src per level
+  const T* src_in;                 // right-hand side of the first small level (global)
+  T* sol_out;                      // its result (global)
+  const T* minv;
+  const T* adense;
+};
+template <typename T>
+size_t subcycle_smem(const SubCycle<T>& S);
+template <typename T>
+int subcycle_init(size_t smem);
+template <typename T>
+void launch_subcycle(cudaStream_t s, const SubCycle<T>& S);
+
 // ---- launchers (kernels_mg.cu) ---------------------------------------------
 // zero_guess: the level's current values are taken as zero (first colour of
 // the first sweep after the coarse unknown was started at zero)
@@ -105,9 +133,11 @@ void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, 
                      int64_t sy, int64_t sz);
 // c32 / cw: optional arrays of 3 pointers (x, y, z) for the FP32 and
 // double-word copies, written in the same pass.
+// bulk_rho: the two bulk densities (rho_pos, rho_neg of the level set), or
+// null; faces between two bulk cells use host-computed values.
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
                       const double* rho, double* cx, double* cy, double* cz, float* const* c32,
-                      float2* const* cw);
+                      float2* const* cw, const double* bulk_rho);
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                        double dx, double dy, double dz, double dt, double* b);
 void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,

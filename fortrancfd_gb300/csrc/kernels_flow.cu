@@ -28,19 +28,28 @@ inline unsigned stride_blocks(size_t n) {
 
 // Smoothed Heaviside H(phi/eps) = (1 + x + sin(pi x)/pi)/2 on |x| < 1, then
 // rho = rho_pos H + rho_neg (1 - H).
+// Outside the band |phi| > eps_out (eps_out slightly above eps (1 - 1e-12),
+// set by the host) the division phi/eps would land past the clipping
+// threshold anyway, so H is 0 or 1 without computing it: the same result as
+// the full branch, with the FP64 division done only in the band.
 __global__ void __launch_bounds__(256) k_rho_from_phi(int nx, int ny, int nz, Strided phi,
-                                                      double eps, double rho_pos,
+                                                      double eps, double eps_out, double rho_pos,
                                                       double rho_neg, double* rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const double pi = 3.141592653589793;
-  const double x = phi.data[i + j * phi.sy + k * phi.sz] / eps;
+  const double ph = phi.data[i + j * phi.sy + k * phi.sz];
   double h;
-  if (x > 1.0 - 1e-12) h = 1.0;
-  else if (x < -1.0 + 1e-12) h = 0.0;
-  else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+  if (ph > eps_out) h = 1.0;
+  else if (ph < -eps_out) h = 0.0;
+  else {
+    const double x = ph / eps;
+    if (x > 1.0 - 1e-12) h = 1.0;
+    else if (x < -1.0 + 1e-12) h = 0.0;
+    else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+  }
   h = fmax(fmin(h, 1.0), 0.0);
   rho[((size_t)k * ny + j) * nx + i] = rho_pos * h + rho_neg * (1.0 - h);
 }
@@ -68,6 +77,13 @@ __global__ void __launch_bounds__(256) k_copy_out(int nx, int ny, int nz, const 
 // it is an exact scaling and is done as a multiplication by 1/h^2 (same
 // result, one FP64 division instead of two).  Optionally also writes the
 // FP32 copies of the cycle and the double-word copies of the defect kernel.
+struct BulkFaces {
+  double s[2];        // 2 rho of the two bulk densities
+  double c[3][2];     // face coefficient per axis and bulk density
+  float c32[3][2];
+  float2 cw[3][2];
+};
+
 struct FaceOut {
   double* c;
   float* c32;
@@ -83,28 +99,38 @@ __device__ __forceinline__ void face_store(const FaceOut& o, size_t q, double v)
   }
 }
 
+// The face value for rho_i + rho_nb = s along axis a (0 on walls); faces
+// between two cells of a bulk density (s equal to one of the two precomputed
+// sums) take the host-computed values, computed with the same IEEE operations.
+__device__ __forceinline__ void face_value(const BulkFaces& B, int a, double s, double h2,
+                                           double ih2, bool pow2, const FaceOut& o, size_t q) {
+  for (int v = 0; v < 2; ++v)
+    if (s == B.s[v]) {
+      o.c[q] = B.c[a][v];
+      if (o.c32) o.c32[q] = B.c32[a][v];
+      if (o.cw) o.cw[q] = B.cw[a][v];
+      return;
+    }
+  const double t = 2.0 / s;
+  face_store(o, q, pow2 ? t * ih2 : t / h2);
+}
+
 __global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, double3 h2, double3 ih2,
-                                                   int pow2, const double* __restrict__ rho,
-                                                   FaceOut ox, FaceOut oy, FaceOut oz) {
+                                                   int pow2, BulkFaces B,
+                                                   const double* __restrict__ rho, FaceOut ox,
+                                                   FaceOut oy, FaceOut oz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
   const double r = rho[q];
-  double c;
-  c = 0.0;
-  if (i > 0) { const double t = 2.0 / (r + rho[q - 1]); c = (pow2 & 1) ? t * ih2.x : t / h2.x; }
-  face_store(ox, q, c);
-  c = 0.0;
-  if (j > 0) { const double t = 2.0 / (r + rho[q - nx]); c = (pow2 & 2) ? t * ih2.y : t / h2.y; }
-  face_store(oy, q, c);
-  c = 0.0;
-  if (k > 0) {
-    const double t = 2.0 / (r + rho[q - (size_t)nx * ny]);
-    c = (pow2 & 4) ? t * ih2.z : t / h2.z;
-  }
-  face_store(oz, q, c);
+  if (i > 0) face_value(B, 0, r + rho[q - 1], h2.x, ih2.x, pow2 & 1, ox, q);
+  else face_store(ox, q, 0.0);
+  if (j > 0) face_value(B, 1, r + rho[q - nx], h2.y, ih2.y, pow2 & 2, oy, q);
+  else face_store(oy, q, 0.0);
+  if (k > 0) face_value(B, 2, r + rho[q - (size_t)nx * ny], h2.z, ih2.z, pow2 & 4, oz, q);
+  else face_store(oz, q, 0.0);
 }
 
 // b = div(u)/dt with MAC faces: u(f,j,k) on the x-face at f*dx, f = 0..nx.
@@ -317,8 +343,10 @@ static inline dim3 grid3(int nx, int ny, int nz) {
 
 void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, double eps,
                          double rho_pos, double rho_neg, double* rho) {
-  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, phi, eps, rho_pos, rho_neg,
-                                                          rho);
+  // phi > eps_out implies fl(phi/eps) > 1 - 1e-12 (margin 1e-15 >> rounding)
+  const double eps_out = eps * (1.0 - 1e-12) * (1.0 + 1e-15);
+  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, phi, eps, eps_out, rho_pos,
+                                                          rho_neg, rho);
 }
 
 void launch_copy_in(cudaStream_t s, int nx, int ny, int nz, Strided src, double* dst) {
@@ -337,14 +365,28 @@ static bool is_pow2(double v) {
 
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
                       const double* rho, double* cx, double* cy, double* cz, float* const* c32,
-                      float2* const* cw) {
+                      float2* const* cw, const double* bulk_rho) {
   const int pow2 = (is_pow2(dx2) ? 1 : 0) | (is_pow2(dy2) ? 2 : 0) | (is_pow2(dz2) ? 4 : 0);
+  const double h2[3] = {dx2, dy2, dz2};
+  BulkFaces B;
+  for (int v = 0; v < 2; ++v) {
+    // NaN never compares equal: no bulk shortcut without known bulk densities
+    B.s[v] = bulk_rho ? bulk_rho[v] + bulk_rho[v] : std::nan("");
+    for (int a = 0; a < 3; ++a) {
+      const double t = 2.0 / B.s[v];
+      const double c = ((pow2 >> a) & 1) ? t * (1.0 / h2[a]) : t / h2[a];
+      B.c[a][v] = c;
+      B.c32[a][v] = (float)c;
+      const float hi = (float)c;
+      B.cw[a][v] = make_float2(hi, (float)(c - (double)hi));
+    }
+  }
   const FaceOut ox{cx, c32 ? c32[0] : nullptr, cw ? cw[0] : nullptr};
   const FaceOut oy{cy, c32 ? c32[1] : nullptr, cw ? cw[1] : nullptr};
   const FaceOut oz{cz, c32 ? c32[2] : nullptr, cw ? cw[2] : nullptr};
   k_face_coef<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
       nx, ny, nz, make_double3(dx2, dy2, dz2), make_double3(1.0 / dx2, 1.0 / dy2, 1.0 / dz2), pow2,
-      rho, ox, oy, oz);
+      B, rho, ox, oy, oz);
 }
 
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,

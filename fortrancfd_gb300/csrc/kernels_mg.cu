@@ -39,6 +39,24 @@ __device__ __forceinline__ void stencil(const LevelView<T>& L, const T* __restri
   if (k < L.nz - 1) { c = L.cz[q + sz]; s += c * p[q + sz]; d += c; }
 }
 
+// Flux sum sum_f coe_f (p_nb - p_i) of cell (i,j,k), differences first so the
+// rounding is relative to each flux rather than to d |p| (order x-, x+, y-,
+// y+, z-, z+).
+template <typename T>
+__device__ __forceinline__ T flux_sum(const LevelView<T>& L, const T* __restrict__ p, int i, int j,
+                                      int k, size_t q) {
+  const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+  const T pc = p[q];
+  T s = T(0);
+  if (i > 0) s += L.cx[q] * (p[q - 1] - pc);
+  if (i < L.nx - 1) s += L.cx[q + 1] * (p[q + 1] - pc);
+  if (j > 0) s += L.cy[q] * (p[q - sy] - pc);
+  if (j < L.ny - 1) s += L.cy[q + sy] * (p[q + sy] - pc);
+  if (k > 0) s += L.cz[q] * (p[q - sz] - pc);
+  if (k < L.nz - 1) s += L.cz[q + sz] * (p[q + sz] - pc);
+  return s;
+}
+
 // One colour of a red-black Gauss-Seidel sweep: cells with (i+j+k)%2 == color
 // get p_i = (s - b_i)/d (the reference's p_i = (src - sum coe p_nb)/c with
 // c = -d).  One thread per cell of the colour.
@@ -195,7 +213,7 @@ __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, LevelView<T> C)
     }
 }
 
-// FP64 residual r = src - A sol with sum r^2.  Blocks stride over (y, z) rows,
+// FP64 residual r = src - A sol (flux form) with sum r^2.  Blocks stride over (y, z) rows,
 // threads over x; r is stored as TO (double, or float for the FP32 cycle).
 template <typename TO>
 __global__ void __launch_bounds__(kRedThreads) k_residual_norm(LevelView<double> L, TO* r,
@@ -207,9 +225,7 @@ __global__ void __launch_bounds__(kRedThreads) k_residual_norm(LevelView<double>
     const int j = row % L.ny, k = row / L.ny;
     for (int i = threadIdx.x; i < L.nx; i += blockDim.x) {
       const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
-      double s, d;
-      stencil(L, L.sol, i, j, k, q, s, d);
-      const double rr = L.src[q] - (s - d * L.sol[q]);
+      const double rr = L.src[q] - flux_sum(L, L.sol, i, j, k, q);
       if (r) r[q] = (TO)rr;
       acc[0] += rr * rr;
     }

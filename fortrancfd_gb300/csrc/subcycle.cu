@@ -1,0 +1,215 @@
+// The bottom of the V-cycle in one thread block (sm_103a).
+//
+// Levels with at most kSubMaxCells cells are launch-latency bound: a sweep of
+// 16^3 cells is a few microseconds of launch and drain for nanoseconds of
+// work.  This kernel runs everything from level lc down and back up --
+// sweeps, residual + restriction, the dense coarsest solve, prolongation --
+// in one block, with every level's unknown and right-hand side in shared
+// memory and the face coefficients read through L1.  Phases are separated by
+// __syncthreads().  Each step does the arithmetic of the corresponding
+// separate kernel in the same order (red-black update, children summed in z,
+// y, x order, slopes added x, y, z), so the cycle is the same cycle.
+#include "gbmg_internal.h"
+#include "pdl.cuh"
+
+namespace gbmg {
+
+namespace {
+
+constexpr int kSubThreads = 1024;
+
+template <typename T>
+__device__ __forceinline__ void sub_stencil(const SubLevel<T>& L, const T* __restrict__ p, int i,
+                                            int j, int k, int q, T& s, T& d) {
+  const int sy = L.nx, sz = L.nx * L.ny;
+  T c;
+  s = T(0);
+  d = T(0);
+  if (i > 0) { c = L.cx[q]; s += c * p[q - 1]; d += c; }
+  if (i < L.nx - 1) { c = L.cx[q + 1]; s += c * p[q + 1]; d += c; }
+  if (j > 0) { c = L.cy[q]; s += c * p[q - sy]; d += c; }
+  if (j < L.ny - 1) { c = L.cy[q + sy]; s += c * p[q + sy]; d += c; }
+  if (k > 0) { c = L.cz[q]; s += c * p[q - sz]; d += c; }
+  if (k < L.nz - 1) { c = L.cz[q + sz]; s += c * p[q + sz]; d += c; }
+}
+
+// one colour of a red-black sweep on a shared-memory level
+template <typename T>
+__device__ void sub_colour(const SubLevel<T>& L, T* sol, const T* src, int color, bool zero) {
+  const int n = L.nx * L.ny * L.nz;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q % L.nx, j = (q / L.nx) % L.ny, k = q / (L.nx * L.ny);
+    if (((i + j + k) & 1) != color) continue;
+    T s, d;
+    if (zero) {
+      T dd;
+      sub_stencil(L, sol, i, j, k, q, s, dd);  // for d only; p is ignored
+      s = T(0);
+      d = dd;
+    } else {
+      sub_stencil(L, sol, i, j, k, q, s, d);
+    }
+    sol[q] = (s - src[q]) / d;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ void sub_sweep(const SubLevel<T>& L, T* sol, const T* src, int first, bool zero) {
+  sub_colour(L, sol, src, first, zero);
+  sub_colour(L, sol, src, 1 - first, false);
+}
+
+// coarse src = mean of the children's residuals (fine -> coarse, shared memory)
+template <typename T>
+__device__ void sub_restrict(const SubLevel<T>& F, const T* fsol, const T* fsrc,
+                             const SubLevel<T>& C, T* csrc) {
+  const int n = C.nx * C.ny * C.nz;
+  for (int cq = threadIdx.x; cq < n; cq += blockDim.x) {
+    const int I = cq % C.nx, J = (cq / C.nx) % C.ny, K = cq / (C.nx * C.ny);
+    T acc = T(0);
+    for (int dz = 0; dz < F.fz; ++dz)
+      for (int dy = 0; dy < F.fy; ++dy)
+        for (int dx = 0; dx < F.fx; ++dx) {
+          const int i = F.fx * I + dx, j = F.fy * J + dy, k = F.fz * K + dz;
+          const int q = (k * F.ny + j) * F.nx + i;
+          T s, d;
+          sub_stencil(F, fsol, i, j, k, q, s, d);
+          acc += fsrc[q] - (s - d * fsol[q]);
+        }
+    csrc[cq] = acc * (T(1) / T(F.fx * F.fy * F.fz));
+  }
+  __syncthreads();
+}
+
+// fine sol += central-slope interpolation of the coarse sol
+template <typename T>
+__device__ void sub_prolong(const SubLevel<T>& F, T* fsol, const SubLevel<T>& C, const T* e) {
+  const int n = F.nx * F.ny * F.nz;
+  const int csy = C.nx, csz = C.nx * C.ny;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q % F.nx, j = (q / F.nx) % F.ny, k = q / (F.nx * F.ny);
+    const int I = i / F.fx, J = j / F.fy, K = k / F.fz;
+    const int cq = K * csz + J * csy + I;
+    const T ec = e[cq];
+    T val = ec;
+    if (F.fx == 2) {
+      const T m = T(0.5) * ((I < C.nx - 1 ? e[cq + 1] : ec) - (I > 0 ? e[cq - 1] : ec));
+      val += (i & 1) ? T(0.25) * m : -(T(0.25) * m);
+    }
+    if (F.fy == 2) {
+      const T m = T(0.5) * ((J < C.ny - 1 ? e[cq + csy] : ec) - (J > 0 ? e[cq - csy] : ec));
+      val += (j & 1) ? T(0.25) * m : -(T(0.25) * m);
+    }
+    if (F.fz == 2) {
+      const T m = T(0.5) * ((K < C.nz - 1 ? e[cq + csz] : ec) - (K > 0 ? e[cq - csz] : ec));
+      val += (k & 1) ? T(0.25) * m : -(T(0.25) * m);
+    }
+    fsol[q] += val;
+  }
+  __syncthreads();
+}
+
+// x = Minv b, one refinement step when max|b - A x| > 1e-10, mean projection
+// (as k_coarse_solve)
+template <typename T>
+__device__ void sub_coarse(int n, const T* __restrict__ minv, const T* __restrict__ a, const T* b,
+                           T* x, T* scratch) {
+  T* se = scratch;           // n
+  int* refine = reinterpret_cast<int*>(scratch + n);
+  const int t = threadIdx.x;
+  if (t == 0) *refine = 0;
+  __syncthreads();
+  if (t < n) {
+    T acc = T(0);
+    for (int q = 0; q < n; ++q) acc += minv[t * n + q] * b[q];
+    x[t] = acc;
+  }
+  __syncthreads();
+  if (t < n) {
+    T e = b[t];
+    for (int q = 0; q < n; ++q) e -= a[t * n + q] * x[q];
+    se[t] = e;
+    if (fabs((double)e) > 1e-10) atomicOr(refine, 1);
+  }
+  __syncthreads();
+  if (*refine && t < n) {
+    T acc = T(0);
+    for (int q = 0; q < n; ++q) acc += minv[t * n + q] * se[q];
+    x[t] += acc;
+  }
+  __syncthreads();
+  if (t == 0) {
+    T s = T(0);
+    for (int q = 0; q < n; ++q) s += x[q];
+    se[0] = s / T(n);
+  }
+  __syncthreads();
+  if (t < n) x[t] -= se[0];
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
+  pdl_enter();
+  extern __shared__ unsigned char sub_raw[];
+  T* base = reinterpret_cast<T*>(sub_raw);
+  const int nl = S.nlev;
+  T* sol[kSubMaxLevels];
+  T* src[kSubMaxLevels];
+  for (int l = 0; l < nl; ++l) {
+    sol[l] = base + S.off[l];
+    src[l] = sol[l] + S.lv[l].nx * S.lv[l].ny * S.lv[l].nz;
+  }
+  T* scratch = base + S.off[nl];
+  {
+    const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
+    for (int q = threadIdx.x; q < n0; q += blockDim.x) src[0][q] = S.src_in[q];
+  }
+  __syncthreads();
+  for (int l = 0; l < nl - 1; ++l) {
+    for (int it = 0; it < S.nu1; ++it) sub_sweep(S.lv[l], sol[l], src[l], 0, it == 0);
+    if (S.nu1 == 0) {
+      const int n = S.lv[l].nx * S.lv[l].ny * S.lv[l].nz;
+      for (int q = threadIdx.x; q < n; q += blockDim.x) sol[l][q] = T(0);
+      __syncthreads();
+    }
+    sub_restrict(S.lv[l], sol[l], src[l], S.lv[l + 1], src[l + 1]);
+  }
+  sub_coarse(S.n_coarse, S.minv, S.adense, src[nl - 1], sol[nl - 1], scratch);
+  for (int l = nl - 2; l >= 0; --l) {
+    sub_prolong(S.lv[l], sol[l], S.lv[l + 1], sol[l + 1]);
+    for (int it = 0; it < S.nu2; ++it) sub_sweep(S.lv[l], sol[l], src[l], S.reverse ? 1 : 0, false);
+  }
+  const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
+  for (int q = threadIdx.x; q < n0; q += blockDim.x) S.sol_out[q] = sol[0][q];
+}
+
+}  // namespace
+
+template <typename T>
+size_t subcycle_smem(const SubCycle<T>& S) {
+  return (size_t)(S.off[S.nlev] + 2 * kMaxCoarse + 8) * sizeof(T);
+}
+
+template <typename T>
+int subcycle_init(size_t smem) {
+  return cudaFuncSetAttribute(k_subcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem) == cudaSuccess
+             ? 0
+             : -1;
+}
+
+template <typename T>
+void launch_subcycle(cudaStream_t s, const SubCycle<T>& S) {
+  launch_pdl(k_subcycle<T>, dim3(1), dim3(kSubThreads), subcycle_smem(S), s, S);
+}
+
+template size_t subcycle_smem<float>(const SubCycle<float>&);
+template size_t subcycle_smem<double>(const SubCycle<double>&);
+template int subcycle_init<float>(size_t);
+template int subcycle_init<double>(size_t);
+template void launch_subcycle<float>(cudaStream_t, const SubCycle<float>&);
+template void launch_subcycle<double>(cudaStream_t, const SubCycle<double>&);
+
+}  // namespace gbmg

@@ -198,18 +198,28 @@ void or_apply(const or_grid* g, const double* cx, const double* cy, const double
       }
 }
 
-/* r = b - A p; returns sum r^2 (multigrid_residual, DD3 multigrid_solver.f90:162-222). */
+/* r = b - A p; returns sum r^2 (multigrid_residual, DD3 multigrid_solver.f90:162-222).
+ * The flux form b - sum_f coe_f (p_nb - p_i) (differences first) keeps the
+ * rounding relative to each flux, so tight tolerances stay reachable. */
 double or_residual(const or_grid* g, const double* cx, const double* cy, const double* cz,
                    const double* p, const double* b, double* r) {
   const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t sy = nx, sz = (size_t)nx * ny;
   double s2 = 0.0;
 #pragma omp parallel for schedule(static) reduction(+ : s2)
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j)
       for (int i = 0; i < nx; ++i) {
-        double d, s = stencil_sum(nx, ny, nz, cx, cy, cz, p, i, j, k, &d);
         size_t q = ((size_t)k * ny + j) * nx + i;
-        double rr = b[q] - (s - d * p[q]);
+        const double pc = p[q];
+        double s = 0.0;
+        if (i > 0) s += cx[q] * (p[q - 1] - pc);
+        if (i < nx - 1) s += cx[q + 1] * (p[q + 1] - pc);
+        if (j > 0) s += cy[q] * (p[q - sy] - pc);
+        if (j < ny - 1) s += cy[q + sy] * (p[q + sy] - pc);
+        if (k > 0) s += cz[q] * (p[q - sz] - pc);
+        if (k < nz - 1) s += cz[q + sz] * (p[q + sz] - pc);
+        double rr = b[q] - s;
         if (r) r[q] = rr;
         s2 += rr * rr;
       }

@@ -52,6 +52,19 @@ def test_rho_from_phi(cuda):
         got = s.level_coef(0)
         for a, b in zip(got, c.coef):
             np.testing.assert_allclose(a, b, rtol=1e-13, atol=0)
+        # faces between two cells outside the interface band take the
+        # precomputed bulk values: those must be bit-identical to the oracle's
+        bulk = np.abs(c.phi) > c.case.eps * (1 + 1e-9)
+        for ax, (a, b) in enumerate(zip(got, c.coef)):
+            axis = 2 - ax
+            both = bulk.copy()
+            sl_hi = [slice(None)] * 3
+            sl_lo = [slice(None)] * 3
+            sl_hi[axis] = slice(1, None)
+            sl_lo[axis] = slice(None, -1)
+            both[tuple(sl_hi)] &= bulk[tuple(sl_lo)]
+            assert both.sum() > 0
+            np.testing.assert_array_equal(a[both], b[both])
 
 
 @pytest.mark.parametrize("idx,scale", [(0, 2), (1, 8)])
@@ -272,5 +285,21 @@ def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale, krylo
             s.ppe_init(c.rho)
             out[levels] = s.solve(c.b, tol=1e-10)
     (p0, s0), (p1, s1) = out["0"], out["99"]
+    assert s0["cycles"] == s1["cycles"]
+    assert rel_l2(p1, p0) <= 1e-12
+
+
+@pytest.mark.parametrize("precision,idx,scale", [("fp64", 1, 4), ("mixed", 1, 2), ("mixed", 0, 1)])
+def test_single_block_bottom_matches_separate_launches(cuda, monkeypatch, precision, idx, scale):
+    """The levels of at most 4096 cells run in one block (GBMG_SUBCYCLE=0 runs
+    them as separate launches); same cycle, same answer."""
+    c = cases.config(idx, scale)
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("GBMG_SUBCYCLE", flag)
+        with solver(c, precision=precision) as s:
+            s.ppe_init(c.rho)
+            out[flag] = s.solve(c.b, tol=1e-10)
+    (p0, s0), (p1, s1) = out["0"], out["1"]
     assert s0["cycles"] == s1["cycles"]
     assert rel_l2(p1, p0) <= 1e-12
