@@ -302,7 +302,7 @@ def adjoint_section(dev, stream, reps=5, scale=1):
         g = x.grad
 
         def J(ph):
-            q = pressure_solve(ph, b, s64, tol=1e-14, **kw)
+            q = pressure_solve(ph, b, s64, tol=1e-12, **kw)
             return 0.5 * ((q - p_t) ** 2).sum()
 
         rng = np.random.default_rng(7)

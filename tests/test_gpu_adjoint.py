@@ -3,8 +3,9 @@ oracle adjoint, and autograd gradients (with respect to b and to the level set
 phi, through H_eps and beta) against central finite differences.
 
 Tolerances: the adjoint kernel does the oracle's arithmetic (1e-12 relative);
-gradients from FP64 solves match central differences with step 1e-6 to 1e-6
-relative along random unit directions; the mixed-precision forward and
+gradients from FP64 solves to a relative residual of 1e-13 (a few times the
+FP64 floor of these density-ratio-1000 cases) match central differences with
+step 1e-6 to 1e-6 relative along random unit directions; the mixed-precision forward and
 backward match the FP64 oracle adjoint to 1e-6 relative L2.
 """
 import numpy as np
@@ -56,10 +57,10 @@ def test_gradients_match_central_differences(cuda, wrt):
     kw = dict(eps=case.eps, rho_pos=case.rho_pos, rho_neg=case.rho_neg)
     with PressurePoisson(case.shape, case.spacing, krylov=True, max_cycles=600) as s, \
             PressurePoisson(case.shape, case.spacing, krylov=True, max_cycles=600) as st:
-        p_t = pressure_solve(phi, bt, st, tol=1e-14, **kw).detach()
+        p_t = pressure_solve(phi, bt, st, tol=1e-13, **kw).detach()
 
         def J(ph, bb):
-            p = pressure_solve(ph, bb, s, tol=1e-14, **kw)
+            p = pressure_solve(ph, bb, s, tol=1e-13, **kw)
             return 0.5 * ((p - p_t) ** 2).sum()
 
         x = (phi if wrt == "phi" else b).clone().requires_grad_(True)
@@ -109,15 +110,15 @@ def test_rho_input_function(cuda):
     rho = torch.from_numpy(orc.rho_from_phi(phi.cpu().numpy(), case.eps, case.rho_pos,
                                             case.rho_neg)).to(cuda).requires_grad_(True)
     with PressurePoisson(case.shape, case.spacing, krylov=True, max_cycles=400) as s:
-        p = PressureSolveRho.apply(rho, b, s, 1e-14)
+        p = PressureSolveRho.apply(rho, b, s, 1e-13)
         (0.5 * (p ** 2).sum()).backward()
         g = rho.grad
         v = torch.from_numpy(np.random.default_rng(3).standard_normal(case.shape)).to(cuda)
         v /= v.norm()
         h = 1e-6 * float(rho.detach().abs().max())
         with torch.no_grad():
-            jp = 0.5 * (PressureSolveRho.apply(rho.detach() + h * v, b, s, 1e-14) ** 2).sum()
-            jm = 0.5 * (PressureSolveRho.apply(rho.detach() - h * v, b, s, 1e-14) ** 2).sum()
+            jp = 0.5 * (PressureSolveRho.apply(rho.detach() + h * v, b, s, 1e-13) ** 2).sum()
+            jm = 0.5 * (PressureSolveRho.apply(rho.detach() - h * v, b, s, 1e-13) ** 2).sum()
     fd = float((jp - jm) / (2 * h))
     assert abs(fd - float((g * v).sum())) <= 1e-6 * abs(fd)
 
@@ -133,7 +134,7 @@ def test_rollout_gradient_matches_central_differences(cuda):
     with PressurePoisson(case.shape, case.spacing, krylov=True, max_cycles=400) as s:
         c = c0.clone().requires_grad_(True)
         r = r0.clone().requires_grad_(True)
-        J = rollout_loss(c, r, case, s, steps=3, tol=1e-14)
+        J = rollout_loss(c, r, case, s, steps=3, tol=1e-13)
         J.backward()
         h = 1e-6
         checks = [("c", 0, 2), ("c", 1, 0), ("c", 3, 1), ("r", 2, None), ("r", 0, None)]
@@ -145,12 +146,12 @@ def test_rollout_gradient_matches_central_differences(cuda):
                 d[i] = h
             with torch.no_grad():
                 if kind == "c":
-                    jp = rollout_loss(c0 + d, r0, case, s, steps=3, tol=1e-14)
-                    jm = rollout_loss(c0 - d, r0, case, s, steps=3, tol=1e-14)
+                    jp = rollout_loss(c0 + d, r0, case, s, steps=3, tol=1e-13)
+                    jm = rollout_loss(c0 - d, r0, case, s, steps=3, tol=1e-13)
                     ad = float(c.grad[i, a])
                 else:
-                    jp = rollout_loss(c0, r0 + d, case, s, steps=3, tol=1e-14)
-                    jm = rollout_loss(c0, r0 - d, case, s, steps=3, tol=1e-14)
+                    jp = rollout_loss(c0, r0 + d, case, s, steps=3, tol=1e-13)
+                    jm = rollout_loss(c0, r0 - d, case, s, steps=3, tol=1e-13)
                     ad = float(r.grad[i])
             fd = float((jp - jm) / (2 * h))
             assert abs(fd - ad) <= 1e-5 * abs(fd) + 1e-9 * abs(float(J)), (kind, i, a, fd, ad)
