@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ms per 256³ Poisson solve to 1e-10 rel. residual: FP32-in-FP64 vs FP64 MG"
 TOL = 1e-10
+NU1, NU2 = 2, 2  # V(2,2), the library's default
 
 
 def parse():
@@ -154,8 +155,8 @@ def measured_peaks():
 
 
 def traffic_per_cell():
-    """dram bytes per fine cell per launch, per kernel class, from an ncu capture
-    summarised in profiles/ (None when no capture was made)."""
+    """dram bytes (read + write) per fine cell processed, per kernel class, from
+    an ncu capture summarised in profiles/ (empty when no capture was made)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
@@ -166,10 +167,19 @@ def traffic_per_cell():
 
 # algorithmic bytes per fine cell per launch of each kernel class, mixed solve:
 # FP32 cycle arrays (w = 4) and the double-word defect kernel
+# per sweep for the smoother (a two-colour sweep is two launches: the bench
+# scales by the sweeps a launch covers).  With the density form (the default
+# for an operator set from rho or phi) the FP32 finest-level kernels read the
+# cell density (w) instead of three face-coefficient arrays (3w).
+def rho_form():
+    return os.environ.get("GBMG_RHO_COEF", "1") != "0"
+
+
 def algorithmic_bytes_per_cell(cls, w=4):
+    c = w if rho_form() else 3.0 * w
     return {
-        "smooth_fine": 6.0 * w,                  # one fused sweep: p, b, bx, by, bz read, p' write
-        "restrict_fine": 5.0 * w + 2.0 * w / 8,  # p, b, bx, by, bz -> coarse b, sol
+        "smooth_fine": 3.0 * w + c,              # one sweep: p, b, coefficients read, p' write
+        "restrict_fine": 2.0 * w + c + 2.0 * w / 8,  # p, b, coefficients -> coarse b, sol
         "prolong_fine": 2.0 * w + w / 8,         # p r/w + coarse e
         "residual": 56.0,                        # defect: p(8) + e(4) + b(8) + 3 coefs(24) in,
                                                  # p(8) + r32(4) out
@@ -345,7 +355,7 @@ def run_ours(args):
 
     phi = dev_t(phi_h)
     u, v, w = dev_t(u_h), dev_t(v_h), dev_t(w_h)
-    kw = dict(krylov=args.krylov, stream=stream)
+    kw = dict(krylov=args.krylov, stream=stream, nu1=NU1, nu2=NU2)
 
     def barrier():
         if world > 1:
@@ -407,7 +417,7 @@ def run_ours(args):
             mixed.set_profiling(True)
             p.zero_()
             mixed.rho_mu(phi, case.eps, case.rho_pos, case.rho_neg)
-            mixed.solve(b, p, tol=TOL)
+            _, st_prof = mixed.solve(b, p, tol=TOL)
             prof = mixed.profile()
             mixed.set_profiling(False)
         total = sum(v[0] for v in prof.values())
@@ -415,15 +425,21 @@ def run_ours(args):
                         key=lambda kv: -kv[1][0])
         cls, (ms_cls, cnt) = ranked[0]
         per_launch_ms = ms_cls / max(cnt, 1)
-        alg = algorithmic_bytes_per_cell(cls, 4) * n
+        # fine cells one launch processes: a smoother launch covers
+        # sweeps/launches of a sweep (1/2 for the two-colour launches)
+        units = n
+        if cls == "smooth_fine":
+            units = n * st_prof["cycles"] * (NU1 + NU2) / max(cnt, 1)
+        alg = algorithmic_bytes_per_cell(cls, 4) * units
         peak, peak_kind = measured_peaks()
         achieved = alg / (per_launch_ms * 1e-3) / 1e9
         tr = traffic_per_cell().get(cls)
         roofline = {"kernel": cls, "bound": "hbm", "achieved": achieved, "peak": peak,
                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                    "traffic": (tr * n if tr else None), "launch_ms": per_launch_ms,
+                    "traffic": (tr * units if tr else None), "launch_ms": per_launch_ms,
                     "share": ms_cls / total if total else None,
-                    "algorithmic_bytes_per_launch": alg}
+                    "algorithmic_bytes_per_launch": alg, "cells_per_launch": units,
+                    "coefficients": "density form" if rho_form() else "stored FP32"}
 
     e2e = None
     if not args.no_e2e:

@@ -40,6 +40,10 @@ struct Level {
   float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
   float* buf_a = nullptr;  // the buffer sol32 pointed to at allocation
   SweepMaps* tmaps = nullptr;  // TMA maps with p = buffer A and p = buffer B (host memory)
+  // FP32 kernels take the coefficients from this density instead of cx32..cz32
+  // (finest level of a mixed solve whose operator came from rho or phi)
+  const float* rho32 = nullptr;
+  float k32[3] = {0.f, 0.f, 0.f};  // 2/h^2 per axis
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -60,6 +64,7 @@ struct gbmg_handle {
   double* b = nullptr;    // mean-free right-hand side
   double* p = nullptr;    // pressure being solved for
   double* rho = nullptr;  // cell density of the current operator
+  float* rho32 = nullptr; // its FP32 copy (mixed precision)
   double* vel[3] = {nullptr, nullptr, nullptr};
   size_t vel_n[3] = {0, 0, 0};
   double* aux[2] = {nullptr, nullptr};  // adjoint outputs / staging, allocated on first use
@@ -209,7 +214,7 @@ LevelView<double> v64(const Level& l) {
 }
 LevelView<float> v32(const Level& l) {
   return LevelView<float>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
-                          l.sol32, l.src32};
+                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2]};
 }
 template <typename T>
 LevelView<T> view(const Level& l);
@@ -372,7 +377,7 @@ int free_all(gbmg_handle* h) {
     delete[] v.tmaps;
     v.tmaps = nullptr;
   }
-  dfree(h->b); dfree(h->p); dfree(h->rho);
+  dfree(h->b); dfree(h->p); dfree(h->rho); dfree(h->rho32);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->aux[0]); dfree(h->aux[1]);
@@ -499,6 +504,7 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->p, h->n0));
   GB_TRY(dmalloc(h, &h->rho, h->n0));
   if (h->mixed) {
+    GB_TRY(dmalloc(h, &h->rho32, h->n0));
     GB_TRY(dmalloc(h, &h->pw[0], h->n0));
     GB_TRY(dmalloc(h, &h->pw[1], h->n0));
     GB_TRY(dmalloc(h, &h->bw, h->n0));
@@ -613,6 +619,24 @@ int build_hierarchy(gbmg_handle* h) {
   return GBMG_OK;
 }
 
+// Whether the FP32 finest-level kernels compute their coefficients from the
+// density (on: the operator came from rho/phi; GBMG_RHO_COEF=0 turns it off;
+// the TMA and fused sweeps read stored coefficients).  Captured graphs hold
+// the level views, so a change drops them.
+void set_rho_form(gbmg_handle* h, bool on) {
+  Level& f = h->lv[0];
+  bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0;
+  if (const char* e = std::getenv("GBMG_RHO_COEF"))
+    if (std::atoi(e) == 0) want = false;
+  const float* r = want ? h->rho32 : nullptr;
+  if (r != f.rho32) reset_graphs(h);
+  f.rho32 = r;
+  const gbmg_grid& g = h->grid;
+  f.k32[0] = (float)(2.0 / (g.dx * g.dx));
+  f.k32[1] = (float)(2.0 / (g.dy * g.dy));
+  f.k32[2] = (float)(2.0 / (g.dz * g.dz));
+}
+
 int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   const gbmg_grid& g = h->grid;
   Level& f = h->lv[0];
@@ -623,6 +647,9 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
                           h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
                           h->mixed ? cw : nullptr, bulk_rho));
   h->fine_copies = h->mixed;
+  if (h->mixed)
+    LAUNCH(h, GBMG_PROF_SETUP, launch_double_to_float(h->stream, h->rho, h->rho32, h->n0));
+  set_rho_form(h, true);
   GB_TRY(check_launch(h, "face_coef"));
   h->rho_ready = true;
   return build_hierarchy(h);
@@ -979,6 +1006,7 @@ int gbmg_set_coef(gbmg_handle* h, gbmg_field cx, gbmg_field cy, gbmg_field cz, i
                                h->stream));
   h->rho_ready = false;
   h->fine_copies = false;
+  set_rho_form(h, false);
   GB_TRY(build_hierarchy(h));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;

@@ -29,6 +29,11 @@ struct LevelView {
   const T* idiag;        // 1/diagonal, or nullptr (computed on the fly)
   T* sol;
   T* src;
+  // Coefficients from the cell density (FP32 finest level): when rho is set,
+  // the face coefficient between cells a and b along axis x is
+  // kx / (rho_a + rho_b) with kx = 2/dx^2, and cx, cy, cz are not read.
+  const T* rho = nullptr;
+  T kx = T(0), ky = T(0), kz = T(0);
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,

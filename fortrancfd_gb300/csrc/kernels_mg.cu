@@ -11,6 +11,7 @@
 // zero coefficients on walls.
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 
 #include "gbmg_internal.h"
 #include "pdl.cuh"
@@ -39,6 +40,50 @@ __device__ __forceinline__ void stencil(const LevelView<T>& L, const T* __restri
   if (k < L.nz - 1) { c = L.cz[q + sz]; s += c * p[q + sz]; d += c; }
 }
 
+// Face coefficient k/(rho_a + rho_b) of the density form.  FP32 uses the
+// fast reciprocal-based division (within 2 ulp): these coefficients only
+// drive the FP32 smoother and restriction of the mixed-precision cycle, whose
+// result is corrected against the FP64 operator.
+template <typename T>
+__device__ __forceinline__ T rho_face(T k, T ra, T rb) {
+  if constexpr (std::is_same<T, float>::value) return __fdividef(k, ra + rb);
+  else return k / (ra + rb);
+}
+
+// stencil() with the coefficients computed from the density (same order).
+template <typename T>
+__device__ __forceinline__ void stencil_rho(const LevelView<T>& L, const T* __restrict__ p, int i,
+                                            int j, int k, size_t q, T& s, T& d) {
+  const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+  const T* __restrict__ r = L.rho;
+  const T rc = r[q];
+  T c;
+  s = T(0);
+  d = T(0);
+  if (i > 0) { c = rho_face(L.kx, rc, r[q - 1]); s += c * p[q - 1]; d += c; }
+  if (i < L.nx - 1) { c = rho_face(L.kx, rc, r[q + 1]); s += c * p[q + 1]; d += c; }
+  if (j > 0) { c = rho_face(L.ky, rc, r[q - sy]); s += c * p[q - sy]; d += c; }
+  if (j < L.ny - 1) { c = rho_face(L.ky, rc, r[q + sy]); s += c * p[q + sy]; d += c; }
+  if (k > 0) { c = rho_face(L.kz, rc, r[q - sz]); s += c * p[q - sz]; d += c; }
+  if (k < L.nz - 1) { c = rho_face(L.kz, rc, r[q + sz]); s += c * p[q + sz]; d += c; }
+}
+
+// The diagonal sum_f coe_f alone (same order as stencil_rho).
+template <typename T>
+__device__ __forceinline__ T diag_rho(const LevelView<T>& L, int i, int j, int k, size_t q) {
+  const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
+  const T* __restrict__ r = L.rho;
+  const T rc = r[q];
+  T d = T(0);
+  if (i > 0) d += rho_face(L.kx, rc, r[q - 1]);
+  if (i < L.nx - 1) d += rho_face(L.kx, rc, r[q + 1]);
+  if (j > 0) d += rho_face(L.ky, rc, r[q - sy]);
+  if (j < L.ny - 1) d += rho_face(L.ky, rc, r[q + sy]);
+  if (k > 0) d += rho_face(L.kz, rc, r[q - sz]);
+  if (k < L.nz - 1) d += rho_face(L.kz, rc, r[q + sz]);
+  return d;
+}
+
 // Flux sum sum_f coe_f (p_nb - p_i) of cell (i,j,k), differences first so the
 // rounding is relative to each flux rather than to d |p| (order x-, x+, y-,
 // y+, z-, z+).
@@ -62,7 +107,8 @@ __device__ __forceinline__ T flux_sum(const LevelView<T>& L, const T* __restrict
 // c = -d).  One thread per cell of the colour.
 // kZero: the level's current values are taken as zero (the first colour of
 // the first sweep from a zero initial guess), so p_i = -b_i/d and p is not read.
-template <typename T, bool kIdiag, bool kZero>
+// kRho: coefficients from the density (stencil_rho).
+template <typename T, bool kIdiag, bool kZero, bool kRho>
 __global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
   pdl_enter();
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -72,7 +118,14 @@ __global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
   if (i >= L.nx) return;
   const size_t q = ((size_t)k * L.ny + j) * L.nx + i;
   T s, d;
-  if (kZero) {
+  if (kRho) {
+    if (kZero) {
+      s = T(0);
+      d = diag_rho(L, i, j, k, q);
+    } else {
+      stencil_rho(L, L.sol, i, j, k, q, s, d);
+    }
+  } else if (kZero) {
     const size_t sy = (size_t)L.nx, sz = (size_t)L.nx * L.ny;
     s = T(0);
     d = T(0);
@@ -97,7 +150,7 @@ template <> struct Vec2<double> { using type = double2; };
 // Fused residual + restriction: coarse src = mean over the children of
 // (src - A sol) on the fine level; coarse sol = 0.  One thread per coarse
 // cell; the children are summed in the order z, y, x (the oracle's).
-template <typename T>
+template <typename T, bool kRho>
 __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C, int zero_sol) {
   pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -117,19 +170,38 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
         const size_t q = ((size_t)k * F.ny + j) * F.nx + i0;
         const V2 p = *reinterpret_cast<const V2*>(F.sol + q);
         const V2 b = *reinterpret_cast<const V2*>(F.src + q);
-        const V2 cxp = *reinterpret_cast<const V2*>(F.cx + q);
         const bool xl = i0 > 0, xr = i0 + 2 < F.nx;
         const bool yl = j > 0, yr = j < F.ny - 1, zl = k > 0, zr = k < F.nz - 1;
         const T pl = xl ? F.sol[q - 1] : T(0), pr = xr ? F.sol[q + 2] : T(0);
-        const T cxr = xr ? F.cx[q + 2] : T(0);
         const V2 pym = yl ? *reinterpret_cast<const V2*>(F.sol + q - sy) : zero2;
         const V2 pyp = yr ? *reinterpret_cast<const V2*>(F.sol + q + sy) : zero2;
         const V2 pzm = zl ? *reinterpret_cast<const V2*>(F.sol + q - sz) : zero2;
         const V2 pzp = zr ? *reinterpret_cast<const V2*>(F.sol + q + sz) : zero2;
-        const V2 cym = *reinterpret_cast<const V2*>(F.cy + q);
-        const V2 cyp = yr ? *reinterpret_cast<const V2*>(F.cy + q + sy) : zero2;
-        const V2 czm = *reinterpret_cast<const V2*>(F.cz + q);
-        const V2 czp = zr ? *reinterpret_cast<const V2*>(F.cz + q + sz) : zero2;
+        V2 cxp, cym, cyp, czm, czp;
+        T cxr;
+        if constexpr (kRho) {
+          // the children's faces from the density (walls: 0, never used)
+          const T* __restrict__ rp = F.rho;
+          const V2 r = *reinterpret_cast<const V2*>(rp + q);
+          const auto face2 = [&](T kk, bool has, size_t qn) {
+            if (!has) return zero2;
+            const V2 rn = *reinterpret_cast<const V2*>(rp + qn);
+            return V2{rho_face(kk, r.x, rn.x), rho_face(kk, r.y, rn.y)};
+          };
+          cxp = V2{xl ? rho_face(F.kx, r.x, rp[q - 1]) : T(0), rho_face(F.kx, r.x, r.y)};
+          cxr = xr ? rho_face(F.kx, r.y, rp[q + 2]) : T(0);
+          cym = face2(F.ky, yl, q - sy);
+          cyp = face2(F.ky, yr, q + sy);
+          czm = face2(F.kz, zl, q - sz);
+          czp = face2(F.kz, zr, q + sz);
+        } else {
+          cxp = *reinterpret_cast<const V2*>(F.cx + q);
+          cxr = xr ? F.cx[q + 2] : T(0);
+          cym = *reinterpret_cast<const V2*>(F.cy + q);
+          cyp = yr ? *reinterpret_cast<const V2*>(F.cy + q + sy) : zero2;
+          czm = *reinterpret_cast<const V2*>(F.cz + q);
+          czp = zr ? *reinterpret_cast<const V2*>(F.cz + q + sz) : zero2;
+        }
         // child x = i0: neighbours x- (pl, cx[i0]), x+ (p.y, cx[i0+1]); same order as stencil()
         {
           T s = T(0), d = T(0), c;
@@ -159,7 +231,8 @@ __global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, LevelView<T> C
           const int i = F.fx * I + dx, j = F.fy * J + dy, k = F.fz * K + dz;
           const size_t q = ((size_t)k * F.ny + j) * F.nx + i;
           T s, d;
-          stencil(F, F.sol, i, j, k, q, s, d);
+          if constexpr (kRho) stencil_rho(F, F.sol, i, j, k, q, s, d);
+          else stencil(F, F.sol, i, j, k, q, s, d);
           acc += F.src[q] - (s - d * F.sol[q]);
         }
   }
@@ -443,12 +516,19 @@ template <typename T>
 void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_guess) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)(L.nx + 1) / 2, 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
+  if constexpr (std::is_same<T, float>::value) {
+    if (L.rho) {
+      if (zero_guess) launch_pdl(k_smooth<T, false, true, true>, grd, blk, 0, s, L, color);
+      else launch_pdl(k_smooth<T, false, false, true>, grd, blk, 0, s, L, color);
+      return;
+    }
+  }
   if (L.idiag) {
-    if (zero_guess) launch_pdl(k_smooth<T, true, true>, grd, blk, 0, s, L, color);
-    else launch_pdl(k_smooth<T, true, false>, grd, blk, 0, s, L, color);
+    if (zero_guess) launch_pdl(k_smooth<T, true, true, false>, grd, blk, 0, s, L, color);
+    else launch_pdl(k_smooth<T, true, false, false>, grd, blk, 0, s, L, color);
   } else {
-    if (zero_guess) launch_pdl(k_smooth<T, false, true>, grd, blk, 0, s, L, color);
-    else launch_pdl(k_smooth<T, false, false>, grd, blk, 0, s, L, color);
+    if (zero_guess) launch_pdl(k_smooth<T, false, true, false>, grd, blk, 0, s, L, color);
+    else launch_pdl(k_smooth<T, false, false, false>, grd, blk, 0, s, L, color);
   }
 }
 
@@ -456,7 +536,13 @@ template <typename T>
 void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, bool zero_sol) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-  launch_pdl(k_restrict<T>, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
+  if constexpr (std::is_same<T, float>::value) {
+    if (F.rho) {
+      launch_pdl(k_restrict<T, true>, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
+      return;
+    }
+  }
+  launch_pdl(k_restrict<T, false>, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
 }
 
 template <typename T>

@@ -44,7 +44,8 @@ def step_rhs(case, solver: PressurePoisson, k, device):
     return solver.divergence(t[0], t[1], t[2], case.dt)
 
 
-def rollout_loss(centers, radii, case, solver: PressurePoisson, steps=None, tol=1e-10):
+def rollout_loss(centers, radii, case, solver: PressurePoisson, steps=None, tol=1e-10,
+                 adjoint_tol=None):
     """J = sum_k |p_k|^2/2 over the rollout; differentiable in centers, radii."""
     steps = case.extra.get("steps", 20) if steps is None else steps
     shift = torch.tensor(case.extra.get("shift", (0.0, 0.0, 0.5)), dtype=centers.dtype,
@@ -54,6 +55,6 @@ def rollout_loss(centers, radii, case, solver: PressurePoisson, steps=None, tol=
         ck = centers + shift * (k * case.dt)
         phi = checkpoint(level_set, ck, radii, case.shape, case.extent, use_reentrant=False)
         b = step_rhs(case, solver, k, centers.device)
-        p = pressure_solve(phi, b, solver, case.eps, case.rho_pos, case.rho_neg, tol)
+        p = pressure_solve(phi, b, solver, case.eps, case.rho_pos, case.rho_neg, tol, adjoint_tol)
         J = J + 0.5 * (p * p).sum()
     return J

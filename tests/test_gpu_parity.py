@@ -278,6 +278,7 @@ def test_tma_sweep_matches_two_colour_sweep(cuda, monkeypatch, idx, scale, krylo
     runs its post-smoother black-first."""
     c = cases.config(idx, scale)
     out = {}
+    monkeypatch.setenv("GBMG_RHO_COEF", "0")  # both read the stored FP32 coefficients
     for levels in ("0", "99"):
         monkeypatch.setenv("GBMG_TMA_LEVELS", levels)
         monkeypatch.setenv("GBMG_TMA_DEFECT", "0" if levels == "0" else "1")
@@ -303,3 +304,25 @@ def test_single_block_bottom_matches_separate_launches(cuda, monkeypatch, precis
     (p0, s0), (p1, s1) = out["0"], out["1"]
     assert s0["cycles"] == s1["cycles"]
     assert rel_l2(p1, p0) <= 1e-12
+
+
+@pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (0, 1, False), (4, 4, True)])
+def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
+    """The FP32 finest-level smoother and restriction computing their face
+    coefficients from the density (the default for an operator set from rho)
+    against the stored FP32 coefficients (GBMG_RHO_COEF=0): the FP32 values
+    differ by a few ulp, so the preconditioner changes slightly; both solves
+    reach the tolerance, agree with the FP64 oracle to tol-scaled accuracy and
+    take the same number of cycles to within one."""
+    c = cases.config(idx, scale)
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("GBMG_RHO_COEF", flag)
+        with solver(c, precision="mixed", krylov=krylov, max_cycles=400) as s:
+            s.ppe_init(c.rho)
+            out[flag] = s.solve(c.b, tol=1e-10)
+    want, _ = orc.mg_solve(c.coef, c.b, tol=1e-13, max_cycles=400, krylov=1)
+    for flag, (p, st) in out.items():
+        assert st["rel_residual"] < 1e-10, flag
+        assert rel_l2(p, want) <= 1e-6, flag
+    assert abs(out["0"][1]["cycles"] - out["1"][1]["cycles"]) <= 1
