@@ -322,3 +322,36 @@ class PressurePoisson:
         cnt = (C.c_int64 * n)()
         self._check(self._L.gbmg_profile(self._h, ms, cnt, n), "profile")
         return {name: (ms[i], cnt[i]) for i, name in enumerate(_lib.PROF_CLASSES)}
+
+
+def div_stats_noalloc(u, v, w, spacing, device=None, stream=None):
+    """(max |div u|, mean |div u|) of face velocities in CUDA float64 tensors,
+    through gbmg_div_stats_noalloc: no handle and no device allocation (the
+    scratch is a static device array).  The first call on a device does a
+    one-time set-up; calls from several host threads at once race on the
+    shared scratch.  Work runs on `stream` (default: torch's current stream)
+    and the call returns after it finished."""
+    L = _lib.load()
+    if torch is None or not all(_is_torch(a) and a.is_cuda for a in (u, v)):
+        raise TypeError("div_stats_noalloc takes CUDA float64 tensors")
+    u3, v3 = _as3(u), _as3(v)
+    nz, ny, nx1 = u3.shape
+    nx = nx1 - 1
+    shape = (nz, ny, nx)
+    fu, _ = _field(u3, (nz, ny, nx + 1))
+    fv, _ = _field(v3, (nz, ny + 1, nx))
+    fw, _ = _field(w if nz > 1 else None, (nz + 1, ny, nx))
+    dx, dy = spacing[0], spacing[1]
+    dz = spacing[2] if len(spacing) > 2 else 1.0
+    g = _lib.Grid(nx, ny, nz, dx, dy, dz)
+    dev = u3.device.index if device is None else device
+    if stream is None:
+        stream = torch.cuda.current_stream(u3.device).cuda_stream
+    mx, mean = C.c_double(), C.c_double()
+    err = C.create_string_buffer(256)
+    rc = L.gbmg_div_stats_noalloc(C.byref(g), fu, fv, fw, C.byref(mx), C.byref(mean), dev,
+                                  stream, err, len(err))
+    if rc != _lib.GBMG_OK:
+        raise GBMGError(f"div_stats_noalloc: {L.gbmg_strerror(rc).decode()}: "
+                        f"{err.value.decode()} (shape {shape})")
+    return mx.value, mean.value

@@ -35,6 +35,7 @@
 #ifndef GBMG_H
 #define GBMG_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -155,6 +156,29 @@ int gbmg_residual(gbmg_handle* h, gbmg_field b, gbmg_field p, gbmg_field r, doub
  * ("Two phase flows/newOpenMP/2D/src/ns_solver/ns_solvers.f90:55-83"). */
 int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double* max_div,
                    double* mean_div, int mem);
+
+/* gbmg_div_stats without a handle and without allocating (no counterpart in
+ * the reference; the statistics are those of ns_check_convergence_div).  For
+ * callers that must not allocate device memory while they run: a time loop
+ * that checks the divergence after every step while other streams keep working
+ * (cudaFree synchronizes the whole device, so an allocating check would stall
+ * them each step), and a code whose device memory is committed to its own
+ * fields, with no room for the multigrid hierarchy gbmg_create allocates.
+ * u, v, w: DEVICE arrays in the MAC layout above (w ignored when nz = 1);
+ * device: CUDA device (-1 = current); stream: cudaStream_t (NULL = default);
+ * err: optional buffer (err_len bytes) for the error text.
+ * The scratch is a static 33 KB device array: partial sums of at most 2048
+ * blocks (the call needs 8 per SM) plus result slots; grids whose rows of
+ * cells (ny*nz) exceed 2^31 - 1, or a device whose reduction needs more than
+ * 2048 blocks, are rejected with GBMG_INVALID_ARG and a message in err.
+ * The first call on each device does a one-time set-up (takes the scratch's
+ * address, zeroes its counter, synchronizes the stream); make it before any
+ * stream capture.  Calls share the one scratch of their device: two calls in
+ * flight at once (from two host threads) race and corrupt each other's sums.
+ * Every call returns after its stream has finished it. */
+int gbmg_div_stats_noalloc(const gbmg_grid* grid, gbmg_field u, gbmg_field v, gbmg_field w,
+                           double* max_div, double* mean_div, int device, void* stream,
+                           char* err, size_t err_len);
 
 /* Adjoint of the solve (no reference counterpart: the differentiable
  * projection of this library).  Given the solution p of A p = b and the
