@@ -41,6 +41,9 @@ sys.path.insert(0, ROOT)
 METRIC = "ms per 256³ Poisson solve to 1e-10 rel. residual: FP32-in-FP64 vs FP64 MG"
 TOL = 1e-10
 NU1, NU2 = 2, 2  # V(2,2), the library's default
+# adjoint solves: the right-hand side p - p_t is smooth, so A^+ of it is large
+# and the attainable relative residual is higher than the forward's
+ADJ_TOL = 1e-8
 
 
 def parse():
@@ -300,7 +303,7 @@ def adjoint_section(dev, stream, reps=5, scale=1):
             x = phi.clone().requires_grad_(True)
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(stream)
-            p = pressure_solve(x, b, s, tol=1e-10, **kw)
+            p = pressure_solve(x, b, s, tol=1e-10, adjoint_tol=ADJ_TOL, **kw)
             e1.record(stream)
             loss = 0.5 * ((p - p_t) ** 2).sum()
             loss.backward()
@@ -327,7 +330,7 @@ def adjoint_section(dev, stream, reps=5, scale=1):
         s64.close()
     f, bk = float(np.median(fw)), float(np.median(bw))
     return {"workload": f"{case.name}: {case.shape[2]}x{case.shape[1]} cells, 8 circles, mixed "
-                        "precision, flexible CG, tol 1e-10",
+                        "precision, flexible CG, tol 1e-10 forward, 1e-8 adjoint",
             "forward_ms": f, "backward_ms": bk, "backward_over_forward": bk / f,
             "fd_max_rel_err": max(errs), "fd_directions": len(errs)}
 
@@ -471,7 +474,10 @@ def run_ours(args):
 
     adj = None
     if not args.no_adjoint:
-        adj = adjoint_section(dev, stream, scale=max(1, args.scale))
+        try:
+            adj = adjoint_section(dev, stream, scale=max(1, args.scale))
+        except Exception as exc:  # report, keep the headline line
+            adj = {"error": f"{type(exc).__name__}: {exc}"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

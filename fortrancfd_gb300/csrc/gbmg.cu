@@ -44,6 +44,7 @@ struct Level {
   // (finest level of a mixed solve whose operator came from rho or phi)
   const float* rho32 = nullptr;
   float k32[3] = {0.f, 0.f, 0.f};  // 2/h^2 per axis
+  int split = 0;  // sol32, src32 and rho32 in the colour-split layout
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -85,7 +86,9 @@ struct gbmg_handle {
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   int* derr = nullptr;   // device error flags (TMA wait timeouts)
-  DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B]
+  DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B],
+                                // then [p buffer] with a colour-split e (buffer A)
+  bool dmaps_split = false;     // whether the colour-split entries were made
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
@@ -214,7 +217,7 @@ LevelView<double> v64(const Level& l) {
 }
 LevelView<float> v32(const Level& l) {
   return LevelView<float>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
-                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2]};
+                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split};
 }
 template <typename T>
 LevelView<T> view(const Level& l);
@@ -358,12 +361,14 @@ DwOperator dw_op(const gbmg_handle* h) {
 // p_out = p_in + e, r32 = b - A p_out (double-word), |r|^2 -> slot; pc = p_in buffer.
 void enqueue_defect(gbmg_handle* h, int pc, const float* e, float* r32, int slot) {
   const Level& f = h->lv[0];
-  if (h->dmaps) {
+  const bool split = f.split != 0;
+  if (h->dmaps && (!split || h->dmaps_split)) {
     const int ei = e == nullptr ? 0 : (e == f.buf_a ? 1 : 2);
-    launch_defect_tma(h->stream, h->dmaps[pc * 3 + ei], f.nx, f.ny, f.nz, e != nullptr,
-                      h->pw[1 - pc], r32, h->red, slot, h->derr);
+    const int mi = split && e ? 6 + pc : pc * 3 + ei;
+    launch_defect_tma(h->stream, h->dmaps[mi], f.nx, f.ny, f.nz, e != nullptr, h->pw[1 - pc], r32,
+                      h->red, slot, h->derr, split);
   } else {
-    launch_defect(h->stream, dw_op(h), h->pw[pc], h->pw[1 - pc], e, r32, h->red, slot);
+    launch_defect(h->stream, dw_op(h), h->pw[pc], h->pw[1 - pc], e, r32, h->red, slot, split);
   }
 }
 
@@ -427,16 +432,25 @@ int setup_tma(gbmg_handle* h) {
   f.buf_a = f.sol32;
   const char* ed = std::getenv("GBMG_TMA_DEFECT");
   if (f.nx % 4 == 0 && !(ed && std::atoi(ed) == 0) && defect_tma_init() == 0) {
-    DefectMaps* m = new DefectMaps[6];
+    DefectMaps* m = new DefectMaps[8];
     bool ok = true;
     for (int pc = 0; pc < 2; ++pc)
       for (int ei = 0; ei < 3; ++ei) {
         const float* e = ei == 0 ? nullptr : (ei == 1 ? f.sol32 : f.alt32);
         ok = ok && make_defect_maps(&m[pc * 3 + ei], h->pw[pc], e, h->bw, h->cxw, h->cyw, h->czw,
-                                    f.nx, f.ny, f.nz);
+                                    f.nx, f.ny, f.nz, false);
       }
-    if (ok) h->dmaps = m;
-    else delete[] m;
+    if (ok) {
+      h->dmaps = m;
+      // colour-split e: rows of nx/2 floats must be 16-byte multiples
+      bool oks = f.nx % 8 == 0;
+      for (int pc = 0; pc < 2 && oks; ++pc)
+        oks = make_defect_maps(&m[6 + pc], h->pw[pc], f.sol32, h->bw, h->cxw, h->cyw, h->czw,
+                               f.nx, f.ny, f.nz, true);
+      h->dmaps_split = oks;
+    } else {
+      delete[] m;
+    }
   }
   if (smooth_tma_init() != 0) return GBMG_OK;  // keep the two-colour sweeps
   for (int l = 0; l < h->L && l < want; ++l) {
@@ -621,16 +635,22 @@ int build_hierarchy(gbmg_handle* h) {
 
 // Whether the FP32 finest-level kernels compute their coefficients from the
 // density (on: the operator came from rho/phi; GBMG_RHO_COEF=0 turns it off;
-// the TMA and fused sweeps read stored coefficients).  Captured graphs hold
-// the level views, so a change drops them.
+// the TMA and fused sweeps read stored coefficients), and whether that level
+// is stored colour-split (density form, nx even, x halved by the first
+// coarsening, the level outside the single-block bottom; GBMG_SPLIT=0 turns
+// it off).  Captured graphs hold the level views, so a change drops them.
 void set_rho_form(gbmg_handle* h, bool on) {
   Level& f = h->lv[0];
   bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0;
   if (const char* e = std::getenv("GBMG_RHO_COEF"))
     if (std::atoi(e) == 0) want = false;
+  bool split = want && f.nx % 2 == 0 && h->L > 1 && f.fx == 2 && h->sub_lc > 0;
+  if (const char* e = std::getenv("GBMG_SPLIT"))
+    if (std::atoi(e) == 0) split = false;
   const float* r = want ? h->rho32 : nullptr;
-  if (r != f.rho32) reset_graphs(h);
+  if (r != f.rho32 || (int)split != f.split) reset_graphs(h);
   f.rho32 = r;
+  f.split = split ? 1 : 0;
   const gbmg_grid& g = h->grid;
   f.k32[0] = (float)(2.0 / (g.dx * g.dx));
   f.k32[1] = (float)(2.0 / (g.dy * g.dy));
@@ -647,9 +667,11 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
                           h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
                           h->mixed ? cw : nullptr, bulk_rho));
   h->fine_copies = h->mixed;
-  if (h->mixed)
-    LAUNCH(h, GBMG_PROF_SETUP, launch_double_to_float(h->stream, h->rho, h->rho32, h->n0));
   set_rho_form(h, true);
+  if (h->mixed && f.split)
+    LAUNCH(h, GBMG_PROF_SETUP, launch_to_split(h->stream, h->rho, h->rho32, f.nx, f.ny, f.nz));
+  else if (h->mixed)
+    LAUNCH(h, GBMG_PROF_SETUP, launch_double_to_float(h->stream, h->rho, h->rho32, h->n0));
   GB_TRY(check_launch(h, "face_coef"));
   h->rho_ready = true;
   return build_hierarchy(h);
@@ -709,10 +731,12 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
       f.sol = h->kz; f.src = h->kr;
       GB_TRY(enqueue_vcycle<double>(h, true, zg));
     } else {
-      LAUNCH(h, V, launch_double_to_float(s, h->kr, f.src32, n));
+      if (f.split) LAUNCH(h, V, launch_to_split(s, h->kr, f.src32, f.nx, f.ny, f.nz));
+      else LAUNCH(h, V, launch_double_to_float(s, h->kr, f.src32, n));
       if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
       GB_TRY(enqueue_vcycle<float>(h, true, zg));
-      LAUNCH(h, V, launch_float_to_double(s, f.sol32, h->kz, n));
+      if (f.split) LAUNCH(h, V, launch_from_split(s, f.sol32, h->kz, f.nx, f.ny, f.nz));
+      else LAUNCH(h, V, launch_float_to_double(s, f.sol32, h->kz, n));
     }
     LAUNCH(h, V, launch_sum(s, h->kz, n, h->red, kSlotSum));
     LAUNCH(h, V, launch_shift_by_mean(s, h->kz, h->kz, n, h->red, kSlotSum, -1));

@@ -34,6 +34,9 @@ struct LevelView {
   // kx / (rho_a + rho_b) with kx = 2/dx^2, and cx, cy, cz are not read.
   const T* rho = nullptr;
   T kx = T(0), ky = T(0), kz = T(0);
+  // sol, src and rho in the colour-split layout (FP32 finest level, density
+  // form, nx even): cell (i,j,k) at ((i+j+k)&1)*n/2 + q/2, q the natural index
+  int split = 0;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,
@@ -138,6 +141,14 @@ void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, 
                      int64_t sy, int64_t sz);
 // c32 / cw: optional arrays of 3 pointers (x, y, z) for the FP32 and
 // double-word copies, written in the same pass.
+// ---- colour-split FP32 finest level (kernels_split.cu) ----
+void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess);
+void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
+                           bool zero_sol);
+void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C);
+void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz);
+void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz);
+
 // bulk_rho: the two bulk densities (rho_pos, rho_neg of the level set), or
 // null; faces between two bulk cells use host-computed values.
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
@@ -185,19 +196,21 @@ struct DwOperator {
   const float2* b;
 };
 dim3 defect_grid(int nx, int ny, int nz);
-// p_out = p_in + e (e may be null), r32 = float(b - A p_out), slot <- sum r^2
+// p_out = p_in + e (e may be null), r32 = float(b - A p_out), slot <- sum r^2;
+// split: e and r32 in the colour-split layout
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
-                   const float* e, float* r32, const ReduceScratch& R, int slot);
+                   const float* e, float* r32, const ReduceScratch& R, int slot, bool split);
 // TMA-fed k_defect (finest level with nx % 4 == 0): maps of p, e, b, cx, cy, cz.
 struct DefectMaps {
   CUtensorMap p, e, b, cx, cy, cz;
 };
 bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
                       const float2* cx, const float2* cy, const float2* cz, int nx, int ny,
-                      int nz);
+                      int nz, bool split_e);
 int defect_tma_init();
 void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
-                       float2* pout, float* r32, const ReduceScratch& R, int slot, int* err);
+                       float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
+                       bool split);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
 // out = double(p) - result[slot]/n

@@ -517,6 +517,10 @@ void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_g
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)(L.nx + 1) / 2, 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
   if constexpr (std::is_same<T, float>::value) {
+    if (L.split) {
+      launch_smooth_split(s, L, color, zero_guess);
+      return;
+    }
     if (L.rho) {
       if (zero_guess) launch_pdl(k_smooth<T, false, true, true>, grd, blk, 0, s, L, color);
       else launch_pdl(k_smooth<T, false, false, true>, grd, blk, 0, s, L, color);
@@ -537,6 +541,10 @@ void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& 
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
   if constexpr (std::is_same<T, float>::value) {
+    if (F.split) {
+      launch_restrict_split(s, F, C, zero_sol);
+      return;
+    }
     if (F.rho) {
       launch_pdl(k_restrict<T, true>, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
       return;
@@ -549,6 +557,12 @@ template <typename T>
 void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+  if constexpr (std::is_same<T, float>::value) {
+    if (F.split) {
+      launch_prolong_split(s, F, C);
+      return;
+    }
+  }
   launch_pdl(k_prolong<T>, grd, blk, 0, s, F, C);
 }
 
