@@ -45,6 +45,7 @@ struct Level {
   const float* rho32 = nullptr;
   float k32[3] = {0.f, 0.f, 0.f};  // 2/h^2 per axis
   int split = 0;  // sol32, src32 and rho32 in the colour-split layout
+  size_t hstride = 0;  // distance between the colour halves (elements)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -217,7 +218,8 @@ LevelView<double> v64(const Level& l) {
 }
 LevelView<float> v32(const Level& l) {
   return LevelView<float>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
-                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split};
+                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split,
+                          l.hstride};
 }
 template <typename T>
 LevelView<T> view(const Level& l);
@@ -362,13 +364,14 @@ DwOperator dw_op(const gbmg_handle* h) {
 void enqueue_defect(gbmg_handle* h, int pc, const float* e, float* r32, int slot) {
   const Level& f = h->lv[0];
   const bool split = f.split != 0;
+  const size_t hs = split ? f.hstride : 0;
   if (h->dmaps && (!split || h->dmaps_split)) {
     const int ei = e == nullptr ? 0 : (e == f.buf_a ? 1 : 2);
     const int mi = split && e ? 6 + pc : pc * 3 + ei;
     launch_defect_tma(h->stream, h->dmaps[mi], f.nx, f.ny, f.nz, e != nullptr, h->pw[1 - pc], r32,
-                      h->red, slot, h->derr, split);
+                      h->red, slot, h->derr, hs);
   } else {
-    launch_defect(h->stream, dw_op(h), h->pw[pc], h->pw[1 - pc], e, r32, h->red, slot, split);
+    launch_defect(h->stream, dw_op(h), h->pw[pc], h->pw[1 - pc], e, r32, h->red, slot, hs);
   }
 }
 
@@ -438,19 +441,10 @@ int setup_tma(gbmg_handle* h) {
       for (int ei = 0; ei < 3; ++ei) {
         const float* e = ei == 0 ? nullptr : (ei == 1 ? f.sol32 : f.alt32);
         ok = ok && make_defect_maps(&m[pc * 3 + ei], h->pw[pc], e, h->bw, h->cxw, h->cyw, h->czw,
-                                    f.nx, f.ny, f.nz, false);
+                                    f.nx, f.ny, f.nz, 0);
       }
-    if (ok) {
-      h->dmaps = m;
-      // colour-split e: rows of nx/2 floats must be 16-byte multiples
-      bool oks = f.nx % 8 == 0;
-      for (int pc = 0; pc < 2 && oks; ++pc)
-        oks = make_defect_maps(&m[6 + pc], h->pw[pc], f.sol32, h->bw, h->cxw, h->cyw, h->czw,
-                               f.nx, f.ny, f.nz, true);
-      h->dmaps_split = oks;
-    } else {
-      delete[] m;
-    }
+    if (ok) h->dmaps = m;  // the colour-split entries 6, 7 are made by set_rho_form
+    else delete[] m;
   }
   if (smooth_tma_init() != 0) return GBMG_OK;  // keep the two-colour sweeps
   for (int l = 0; l < h->L && l < want; ++l) {
@@ -504,12 +498,15 @@ int allocate(gbmg_handle* h) {
       GB_TRY(dmalloc(h, &v.src, v.n));
     }
     if (h->mixed) {
+      // the finest level's unknown and right-hand side may be stored
+      // colour-split, with a pad between the halves
+      const size_t nv = l == 0 ? v.n + kSplitPadMax : v.n;
       GB_TRY(dmalloc(h, &v.cx32, v.n));
       GB_TRY(dmalloc(h, &v.cy32, v.n));
       GB_TRY(dmalloc(h, &v.cz32, v.n));
-      GB_TRY(dmalloc(h, &v.sol32, v.n));
+      GB_TRY(dmalloc(h, &v.sol32, nv));
       GB_TRY(dmalloc(h, &v.alt32, v.n));
-      GB_TRY(dmalloc(h, &v.src32, v.n));
+      GB_TRY(dmalloc(h, &v.src32, nv));
     }
   }
   (void)need64;
@@ -518,7 +515,7 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->p, h->n0));
   GB_TRY(dmalloc(h, &h->rho, h->n0));
   if (h->mixed) {
-    GB_TRY(dmalloc(h, &h->rho32, h->n0));
+    GB_TRY(dmalloc(h, &h->rho32, h->n0 + kSplitPadMax));
     GB_TRY(dmalloc(h, &h->pw[0], h->n0));
     GB_TRY(dmalloc(h, &h->pw[1], h->n0));
     GB_TRY(dmalloc(h, &h->bw, h->n0));
@@ -634,23 +631,38 @@ int build_hierarchy(gbmg_handle* h) {
 }
 
 // Whether the FP32 finest-level kernels compute their coefficients from the
-// density (on: the operator came from rho/phi; GBMG_RHO_COEF=0 turns it off;
-// the TMA and fused sweeps read stored coefficients), and whether that level
+// density (GBMG_RHO_COEF=1 and an operator from rho/phi; the TMA and fused
+// sweeps read stored coefficients), and whether that level
 // is stored colour-split (density form, nx even, x halved by the first
 // coarsening, the level outside the single-block bottom; GBMG_SPLIT=0 turns
 // it off).  Captured graphs hold the level views, so a change drops them.
 void set_rho_form(gbmg_handle* h, bool on) {
   Level& f = h->lv[0];
   bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0;
-  if (const char* e = std::getenv("GBMG_RHO_COEF"))
-    if (std::atoi(e) == 0) want = false;
+  const char* ev = std::getenv("GBMG_RHO_COEF");  // opt-in: GBMG_RHO_COEF=1
+  if (!ev || std::atoi(ev) == 0) want = false;
   bool split = want && f.nx % 2 == 0 && h->L > 1 && f.fx == 2 && h->sub_lc > 0;
   if (const char* e = std::getenv("GBMG_SPLIT"))
     if (std::atoi(e) == 0) split = false;
+  // the halves sit n/2 + pad apart (pad a multiple of 4 floats: 16-byte
+  // aligned halves for the TMA maps); GBMG_SPLIT_PAD overrides the pad
+  size_t pad = 4128;
+  if (const char* e = std::getenv("GBMG_SPLIT_PAD")) pad = (size_t)std::max(0, std::atoi(e));
+  pad = std::min(pad, kSplitPadMax) & ~size_t(3);
+  const size_t hs = split ? f.n / 2 + pad : 0;
   const float* r = want ? h->rho32 : nullptr;
-  if (r != f.rho32 || (int)split != f.split) reset_graphs(h);
+  if (r != f.rho32 || (int)split != f.split || hs != f.hstride) reset_graphs(h);
+  if (split && h->dmaps && hs != f.hstride) {
+    // colour-split e maps (rows of nx/2 floats must be 16-byte multiples)
+    bool oks = f.nx % 8 == 0;
+    for (int pc = 0; pc < 2 && oks; ++pc)
+      oks = make_defect_maps(&h->dmaps[6 + pc], h->pw[pc], f.sol32, h->bw, h->cxw, h->cyw, h->czw,
+                             f.nx, f.ny, f.nz, hs);
+    h->dmaps_split = oks;
+  }
   f.rho32 = r;
   f.split = split ? 1 : 0;
+  f.hstride = hs;
   const gbmg_grid& g = h->grid;
   f.k32[0] = (float)(2.0 / (g.dx * g.dx));
   f.k32[1] = (float)(2.0 / (g.dy * g.dy));
@@ -669,7 +681,8 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   h->fine_copies = h->mixed;
   set_rho_form(h, true);
   if (h->mixed && f.split)
-    LAUNCH(h, GBMG_PROF_SETUP, launch_to_split(h->stream, h->rho, h->rho32, f.nx, f.ny, f.nz));
+    LAUNCH(h, GBMG_PROF_SETUP,
+           launch_to_split(h->stream, h->rho, h->rho32, f.nx, f.ny, f.nz, f.hstride));
   else if (h->mixed)
     LAUNCH(h, GBMG_PROF_SETUP, launch_double_to_float(h->stream, h->rho, h->rho32, h->n0));
   GB_TRY(check_launch(h, "face_coef"));
@@ -731,11 +744,12 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
       f.sol = h->kz; f.src = h->kr;
       GB_TRY(enqueue_vcycle<double>(h, true, zg));
     } else {
-      if (f.split) LAUNCH(h, V, launch_to_split(s, h->kr, f.src32, f.nx, f.ny, f.nz));
+      if (f.split) LAUNCH(h, V, launch_to_split(s, h->kr, f.src32, f.nx, f.ny, f.nz, f.hstride));
       else LAUNCH(h, V, launch_double_to_float(s, h->kr, f.src32, n));
       if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
       GB_TRY(enqueue_vcycle<float>(h, true, zg));
-      if (f.split) LAUNCH(h, V, launch_from_split(s, f.sol32, h->kz, f.nx, f.ny, f.nz));
+      if (f.split)
+        LAUNCH(h, V, launch_from_split(s, f.sol32, h->kz, f.nx, f.ny, f.nz, f.hstride));
       else LAUNCH(h, V, launch_float_to_double(s, f.sol32, h->kz, n));
     }
     LAUNCH(h, V, launch_sum(s, h->kz, n, h->red, kSlotSum));

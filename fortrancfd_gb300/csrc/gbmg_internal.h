@@ -35,8 +35,10 @@ struct LevelView {
   const T* rho = nullptr;
   T kx = T(0), ky = T(0), kz = T(0);
   // sol, src and rho in the colour-split layout (FP32 finest level, density
-  // form, nx even): cell (i,j,k) at ((i+j+k)&1)*n/2 + q/2, q the natural index
+  // form, nx even): cell (i,j,k) at ((i+j+k)&1)*hstride + q/2, q the natural
+  // index, hstride >= n/2 the distance between the two colour halves
   int split = 0;
+  size_t hstride = 0;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,
@@ -146,8 +148,12 @@ void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, b
 void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
                            bool zero_sol);
 void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C);
-void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz);
-void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz);
+void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz,
+                     size_t hstride);
+void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz,
+                       size_t hstride);
+// elements reserved past n in each split FP32 finest-level array for the pad
+constexpr size_t kSplitPadMax = 65536;
 
 // bulk_rho: the two bulk densities (rho_pos, rho_neg of the level set), or
 // null; faces between two bulk cells use host-computed values.
@@ -199,18 +205,19 @@ dim3 defect_grid(int nx, int ny, int nz);
 // p_out = p_in + e (e may be null), r32 = float(b - A p_out), slot <- sum r^2;
 // split: e and r32 in the colour-split layout
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
-                   const float* e, float* r32, const ReduceScratch& R, int slot, bool split);
+                   const float* e, float* r32, const ReduceScratch& R, int slot, size_t hstride);
 // TMA-fed k_defect (finest level with nx % 4 == 0): maps of p, e, b, cx, cy, cz.
 struct DefectMaps {
   CUtensorMap p, e, b, cx, cy, cz;
+  CUtensorMap e1;  // colour-split e: e holds the colour-0 half, e1 the colour-1 half
 };
 bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
                       const float2* cx, const float2* cy, const float2* cz, int nx, int ny,
-                      int nz, bool split_e);
+                      int nz, size_t split_hstride);
 int defect_tma_init();
 void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
-                       bool split);
+                       size_t hstride);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
 // out = double(p) - result[slot]/n

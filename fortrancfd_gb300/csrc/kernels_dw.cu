@@ -36,16 +36,15 @@ struct DefectRing {
 };
 
 // Index of natural cell q = (k, y, x) in an FP32 finest-level array: the
-// natural index, or the colour-split one ((x+y+k)&1)*n/2 + q/2.
-__device__ __forceinline__ size_t fine_index(size_t q, int x, int y, int k, size_t half, int split) {
-  return split ? (size_t)((x + y + k) & 1) * half + (q >> 1) : q;
+// natural index (hstride 0), or the colour-split one ((x+y+k)&1)*hstride + q/2.
+__device__ __forceinline__ size_t fine_index(size_t q, int x, int y, int k, size_t hstride) {
+  return hstride ? (size_t)((x + y + k) & 1) * hstride + (q >> 1) : q;
 }
 
 __device__ __forceinline__ void defect_load(const DwOperator& A, const float2* __restrict__ pin,
                                             float2* __restrict__ pout, const float* __restrict__ e,
                                             DefectRing& R, int k, int x0, int y0, int z0, int z1,
-                                            int tid, int split) {
-  const size_t half = (size_t)A.nx * A.ny * A.nz / 2;
+                                            int tid, size_t hstride) {
   const int slot = k % 3;
   const size_t sz = (size_t)A.nx * A.ny;
   for (int t = tid; t < kDSX * kDSY; t += kDTX * kDTY) {
@@ -55,7 +54,7 @@ __device__ __forceinline__ void defect_load(const DwOperator& A, const float2* _
     if (x >= 0 && x < A.nx && y >= 0 && y < A.ny) {
       const size_t q = (size_t)k * sz + (size_t)y * A.nx + x;
       dw a = dw_ldg(pin + q);
-      if (e) a = dw_add_f(a, __ldg(e + fine_index(q, x, y, k, half, split)));
+      if (e) a = dw_add_f(a, __ldg(e + fine_index(q, x, y, k, hstride)));
       v = make_float2(a.hi, a.lo);
       if (lx >= 1 && lx <= kDTX && ly >= 1 && ly <= kDTY && k >= z0 && k < z1) pout[q] = v;
     }
@@ -67,10 +66,9 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
                                                         float2* __restrict__ pout,
                                                         const float* __restrict__ e,
                                                         float* __restrict__ r32, ReduceScratch R,
-                                                        int slot, int split) {
+                                                        int slot, size_t hstride) {
   pdl_enter();
   __shared__ DefectRing ring;
-  const size_t half = (size_t)A.nx * A.ny * A.nz / 2;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
   const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
   const int z0 = blockIdx.z * kDZ, z1 = min(z0 + kDZ, A.nz);
@@ -78,10 +76,10 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
   const bool mine = x < A.nx && y < A.ny;
   const size_t sy = (size_t)A.nx, sz = (size_t)A.nx * A.ny;
   float s2 = 0.f;
-  if (z0 > 0) defect_load(A, pin, pout, e, ring, z0 - 1, x0, y0, z0, z1, tid, split);
-  defect_load(A, pin, pout, e, ring, z0, x0, y0, z0, z1, tid, split);
+  if (z0 > 0) defect_load(A, pin, pout, e, ring, z0 - 1, x0, y0, z0, z1, tid, hstride);
+  defect_load(A, pin, pout, e, ring, z0, x0, y0, z0, z1, tid, hstride);
   for (int k = z0; k < z1; ++k) {
-    if (k + 1 < A.nz) defect_load(A, pin, pout, e, ring, k + 1, x0, y0, z0, z1, tid, split);
+    if (k + 1 < A.nz) defect_load(A, pin, pout, e, ring, k + 1, x0, y0, z0, z1, tid, hstride);
     __syncthreads();
     if (mine) {
       const int s0 = k % 3, sm = (k + 2) % 3, sp = (k + 1) % 3;
@@ -103,7 +101,7 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
 #undef DW_TERM
       const dw r = dw_sub(dw_ldg(A.b + q), acc.value());
       const float rf = dw_to_float(r);
-      r32[fine_index(q, x, y, k, half, split)] = rf;
+      r32[fine_index(q, x, y, k, hstride)] = rf;
       s2 = fmaf(rf, rf, s2);
     }
     __syncthreads();
@@ -117,8 +115,8 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
 // cx, cy, cz (float pairs, through FP32 maps of doubled x extent, box from
 // x0-2) and e (FP32, box from x0-4) stream into a 4-slot ring two planes ahead
 // of the compute.  With the colour-split finest level, e comes as two boxes
-// (its colour-0 and colour-1 planes, x halved, box from x0/2-4) out of one map
-// over the split array seen as nx/2 x ny x 2nz.  Wall coefficients are stored as zeros and TMA zero-fills
+// (its colour-0 and colour-1 planes, x halved, box from x0/2-4) out of two
+// maps, one per colour half.  Wall coefficients are stored as zeros and TMA zero-fills
 // out-of-range box cells, so x and y walls add exact zeros.
 constexpr int kQBX = kDTX + 4;         // float-pair box width, from x0 - 2
 constexpr int kQBY = kDTY + 2;         // box height, from y0 - 1
@@ -145,9 +143,9 @@ __device__ __forceinline__ float* qtile_e(unsigned char* base, int slot) {
 __global__ void __launch_bounds__(kDTX * kDTY, 3)
     k_defect_tma(const __grid_constant__ DefectMaps maps, int nx, int ny, int nz, int use_e,
                  float2* __restrict__ pout, float* __restrict__ r32, ReduceScratch R, int slot,
-                 int* err, int split) {
+                 int* err, size_t hstride) {
   pdl_enter();
-  const size_t half = (size_t)nx * ny * nz / 2;
+  const bool split = hstride != 0;
   extern __shared__ unsigned char dsm_raw[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(dsm_raw) + 127) & ~uintptr_t(127));
@@ -174,7 +172,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
     tma_load_3d(qtile(base, s, 4), &maps.cz, xq, yq, k, &bar[s]);
     if (use_e && split) {
       tma_load_3d(qtile_e(base, s), &maps.e, (x0 >> 1) - 4, yq, k, &bar[s]);
-      tma_load_3d(qtile_e(base, s) + kQSEOff, &maps.e, (x0 >> 1) - 4, yq, nz + k, &bar[s]);
+      tma_load_3d(qtile_e(base, s) + kQSEOff, &maps.e1, (x0 >> 1) - 4, yq, k, &bar[s]);
     } else if (use_e) {
       tma_load_3d(qtile_e(base, s), &maps.e, x0 - 4, yq, k, &bar[s]);
     }
@@ -241,7 +239,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       const dw r = dw_sub(dw{b2.x, b2.y}, acc.value());
       const size_t q = ((size_t)k * ny + y) * nx + x;
       const float rf = dw_to_float(r);
-      r32[fine_index(q, x, y, k, half, split)] = rf;
+      r32[fine_index(q, x, y, k, hstride)] = rf;
       pout[q] = P[t];
       s2 = fmaf(rf, rf, s2);
     }
@@ -291,14 +289,14 @@ dim3 defect_grid(int nx, int ny, int nz) {
 }
 
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
-                   const float* e, float* r32, const ReduceScratch& R, int slot, bool split) {
+                   const float* e, float* r32, const ReduceScratch& R, int slot, size_t hstride) {
   launch_pdl(k_defect, defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s, A, pin, pout, e,
-             r32, R, slot, split ? 1 : 0);
+             r32, R, slot, hstride);
 }
 
 bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,
                       const float2* cx, const float2* cy, const float2* cz, int nx, int ny,
-                      int nz, bool split_e) {
+                      int nz, size_t split_hstride) {
   const CUtensorMapDataType f32 = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   const int nx2 = 2 * nx, bx2 = 2 * kQBX;
   bool ok = make_tensor_map_3d(&m->p, p, f32, 4, nx2, ny, nz, bx2, kQBY) &&
@@ -306,9 +304,16 @@ bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const floa
             make_tensor_map_3d(&m->cx, cx, f32, 4, nx2, ny, nz, bx2, kQBY) &&
             make_tensor_map_3d(&m->cy, cy, f32, 4, nx2, ny, nz, bx2, kQBY) &&
             make_tensor_map_3d(&m->cz, cz, f32, 4, nx2, ny, nz, bx2, kQBY);
-  if (e && split_e) ok = ok && make_tensor_map_3d(&m->e, e, f32, 4, nx / 2, ny, 2 * nz, kQSEX, kQBY);
-  else if (e) ok = ok && make_tensor_map_3d(&m->e, e, f32, 4, nx, ny, nz, kQEX, kQBY);
-  else m->e = m->p;
+  if (e && split_hstride) {
+    ok = ok && make_tensor_map_3d(&m->e, e, f32, 4, nx / 2, ny, nz, kQSEX, kQBY) &&
+         make_tensor_map_3d(&m->e1, e + split_hstride, f32, 4, nx / 2, ny, nz, kQSEX, kQBY);
+  } else if (e) {
+    ok = ok && make_tensor_map_3d(&m->e, e, f32, 4, nx, ny, nz, kQEX, kQBY);
+    m->e1 = m->e;
+  } else {
+    m->e = m->p;
+    m->e1 = m->p;
+  }
   return ok;
 }
 
@@ -321,9 +326,9 @@ int defect_tma_init() {
 
 void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, int nz, bool use_e,
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
-                       bool split) {
+                       size_t hstride) {
   launch_pdl(k_defect_tma, defect_grid(nx, ny, nz), dim3(kDTX, kDTY), kQSmem, s, maps, nx, ny, nz,
-             use_e ? 1 : 0, pout, r32, R, slot, err, split ? 1 : 0);
+             use_e ? 1 : 0, pout, r32, R, slot, err, hstride);
 }
 
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {

@@ -134,29 +134,38 @@ __global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, doubl
 }
 
 // b = div(u)/dt with MAC faces: u(f,j,k) on the x-face at f*dx, f = 0..nx.
+// x / h, as a product with the exact reciprocal when h is a power of two
+// (bit-identical to the division and without its FP64 cost); pow2 is the
+// host's is_pow2(h), ih = 1/h.
+__device__ __forceinline__ double over(double x, double h, double ih, bool pow2) {
+  return pow2 ? x * ih : x / h;
+}
+
 __global__ void __launch_bounds__(256) k_divergence(int nx, int ny, int nz, Strided u, Strided v,
-                                                    Strided w, double dx, double dy,
-                                                    double dz, double dt, double* b) {
+                                                    Strided w, double3 h, double3 ih, int pow2,
+                                                    double dt, double* b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const int64_t qu = i + j * u.sy + k * u.sz;
   const int64_t qv = i + j * v.sy + k * v.sz;
-  double d = (u.data[qu + 1] - u.data[qu]) / dx + (v.data[qv + v.sy] - v.data[qv]) / dy;
+  double d = over(u.data[qu + 1] - u.data[qu], h.x, ih.x, pow2 & 1) +
+             over(v.data[qv + v.sy] - v.data[qv], h.y, ih.y, pow2 & 2);
   if (w.data) {
     const int64_t qw = i + j * w.sy + k * w.sz;
-    d += (w.data[qw + w.sz] - w.data[qw]) / dz;
+    d += over(w.data[qw + w.sz] - w.data[qw], h.z, ih.z, pow2 & 4);
   }
   b[((size_t)k * ny + j) * nx + i] = d / dt;
 }
 
 // u_f -= dt (p_i - p_{i-1})/dx / ((rho_i + rho_{i-1})/2) on every interior
 // face; each cell corrects its low faces.
+// (halving is exact, so /2 is taken as *0.5)
 __global__ void __launch_bounds__(256) k_correct(int nx, int ny, int nz,
                                                  const double* __restrict__ rho,
-                                                 const double* __restrict__ p, double dx,
-                                                 double dy, double dz, double dt, double* u,
+                                                 const double* __restrict__ p, double3 h,
+                                                 double3 ih, int pow2, double dt, double* u,
                                                  int64_t usy, int64_t usz, double* v, int64_t vsy,
                                                  int64_t vsz, double* w, int64_t wsy, int64_t wsz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -165,19 +174,19 @@ __global__ void __launch_bounds__(256) k_correct(int nx, int ny, int nz,
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
   if (i > 0) {
-    const double rf = (rho[q] + rho[q - 1]) / 2.0;
-    const double px = (p[q] - p[q - 1]) / dx;
+    const double rf = (rho[q] + rho[q - 1]) * 0.5;
+    const double px = over(p[q] - p[q - 1], h.x, ih.x, pow2 & 1);
     u[i + j * usy + k * usz] -= dt * px / rf;
   }
   if (j > 0) {
-    const double rf = (rho[q] + rho[q - nx]) / 2.0;
-    const double py = (p[q] - p[q - nx]) / dy;
+    const double rf = (rho[q] + rho[q - nx]) * 0.5;
+    const double py = over(p[q] - p[q - nx], h.y, ih.y, pow2 & 2);
     v[i + j * vsy + k * vsz] -= dt * py / rf;
   }
   if (k > 0 && w) {
     const size_t sz = (size_t)nx * ny;
-    const double rf = (rho[q] + rho[q - sz]) / 2.0;
-    const double pz = (p[q] - p[q - sz]) / dz;
+    const double rf = (rho[q] + rho[q - sz]) * 0.5;
+    const double pz = over(p[q] - p[q - sz], h.z, ih.z, pow2 & 4);
     w[i + j * wsy + k * wsz] -= dt * pz / rf;
   }
 }
@@ -391,15 +400,20 @@ void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double
 
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                        double dx, double dy, double dz, double dt, double* b) {
-  k_divergence<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, dt, b);
+  const int pow2 = (is_pow2(dx) ? 1 : 0) | (is_pow2(dy) ? 2 : 0) | (is_pow2(dz) ? 4 : 0);
+  k_divergence<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
+      nx, ny, nz, u, v, w, make_double3(dx, dy, dz), make_double3(1.0 / dx, 1.0 / dy, 1.0 / dz),
+      pow2, dt, b);
 }
 
 void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,
                     double dx, double dy, double dz, double dt, double* u, int64_t usy,
                     int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w, int64_t wsy,
                     int64_t wsz) {
-  k_correct<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, rho, p, dx, dy, dz, dt, u, usy,
-                                                     usz, v, vsy, vsz, w, wsy, wsz);
+  const int pow2 = (is_pow2(dx) ? 1 : 0) | (is_pow2(dy) ? 2 : 0) | (is_pow2(dz) ? 4 : 0);
+  k_correct<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
+      nx, ny, nz, rho, p, make_double3(dx, dy, dz), make_double3(1.0 / dx, 1.0 / dy, 1.0 / dz),
+      pow2, dt, u, usy, usz, v, vsy, vsz, w, wsy, wsz);
 }
 
 void launch_adjoint(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,

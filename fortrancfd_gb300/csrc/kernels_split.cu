@@ -7,7 +7,10 @@
 // (p, b, rho) holds the cells of colour 0 ((i+j+k) even) in its first half
 // and those of colour 1 in its second half, each half in natural order with
 // x halved: cell (i, j, k) lives at
-//     ((i + j + k) & 1) * n/2 + ((k*ny + j)*nx + i)/2        (nx even).
+//     ((i + j + k) & 1) * hstride + ((k*ny + j)*nx + i)/2        (nx even),
+// hstride = n/2 plus a small pad, so that the halves do not sit a power of two
+// apart (same-offset accesses to both halves would fall on the same DRAM
+// channels).
 // All six neighbours of a cell are of the other colour, at half-index offsets
 // -1/0 or 0/+1 (x, by the cell's parity), -+nx/2 (y) and -+nx*ny/2 (z), so a
 // colour launch reads the other half of p and rho and its own half of b and
@@ -37,7 +40,7 @@ __global__ void __launch_bounds__(256) k_smooth_split(LevelView<float> L, int co
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (m >= hx || j >= L.ny) return;
-  const size_t half = (size_t)hx * L.ny * L.nz;
+  const size_t half = L.hstride;
   const size_t sy = (size_t)hx, sz = (size_t)hx * L.ny;
   const size_t h = (size_t)k * sz + (size_t)j * sy + m;
   const int par = (j + k + color) & 1;
@@ -76,7 +79,7 @@ __global__ void __launch_bounds__(256) k_restrict_split(LevelView<float> F, Leve
   const int K = blockIdx.z;
   if (I >= C.nx || J >= C.ny) return;
   const int hx = F.nx >> 1;
-  const size_t half = (size_t)hx * F.ny * F.nz;
+  const size_t half = F.hstride;
   const size_t sy = (size_t)hx, sz = (size_t)hx * F.ny;
   float acc = 0.f;
   for (int dz = 0; dz < F.fz; ++dz)
@@ -153,7 +156,7 @@ __global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, Level
   if (F.fy == 2) my = 0.5f * ((J < C.ny - 1 ? e[cq + csy] : ec) - (J > 0 ? e[cq - csy] : ec));
   if (F.fz == 2) mz = 0.5f * ((K < C.nz - 1 ? e[cq + csz] : ec) - (K > 0 ? e[cq - csz] : ec));
   const int hx = F.nx >> 1;
-  const size_t half = (size_t)hx * F.ny * F.nz;
+  const size_t half = F.hstride;
   for (int dz = 0; dz < F.fz; ++dz)
     for (int dy = 0; dy < F.fy; ++dy) {
       const int j = F.fy * J + dy, k = F.fz * K + dz;
@@ -171,24 +174,22 @@ __global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, Level
 
 // double (natural) -> float (split), and float (split) -> double (natural)
 __global__ void k_to_split(const double* __restrict__ a, float* __restrict__ out, int nx, int ny,
-                           int nz) {
+                           int nz, size_t half) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
-  const size_t half = (size_t)nx * ny * nz / 2;
   out[(size_t)((i + j + k) & 1) * half + (q >> 1)] = (float)a[q];
 }
 
 __global__ void k_from_split(const float* __restrict__ a, double* __restrict__ out, int nx, int ny,
-                             int nz) {
+                             int nz, size_t half) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
-  const size_t half = (size_t)nx * ny * nz / 2;
   out[q] = (double)a[(size_t)((i + j + k) & 1) * half + (q >> 1)];
 }
 
@@ -214,16 +215,18 @@ void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const Level
   launch_pdl(k_prolong_split, grd, blk, 0, s, F, C);
 }
 
-void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz) {
+void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz,
+                     size_t hstride) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)nx, 32), cdiv((size_t)ny, 8), (unsigned)nz);
-  k_to_split<<<grd, blk, 0, s>>>(a, out, nx, ny, nz);
+  k_to_split<<<grd, blk, 0, s>>>(a, out, nx, ny, nz, hstride);
 }
 
-void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz) {
+void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz,
+                       size_t hstride) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)nx, 32), cdiv((size_t)ny, 8), (unsigned)nz);
-  k_from_split<<<grd, blk, 0, s>>>(a, out, nx, ny, nz);
+  k_from_split<<<grd, blk, 0, s>>>(a, out, nx, ny, nz, hstride);
 }
 
 }  // namespace gbmg
