@@ -30,7 +30,7 @@ EXPORTS = (
     "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence", "gbmg_residual",
     "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims", "gbmg_kernel_launches",
     "gbmg_strerror", "gbmg_last_error", "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint",
-    "gbmg_div_stats_noalloc",
+    "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -111,6 +111,9 @@ def load(build_if_missing: bool = True):
         L.gbmg_adjoint.argtypes = [H, Field, Field, Field, C.c_double, C.c_double, C.c_double,
                                    Field, Field, C.c_int]
         L.gbmg_profile.argtypes = [H, P(C.c_double), P(C.c_int64), C.c_int32]
+        L.gbmg_set_split.argtypes = [H, Field, C.c_double, C.c_int]
+        L.gbmg_project_split.argtypes = [H, Field, Field, Field, Field, Field, C.c_double,
+                                         C.c_double, C.c_int, P(Stats)]
         L.gbmg_div_stats_noalloc.argtypes = [P(Grid), Field, Field, Field, P(C.c_double),
                                              P(C.c_double), C.c_int, C.c_void_p, C.c_char_p,
                                              C.c_size_t]
@@ -118,7 +121,7 @@ def load(build_if_missing: bool = True):
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",
                      "gbmg_residual", "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims",
                      "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint",
-                     "gbmg_div_stats_noalloc"):
+                     "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split"):
             getattr(L, name).restype = C.c_int
         _lib = L
         return _lib

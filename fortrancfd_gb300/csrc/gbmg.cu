@@ -105,6 +105,8 @@ struct gbmg_handle {
   bool coef_ready = false;
   bool fine_copies = false;  // finest FP32 / double-word coefficients already written
   bool rho_ready = false;
+  bool split_ready = false;  // gbmg_set_split: constant Laplacian + density for the split source
+  double split_rho12 = 0.0;
   std::string err;
 };
 
@@ -679,6 +681,7 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
                           h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
                           h->mixed ? cw : nullptr, bulk_rho));
   h->fine_copies = h->mixed;
+  h->split_ready = false;
   set_rho_form(h, true);
   if (h->mixed && f.split)
     LAUNCH(h, GBMG_PROF_SETUP,
@@ -907,6 +910,32 @@ int begin(gbmg_handle* h) {
   return GBMG_OK;
 }
 
+// Face velocities on the device: the caller's arrays (device memory) or
+// staging copies of them (host memory).
+int stage_velocity(gbmg_handle* h, const gbmg_field* const fv[3], bool has_w, int mem,
+                   double* dv[3], gbmg_field dfield[3]) {
+  const gbmg_grid& g = h->grid;
+  const int ext[3][3] = {{g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz}, {g.nx, g.ny, g.nz + 1}};
+  for (int a = 0; a < 3; ++a) {
+    if (a == 2 && !has_w) continue;
+    const size_t n = (size_t)ext[a][0] * ext[a][1] * ext[a][2];
+    if (mem == GBMG_MEM_DEVICE) {
+      dv[a] = fv[a]->data;
+      dfield[a] = *fv[a];
+    } else {
+      if (h->vel_n[a] < n) {
+        dfree(h->vel[a]);
+        GB_TRY(dmalloc(h, &h->vel[a], n));
+        h->vel_n[a] = n;
+      }
+      GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
+      dv[a] = h->vel[a];
+      dfield[a] = gbmg_field{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
+    }
+  }
+  return GBMG_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1043,6 +1072,7 @@ int gbmg_set_coef(gbmg_handle* h, gbmg_field cx, gbmg_field cy, gbmg_field cz, i
     GB_CUDA(h, cudaMemsetAsync(f.cy + (size_t)k * g.nx * g.ny, 0, (size_t)g.nx * sizeof(double),
                                h->stream));
   h->rho_ready = false;
+  h->split_ready = false;
   h->fine_copies = false;
   set_rho_form(h, false);
   GB_TRY(build_hierarchy(h));
@@ -1100,24 +1130,7 @@ int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_
   const gbmg_field* fv[3] = {&u, &v, &w};
   double* dv[3] = {nullptr, nullptr, nullptr};
   gbmg_field dfield[3];
-  for (int a = 0; a < 3; ++a) {
-    if (a == 2 && !has_w) continue;
-    const size_t n = (size_t)ext[a][0] * ext[a][1] * ext[a][2];
-    const bool direct = mem == GBMG_MEM_DEVICE;
-    if (direct) {
-      dv[a] = fv[a]->data;
-      dfield[a] = *fv[a];
-    } else {
-      if (h->vel_n[a] < n) {
-        dfree(h->vel[a]);
-        GB_TRY(dmalloc(h, &h->vel[a], n));
-        h->vel_n[a] = n;
-      }
-      GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
-      dv[a] = h->vel[a];
-      dfield[a] = gbmg_field{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
-    }
-  }
+  GB_TRY(stage_velocity(h, fv, has_w, mem, dv, dfield));
   // b = div(u*)/dt into h->b (the RHS of ppe_sor_solver)
   Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
   Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
@@ -1136,6 +1149,90 @@ int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_
                  has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0);
   h->launches += 1;
   GB_TRY(check_launch(h, "correct"));
+  if (mem == GBMG_MEM_HOST)
+    for (int a = 0; a < 3; ++a) {
+      if (a == 2 && !has_w) continue;
+      GB_TRY(download(h, dv[a], ext[a][0], ext[a][1], ext[a][2], mem, *fv[a]));
+    }
+  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
+  GB_CUDA(h, cudaEventRecord(h->ev1, s));
+  GB_CUDA(h, cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st->ms = ms;
+  return status;
+}
+
+int gbmg_set_split(gbmg_handle* h, gbmg_field rho, double rho_12, int mem) {
+  GB_TRY(begin(h));
+  GB_TRY(validate_field(h, rho, "rho"));
+  if (!(rho_12 > 0)) { h->err = "rho_12 must be > 0"; return GBMG_INVALID_ARG; }
+  const gbmg_grid& g = h->grid;
+  GB_TRY(upload(h, rho, g.nx, g.ny, g.nz, mem, h->rho));
+  Level& f = h->lv[0];
+  float* c32[3] = {f.cx32, f.cy32, f.cz32};
+  float2* cw[3] = {h->cxw, h->cyw, h->czw};
+  LAUNCH(h, GBMG_PROF_SETUP,
+         launch_face_const(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz, f.cx,
+                           f.cy, f.cz, h->mixed ? c32 : nullptr, h->mixed ? cw : nullptr));
+  GB_TRY(check_launch(h, "face_const"));
+  h->fine_copies = h->mixed;
+  set_rho_form(h, false);
+  h->rho_ready = false;  // the operator is not the density's: no plain projection or adjoint
+  GB_TRY(build_hierarchy(h));
+  h->split_ready = true;
+  h->split_rho12 = rho_12;
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_project_split(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w,
+                       gbmg_field p_hat, gbmg_field p, double dt, double tol, int mem,
+                       gbmg_stats* stats) {
+  GB_TRY(begin(h));
+  gbmg_stats local{};
+  gbmg_stats* st = stats ? stats : &local;
+  std::memset(st, 0, sizeof(*st));
+  if (!h->split_ready || !h->coef_ready) {
+    h->err = "the split projection needs gbmg_set_split first";
+    return GBMG_STATE_ERROR;
+  }
+  GB_TRY(validate_field(h, u, "u"));
+  GB_TRY(validate_field(h, v, "v"));
+  GB_TRY(validate_field(h, p_hat, "p_hat"));
+  GB_TRY(validate_field(h, p, "p"));
+  const bool has_w = h->grid.nz > 1;
+  if (has_w) GB_TRY(validate_field(h, w, "w"));
+  if (!(dt > 0) || !(tol > 0)) { h->err = "dt and tol must be > 0"; return GBMG_INVALID_ARG; }
+  const gbmg_grid& g = h->grid;
+  const cudaStream_t s = h->stream;
+  GB_CUDA(h, cudaEventRecord(h->ev0, s));
+  const gbmg_field* fv[3] = {&u, &v, &w};
+  double* dv[3] = {nullptr, nullptr, nullptr};
+  gbmg_field dfield[3];
+  GB_TRY(stage_velocity(h, fv, has_w, mem, dv, dfield));
+  // p^ into aux[0]; the solve starts from it (the reference's mg sol = p%tmp)
+  if (!h->aux[0]) GB_TRY(dmalloc(h, &h->aux[0], h->n0));
+  GB_TRY(upload(h, p_hat, g.nx, g.ny, g.nz, mem, h->aux[0]));
+  Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
+  Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
+  launch_psplit_rhs(s, g.nx, g.ny, g.nz, h->rho, su, sv, sw, h->aux[0], h->split_rho12, g.dx,
+                    g.dy, g.dz, dt, h->b);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "split source"));
+  double bnorm = 0.0;
+  GB_TRY(finish_rhs(h, &bnorm));
+  GB_CUDA(h, cudaMemcpyAsync(h->p, h->aux[0], h->n0 * sizeof(double), cudaMemcpyDeviceToDevice,
+                             s));
+  const int status = solve_internal(h, tol, bnorm, st);
+  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
+  launch_psplit_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, h->aux[0], h->split_rho12, g.dx, g.dy,
+                        g.dz, dt, dv[0], dfield[0].sy, dfield[0].sz, dv[1], dfield[1].sy,
+                        dfield[1].sz, has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0,
+                        has_w ? dfield[2].sz : 0);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "split correction"));
+  const int ext[3][3] = {{g.nx + 1, g.ny, g.nz}, {g.nx, g.ny + 1, g.nz}, {g.nx, g.ny, g.nz + 1}};
   if (mem == GBMG_MEM_HOST)
     for (int a = 0; a < 3; ++a) {
       if (a == 2 && !has_w) continue;

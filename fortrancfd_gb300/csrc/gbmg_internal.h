@@ -143,6 +143,20 @@ void launch_copy_out(cudaStream_t s, int nx, int ny, int nz, const double* src, 
                      int64_t sy, int64_t sz);
 // c32 / cw: optional arrays of 3 pointers (x, y, z) for the FP32 and
 // double-word copies, written in the same pass.
+// ---- pressure-split projection (psplit.cu) ----
+// src = rho_12 div(u*)/dt + the split term of p^ (ppe_mg_solver_src)
+void launch_psplit_rhs(cudaStream_t s, int nx, int ny, int nz, const double* rho, Strided u,
+                       Strided v, Strided w, const double* ph, double rho12, double dx, double dy,
+                       double dz, double dt, double* src);
+// u_f -= dt ((1/rho_12) dp/h + (beta_f - 1/rho_12) dp^/h) (ppe_mg_correction)
+void launch_psplit_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho,
+                           const double* p, const double* ph, double rho12, double dx, double dy,
+                           double dz, double dt, double* u, int64_t usy, int64_t usz, double* v,
+                           int64_t vsy, int64_t vsz, double* w, int64_t wsy, int64_t wsz);
+// constant-coefficient Laplacian: coe = 1/h^2 on interior faces (c32, cw optional)
+void launch_face_const(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
+                       double* cx, double* cy, double* cz, float* const* c32, float2* const* cw);
+
 // ---- colour-split FP32 finest level (kernels_split.cu) ----
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess);
 void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,

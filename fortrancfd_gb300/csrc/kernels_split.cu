@@ -68,6 +68,76 @@ __global__ void __launch_bounds__(256) k_smooth_split(LevelView<float> L, int co
   L.sol[own] = v / d;
 }
 
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ void unpack(float4 v, float (&a)[4]) { a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; }
+
+// k_smooth_split with four cells per thread (half indices m0..m0+3 of a row,
+// nx % 8 == 0): every load is a float4 except the one-element x edge of the
+// window, and the index and bounds work is shared by the four cells.  The
+// per-cell arithmetic is k_smooth_split's, in the same order.
+template <bool kZero>
+__global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int color) {
+  pdl_enter();
+  const int hx = L.nx >> 1;
+  const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (m0 >= hx || j >= L.ny) return;
+  const size_t sy = (size_t)hx, sz = (size_t)hx * L.ny;
+  const size_t h = (size_t)k * sz + (size_t)j * sy + m0;
+  const int par = (j + k + color) & 1;
+  const float* __restrict__ ro = L.rho + (size_t)(1 - color) * L.hstride + h;
+  const float* __restrict__ po = L.sol + (size_t)(1 - color) * L.hstride + h;
+  const size_t own = (size_t)color * L.hstride + h;
+  float rc[4], b[4];
+  unpack(ld4(L.rho + own), rc);
+  unpack(ld4(L.src + own), b);
+  // x window: the other colour's half indices m0-1+par .. m0+3+par
+  float rxm[4], rxp[4], pxm[4] = {0.f, 0.f, 0.f, 0.f}, pxp[4] = {0.f, 0.f, 0.f, 0.f};
+  {
+    float rv[4], pv[4] = {0.f, 0.f, 0.f, 0.f};
+    unpack(ld4(ro), rv);
+    if (!kZero) unpack(ld4(po), pv);
+    float re = 0.f, pe = 0.f;
+    if (par) {
+      if (m0 + 4 < hx) { re = ro[4]; if (!kZero) pe = po[4]; }
+      rxm[0] = rv[0]; rxm[1] = rv[1]; rxm[2] = rv[2]; rxm[3] = rv[3];
+      rxp[0] = rv[1]; rxp[1] = rv[2]; rxp[2] = rv[3]; rxp[3] = re;
+      pxm[0] = pv[0]; pxm[1] = pv[1]; pxm[2] = pv[2]; pxm[3] = pv[3];
+      pxp[0] = pv[1]; pxp[1] = pv[2]; pxp[2] = pv[3]; pxp[3] = pe;
+    } else {
+      if (m0 > 0) { re = ro[-1]; if (!kZero) pe = po[-1]; }
+      rxm[0] = re; rxm[1] = rv[0]; rxm[2] = rv[1]; rxm[3] = rv[2];
+      rxp[0] = rv[0]; rxp[1] = rv[1]; rxp[2] = rv[2]; rxp[3] = rv[3];
+      pxm[0] = pe; pxm[1] = pv[0]; pxm[2] = pv[1]; pxm[3] = pv[2];
+      pxp[0] = pv[0]; pxp[1] = pv[1]; pxp[2] = pv[2]; pxp[3] = pv[3];
+    }
+  }
+  const bool yl = j > 0, yr = j < L.ny - 1, zl = k > 0, zr = k < L.nz - 1;
+  float rym[4] = {}, ryp[4] = {}, rzm[4] = {}, rzp[4] = {};
+  float pym[4] = {}, pyp[4] = {}, pzm[4] = {}, pzp[4] = {};
+  if (yl) { unpack(ld4(ro - sy), rym); if (!kZero) unpack(ld4(po - sy), pym); }
+  if (yr) { unpack(ld4(ro + sy), ryp); if (!kZero) unpack(ld4(po + sy), pyp); }
+  if (zl) { unpack(ld4(ro - sz), rzm); if (!kZero) unpack(ld4(po - sz), pzm); }
+  if (zr) { unpack(ld4(ro + sz), rzp); if (!kZero) unpack(ld4(po + sz), pzp); }
+  float out[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int i = 2 * (m0 + c) + par;
+    float s = 0.f, d = 0.f, cc;
+    if (i > 0) { cc = face(L.kx, rc[c], rxm[c]); if (!kZero) s += cc * pxm[c]; d += cc; }
+    if (i < L.nx - 1) { cc = face(L.kx, rc[c], rxp[c]); if (!kZero) s += cc * pxp[c]; d += cc; }
+    if (yl) { cc = face(L.ky, rc[c], rym[c]); if (!kZero) s += cc * pym[c]; d += cc; }
+    if (yr) { cc = face(L.ky, rc[c], ryp[c]); if (!kZero) s += cc * pyp[c]; d += cc; }
+    if (zl) { cc = face(L.kz, rc[c], rzm[c]); if (!kZero) s += cc * pzm[c]; d += cc; }
+    if (zr) { cc = face(L.kz, rc[c], rzp[c]); if (!kZero) s += cc * pzp[c]; d += cc; }
+    const float v = s - b[c];
+    out[c] = v / d;
+  }
+  st4(L.sol + own, make_float4(out[0], out[1], out[2], out[3]));
+}
+
 // Fused residual + restriction out of the split finest level (fx = 2): one
 // thread per coarse cell; per child row the children x = 2I (colour ca) and
 // x = 2I+1 (colour 1-ca) share the half index of the row plus I.
@@ -140,6 +210,165 @@ __global__ void __launch_bounds__(256) k_restrict_split(LevelView<float> F, Leve
   if (zero_sol) C.sol[cq] = 0.f;
 }
 
+// k_restrict_split for four coarse cells per thread (I0..I0+3, C.nx % 4 == 0):
+// float4 loads of each child row, the same per-cell arithmetic and order.
+__global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, LevelView<float> C,
+                                                         int zero_sol) {
+  pdl_enter();
+  const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I0 >= C.nx || J >= C.ny) return;
+  const int hx = F.nx >> 1;
+  const size_t half = F.hstride;
+  const size_t sy = (size_t)hx, sz = (size_t)hx * F.ny;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int dz = 0; dz < F.fz; ++dz)
+    for (int dy = 0; dy < F.fy; ++dy) {
+      const int j = F.fy * J + dy, k = F.fz * K + dz;
+      const int ca = (j + k) & 1;
+      const size_t h = (size_t)k * sz + (size_t)j * sy + I0;
+      const float* Pa = F.sol + (size_t)ca * half + h;
+      const float* Pb = F.sol + (size_t)(1 - ca) * half + h;
+      const float* Ra = F.rho + (size_t)ca * half + h;
+      const float* Rb = F.rho + (size_t)(1 - ca) * half + h;
+      const bool yl = j > 0, yr = j < F.ny - 1, zl = k > 0, zr = k < F.nz - 1;
+      float pa[4], pb[4], ra[4], rb[4], ba[4], bb[4];
+      unpack(ld4(Pa), pa);
+      unpack(ld4(Pb), pb);
+      unpack(ld4(Ra), ra);
+      unpack(ld4(Rb), rb);
+      unpack(ld4(F.src + (size_t)ca * half + h), ba);
+      unpack(ld4(F.src + (size_t)(1 - ca) * half + h), bb);
+      const bool xl0 = I0 > 0, xr3 = 2 * (I0 + 3) + 2 < F.nx;
+      // x-: cell 2I-1 (b's colour, index I-1); x+ of b: cell 2I+2 (a's colour, I+1)
+      const float pl_e = xl0 ? Pb[-1] : 0.f, rl_e = xl0 ? Rb[-1] : 0.f;
+      const float pr_e = xr3 ? Pa[4] : 0.f, rr_e = xr3 ? Ra[4] : 0.f;
+      float pym_a[4] = {}, pym_b[4] = {}, pyp_a[4] = {}, pyp_b[4] = {};
+      float pzm_a[4] = {}, pzm_b[4] = {}, pzp_a[4] = {}, pzp_b[4] = {};
+      float rym_a[4] = {}, rym_b[4] = {}, ryp_a[4] = {}, ryp_b[4] = {};
+      float rzm_a[4] = {}, rzm_b[4] = {}, rzp_a[4] = {}, rzp_b[4] = {};
+      if (yl) {
+        unpack(ld4(Pb - sy), pym_a); unpack(ld4(Pa - sy), pym_b);
+        unpack(ld4(Rb - sy), rym_a); unpack(ld4(Ra - sy), rym_b);
+      }
+      if (yr) {
+        unpack(ld4(Pb + sy), pyp_a); unpack(ld4(Pa + sy), pyp_b);
+        unpack(ld4(Rb + sy), ryp_a); unpack(ld4(Ra + sy), ryp_b);
+      }
+      if (zl) {
+        unpack(ld4(Pb - sz), pzm_a); unpack(ld4(Pa - sz), pzm_b);
+        unpack(ld4(Rb - sz), rzm_a); unpack(ld4(Ra - sz), rzm_b);
+      }
+      if (zr) {
+        unpack(ld4(Pb + sz), pzp_a); unpack(ld4(Pa + sz), pzp_b);
+        unpack(ld4(Rb + sz), rzp_a); unpack(ld4(Ra + sz), rzp_b);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int I = I0 + c;
+        const bool xl = 2 * I > 0, xr = 2 * I + 2 < F.nx;
+        const float pl = c == 0 ? pl_e : pb[c - 1], rl = c == 0 ? rl_e : rb[c - 1];
+        const float pr = c == 3 ? pr_e : pa[c + 1], rr = c == 3 ? rr_e : ra[c + 1];
+        const float cxa = xl ? face(F.kx, ra[c], rl) : 0.f;
+        const float cab = face(F.kx, ra[c], rb[c]);
+        const float cxr = xr ? face(F.kx, rb[c], rr) : 0.f;
+        const float cym_a = yl ? face(F.ky, ra[c], rym_a[c]) : 0.f;
+        const float cym_b = yl ? face(F.ky, rb[c], rym_b[c]) : 0.f;
+        const float cyp_a = yr ? face(F.ky, ra[c], ryp_a[c]) : 0.f;
+        const float cyp_b = yr ? face(F.ky, rb[c], ryp_b[c]) : 0.f;
+        const float czm_a = zl ? face(F.kz, ra[c], rzm_a[c]) : 0.f;
+        const float czm_b = zl ? face(F.kz, rb[c], rzm_b[c]) : 0.f;
+        const float czp_a = zr ? face(F.kz, ra[c], rzp_a[c]) : 0.f;
+        const float czp_b = zr ? face(F.kz, rb[c], rzp_b[c]) : 0.f;
+        {
+          float s = 0.f, d = 0.f, cc;
+          if (xl) { cc = cxa; s += cc * pl; d += cc; }
+          cc = cab; s += cc * pb[c]; d += cc;
+          if (yl) { cc = cym_a; s += cc * pym_a[c]; d += cc; }
+          if (yr) { cc = cyp_a; s += cc * pyp_a[c]; d += cc; }
+          if (zl) { cc = czm_a; s += cc * pzm_a[c]; d += cc; }
+          if (zr) { cc = czp_a; s += cc * pzp_a[c]; d += cc; }
+          acc[c] += ba[c] - (s - d * pa[c]);
+        }
+        {
+          float s = 0.f, d = 0.f, cc;
+          cc = cab; s += cc * pa[c]; d += cc;
+          if (xr) { cc = cxr; s += cc * pr; d += cc; }
+          if (yl) { cc = cym_b; s += cc * pym_b[c]; d += cc; }
+          if (yr) { cc = cyp_b; s += cc * pyp_b[c]; d += cc; }
+          if (zl) { cc = czm_b; s += cc * pzm_b[c]; d += cc; }
+          if (zr) { cc = czp_b; s += cc * pzp_b[c]; d += cc; }
+          acc[c] += bb[c] - (s - d * pb[c]);
+        }
+      }
+    }
+  const size_t cq = ((size_t)K * C.ny + J) * C.nx + I0;
+  const float sc = 1.f / (float)(F.fx * F.fy * F.fz);
+  st4(C.src + cq, make_float4(acc[0] * sc, acc[1] * sc, acc[2] * sc, acc[3] * sc));
+  if (zero_sol) st4(C.sol + cq, make_float4(0.f, 0.f, 0.f, 0.f));
+}
+
+// k_prolong_split for four coarse cells per thread (C.nx % 4 == 0).
+__global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, LevelView<float> C) {
+  pdl_enter();
+  const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  const int K = blockIdx.z;
+  if (I0 >= C.nx || J >= C.ny) return;
+  const size_t csy = (size_t)C.nx, csz = (size_t)C.nx * C.ny;
+  const size_t cq = (size_t)K * csz + (size_t)J * csy + I0;
+  const float* e = C.sol + cq;
+  float ec[4], eym[4], eyp[4], ezm[4], ezp[4];
+  unpack(ld4(e), ec);
+  const float el = I0 > 0 ? e[-1] : ec[0];
+  const float er = I0 + 4 < C.nx ? e[4] : ec[3];
+  float mx[4], my[4] = {0.f, 0.f, 0.f, 0.f}, mz[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float hi = c == 3 ? er : ec[c + 1];
+    const float lo = c == 0 ? el : ec[c - 1];
+    mx[c] = 0.5f * (hi - lo);
+  }
+  if (F.fy == 2) {
+    if (J < C.ny - 1) unpack(ld4(e + csy), eyp); else unpack(ld4(e), eyp);
+    if (J > 0) unpack(ld4(e - csy), eym); else unpack(ld4(e), eym);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) my[c] = 0.5f * (eyp[c] - eym[c]);
+  }
+  if (F.fz == 2) {
+    if (K < C.nz - 1) unpack(ld4(e + csz), ezp); else unpack(ld4(e), ezp);
+    if (K > 0) unpack(ld4(e - csz), ezm); else unpack(ld4(e), ezm);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) mz[c] = 0.5f * (ezp[c] - ezm[c]);
+  }
+  const int hx = F.nx >> 1;
+  const size_t half = F.hstride;
+  for (int dz = 0; dz < F.fz; ++dz)
+    for (int dy = 0; dy < F.fy; ++dy) {
+      const int j = F.fy * J + dy, k = F.fz * K + dz;
+      const int ca = (j + k) & 1;
+      const size_t h = ((size_t)k * F.ny + j) * hx + I0;
+      float* A = F.sol + (size_t)ca * half + h;
+      float* B = F.sol + (size_t)(1 - ca) * half + h;
+      float a[4], b[4];
+      unpack(ld4(A), a);
+      unpack(ld4(B), b);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float ty = dy ? 0.25f * my[c] : -(0.25f * my[c]);
+        const float tz = dz ? 0.25f * mz[c] : -(0.25f * mz[c]);
+        float v0 = ec[c] + -(0.25f * mx[c]), v1 = ec[c] + 0.25f * mx[c];
+        if (F.fy == 2) { v0 += ty; v1 += ty; }
+        if (F.fz == 2) { v0 += tz; v1 += tz; }
+        a[c] += v0;
+        b[c] += v1;
+      }
+      st4(A, make_float4(a[0], a[1], a[2], a[3]));
+      st4(B, make_float4(b[0], b[1], b[2], b[3]));
+    }
+}
+
 // Prolongation + correction into the split finest level (fx = 2), as k_prolong.
 __global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, LevelView<float> C) {
   pdl_enter();
@@ -195,8 +424,19 @@ __global__ void k_from_split(const float* __restrict__ a, double* __restrict__ o
 
 }  // namespace
 
+// the four-cell kernels need rows of whole float4 groups in each half
+inline bool vec4_ok(const LevelView<float>& F) {
+  return F.nx % 8 == 0 && F.hstride % 4 == 0;
+}
+
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess) {
   const dim3 blk(32, 8, 1);
+  if (vec4_ok(L)) {
+    const dim3 g4(cdiv((size_t)(L.nx / 8), 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
+    if (zero_guess) launch_pdl(k_smooth_split4<true>, g4, blk, 0, s, L, color);
+    else launch_pdl(k_smooth_split4<false>, g4, blk, 0, s, L, color);
+    return;
+  }
   const dim3 grd(cdiv((size_t)(L.nx / 2), 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
   if (zero_guess) launch_pdl(k_smooth_split<true>, grd, blk, 0, s, L, color);
   else launch_pdl(k_smooth_split<false>, grd, blk, 0, s, L, color);
@@ -205,12 +445,22 @@ void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, b
 void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
                            bool zero_sol) {
   const dim3 blk(32, 8, 1);
+  if (vec4_ok(F) && C.nx % 4 == 0) {
+    const dim3 g4(cdiv((size_t)(C.nx / 4), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+    launch_pdl(k_restrict_split4, g4, blk, 0, s, F, C, zero_sol ? 1 : 0);
+    return;
+  }
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
   launch_pdl(k_restrict_split, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
 }
 
 void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C) {
   const dim3 blk(32, 8, 1);
+  if (vec4_ok(F) && C.nx % 4 == 0) {
+    const dim3 g4(cdiv((size_t)(C.nx / 4), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+    launch_pdl(k_prolong_split4, g4, blk, 0, s, F, C);
+    return;
+  }
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
   launch_pdl(k_prolong_split, grd, blk, 0, s, F, C);
 }

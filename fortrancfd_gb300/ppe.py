@@ -221,6 +221,35 @@ class PressurePoisson:
         self._finish(rc, stats, check, "ppe_solver")
         return p, stats
 
+    def ppe_mg_solver_init(self, rho, rho_12):
+        """The pressure-split form of the DomainDecomposition solver
+        (ppe_mg_solver_init): store rho and rho_12 and make the operator the
+        constant-coefficient Laplacian.  ppe_init / rho_mu switch back."""
+        f, m = _field(rho, self.shape)
+        self._sync_torch(rho)
+        self._check(self._L.gbmg_set_split(self._h, f, float(rho_12), m), "ppe_mg_solver_init")
+
+    def ppe_mg_solver(self, u, v, w, dt, p_hat, tol=1e-10, p=None, check=True):
+        """ppe_mg_solver: split source from u* and p_hat, solve the Laplacian
+        from p_hat, ppe_mg_correction on u, v, w in place.  Returns (p, stats)."""
+        if p is None:
+            p = torch.empty_like(p_hat) if _is_torch(p_hat) else np.empty(self.shape)
+        su, sv, sw = self._faces()
+        fu, m1 = _field(u, su)
+        fv, m2 = _field(v, sv)
+        fw, m3 = _field(w if self.shape[0] > 1 else None, sw)
+        fh, m4 = _field(p_hat, self.shape)
+        fp, m5 = _field(p, self.shape)
+        m = _mem_of((fu, m1), (fv, m2), (fh, m4), (fp, m5),
+                    *(((fw, m3),) if m3 is not None else ()))
+        self._sync_torch(u, v, w, p_hat, p)
+        st = _lib.Stats()
+        rc = self._L.gbmg_project_split(self._h, fu, fv, fw, fh, fp, float(dt), float(tol), m,
+                                        C.byref(st))
+        stats = st.as_dict()
+        self._finish(rc, stats, check, "ppe_mg_solver")
+        return p, stats
+
     def _finish(self, rc, stats, check, what):
         if rc in (_lib.GBMG_OK,):
             return

@@ -141,6 +141,26 @@ int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
 int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_field p,
                  double dt, double tol, int mem, gbmg_stats* stats);
 
+/* Pressure-split projection, the form of the DomainDecomposition solver's
+ * pressure step ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90"):
+ * the multigrid solves the constant-coefficient Laplacian
+ *     lap p = rho_12 div(u*)/dt + div((1 - rho_12 beta) grad p_hat)
+ * (ppe_mg_solver_init :62-136 and ppe_mg_solver_src :138-221, with beta =
+ * 2/(rho_i + rho_nb) and zero-gradient ghosts at the walls), then corrects
+ *     u_f -= dt [ (p_nb - p_i)/(rho_12 h) + (beta_f - 1/rho_12)(p_hat_nb - p_hat_i)/h ]
+ * (ppe_mg_correction :223-276).  gbmg_set_split stores the cell density and
+ * rho_12 and makes the handle's operator the Laplacian (coe = 1/h^2, walls
+ * folded); gbmg_set_rho/phi/coef switch back.  gbmg_project_split starts the
+ * solve from p_hat (the reference extrapolates p_hat = 2 p^n - p^{n-1} after
+ * its third step and uses p^n before) and writes the mean-free pressure to
+ * p; wall faces of u, v, w are left as given.  The reference's restarts of a
+ * stagnating stationary cycle (ns_ppe_mg_solver.f90:29-44) are not needed:
+ * the solve runs to the relative residual tol. */
+int gbmg_set_split(gbmg_handle* h, gbmg_field rho, double rho_12, int mem);
+int gbmg_project_split(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w,
+                       gbmg_field p_hat, gbmg_field p, double dt, double tol, int mem,
+                       gbmg_stats* stats);
+
 /* b = div(u)/dt (the right-hand side of ppe_sor_solver, ns_ppe_solver.f90:77-89),
  * without mean removal. */
 int gbmg_divergence(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, double dt,

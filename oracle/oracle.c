@@ -273,6 +273,86 @@ void or_correct(const or_grid* g, const double* rho, const double* p, double dt,
       }
 }
 
+/* ------------------------------------------------------------------------- */
+/* Pressure-split projection of the DomainDecomposition solver                */
+/* (DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90): the constant- */
+/* coefficient Laplacian is solved for p with the split source               */
+/*   src = rho_12 div(u*)/dt + c p^_i + sum_f coe_f p^_nb                      */
+/* (ppe_mg_solver_init :62-136, ppe_mg_solver_src :138-221): coe_f =          */
+/* (1 - 2 rho_12/(rho_i + rho_nb))/h^2 on all six faces, c = -(r+l+f+b+u+d),  */
+/* with the zero-gradient ghosts of job_bc (DomainDecomposition/3D/lib/data/  */
+/* branches.f90:243-288) for rho and p^ at the walls; the terms are added in  */
+/* the reference's order.  nz == 1 drops the z terms (the 2D form).           */
+/* ------------------------------------------------------------------------- */
+void or_split_rhs(const or_grid* g, const double* rho, const double* u, const double* v,
+                  const double* w, const double* ph, double rho12, double dt, double* src) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const double dx2 = g->dx * g->dx, dy2 = g->dy * g->dy, dz2 = g->dz * g->dz;
+  const int three = nz > 1;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t sz = (size_t)nx * ny;
+        const size_t q = ((size_t)k * ny + j) * nx + i;
+        /* neighbour indices with the walls clamped to the cell (ghost = copy) */
+        const size_t qr = i < nx - 1 ? q + 1 : q, ql = i > 0 ? q - 1 : q;
+        const size_t qf = j < ny - 1 ? q + nx : q, qb = j > 0 ? q - nx : q;
+        const size_t qu = k < nz - 1 ? q + sz : q, qd = k > 0 ? q - sz : q;
+        const double r = (1.0 - 2.0 * rho12 / (rho[q] + rho[qr])) / dx2;
+        const double l = (1.0 - 2.0 * rho12 / (rho[q] + rho[ql])) / dx2;
+        const double f = (1.0 - 2.0 * rho12 / (rho[q] + rho[qf])) / dy2;
+        const double b = (1.0 - 2.0 * rho12 / (rho[q] + rho[qb])) / dy2;
+        double up = 0.0, dn = 0.0, c;
+        if (three) {
+          up = (1.0 - 2.0 * rho12 / (rho[q] + rho[qu])) / dz2;
+          dn = (1.0 - 2.0 * rho12 / (rho[q] + rho[qd])) / dz2;
+          c = -(r + l + f + b + up + dn);
+        } else {
+          c = -(r + l + f + b);
+        }
+        const size_t fu = ((size_t)k * ny + j) * (nx + 1) + i;
+        const size_t fv = ((size_t)k * (ny + 1) + j) * nx + i;
+        double d = (u[fu + 1] - u[fu]) / g->dx + (v[fv + nx] - v[fv]) / g->dy;
+        if (three) d += (w[q + sz] - w[q]) / g->dz;
+        d = d / dt;
+        double sv = d * rho12 + c * ph[q] + r * ph[qr] + l * ph[ql] + f * ph[qf] + b * ph[qb];
+        if (three) sv = sv + up * ph[qu] + dn * ph[qd];
+        src[q] = sv;
+      }
+}
+
+/* ppe_mg_correction (ns_ppe_mg_solver.f90:223-276) on the interior faces:    */
+/*   u_f -= dt [ (1/rho_12)(p_nb - p_i)/h + (2/(rho_i+rho_nb) - 1/rho_12)      */
+/*               (p^_nb - p^_i)/h ]                                           */
+/* (wall faces get p and p^ differences of zero from the ghosts and stay).    */
+void or_split_correct(const or_grid* g, const double* rho, const double* p, const double* ph,
+                      double rho12, double dt, double* u, double* v, double* w) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t sz = (size_t)nx * ny;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t q = ((size_t)k * ny + j) * nx + i;
+        if (i < nx - 1) {
+          double s = 1.0 / rho12 * (p[q + 1] - p[q]) / g->dx;
+          s = s + (2.0 / (rho[q] + rho[q + 1]) - 1.0 / rho12) * (ph[q + 1] - ph[q]) / g->dx;
+          u[((size_t)k * ny + j) * (nx + 1) + i + 1] -= s * dt;
+        }
+        if (j < ny - 1) {
+          double s = 1.0 / rho12 * (p[q + nx] - p[q]) / g->dy;
+          s = s + (2.0 / (rho[q] + rho[q + nx]) - 1.0 / rho12) * (ph[q + nx] - ph[q]) / g->dy;
+          v[((size_t)k * (ny + 1) + j + 1) * nx + i] -= s * dt;
+        }
+        if (k < nz - 1 && w) {
+          double s = 1.0 / rho12 * (p[q + sz] - p[q]) / g->dz;
+          s = s + (2.0 / (rho[q] + rho[q + sz]) - 1.0 / rho12) * (ph[q + sz] - ph[q]) / g->dz;
+          w[q + sz] -= s * dt;
+        }
+      }
+}
+
 /* a13: max and mean |div u| (ns_check_convergence_div, NO2/src/ns_solver/ns_solvers.f90:55-83). */
 void or_div_stats(const or_grid* g, const double* u, const double* v, const double* w,
                   double* out_max, double* out_mean) {

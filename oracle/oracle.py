@@ -55,6 +55,10 @@ def lib():
         L.or_residual.restype = C.c_double
         L.or_remove_mean.argtypes = [_D, C.c_int64]
         L.or_correct.argtypes = [C.POINTER(Grid), _D, _D, C.c_double, _D, _D, _D]
+        L.or_split_rhs.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D, C.c_double, C.c_double,
+                                   _D]
+        L.or_split_correct.argtypes = [C.POINTER(Grid), _D, _D, _D, C.c_double, C.c_double, _D,
+                                       _D, _D]
         L.or_div_stats.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D]
         L.or_sor_solve.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D, C.c_double, C.c_double,
                                    C.c_int64, _D]
@@ -147,6 +151,22 @@ def correct(rho, p, dt, u, v, w, spacing):
     g = grid(p.shape, spacing)
     u, v, w = (np.array(a, np.float64, copy=True) for a in (u, v, w))
     lib().or_correct(C.byref(g), _p(rho), _p(p), dt, _p(u), _p(v), _p(w))
+    return u, v, w
+
+
+def split_rhs(rho, u, v, w, p_hat, rho12, dt, spacing):
+    """Source of the pressure-split projection (or_split_rhs)."""
+    g = grid(rho.shape, spacing)
+    src = np.empty_like(rho)
+    lib().or_split_rhs(C.byref(g), _p(rho), _p(u), _p(v), _p(w), _p(p_hat), rho12, dt, _p(src))
+    return src
+
+
+def split_correct(rho, p, p_hat, rho12, dt, u, v, w, spacing):
+    """ppe_mg_correction on copies of u, v, w (or_split_correct)."""
+    g = grid(p.shape, spacing)
+    u, v, w = (np.array(a, np.float64, copy=True) for a in (u, v, w))
+    lib().or_split_correct(C.byref(g), _p(rho), _p(p), _p(p_hat), rho12, dt, _p(u), _p(v), _p(w))
     return u, v, w
 
 

@@ -354,3 +354,78 @@ class DDMultigrid:
             self.v_cycle()
             out.append(unpad(f.sol).copy())
         return out
+
+
+# ---------------------------------------------------------------------------
+# Pressure-split projection of the DomainDecomposition solver
+# ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90"):
+# ppe_mg_solver_init :62-136, ppe_mg_solver_src :138-221,
+# ppe_mg_correction :223-276, on one subdomain with job_bc ghosts.
+# ---------------------------------------------------------------------------
+def ppe_mg_split_src(rho, u, v, w, p_hat, rho_12, dt, dx, dy, dz):
+    """coe%src of ppe_mg_solver_src (after ppe_mg_solver_init); u, v, w in the
+    (nz, ny, nx+1) / (nz, ny+1, nx) / (nz+1, ny, nx) face layout, the
+    reference's vel%x(i) being u[k, j, i] with 1-based i (face i+1/2)."""
+    nz, ny, nx = rho.shape
+    R = pad(rho)
+    T = pad(p_hat)
+    three_d = nz > 1
+    src = np.zeros((nz, ny, nx))
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                r = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i + 1, j, k])
+                l = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i - 1, j, k])
+                f = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i, j + 1, k])
+                b = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i, j - 1, k])
+                r = r / dx ** 2.0
+                l = l / dx ** 2.0
+                f = f / dy ** 2.0
+                b = b / dy ** 2.0
+                if three_d:
+                    uu = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i, j, k + 1])
+                    dd = 1.0 - 2.0 * rho_12 / (R[i, j, k] + R[i, j, k - 1])
+                    uu = uu / dz ** 2.0
+                    dd = dd / dz ** 2.0
+                    c = -(r + l + f + b + uu + dd)
+                    s = ((u[k - 1, j - 1, i] - u[k - 1, j - 1, i - 1]) / dx
+                         + (v[k - 1, j, i - 1] - v[k - 1, j - 1, i - 1]) / dy
+                         + (w[k, j - 1, i - 1] - w[k - 1, j - 1, i - 1]) / dz) / dt
+                    s = (s * rho_12 + c * T[i, j, k]
+                         + r * T[i + 1, j, k] + l * T[i - 1, j, k]
+                         + f * T[i, j + 1, k] + b * T[i, j - 1, k]
+                         + uu * T[i, j, k + 1] + dd * T[i, j, k - 1])
+                else:
+                    c = -(r + l + f + b)
+                    s = ((u[k - 1, j - 1, i] - u[k - 1, j - 1, i - 1]) / dx
+                         + (v[k - 1, j, i - 1] - v[k - 1, j - 1, i - 1]) / dy) / dt
+                    s = (s * rho_12 + c * T[i, j, k]
+                         + r * T[i + 1, j, k] + l * T[i - 1, j, k]
+                         + f * T[i, j + 1, k] + b * T[i, j - 1, k])
+                src[k - 1, j - 1, i - 1] = s
+    return src
+
+
+def ppe_mg_split_correction(rho, p, p_hat, u, v, w, rho_12, dt, dx, dy, dz):
+    """ppe_mg_correction on copies of u, v, w (every cell's high faces; the
+    wall faces see zero differences through the ghosts)."""
+    nz, ny, nx = rho.shape
+    R, P, T = pad(rho), pad(p), pad(p_hat)
+    u, v, w = u.copy(), v.copy(), w.copy()
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                s = 1.0 / rho_12 * (P[i + 1, j, k] - P[i, j, k]) / dx
+                s = s + (2.0 / (R[i, j, k] + R[i + 1, j, k]) - 1.0 / rho_12) * \
+                    (T[i + 1, j, k] - T[i, j, k]) / dx
+                u[k - 1, j - 1, i] = u[k - 1, j - 1, i] - s * dt
+                s = 1.0 / rho_12 * (P[i, j + 1, k] - P[i, j, k]) / dy
+                s = s + (2.0 / (R[i, j, k] + R[i, j + 1, k]) - 1.0 / rho_12) * \
+                    (T[i, j + 1, k] - T[i, j, k]) / dy
+                v[k - 1, j, i - 1] = v[k - 1, j, i - 1] - s * dt
+                if nz > 1:
+                    s = 1.0 / rho_12 * (P[i, j, k + 1] - P[i, j, k]) / dz
+                    s = s + (2.0 / (R[i, j, k] + R[i, j, k + 1]) - 1.0 / rho_12) * \
+                        (T[i, j, k + 1] - T[i, j, k]) / dz
+                    w[k, j - 1, i - 1] = w[k, j - 1, i - 1] - s * dt
+    return u, v, w
