@@ -50,6 +50,14 @@ __device__ __forceinline__ T rho_face(T k, T ra, T rb) {
   else return k / (ra + rb);
 }
 
+// The density-form smoother's update (s - b)/d, with the fast division
+// (within 2 ulp; only the FP32 preconditioner uses it).
+template <typename T>
+__device__ __forceinline__ T rho_update(T v, T d) {
+  if constexpr (std::is_same<T, float>::value) return __fdividef(v, d);
+  else return v / d;
+}
+
 // stencil() with the coefficients computed from the density (same order).
 template <typename T>
 __device__ __forceinline__ void stencil_rho(const LevelView<T>& L, const T* __restrict__ p, int i,
@@ -140,6 +148,7 @@ __global__ void __launch_bounds__(256) k_smooth(LevelView<T> L, int color) {
   }
   const T v = s - L.src[q];
   if (kIdiag) L.sol[q] = v * L.idiag[q];
+  else if (kRho) L.sol[q] = rho_update(v, d);
   else L.sol[q] = v / d;
 }
 

@@ -30,6 +30,7 @@ namespace {
 inline unsigned cdiv(size_t a, unsigned b) { return (unsigned)((a + b - 1) / b); }
 
 __device__ __forceinline__ float face(float k, float ra, float rb) { return __fdividef(k, ra + rb); }
+__device__ __forceinline__ float rho_update(float v, float d) { return __fdividef(v, d); }
 
 // One colour of a red-black sweep, one thread per cell of the colour.
 template <bool kZero>
@@ -64,8 +65,7 @@ __global__ void __launch_bounds__(256) k_smooth_split(LevelView<float> L, int co
   SPLIT_TERM(k > 0, L.kz, h - sz)
   SPLIT_TERM(k < L.nz - 1, L.kz, h + sz)
 #undef SPLIT_TERM
-  const float v = s - L.src[own];
-  L.sol[own] = v / d;
+  L.sol[own] = rho_update(s - L.src[own], d);
 }
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
@@ -93,13 +93,16 @@ __global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int c
   float rc[4], b[4];
   unpack(ld4(L.rho + own), rc);
   unpack(ld4(L.src + own), b);
+  // A wall face gets neighbour density +inf, so its coefficient k/(rho + inf)
+  // is exactly 0 and the term adds nothing: the faces need no branches.
+  const float inf = __int_as_float(0x7f800000);
   // x window: the other colour's half indices m0-1+par .. m0+3+par
   float rxm[4], rxp[4], pxm[4] = {0.f, 0.f, 0.f, 0.f}, pxp[4] = {0.f, 0.f, 0.f, 0.f};
   {
     float rv[4], pv[4] = {0.f, 0.f, 0.f, 0.f};
     unpack(ld4(ro), rv);
     if (!kZero) unpack(ld4(po), pv);
-    float re = 0.f, pe = 0.f;
+    float re = inf, pe = 0.f;
     if (par) {
       if (m0 + 4 < hx) { re = ro[4]; if (!kZero) pe = po[4]; }
       rxm[0] = rv[0]; rxm[1] = rv[1]; rxm[2] = rv[2]; rxm[3] = rv[3];
@@ -114,26 +117,24 @@ __global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int c
       pxp[0] = pv[0]; pxp[1] = pv[1]; pxp[2] = pv[2]; pxp[3] = pv[3];
     }
   }
-  const bool yl = j > 0, yr = j < L.ny - 1, zl = k > 0, zr = k < L.nz - 1;
-  float rym[4] = {}, ryp[4] = {}, rzm[4] = {}, rzp[4] = {};
+  float rym[4] = {inf, inf, inf, inf}, ryp[4] = {inf, inf, inf, inf};
+  float rzm[4] = {inf, inf, inf, inf}, rzp[4] = {inf, inf, inf, inf};
   float pym[4] = {}, pyp[4] = {}, pzm[4] = {}, pzp[4] = {};
-  if (yl) { unpack(ld4(ro - sy), rym); if (!kZero) unpack(ld4(po - sy), pym); }
-  if (yr) { unpack(ld4(ro + sy), ryp); if (!kZero) unpack(ld4(po + sy), pyp); }
-  if (zl) { unpack(ld4(ro - sz), rzm); if (!kZero) unpack(ld4(po - sz), pzm); }
-  if (zr) { unpack(ld4(ro + sz), rzp); if (!kZero) unpack(ld4(po + sz), pzp); }
+  if (j > 0) { unpack(ld4(ro - sy), rym); if (!kZero) unpack(ld4(po - sy), pym); }
+  if (j < L.ny - 1) { unpack(ld4(ro + sy), ryp); if (!kZero) unpack(ld4(po + sy), pyp); }
+  if (k > 0) { unpack(ld4(ro - sz), rzm); if (!kZero) unpack(ld4(po - sz), pzm); }
+  if (k < L.nz - 1) { unpack(ld4(ro + sz), rzp); if (!kZero) unpack(ld4(po + sz), pzp); }
   float out[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const int i = 2 * (m0 + c) + par;
     float s = 0.f, d = 0.f, cc;
-    if (i > 0) { cc = face(L.kx, rc[c], rxm[c]); if (!kZero) s += cc * pxm[c]; d += cc; }
-    if (i < L.nx - 1) { cc = face(L.kx, rc[c], rxp[c]); if (!kZero) s += cc * pxp[c]; d += cc; }
-    if (yl) { cc = face(L.ky, rc[c], rym[c]); if (!kZero) s += cc * pym[c]; d += cc; }
-    if (yr) { cc = face(L.ky, rc[c], ryp[c]); if (!kZero) s += cc * pyp[c]; d += cc; }
-    if (zl) { cc = face(L.kz, rc[c], rzm[c]); if (!kZero) s += cc * pzm[c]; d += cc; }
-    if (zr) { cc = face(L.kz, rc[c], rzp[c]); if (!kZero) s += cc * pzp[c]; d += cc; }
-    const float v = s - b[c];
-    out[c] = v / d;
+    cc = face(L.kx, rc[c], rxm[c]); if (!kZero) s += cc * pxm[c]; d += cc;
+    cc = face(L.kx, rc[c], rxp[c]); if (!kZero) s += cc * pxp[c]; d += cc;
+    cc = face(L.ky, rc[c], rym[c]); if (!kZero) s += cc * pym[c]; d += cc;
+    cc = face(L.ky, rc[c], ryp[c]); if (!kZero) s += cc * pyp[c]; d += cc;
+    cc = face(L.kz, rc[c], rzm[c]); if (!kZero) s += cc * pzm[c]; d += cc;
+    cc = face(L.kz, rc[c], rzp[c]); if (!kZero) s += cc * pzp[c]; d += cc;
+    out[c] = rho_update(s - b[c], d);
   }
   st4(L.sol + own, make_float4(out[0], out[1], out[2], out[3]));
 }
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
   const int hx = F.nx >> 1;
   const size_t half = F.hstride;
   const size_t sy = (size_t)hx, sz = (size_t)hx * F.ny;
+  const float inf = __int_as_float(0x7f800000);  // wall neighbour: coefficient exactly 0
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   for (int dz = 0; dz < F.fz; ++dz)
     for (int dy = 0; dy < F.fy; ++dy) {
@@ -232,7 +234,6 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
       const float* Pb = F.sol + (size_t)(1 - ca) * half + h;
       const float* Ra = F.rho + (size_t)ca * half + h;
       const float* Rb = F.rho + (size_t)(1 - ca) * half + h;
-      const bool yl = j > 0, yr = j < F.ny - 1, zl = k > 0, zr = k < F.nz - 1;
       float pa[4], pb[4], ra[4], rb[4], ba[4], bb[4];
       unpack(ld4(Pa), pa);
       unpack(ld4(Pb), pb);
@@ -240,65 +241,55 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
       unpack(ld4(Rb), rb);
       unpack(ld4(F.src + (size_t)ca * half + h), ba);
       unpack(ld4(F.src + (size_t)(1 - ca) * half + h), bb);
-      const bool xl0 = I0 > 0, xr3 = 2 * (I0 + 3) + 2 < F.nx;
       // x-: cell 2I-1 (b's colour, index I-1); x+ of b: cell 2I+2 (a's colour, I+1)
-      const float pl_e = xl0 ? Pb[-1] : 0.f, rl_e = xl0 ? Rb[-1] : 0.f;
-      const float pr_e = xr3 ? Pa[4] : 0.f, rr_e = xr3 ? Ra[4] : 0.f;
+      float pl_e = 0.f, rl_e = inf, pr_e = 0.f, rr_e = inf;
+      if (I0 > 0) { pl_e = Pb[-1]; rl_e = Rb[-1]; }
+      if (2 * (I0 + 3) + 2 < F.nx) { pr_e = Pa[4]; rr_e = Ra[4]; }
       float pym_a[4] = {}, pym_b[4] = {}, pyp_a[4] = {}, pyp_b[4] = {};
       float pzm_a[4] = {}, pzm_b[4] = {}, pzp_a[4] = {}, pzp_b[4] = {};
-      float rym_a[4] = {}, rym_b[4] = {}, ryp_a[4] = {}, ryp_b[4] = {};
-      float rzm_a[4] = {}, rzm_b[4] = {}, rzp_a[4] = {}, rzp_b[4] = {};
-      if (yl) {
+      float rym_a[4] = {inf, inf, inf, inf}, rym_b[4] = {inf, inf, inf, inf};
+      float ryp_a[4] = {inf, inf, inf, inf}, ryp_b[4] = {inf, inf, inf, inf};
+      float rzm_a[4] = {inf, inf, inf, inf}, rzm_b[4] = {inf, inf, inf, inf};
+      float rzp_a[4] = {inf, inf, inf, inf}, rzp_b[4] = {inf, inf, inf, inf};
+      if (j > 0) {
         unpack(ld4(Pb - sy), pym_a); unpack(ld4(Pa - sy), pym_b);
         unpack(ld4(Rb - sy), rym_a); unpack(ld4(Ra - sy), rym_b);
       }
-      if (yr) {
+      if (j < F.ny - 1) {
         unpack(ld4(Pb + sy), pyp_a); unpack(ld4(Pa + sy), pyp_b);
         unpack(ld4(Rb + sy), ryp_a); unpack(ld4(Ra + sy), ryp_b);
       }
-      if (zl) {
+      if (k > 0) {
         unpack(ld4(Pb - sz), pzm_a); unpack(ld4(Pa - sz), pzm_b);
         unpack(ld4(Rb - sz), rzm_a); unpack(ld4(Ra - sz), rzm_b);
       }
-      if (zr) {
+      if (k < F.nz - 1) {
         unpack(ld4(Pb + sz), pzp_a); unpack(ld4(Pa + sz), pzp_b);
         unpack(ld4(Rb + sz), rzp_a); unpack(ld4(Ra + sz), rzp_b);
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const int I = I0 + c;
-        const bool xl = 2 * I > 0, xr = 2 * I + 2 < F.nx;
         const float pl = c == 0 ? pl_e : pb[c - 1], rl = c == 0 ? rl_e : rb[c - 1];
         const float pr = c == 3 ? pr_e : pa[c + 1], rr = c == 3 ? rr_e : ra[c + 1];
-        const float cxa = xl ? face(F.kx, ra[c], rl) : 0.f;
         const float cab = face(F.kx, ra[c], rb[c]);
-        const float cxr = xr ? face(F.kx, rb[c], rr) : 0.f;
-        const float cym_a = yl ? face(F.ky, ra[c], rym_a[c]) : 0.f;
-        const float cym_b = yl ? face(F.ky, rb[c], rym_b[c]) : 0.f;
-        const float cyp_a = yr ? face(F.ky, ra[c], ryp_a[c]) : 0.f;
-        const float cyp_b = yr ? face(F.ky, rb[c], ryp_b[c]) : 0.f;
-        const float czm_a = zl ? face(F.kz, ra[c], rzm_a[c]) : 0.f;
-        const float czm_b = zl ? face(F.kz, rb[c], rzm_b[c]) : 0.f;
-        const float czp_a = zr ? face(F.kz, ra[c], rzp_a[c]) : 0.f;
-        const float czp_b = zr ? face(F.kz, rb[c], rzp_b[c]) : 0.f;
         {
           float s = 0.f, d = 0.f, cc;
-          if (xl) { cc = cxa; s += cc * pl; d += cc; }
+          cc = face(F.kx, ra[c], rl); s += cc * pl; d += cc;
           cc = cab; s += cc * pb[c]; d += cc;
-          if (yl) { cc = cym_a; s += cc * pym_a[c]; d += cc; }
-          if (yr) { cc = cyp_a; s += cc * pyp_a[c]; d += cc; }
-          if (zl) { cc = czm_a; s += cc * pzm_a[c]; d += cc; }
-          if (zr) { cc = czp_a; s += cc * pzp_a[c]; d += cc; }
+          cc = face(F.ky, ra[c], rym_a[c]); s += cc * pym_a[c]; d += cc;
+          cc = face(F.ky, ra[c], ryp_a[c]); s += cc * pyp_a[c]; d += cc;
+          cc = face(F.kz, ra[c], rzm_a[c]); s += cc * pzm_a[c]; d += cc;
+          cc = face(F.kz, ra[c], rzp_a[c]); s += cc * pzp_a[c]; d += cc;
           acc[c] += ba[c] - (s - d * pa[c]);
         }
         {
           float s = 0.f, d = 0.f, cc;
           cc = cab; s += cc * pa[c]; d += cc;
-          if (xr) { cc = cxr; s += cc * pr; d += cc; }
-          if (yl) { cc = cym_b; s += cc * pym_b[c]; d += cc; }
-          if (yr) { cc = cyp_b; s += cc * pyp_b[c]; d += cc; }
-          if (zl) { cc = czm_b; s += cc * pzm_b[c]; d += cc; }
-          if (zr) { cc = czp_b; s += cc * pzp_b[c]; d += cc; }
+          cc = face(F.kx, rb[c], rr); s += cc * pr; d += cc;
+          cc = face(F.ky, rb[c], rym_b[c]); s += cc * pym_b[c]; d += cc;
+          cc = face(F.ky, rb[c], ryp_b[c]); s += cc * pyp_b[c]; d += cc;
+          cc = face(F.kz, rb[c], rzm_b[c]); s += cc * pzm_b[c]; d += cc;
+          cc = face(F.kz, rb[c], rzp_b[c]); s += cc * pzp_b[c]; d += cc;
           acc[c] += bb[c] - (s - d * pb[c]);
         }
       }
