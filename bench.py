@@ -171,11 +171,12 @@ def traffic_per_cell():
 # algorithmic bytes per fine cell per launch of each kernel class, mixed solve:
 # FP32 cycle arrays (w = 4) and the double-word defect kernel
 # per sweep for the smoother (a two-colour sweep is two launches: the bench
-# scales by the sweeps a launch covers).  With the density form (opt-in,
-# GBMG_RHO_COEF=1) the FP32 finest-level kernels read the cell density (w)
-# instead of three face-coefficient arrays (3w).
+# scales by the sweeps a launch covers).  With the density form (the default
+# for an operator from rho or phi; GBMG_RHO_COEF=0 stores coefficients) the
+# FP32 finest-level kernels read the cell density (w) instead of three
+# face-coefficient arrays (3w).
 def rho_form():
-    return os.environ.get("GBMG_RHO_COEF", "0") != "0"
+    return os.environ.get("GBMG_RHO_COEF", "1") != "0"
 
 
 def algorithmic_bytes_per_cell(cls, w=4):

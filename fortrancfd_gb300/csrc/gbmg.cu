@@ -633,16 +633,16 @@ int build_hierarchy(gbmg_handle* h) {
 }
 
 // Whether the FP32 finest-level kernels compute their coefficients from the
-// density (GBMG_RHO_COEF=1 and an operator from rho/phi; the TMA and fused
-// sweeps read stored coefficients), and whether that level
+// density (an operator from rho/phi; GBMG_RHO_COEF=0 turns it off; the TMA
+// and fused sweeps read stored coefficients), and whether that level
 // is stored colour-split (density form, nx even, x halved by the first
 // coarsening, the level outside the single-block bottom; GBMG_SPLIT=0 turns
 // it off).  Captured graphs hold the level views, so a change drops them.
 void set_rho_form(gbmg_handle* h, bool on) {
   Level& f = h->lv[0];
   bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0;
-  const char* ev = std::getenv("GBMG_RHO_COEF");  // opt-in: GBMG_RHO_COEF=1
-  if (!ev || std::atoi(ev) == 0) want = false;
+  if (const char* e = std::getenv("GBMG_RHO_COEF"))
+    if (std::atoi(e) == 0) want = false;
   bool split = want && f.nx % 2 == 0 && h->L > 1 && f.fx == 2 && h->sub_lc > 0;
   if (const char* e = std::getenv("GBMG_SPLIT"))
     if (std::atoi(e) == 0) split = false;

@@ -157,6 +157,21 @@ void launch_psplit_correct(cudaStream_t s, int nx, int ny, int nz, const double*
 void launch_face_const(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
                        double* cx, double* cy, double* cz, float* const* c32, float2* const* cw);
 
+// ---- density-form FP32 arithmetic (the finest level of the mixed cycle) ----
+// Approximate reciprocal (rcp.approx.ftz: one MUFU.RCP, within 1 ulp; +inf ->
+// +0, so a wall neighbour given density +inf contributes a zero coefficient).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// face coefficient k/(rho_a + rho_b), k = 2/h^2
+__device__ __forceinline__ float rho_face32(float k, float ra, float rb) {
+  return k * rcp_approx(ra + rb);
+}
+// the smoother's update (s - b)/d
+__device__ __forceinline__ float rho_update32(float v, float d) { return v * rcp_approx(d); }
+
 // ---- colour-split FP32 finest level (kernels_split.cu) ----
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess);
 void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,

@@ -41,20 +41,20 @@ __device__ __forceinline__ void stencil(const LevelView<T>& L, const T* __restri
 }
 
 // Face coefficient k/(rho_a + rho_b) of the density form.  FP32 uses the
-// fast reciprocal-based division (within 2 ulp): these coefficients only
-// drive the FP32 smoother and restriction of the mixed-precision cycle, whose
-// result is corrected against the FP64 operator.
+// approximate reciprocal (within 1 ulp): these coefficients only drive the
+// FP32 smoother and restriction of the mixed-precision cycle, whose result is
+// corrected against the FP64 operator.
 template <typename T>
 __device__ __forceinline__ T rho_face(T k, T ra, T rb) {
-  if constexpr (std::is_same<T, float>::value) return __fdividef(k, ra + rb);
+  if constexpr (std::is_same<T, float>::value) return rho_face32(k, ra, rb);
   else return k / (ra + rb);
 }
 
-// The density-form smoother's update (s - b)/d, with the fast division
-// (within 2 ulp; only the FP32 preconditioner uses it).
+// The density-form smoother's update (s - b)/d, with the approximate
+// reciprocal (only the FP32 preconditioner uses it).
 template <typename T>
 __device__ __forceinline__ T rho_update(T v, T d) {
-  if constexpr (std::is_same<T, float>::value) return __fdividef(v, d);
+  if constexpr (std::is_same<T, float>::value) return rho_update32(v, d);
   else return v / d;
 }
 

@@ -29,8 +29,8 @@ namespace {
 
 inline unsigned cdiv(size_t a, unsigned b) { return (unsigned)((a + b - 1) / b); }
 
-__device__ __forceinline__ float face(float k, float ra, float rb) { return __fdividef(k, ra + rb); }
-__device__ __forceinline__ float rho_update(float v, float d) { return __fdividef(v, d); }
+__device__ __forceinline__ float face(float k, float ra, float rb) { return rho_face32(k, ra, rb); }
+__device__ __forceinline__ float rho_update(float v, float d) { return rho_update32(v, d); }
 
 // One colour of a red-black sweep, one thread per cell of the colour.
 template <bool kZero>

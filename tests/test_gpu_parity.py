@@ -309,7 +309,7 @@ def test_single_block_bottom_matches_separate_launches(cuda, monkeypatch, precis
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (0, 1, False), (4, 4, True)])
 def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     """The FP32 finest-level smoother and restriction computing their face
-    coefficients from the density (GBMG_RHO_COEF=1, an operator set from rho)
+    coefficients from the density (the default for an operator set from rho)
     against the stored FP32 coefficients (GBMG_RHO_COEF=0): the FP32 values
     differ by a few ulp, so the preconditioner changes slightly; both solves
     reach the tolerance, agree with the FP64 oracle to tol-scaled accuracy and
@@ -332,9 +332,9 @@ def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     (1, 4, False, None), (1, 2, True, None), (0, 1, False, None), (4, 4, True, None),
     (None, None, False, (16, 16, 12))])
 def test_colour_split_layout_is_bit_identical(cuda, monkeypatch, idx, scale, krylov, shape):
-    """The colour-split FP32 finest level (on with the density form,
-    GBMG_RHO_COEF=1) does the natural-layout kernels' arithmetic in the same
-    order (GBMG_SPLIT=0 keeps the natural layout): same cycles, same bits.
+    """The colour-split FP32 finest level (the default, with the density
+    form) does the natural-layout kernels' arithmetic in the same order
+    (GBMG_SPLIT=0 keeps the natural layout): same cycles, same bits.
     The 16 x 16 x 12 grid has nx % 8 != 0, so its defect runs without TMA."""
     if shape is None:
         c = cases.config(idx, scale)
