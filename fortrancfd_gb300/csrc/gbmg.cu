@@ -46,6 +46,7 @@ struct Level {
   float k32[3] = {0.f, 0.f, 0.f};  // 2/h^2 per axis
   int split = 0;  // sol32, src32 and rho32 in the colour-split layout
   size_t hstride = 0;  // distance between the colour halves (elements)
+  int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -230,6 +231,23 @@ LevelView<double> view<double>(const Level& l) { return v64(l); }
 template <>
 LevelView<float> view<float>(const Level& l) { return v32(l); }
 
+// The view for the next launch on level l: split levels alternate the z
+// direction of their kernels launch by launch (an L2 hint; results do not
+// depend on it).
+template <typename T>
+LevelView<T> view_next(Level& l);
+template <>
+LevelView<double> view_next<double>(Level& l) { return v64(l); }
+template <>
+LevelView<float> view_next<float>(Level& l) {
+  LevelView<float> v = v32(l);
+  if (l.split) {
+    v.zrev = l.zrev;
+    l.zrev ^= 1;
+  }
+  return v;
+}
+
 template <typename T> const T* minv_of(const gbmg_handle* h);
 template <> const double* minv_of<double>(const gbmg_handle* h) { return h->minv; }
 template <> const float* minv_of<float>(const gbmg_handle* h) { return h->minv32; }
@@ -270,8 +288,8 @@ void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
     LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
     std::swap(lv.sol32, lv.alt32);
   } else {
-    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, first_color, zero_guess));
-    LAUNCH(h, cs, launch_smooth<float>(h->stream, V, 1 - first_color));
+    LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), first_color, zero_guess));
+    LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), 1 - first_color));
   }
 }
 
@@ -315,7 +333,7 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
     for (int it = 0; it < h->prm.nu1; ++it)
       sweep<T>(h, l, 0, it == 0 && (l > 0 || zero_fine));
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
-           launch_restrict<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
+           launch_restrict<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
   }
   if (h->sub_lc < L) {
     LAUNCH(h, GBMG_PROF_COARSE_SOLVE, launch_subcycle<T>(s, make_subcycle<T>(h, reverse_post)));
@@ -326,7 +344,7 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
   }
   for (int l = top - 1; l >= 0; --l) {
     LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
-           launch_prolong<T>(s, view<T>(h->lv[l]), view<T>(h->lv[l + 1])));
+           launch_prolong<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1])));
     for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0, false);
   }
   return check_launch(h, "v-cycle");

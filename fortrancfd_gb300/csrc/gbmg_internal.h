@@ -39,6 +39,10 @@ struct LevelView {
   // index, hstride >= n/2 the distance between the two colour halves
   int split = 0;
   size_t hstride = 0;
+  // traverse the z planes from the top (split kernels): consecutive launches
+  // on the finest level alternate direction, so each starts on the planes the
+  // previous one touched last, which are still in L2
+  int zrev = 0;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,

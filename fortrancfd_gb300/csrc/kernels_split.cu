@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int c
   const int hx = L.nx >> 1;
   const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int k = L.zrev ? L.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
   if (m0 >= hx || j >= L.ny) return;
   const size_t sy = (size_t)hx, sz = (size_t)hx * L.ny;
   const size_t h = (size_t)k * sz + (size_t)j * sy + m0;
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
   pdl_enter();
   const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  const int K = blockIdx.z;
+  const int K = F.zrev ? C.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
   if (I0 >= C.nx || J >= C.ny) return;
   const int hx = F.nx >> 1;
   const size_t half = F.hstride;
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, Leve
   pdl_enter();
   const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  const int K = blockIdx.z;
+  const int K = F.zrev ? C.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
   if (I0 >= C.nx || J >= C.ny) return;
   const size_t csy = (size_t)C.nx, csz = (size_t)C.nx * C.ny;
   const size_t cq = (size_t)K * csz + (size_t)J * csy + I0;
