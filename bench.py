@@ -49,7 +49,7 @@ ADJ_TOL = 1e-8
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1, help="synthetic case index (1 = 256^3 sphere)")
@@ -106,7 +106,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -116,7 +116,15 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def window(self, t0, t1):
+        """Keep the samples read between t0 and t1 (the timed region, plus
+        one sampling interval of slack for the pipe)."""
+        inside = [(t, ln) for t, ln in self.lines if t0 <= t <= t1 + 0.06]
+        self.in_window = bool(inside)
+        if inside:
+            self.lines = inside
 
     def __exit__(self, *exc):
         if self.proc:
@@ -129,7 +137,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        for _, ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -144,7 +152,9 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm),
+                "window": "timed region" if getattr(self, "in_window", False)
+                else "warm-up and timed region (no sample read inside the timed region)"}
 
 
 def measured_peaks():
@@ -373,7 +383,10 @@ def run_ours(args):
             _, st = solver.solve(b, p, tol=TOL)
             return st
 
-        with torch.cuda.stream(stream):
+        sampler = ClockSampler(dev.index if dev.index is not None else 0)
+        # the sampler starts before the warm-up so that nvidia-smi is running
+        # when the timed region begins; only the samples inside it are kept
+        with torch.cuda.stream(stream), (sampler if sample_clocks else _Null()):
             for _ in range(warmup):
                 st = step()
             barrier()
@@ -381,14 +394,16 @@ def run_ours(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             launches0 = solver.kernel_launches
-            sampler = ClockSampler(dev.index if dev.index is not None else 0)
-            with (sampler if sample_clocks else _Null()):
-                e0.record(stream)
-                for _ in range(steps):
-                    st = step()
-                e1.record(stream)
-                torch.cuda.synchronize()
+            t0 = time.monotonic()
+            e0.record(stream)
+            for _ in range(steps):
+                st = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t1 = time.monotonic()
             barrier()
+        if sample_clocks:
+            sampler.window(t0, t1)
             ms = e0.elapsed_time(e1)
             launches = solver.kernel_launches - launches0
         ms = max_over_ranks(ms, dev)

@@ -41,7 +41,7 @@ class PressureSolve(torch.autograd.Function):
         phi, p = ctx.saved_tensors
         eps, rho_pos, rho_neg, tol = ctx.args
         s = ctx.solver
-        s.rho_mu(phi.detach(), eps, rho_pos, rho_neg)  # the solver may have moved on
+        s.ensure_rho_mu(phi.detach(), eps, rho_pos, rho_neg)  # rebuilt if the solver moved on
         lam = torch.zeros_like(p)
         s.solve(grad_p.contiguous(), lam, tol=tol)
         grad_phi = None
@@ -68,7 +68,7 @@ class PressureSolveRho(torch.autograd.Function):
     def backward(ctx, grad_p):
         rho, p = ctx.saved_tensors
         s = ctx.solver
-        s.ppe_init(rho.detach())
+        s.ensure_ppe_init(rho.detach())
         lam = torch.zeros_like(p)
         s.solve(grad_p.contiguous(), lam, tol=ctx.tol)
         grad_rho = s.adjoint(p, lam)[0] if ctx.needs_input_grad[0] else None

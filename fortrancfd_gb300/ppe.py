@@ -165,17 +165,42 @@ class PressurePoisson:
         return (nz, ny, nx + 1), (nz, ny + 1, nx), (nz + 1, ny, nx)
 
     # -- coefficients (ppe_sor_init, rho_mu) -------------------------------------
+    @staticmethod
+    def _key(a, *extra):
+        """Identity of an operator input: a CUDA tensor's storage, offset and
+        version counter (so an in-place change is seen), or None."""
+        if _is_torch(a) and a.is_cuda:
+            return (a.data_ptr(), tuple(a.shape), tuple(a.stride()), a._version) + extra
+        return None
+
     def ppe_init(self, rho):
         """ppe_sor_init: face coefficients 2/(rho_i + rho_nb)/h^2 from cell density."""
         f, m = _field(rho, self.shape)
         self._sync_torch(rho)
+        self._op_key = None
         self._check(self._L.gbmg_set_rho(self._h, f, m), "ppe_init")
+        self._op_key = self._key(rho, "rho")
 
     def rho_mu(self, phi, eps, rho_pos=1.0, rho_neg=1e-3):
         """rho_mu + ppe_sor_init: rho = rho_pos H(phi) + rho_neg (1 - H(phi))."""
         f, m = _field(phi, self.shape)
         self._sync_torch(phi)
+        self._op_key = None
         self._check(self._L.gbmg_set_phi(self._h, f, eps, rho_pos, rho_neg, m), "rho_mu")
+        self._op_key = self._key(phi, "phi", float(eps), float(rho_pos), float(rho_neg))
+
+    def ensure_rho_mu(self, phi, eps, rho_pos=1.0, rho_neg=1e-3):
+        """rho_mu, skipped when the operator was last built from this very
+        tensor (same storage and version) with the same parameters."""
+        key = self._key(phi, "phi", float(eps), float(rho_pos), float(rho_neg))
+        if key is None or key != getattr(self, "_op_key", None):
+            self.rho_mu(phi, eps, rho_pos, rho_neg)
+
+    def ensure_ppe_init(self, rho):
+        """ppe_init, skipped when the operator was last built from this tensor."""
+        key = self._key(rho, "rho")
+        if key is None or key != getattr(self, "_op_key", None):
+            self.ppe_init(rho)
 
     def set_coef(self, cx, cy, cz):
         """Face coefficients given directly (cell-shaped low-face arrays)."""
@@ -184,6 +209,7 @@ class PressurePoisson:
         fz, m3 = _field(cz, self.shape)
         m = _mem_of((fx, m1), (fy, m2), (fz, m3))
         self._sync_torch(cx, cy, cz)
+        self._op_key = None
         self._check(self._L.gbmg_set_coef(self._h, fx, fy, fz, m), "set_coef")
 
     # -- solves ------------------------------------------------------------------
@@ -227,6 +253,7 @@ class PressurePoisson:
         constant-coefficient Laplacian.  ppe_init / rho_mu switch back."""
         f, m = _field(rho, self.shape)
         self._sync_torch(rho)
+        self._op_key = None
         self._check(self._L.gbmg_set_split(self._h, f, float(rho_12), m), "ppe_mg_solver_init")
 
     def ppe_mg_solver(self, u, v, w, dt, p_hat, tol=1e-10, p=None, check=True):
