@@ -402,10 +402,10 @@ def run_ours(args):
             torch.cuda.synchronize()
             t1 = time.monotonic()
             barrier()
+        ms = e0.elapsed_time(e1)
+        launches = solver.kernel_launches - launches0
         if sample_clocks:
             sampler.window(t0, t1)
-            ms = e0.elapsed_time(e1)
-            launches = solver.kernel_launches - launches0
         ms = max_over_ranks(ms, dev)
         return ms, st, launches, (sampler.summary() if sample_clocks else None)
 
