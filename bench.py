@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-multi", action="store_true", help="skip the 512^3 16-bubble section")
+    ap.add_argument("--no-rollout", action="store_true", help="skip the 20-step rollout section")
     return ap.parse_args()
 
 
@@ -286,6 +288,110 @@ def cpu_baseline(case, phi, u, v, w, budget_s):
                       f"{threads} threads, {st['cycles']} cycles each (oracle restatement)"}
 
 
+def _device_velocity(shape, seed, dev):
+    """u*, v*, w* ~ N(0,1) on interior faces, 0 on wall faces, drawn on the
+    device from a seeded generator (for the large sections, where host
+    generation would dominate the run)."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    nz, ny, nx = shape
+    u = torch.randn((nz, ny, nx + 1), generator=g, device=dev, dtype=torch.float64)
+    v = torch.randn((nz, ny + 1, nx), generator=g, device=dev, dtype=torch.float64)
+    w = torch.randn((nz + 1, ny, nx), generator=g, device=dev, dtype=torch.float64)
+    u[..., 0] = 0.0
+    u[..., -1] = 0.0
+    v[:, 0, :] = 0.0
+    v[:, -1, :] = 0.0
+    w[0] = 0.0
+    w[-1] = 0.0
+    return u, v, w
+
+
+def multi_bubble_section(dev, stream, scale=1, reps=2):
+    """The 512³ sixteen-bubble case: mixed precision (flexible CG around the
+    FP32 V-cycle, the mode these small light bubbles need) against the FP64
+    GPU solve of the same system."""
+    import torch
+
+    from fortrancfd_gb300 import PressurePoisson, inputs
+    from fortrancfd_gb300.rollout import level_set
+
+    case = inputs.config(2, scale)
+    with torch.cuda.stream(stream):
+        c = torch.from_numpy(case.centers.copy()).to(dev)
+        r = torch.from_numpy(case.radii.copy()).to(dev)
+        phi = level_set(c, r, case.shape, case.extent)
+        u, v, w = _device_velocity(case.shape, case.seed, dev)
+        out = {}
+        ps = {}
+        for prec in ("mixed", "fp64"):
+            s = PressurePoisson(case.shape, case.spacing, precision=prec, krylov=True,
+                                max_cycles=400, stream=stream)
+            b = s.divergence(u, v, w, case.dt)
+            p = torch.zeros_like(b)
+            times = []
+            for it in range(reps + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                p.zero_()
+                e0.record(stream)
+                s.rho_mu(phi, case.eps, case.rho_pos, case.rho_neg)
+                _, st = s.solve(b, p, tol=TOL)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if it:
+                    times.append(e0.elapsed_time(e1))
+            out[prec] = {"ms_per_solve": float(np.median(times)), "cycles": st["cycles"],
+                         "rel_residual": st["rel_residual"]}
+            ps[prec] = p
+            s.close()
+        out["p_rel_diff_mixed_vs_fp64"] = float((ps["mixed"] - ps["fp64"]).norm() /
+                                               ps["fp64"].norm())
+        out["mixed_over_fp64"] = out["mixed"]["ms_per_solve"] / out["fp64"]["ms_per_solve"]
+    nz, ny, nx = case.shape
+    out["workload"] = (f"{case.name}: {nx}x{ny}x{nz} cells, {len(case.radii)} bubbles, density "
+                       "ratio 1000, flexible CG around one V(2,2) cycle, tol 1e-10; inputs drawn "
+                       "on the device")
+    return out
+
+
+def rollout_section(dev, stream, scale=1, steps=20):
+    """The 20-step differentiable projection rollout (128x128x256, 4 bubbles):
+    forward (20 mixed solves) and backward (20 adjoint solves and the
+    checkpointed level sets) device times, gradient w.r.t. centres and radii."""
+    import torch
+
+    from fortrancfd_gb300 import PressurePoisson, inputs
+    from fortrancfd_gb300.rollout import rollout_loss
+
+    case = inputs.config(4, scale)
+    with torch.cuda.stream(stream):
+        s = PressurePoisson(case.shape, case.spacing, precision="mixed", krylov=True,
+                            max_cycles=400, stream=stream)
+        c = torch.from_numpy(case.centers.copy()).to(dev).requires_grad_(True)
+        r = torch.from_numpy(case.radii.copy()).to(dev).requires_grad_(True)
+        fw, bw = [], []
+        for it in range(2):
+            c.grad = None
+            r.grad = None
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            J = rollout_loss(c, r, case, s, steps=steps, tol=TOL, adjoint_tol=ADJ_TOL)
+            e1.record(stream)
+            J.backward()
+            e2.record(stream)
+            torch.cuda.synchronize()
+            if it:
+                fw.append(e0.elapsed_time(e1))
+                bw.append(e1.elapsed_time(e2))
+        s.close()
+    nz, ny, nx = case.shape
+    return {"workload": f"{case.name}: {nx}x{ny}x{nz} cells, 4 bubbles, {steps} steps, mixed "
+                        "precision, flexible CG, tol 1e-10 forward, 1e-8 adjoint",
+            "forward_ms": fw[0], "backward_ms": bw[0], "backward_over_forward": bw[0] / fw[0],
+            "grad_norm_centres": float(c.grad.norm()), "grad_norm_radii": float(r.grad.norm())}
+
+
 def adjoint_section(dev, stream, reps=5, scale=1):
     """The differentiable solve on the 1024^2 eight-circle case: forward
     (operator from phi + mixed-precision solve) and backward (operator rebuild,
@@ -495,6 +601,19 @@ def run_ours(args):
         except Exception as exc:  # report, keep the headline line
             adj = {"error": f"{type(exc).__name__}: {exc}"}
 
+    multi = roll = None
+    if not args.no_multi:
+        try:
+            multi = multi_bubble_section(dev, stream, scale=max(1, args.scale))
+        except Exception as exc:
+            multi = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
+    if not args.no_rollout:
+        try:
+            roll = rollout_section(dev, stream, scale=max(1, args.scale))
+        except Exception as exc:
+            roll = {"error": f"{type(exc).__name__}: {exc}"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
@@ -516,7 +635,8 @@ def run_ours(args):
                                  "each FP64 field alone exceeds it",
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "adjoint": adj}
+                "gpu_launches": launches, "adjoint": adj, "multi_bubble": multi,
+                "rollout": roll}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
         print(json.dumps(line), flush=True)

@@ -308,7 +308,7 @@ SubCycle<T> make_subcycle(gbmg_handle* h, bool reverse) {
     const LevelView<T> V = view<T>(h->lv[lc + i]);
     S.lv[i] = SubLevel<T>{V.nx, V.ny, V.nz, V.fx, V.fy, V.fz, V.cx, V.cy, V.cz};
     S.off[i] = off;
-    off += 2 * V.nx * V.ny * V.nz;
+    off += 5 * V.nx * V.ny * V.nz;  // sol, src and the three coefficient arrays
   }
   S.off[S.nlev] = off;
   const LevelView<T> V0 = view<T>(h->lv[lc]);

@@ -4,9 +4,9 @@
 // 16^3 cells is a few microseconds of launch and drain for nanoseconds of
 // work.  This kernel runs everything from level lc down and back up --
 // sweeps, residual + restriction, the dense coarsest solve, prolongation --
-// in one block, with every level's unknown and right-hand side in shared
-// memory and the face coefficients read through L1.  Phases are separated by
-// __syncthreads().  Each step does the arithmetic of the corresponding
+// in one block, with every level's unknown, right-hand side and face
+// coefficients in shared memory (the coefficients are staged once at the
+// start, so no phase waits on L2).  Phases are separated by __syncthreads().  Each step does the arithmetic of the corresponding
 // separate kernel in the same order (red-black update, children summed in z,
 // y, x order, slopes added x, y, z), so the cycle is the same cycle.
 #include "gbmg_internal.h"
@@ -149,40 +149,58 @@ __device__ void sub_coarse(int n, const T* __restrict__ minv, const T* __restric
   __syncthreads();
 }
 
+// Shared memory per level: sol, src, then the three face-coefficient arrays
+// (staged once at the start, so no phase waits on L2), n cells each.
 template <typename T>
 __global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
   pdl_enter();
   extern __shared__ unsigned char sub_raw[];
   T* base = reinterpret_cast<T*>(sub_raw);
   const int nl = S.nlev;
-  T* sol[kSubMaxLevels];
-  T* src[kSubMaxLevels];
+  const auto cells = [&](int l) { return S.lv[l].nx * S.lv[l].ny * S.lv[l].nz; };
+  const auto sol = [&](int l) { return base + S.off[l]; };
+  const auto src = [&](int l) { return base + S.off[l] + cells(l); };
   for (int l = 0; l < nl; ++l) {
-    sol[l] = base + S.off[l];
-    src[l] = sol[l] + S.lv[l].nx * S.lv[l].ny * S.lv[l].nz;
+    const int n = cells(l);
+    T* c = base + S.off[l] + 2 * n;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      c[q] = S.lv[l].cx[q];
+      c[n + q] = S.lv[l].cy[q];
+      c[2 * n + q] = S.lv[l].cz[q];
+    }
   }
+  // level l with its coefficients in shared memory
+  const auto lv = [&](int l) {
+    SubLevel<T> L = S.lv[l];
+    const int n = L.nx * L.ny * L.nz;
+    const T* c = base + S.off[l] + 2 * n;
+    L.cx = c;
+    L.cy = c + n;
+    L.cz = c + 2 * n;
+    return L;
+  };
   T* scratch = base + S.off[nl];
   {
     const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
-    for (int q = threadIdx.x; q < n0; q += blockDim.x) src[0][q] = S.src_in[q];
+    for (int q = threadIdx.x; q < n0; q += blockDim.x) src(0)[q] = S.src_in[q];
   }
   __syncthreads();
   for (int l = 0; l < nl - 1; ++l) {
-    for (int it = 0; it < S.nu1; ++it) sub_sweep(S.lv[l], sol[l], src[l], 0, it == 0);
+    for (int it = 0; it < S.nu1; ++it) sub_sweep(lv(l), sol(l), src(l), 0, it == 0);
     if (S.nu1 == 0) {
       const int n = S.lv[l].nx * S.lv[l].ny * S.lv[l].nz;
-      for (int q = threadIdx.x; q < n; q += blockDim.x) sol[l][q] = T(0);
+      for (int q = threadIdx.x; q < n; q += blockDim.x) sol(l)[q] = T(0);
       __syncthreads();
     }
-    sub_restrict(S.lv[l], sol[l], src[l], S.lv[l + 1], src[l + 1]);
+    sub_restrict(lv(l), sol(l), src(l), lv(l + 1), src(l + 1));
   }
-  sub_coarse(S.n_coarse, S.minv, S.adense, src[nl - 1], sol[nl - 1], scratch);
+  sub_coarse(S.n_coarse, S.minv, S.adense, src(nl - 1), sol(nl - 1), scratch);
   for (int l = nl - 2; l >= 0; --l) {
-    sub_prolong(S.lv[l], sol[l], S.lv[l + 1], sol[l + 1]);
-    for (int it = 0; it < S.nu2; ++it) sub_sweep(S.lv[l], sol[l], src[l], S.reverse ? 1 : 0, false);
+    sub_prolong(lv(l), sol(l), lv(l + 1), sol(l + 1));
+    for (int it = 0; it < S.nu2; ++it) sub_sweep(lv(l), sol(l), src(l), S.reverse ? 1 : 0, false);
   }
   const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
-  for (int q = threadIdx.x; q < n0; q += blockDim.x) S.sol_out[q] = sol[0][q];
+  for (int q = threadIdx.x; q < n0; q += blockDim.x) S.sol_out[q] = sol(0)[q];
 }
 
 }  // namespace
