@@ -66,6 +66,55 @@ __device__ __forceinline__ dw dw_from_double(double x) {
 
 __device__ __forceinline__ double dw_to_double(dw a) { return (double)a.hi + (double)a.lo; }
 
+// The same conversions with integer operations in place of the FP64
+// conversion instructions, which GB300 runs at its FP64 rate (1/57 of FP32):
+// results are bit-identical to dw_from_double / dw_to_double.
+//
+// dw_from_double_int: hi is x rounded to nearest-even at 24 bits, built from
+// x's exponent and top significand bits; the remainder x - hi is the exact
+// integer r = m - (top << 29) times 2^(e - 1075), and lo is r rounded to a
+// float (an exact int -> float rounding, then an exact power-of-two
+// scaling).  Inputs below 2^-74 (where lo could be subnormal) or near float
+// overflow take the FP64 path; zeros give (+-0, +0) as dw_from_double does.
+__device__ __forceinline__ dw dw_from_double_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned s = (unsigned)(b >> 63);
+  if ((b << 1) == 0ull) return dw{__uint_as_float(s << 31), 0.f};
+  const int e = (int)((b >> 52) & 0x7ffull);
+  const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+  long long top = (long long)(m >> 29);
+  const long long rb = (long long)(m & ((1ull << 29) - 1));
+  top += (rb > (1ll << 28) || (rb == (1ll << 28) && (top & 1))) ? 1 : 0;
+  const int carry = top == (1ll << 24) ? 1 : 0;
+  const int fe = e - 896 + carry;
+  if (e < 949 || fe > 254) return dw_from_double(x);
+  const unsigned hb =
+      (s << 31) | ((unsigned)fe << 23) | ((unsigned)(carry ? (top >> 1) : top) & 0x7fffffu);
+  const int r = (int)((long long)m - (top << 29));
+  float lo = 0.f;
+  if (r != 0) {
+    lo = __int_as_float(__float_as_int(__int2float_rn(r)) + (e - 1075) * (1 << 23));
+    if (s) lo = -lo;
+  }
+  return dw{__uint_as_float(hb), lo};
+}
+
+// float -> double, exactly, by moving the exponent and significand bits
+// (zeros included); subnormals, infinities and NaNs use the conversion.
+__device__ __forceinline__ double float_to_double_int(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+  if ((u << 1) == 0u) return __longlong_as_double((long long)sgn);
+  if (e == 0u || e == 255u) return (double)f;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+__device__ __forceinline__ double dw_to_double_int(dw a) {
+  return float_to_double_int(a.hi) + float_to_double_int(a.lo);
+}
+
 // Accumulator of sum_f c_f (p_nb - p_c) with cascaded summation: the high
 // parts are added error-free with TwoSum, everything of order u|term| goes
 // into one float.  Absolute error O(u^2 sum |c_f (p_nb - p_c)|), the bound the

@@ -658,7 +658,9 @@ int build_hierarchy(gbmg_handle* h) {
 // it off).  Captured graphs hold the level views, so a change drops them.
 void set_rho_form(gbmg_handle* h, bool on) {
   Level& f = h->lv[0];
-  bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0;
+  // (with the finest level inside the single-block bottom, sub_lc == 0, that
+  // block reads stored coefficients and the density form has no user)
+  bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0 && h->sub_lc > 0;
   if (const char* e = std::getenv("GBMG_RHO_COEF"))
     if (std::atoi(e) == 0) want = false;
   bool split = want && f.nx % 2 == 0 && h->L > 1 && f.fx == 2 && h->sub_lc > 0;
@@ -692,15 +694,17 @@ void set_rho_form(gbmg_handle* h, bool on) {
 int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   const gbmg_grid& g = h->grid;
   Level& f = h->lv[0];
-  float* c32[3] = {f.cx32, f.cy32, f.cz32};
-  float2* cw[3] = {h->cxw, h->cyw, h->czw};
-  LAUNCH(h, GBMG_PROF_SETUP,
-         launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
-                          h->rho, f.cx, f.cy, f.cz, h->mixed ? c32 : nullptr,
-                          h->mixed ? cw : nullptr, bulk_rho));
-  h->fine_copies = h->mixed;
   h->split_ready = false;
   set_rho_form(h, true);
+  // the FP32 finest-level coefficients are only read without the density form
+  float* c32[3] = {f.cx32, f.cy32, f.cz32};
+  float2* cw[3] = {h->cxw, h->cyw, h->czw};
+  const bool want32 = h->mixed && !f.rho32;
+  LAUNCH(h, GBMG_PROF_SETUP,
+         launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
+                          h->rho, f.cx, f.cy, f.cz, want32 ? c32 : nullptr,
+                          h->mixed ? cw : nullptr, bulk_rho));
+  h->fine_copies = h->mixed;
   if (h->mixed && f.split)
     LAUNCH(h, GBMG_PROF_SETUP,
            launch_to_split(h->stream, h->rho, h->rho32, f.nx, f.ny, f.nz, f.hstride));

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
 __global__ void k_to_dw(const double* __restrict__ a, float2* __restrict__ out, size_t n) {
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
        q += (size_t)gridDim.x * blockDim.x) {
-    const dw v = dw_from_double(a[q]);
+    const dw v = dw_from_double_int(a[q]);
     out[q] = make_float2(v.hi, v.lo);
   }
 }
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict
   double acc[1] = {0.0};
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
        q += (size_t)gridDim.x * blockDim.x)
-    acc[0] += dw_to_double(dw_ldg(p + q));
+    acc[0] += dw_to_double_int(dw_ldg(p + q));
   grid_sum_finish<1>(acc, R, slot);
 }
 
@@ -273,7 +273,7 @@ __global__ void k_dw_out(const float2* __restrict__ p, double* __restrict__ out,
   const double m = R.result[slot] / (double)n;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
        q += (size_t)gridDim.x * blockDim.x)
-    out[q] = dw_to_double(dw_ldg(p + q)) - m;
+    out[q] = dw_to_double_int(dw_ldg(p + q)) - m;
 }
 
 inline unsigned stride_blocks(size_t n) {

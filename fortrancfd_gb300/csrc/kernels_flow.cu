@@ -11,7 +11,9 @@
 // ns_solvers.f90:55-83").
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
+#include "dword.cuh"
 #include "gbmg_internal.h"
 #include "reduce.cuh"
 
@@ -32,26 +34,35 @@ inline unsigned stride_blocks(size_t n) {
 // set by the host) the division phi/eps would land past the clipping
 // threshold anyway, so H is 0 or 1 without computing it: the same result as
 // the full branch, with the FP64 division done only in the band.
+// The outside test compares bit patterns (|phi| > eps_out as integers;
+// NaN stays on the full branch), and outside cells store the two bulk values
+// rho_pos*1 + rho_neg*0 and rho_pos*0 + rho_neg*1 computed by the host: the
+// full formula's result for H = 1 and 0, without FP64 work.
 __global__ void __launch_bounds__(256) k_rho_from_phi(int nx, int ny, int nz, Strided phi,
-                                                      double eps, double eps_out, double rho_pos,
-                                                      double rho_neg, double* rho) {
+                                                      double eps, long long eps_out_bits,
+                                                      double rho_pos, double rho_neg,
+                                                      double bulk_pos, double bulk_neg,
+                                                      double* rho) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const double pi = 3.141592653589793;
   const double ph = phi.data[i + j * phi.sy + k * phi.sz];
-  double h;
-  if (ph > eps_out) h = 1.0;
-  else if (ph < -eps_out) h = 0.0;
-  else {
-    const double x = ph / eps;
-    if (x > 1.0 - 1e-12) h = 1.0;
-    else if (x < -1.0 + 1e-12) h = 0.0;
-    else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+  const long long pb = __double_as_longlong(ph);
+  const long long mag = pb & 0x7fffffffffffffffll;
+  double* out = rho + ((size_t)k * ny + j) * nx + i;
+  if (mag > eps_out_bits && mag <= 0x7ff0000000000000ll) {
+    *out = pb < 0 ? bulk_neg : bulk_pos;
+    return;
   }
+  double h;
+  const double x = ph / eps;
+  if (x > 1.0 - 1e-12) h = 1.0;
+  else if (x < -1.0 + 1e-12) h = 0.0;
+  else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
   h = fmax(fmin(h, 1.0), 0.0);
-  rho[((size_t)k * ny + j) * nx + i] = rho_pos * h + rho_neg * (1.0 - h);
+  *out = rho_pos * h + rho_neg * (1.0 - h);
 }
 
 __global__ void __launch_bounds__(256) k_copy_in(int nx, int ny, int nz, Strided src, double* dst) {
@@ -78,7 +89,8 @@ __global__ void __launch_bounds__(256) k_copy_out(int nx, int ny, int nz, const 
 // result, one FP64 division instead of two).  Optionally also writes the
 // FP32 copies of the cycle and the double-word copies of the defect kernel.
 struct BulkFaces {
-  double s[2];        // 2 rho of the two bulk densities
+  long long r[2];     // bit patterns of the two bulk densities (never equal to a double
+                      // when there are none: a NaN pattern no density takes)
   double c[3][2];     // face coefficient per axis and bulk density
   float c32[3][2];
   float2 cw[3][2];
@@ -94,24 +106,28 @@ __device__ __forceinline__ void face_store(const FaceOut& o, size_t q, double v)
   o.c[q] = v;
   if (o.c32) o.c32[q] = (float)v;
   if (o.cw) {
-    const float hi = __double2float_rn(v);
-    o.cw[q] = make_float2(hi, __double2float_rn(v - (double)hi));
+    const dw d = dw_from_double_int(v);
+    o.cw[q] = make_float2(d.hi, d.lo);
   }
 }
 
 // The face value for rho_i + rho_nb = s along axis a (0 on walls); faces
 // between two cells of a bulk density (s equal to one of the two precomputed
 // sums) take the host-computed values, computed with the same IEEE operations.
-__device__ __forceinline__ void face_value(const BulkFaces& B, int a, double s, double h2,
-                                           double ih2, bool pow2, const FaceOut& o, size_t q) {
+// ra, rb: the two cells' densities.  The bulk test compares bit patterns
+// (integer operations; FP64 compares and adds run at GB300's FP64 rate).
+__device__ __forceinline__ void face_value(const BulkFaces& B, int a, double ra, double rb,
+                                           double h2, double ih2, bool pow2, const FaceOut& o,
+                                           size_t q) {
+  const long long ba = __double_as_longlong(ra), bb = __double_as_longlong(rb);
   for (int v = 0; v < 2; ++v)
-    if (s == B.s[v]) {
+    if (ba == B.r[v] && bb == B.r[v]) {
       o.c[q] = B.c[a][v];
       if (o.c32) o.c32[q] = B.c32[a][v];
       if (o.cw) o.cw[q] = B.cw[a][v];
       return;
     }
-  const double t = 2.0 / s;
+  const double t = 2.0 / (ra + rb);
   face_store(o, q, pow2 ? t * ih2 : t / h2);
 }
 
@@ -125,11 +141,11 @@ __global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, doubl
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
   const double r = rho[q];
-  if (i > 0) face_value(B, 0, r + rho[q - 1], h2.x, ih2.x, pow2 & 1, ox, q);
+  if (i > 0) face_value(B, 0, r, rho[q - 1], h2.x, ih2.x, pow2 & 1, ox, q);
   else face_store(ox, q, 0.0);
-  if (j > 0) face_value(B, 1, r + rho[q - nx], h2.y, ih2.y, pow2 & 2, oy, q);
+  if (j > 0) face_value(B, 1, r, rho[q - nx], h2.y, ih2.y, pow2 & 2, oy, q);
   else face_store(oy, q, 0.0);
-  if (k > 0) face_value(B, 2, r + rho[q - (size_t)nx * ny], h2.z, ih2.z, pow2 & 4, oz, q);
+  if (k > 0) face_value(B, 2, r, rho[q - (size_t)nx * ny], h2.z, ih2.z, pow2 & 4, oz, q);
   else face_store(oz, q, 0.0);
 }
 
@@ -352,10 +368,14 @@ static inline dim3 grid3(int nx, int ny, int nz) {
 
 void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, double eps,
                          double rho_pos, double rho_neg, double* rho) {
-  // phi > eps_out implies fl(phi/eps) > 1 - 1e-12 (margin 1e-15 >> rounding)
+  // |phi| > eps_out implies |fl(phi/eps)| > 1 - 1e-12 (margin 1e-15 >> rounding)
   const double eps_out = eps * (1.0 - 1e-12) * (1.0 + 1e-15);
-  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, phi, eps, eps_out, rho_pos,
-                                                          rho_neg, rho);
+  long long eps_bits;
+  std::memcpy(&eps_bits, &eps_out, sizeof eps_bits);
+  const double bulk_pos = rho_pos * 1.0 + rho_neg * (1.0 - 1.0);
+  const double bulk_neg = rho_pos * 0.0 + rho_neg * (1.0 - 0.0);
+  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
+      nx, ny, nz, phi, eps, eps_bits, rho_pos, rho_neg, bulk_pos, bulk_neg, rho);
 }
 
 void launch_copy_in(cudaStream_t s, int nx, int ny, int nz, Strided src, double* dst) {
@@ -379,10 +399,13 @@ void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double
   const double h2[3] = {dx2, dy2, dz2};
   BulkFaces B;
   for (int v = 0; v < 2; ++v) {
-    // NaN never compares equal: no bulk shortcut without known bulk densities
-    B.s[v] = bulk_rho ? bulk_rho[v] + bulk_rho[v] : std::nan("");
+    double rv = std::nan("");
+    if (bulk_rho) rv = bulk_rho[v];
+    std::memcpy(&B.r[v], &rv, sizeof rv);
+    if (!bulk_rho) B.r[v] = 0x7ff8dead0000beefll;  // a NaN pattern: matches no density
+    const double sv = rv + rv;
     for (int a = 0; a < 3; ++a) {
-      const double t = 2.0 / B.s[v];
+      const double t = 2.0 / sv;
       const double c = ((pow2 >> a) & 1) ? t * (1.0 / h2[a]) : t / h2[a];
       B.c[a][v] = c;
       B.c32[a][v] = (float)c;

@@ -15,6 +15,7 @@
 // two spacing are products with its exact reciprocal.
 #include <cmath>
 
+#include "dword.cuh"
 #include "gbmg_internal.h"
 
 namespace gbmg {
@@ -148,8 +149,8 @@ __global__ void __launch_bounds__(256) k_face_const(int nx, int ny, int nz, doub
     const double vv[3] = {vx, vy, vz};
     float2* o[3] = {cxw, cyw, czw};
     for (int a = 0; a < 3; ++a) {
-      const float hi = __double2float_rn(vv[a]);
-      o[a][q] = make_float2(hi, __double2float_rn(vv[a] - (double)hi));
+      const dw d = dw_from_double_int(vv[a]);
+      o[a][q] = make_float2(d.hi, d.lo);
     }
   }
 }

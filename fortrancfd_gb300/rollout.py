@@ -3,16 +3,14 @@
 The bubbles' level set is phi = min_b (|x - c_b| - r_b) written in torch, so
 it is differentiable with respect to the centres c_b and radii r_b; each step
 translates the bubbles rigidly, builds b_k = div(u*_k)/dt from a fresh seeded
-u*_k on the GPU, and solves p_k = PressureSolve(phi_k, b_k).  The loss is
+u*_k drawn on the GPU, and solves p_k = PressureSolve(phi_k, b_k).  The loss is
 J = sum_k |p_k|^2 / 2.  Memory per step: PressureSolve keeps phi_k and p_k
 only (the operator is rebuilt and the adjoint solved in backward), and the
 level-set construction is checkpointed (recomputed in backward).
 """
-import numpy as np
 import torch
 from torch.utils.checkpoint import checkpoint
 
-from . import inputs
 from .autograd import pressure_solve
 from .ppe import PressurePoisson
 
@@ -37,11 +35,29 @@ def level_set(centers, radii, shape, extent):
     return phi
 
 
+def step_velocity(case, k, device):
+    """u*_k, v*_k, w*_k ~ N(0,1) on interior faces, 0 on walls, drawn on the
+    device from a generator seeded with (case.seed, k)."""
+    g = torch.Generator(device=device)
+    g.manual_seed(int(case.seed) * 100003 + 1000 + int(k))
+    nz, ny, nx = case.shape
+    f64 = torch.float64
+    u = torch.randn((nz, ny, nx + 1), generator=g, device=device, dtype=f64)
+    v = torch.randn((nz, ny + 1, nx), generator=g, device=device, dtype=f64)
+    w = torch.randn((nz + 1, ny, nx), generator=g, device=device, dtype=f64)
+    u[..., 0] = 0.0
+    u[..., -1] = 0.0
+    v[:, 0, :] = 0.0
+    v[:, -1, :] = 0.0
+    w[0] = 0.0
+    w[-1] = 0.0
+    return u, v, w
+
+
 def step_rhs(case, solver: PressurePoisson, k, device):
-    """b_k = div(u*_k)/dt on the GPU, u*_k ~ N(0,1) from seed (case.seed, k)."""
-    u, v, w = inputs.velocity(case, seed=[case.seed, 1000 + k])
-    t = [torch.from_numpy(np.ascontiguousarray(a)).to(device) for a in (u, v, w)]
-    return solver.divergence(t[0], t[1], t[2], case.dt)
+    """b_k = div(u*_k)/dt on the GPU from step_velocity."""
+    u, v, w = step_velocity(case, k, device)
+    return solver.divergence(u, v, w, case.dt)
 
 
 def rollout_loss(centers, radii, case, solver: PressurePoisson, steps=None, tol=1e-10,
