@@ -422,10 +422,12 @@ def adjoint_section(dev, stream, reps=5, scale=1):
             e0.record(stream)
             p = pressure_solve(x, b, s, tol=1e-10, adjoint_tol=ADJ_TOL, **kw)
             e1.record(stream)
+            fwd_cycles = s.last_stats["cycles"]
             loss = 0.5 * ((p - p_t) ** 2).sum()
             loss.backward()
             e2.record(stream)
             torch.cuda.synchronize()
+            adj_cycles = s.last_stats["cycles"]
             if it:
                 fw.append(e0.elapsed_time(e1))
                 bw.append(e1.elapsed_time(e2))
@@ -449,6 +451,7 @@ def adjoint_section(dev, stream, reps=5, scale=1):
     return {"workload": f"{case.name}: {case.shape[2]}x{case.shape[1]} cells, 8 circles, mixed "
                         "precision, flexible CG, tol 1e-10 forward, 1e-8 adjoint",
             "forward_ms": f, "backward_ms": bk, "backward_over_forward": bk / f,
+            "forward_iterations": fwd_cycles, "adjoint_iterations": adj_cycles,
             "fd_max_rel_err": max(errs), "fd_directions": len(errs)}
 
 

@@ -225,6 +225,7 @@ class PressurePoisson:
         st = _lib.Stats()
         rc = self._L.gbmg_solve(self._h, fb, fp, float(tol), m, C.byref(st))
         stats = st.as_dict()
+        self.last_stats = stats
         self._finish(rc, stats, check, "solve")
         return p, stats
 
