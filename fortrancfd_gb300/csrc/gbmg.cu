@@ -87,7 +87,10 @@ struct gbmg_handle {
   int pcur = 0;  // which pw holds the current pressure
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
-  int* derr = nullptr;   // device error flags (TMA wait timeouts)
+  int* derr = nullptr;   // device error flags (TMA wait and grid barrier timeouts)
+  unsigned* bar = nullptr;  // grid barrier of the mid-cycle kernel: arrivals, generation
+  bool mid_ok = false;      // middle levels in one cooperative launch
+  int mid_grid = 0;         // its block count (all resident)
   DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B],
                                 // then [p buffer] with a colour-split e (buffer A)
   bool dmaps_split = false;     // whether the colour-split entries were made
@@ -319,6 +322,22 @@ SubCycle<T> make_subcycle(gbmg_handle* h, bool reverse) {
   return S;
 }
 
+// Levels 1 .. top-1 and the bottom block as one cooperative launch.
+template <typename T>
+MidCycle<T> make_midcycle(gbmg_handle* h, bool reverse) {
+  MidCycle<T> M{};
+  const int top = h->sub_lc;
+  M.nmid = top - 1;
+  for (int i = 0; i <= M.nmid; ++i) M.lv[i] = view<T>(h->lv[1 + i]);
+  M.bottom = make_subcycle<T>(h, reverse);
+  M.nu1 = h->prm.nu1;
+  M.nu2 = h->prm.nu2;
+  M.reverse = reverse ? 1 : 0;
+  M.bar = h->bar;
+  M.err = h->derr;
+  return M;
+}
+
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
 // the post-smoothing colours black-first (symmetric preconditioner for CG).
 // zero_fine: the level-0 unknown starts at zero (correction and Krylov
@@ -329,6 +348,23 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
   const cudaStream_t s = h->stream;
   const bool pre = h->prm.nu1 > 0;
   const int top = std::min(h->sub_lc, L - 1);  // levels above the bottom block
+  if (h->mid_ok) {
+    // finest level by its own kernels, the rest in one cooperative launch
+    for (int it = 0; it < h->prm.nu1; ++it) sweep<T>(h, 0, 0, it == 0 && zero_fine);
+    LAUNCH(h, GBMG_PROF_RESTRICT_FINE,
+           launch_restrict<T>(s, view_next<T>(h->lv[0]), view<T>(h->lv[1]), !pre));
+    cudaError_t e = cudaSuccess;
+    LAUNCH(h, GBMG_PROF_SMOOTH_COARSE,
+           e = launch_midcycle<T>(s, make_midcycle<T>(h, reverse_post), h->mid_grid));
+    if (e != cudaSuccess) {
+      h->err = std::string("mid-cycle launch: ") + cudaGetErrorString(e);
+      return GBMG_CUDA_ERROR;
+    }
+    LAUNCH(h, GBMG_PROF_PROLONG_FINE,
+           launch_prolong<T>(s, view_next<T>(h->lv[0]), view<T>(h->lv[1])));
+    for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, 0, reverse_post ? 1 : 0, false);
+    return check_launch(h, "v-cycle");
+  }
   for (int l = 0; l < top; ++l) {
     for (int it = 0; it < h->prm.nu1; ++it)
       sweep<T>(h, l, 0, it == 0 && (l > 0 || zero_fine));
@@ -411,6 +447,7 @@ int free_all(gbmg_handle* h) {
   dfree(h->aux[0]); dfree(h->aux[1]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
   dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
+  dfree(h->bar);
   delete[] h->dmaps;
   h->dmaps = nullptr;
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
@@ -444,6 +481,30 @@ void setup_subcycle(gbmg_handle* h) {
   const SubCycle<T> S = make_subcycle<T>(h, false);
   const size_t smem = subcycle_smem<T>(S);
   if (smem > 200 * 1024 || subcycle_init<T>(smem) != 0) h->sub_lc = h->L;
+}
+
+// The cooperative mid-cycle: levels strictly between the finest and the
+// bottom block (at least one of them), GBMG_MIDCYCLE=0 switches it off.
+template <typename T>
+int setup_midcycle(gbmg_handle* h) {
+  h->mid_ok = false;
+  if (const char* e = std::getenv("GBMG_MIDCYCLE"))
+    if (std::atoi(e) == 0) return GBMG_OK;
+  const int nmid = h->sub_lc - 1;
+  if (h->sub_lc >= h->L || nmid < 1 || nmid > kMidMaxLevels) return GBMG_OK;
+  const size_t smem = subcycle_smem<T>(make_subcycle<T>(h, false));
+  int grid = 0;
+  if (midcycle_init<T>(smem, &grid) != 0 || grid < 1) {
+    cudaGetLastError();
+    return GBMG_OK;  // keep the separate launches
+  }
+  if (!h->bar) {
+    GB_TRY(dmalloc(h, &h->bar, 2));
+    GB_CUDA(h, cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), h->stream));
+  }
+  h->mid_grid = grid;
+  h->mid_ok = true;
+  return GBMG_OK;
 }
 
 int setup_tma(gbmg_handle* h) {
@@ -570,6 +631,8 @@ int allocate(gbmg_handle* h) {
   if (h->mixed) GB_TRY(setup_tma(h));
   if (h->mixed) setup_subcycle<float>(h);
   else setup_subcycle<double>(h);
+  if (h->mixed) GB_TRY(setup_midcycle<float>(h));
+  else GB_TRY(setup_midcycle<double>(h));
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -897,7 +960,8 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     GB_CUDA(h, cudaMemcpyAsync(&flags, h->derr, sizeof(int), cudaMemcpyDeviceToHost, s));
     GB_CUDA(h, cudaStreamSynchronize(s));
     if (flags) {
-      h->err = "a TMA wait timed out inside the sweep kernel";
+      h->err = (flags & 2) ? "the grid barrier of the mid-cycle kernel timed out"
+                           : "a TMA wait timed out inside the sweep kernel";
       cudaMemsetAsync(h->derr, 0, sizeof(int), s);
       return GBMG_CUDA_ERROR;
     }

@@ -88,6 +88,26 @@ struct SubCycle {
   const T* minv;
   const T* adense;
 };
+// The middle levels (between the finest and the bottom block) in one
+// cooperative launch (subcycle.cu).
+constexpr int kMidMaxLevels = 8;
+constexpr int kMidThreads = 512;
+template <typename T>
+struct MidCycle {
+  int nmid;                          // middle levels, lv[0 .. nmid-1], finest first
+  LevelView<T> lv[kMidMaxLevels + 1];  // ... and lv[nmid], the bottom's top level
+  SubCycle<T> bottom;                // the single-block bottom, from lv[nmid] down
+  int nu1, nu2, reverse;
+  unsigned* bar;                     // grid barrier: arrivals, generation
+  int* err;                          // device error flags
+};
+template <typename T>
+size_t midcycle_smem(const MidCycle<T>& M);
+template <typename T>
+int midcycle_init(size_t smem, int* grid_blocks);
+template <typename T>
+cudaError_t launch_midcycle(cudaStream_t s, const MidCycle<T>& M, int grid_blocks);
+
 template <typename T>
 size_t subcycle_smem(const SubCycle<T>& S);
 template <typename T>

@@ -10,6 +10,7 @@
 // separate kernel in the same order (red-black update, children summed in z,
 // y, x order, slopes added x, y, z), so the cycle is the same cycle.
 #include "gbmg_internal.h"
+#include "mg_cells.cuh"
 #include "pdl.cuh"
 
 namespace gbmg {
@@ -152,10 +153,7 @@ __device__ void sub_coarse(int n, const T* __restrict__ minv, const T* __restric
 // Shared memory per level: sol, src, then the three face-coefficient arrays
 // (staged once at the start, so no phase waits on L2), n cells each.
 template <typename T>
-__global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
-  pdl_enter();
-  extern __shared__ unsigned char sub_raw[];
-  T* base = reinterpret_cast<T*>(sub_raw);
+__device__ void subcycle_body(const SubCycle<T>& S, T* base) {
   const int nl = S.nlev;
   const auto cells = [&](int l) { return S.lv[l].nx * S.lv[l].ny * S.lv[l].nz; };
   const auto sol = [&](int l) { return base + S.off[l]; };
@@ -182,7 +180,7 @@ __global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
   T* scratch = base + S.off[nl];
   {
     const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
-    for (int q = threadIdx.x; q < n0; q += blockDim.x) src(0)[q] = S.src_in[q];
+    for (int q = threadIdx.x; q < n0; q += blockDim.x) src(0)[q] = __ldcg(S.src_in + q);
   }
   __syncthreads();
   for (int l = 0; l < nl - 1; ++l) {
@@ -201,6 +199,137 @@ __global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
   }
   const int n0 = S.lv[0].nx * S.lv[0].ny * S.lv[0].nz;
   for (int q = threadIdx.x; q < n0; q += blockDim.x) S.sol_out[q] = sol(0)[q];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSubThreads) k_subcycle(SubCycle<T> S) {
+  pdl_enter();
+  extern __shared__ unsigned char sub_raw[];
+  subcycle_body(S, reinterpret_cast<T*>(sub_raw));
+}
+
+// ---- the middle of the cycle: one cooperative launch ------------------------
+// Levels between the finest and the single-block bottom (128^3 .. 32^3 for a
+// 256^3 grid) take a few microseconds of work per sweep colour but one launch
+// each, ~30 launches per cycle.  k_midcycle runs all their phases -- sweeps,
+// residual + restriction, the bottom block (block 0 alone, in its shared
+// memory), prolongation -- in one cooperative launch whose blocks are all
+// resident, separated by a grid barrier.  Every phase calls the per-cell
+// functions of the separate kernels (mg_cells.cuh), reading the unknowns past
+// L1 because other blocks rewrite them between phases, so the cycle is the
+// same cycle, bit for bit.
+//
+// The barrier is bounded: a block that waits more than kBarrierSpins polls
+// sets kErrBarrierTimeout and the kernel returns (every other block then
+// times out at its next barrier), so a fault of the co-residency assumption
+// can only end the launch, never hang it.
+constexpr unsigned kBarrierSpins = 1u << 22;
+constexpr int kErrBarrierTimeout = 2;
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = bar + 1;
+    const unsigned g = *gen;
+    int good = 1;
+    __threadfence();
+    if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          atomicOr(err, kErrBarrierTimeout);
+          good = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ void mid_colour(const LevelView<T>& L, int color, bool zero) {
+  const int hx = (L.nx + 1) / 2;
+  const size_t n = (size_t)hx * L.ny * L.nz;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int m = (int)(t % hx);
+    const size_t row = t / hx;
+    const int j = (int)(row % L.ny), k = (int)(row / L.ny);
+    const int i = 2 * m + ((j + k + color) & 1);
+    if (i >= L.nx) continue;
+    if (L.idiag) {
+      if (zero) cells::smooth_cell<T, true, true, false, true>(L, i, j, k);
+      else cells::smooth_cell<T, true, false, false, true>(L, i, j, k);
+    } else {
+      if (zero) cells::smooth_cell<T, false, true, false, true>(L, i, j, k);
+      else cells::smooth_cell<T, false, false, false, true>(L, i, j, k);
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void mid_restrict(const LevelView<T>& F, const LevelView<T>& C,
+                                             int zero_sol) {
+  const size_t n = (size_t)C.nx * C.ny * C.nz;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int I = (int)(t % C.nx);
+    const size_t row = t / C.nx;
+    cells::restrict_cell<T, false, true>(F, C, I, (int)(row % C.ny), (int)(row / C.ny), zero_sol);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void mid_prolong(const LevelView<T>& F, const LevelView<T>& C) {
+  const size_t n = (size_t)C.nx * C.ny * C.nz;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const int I = (int)(t % C.nx);
+    const size_t row = t / C.nx;
+    cells::prolong_cell<T, true>(F, C, I, (int)(row % C.ny), (int)(row / C.ny));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMidThreads) k_midcycle(MidCycle<T> M) {
+  extern __shared__ unsigned char mid_raw[];
+  T* base = reinterpret_cast<T*>(mid_raw);
+  const int nm = M.nmid;
+  // down: levels 0 .. nm-1 of M.lv are the middle levels, M.lv[nm] the bottom's top
+  for (int l = 0; l < nm; ++l) {
+    for (int it = 0; it < M.nu1; ++it) {
+      mid_colour(M.lv[l], 0, it == 0);
+      if (!grid_barrier(M.bar, M.err)) return;
+      mid_colour(M.lv[l], 1, false);
+      if (!grid_barrier(M.bar, M.err)) return;
+    }
+    mid_restrict(M.lv[l], M.lv[l + 1], M.nu1 > 0 ? 0 : 1);
+    if (!grid_barrier(M.bar, M.err)) return;
+  }
+  if (blockIdx.x == 0) subcycle_body(M.bottom, base);
+  if (!grid_barrier(M.bar, M.err)) return;
+  const int c0 = M.reverse ? 1 : 0;
+  for (int l = nm - 1; l >= 0; --l) {
+    mid_prolong(M.lv[l], M.lv[l + 1]);
+    if (!grid_barrier(M.bar, M.err)) return;
+    for (int it = 0; it < M.nu2; ++it) {
+      mid_colour(M.lv[l], c0, false);
+      if (!grid_barrier(M.bar, M.err)) return;
+      mid_colour(M.lv[l], 1 - c0, false);
+      if (l > 0 || it + 1 < M.nu2)  // the last phase ends with the kernel
+        if (!grid_barrier(M.bar, M.err)) return;
+    }
+  }
 }
 
 }  // namespace
@@ -229,5 +358,48 @@ template int subcycle_init<float>(size_t);
 template int subcycle_init<double>(size_t);
 template void launch_subcycle<float>(cudaStream_t, const SubCycle<float>&);
 template void launch_subcycle<double>(cudaStream_t, const SubCycle<double>&);
+
+template <typename T>
+size_t midcycle_smem(const MidCycle<T>& M) {
+  return subcycle_smem(M.bottom);  // block 0 runs the bottom in its shared memory
+}
+
+template <typename T>
+int midcycle_init(size_t smem, int* grid_blocks) {
+  if (cudaFuncSetAttribute(k_midcycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0, dev = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_midcycle<T>, kMidThreads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    return -1;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+  *grid_blocks = per_sm * sms;
+  return 0;
+}
+
+template <typename T>
+cudaError_t launch_midcycle(cudaStream_t s, const MidCycle<T>& M, int grid_blocks) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid_blocks);
+  cfg.blockDim = dim3(kMidThreads);
+  cfg.dynamicSmemBytes = midcycle_smem(M);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_midcycle<T>, M);
+}
+
+template size_t midcycle_smem<float>(const MidCycle<float>&);
+template size_t midcycle_smem<double>(const MidCycle<double>&);
+template int midcycle_init<float>(size_t, int*);
+template int midcycle_init<double>(size_t, int*);
+template cudaError_t launch_midcycle<float>(cudaStream_t, const MidCycle<float>&, int);
+template cudaError_t launch_midcycle<double>(cudaStream_t, const MidCycle<double>&, int);
 
 }  // namespace gbmg

@@ -350,3 +350,21 @@ def test_colour_split_layout_is_bit_identical(cuda, monkeypatch, idx, scale, kry
     (p0, s0), (p1, s1) = out["0"], out["1"]
     assert s0["status"] == 0 and s0["cycles"] == s1["cycles"]
     np.testing.assert_array_equal(p1, p0)
+
+
+@pytest.mark.parametrize("precision,idx,scale,krylov", [
+    ("mixed", 1, 2, False), ("fp64", 1, 2, False), ("mixed", 4, 2, True), ("fp64", 1, 4, True)])
+def test_cooperative_mid_cycle_is_bit_identical(cuda, monkeypatch, precision, idx, scale, krylov):
+    """The levels between the finest and the single-block bottom run as one
+    cooperative launch (GBMG_MIDCYCLE=0 runs them as separate launches) with
+    the same per-cell functions: same cycles, same bits."""
+    c = cases.config(idx, scale)
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("GBMG_MIDCYCLE", flag)
+        with solver(c, precision=precision, krylov=krylov, max_cycles=400) as s:
+            s.ppe_init(c.rho)
+            out[flag] = s.solve(c.b, tol=1e-10)
+    (p0, s0), (p1, s1) = out["0"], out["1"]
+    assert s0["status"] == 0 and s0["cycles"] == s1["cycles"]
+    np.testing.assert_array_equal(p1, p0)
