@@ -963,6 +963,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
       h->err = (flags & 2) ? "the grid barrier of the mid-cycle kernel timed out"
                            : "a TMA wait timed out inside the sweep kernel";
       cudaMemsetAsync(h->derr, 0, sizeof(int), s);
+      if (h->bar) cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), s);  // arrivals left over
       return GBMG_CUDA_ERROR;
     }
   }
