@@ -484,12 +484,16 @@ void setup_subcycle(gbmg_handle* h) {
 }
 
 // The cooperative mid-cycle: levels strictly between the finest and the
-// bottom block (at least one of them), GBMG_MIDCYCLE=0 switches it off.
+// bottom block (at least one of them).  Opt-in (GBMG_MIDCYCLE=1): on the 256^3
+// benchmark it measured 263 us per cycle against about 150 us for the same
+// levels as separate launches overlapped by programmatic dependent launch in
+// the captured graph (its bottom phase runs on one block while the others
+// wait, and each of its ~36 phases ends in a grid barrier).
 template <typename T>
 int setup_midcycle(gbmg_handle* h) {
   h->mid_ok = false;
-  if (const char* e = std::getenv("GBMG_MIDCYCLE"))
-    if (std::atoi(e) == 0) return GBMG_OK;
+  const char* ev = std::getenv("GBMG_MIDCYCLE");
+  if (!ev || std::atoi(ev) == 0) return GBMG_OK;
   const int nmid = h->sub_lc - 1;
   if (h->sub_lc >= h->L || nmid < 1 || nmid > kMidMaxLevels) return GBMG_OK;
   const size_t smem = subcycle_smem<T>(make_subcycle<T>(h, false));

@@ -355,9 +355,9 @@ def test_colour_split_layout_is_bit_identical(cuda, monkeypatch, idx, scale, kry
 @pytest.mark.parametrize("precision,idx,scale,krylov", [
     ("mixed", 1, 2, False), ("fp64", 1, 2, False), ("mixed", 4, 2, True), ("fp64", 1, 4, True)])
 def test_cooperative_mid_cycle_is_bit_identical(cuda, monkeypatch, precision, idx, scale, krylov):
-    """The levels between the finest and the single-block bottom run as one
-    cooperative launch (GBMG_MIDCYCLE=0 runs them as separate launches) with
-    the same per-cell functions: same cycles, same bits."""
+    """The levels between the finest and the single-block bottom as one
+    cooperative launch (GBMG_MIDCYCLE=1; the default runs them as separate
+    launches) with the same per-cell functions: same cycles, same bits."""
     c = cases.config(idx, scale)
     out = {}
     for flag in ("0", "1"):
