@@ -309,7 +309,14 @@ SubCycle<T> make_subcycle(gbmg_handle* h, bool reverse) {
   int off = 0;
   for (int i = 0; i < S.nlev; ++i) {
     const LevelView<T> V = view<T>(h->lv[lc + i]);
-    S.lv[i] = SubLevel<T>{V.nx, V.ny, V.nz, V.fx, V.fy, V.fz, V.cx, V.cy, V.cz};
+    const auto log2_of = [](int v) {
+      int l = 0;
+      while ((1 << l) < v) ++l;
+      return (1 << l) == v ? l : -1;
+    };
+    const int lx = log2_of(V.nx), ly = log2_of(V.ny);
+    S.lv[i] = SubLevel<T>{V.nx, V.ny, V.nz, V.fx, V.fy, V.fz, V.cx, V.cy, V.cz,
+                          (lx >= 0 && ly >= 0) ? lx : -1, (lx >= 0 && ly >= 0) ? ly : -1};
     S.off[i] = off;
     off += 5 * V.nx * V.ny * V.nz;  // sol, src and the three coefficient arrays
   }

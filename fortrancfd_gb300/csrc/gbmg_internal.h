@@ -77,6 +77,7 @@ struct SubLevel {
   const T* cx;
   const T* cy;
   const T* cz;
+  int lx, ly;  // log2 of nx and ny when both are powers of two (index by shifts), else -1
 };
 template <typename T>
 struct SubCycle {

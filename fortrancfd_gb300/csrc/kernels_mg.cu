@@ -193,27 +193,33 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
     W[e] = 0.0;
   }
   __syncthreads();
-  // right-looking Cholesky, lower triangle in place
+  // right-looking Cholesky, lower triangle in place; the trailing update is
+  // walked as a 16 x 16 thread grid over (row, column) without divisions
+  __shared__ double rdiag[kMaxCoarse];  // 1/L_jj
+  const int tx = t % 16, ty = t / 16;
   for (int j = 0; j < n; ++j) {
-    if (t == 0) M[j * n + j] = sqrt(M[j * n + j]);
+    if (t == 0) {
+      const double d = sqrt(M[j * n + j]);
+      M[j * n + j] = d;
+      rdiag[j] = 1.0 / d;
+    }
     __syncthreads();
-    const double djj = M[j * n + j];
-    for (int i = j + 1 + t; i < n; i += nt) M[i * n + j] /= djj;
+    const double rjj = rdiag[j];
+    for (int i = j + 1 + t; i < n; i += nt) M[i * n + j] *= rjj;
     __syncthreads();
-    const int m = n - j - 1;  // trailing block (j+1..n-1)^2, lower part
-    for (int e = t; e < m * m; e += nt) {
-      const int i = j + 1 + e / m, k = j + 1 + e % m;
-      if (k <= i) M[i * n + k] -= M[i * n + j] * M[k * n + j];
+    for (int i = j + 1 + ty; i < n; i += 16) {
+      const double lij = M[i * n + j];
+      for (int k = j + 1 + tx; k <= i; k += 16) M[i * n + k] -= lij * M[k * n + j];
     }
     __syncthreads();
   }
   // W = L^{-1}: forward substitution, one column per thread
   for (int c = t; c < n; c += nt) {
-    W[c * n + c] = 1.0 / M[c * n + c];
+    W[c * n + c] = rdiag[c];
     for (int i = c + 1; i < n; ++i) {
       double acc = 0.0;
       for (int k = c; k < i; ++k) acc += M[i * n + k] * W[k * n + c];
-      W[i * n + c] = -acc / M[i * n + i];
+      W[i * n + c] = -acc * rdiag[i];
     }
   }
   __syncthreads();

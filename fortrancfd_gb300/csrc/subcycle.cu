@@ -34,13 +34,43 @@ __device__ __forceinline__ void sub_stencil(const SubLevel<T>& L, const T* __res
   if (k < L.nz - 1) { c = L.cz[q + sz]; s += c * p[q + sz]; d += c; }
 }
 
-// one colour of a red-black sweep on a shared-memory level
+// (i, j, k) of cell q: shifts and masks for power-of-two levels
+template <typename T>
+__device__ __forceinline__ void sub_ijk(const SubLevel<T>& L, int q, int& i, int& j, int& k) {
+  if (L.lx >= 0) {
+    i = q & (L.nx - 1);
+    j = (q >> L.lx) & (L.ny - 1);
+    k = q >> (L.lx + L.ly);
+  } else {
+    i = q % L.nx;
+    j = (q / L.nx) % L.ny;
+    k = q / (L.nx * L.ny);
+  }
+}
+
+// one colour of a red-black sweep on a shared-memory level: the threads walk
+// the cells of the colour only (one per x pair of each row)
 template <typename T>
 __device__ void sub_colour(const SubLevel<T>& L, T* sol, const T* src, int color, bool zero) {
-  const int n = L.nx * L.ny * L.nz;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int i = q % L.nx, j = (q / L.nx) % L.ny, k = q / (L.nx * L.ny);
-    if (((i + j + k) & 1) != color) continue;
+  const int hx = (L.nx + 1) >> 1;
+  const int npair = hx * L.ny * L.nz;
+  const bool shifts = L.lx >= 1;  // nx a power of two >= 2: hx = nx/2 = 2^(lx-1)
+  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+    int m, j, k;
+    if (shifts) {
+      m = t & (hx - 1);
+      const int row = t >> (L.lx - 1);
+      j = row & (L.ny - 1);
+      k = row >> L.ly;
+    } else {
+      m = t % hx;
+      const int row = t / hx;
+      j = row % L.ny;
+      k = row / L.ny;
+    }
+    const int i = 2 * m + ((j + k + color) & 1);
+    if (i >= L.nx) continue;
+    const int q = (k * L.ny + j) * L.nx + i;
     T s, d;
     if (zero) {
       T dd;
@@ -67,7 +97,8 @@ __device__ void sub_restrict(const SubLevel<T>& F, const T* fsol, const T* fsrc,
                              const SubLevel<T>& C, T* csrc) {
   const int n = C.nx * C.ny * C.nz;
   for (int cq = threadIdx.x; cq < n; cq += blockDim.x) {
-    const int I = cq % C.nx, J = (cq / C.nx) % C.ny, K = cq / (C.nx * C.ny);
+    int I, J, K;
+    sub_ijk(C, cq, I, J, K);
     T acc = T(0);
     for (int dz = 0; dz < F.fz; ++dz)
       for (int dy = 0; dy < F.fy; ++dy)
@@ -89,8 +120,9 @@ __device__ void sub_prolong(const SubLevel<T>& F, T* fsol, const SubLevel<T>& C,
   const int n = F.nx * F.ny * F.nz;
   const int csy = C.nx, csz = C.nx * C.ny;
   for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int i = q % F.nx, j = (q / F.nx) % F.ny, k = q / (F.nx * F.ny);
-    const int I = i / F.fx, J = j / F.fy, K = k / F.fz;
+    int i, j, k;
+    sub_ijk(F, q, i, j, k);
+    const int I = i >> (F.fx - 1), J = j >> (F.fy - 1), K = k >> (F.fz - 1);
     const int cq = K * csz + J * csy + I;
     const T ec = e[cq];
     T val = ec;
