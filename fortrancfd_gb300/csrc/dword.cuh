@@ -120,22 +120,30 @@ __device__ __forceinline__ double dw_to_double_int(dw a) {
 // into one float.  Absolute error O(u^2 sum |c_f (p_nb - p_c)|), the bound the
 // residual needs; about 19 FP32 operations per term instead of ~30 with the
 // normalised double-word operations.
+// One flux term t = c (nb - pc), unnormalised (th + tl).  Every operation is
+// sign-symmetric, so flux_term(c, pc, nb) is exactly -flux_term(c, nb, pc):
+// a face's term can be computed once and used, negated, by its other cell.
+__device__ __forceinline__ dw flux_term(dw c, dw nb, dw pc) {
+  // d = nb - pc: TwoSum of the high parts plus the low parts, unnormalised
+  const dw s = two_sum(nb.hi, -pc.hi);
+  const float dlo = s.lo + (nb.lo - pc.lo);
+  // t = c * d: TwoProd of the high parts plus the cross terms
+  const float th = c.hi * s.hi;
+  float tl = fmaf(c.hi, s.hi, -th);
+  tl = fmaf(c.hi, dlo, tl);
+  tl = fmaf(c.lo, s.hi, tl);
+  return dw{th, tl};
+}
+
 struct flux_acc {
   float hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add_term(dw c, dw nb, dw pc) {
-    // d = nb - pc: TwoSum of the high parts plus the low parts, unnormalised
-    const dw s = two_sum(nb.hi, -pc.hi);
-    const float dlo = s.lo + (nb.lo - pc.lo);
-    // t = c * d: TwoProd of the high parts plus the cross terms
-    const float th = c.hi * s.hi;
-    float tl = fmaf(c.hi, s.hi, -th);
-    tl = fmaf(c.hi, dlo, tl);
-    tl = fmaf(c.lo, s.hi, tl);
-    // acc += t
-    const dw a = two_sum(hi, th);
+  // acc += t
+  __device__ __forceinline__ void add(dw t) {
+    const dw a = two_sum(hi, t.hi);
     hi = a.hi;
-    lo += a.lo + tl;
+    lo += a.lo + t.lo;
   }
+  __device__ __forceinline__ void add_term(dw c, dw nb, dw pc) { add(flux_term(c, nb, pc)); }
   __device__ __forceinline__ dw value() const { return fast_two_sum(hi, lo); }
 };
 

@@ -183,12 +183,10 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
     for (int k = plo; k <= pre_end; ++k) issue(k);
   int issued = pre_end, waited = plo - 1;
   float s2 = 0.f;
+  dw fz_carry{0.f, 0.f};  // z flux between planes k-1 and k, computed at plane k-1
   for (int k = z0; k < z1; ++k) {
-    if (k + 2 <= phi && k + 2 > issued) {
-      if (tid == 0) issue(k + 2);
-      issued = k + 2;
-    }
     const int need = min(k + 1, phi);
+    bool synced = false;
     while (waited < need) {
       ++waited;
       const int s = waited % kQSlots;
@@ -213,37 +211,67 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
         }
       }
       __syncthreads();
+      synced = true;
     }
-    const int x = x0 + tx, y = y0 + ty;
-    if (x < nx && y < ny) {
+    // Plane k+2 goes to the slot plane k-2 used: every thread has passed the
+    // barrier after its compute of plane k-1, the last reader of that slot.
+    if (k + 2 <= phi && k + 2 > issued) {
+      if (!synced) __syncthreads();
+      if (tid == 0) issue(k + 2);
+      issued = k + 2;
+    }
+    // Face terms: x- from this thread, x+ from the next lane's x- (lane 31
+    // computes its own), y both, z- carried from the previous plane's z+
+    // (computed here at the first plane of the chunk), z+ here.  Each face
+    // term is bit-identical to the one its cell would compute (flux_term is
+    // sign-symmetric), added in the order x-, x+, y-, y+, z-, z+.  Every lane
+    // of the warp computes (tile cells outside the grid read zero-filled box
+    // entries), so the shuffles see the whole warp.
+    {
+      const int x = x0 + tx, y = y0 + ty;
       const int s0 = k % kQSlots, sm = (k + kQSlots - 1) % kQSlots, sp = (k + 1) % kQSlots;
       const int t = (ty + 1) * kQBX + (tx + 2);
       const float2* P = qtile(base, s0, 0);
       const float2* CX = qtile(base, s0, 2);
       const float2* CY = qtile(base, s0, 3);
-      const dw pc{P[t].x, P[t].y};
-      flux_acc acc;
-#define DWQ_TERM(cv, nbv)                                              \
-      {                                                                \
-        const float2 c2 = cv, n2 = nbv;                                \
-        acc.add_term(dw{c2.x, c2.y}, dw{n2.x, n2.y}, pc);              \
+      const float2 pc2 = P[t];
+      const dw pc{pc2.x, pc2.y};
+      const auto ld = [](const float2* a, int i) { const float2 v = a[i]; return dw{v.x, v.y}; };
+      const dw fxm = flux_term(ld(CX, t), ld(P, t - 1), pc);  // c (p_{x-1} - p_c)
+      dw fxp;
+      {
+        // the next lane's x- term is c (p_c - p_{x+1}) from its side: negate
+        const float hi = __shfl_down_sync(0xffffffffu, fxm.hi, 1);
+        const float lo = __shfl_down_sync(0xffffffffu, fxm.lo, 1);
+        fxp = dw{-hi, -lo};
+        if (tx == kDTX - 1) fxp = flux_term(ld(CX, t + 1), ld(P, t + 1), pc);
       }
-      DWQ_TERM(CX[t], P[t - 1])
-      DWQ_TERM(CX[t + 1], P[t + 1])
-      DWQ_TERM(CY[t], P[t - kQBX])
-      DWQ_TERM(CY[t + kQBX], P[t + kQBX])
-      if (k > 0) DWQ_TERM(qtile(base, s0, 4)[t], qtile(base, sm, 0)[t])
-      if (k < nz - 1) DWQ_TERM(qtile(base, sp, 4)[t], qtile(base, sp, 0)[t])
-#undef DWQ_TERM
-      const float2 b2 = qtile(base, s0, 1)[t];
-      const dw r = dw_sub(dw{b2.x, b2.y}, acc.value());
-      const size_t q = ((size_t)k * ny + y) * nx + x;
-      const float rf = dw_to_float(r);
-      r32[fine_index(q, x, y, k, hstride)] = rf;
-      pout[q] = P[t];
-      s2 = fmaf(rf, rf, s2);
+      const dw fym = flux_term(ld(CY, t), ld(P, t - kQBX), pc);
+      const dw fyp = flux_term(ld(CY, t + kQBX), ld(P, t + kQBX), pc);
+      dw fzm{0.f, 0.f}, fzp{0.f, 0.f};
+      if (k > 0) {
+        if (k == z0) fzm = flux_term(ld(qtile(base, s0, 4), t), ld(qtile(base, sm, 0), t), pc);
+        else fzm = dw{-fz_carry.hi, -fz_carry.lo};
+      }
+      if (k < nz - 1) fzp = flux_term(ld(qtile(base, sp, 4), t), ld(qtile(base, sp, 0), t), pc);
+      fz_carry = fzp;
+      if (x < nx && y < ny) {
+        flux_acc acc;
+        acc.add(fxm);
+        acc.add(fxp);
+        acc.add(fym);
+        acc.add(fyp);
+        if (k > 0) acc.add(fzm);
+        if (k < nz - 1) acc.add(fzp);
+        const float2 b2 = qtile(base, s0, 1)[t];
+        const dw r = dw_sub(dw{b2.x, b2.y}, acc.value());
+        const size_t q = ((size_t)k * ny + y) * nx + x;
+        const float rf = dw_to_float(r);
+        r32[fine_index(q, x, y, k, hstride)] = rf;
+        pout[q] = pc2;
+        s2 = fmaf(rf, rf, s2);
+      }
     }
-    __syncthreads();
   }
   double v[1] = {(double)s2};
   grid_sum_finish<1>(v, R, slot);
