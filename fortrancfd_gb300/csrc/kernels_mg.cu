@@ -163,23 +163,23 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
   double* W = smem + (size_t)n * n;   // n x n, becomes L^{-1} (lower triangle)
   __shared__ double dsum_sh;
   const int t = threadIdx.x, nt = blockDim.x;
-  for (int e = t; e < n * n; e += nt) adense[e] = 0.0;
+  for (int e = t; e < n * n; e += nt) M[e] = 0.0;
   __syncthreads();
   if (t == 0) {
-    // assemble A in the oracle's order (serial, n <= 64)
+    // assemble A in shared memory in the oracle's order (serial, n <= 64)
     double dsum = 0.0;
     for (int k = 0; k < C.nz; ++k)
       for (int j = 0; j < C.ny; ++j)
         for (int i = 0; i < C.nx; ++i) {
           const int q = (k * C.ny + j) * C.nx + i;
           double d = 0.0, c;
-          if (i > 0) { c = C.cx[q]; adense[q * n + q - 1] += c; d += c; }
-          if (i < C.nx - 1) { c = C.cx[q + 1]; adense[q * n + q + 1] += c; d += c; }
-          if (j > 0) { c = C.cy[q]; adense[q * n + q - C.nx] += c; d += c; }
-          if (j < C.ny - 1) { c = C.cy[q + C.nx]; adense[q * n + q + C.nx] += c; d += c; }
-          if (k > 0) { c = C.cz[q]; adense[q * n + q - C.nx * C.ny] += c; d += c; }
-          if (k < C.nz - 1) { c = C.cz[q + C.nx * C.ny]; adense[q * n + q + C.nx * C.ny] += c; d += c; }
-          adense[q * n + q] -= d;
+          if (i > 0) { c = C.cx[q]; M[q * n + q - 1] += c; d += c; }
+          if (i < C.nx - 1) { c = C.cx[q + 1]; M[q * n + q + 1] += c; d += c; }
+          if (j > 0) { c = C.cy[q]; M[q * n + q - C.nx] += c; d += c; }
+          if (j < C.ny - 1) { c = C.cy[q + C.nx]; M[q * n + q + C.nx] += c; d += c; }
+          if (k > 0) { c = C.cz[q]; M[q * n + q - C.nx * C.ny] += c; d += c; }
+          if (k < C.nz - 1) { c = C.cz[q + C.nx * C.ny]; M[q * n + q + C.nx * C.ny] += c; d += c; }
+          M[q * n + q] -= d;
           dsum += d;
         }
     double s = n > 0 ? dsum / n : 1.0;
@@ -189,7 +189,10 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
   __syncthreads();
   const double sn = dsum_sh / n;
   for (int e = t; e < n * n; e += nt) {
-    M[e] = sn - adense[e];
+    const double a = M[e];
+    adense[e] = a;
+    if (adense32) adense32[e] = (float)a;
+    M[e] = sn - a;
     W[e] = 0.0;
   }
   __syncthreads();
@@ -230,7 +233,6 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
     for (int k = max(r, q); k < n; ++k) acc += W[k * n + r] * W[k * n + q];
     minv[e] = -acc;
     if (minv32) minv32[e] = (float)(-acc);
-    if (adense32) adense32[e] = (float)adense[e];
   }
 }
 

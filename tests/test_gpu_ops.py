@@ -1,7 +1,7 @@
 """torch.ops.gbmg.solve: registration (CPU) and, on the GPU, the solve against
 the FP64 oracle (1e-8 relative at tol 1e-12), its gradients against the
 autograd Function on the same kernels (1e-8), and its rho gradient against
-central differences (1e-6 relative; forward 1e-13, adjoint 1e-10)."""
+central differences (2e-6 relative; forward 1e-13, adjoint 1e-10)."""
 import numpy as np
 import pytest
 import torch
@@ -73,4 +73,5 @@ def test_rho_gradient_matches_central_differences(cuda):
         jp = 0.5 * (torch.ops.gbmg.solve(rho0 + h * v, b0, *args) ** 2).sum()
         jm = 0.5 * (torch.ops.gbmg.solve(rho0 - h * v, b0, *args) ** 2).sum()
     fd = float((jp - jm) / (2 * h))
-    assert abs(fd - float((rho.grad * v).sum())) <= 1e-6 * abs(fd)
+    # as the autograd Function's rho test: 2e-6 (the adjoint's FP64 floor)
+    assert abs(fd - float((rho.grad * v).sum())) <= 2e-6 * abs(fd)
