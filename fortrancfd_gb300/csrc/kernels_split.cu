@@ -18,6 +18,7 @@
 // sweep.  The kernels here do the arithmetic of the natural-layout kernels
 // (k_smooth, k_restrict, k_prolong with the density form) in the same order,
 // so both layouts give bit-identical results.
+#include <cstdlib>
 #include <type_traits>
 
 #include "gbmg_internal.h"
@@ -211,12 +212,32 @@ __global__ void __launch_bounds__(256) k_restrict_split(LevelView<float> F, Leve
   if (zero_sol) C.sol[cq] = 0.f;
 }
 
-// k_restrict_split for four coarse cells per thread (I0..I0+3, C.nx % 4 == 0):
-// float4 loads of each child row, the same per-cell arithmetic and order.
-__global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, LevelView<float> C,
+// k_restrict_split for W coarse cells per thread (I0..I0+W-1, C.nx % W == 0):
+// float4 (W = 4) or float2 (W = 2) loads of each child row, the same per-cell
+// arithmetic and order.  W = 2 keeps half the loads live (fewer registers,
+// more resident warps).
+template <int W>
+__device__ __forceinline__ void ldw(const float* p, float (&a)[W]) {
+  if constexpr (W == 4) {
+    unpack(ld4(p), a);
+  } else {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    a[0] = v.x;
+    a[1] = v.y;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void stw(float* p, const float (&a)[W]) {
+  if constexpr (W == 4) st4(p, make_float4(a[0], a[1], a[2], a[3]));
+  else *reinterpret_cast<float2*>(p) = make_float2(a[0], a[1]);
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) k_restrict_splitv(LevelView<float> F, LevelView<float> C,
                                                          int zero_sol) {
   pdl_enter();
-  const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int I0 = W * (blockIdx.x * blockDim.x + threadIdx.x);
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int K = F.zrev ? C.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
   if (I0 >= C.nx || J >= C.ny) return;
@@ -224,7 +245,7 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
   const size_t half = F.hstride;
   const size_t sy = (size_t)hx, sz = (size_t)hx * F.ny;
   const float inf = __int_as_float(0x7f800000);  // wall neighbour: coefficient exactly 0
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  float acc[W] = {};
   for (int dz = 0; dz < F.fz; ++dz)
     for (int dy = 0; dy < F.fy; ++dy) {
       const int j = F.fy * J + dy, k = F.fz * K + dz;
@@ -234,43 +255,43 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
       const float* Pb = F.sol + (size_t)(1 - ca) * half + h;
       const float* Ra = F.rho + (size_t)ca * half + h;
       const float* Rb = F.rho + (size_t)(1 - ca) * half + h;
-      float pa[4], pb[4], ra[4], rb[4], ba[4], bb[4];
-      unpack(ld4(Pa), pa);
-      unpack(ld4(Pb), pb);
-      unpack(ld4(Ra), ra);
-      unpack(ld4(Rb), rb);
-      unpack(ld4(F.src + (size_t)ca * half + h), ba);
-      unpack(ld4(F.src + (size_t)(1 - ca) * half + h), bb);
+      float pa[W], pb[W], ra[W], rb[W], ba[W], bb[W];
+      ldw<W>(Pa, pa);
+      ldw<W>(Pb, pb);
+      ldw<W>(Ra, ra);
+      ldw<W>(Rb, rb);
+      ldw<W>(F.src + (size_t)ca * half + h, ba);
+      ldw<W>(F.src + (size_t)(1 - ca) * half + h, bb);
       // x-: cell 2I-1 (b's colour, index I-1); x+ of b: cell 2I+2 (a's colour, I+1)
       float pl_e = 0.f, rl_e = inf, pr_e = 0.f, rr_e = inf;
       if (I0 > 0) { pl_e = Pb[-1]; rl_e = Rb[-1]; }
-      if (2 * (I0 + 3) + 2 < F.nx) { pr_e = Pa[4]; rr_e = Ra[4]; }
-      float pym_a[4] = {}, pym_b[4] = {}, pyp_a[4] = {}, pyp_b[4] = {};
-      float pzm_a[4] = {}, pzm_b[4] = {}, pzp_a[4] = {}, pzp_b[4] = {};
-      float rym_a[4] = {inf, inf, inf, inf}, rym_b[4] = {inf, inf, inf, inf};
-      float ryp_a[4] = {inf, inf, inf, inf}, ryp_b[4] = {inf, inf, inf, inf};
-      float rzm_a[4] = {inf, inf, inf, inf}, rzm_b[4] = {inf, inf, inf, inf};
-      float rzp_a[4] = {inf, inf, inf, inf}, rzp_b[4] = {inf, inf, inf, inf};
+      if (2 * (I0 + W - 1) + 2 < F.nx) { pr_e = Pa[W]; rr_e = Ra[W]; }
+      float pym_a[W] = {}, pym_b[W] = {}, pyp_a[W] = {}, pyp_b[W] = {};
+      float pzm_a[W] = {}, pzm_b[W] = {}, pzp_a[W] = {}, pzp_b[W] = {};
+      float rym_a[W], rym_b[W], ryp_a[W], ryp_b[W], rzm_a[W], rzm_b[W], rzp_a[W], rzp_b[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c)
+        rym_a[c] = rym_b[c] = ryp_a[c] = ryp_b[c] = rzm_a[c] = rzm_b[c] = rzp_a[c] = rzp_b[c] = inf;
       if (j > 0) {
-        unpack(ld4(Pb - sy), pym_a); unpack(ld4(Pa - sy), pym_b);
-        unpack(ld4(Rb - sy), rym_a); unpack(ld4(Ra - sy), rym_b);
+        ldw<W>(Pb - sy, pym_a); ldw<W>(Pa - sy, pym_b);
+        ldw<W>(Rb - sy, rym_a); ldw<W>(Ra - sy, rym_b);
       }
       if (j < F.ny - 1) {
-        unpack(ld4(Pb + sy), pyp_a); unpack(ld4(Pa + sy), pyp_b);
-        unpack(ld4(Rb + sy), ryp_a); unpack(ld4(Ra + sy), ryp_b);
+        ldw<W>(Pb + sy, pyp_a); ldw<W>(Pa + sy, pyp_b);
+        ldw<W>(Rb + sy, ryp_a); ldw<W>(Ra + sy, ryp_b);
       }
       if (k > 0) {
-        unpack(ld4(Pb - sz), pzm_a); unpack(ld4(Pa - sz), pzm_b);
-        unpack(ld4(Rb - sz), rzm_a); unpack(ld4(Ra - sz), rzm_b);
+        ldw<W>(Pb - sz, pzm_a); ldw<W>(Pa - sz, pzm_b);
+        ldw<W>(Rb - sz, rzm_a); ldw<W>(Ra - sz, rzm_b);
       }
       if (k < F.nz - 1) {
-        unpack(ld4(Pb + sz), pzp_a); unpack(ld4(Pa + sz), pzp_b);
-        unpack(ld4(Rb + sz), rzp_a); unpack(ld4(Ra + sz), rzp_b);
+        ldw<W>(Pb + sz, pzp_a); ldw<W>(Pa + sz, pzp_b);
+        ldw<W>(Rb + sz, rzp_a); ldw<W>(Ra + sz, rzp_b);
       }
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
+      for (int c = 0; c < W; ++c) {
         const float pl = c == 0 ? pl_e : pb[c - 1], rl = c == 0 ? rl_e : rb[c - 1];
-        const float pr = c == 3 ? pr_e : pa[c + 1], rr = c == 3 ? rr_e : ra[c + 1];
+        const float pr = c == W - 1 ? pr_e : pa[c + 1], rr = c == W - 1 ? rr_e : ra[c + 1];
         const float cab = face(F.kx, ra[c], rb[c]);
         {
           float s = 0.f, d = 0.f, cc;
@@ -296,8 +317,14 @@ __global__ void __launch_bounds__(256) k_restrict_split4(LevelView<float> F, Lev
     }
   const size_t cq = ((size_t)K * C.ny + J) * C.nx + I0;
   const float sc = 1.f / (float)(F.fx * F.fy * F.fz);
-  st4(C.src + cq, make_float4(acc[0] * sc, acc[1] * sc, acc[2] * sc, acc[3] * sc));
-  if (zero_sol) st4(C.sol + cq, make_float4(0.f, 0.f, 0.f, 0.f));
+  float out[W], zero[W];
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    out[c] = acc[c] * sc;
+    zero[c] = 0.f;
+  }
+  stw<W>(C.src + cq, out);
+  if (zero_sol) stw<W>(C.sol + cq, zero);
 }
 
 // k_prolong_split for four coarse cells per thread (C.nx % 4 == 0).
@@ -437,8 +464,15 @@ void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const Leve
                            bool zero_sol) {
   const dim3 blk(32, 8, 1);
   if (vec4_ok(F) && C.nx % 4 == 0) {
-    const dim3 g4(cdiv((size_t)(C.nx / 4), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-    launch_pdl(k_restrict_split4, g4, blk, 0, s, F, C, zero_sol ? 1 : 0);
+    // two coarse cells per thread unless GBMG_RESTRICT_VEC=4
+    static int vec = 0;
+    if (vec == 0) {
+      const char* e = std::getenv("GBMG_RESTRICT_VEC");
+      vec = (e && std::atoi(e) == 4) ? 4 : 2;
+    }
+    const dim3 gv(cdiv((size_t)(C.nx / vec), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+    if (vec == 4) launch_pdl(k_restrict_splitv<4>, gv, blk, 0, s, F, C, zero_sol ? 1 : 0);
+    else launch_pdl(k_restrict_splitv<2>, gv, blk, 0, s, F, C, zero_sol ? 1 : 0);
     return;
   }
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
