@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
   float s2 = 0.f;
   dw fz_carry{0.f, 0.f};  // z flux between planes k-1 and k, computed at plane k-1
   for (int k = z0; k < z1; ++k) {
+    if (k + 2 <= phi && k + 2 > issued) {
+      if (tid == 0) issue(k + 2);
+      issued = k + 2;
+    }
     const int need = min(k + 1, phi);
-    bool synced = false;
     while (waited < need) {
       ++waited;
       const int s = waited % kQSlots;
@@ -211,22 +214,11 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
         }
       }
       __syncthreads();
-      synced = true;
     }
-    // Plane k+2 goes to the slot plane k-2 used: every thread has passed the
-    // barrier after its compute of plane k-1, the last reader of that slot.
-    if (k + 2 <= phi && k + 2 > issued) {
-      if (!synced) __syncthreads();
-      if (tid == 0) issue(k + 2);
-      issued = k + 2;
-    }
-    // Face terms: x- from this thread, x+ from the next lane's x- (lane 31
-    // computes its own), y both, z- carried from the previous plane's z+
-    // (computed here at the first plane of the chunk), z+ here.  Each face
-    // term is bit-identical to the one its cell would compute (flux_term is
-    // sign-symmetric), added in the order x-, x+, y-, y+, z-, z+.  Every lane
-    // of the warp computes (tile cells outside the grid read zero-filled box
-    // entries), so the shuffles see the whole warp.
+    // Face terms in the order x-, x+, y-, y+, z-, z+; the z- term is the
+    // previous plane's z+ term negated (flux_term is sign-symmetric, so this
+    // is bit-identical to computing it), except at the first plane of the
+    // chunk.
     {
       const int x = x0 + tx, y = y0 + ty;
       const int s0 = k % kQSlots, sm = (k + kQSlots - 1) % kQSlots, sp = (k + 1) % kQSlots;
@@ -238,14 +230,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       const dw pc{pc2.x, pc2.y};
       const auto ld = [](const float2* a, int i) { const float2 v = a[i]; return dw{v.x, v.y}; };
       const dw fxm = flux_term(ld(CX, t), ld(P, t - 1), pc);  // c (p_{x-1} - p_c)
-      dw fxp;
-      {
-        // the next lane's x- term is c (p_c - p_{x+1}) from its side: negate
-        const float hi = __shfl_down_sync(0xffffffffu, fxm.hi, 1);
-        const float lo = __shfl_down_sync(0xffffffffu, fxm.lo, 1);
-        fxp = dw{-hi, -lo};
-        if (tx == kDTX - 1) fxp = flux_term(ld(CX, t + 1), ld(P, t + 1), pc);
-      }
+      const dw fxp = flux_term(ld(CX, t + 1), ld(P, t + 1), pc);
       const dw fym = flux_term(ld(CY, t), ld(P, t - kQBX), pc);
       const dw fyp = flux_term(ld(CY, t + kQBX), ld(P, t + kQBX), pc);
       dw fzm{0.f, 0.f}, fzp{0.f, 0.f};
@@ -272,6 +257,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
         s2 = fmaf(rf, rf, s2);
       }
     }
+    __syncthreads();
   }
   double v[1] = {(double)s2};
   grid_sum_finish<1>(v, R, slot);
