@@ -368,3 +368,21 @@ def test_cooperative_mid_cycle_is_bit_identical(cuda, monkeypatch, precision, id
     (p0, s0), (p1, s1) = out["0"], out["1"]
     assert s0["status"] == 0 and s0["cycles"] == s1["cycles"]
     np.testing.assert_array_equal(p1, p0)
+
+
+@pytest.mark.parametrize("shape", [(6, 10, 8), (12, 20, 16), (1, 12, 20), (4, 6, 10),
+                                   (8, 8, 24)])
+def test_mixed_small_and_ragged_grids(cuda, shape):
+    """Mixed precision on small grids that take the other code paths: nx % 8
+    != 0 (scalar colour-split kernels, defect without TMA), 2D, two-level
+    hierarchies."""
+    case = inputs.custom(shape, centers=((0.5, 0.4, 0.5),), radii=(0.3,), seed=3)
+    c = cases.Built(case)
+    p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-10)
+    with solver(c, precision="mixed") as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == st_or["status"] == 0
+    assert st["rel_residual"] < 1e-10
+    assert st["cycles"] <= st_or["cycles"] + 2
+    assert rel_l2(p, p_or) <= 1e-8
