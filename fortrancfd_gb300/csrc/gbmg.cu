@@ -75,7 +75,7 @@ struct gbmg_handle {
   double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
   // coarsest level
   int nc = 0;
-  double *minv = nullptr, *adense = nullptr;
+  double *minv = nullptr, *adense = nullptr, *cwork = nullptr;
   float *minv32 = nullptr, *adense32 = nullptr;
   // reductions
   ReduceScratch red{};
@@ -453,7 +453,7 @@ int free_all(gbmg_handle* h) {
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->aux[0]); dfree(h->aux[1]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
-  dfree(h->minv); dfree(h->adense); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
+  dfree(h->minv); dfree(h->adense); dfree(h->cwork); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   dfree(h->bar);
   delete[] h->dmaps;
   h->dmaps = nullptr;
@@ -624,6 +624,7 @@ int allocate(gbmg_handle* h) {
   }
   GB_TRY(dmalloc(h, &h->minv, (size_t)nc * nc));
   GB_TRY(dmalloc(h, &h->adense, (size_t)nc * nc));
+  GB_TRY(dmalloc(h, &h->cwork, (size_t)2 * nc * nc + nc));
   GB_TRY(dmalloc(h, &h->minv32, (size_t)nc * nc));
   GB_TRY(dmalloc(h, &h->adense32, (size_t)nc * nc));
   const size_t rows = (size_t)h->lv[0].ny * h->lv[0].nz;
@@ -712,7 +713,7 @@ int build_hierarchy(gbmg_handle* h) {
     }
   }
   LAUNCH(h, GBMG_PROF_SETUP,
-         launch_coarse_invert(s, v64(h->lv[h->L - 1]), h->minv, h->adense, h->minv32, h->adense32));
+         launch_coarse_invert(s, v64(h->lv[h->L - 1]), h->minv, h->adense, h->minv32, h->adense32, h->cwork));
   if (h->mixed && !h->fine_copies) {
     const Level& f = h->lv[0];
     LAUNCH(h, GBMG_PROF_SETUP, launch_to_dw(s, f.cx, h->cxw, f.n));

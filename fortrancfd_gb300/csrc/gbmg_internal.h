@@ -149,8 +149,9 @@ void launch_residual_norm(cudaStream_t s, const LevelView<double>& L, TO* r,
                           const ReduceScratch& R, int slot);
 template <typename T>
 void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, const T* b, T* x);
+// work: 2 n^2 + n doubles of scratch (n = cells of the coarsest level)
 void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
-                          double* adense, float* minv32, float* adense32);
+                          double* adense, float* minv32, float* adense32, double* work);
 void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,
                     double* cz, int cnx, int cny, int cnz);
 void launch_idiag(cudaStream_t s, const LevelView<double>& L, double* idiag);

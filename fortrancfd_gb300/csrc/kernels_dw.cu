@@ -264,20 +264,18 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
 }
 
 __global__ void k_to_dw(const double* __restrict__ a, float2* __restrict__ out, size_t n) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x) {
-    const dw v = dw_from_double_int(a[q]);
+  stride4(n, [&](size_t q) { return a[q]; }, [&](size_t q, double x) {
+    const dw v = dw_from_double_int(x);
     out[q] = make_float2(v.hi, v.lo);
-  }
+  });
 }
 
 // slot <- sum of the double values of p (for the final mean projection)
 __global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict__ p, size_t n,
                                                         ReduceScratch R, int slot) {
   double acc[1] = {0.0};
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    acc[0] += dw_to_double_int(dw_ldg(p + q));
+  stride4(n, [&](size_t q) { return dw_ldg(p + q); },
+          [&](size_t, dw v) { acc[0] += dw_to_double_int(v); });
   grid_sum_finish<1>(acc, R, slot);
 }
 
@@ -285,9 +283,8 @@ __global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict
 __global__ void k_dw_out(const float2* __restrict__ p, double* __restrict__ out, size_t n,
                          ReduceScratch R, int slot) {
   const double m = R.result[slot] / (double)n;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    out[q] = dw_to_double_int(dw_ldg(p + q)) - m;
+  stride4(n, [&](size_t q) { return dw_ldg(p + q); },
+          [&](size_t q, dw v) { out[q] = dw_to_double_int(v) - m; });
 }
 
 inline unsigned stride_blocks(size_t n) {

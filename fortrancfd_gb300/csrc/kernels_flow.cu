@@ -280,12 +280,10 @@ __global__ void __launch_bounds__(kRedThreads) k_div_stats(int nx, int ny, int n
 __global__ void __launch_bounds__(kRedThreads) k_sum(const double* __restrict__ x, size_t n,
                                                      ReduceScratch R, int slot) {
   double acc[2] = {0.0, 0.0};
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x) {
-    const double a = x[q];
+  stride4(n, [&](size_t q) { return x[q]; }, [&](size_t, double a) {
     acc[0] += a;
     acc[1] += a * a;
-  }
+  });
   grid_sum_finish<2>(acc, R, slot);
 }
 
@@ -295,31 +293,25 @@ __global__ void __launch_bounds__(kRedThreads) k_shift_by_mean(const double* __r
                                                                int slot2) {
   const double m = R.result[slot] / (double)n;
   double acc[1] = {0.0};
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x) {
-    const double a = x[q] - m;
+  stride4(n, [&](size_t q) { return x[q]; }, [&](size_t q, double xq) {
+    const double a = xq - m;
     y[q] = a;
     acc[0] += a * a;
-  }
+  });
   if (slot2 >= 0) grid_sum_finish<1>(acc, R, slot2);
 }
 
 __global__ void k_add_float(double* p, const float* __restrict__ e, size_t n) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    p[q] += (double)e[q];
+  stride4(n, [&](size_t q) { return make_double2(p[q], (double)e[q]); },
+          [&](size_t q, double2 v) { p[q] = v.x + v.y; });
 }
 
 __global__ void k_f2d(const float* __restrict__ a, double* b, size_t n) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    b[q] = (double)a[q];
+  stride4(n, [&](size_t q) { return a[q]; }, [&](size_t q, float v) { b[q] = (double)v; });
 }
 
 __global__ void k_d2f(const double* __restrict__ a, float* b, size_t n) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    b[q] = (float)a[q];
+  stride4(n, [&](size_t q) { return a[q]; }, [&](size_t q, double v) { b[q] = (float)v; });
 }
 
 // slot <- a.b, slot+1 <- a.c (c may be null)
@@ -328,11 +320,11 @@ __global__ void __launch_bounds__(kRedThreads) k_dot2(const double* __restrict__
                                                       const double* __restrict__ c, size_t n,
                                                       ReduceScratch R, int slot) {
   double acc[2] = {0.0, 0.0};
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x) {
-    acc[0] += a[q] * b[q];
-    if (c) acc[1] += a[q] * c[q];
-  }
+  stride4(n, [&](size_t q) { return make_double3(a[q], b[q], c ? c[q] : 0.0); },
+          [&](size_t, double3 v) {
+            acc[0] += v.x * v.y;
+            if (c) acc[1] += v.x * v.z;
+          });
   grid_sum_finish<2>(acc, R, slot);
 }
 
@@ -342,11 +334,11 @@ __global__ void k_pcg_direction(double* d, double* zold, const double* __restric
                                 ReduceScratch R, int first) {
   const double rz = R.result[kSlotDot], rzo = R.result[kSlotDot + 1];
   const double beta = first ? 0.0 : (rz - rzo) / R.result[kSlotDot2 + 1];
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x) {
-    d[q] = first ? z[q] : z[q] + beta * d[q];
-    zold[q] = z[q];
-  }
+  stride4(n, [&](size_t q) { return make_double2(z[q], first ? 0.0 : d[q]); },
+          [&](size_t q, double2 v) {
+            d[q] = first ? v.x : v.x + beta * v.y;
+            zold[q] = v.x;
+          });
 }
 
 __global__ void k_pcg_keep_rz(ReduceScratch R) { R.result[kSlotDot2 + 1] = R.result[kSlotDot]; }
@@ -354,9 +346,8 @@ __global__ void k_pcg_keep_rz(ReduceScratch R) { R.result[kSlotDot2 + 1] = R.res
 // x += alpha d with alpha = (r.z)/(d.q)
 __global__ void k_pcg_step(double* x, const double* __restrict__ d, size_t n, ReduceScratch R) {
   const double alpha = R.result[kSlotDot] / R.result[kSlotDot2];
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    x[q] += alpha * d[q];
+  stride4(n, [&](size_t q) { return make_double2(x[q], d[q]); },
+          [&](size_t q, double2 v) { x[q] = v.x + alpha * v.y; });
 }
 
 }  // namespace

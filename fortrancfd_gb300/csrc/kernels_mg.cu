@@ -146,42 +146,50 @@ __global__ void __launch_bounds__(kMaxCoarse) k_coarse_solve(int n, const T* __r
   if (t < n) x[t] = sx[t] - red[0];
 }
 
-// Coarsest-level operator and its inverse, one block, FP64.  The dense
-// Neumann matrix A is singular (constant null space) and negative
-// semi-definite; M = s 11^T/n - A (s = mean diagonal) is symmetric positive
-// definite, and -M^{-1} b is the mean-free solution of A x = b for a
-// mean-free b.  M = L L^T by Cholesky in shared memory, W = L^{-1} column by
-// column, M^{-1} = W^T W: about n^3/2 multiply-adds instead of Gauss-Jordan's
-// 2n^3.  The reference LU-factors the singular matrix with LAPACK dgesv
-// instead ("DomainDecomposition/3D/lib/data/tree_multigrid.f90:134-173").
-__global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, double* minv,
-                                                       double* adense, float* minv32,
-                                                       float* adense32) {
+// Coarsest-level operator and its inverse, FP64.  The dense Neumann matrix A
+// is singular (constant null space) and negative semi-definite;
+// M = s 11^T/n - A (s = mean diagonal) is symmetric positive definite, and
+// -M^{-1} b is the mean-free solution of A x = b for a mean-free b.
+// M = L L^T by Cholesky in shared memory (one block), W = L^{-1} one column
+// per block, M^{-1} = W^T W one row per block: about n^3/2 multiply-adds
+// instead of Gauss-Jordan's 2n^3, and the two triangular products, which are
+// FP64-pipe bound on one SM, spread over n SMs.  The reference LU-factors the
+// singular matrix with LAPACK dgesv instead
+// ("DomainDecomposition/3D/lib/data/tree_multigrid.f90:134-173").
+//
+// work holds L (n x n, lower triangle), 1/L_jj (n) and W (n x n).
+__global__ void __launch_bounds__(256) k_coarse_factor(LevelView<double> C, double* adense,
+                                                       float* adense32, double* work) {
   extern __shared__ double smem[];
   const int n = C.nx * C.ny * C.nz;
-  double* M = smem;                   // n x n, becomes L (lower triangle)
-  double* W = smem + (size_t)n * n;   // n x n, becomes L^{-1} (lower triangle)
+  double* M = smem;  // n x n, becomes L (lower triangle)
   __shared__ double dsum_sh;
+  __shared__ double drow[kMaxCoarse];
   const int t = threadIdx.x, nt = blockDim.x;
   for (int e = t; e < n * n; e += nt) M[e] = 0.0;
   __syncthreads();
+  // assemble A, one row per thread; the diagonal sums its faces in the order
+  // x-, x+, y-, y+, z-, z+ and the mean diagonal sums the rows in order
+  if (t < n) {
+    const int q = t, sy = C.nx, sz = C.nx * C.ny;
+    const int i = q % C.nx, j = (q / C.nx) % C.ny, k = q / sz;
+    const double cxl = i > 0 ? C.cx[q] : 0.0, cxr = i < C.nx - 1 ? C.cx[q + 1] : 0.0;
+    const double cyl = j > 0 ? C.cy[q] : 0.0, cyr = j < C.ny - 1 ? C.cy[q + sy] : 0.0;
+    const double czl = k > 0 ? C.cz[q] : 0.0, czr = k < C.nz - 1 ? C.cz[q + sz] : 0.0;
+    double d = 0.0;
+    if (i > 0) { M[q * n + q - 1] = cxl; d += cxl; }
+    if (i < C.nx - 1) { M[q * n + q + 1] = cxr; d += cxr; }
+    if (j > 0) { M[q * n + q - sy] = cyl; d += cyl; }
+    if (j < C.ny - 1) { M[q * n + q + sy] = cyr; d += cyr; }
+    if (k > 0) { M[q * n + q - sz] = czl; d += czl; }
+    if (k < C.nz - 1) { M[q * n + q + sz] = czr; d += czr; }
+    M[q * n + q] = -d;
+    drow[q] = d;
+  }
+  __syncthreads();
   if (t == 0) {
-    // assemble A in shared memory in the oracle's order (serial, n <= 64)
     double dsum = 0.0;
-    for (int k = 0; k < C.nz; ++k)
-      for (int j = 0; j < C.ny; ++j)
-        for (int i = 0; i < C.nx; ++i) {
-          const int q = (k * C.ny + j) * C.nx + i;
-          double d = 0.0, c;
-          if (i > 0) { c = C.cx[q]; M[q * n + q - 1] += c; d += c; }
-          if (i < C.nx - 1) { c = C.cx[q + 1]; M[q * n + q + 1] += c; d += c; }
-          if (j > 0) { c = C.cy[q]; M[q * n + q - C.nx] += c; d += c; }
-          if (j < C.ny - 1) { c = C.cy[q + C.nx]; M[q * n + q + C.nx] += c; d += c; }
-          if (k > 0) { c = C.cz[q]; M[q * n + q - C.nx * C.ny] += c; d += c; }
-          if (k < C.nz - 1) { c = C.cz[q + C.nx * C.ny]; M[q * n + q + C.nx * C.ny] += c; d += c; }
-          M[q * n + q] -= d;
-          dsum += d;
-        }
+    for (int q = 0; q < n; ++q) dsum += drow[q];
     double s = n > 0 ? dsum / n : 1.0;
     if (s <= 0.0) s = 1.0;
     dsum_sh = s;
@@ -193,21 +201,22 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
     adense[e] = a;
     if (adense32) adense32[e] = (float)a;
     M[e] = sn - a;
-    W[e] = 0.0;
   }
   __syncthreads();
   // right-looking Cholesky, lower triangle in place; the trailing update is
   // walked as a 16 x 16 thread grid over (row, column) without divisions
-  __shared__ double rdiag[kMaxCoarse];  // 1/L_jj
+  double* rdiag = work + (size_t)n * n;  // 1/L_jj
+  __shared__ double rd_sh;
   const int tx = t % 16, ty = t / 16;
   for (int j = 0; j < n; ++j) {
     if (t == 0) {
       const double d = sqrt(M[j * n + j]);
       M[j * n + j] = d;
-      rdiag[j] = 1.0 / d;
+      rd_sh = 1.0 / d;
+      rdiag[j] = rd_sh;
     }
     __syncthreads();
-    const double rjj = rdiag[j];
+    const double rjj = rd_sh;
     for (int i = j + 1 + t; i < n; i += nt) M[i * n + j] *= rjj;
     __syncthreads();
     for (int i = j + 1 + ty; i < n; i += 16) {
@@ -216,24 +225,42 @@ __global__ void __launch_bounds__(256) k_coarse_invert(LevelView<double> C, doub
     }
     __syncthreads();
   }
-  // W = L^{-1}: forward substitution, one column per thread
-  for (int c = t; c < n; c += nt) {
-    W[c * n + c] = rdiag[c];
-    for (int i = c + 1; i < n; ++i) {
-      double acc = 0.0;
-      for (int k = c; k < i; ++k) acc += M[i * n + k] * W[k * n + c];
-      W[i * n + c] = -acc * rdiag[i];
-    }
-  }
-  __syncthreads();
-  // (A - s 11^T/n)^{-1} = -M^{-1} = -W^T W
-  for (int e = t; e < n * n; e += nt) {
-    const int r = e / n, q = e % n;
+  for (int e = t; e < n * n; e += nt) work[e] = M[e];
+}
+
+// W = L^{-1}, column c in block c (one warp): row by row forward
+// substitution, the dot product of each row split over the lanes.
+__global__ void __launch_bounds__(32) k_coarse_lower_inv(int n, double* work) {
+  const double* Lm = work;
+  const double* rdiag = work + (size_t)n * n;
+  double* W = work + (size_t)n * n + n;
+  __shared__ double col[kMaxCoarse];
+  const int c = blockIdx.x, lane = threadIdx.x;
+  for (int i = lane; i < n; i += 32) col[i] = 0.0;
+  __syncwarp();
+  if (lane == 0) col[c] = rdiag[c];
+  __syncwarp();
+  for (int i = c + 1; i < n; ++i) {
     double acc = 0.0;
-    for (int k = max(r, q); k < n; ++k) acc += W[k * n + r] * W[k * n + q];
-    minv[e] = -acc;
-    if (minv32) minv32[e] = (float)(-acc);
+    for (int k = c + lane; k < i; k += 32) acc += Lm[(size_t)i * n + k] * col[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) col[i] = -acc * rdiag[i];
+    __syncwarp();
   }
+  for (int i = lane; i < n; i += 32) W[(size_t)i * n + c] = col[i];
+}
+
+// (A - s 11^T/n)^{-1} = -M^{-1} = -W^T W, row r in block r.
+__global__ void __launch_bounds__(kMaxCoarse) k_coarse_gram(int n, const double* __restrict__ work,
+                                                           double* minv, float* minv32) {
+  const double* W = work + (size_t)n * n + n;
+  const int r = blockIdx.x, q = threadIdx.x;
+  if (q >= n) return;
+  double acc = 0.0;
+  for (int k = max(r, q); k < n; ++k) acc += W[(size_t)k * n + r] * W[(size_t)k * n + q];
+  minv[(size_t)r * n + q] = -acc;
+  if (minv32) minv32[(size_t)r * n + q] = (float)(-acc);
 }
 
 // Coarse face coefficients, rediscretised on spacing 2h from the mean of the
@@ -248,6 +275,43 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
   if (I >= cnx || J >= cny) return;
   const size_t cq = ((size_t)K * cny + J) * cnx + I;
   const double tang = 1.0 / (double)(F.fx * F.fy * F.fz);
+  const size_t sy = (size_t)F.nx, sz = (size_t)F.nx * F.ny;
+  const size_t q0 = (size_t)F.fz * K * sz + (size_t)F.fy * J * sy + (size_t)F.fx * I;
+  if (F.fx <= 2 && F.fy <= 2 && F.fz <= 2) {
+    // all (at most 12) loads issued before the sums, which keep the order
+    // dz, dy, dx of the general loop below
+    double t[3][4];
+    bool use[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double* fc = a == 0 ? F.cx : (a == 1 ? F.cy : F.cz);
+      const int idx = a == 0 ? I : (a == 1 ? J : K);
+      const int fa = a == 0 ? F.fx : (a == 1 ? F.fy : F.fz);
+      const bool live = idx > 0 && fa > 1;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        // the two tangential offsets of slot m, in the loop order z, y, x
+        const int hi = m >> 1, lo = m & 1;
+        const int dz = a == 2 ? 0 : hi, dy = a == 1 ? 0 : (a == 0 ? lo : hi), dx = a == 0 ? 0 : lo;
+        use[a][m] = live && dz < F.fz && dy < F.fy && dx < F.fx;
+        t[a][m] = use[a][m] ? fc[q0 + dz * sz + dy * sy + dx] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      double* cc = a == 0 ? cx : (a == 1 ? cy : cz);
+      const int idx = a == 0 ? I : (a == 1 ? J : K);
+      const int fa = a == 0 ? F.fx : (a == 1 ? F.fy : F.fz);
+      if (idx == 0 || fa == 1) { cc[cq] = 0.0; continue; }
+      double acc = 0.0;
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        if (use[a][m]) acc += t[a][m];
+      acc *= tang * fa;
+      cc[cq] = acc / (double)(fa * fa);
+    }
+    return;
+  }
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const double* fc = a == 0 ? F.cx : (a == 1 ? F.cy : F.cz);
@@ -260,8 +324,7 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
       for (int dy = 0; dy < F.fy; ++dy)
         for (int dx = 0; dx < F.fx; ++dx) {
           if ((a == 0 && dx) || (a == 1 && dy) || (a == 2 && dz)) continue;
-          const size_t fq = ((size_t)(F.fz * K + dz) * F.ny + (F.fy * J + dy)) * F.nx + (F.fx * I + dx);
-          acc += fc[fq];
+          acc += fc[q0 + dz * sz + dy * sy + dx];
         }
     acc *= tang * fa;
     cc[cq] = acc / (double)(fa * fa);
@@ -286,9 +349,7 @@ __global__ void __launch_bounds__(256) k_idiag(LevelView<double> L, double* idia
 }
 
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-       q += (size_t)gridDim.x * blockDim.x)
-    b[q] = (float)a[q];
+  stride4(n, [&](size_t q) { return a[q]; }, [&](size_t q, double v) { b[q] = (float)v; });
 }
 
 }  // namespace
@@ -381,11 +442,13 @@ void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, 
 }
 
 void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
-                          double* adense, float* minv32, float* adense32) {
+                          double* adense, float* minv32, float* adense32, double* work) {
   const int n = C.nx * C.ny * C.nz;
-  const size_t shm = (size_t)2 * n * n * sizeof(double);
-  cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  k_coarse_invert<<<1, 256, shm, s>>>(C, minv, adense, minv32, adense32);
+  const size_t shm = (size_t)n * n * sizeof(double);
+  cudaFuncSetAttribute(k_coarse_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  k_coarse_factor<<<1, 256, shm, s>>>(C, adense, adense32, work);
+  k_coarse_lower_inv<<<n, 32, 0, s>>>(n, work);
+  k_coarse_gram<<<n, kMaxCoarse, 0, s>>>(n, work, minv, minv32);
 }
 
 void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,

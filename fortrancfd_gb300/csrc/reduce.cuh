@@ -13,6 +13,27 @@ namespace gbmg {
 
 constexpr int kRedThreads = 256;
 
+// Grid-stride traversal of [0, n) that loads four strided elements (q, q+s,
+// q+2s, q+3s) before using any, so their memory requests are in flight
+// together; use(q, v) runs in the same order as in a one-at-a-time loop, so
+// sums come out bit for bit the same.
+template <typename Load, typename Use>
+__device__ __forceinline__ void stride4(size_t n, Load load, Use use) {
+  const size_t s = (size_t)gridDim.x * blockDim.x;
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; q + 3 * s < n; q += 4 * s) {
+    const auto v0 = load(q);
+    const auto v1 = load(q + s);
+    const auto v2 = load(q + 2 * s);
+    const auto v3 = load(q + 3 * s);
+    use(q, v0);
+    use(q + s, v1);
+    use(q + 2 * s, v2);
+    use(q + 3 * s, v3);
+  }
+  for (; q < n; q += s) use(q, load(q));
+}
+
 // Sum over the block of NV values; the result is valid in thread 0.
 template <int NV>
 __device__ inline void block_sum(double (&v)[NV]) {
