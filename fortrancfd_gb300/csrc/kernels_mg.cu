@@ -274,12 +274,15 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
   const int K = blockIdx.z;
   if (I >= cnx || J >= cny) return;
   const size_t cq = ((size_t)K * cny + J) * cnx + I;
-  const double tang = 1.0 / (double)(F.fx * F.fy * F.fz);
   const size_t sy = (size_t)F.nx, sz = (size_t)F.nx * F.ny;
   const size_t q0 = (size_t)F.fz * K * sz + (size_t)F.fy * J * sy + (size_t)F.fx * I;
   if (F.fx <= 2 && F.fy <= 2 && F.fz <= 2) {
     // all (at most 12) loads issued before the sums, which keep the order
-    // dz, dy, dx of the general loop below
+    // dz, dy, dx of the general loop below.  The factors are powers of two, so
+    // 1/(fx fy fz) and the division by fa^2 are exact products: GB300 runs an
+    // FP64 division as a long sequence on its slow FP64 pipe.
+    const int f3 = F.fx * F.fy * F.fz;
+    const double tang = f3 == 1 ? 1.0 : (f3 == 2 ? 0.5 : (f3 == 4 ? 0.25 : 0.125));
     double t[3][4];
     bool use[3][4];
 #pragma unroll
@@ -308,10 +311,11 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
       for (int m = 0; m < 4; ++m)
         if (use[a][m]) acc += t[a][m];
       acc *= tang * fa;
-      cc[cq] = acc / (double)(fa * fa);
+      cc[cq] = acc * (fa == 2 ? 0.25 : 1.0);
     }
     return;
   }
+  const double tang = 1.0 / (double)(F.fx * F.fy * F.fz);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const double* fc = a == 0 ? F.cx : (a == 1 ? F.cy : F.cz);
