@@ -87,6 +87,9 @@ struct gbmg_handle {
   int pcur = 0;  // which pw holds the current pressure
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
+  bool sub_cluster = false;  // ... on a thread-block cluster (k_cluster_cycle)
+  int cl_ranks = 8;          // blocks of that cluster
+  int cl_single = 4096;      // its levels of at most this many cells run whole in block 0
   int* derr = nullptr;   // device error flags (TMA wait and grid barrier timeouts)
   unsigned* bar = nullptr;  // grid barrier of the mid-cycle kernel: arrivals, generation
   bool mid_ok = false;      // middle levels in one cooperative launch
@@ -378,7 +381,16 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
            launch_restrict<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
   }
-  if (h->sub_lc < L) {
+  if (h->sub_lc < L && h->sub_cluster) {
+    cudaError_t e = cudaSuccess;
+    LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
+           e = launch_cluster_cycle<T>(s, make_cluster_cycle(make_subcycle<T>(h, reverse_post),
+                                                              h->cl_ranks, h->cl_single)));
+    if (e != cudaSuccess) {
+      h->err = std::string("cluster bottom-cycle launch: ") + cudaGetErrorString(e);
+      return GBMG_CUDA_ERROR;
+    }
+  } else if (h->sub_lc < L) {
     LAUNCH(h, GBMG_PROF_COARSE_SOLVE, launch_subcycle<T>(s, make_subcycle<T>(h, reverse_post)));
   } else {
     const LevelView<T> C = view<T>(h->lv[L - 1]);
@@ -474,11 +486,42 @@ int free_all(gbmg_handle* h) {
 // multiple of 16 bytes (GBMG_TMA_LEVELS overrides how many finest levels).
 // The one-block bottom of the cycle: the first level >= 1 with at most
 // kSubMaxCells cells and at least one coarser level below it.
+//
+// The bottom runs on a thread-block cluster instead (GBMG_CLUSTER=1; the
+// opt-in cooperative mid-cycle needs the one-block bottom), from the first
+// level >= 1 with at most kClusterMaxCells cells, when that level has at
+// least as many z planes as the cluster has blocks and the cluster fits:
+// GBMG_CLUSTER_RANKS blocks (default 8, at most 16), levels of at most
+// GBMG_CLUSTER_SINGLE cells (default 4096) whole in block 0.
 template <typename T>
 void setup_subcycle(gbmg_handle* h) {
   h->sub_lc = h->L;
+  h->sub_cluster = false;
   if (const char* e = std::getenv("GBMG_SUBCYCLE"))
     if (std::atoi(e) == 0) return;
+  bool cluster = false;
+  if (const char* e = std::getenv("GBMG_CLUSTER")) cluster = std::atoi(e) != 0;
+  if (const char* e = std::getenv("GBMG_MIDCYCLE")) cluster = cluster && std::atoi(e) == 0;
+  if (const char* e = std::getenv("GBMG_CLUSTER_RANKS"))
+    h->cl_ranks = std::min(kClusterMaxRanks, std::max(1, std::atoi(e)));
+  if (const char* e = std::getenv("GBMG_CLUSTER_SINGLE")) h->cl_single = std::max(0, std::atoi(e));
+  if (cluster) {
+    for (int l = 1; l + 1 < h->L; ++l)
+      if (h->lv[l].n <= (size_t)kClusterMaxCells && h->L - l <= kSubMaxLevels) {
+        if (h->lv[l].nz >= h->cl_ranks) {
+          h->sub_lc = l;
+          const ClusterCycle<T> P =
+              make_cluster_cycle(make_subcycle<T>(h, false), h->cl_ranks, h->cl_single);
+          const size_t smem = cluster_smem<T>(P);
+          if (smem <= 200 * 1024 && cluster_init<T>(smem, h->cl_ranks) == 0) {
+            h->sub_cluster = true;
+            return;
+          }
+          h->sub_lc = h->L;
+        }
+        break;
+      }
+  }
   for (int l = 1; l + 1 < h->L; ++l)
     if (h->lv[l].n <= (size_t)kSubMaxCells && h->L - l <= kSubMaxLevels) {
       h->sub_lc = l;

@@ -89,6 +89,30 @@ struct SubCycle {
   const T* minv;
   const T* adense;
 };
+// The bottom of the cycle from a level of up to kClusterMaxCells cells on one
+// thread-block cluster of `ranks` blocks (subcycle.cu): the finer levels split
+// by z planes over the blocks, the coarsest ones ("single" levels, at most
+// `single_cells` cells) whole in block 0.
+constexpr int kClusterMaxRanks = 16;
+constexpr int kClusterMaxCells = 32768;
+template <typename T>
+struct ClusterCycle {
+  SubCycle<T> S;               // levels, global arrays, coarse inverse (S.off unused)
+  int ranks;                   // blocks of the cluster
+  int nsplit;                  // levels [0, nsplit) split by planes, the rest in block 0
+  int pz[kSubMaxLevels];       // z planes per block of each level (nz for a single level)
+  int lpz[kSubMaxLevels];      // log2(pz), or -1 when pz is not a power of two
+  int off[kSubMaxLevels + 1];  // shared-memory offset (elements) of each level's
+                               // sol, src, cx, cy, cz; off[nlev]: coarse scratch
+};
+template <typename T>
+ClusterCycle<T> make_cluster_cycle(const SubCycle<T>& S, int ranks, int single_cells);
+template <typename T>
+size_t cluster_smem(const ClusterCycle<T>& P);
+template <typename T>
+int cluster_init(size_t smem, int ranks);
+template <typename T>
+cudaError_t launch_cluster_cycle(cudaStream_t s, const ClusterCycle<T>& P);
 // The middle levels (between the finest and the bottom block) in one
 // cooperative launch (subcycle.cu).
 constexpr int kMidMaxLevels = 8;

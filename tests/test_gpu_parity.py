@@ -306,6 +306,39 @@ def test_single_block_bottom_matches_separate_launches(cuda, monkeypatch, precis
     assert rel_l2(p1, p0) <= 1e-12
 
 
+@pytest.mark.parametrize("precision,idx,scale,krylov", [
+    ("mixed", 1, 8, False), ("mixed", 1, 4, False), ("fp64", 1, 4, False), ("mixed", 4, 2, True),
+    ("fp64", 4, 4, True), ("mixed", 2, 8, False)])
+def test_cluster_bottom_is_bit_identical(cuda, monkeypatch, precision, idx, scale, krylov):
+    """The bottom of the cycle from the first level of at most 32^3 cells on
+    a thread-block cluster (GBMG_CLUSTER=1; 8 or 16 blocks, the finer levels
+    split by z planes, the coarsest whole in block 0 or split too), against
+    the one-block bottom from 16^3 plus separate launches above it.  FP32
+    cycles: the same per-cell arithmetic, so the same bits.  FP64 cycles: the
+    separate FP64 sweeps multiply by a stored inverse diagonal where the
+    bottom divides, so a level that moves into the cluster rounds
+    differently: same cycle count, pressure within 1e-12."""
+    c = cases.config(idx, scale)
+
+    def run(env):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        with solver(c, precision=precision, krylov=krylov, max_cycles=400) as s:
+            s.ppe_init(c.rho)
+            return s.solve(c.b, tol=1e-10)
+
+    p0, s0 = run({"GBMG_CLUSTER": "0"})
+    assert s0["status"] == 0
+    for ranks, single in (("8", "0"), ("8", "4096"), ("16", "4096"), ("16", "0")):
+        p1, s1 = run({"GBMG_CLUSTER": "1", "GBMG_CLUSTER_RANKS": ranks,
+                      "GBMG_CLUSTER_SINGLE": single})
+        assert s1["cycles"] == s0["cycles"], (ranks, single)
+        if precision == "mixed":
+            np.testing.assert_array_equal(p1, p0, err_msg=f"ranks {ranks} single {single}")
+        else:
+            assert rel_l2(p1, p0) <= 1e-12, (ranks, single)
+
+
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (0, 1, False), (4, 4, True)])
 def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     """The FP32 finest-level smoother and restriction computing their face
