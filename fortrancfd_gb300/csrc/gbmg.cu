@@ -47,6 +47,7 @@ struct Level {
   int split = 0;  // sol32, src32 and rho32 in the colour-split layout
   size_t hstride = 0;  // distance between the colour halves (elements)
   int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
+  int zmarch = 0, zc = 16;  // z-marching colour sweep of the split level (LevelView)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -226,9 +227,12 @@ LevelView<double> v64(const Level& l) {
   return LevelView<double>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx, l.cy, l.cz, l.idiag, l.sol, l.src};
 }
 LevelView<float> v32(const Level& l) {
-  return LevelView<float>{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
-                          l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split,
-                          l.hstride};
+  LevelView<float> v{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
+                     l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split,
+                     l.hstride};
+  v.zmarch = l.zmarch;
+  v.zc = l.zc;
+  return v;
 }
 template <typename T>
 LevelView<T> view(const Level& l);
@@ -800,6 +804,15 @@ void set_rho_form(gbmg_handle* h, bool on) {
                              f.nx, f.ny, f.nz, hs);
     h->dmaps_split = oks;
   }
+  // z-marching colour sweep of the split level: GBMG_SMOOTH_Z=1 (blocks of
+  // 8 rows) or 2 (16 rows), GBMG_SMOOTH_ZC planes per thread (default 16)
+  int zm = 0, zc = 16;
+  if (const char* e = std::getenv("GBMG_SMOOTH_Z")) zm = std::min(2, std::max(0, std::atoi(e)));
+  if (const char* e = std::getenv("GBMG_SMOOTH_ZC")) zc = std::max(1, std::atoi(e));
+  if (!split) zm = 0;
+  if (zm != f.zmarch || zc != f.zc) reset_graphs(h);
+  f.zmarch = zm;
+  f.zc = zc;
   f.rho32 = r;
   f.split = split ? 1 : 0;
   f.hstride = hs;

@@ -43,6 +43,9 @@ struct LevelView {
   // on the finest level alternate direction, so each starts on the planes the
   // previous one touched last, which are still in L2
   int zrev = 0;
+  // finest-level sweep marching over chunks of zc z planes per thread
+  // (k_smooth_split4z): 0 off, 1 blocks of 8 rows, 2 blocks of 16 rows
+  int zmarch = 0, zc = 16;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,

@@ -339,6 +339,30 @@ def test_cluster_bottom_is_bit_identical(cuda, monkeypatch, precision, idx, scal
             assert rel_l2(p1, p0) <= 1e-12, (ranks, single)
 
 
+@pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (1, 8, False), (4, 2, True),
+                                            (2, 4, False)])
+def test_z_marching_sweep_is_bit_identical(cuda, monkeypatch, idx, scale, krylov):
+    """The finest-level colour sweep marching over chunks of z planes per
+    thread (GBMG_SMOOTH_Z=1 or 2, chunks of GBMG_SMOOTH_ZC planes, including
+    chunks that do not divide the grid) against the one-plane-per-thread sweep:
+    the same per-cell arithmetic, so the same bits."""
+    c = cases.config(idx, scale)
+
+    def run(env):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        with solver(c, precision="mixed", krylov=krylov, max_cycles=400) as s:
+            s.ppe_init(c.rho)
+            return s.solve(c.b, tol=1e-10)
+
+    p0, s0 = run({"GBMG_SMOOTH_Z": "0"})
+    assert s0["status"] == 0
+    for mode, zc in (("1", "16"), ("2", "16"), ("1", "5"), ("2", "1")):
+        p1, s1 = run({"GBMG_SMOOTH_Z": mode, "GBMG_SMOOTH_ZC": zc})
+        assert s1["cycles"] == s0["cycles"], (mode, zc)
+        np.testing.assert_array_equal(p1, p0, err_msg=f"mode {mode} chunk {zc}")
+
+
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (0, 1, False), (4, 4, True)])
 def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     """The FP32 finest-level smoother and restriction computing their face
