@@ -340,7 +340,7 @@ def test_cluster_bottom_is_bit_identical(cuda, monkeypatch, precision, idx, scal
 
 
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (1, 8, False), (4, 2, True),
-                                            (2, 4, False)])
+                                            (2, 4, True)])
 def test_z_marching_sweep_is_bit_identical(cuda, monkeypatch, idx, scale, krylov):
     """The finest-level colour sweep marching over chunks of z planes per
     thread (GBMG_SMOOTH_Z=1 or 2, chunks of GBMG_SMOOTH_ZC planes, including
