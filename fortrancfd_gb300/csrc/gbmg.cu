@@ -48,6 +48,7 @@ struct Level {
   size_t hstride = 0;  // distance between the colour halves (elements)
   int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
   int zmarch = 0, zc = 16;  // z-marching colour sweep of the split level (LevelView)
+  int minb = 0;             // register bound of the split level's colour sweep (LevelView)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -232,6 +233,7 @@ LevelView<float> v32(const Level& l) {
                      l.hstride};
   v.zmarch = l.zmarch;
   v.zc = l.zc;
+  v.minb = l.minb;
   return v;
 }
 template <typename T>
@@ -810,9 +812,12 @@ void set_rho_form(gbmg_handle* h, bool on) {
   if (const char* e = std::getenv("GBMG_SMOOTH_Z")) zm = std::min(2, std::max(0, std::atoi(e)));
   if (const char* e = std::getenv("GBMG_SMOOTH_ZC")) zc = std::max(1, std::atoi(e));
   if (!split) zm = 0;
-  if (zm != f.zmarch || zc != f.zc) reset_graphs(h);
+  int minb = 0;
+  if (const char* e = std::getenv("GBMG_SMOOTH_MINB")) minb = std::atoi(e);
+  if (zm != f.zmarch || zc != f.zc || minb != f.minb) reset_graphs(h);
   f.zmarch = zm;
   f.zc = zc;
+  f.minb = minb;
   f.rho32 = r;
   f.split = split ? 1 : 0;
   f.hstride = hs;

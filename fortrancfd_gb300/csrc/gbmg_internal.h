@@ -46,6 +46,9 @@ struct LevelView {
   // finest-level sweep marching over chunks of zc z planes per thread
   // (k_smooth_split4z): 0 off, 1 blocks of 8 rows, 2 blocks of 16 rows
   int zmarch = 0, zc = 16;
+  // resident blocks per SM requested from the compiler for the finest-level
+  // colour sweep (0: its own register choice)
+  int minb = 0;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,

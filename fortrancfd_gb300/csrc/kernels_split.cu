@@ -78,8 +78,8 @@ __device__ __forceinline__ void unpack(float4 v, float (&a)[4]) { a[0] = v.x; a[
 // nx % 8 == 0): every load is a float4 except the one-element x edge of the
 // window, and the index and bounds work is shared by the four cells.  The
 // per-cell arithmetic is k_smooth_split's, in the same order.
-template <bool kZero>
-__global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int color) {
+template <bool kZero, int kMinBlocks = 1>
+__global__ void __launch_bounds__(256, kMinBlocks) k_smooth_split4(LevelView<float> L, int color) {
   pdl_enter();
   const int hx = L.nx >> 1;
   const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
@@ -613,7 +613,12 @@ void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, b
   }
   if (vec4_ok(L)) {
     const dim3 g4(cdiv((size_t)(L.nx / 8), 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
+    // L.minb: resident blocks per SM the compiler is asked to allow for
+    // (fewer registers per thread), 0 = its own choice
     if (zero_guess) launch_pdl(k_smooth_split4<true>, g4, blk, 0, s, L, color);
+    else if (L.minb == 5) launch_pdl(k_smooth_split4<false, 5>, g4, blk, 0, s, L, color);
+    else if (L.minb == 6) launch_pdl(k_smooth_split4<false, 6>, g4, blk, 0, s, L, color);
+    else if (L.minb == 8) launch_pdl(k_smooth_split4<false, 8>, g4, blk, 0, s, L, color);
     else launch_pdl(k_smooth_split4<false>, g4, blk, 0, s, L, color);
     return;
   }
