@@ -88,6 +88,10 @@ struct gbmg_handle {
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
   int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
+  // FP32 levels [fused_lo, fused_hi) above the bottom block sweep with the
+  // fused kernel, fused_kz z planes per block (GBMG_FUSED_COARSE = number of
+  // levels from level 1, GBMG_FUSED_KZ)
+  int fused_lo = 0, fused_hi = 0, fused_kz = 4;
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   bool sub_cluster = false;  // ... on a thread-block cluster (k_cluster_cycle)
   int cl_ranks = 8;          // blocks of that cluster
@@ -290,14 +294,16 @@ void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   Level& lv = h->lv[l];
   const LevelView<float> V = v32(lv);
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-  if (zero_guess && (lv.tmaps || h->fused_levels > l))  // out-of-place sweeps read p
+  const bool fused = h->fused_levels > l || (l >= h->fused_lo && l < h->fused_hi);
+  if (zero_guess && (lv.tmaps || fused))  // out-of-place sweeps read p
     cudaMemsetAsync(lv.sol32, 0, lv.n * sizeof(float), h->stream);
   if (lv.tmaps) {
     const SweepMaps& m = lv.tmaps[lv.sol32 == lv.buf_a ? 0 : 1];
     LAUNCH(h, cs, launch_smooth_tma(h->stream, m, lv.nx, lv.ny, lv.nz, lv.alt32, first_color, h->derr));
     std::swap(lv.sol32, lv.alt32);
-  } else if (h->fused_levels > l) {
-    LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color));
+  } else if (fused) {
+    LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color,
+                                             l == 0 ? 0 : h->fused_kz));
     std::swap(lv.sol32, lv.alt32);
   } else {
     LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), first_color, zero_guess));
@@ -694,6 +700,13 @@ int allocate(gbmg_handle* h) {
   else setup_subcycle<double>(h);
   if (h->mixed) GB_TRY(setup_midcycle<float>(h));
   else GB_TRY(setup_midcycle<double>(h));
+  if (h->mixed && !h->mid_ok) {
+    if (const char* e = std::getenv("GBMG_FUSED_COARSE")) {
+      h->fused_lo = 1;
+      h->fused_hi = std::max(1, std::min(1 + std::atoi(e), h->sub_lc));
+    }
+    if (const char* e = std::getenv("GBMG_FUSED_KZ")) h->fused_kz = std::max(1, std::atoi(e));
+  }
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -166,7 +166,7 @@ void launch_smooth_tma(cudaStream_t s, const SweepMaps& maps, int nx, int ny, in
 // red first.  Instantiated for float.
 template <typename T>
 void launch_smooth_fused(cudaStream_t s, const LevelView<T>& L, const T* pin, T* pout,
-                         int first_color);
+                         int first_color, int planes = 0);  // planes per block, 0 = 32
 // zero_sol: also set the coarse unknown to zero (not needed when its first
 // sweep starts from a zero guess)
 template <typename T>

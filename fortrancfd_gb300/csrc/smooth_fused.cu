@@ -28,7 +28,7 @@ namespace {
 
 constexpr int kFTX = 64;     // tile width (x), two cells per thread
 constexpr int kFTY = 8;      // tile height (y)
-constexpr int kFZ = 32;      // z planes per block
+constexpr int kFZ = 32;      // default z planes per block
 constexpr int kSX = kFTX + 4;
 constexpr int kSY = kFTY + 4;
 constexpr int kThreads = kFTX / 2 * kFTY;
@@ -91,11 +91,11 @@ __device__ __forceinline__ void red_stage(const LevelView<T>& L, Ring<T>& R, int
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_smooth_fused(LevelView<T> L, const T* __restrict__ pin,
-                                                           T* __restrict__ pout, int c0) {
+                                                           T* __restrict__ pout, int c0, int kz) {
   __shared__ Ring<T> R;
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * kFTX, y0 = blockIdx.y * kFTY;
-  const int z0 = blockIdx.z * kFZ, z1 = min(z0 + kFZ, L.nz);
+  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, L.nz);
   // prologue: planes z0-2 .. z0, and red of plane z0-1 from them
   for (int k = max(z0 - 2, 0); k <= z0; ++k) load_plane(L, pin, R, k, x0, y0, tid);
   __syncthreads();
@@ -135,13 +135,14 @@ __global__ void __launch_bounds__(kThreads) k_smooth_fused(LevelView<T> L, const
 
 template <typename T>
 void launch_smooth_fused(cudaStream_t s, const LevelView<T>& L, const T* pin, T* pout,
-                         int first_color) {
+                         int first_color, int planes) {
+  const int kz = planes > 0 ? planes : kFZ;
   const dim3 grd((unsigned)((L.nx + kFTX - 1) / kFTX), (unsigned)((L.ny + kFTY - 1) / kFTY),
-                 (unsigned)((L.nz + kFZ - 1) / kFZ));
-  k_smooth_fused<T><<<grd, kThreads, 0, s>>>(L, pin, pout, first_color);
+                 (unsigned)((L.nz + kz - 1) / kz));
+  k_smooth_fused<T><<<grd, kThreads, 0, s>>>(L, pin, pout, first_color, kz);
 }
 
 template void launch_smooth_fused<float>(cudaStream_t, const LevelView<float>&, const float*,
-                                         float*, int);
+                                         float*, int, int);
 
 }  // namespace gbmg

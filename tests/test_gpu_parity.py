@@ -363,6 +363,29 @@ def test_z_marching_sweep_is_bit_identical(cuda, monkeypatch, idx, scale, krylov
         np.testing.assert_array_equal(p1, p0, err_msg=f"mode {mode} chunk {zc}")
 
 
+@pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (1, 4, False), (4, 2, True),
+                                            (0, 1, False)])
+def test_fused_coarse_sweeps_are_bit_identical(cuda, monkeypatch, idx, scale, krylov):
+    """Levels 1.. above the bottom block swept by the one-launch fused
+    red-black kernel (GBMG_FUSED_COARSE levels, GBMG_FUSED_KZ planes per
+    block, out of place) against two colour launches: the same bits."""
+    c = cases.config(idx, scale)
+
+    def run(env):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        with solver(c, precision="mixed", krylov=krylov, max_cycles=400) as s:
+            s.ppe_init(c.rho)
+            return s.solve(c.b, tol=1e-10)
+
+    p0, s0 = run({})
+    assert s0["status"] == 0
+    for n, kz in (("1", "4"), ("3", "2"), ("3", "1"), ("2", "32")):
+        p1, s1 = run({"GBMG_FUSED_COARSE": n, "GBMG_FUSED_KZ": kz})
+        assert s1["cycles"] == s0["cycles"], (n, kz)
+        np.testing.assert_array_equal(p1, p0, err_msg=f"levels {n} planes {kz}")
+
+
 @pytest.mark.parametrize("idx,scale,krylov", [(1, 2, False), (0, 1, False), (4, 4, True)])
 def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     """The FP32 finest-level smoother and restriction computing their face
