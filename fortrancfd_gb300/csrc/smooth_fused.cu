@@ -108,7 +108,9 @@ __global__ void __launch_bounds__(kThreads) k_smooth_fused(LevelView<T> L, const
   const int xa = x0 + 2 * tx, y = y0 + ty;
   for (int k = z0; k <= z1; ++k) {
     __syncthreads();
-    if (k + 1 < L.nz && k + 1 <= z1) load_plane(L, pin, R, k + 1, x0, y0, tid);
+    // plane k+1 is read by the red stage of plane k, also at k = z1 (the
+    // red values under the chunk's last black plane)
+    if (k + 1 < L.nz) load_plane(L, pin, R, k + 1, x0, y0, tid);
     __syncthreads();
     if (k < L.nz && k <= z1) red_stage(L, R, k, x0, y0, tid, c0);
     __syncthreads();
