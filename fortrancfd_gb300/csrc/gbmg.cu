@@ -107,6 +107,13 @@ struct gbmg_handle {
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // host transfers of a solve that overlap its kernels: the H2D of the initial
+  // p beside the right-hand side's preparation, the D2H of the result beside
+  // the FP64 certification
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t cev[2] = {nullptr, nullptr};
+  const gbmg_field* dl_field = nullptr;  // set by gbmg_solve for solve_internal
+  bool dl_started = false;
   int64_t launches = 0;
   // profiling: event pairs around launches, summed per kernel class
   bool prof = false;
@@ -487,6 +494,9 @@ int free_all(gbmg_handle* h) {
   for (int i = 0; i < 2 * 512; ++i)
     if (h->pev[i]) cudaEventDestroy(h->pev[i]);
   if (h->ev0) cudaEventDestroy(h->ev0);
+  for (int i = 0; i < 2; ++i)
+    if (h->cev[i]) cudaEventDestroy(h->cev[i]);
+  if (h->cstream) cudaStreamDestroy(h->cstream);
   if (h->ev1) cudaEventDestroy(h->ev1);
   h->ev0 = h->ev1 = nullptr;
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -708,6 +718,8 @@ int allocate(gbmg_handle* h) {
     if (const char* e = std::getenv("GBMG_FUSED_KZ")) h->fused_kz = std::max(1, std::atoi(e));
   }
   GB_CUDA(h, cudaEventCreate(&h->ev0));
+  GB_CUDA(h, cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; ++i) GB_CUDA(h, cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
@@ -718,41 +730,44 @@ bool dense_cells(const gbmg_field& f, int nx, int ny) {
 }
 
 // Copy a field of extent (ex, ey, ez) into a dense device buffer.
-int upload(gbmg_handle* h, const gbmg_field& f, int ex, int ey, int ez, int mem, double* dst) {
+int upload(gbmg_handle* h, const gbmg_field& f, int ex, int ey, int ez, int mem, double* dst,
+           cudaStream_t s = nullptr) {
+  if (!s) s = h->stream;
   if (!f.data) {
     h->err = "null field";
     return GBMG_INVALID_ARG;
   }
   const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   if (dense_cells(f, ex, ey)) {
-    GB_CUDA(h, cudaMemcpyAsync(dst, f.data, (size_t)ex * ey * ez * sizeof(double), kind, h->stream));
+    GB_CUDA(h, cudaMemcpyAsync(dst, f.data, (size_t)ex * ey * ez * sizeof(double), kind, s));
   } else if (mem == GBMG_MEM_DEVICE) {
-    launch_copy_in(h->stream, ex, ey, ez, Strided{f.data, f.sy, f.sz}, dst);
+    launch_copy_in(s, ex, ey, ez, Strided{f.data, f.sy, f.sz}, dst);
     h->launches += 1;
     GB_TRY(check_launch(h, "copy_in"));
   } else {
     for (int k = 0; k < ez; ++k)
       GB_CUDA(h, cudaMemcpy2DAsync(dst + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
                                    f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
-                                   (size_t)ex * sizeof(double), (size_t)ey, kind, h->stream));
+                                   (size_t)ex * sizeof(double), (size_t)ey, kind, s));
   }
   return GBMG_OK;
 }
 
 int download(gbmg_handle* h, const double* src, int ex, int ey, int ez, int mem,
-             const gbmg_field& f) {
+             const gbmg_field& f, cudaStream_t s = nullptr) {
+  if (!s) s = h->stream;
   const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   if (dense_cells(f, ex, ey)) {
-    GB_CUDA(h, cudaMemcpyAsync(f.data, src, (size_t)ex * ey * ez * sizeof(double), kind, h->stream));
+    GB_CUDA(h, cudaMemcpyAsync(f.data, src, (size_t)ex * ey * ez * sizeof(double), kind, s));
   } else if (mem == GBMG_MEM_DEVICE) {
-    launch_copy_out(h->stream, ex, ey, ez, src, f.data, f.sy, f.sz);
+    launch_copy_out(s, ex, ey, ez, src, f.data, f.sy, f.sz);
     h->launches += 1;
     GB_TRY(check_launch(h, "copy_out"));
   } else {
     for (int k = 0; k < ez; ++k)
       GB_CUDA(h, cudaMemcpy2DAsync(f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
                                    src + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
-                                   (size_t)ex * sizeof(double), (size_t)ey, kind, h->stream));
+                                   (size_t)ex * sizeof(double), (size_t)ey, kind, s));
   }
   return GBMG_OK;
 }
@@ -1031,6 +1046,14 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
   }
   GB_TRY(check_launch(h, "mean"));
+  if (h->dl_field) {
+    // p is final: its copy to the host runs beside the certification
+    GB_CUDA(h, cudaEventRecord(h->cev[1], s));
+    GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[1], 0));
+    GB_TRY(download(h, h->p, h->grid.nx, h->grid.ny, h->grid.nz, GBMG_MEM_HOST, *h->dl_field,
+                    h->cstream));
+    h->dl_started = true;
+  }
   if (kind == kGraphMixed && h->prm.certify) {
     // the loop tracked the residual in double-word; restate it in native FP64
     f.sol = h->p; f.src = h->b;
@@ -1266,11 +1289,35 @@ int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
   const gbmg_grid& g = h->grid;
   GB_CUDA(h, cudaEventRecord(h->ev0, h->stream));
   double bnorm = 0.0;
+  const bool host = mem == GBMG_MEM_HOST;
+  if (host) {
+    // host memory: the initial p crosses to the device beside the right-hand
+    // side's upload and preparation, and the result crosses back beside the
+    // certification (the copies run on the handle's second stream)
+    GB_CUDA(h, cudaEventRecord(h->cev[0], h->stream));
+    GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[0], 0));
+    GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p, h->cstream));
+    GB_CUDA(h, cudaEventRecord(h->cev[0], h->cstream));
+  }
   GB_TRY(prepare_rhs(h, b, mem, &bnorm));
-  GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  if (host) GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[0], 0));
+  else GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+  h->dl_field = host ? &p : nullptr;
+  h->dl_started = false;
   const int status = solve_internal(h, tol, bnorm, st);
-  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
-  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
+  h->dl_field = nullptr;
+  const bool downloaded = h->dl_started;
+  if (h->dl_started) {
+    h->dl_started = false;
+    GB_CUDA(h, cudaEventRecord(h->cev[0], h->cstream));
+    GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[0], 0));
+  }
+  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) {
+    cudaStreamSynchronize(h->cstream);
+    return status;
+  }
+  if (!host) GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
+  else if (!downloaded) GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, p));
   GB_CUDA(h, cudaEventRecord(h->ev1, h->stream));
   GB_CUDA(h, cudaEventSynchronize(h->ev1));
   float ms = 0.f;
