@@ -1011,3 +1011,124 @@ void or_set_threads(int n) {
   (void)n;
 #endif
 }
+
+/* ------------------------------------------------------------------------- */
+/* Level-set advection, level_set_rk3_solver (NO2 src/interface_solver/       */
+/* level_set_rk3_solver.f90:1-128; NO3 :1-160): phi_t + div(u phi) = 0 with   */
+/* the cell-centred velocity, the flux split into u+ phi and u- phi           */
+/* (level_set_rk3_source_setup), each part reconstructed at the faces by      */
+/* WENO-JS (wenojs_flux_split, NO2 :131-186, EPS = 1e-13), zero-gradient      */
+/* ghosts for the split fluxes (bc, NO2 src/others/bcs.f90:1-26) and three    */
+/* stages of SSP-RK3 in the reference's incremental form.  nz = 1 is the 2D   */
+/* solver (no z term).                                                        */
+/* ------------------------------------------------------------------------- */
+static inline double ls_sq(double x) { return x * x; }
+
+/* value at face i+1/2 of g(i-2..i+2) = g0..g4, biased to the left */
+static double or_weno_left(double g0, double g1, double g2, double g3, double g4, double eps) {
+  const double b1 = 13.0 * ls_sq((g0 - 2.0 * g1) + g2) + 3.0 * ls_sq((g0 - 4.0 * g1) + 3.0 * g2);
+  const double b2 = 13.0 * ls_sq((g1 - 2.0 * g2) + g3) + 3.0 * ls_sq(g1 - g3);
+  const double b3 = 13.0 * ls_sq((g2 - 2.0 * g3) + g4) + 3.0 * ls_sq((3.0 * g2 - 4.0 * g3) + g4);
+  const double a1 = 1.0 / ls_sq(eps + b1), a2 = 6.0 / ls_sq(eps + b2), a3 = 3.0 / ls_sq(eps + b3);
+  const double s = (a1 + a2) + a3;
+  const double w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  double v = w1 / 3.0 * g0;
+  v = v - (7.0 * w1 + w2) / 6.0 * g1;
+  v = v + ((11.0 * w1 + 5.0 * w2) + 2.0 * w3) / 6.0 * g2;
+  v = v + (2.0 * w2 + 5.0 * w3) / 6.0 * g3;
+  v = v - w3 / 6.0 * g4;
+  return v;
+}
+
+/* value at face i+1/2 of f(i-1..i+3) = f0..f4, biased to the right */
+static double or_weno_right(double f0, double f1, double f2, double f3, double f4, double eps) {
+  const double b3 = 13.0 * ls_sq((f0 - 2.0 * f1) + f2) + 3.0 * ls_sq((f0 - 4.0 * f1) + 3.0 * f2);
+  const double b2 = 13.0 * ls_sq((f1 - 2.0 * f2) + f3) + 3.0 * ls_sq(f1 - f3);
+  const double b1 = 13.0 * ls_sq((f2 - 2.0 * f3) + f4) + 3.0 * ls_sq((3.0 * f2 - 4.0 * f3) + f4);
+  const double a1 = 1.0 / ls_sq(eps + b1), a2 = 6.0 / ls_sq(eps + b2), a3 = 3.0 / ls_sq(eps + b3);
+  const double s = (a1 + a2) + a3;
+  const double w1 = a1 / s, w2 = a2 / s, w3 = a3 / s;
+  double v = w3 * ((-f0 + 5.0 * f1) + 2.0 * f2) / 6.0;
+  v = v + w2 * ((2.0 * f1 + 5.0 * f2) - f3) / 6.0;
+  v = v + w1 * ((11.0 * f2 - 7.0 * f3) + 2.0 * f4) / 6.0;
+  return v;
+}
+
+static inline int ls_clamp(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+
+/* split flux of cell c along one axis: sgn +1 -> u+ phi, -1 -> u- phi */
+static inline double ls_split(const double* phi, const double* vel, size_t c, int sgn) {
+  const double a = vel[c];
+  return sgn > 0 ? 0.5 * (a + fabs(a)) * phi[c] : 0.5 * (a - fabs(a)) * phi[c];
+}
+
+/* L(phi) = -sum over axes of (ss1(i) + ss2(i) - ss1(i-1) - ss2(i-1))/h
+ * (level_set_rk3_source): ss1 the left-biased value of u+ phi, ss2 the
+ * right-biased value of u- phi at face i+1/2 */
+void or_ls_source(const or_grid* g, const double* phi, const double* u, const double* v,
+                  const double* w, double* out) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const double eps = 1.0e-13;
+  const int dims[3] = {nx, ny, nz};
+  const size_t strides[3] = {1, (size_t)nx, (size_t)nx * ny};
+  const double* vel[3] = {u, v, w};
+  const double h[3] = {g->dx, g->dy, g->dz};
+  const int naxes = nz > 1 ? 3 : 2;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int idx[3] = {i, j, k};
+        const size_t q = ((size_t)k * ny + j) * nx + i;
+        double src = 0.0;
+        for (int a = 0; a < naxes; ++a) {
+          const int n = dims[a], c = idx[a];
+          const size_t base = q - (size_t)c * strides[a];
+          double ss1[2], ss2[2];
+          for (int f = 0; f < 2; ++f) {  /* faces c-1/2 (f = 0) and c+1/2 (f = 1) */
+            const int fi = c - 1 + f;     /* the face is fi+1/2 */
+            double gv[5], fv[5];
+            for (int m = 0; m < 5; ++m) {
+              const size_t cg = base + (size_t)ls_clamp(fi - 2 + m, n) * strides[a];
+              const size_t cf = base + (size_t)ls_clamp(fi - 1 + m, n) * strides[a];
+              gv[m] = ls_split(phi, vel[a], cg, 1);
+              fv[m] = ls_split(phi, vel[a], cf, -1);
+            }
+            ss1[f] = or_weno_left(gv[0], gv[1], gv[2], gv[3], gv[4], eps);
+            ss2[f] = or_weno_right(fv[0], fv[1], fv[2], fv[3], fv[4], eps);
+          }
+          const double d = ((ss1[1] + ss2[1]) - ss1[0]) - ss2[0];
+          src = a == 0 ? -(d / h[a]) : src - d / h[a];
+        }
+        out[q] = src;
+      }
+}
+
+/* steps SSP-RK3 steps (level_set_rk3_solver); l1..l3: scratch of n cells */
+void or_ls_advect(const or_grid* g, double* phi, const double* u, const double* v,
+                  const double* w, double dt, int steps) {
+  const size_t n = cells_of(g->nx, g->ny, g->nz);
+  double* l1 = (double*)malloc(n * sizeof(double));
+  double* l2 = (double*)malloc(n * sizeof(double));
+  double* l3 = (double*)malloc(n * sizeof(double));
+  for (int s = 0; s < steps; ++s) {
+    or_ls_source(g, phi, u, v, w, l1);
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < n; ++q) phi[q] = phi[q] + l1[q] * dt;
+    or_ls_source(g, phi, u, v, w, l2);
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < n; ++q) {
+      const double src = (-3.0 * l1[q] + l2[q]) / 4.0;
+      phi[q] = phi[q] + src * dt;
+    }
+    or_ls_source(g, phi, u, v, w, l3);
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < n; ++q) {
+      const double src = ((-l1[q] - l2[q]) + 8.0 * l3[q]) / 12.0;
+      phi[q] = phi[q] + src * dt;
+    }
+  }
+  free(l1);
+  free(l2);
+  free(l3);
+}

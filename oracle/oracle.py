@@ -74,6 +74,8 @@ def lib():
         L.or_mg_level_coef.restype = C.c_int
         L.or_adjoint.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, C.c_double, C.c_double,
                                  C.c_double, _D, _D]
+        L.or_ls_source.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D]
+        L.or_ls_advect.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, C.c_double, C.c_int]
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -244,6 +246,28 @@ def adjoint(rho, p, lam, spacing, phi=None, eps=1.0, rho_pos=1.0, rho_neg=1.0):
     lib().or_adjoint(C.byref(g), _p(rho), _p(p), _p(lam), _p(ph), eps, rho_pos, rho_neg,
                      _p(grad_rho), _p(grad_phi))
     return grad_rho, grad_phi
+
+
+def ls_source(phi, u, v, w, spacing):
+    """L(phi) of level_set_rk3_source: WENO-JS split fluxes of u phi (cell-
+    centred velocity u, v, w; w ignored for a 2D grid)."""
+    phi = np.ascontiguousarray(phi, np.float64)
+    g = grid(phi.shape, spacing)
+    out = np.empty_like(phi)
+    w_ = None if phi.shape[0] == 1 or w is None else np.ascontiguousarray(w, np.float64)
+    lib().or_ls_source(C.byref(g), _p(phi), _p(np.ascontiguousarray(u, np.float64)),
+                       _p(np.ascontiguousarray(v, np.float64)), _p(w_), _p(out))
+    return out
+
+
+def ls_advect(phi, u, v, w, dt, spacing, steps=1):
+    """steps SSP-RK3 steps of level_set_rk3_solver; returns the new phi."""
+    phi = np.array(phi, np.float64, order="C", copy=True)
+    g = grid(phi.shape, spacing)
+    w_ = None if phi.shape[0] == 1 or w is None else np.ascontiguousarray(w, np.float64)
+    lib().or_ls_advect(C.byref(g), _p(phi), _p(np.ascontiguousarray(u, np.float64)),
+                       _p(np.ascontiguousarray(v, np.float64)), _p(w_), float(dt), int(steps))
+    return phi
 
 
 def set_threads(n):

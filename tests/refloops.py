@@ -429,3 +429,134 @@ def ppe_mg_split_correction(rho, p, p_hat, u, v, w, rho_12, dt, dx, dy, dz):
                         (T[i, j, k + 1] - T[i, j, k]) / dz
                     w[k, j - 1, i - 1] = w[k, j - 1, i - 1] - s * dt
     return u, v, w
+
+
+# --- level-set advection ------------------------------------------------------------
+# level_set_rk3_solver / level_set_rk3_source_setup / level_set_rk3_source /
+# wenojs_flux_split: "Two phase flows/newOpenMP/2D/src/interface_solver/
+# level_set_rk3_solver.f90:1-186" (3D: "Two phase flows/newOpenMP/3D+IBM/src/
+# interface_solver/level_set_rk3_solver.f90:1-215"); arrays carry ghc = 3
+# ghost layers on every axis (numpy index = Fortran index + 3).
+LS_GHC = 3
+
+
+def _bc3(a):
+    """bc with ghc ghost layers: copy the first/last interior cell outwards."""
+    g = LS_GHC
+    for ax in range(a.ndim):
+        n = a.shape[ax] - 2 * g
+        for m in range(1, g + 1):
+            lo = [slice(None)] * a.ndim
+            src = [slice(None)] * a.ndim
+            lo[ax] = g - m
+            src[ax] = g
+            a[tuple(lo)] = a[tuple(src)]
+            hi = [slice(None)] * a.ndim
+            srch = [slice(None)] * a.ndim
+            hi[ax] = g + n - 1 + m
+            srch[ax] = g + n - 1
+            a[tuple(hi)] = a[tuple(srch)]
+
+
+def _wenojs_flux_split(f, g, nn):
+    """One line: returns (fp, gm) over i = is-ghc+2 .. ie+ghc-3 (numpy 2 .. nn+2)."""
+    eps = 1.0e-13
+    fp = [0.0] * len(f)
+    gm = [0.0] * len(g)
+    for i in range(2, nn + 3):
+        b1 = 13.0 * (g[i - 2] - 2.0 * g[i - 1] + g[i]) ** 2 + 3.0 * (g[i - 2] - 4.0 * g[i - 1] + 3.0 * g[i]) ** 2
+        b2 = 13.0 * (g[i - 1] - 2.0 * g[i] + g[i + 1]) ** 2 + 3.0 * (g[i - 1] - g[i + 1]) ** 2
+        b3 = 13.0 * (g[i] - 2.0 * g[i + 1] + g[i + 2]) ** 2 + 3.0 * (3.0 * g[i] - 4.0 * g[i + 1] + g[i + 2]) ** 2
+        a1 = 1.0 / (eps + b1) ** 2
+        a2 = 6.0 / (eps + b2) ** 2
+        a3 = 3.0 / (eps + b3) ** 2
+        w1 = a1 / (a1 + a2 + a3)
+        w2 = a2 / (a1 + a2 + a3)
+        w3 = a3 / (a1 + a2 + a3)
+        gm[i] = (w1 / 3.0 * g[i - 2] - (7.0 * w1 + w2) / 6.0 * g[i - 1]
+                 + (11.0 * w1 + 5.0 * w2 + 2.0 * w3) / 6.0 * g[i]
+                 + (2.0 * w2 + 5.0 * w3) / 6.0 * g[i + 1] - w3 / 6.0 * g[i + 2])
+    for i in range(2, nn + 3):
+        b3 = 13.0 * (f[i - 1] - 2.0 * f[i] + f[i + 1]) ** 2 + 3.0 * (f[i - 1] - 4.0 * f[i] + 3.0 * f[i + 1]) ** 2
+        b2 = 13.0 * (f[i] - 2.0 * f[i + 1] + f[i + 2]) ** 2 + 3.0 * (f[i] - f[i + 2]) ** 2
+        b1 = 13.0 * (f[i + 1] - 2.0 * f[i + 2] + f[i + 3]) ** 2 + 3.0 * (3.0 * f[i + 1] - 4.0 * f[i + 2] + f[i + 3]) ** 2
+        a1 = 1.0 / (eps + b1) ** 2
+        a2 = 6.0 / (eps + b2) ** 2
+        a3 = 3.0 / (eps + b3) ** 2
+        w1 = a1 / (a1 + a2 + a3)
+        w2 = a2 / (a1 + a2 + a3)
+        w3 = a3 / (a1 + a2 + a3)
+        fp[i] = (w3 * (-f[i - 1] + 5.0 * f[i] + 2.0 * f[i + 1]) / 6.0
+                 + w2 * (2.0 * f[i] + 5.0 * f[i + 1] - f[i + 2]) / 6.0
+                 + w1 * (11.0 * f[i + 1] - 7.0 * f[i + 2] + 2.0 * f[i + 3]) / 6.0)
+    return fp, gm
+
+
+def level_set_rk3_solver(phi, u, v, w, dt, dx, dy, dz, steps=1):
+    """phi, u, v, w: (nz, ny, nx) cell arrays (w ignored when nz == 1).
+    Returns phi after `steps` steps."""
+    nz, ny, nx = phi.shape
+    three = nz > 1
+    g = LS_GHC
+    # Fortran (i, j, k) layout: numpy arrays of shape (nx+2g, ny+2g, nz+2g)
+    P = np.zeros((nx + 2 * g, ny + 2 * g, nz + 2 * g))
+    P[g:g + nx, g:g + ny, g:g + nz] = np.transpose(phi, (2, 1, 0))
+    vel = [np.transpose(a, (2, 1, 0)) for a in ((u, v, w) if three else (u, v))]
+    h = (dx, dy, dz)
+    n = (nx, ny, nz)
+
+    def source():
+        S1, S2, SS1, SS2 = [], [], [], []
+        for a in range(len(vel)):
+            s1 = np.zeros_like(P)
+            s2 = np.zeros_like(P)
+            for i in range(nx):
+                for j in range(ny):
+                    for k in range(nz):
+                        un = vel[a][i, j, k]
+                        ph = P[g + i, g + j, g + k]
+                        s1[g + i, g + j, g + k] = 0.5 * (un + abs(un)) * ph
+                        s2[g + i, g + j, g + k] = 0.5 * (un - abs(un)) * ph
+            _bc3(s1)
+            _bc3(s2)
+            ss1 = np.zeros_like(P)
+            ss2 = np.zeros_like(P)
+            # lines along axis a through every interior point of the other axes
+            others = [b for b in range(3) if b != a]
+            for p0 in range(n[others[0]]):
+                for p1 in range(n[others[1]]):
+                    idx = [0, 0, 0]
+                    idx[others[0]] = g + p0
+                    idx[others[1]] = g + p1
+                    sl = list(idx)
+                    sl[a] = slice(None)
+                    fp, gm = _wenojs_flux_split(list(s2[tuple(sl)]), list(s1[tuple(sl)]), n[a])
+                    ss2[tuple(sl)] = fp
+                    ss1[tuple(sl)] = gm
+            SS1.append(ss1)
+            SS2.append(ss2)
+        out = np.zeros((nx, ny, nz))
+        for i in range(nx):
+            for j in range(ny):
+                for k in range(nz):
+                    I, J, K = g + i, g + j, g + k
+                    s = -(SS1[0][I, J, K] + SS2[0][I, J, K] - SS1[0][I - 1, J, K] - SS2[0][I - 1, J, K]) / dx \
+                        - (SS1[1][I, J, K] + SS2[1][I, J, K] - SS1[1][I, J - 1, K] - SS2[1][I, J - 1, K]) / dy
+                    if three:
+                        s = s - (SS1[2][I, J, K] + SS2[2][I, J, K] - SS1[2][I, J, K - 1]
+                                 - SS2[2][I, J, K - 1]) / dz
+                    out[i, j, k] = s
+        return out
+
+    for _ in range(steps):
+        l1 = source()
+        P[g:g + nx, g:g + ny, g:g + nz] = P[g:g + nx, g:g + ny, g:g + nz] + l1 * dt
+        _bc3(P)
+        l2 = source()
+        P[g:g + nx, g:g + ny, g:g + nz] = P[g:g + nx, g:g + ny, g:g + nz] + ((-3.0 * l1 + l2) / 4.0) * dt
+        _bc3(P)
+        l3 = source()
+        P[g:g + nx, g:g + ny, g:g + nz] = (P[g:g + nx, g:g + ny, g:g + nz]
+                                          + ((-l1 - l2 + 8.0 * l3) / 12.0) * dt)
+        _bc3(P)
+    return np.ascontiguousarray(np.transpose(P[g:g + nx, g:g + ny, g:g + nz], (2, 1, 0)))
