@@ -31,6 +31,8 @@ EXPORTS = (
     "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims", "gbmg_kernel_launches",
     "gbmg_strerror", "gbmg_last_error", "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint",
     "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split",
+    "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_kernel_launches",
+    "gbmg_ls_last_error",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -117,6 +119,15 @@ def load(build_if_missing: bool = True):
         L.gbmg_div_stats_noalloc.argtypes = [P(Grid), Field, Field, Field, P(C.c_double),
                                              P(C.c_double), C.c_int, C.c_void_p, C.c_char_p,
                                              C.c_size_t]
+        L.gbmg_ls_create.argtypes = [P(Grid), C.c_int, C.c_void_p, P(H)]
+        L.gbmg_ls_destroy.argtypes = [H]
+        L.gbmg_ls_advect.argtypes = [H, Field, Field, Field, Field, C.c_double, C.c_int, C.c_int]
+        L.gbmg_ls_kernel_launches.argtypes = [H]
+        L.gbmg_ls_kernel_launches.restype = C.c_int64
+        L.gbmg_ls_last_error.argtypes = [H]
+        L.gbmg_ls_last_error.restype = C.c_char_p
+        for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect"):
+            getattr(L, name).restype = C.c_int
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",
                      "gbmg_residual", "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims",

@@ -1,0 +1,361 @@
+// Level-set transport on sm_103a: the advection step of the reference's
+// interface solver, level_set_rk3_solver ("Two phase flows/newOpenMP/2D/src/
+// interface_solver/level_set_rk3_solver.f90:1-186"; 3D "Two phase flows/
+// newOpenMP/3D+IBM/src/interface_solver/level_set_rk3_solver.f90:1-215").
+//
+// phi_t + div(u phi) = 0 with the cell-centred velocity: the flux is split
+// into u+ phi and u- phi (level_set_rk3_source_setup), each part is
+// reconstructed at every face by WENO-JS (wenojs_flux_split, EPS = 1e-13) --
+// u+ phi from the five cells left of the face, u- phi from the five cells
+// right of it -- with zero-gradient ghosts (bc: an index outside the grid
+// reads the nearest boundary cell), and three stages of SSP-RK3 in the
+// reference's incremental form advance phi.  nz = 1 is the 2D solver.
+//
+// The faces are reconstructed once each (k_ls_faces, one thread per face,
+// both split parts), then k_ls_stage forms L(phi) per cell in the
+// reference's order and applies the stage.  All arithmetic is FP64 with every
+// product rounded on its own (no fused multiply-add), so the results equal
+// the FP64 oracle bit for bit.  GB300 runs FP64 at about 1/57 of its FP32
+// rate and a face costs two reconstructions of about 20 divisions each, so
+// these kernels are bound by the FP64 pipe, not by memory.
+#include <cstring>
+#include <string>
+
+#include "gbmg.h"
+#include "gbmg_internal.h"
+
+namespace gbmg {
+
+namespace {
+
+__device__ __forceinline__ double dsq(double x) { return __dmul_rn(x, x); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+// value at face i+1/2 of g(i-2..i+2) = g0..g4, biased to the left
+__device__ double weno_left(double g0, double g1, double g2, double g3, double g4, double eps) {
+  const double b1 = add(mul(13.0, dsq(add(sub(g0, mul(2.0, g1)), g2))),
+                        mul(3.0, dsq(add(sub(g0, mul(4.0, g1)), mul(3.0, g2)))));
+  const double b2 = add(mul(13.0, dsq(add(sub(g1, mul(2.0, g2)), g3))), mul(3.0, dsq(sub(g1, g3))));
+  const double b3 = add(mul(13.0, dsq(add(sub(g2, mul(2.0, g3)), g4))),
+                        mul(3.0, dsq(add(sub(mul(3.0, g2), mul(4.0, g3)), g4))));
+  const double a1 = dvd(1.0, dsq(add(eps, b1)));
+  const double a2 = dvd(6.0, dsq(add(eps, b2)));
+  const double a3 = dvd(3.0, dsq(add(eps, b3)));
+  const double s = add(add(a1, a2), a3);
+  const double w1 = dvd(a1, s), w2 = dvd(a2, s), w3 = dvd(a3, s);
+  double v = mul(dvd(w1, 3.0), g0);
+  v = sub(v, mul(dvd(add(mul(7.0, w1), w2), 6.0), g1));
+  v = add(v, mul(dvd(add(add(mul(11.0, w1), mul(5.0, w2)), mul(2.0, w3)), 6.0), g2));
+  v = add(v, mul(dvd(add(mul(2.0, w2), mul(5.0, w3)), 6.0), g3));
+  v = sub(v, mul(dvd(w3, 6.0), g4));
+  return v;
+}
+
+// value at face i+1/2 of f(i-1..i+3) = f0..f4, biased to the right
+__device__ double weno_right(double f0, double f1, double f2, double f3, double f4, double eps) {
+  const double b3 = add(mul(13.0, dsq(add(sub(f0, mul(2.0, f1)), f2))),
+                        mul(3.0, dsq(add(sub(f0, mul(4.0, f1)), mul(3.0, f2)))));
+  const double b2 = add(mul(13.0, dsq(add(sub(f1, mul(2.0, f2)), f3))), mul(3.0, dsq(sub(f1, f3))));
+  const double b1 = add(mul(13.0, dsq(add(sub(f2, mul(2.0, f3)), f4))),
+                        mul(3.0, dsq(add(sub(mul(3.0, f2), mul(4.0, f3)), f4))));
+  const double a1 = dvd(1.0, dsq(add(eps, b1)));
+  const double a2 = dvd(6.0, dsq(add(eps, b2)));
+  const double a3 = dvd(3.0, dsq(add(eps, b3)));
+  const double s = add(add(a1, a2), a3);
+  const double w1 = dvd(a1, s), w2 = dvd(a2, s), w3 = dvd(a3, s);
+  double v = dvd(mul(w3, add(add(-f0, mul(5.0, f1)), mul(2.0, f2))), 6.0);
+  v = add(v, dvd(mul(w2, sub(add(mul(2.0, f1), mul(5.0, f2)), f3)), 6.0));
+  v = add(v, dvd(mul(w1, add(sub(mul(11.0, f2), mul(7.0, f3)), mul(2.0, f4))), 6.0));
+  return v;
+}
+
+__device__ __forceinline__ int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+
+struct LsGrid {
+  int nx, ny, nz;
+  double dx, dy, dz;
+};
+
+// Faces of one axis: face f (0..n) is the reference's face i+1/2 with
+// i = f - 1; ss1 = left-biased WENO of u+ phi, ss2 = right-biased of u- phi.
+// The face arrays are laid out like cell arrays with n+1 entries along the
+// axis.
+__global__ void __launch_bounds__(256) k_ls_faces(LsGrid g, int axis, const double* __restrict__ phi,
+                                                  const double* __restrict__ vel,
+                                                  double* __restrict__ ss1,
+                                                  double* __restrict__ ss2) {
+  const int ex = g.nx + (axis == 0), ey = g.ny + (axis == 1), ez = g.nz + (axis == 2);
+  const size_t nf = (size_t)ex * ey * ez;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  const int a = (int)(t % ex);
+  const size_t r = t / ex;
+  const int b = (int)(r % ey), c = (int)(r / ey);
+  // position of the face along the axis and the line through it
+  const int f = axis == 0 ? a : (axis == 1 ? b : c);
+  const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+  const size_t stride = axis == 0 ? 1 : (axis == 1 ? (size_t)g.nx : (size_t)g.nx * g.ny);
+  const int i0 = axis == 0 ? 0 : a, j0 = axis == 1 ? 0 : b, k0 = axis == 2 ? 0 : c;
+  const size_t base = ((size_t)k0 * g.ny + j0) * g.nx + i0;
+  const int fi = f - 1;
+  double gp[6], gm[6];  // u+ phi and u- phi of cells fi-2 .. fi+3
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const size_t q = base + (size_t)clampi(fi - 2 + m, n) * stride;
+    const double u = vel[q], p = phi[q];
+    gp[m] = mul(mul(0.5, add(u, fabs(u))), p);
+    gm[m] = mul(mul(0.5, sub(u, fabs(u))), p);
+  }
+  const double eps = 1.0e-13;
+  ss1[t] = weno_left(gp[0], gp[1], gp[2], gp[3], gp[4], eps);
+  ss2[t] = weno_right(gm[1], gm[2], gm[3], gm[4], gm[5], eps);
+}
+
+// One stage: l = L(phi) per cell, then phi += src * dt with the stage's
+// combination of l1, l2, l3 (level_set_rk3_solver).
+__global__ void __launch_bounds__(256) k_ls_stage(LsGrid g, int stage, double dt,
+                                                  const double* __restrict__ x1,
+                                                  const double* __restrict__ x2,
+                                                  const double* __restrict__ y1,
+                                                  const double* __restrict__ y2,
+                                                  const double* __restrict__ z1,
+                                                  const double* __restrict__ z2, double* l1,
+                                                  double* l2, double* phi) {
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q % g.nx);
+  const size_t r = q / g.nx;
+  const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+  // face indices: high face of the cell = low face + one step along the axis
+  const size_t fx = ((size_t)k * g.ny + j) * (g.nx + 1) + i;
+  const size_t fy = ((size_t)k * (g.ny + 1) + j) * g.nx + i;
+  const size_t fz = ((size_t)k * g.ny + j) * g.nx + i;
+  double d = sub(sub(add(x1[fx + 1], x2[fx + 1]), x1[fx]), x2[fx]);
+  double src = -dvd(d, g.dx);
+  d = sub(sub(add(y1[fy + g.nx], y2[fy + g.nx]), y1[fy]), y2[fy]);
+  src = sub(src, dvd(d, g.dy));
+  if (g.nz > 1) {
+    const size_t pz = (size_t)g.nx * g.ny;
+    d = sub(sub(add(z1[fz + pz], z2[fz + pz]), z1[fz]), z2[fz]);
+    src = sub(src, dvd(d, g.dz));
+  }
+  double s;
+  if (stage == 1) {
+    l1[q] = src;
+    s = src;
+  } else if (stage == 2) {
+    l2[q] = src;
+    s = dvd(add(mul(-3.0, l1[q]), src), 4.0);
+  } else {
+    s = dvd(add(sub(-l1[q], l2[q]), mul(8.0, src)), 12.0);
+  }
+  phi[q] = add(phi[q], mul(s, dt));
+}
+
+inline unsigned blocks_for(size_t n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+}  // namespace gbmg
+
+using namespace gbmg;
+
+struct gbmg_ls {
+  gbmg_grid grid{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double *phi = nullptr, *u = nullptr, *v = nullptr, *w = nullptr, *l1 = nullptr, *l2 = nullptr;
+  double* face[6] = {};
+  int64_t launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int ls_fail(gbmg_ls* ls, cudaError_t e, const char* what) {
+  ls->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? GBMG_OUT_OF_MEMORY : GBMG_CUDA_ERROR;
+}
+
+#define LS_CUDA(ls, call)                              \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return ls_fail(ls, e_, #call); \
+  } while (0)
+
+size_t ls_cells(const gbmg_grid& g) { return (size_t)g.nx * g.ny * g.nz; }
+
+void ls_free(gbmg_ls* ls) {
+  double** all[] = {&ls->phi, &ls->u, &ls->v, &ls->w, &ls->l1, &ls->l2, &ls->face[0], &ls->face[1],
+                    &ls->face[2], &ls->face[3], &ls->face[4], &ls->face[5]};
+  for (double** p : all)
+    if (*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+}
+
+// host or device field (strided, x contiguous) -> dense device array
+int ls_in(gbmg_ls* ls, const gbmg_field& f, int mem, double* dst) {
+  const gbmg_grid& g = ls->grid;
+  if (!f.data || f.sy < g.nx || f.sz < f.sy * (int64_t)g.ny) {
+    ls->err = "invalid field";
+    return GBMG_INVALID_ARG;
+  }
+  const bool dense = f.sy == g.nx && f.sz == (int64_t)g.nx * g.ny;
+  if (dense) {
+    LS_CUDA(ls, cudaMemcpyAsync(dst, f.data, ls_cells(g) * sizeof(double),
+                                mem == GBMG_MEM_HOST ? cudaMemcpyHostToDevice
+                                                     : cudaMemcpyDeviceToDevice,
+                                ls->stream));
+  } else if (mem == GBMG_MEM_DEVICE) {
+    launch_copy_in(ls->stream, g.nx, g.ny, g.nz, Strided{f.data, f.sy, f.sz}, dst);
+    ls->launches += 1;
+    LS_CUDA(ls, cudaGetLastError());
+  } else {
+    for (int k = 0; k < g.nz; ++k)
+      LS_CUDA(ls, cudaMemcpy2DAsync(dst + (size_t)k * g.nx * g.ny, (size_t)g.nx * sizeof(double),
+                                    f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
+                                    (size_t)g.nx * sizeof(double), (size_t)g.ny,
+                                    cudaMemcpyHostToDevice, ls->stream));
+  }
+  return GBMG_OK;
+}
+
+int ls_out(gbmg_ls* ls, const double* src, int mem, const gbmg_field& f) {
+  const gbmg_grid& g = ls->grid;
+  const bool dense = f.sy == g.nx && f.sz == (int64_t)g.nx * g.ny;
+  if (dense) {
+    LS_CUDA(ls, cudaMemcpyAsync(f.data, src, ls_cells(g) * sizeof(double),
+                                mem == GBMG_MEM_HOST ? cudaMemcpyDeviceToHost
+                                                     : cudaMemcpyDeviceToDevice,
+                                ls->stream));
+  } else if (mem == GBMG_MEM_DEVICE) {
+    launch_copy_out(ls->stream, g.nx, g.ny, g.nz, src, f.data, f.sy, f.sz);
+    ls->launches += 1;
+    LS_CUDA(ls, cudaGetLastError());
+  } else {
+    for (int k = 0; k < g.nz; ++k)
+      LS_CUDA(ls, cudaMemcpy2DAsync(f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
+                                    src + (size_t)k * g.nx * g.ny, (size_t)g.nx * sizeof(double),
+                                    (size_t)g.nx * sizeof(double), (size_t)g.ny,
+                                    cudaMemcpyDeviceToHost, ls->stream));
+  }
+  return GBMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbmg_ls_create(const gbmg_grid* grid, int device, void* stream, gbmg_ls** out) {
+  if (!grid || !out) return GBMG_INVALID_ARG;
+  *out = nullptr;
+  if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0) || !(grid->dy > 0) ||
+      (grid->nz > 1 && !(grid->dz > 0)))
+    return GBMG_INVALID_ARG;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return GBMG_NO_DEVICE;
+  gbmg_ls* ls = new gbmg_ls();
+  ls->grid = *grid;
+  if (device < 0) cudaGetDevice(&device);
+  ls->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete ls;
+    return GBMG_NO_DEVICE;
+  }
+  if (stream) {
+    ls->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&ls->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete ls;
+      return GBMG_CUDA_ERROR;
+    }
+    ls->own_stream = true;
+  }
+  const gbmg_grid& g = *grid;
+  const size_t n = ls_cells(g);
+  const size_t nfx = (size_t)(g.nx + 1) * g.ny * g.nz, nfy = (size_t)g.nx * (g.ny + 1) * g.nz,
+               nfz = (size_t)g.nx * g.ny * (g.nz + 1);
+  const size_t sizes[12] = {n, n, n, n, n, n, nfx, nfx, nfy, nfy, nfz, nfz};
+  double** ptrs[12] = {&ls->phi, &ls->u, &ls->v, &ls->w, &ls->l1, &ls->l2, &ls->face[0],
+                       &ls->face[1], &ls->face[2], &ls->face[3], &ls->face[4], &ls->face[5]};
+  for (int a = 0; a < 12; ++a) {
+    if (cudaMalloc((void**)ptrs[a], sizes[a] * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      ls_free(ls);
+      if (ls->own_stream) cudaStreamDestroy(ls->stream);
+      delete ls;
+      return GBMG_OUT_OF_MEMORY;
+    }
+  }
+  *out = ls;
+  return GBMG_OK;
+}
+
+int gbmg_ls_destroy(gbmg_ls* ls) {
+  if (!ls) return GBMG_INVALID_ARG;
+  cudaSetDevice(ls->device);
+  if (ls->stream) cudaStreamSynchronize(ls->stream);
+  ls_free(ls);
+  if (ls->own_stream && ls->stream) cudaStreamDestroy(ls->stream);
+  delete ls;
+  return GBMG_OK;
+}
+
+int gbmg_ls_advect(gbmg_ls* ls, gbmg_field phi, gbmg_field u, gbmg_field v, gbmg_field w,
+                   double dt, int steps, int mem) {
+  if (!ls) return GBMG_INVALID_ARG;
+  ls->err.clear();
+  if (cudaSetDevice(ls->device) != cudaSuccess) {
+    ls->err = "cudaSetDevice failed";
+    return GBMG_CUDA_ERROR;
+  }
+  if (!(dt > 0) || steps < 0) {
+    ls->err = "dt must be > 0 and steps >= 0";
+    return GBMG_INVALID_ARG;
+  }
+  if (mem != GBMG_MEM_HOST && mem != GBMG_MEM_DEVICE) {
+    ls->err = "mem must be GBMG_MEM_HOST or GBMG_MEM_DEVICE";
+    return GBMG_INVALID_ARG;
+  }
+  const gbmg_grid& g = ls->grid;
+  const bool three = g.nz > 1;
+  int rc;
+  if ((rc = ls_in(ls, phi, mem, ls->phi)) != GBMG_OK) return rc;
+  if ((rc = ls_in(ls, u, mem, ls->u)) != GBMG_OK) return rc;
+  if ((rc = ls_in(ls, v, mem, ls->v)) != GBMG_OK) return rc;
+  if (three && (rc = ls_in(ls, w, mem, ls->w)) != GBMG_OK) return rc;
+  const LsGrid G{g.nx, g.ny, g.nz, g.dx, g.dy, g.dz};
+  const size_t n = ls_cells(g);
+  const double* vel[3] = {ls->u, ls->v, ls->w};
+  const size_t nf[3] = {(size_t)(g.nx + 1) * g.ny * g.nz, (size_t)g.nx * (g.ny + 1) * g.nz,
+                        (size_t)g.nx * g.ny * (g.nz + 1)};
+  for (int s = 0; s < steps; ++s)
+    for (int stage = 1; stage <= 3; ++stage) {
+      for (int a = 0; a < (three ? 3 : 2); ++a) {
+        k_ls_faces<<<blocks_for(nf[a]), 256, 0, ls->stream>>>(G, a, ls->phi, vel[a],
+                                                              ls->face[2 * a], ls->face[2 * a + 1]);
+        ls->launches += 1;
+      }
+      k_ls_stage<<<blocks_for(n), 256, 0, ls->stream>>>(
+          G, stage, dt, ls->face[0], ls->face[1], ls->face[2], ls->face[3], ls->face[4],
+          ls->face[5], ls->l1, ls->l2, ls->phi);
+      ls->launches += 1;
+    }
+  LS_CUDA(ls, cudaGetLastError());
+  if ((rc = ls_out(ls, ls->phi, mem, phi)) != GBMG_OK) return rc;
+  LS_CUDA(ls, cudaStreamSynchronize(ls->stream));
+  return GBMG_OK;
+}
+
+int64_t gbmg_ls_kernel_launches(gbmg_ls* ls) { return ls ? ls->launches : 0; }
+
+const char* gbmg_ls_last_error(gbmg_ls* ls) { return ls ? ls->err.c_str() : ""; }
+
+}  // extern "C"

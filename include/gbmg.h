@@ -246,6 +246,33 @@ int gbmg_set_profiling(gbmg_handle* h, int on);
  * profiling was switched on (arrays of n >= GBMG_PROF_CLASSES entries). */
 int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n);
 
+/* ---- Level-set transport (the interface solver's advection step) ---------
+ * level_set_rk3_solver ("Two phase flows/newOpenMP/2D/src/interface_solver/
+ * level_set_rk3_solver.f90:1-186"; 3D "Two phase flows/newOpenMP/3D+IBM/src/
+ * interface_solver/level_set_rk3_solver.f90:1-215"): phi_t + div(u phi) = 0
+ * with the cell-centred velocity (the reference's nvel, node_vel of the MAC
+ * faces), WENO-JS reconstruction of the split fluxes u+ phi and u- phi
+ * (wenojs_flux_split), zero-gradient ghosts (bc) and three stages of SSP-RK3,
+ * all in FP64.  A separate handle owns its device scratch (phi, u, v, w, two
+ * stage arrays and six face arrays: 12 n doubles). */
+typedef struct gbmg_ls gbmg_ls;
+
+/* device: CUDA device (-1 = current); stream: cudaStream_t (NULL = own). */
+int gbmg_ls_create(const gbmg_grid* grid, int device, void* stream, gbmg_ls** out);
+int gbmg_ls_destroy(gbmg_ls* ls);
+
+/* steps time steps of dt on phi, in place (host or device memory, the
+ * gbmg_field layout of the cell arrays above); u, v, w cell-centred (w
+ * ignored when nz = 1).  Returns after the stream has finished. */
+int gbmg_ls_advect(gbmg_ls* ls, gbmg_field phi, gbmg_field u, gbmg_field v, gbmg_field w,
+                   double dt, int steps, int mem);
+
+/* Kernels launched by this handle since creation. */
+int64_t gbmg_ls_kernel_launches(gbmg_ls* ls);
+
+/* Text of the last error on this handle ("" if none). */
+const char* gbmg_ls_last_error(gbmg_ls* ls);
+
 const char* gbmg_strerror(int status);
 
 /* Text of the last error on this handle ("" if none). */
