@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-multi", action="store_true", help="skip the 512^3 16-bubble section")
     ap.add_argument("--no-rollout", action="store_true", help="skip the 20-step rollout section")
+    ap.add_argument("--no-levelset", action="store_true", help="skip the level-set advection section")
     return ap.parse_args()
 
 
@@ -355,6 +356,46 @@ def multi_bubble_section(dev, stream, scale=1, reps=2):
     return out
 
 
+def levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h, steps=5):
+    """Level-set advection of the same 256³ case (the interface solver's
+    level_set_rk3_solver: WENO-JS split fluxes, SSP-RK3, FP64) with the cell
+    velocity of u* (node_vel), timed with CUDA events; one step of the CPU
+    oracle on all host cores beside it, and the GPU step compared with it."""
+    import torch
+
+    from fortrancfd_gb300 import LevelSet, node_velocity
+    from oracle import oracle as orc
+
+    with torch.cuda.stream(stream):
+        t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (phi_h, u_h, v_h, w_h)]
+        un, vn, wn = (x.contiguous() for x in node_velocity(t[1], t[2], t[3]))
+        phi = t[0].clone()
+        ls = LevelSet(case.shape, case.spacing, stream=stream)
+        ls.advect(phi, un, vn, wn, dt=case.dt, steps=1)  # warm-up, and the step checked below
+        torch.cuda.synchronize()
+        one = phi.cpu().numpy()
+        n0 = ls.kernel_launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ls.advect(phi, un, vn, wn, dt=case.dt, steps=steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        launches = (ls.kernel_launches - n0) // steps
+        ls.close()
+    un_h, vn_h, wn_h = (x.cpu().numpy() for x in (un, vn, wn))
+    t0 = time.perf_counter()
+    ref = orc.ls_advect(phi_h, un_h, vn_h, wn_h, case.dt, case.spacing, steps=1)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    nz, ny, nx = case.shape
+    return {"workload": f"{case.name}: level set of the {nx}x{ny}x{nz} sphere advected by the "
+                        f"cell velocity of u*, dt={case.dt}, WENO-JS + SSP-RK3, FP64",
+            "ms_per_step": ms, "cell_steps_per_s": nx * ny * nz / (ms * 1e-3),
+            "kernels_per_step": launches,
+            "cpu_oracle_ms_per_step": cpu_ms, "cpu_threads": orc.num_threads(),
+            "gpu_equals_oracle": bool(np.array_equal(one, ref))}
+
+
 def rollout_section(dev, stream, scale=1, steps=20):
     """The 20-step differentiable projection rollout (128x128x256, 4 bubbles):
     forward (20 mixed solves) and backward (20 adjoint solves and the
@@ -617,6 +658,13 @@ def run_ours(args):
         except Exception as exc:
             roll = {"error": f"{type(exc).__name__}: {exc}"}
 
+    lset = None
+    if not args.no_levelset:
+        try:
+            lset = levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h)
+        except Exception as exc:
+            lset = {"error": f"{type(exc).__name__}: {exc}"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
@@ -639,7 +687,7 @@ def run_ours(args):
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "adjoint": adj, "multi_bubble": multi,
-                "rollout": roll}
+                "rollout": roll, "levelset": lset}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
         print(json.dumps(line), flush=True)
