@@ -1132,3 +1132,179 @@ void or_ls_advect(const or_grid* g, double* phi, const double* u, const double* 
   free(l2);
   free(l3);
 }
+
+/* ------------------------------------------------------------------------- */
+/* Level-set redistancing, level_set_rk3_redis (NO2 src/interface_solver/     */
+/* level_set_rk3_redis.f90:1-361; NO3 :1-420 for nz > 1).  phi_tau +          */
+/* S (|grad phi| - 1) = 0 in pseudo time rdt with the sign S fixed at the    */
+/* start (ls_funs: S = 2H - 1; btn = 0, level_set_redis_stable: S = phi and  */
+/* phi is first divided by max |grad phi|), the Godunov gradient of WENO-JS  */
+/* one-sided derivatives of the backward differences (level_set_redis_       */
+/* gradient, wenojs_flux with EPS = 1e-10), and for btn = 1 the mass-        */
+/* preserving correction lambda (level_set_redis_lambda: 2D lam = delta,     */
+/* weight 16 over a 3x3 block; 3D lam = (2(1 - rho_12)H + rho_12) delta,     */
+/* weight 51 over 3x3x3).  Three SSP-RK3 stages per iteration; stop when    */
+/* the time passes 3 dx (btn = 1) or 1.5 x the largest extent (btn = 0), or */
+/* when max |change| <= 1e-8 (2D) / 1e-5 (3D).                               */
+/* ------------------------------------------------------------------------- */
+static void or_ls_funs1(double phi, double ls_wid, double* heavy, double* delta, double* sgn) {
+  const double eps = 1.0e-12, pi = acos(-1.0);
+  const double x = phi / ls_wid;
+  double h, hp;
+  if (x > 1.0 - eps) {
+    h = 1.0;
+    hp = 0.0;
+  } else if (x < -1.0 + eps) {
+    h = 0.0;
+    hp = 0.0;
+  } else {
+    h = 0.5 * ((1.0 + x) + sin(pi * x) / pi);
+    hp = 0.5 * (1.0 + cos(pi * x)) / ls_wid;
+  }
+  h = h < 1.0 ? h : 1.0;
+  h = h > 0.0 ? h : 0.0;
+  *heavy = h;
+  *delta = hp;
+  *sgn = 2.0 * h - 1.0;
+}
+
+/* backward difference of phi at cell m of a line (zero-gradient ghosts) */
+static inline double ls_nrm(const double* phi, size_t base, size_t stride, int m, int n, double h) {
+  const int c = ls_clamp(m, n);
+  const int cm = c > 0 ? c - 1 : 0;
+  return (phi[base + (size_t)c * stride] - phi[base + (size_t)cm * stride]) / h;
+}
+
+static inline double ls_max(double a, double b) { return a > b ? a : b; }
+static inline double ls_min(double a, double b) { return a < b ? a : b; }
+
+/* |grad phi| per cell, Godunov upwinding by the sign s (level_set_redis_gradient) */
+void or_ls_gradient(const or_grid* g, const double* phi, const double* s, double* grad) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const int dims[3] = {nx, ny, nz};
+  const size_t strides[3] = {1, (size_t)nx, (size_t)nx * ny};
+  const double h[3] = {g->dx, g->dy, g->dz};
+  const int naxes = nz > 1 ? 3 : 2;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int idx[3] = {i, j, k};
+        const size_t q = ((size_t)k * ny + j) * nx + i;
+        double sum = 0.0;
+        for (int a = 0; a < naxes; ++a) {
+          const int n = dims[a], c = idx[a];
+          const size_t base = q - (size_t)c * strides[a];
+          double f[6];
+          for (int m = 0; m < 6; ++m) f[m] = ls_nrm(phi, base, strides[a], c - 2 + m, n, h[a]);
+          const double s1 = or_weno_right(f[1], f[2], f[3], f[4], f[5], 1.0e-10);
+          const double s2 = or_weno_left(f[0], f[1], f[2], f[3], f[4], 1.0e-10);
+          const double pm = -ls_min(s1, 0.0), pp = ls_max(s1, 0.0);
+          const double mm = -ls_min(s2, 0.0), mp = ls_max(s2, 0.0);
+          const double t = s[q] >= 0.0 ? ls_max(pm, mp) : ls_max(pp, mm);
+          sum = a == 0 ? t * t : sum + t * t;
+        }
+        grad[q] = sqrt(sum);
+      }
+}
+
+/* the mass-preserving correction s1 (level_set_redis_lambda, btn = 1) */
+static void or_ls_lambda(const or_grid* g, const double* phi, const double* s, const double* grad,
+                         double ls_wid, double rho_12, double* s2, double* s3, double* s1) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t n = cells_of(nx, ny, nz);
+  const int three = nz > 1;
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < n; ++q) {
+    double hv, dl, sg;
+    or_ls_funs1(phi[q], ls_wid, &hv, &dl, &sg);
+    const double lam = three ? (2.0 * (1.0 - rho_12) * hv + rho_12) * dl : dl;
+    s2[q] = lam * s[q] * (grad[q] - 1.0);
+    s3[q] = grad[q] * dl * lam;
+  }
+  const double wgt = three ? 51.0 : 16.0;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const size_t q = ((size_t)k * ny + j) * nx + i;
+        double a = wgt * s2[q], b = wgt * s3[q];
+        for (int kk = three ? -1 : 0; kk <= (three ? 1 : 0); ++kk)
+          for (int jj = -1; jj <= 1; ++jj)
+            for (int ii = -1; ii <= 1; ++ii) {
+              const size_t r = ((size_t)ls_clamp(k + kk, nz) * ny + ls_clamp(j + jj, ny)) * nx +
+                               ls_clamp(i + ii, nx);
+              a = a + s2[r];
+              b = b + s3[r];
+            }
+        double hv, dl, sg;
+        or_ls_funs1(phi[q], ls_wid, &hv, &dl, &sg);
+        s1[q] = fabs(b) > 1.0e-12 ? a / b * dl : 0.0;
+      }
+}
+
+int or_ls_redistance(const or_grid* g, double* phi, double ls_wid, double rdt, double rho_12,
+                     int btn, int max_iter, double* last_error) {
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const size_t n = cells_of(nx, ny, nz);
+  const int three = nz > 1;
+  double* s = (double*)malloc(n * sizeof(double));
+  double* grad = (double*)malloc(n * sizeof(double));
+  double* s1 = (double*)calloc(n, sizeof(double));
+  double* s2 = (double*)malloc(n * sizeof(double));
+  double* s3 = (double*)malloc(n * sizeof(double));
+  double* l1 = (double*)malloc(n * sizeof(double));
+  double* l2 = (double*)malloc(n * sizeof(double));
+  double* tmp = (double*)malloc(n * sizeof(double));
+  /* level_set_redis_init */
+  for (size_t q = 0; q < n; ++q) {
+    double hv, dl;
+    or_ls_funs1(phi[q], ls_wid, &hv, &dl, &s[q]);
+  }
+  if (btn == 0) { /* level_set_redis_stable */
+    for (size_t q = 0; q < n; ++q) s[q] = phi[q];
+    or_ls_gradient(g, phi, s, grad);
+    double gm = 0.0;
+    for (size_t q = 0; q < n; ++q) gm = ls_max(gm, grad[q]);
+    for (size_t q = 0; q < n; ++q) phi[q] = phi[q] / gm;
+  }
+  const double ext = three ? ls_max(ls_max(nx * g->dx, ny * g->dy), nz * g->dz)
+                           : ls_max(nx * g->dx, ny * g->dy);
+  const double timestop = btn == 0 ? 1.5 * ext : 3.0 * g->dx;
+  const double tol = three ? 1.0e-5 : 1.0e-8;
+  double time = 0.0, error = 0.0;
+  int iter = 0;
+  while (iter < max_iter) {
+    ++iter;
+    time = time + rdt;
+    memcpy(tmp, phi, n * sizeof(double));
+    for (int stage = 1; stage <= 3; ++stage) {
+      or_ls_gradient(g, phi, s, grad);
+      if (btn == 0) {
+        memset(s1, 0, n * sizeof(double));
+      } else {
+        or_ls_lambda(g, phi, s, grad, ls_wid, rho_12, s2, s3, s1);
+      }
+      for (size_t q = 0; q < n; ++q) {
+        const double l = (s[q] - s1[q]) * grad[q] - s[q];
+        double src;
+        if (stage == 1) {
+          l1[q] = l;
+          src = l;
+        } else if (stage == 2) {
+          l2[q] = l;
+          src = (-3.0 * l1[q] + l) / 4.0;
+        } else {
+          src = ((-l1[q] - l2[q]) + 8.0 * l) / 12.0;
+        }
+        phi[q] = phi[q] - rdt * src;
+      }
+    }
+    error = 0.0;
+    for (size_t q = 0; q < n; ++q) error = ls_max(error, fabs(tmp[q] - phi[q]));
+    if (time > timestop || error <= tol) break;
+  }
+  if (last_error) *last_error = error;
+  free(s); free(grad); free(s1); free(s2); free(s3); free(l1); free(l2); free(tmp);
+  return iter;
+}

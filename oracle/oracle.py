@@ -76,6 +76,10 @@ def lib():
                                  C.c_double, _D, _D]
         L.or_ls_source.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, _D]
         L.or_ls_advect.argtypes = [C.POINTER(Grid), _D, _D, _D, _D, C.c_double, C.c_int]
+        L.or_ls_gradient.argtypes = [C.POINTER(Grid), _D, _D, _D]
+        L.or_ls_redistance.argtypes = [C.POINTER(Grid), _D, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, C.c_int, _D]
+        L.or_ls_redistance.restype = C.c_int
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -268,6 +272,25 @@ def ls_advect(phi, u, v, w, dt, spacing, steps=1):
     lib().or_ls_advect(C.byref(g), _p(phi), _p(np.ascontiguousarray(u, np.float64)),
                        _p(np.ascontiguousarray(v, np.float64)), _p(w_), float(dt), int(steps))
     return phi
+
+
+def ls_gradient(phi, sign, spacing):
+    """|grad phi| of level_set_redis_gradient (Godunov upwinding by sign)."""
+    phi = np.ascontiguousarray(phi, np.float64)
+    g = grid(phi.shape, spacing)
+    out = np.empty_like(phi)
+    lib().or_ls_gradient(C.byref(g), _p(phi), _p(np.ascontiguousarray(sign, np.float64)), _p(out))
+    return out
+
+
+def ls_redistance(phi, ls_wid, rdt, spacing, rho_12=1e-3, btn=1, max_iter=100000):
+    """level_set_rk3_redis(btn); returns (phi, iterations, last max change)."""
+    phi = np.array(phi, np.float64, order="C", copy=True)
+    g = grid(phi.shape, spacing)
+    err = C.c_double(0.0)
+    it = lib().or_ls_redistance(C.byref(g), _p(phi), float(ls_wid), float(rdt), float(rho_12),
+                                int(btn), int(max_iter), C.byref(err))
+    return phi, it, err.value
 
 
 def set_threads(n):

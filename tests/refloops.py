@@ -440,6 +440,11 @@ def ppe_mg_split_correction(rho, p, p_hat, u, v, w, rho_12, dt, dx, dy, dz):
 LS_GHC = 3
 
 
+def _sq(x):
+    """x**2 as the compiled reference evaluates it: one rounded product."""
+    return x * x
+
+
 def _bc3(a):
     """bc with ghc ghost layers: copy the first/last interior cell outwards."""
     g = LS_GHC
@@ -464,12 +469,12 @@ def _wenojs_flux_split(f, g, nn):
     fp = [0.0] * len(f)
     gm = [0.0] * len(g)
     for i in range(2, nn + 3):
-        b1 = 13.0 * (g[i - 2] - 2.0 * g[i - 1] + g[i]) ** 2 + 3.0 * (g[i - 2] - 4.0 * g[i - 1] + 3.0 * g[i]) ** 2
-        b2 = 13.0 * (g[i - 1] - 2.0 * g[i] + g[i + 1]) ** 2 + 3.0 * (g[i - 1] - g[i + 1]) ** 2
-        b3 = 13.0 * (g[i] - 2.0 * g[i + 1] + g[i + 2]) ** 2 + 3.0 * (3.0 * g[i] - 4.0 * g[i + 1] + g[i + 2]) ** 2
-        a1 = 1.0 / (eps + b1) ** 2
-        a2 = 6.0 / (eps + b2) ** 2
-        a3 = 3.0 / (eps + b3) ** 2
+        b1 = 13.0 * _sq(g[i - 2] - 2.0 * g[i - 1] + g[i]) + 3.0 * _sq(g[i - 2] - 4.0 * g[i - 1] + 3.0 * g[i])
+        b2 = 13.0 * _sq(g[i - 1] - 2.0 * g[i] + g[i + 1]) + 3.0 * _sq(g[i - 1] - g[i + 1])
+        b3 = 13.0 * _sq(g[i] - 2.0 * g[i + 1] + g[i + 2]) + 3.0 * _sq(3.0 * g[i] - 4.0 * g[i + 1] + g[i + 2])
+        a1 = 1.0 / _sq(eps + b1)
+        a2 = 6.0 / _sq(eps + b2)
+        a3 = 3.0 / _sq(eps + b3)
         w1 = a1 / (a1 + a2 + a3)
         w2 = a2 / (a1 + a2 + a3)
         w3 = a3 / (a1 + a2 + a3)
@@ -477,12 +482,12 @@ def _wenojs_flux_split(f, g, nn):
                  + (11.0 * w1 + 5.0 * w2 + 2.0 * w3) / 6.0 * g[i]
                  + (2.0 * w2 + 5.0 * w3) / 6.0 * g[i + 1] - w3 / 6.0 * g[i + 2])
     for i in range(2, nn + 3):
-        b3 = 13.0 * (f[i - 1] - 2.0 * f[i] + f[i + 1]) ** 2 + 3.0 * (f[i - 1] - 4.0 * f[i] + 3.0 * f[i + 1]) ** 2
-        b2 = 13.0 * (f[i] - 2.0 * f[i + 1] + f[i + 2]) ** 2 + 3.0 * (f[i] - f[i + 2]) ** 2
-        b1 = 13.0 * (f[i + 1] - 2.0 * f[i + 2] + f[i + 3]) ** 2 + 3.0 * (3.0 * f[i + 1] - 4.0 * f[i + 2] + f[i + 3]) ** 2
-        a1 = 1.0 / (eps + b1) ** 2
-        a2 = 6.0 / (eps + b2) ** 2
-        a3 = 3.0 / (eps + b3) ** 2
+        b3 = 13.0 * _sq(f[i - 1] - 2.0 * f[i] + f[i + 1]) + 3.0 * _sq(f[i - 1] - 4.0 * f[i] + 3.0 * f[i + 1])
+        b2 = 13.0 * _sq(f[i] - 2.0 * f[i + 1] + f[i + 2]) + 3.0 * _sq(f[i] - f[i + 2])
+        b1 = 13.0 * _sq(f[i + 1] - 2.0 * f[i + 2] + f[i + 3]) + 3.0 * _sq(3.0 * f[i + 1] - 4.0 * f[i + 2] + f[i + 3])
+        a1 = 1.0 / _sq(eps + b1)
+        a2 = 6.0 / _sq(eps + b2)
+        a3 = 3.0 / _sq(eps + b3)
         w1 = a1 / (a1 + a2 + a3)
         w2 = a2 / (a1 + a2 + a3)
         w3 = a3 / (a1 + a2 + a3)
@@ -560,3 +565,188 @@ def level_set_rk3_solver(phi, u, v, w, dt, dx, dy, dz, steps=1):
                                           + ((-l1 - l2 + 8.0 * l3) / 12.0) * dt)
         _bc3(P)
     return np.ascontiguousarray(np.transpose(P[g:g + nx, g:g + ny, g:g + nz], (2, 1, 0)))
+
+
+# --- level-set redistancing ---------------------------------------------------------
+# level_set_rk3_redis / level_set_redis_init / level_set_redis_stable /
+# level_set_rk3_redis_solver / level_set_redis_gradient / wenojs_flux /
+# level_set_redis_lambda: "Two phase flows/newOpenMP/2D/src/interface_solver/
+# level_set_rk3_redis.f90:1-361" (3D: "Two phase flows/newOpenMP/3D+IBM/src/
+# interface_solver/level_set_rk3_redis.f90"); ls_funs: ".../3D+IBM/src/
+# interface_solver/others.f90:1-37".  Fortran (i, j, k) arrays with ghc = 3.
+def _ls_funs(P, ls_wid):
+    eps = 1.0e-12
+    pi = math.acos(-1.0)
+    H = np.zeros_like(P)
+    D = np.zeros_like(P)
+    S = np.zeros_like(P)
+    for idx in np.ndindex(P.shape):
+        x = P[idx] / ls_wid
+        if x > 1.0 - eps:
+            heavy, hp = 1.0, 0.0
+        elif x < -1.0 + eps:
+            heavy, hp = 0.0, 0.0
+        else:
+            heavy = 0.5 * (1.0 + x + math.sin(pi * x) / pi)
+            hp = 0.5 * (1.0 + math.cos(pi * x)) / ls_wid
+        heavy = max(min(heavy, 1.0), 0.0)
+        H[idx], D[idx], S[idx] = heavy, hp, 2.0 * heavy - 1.0
+    return H, D, S
+
+
+def _wenojs_flux(f, nn):
+    """One line: (fp, fm) over i = is-1 .. ie (numpy 2 .. nn+2), EPS = 1e-10."""
+    eps = 1.0e-10
+    fp = [0.0] * len(f)
+    fm = [0.0] * len(f)
+    for i in range(2, nn + 3):
+        b1 = 13.0 * _sq(f[i - 2] - 2.0 * f[i - 1] + f[i]) + 3.0 * _sq(f[i - 2] - 4.0 * f[i - 1] + 3.0 * f[i])
+        b2 = 13.0 * _sq(f[i - 1] - 2.0 * f[i] + f[i + 1]) + 3.0 * _sq(f[i - 1] - f[i + 1])
+        b3 = 13.0 * _sq(f[i] - 2.0 * f[i + 1] + f[i + 2]) + 3.0 * _sq(3.0 * f[i] - 4.0 * f[i + 1] + f[i + 2])
+        a1 = 1.0 / _sq(eps + b1)
+        a2 = 6.0 / _sq(eps + b2)
+        a3 = 3.0 / _sq(eps + b3)
+        w1 = a1 / (a1 + a2 + a3)
+        w2 = a2 / (a1 + a2 + a3)
+        w3 = a3 / (a1 + a2 + a3)
+        fm[i] = (w1 / 3.0 * f[i - 2] - (7.0 * w1 + w2) / 6.0 * f[i - 1]
+                 + (11.0 * w1 + 5.0 * w2 + 2.0 * w3) / 6.0 * f[i]
+                 + (2.0 * w2 + 5.0 * w3) / 6.0 * f[i + 1] - w3 / 6.0 * f[i + 2])
+        b3 = 13.0 * _sq(f[i - 1] - 2.0 * f[i] + f[i + 1]) + 3.0 * _sq(f[i - 1] - 4.0 * f[i] + 3.0 * f[i + 1])
+        b2 = 13.0 * _sq(f[i] - 2.0 * f[i + 1] + f[i + 2]) + 3.0 * _sq(f[i] - f[i + 2])
+        b1 = 13.0 * _sq(f[i + 1] - 2.0 * f[i + 2] + f[i + 3]) + 3.0 * _sq(3.0 * f[i + 1] - 4.0 * f[i + 2] + f[i + 3])
+        a1 = 1.0 / _sq(eps + b1)
+        a2 = 6.0 / _sq(eps + b2)
+        a3 = 3.0 / _sq(eps + b3)
+        w1 = a1 / (a1 + a2 + a3)
+        w2 = a2 / (a1 + a2 + a3)
+        w3 = a3 / (a1 + a2 + a3)
+        fp[i] = (w3 * (-f[i - 1] + 5.0 * f[i] + 2.0 * f[i + 1]) / 6.0
+                 + w2 * (2.0 * f[i] + 5.0 * f[i + 1] - f[i + 2]) / 6.0
+                 + w1 * (11.0 * f[i + 1] - 7.0 * f[i + 2] + 2.0 * f[i + 3]) / 6.0)
+    return fp, fm
+
+
+def level_set_rk3_redis(phi, ls_wid, rdt, dx, dy, dz, rho_12=1e-3, btn=1, max_iter=100000):
+    """phi: (nz, ny, nx).  Returns (phi, iterations, last error)."""
+    nz, ny, nx = phi.shape
+    three = nz > 1
+    g = LS_GHC
+    n = (nx, ny, nz)
+    h = (dx, dy, dz)
+    axes = 3 if three else 2
+    P = np.zeros((nx + 2 * g, ny + 2 * g, nz + 2 * g))
+    P[g:g + nx, g:g + ny, g:g + nz] = np.transpose(phi, (2, 1, 0))
+    _bc3(P)
+    inner = (slice(g, g + nx), slice(g, g + ny), slice(g, g + nz))
+
+    def gradient(sign_tmp):
+        S1, S2 = [], []
+        for a in range(axes):
+            N = np.zeros_like(P)
+            for i in range(nx):
+                for j in range(ny):
+                    for k in range(nz):
+                        c = [g + i, g + j, g + k]
+                        m = list(c)
+                        m[a] -= 1
+                        N[tuple(c)] = (P[tuple(c)] - P[tuple(m)]) / h[a]
+            _bc3(N)
+            s1 = np.zeros_like(P)
+            s2 = np.zeros_like(P)
+            others = [b for b in range(3) if b != a]
+            for p0 in range(n[others[0]]):
+                for p1 in range(n[others[1]]):
+                    idx = [0, 0, 0]
+                    idx[others[0]] = g + p0
+                    idx[others[1]] = g + p1
+                    sl = list(idx)
+                    sl[a] = slice(None)
+                    fp, fm = _wenojs_flux(list(N[tuple(sl)]), n[a])
+                    s1[tuple(sl)] = fp
+                    s2[tuple(sl)] = fm
+            S1.append(s1)
+            S2.append(s2)
+        G = np.zeros_like(P)
+        for i in range(nx):
+            for j in range(ny):
+                for k in range(nz):
+                    I = (g + i, g + j, g + k)
+                    tot = 0.0
+                    for a in range(axes):
+                        pm = -min(S1[a][I], 0.0)
+                        pp = max(S1[a][I], 0.0)
+                        mm = -min(S2[a][I], 0.0)
+                        mp = max(S2[a][I], 0.0)
+                        t = max(pm, mp) if sign_tmp[I] >= 0.0 else max(pp, mm)
+                        tot = _sq(t) if a == 0 else tot + _sq(t)
+                    G[I] = math.sqrt(tot)
+        return G
+
+    def lam_s1(sign_tmp, G):
+        if btn == 0:
+            return np.zeros_like(P)
+        H, D, _ = _ls_funs(P, ls_wid)
+        s2 = np.zeros_like(P)
+        s3 = np.zeros_like(P)
+        for I in np.ndindex(nx, ny, nz):
+            J = (g + I[0], g + I[1], g + I[2])
+            lam = (2.0 * (1.0 - rho_12) * H[J] + rho_12) * D[J] if three else D[J]
+            s2[J] = lam * sign_tmp[J] * (G[J] - 1.0)
+            s3[J] = G[J] * D[J] * lam
+        _bc3(s2)
+        _bc3(s3)
+        out = np.zeros_like(P)
+        wgt = 51.0 if three else 16.0
+        kr = (-1, 0, 1) if three else (0,)
+        for I in np.ndindex(nx, ny, nz):
+            J = (g + I[0], g + I[1], g + I[2])
+            a = wgt * s2[J]
+            b = wgt * s3[J]
+            for kk in kr:
+                for jj in (-1, 0, 1):
+                    for ii in (-1, 0, 1):
+                        K = (J[0] + ii, J[1] + jj, J[2] + kk)
+                        a = a + s2[K]
+                        b = b + s3[K]
+            out[J] = a / b * D[J] if abs(b) > 1.0e-12 else 0.0
+        return out
+
+    _, _, sign_tmp = _ls_funs(P, ls_wid)
+    if btn == 0:
+        sign_tmp = P.copy()
+        G = gradient(sign_tmp)
+        gmax = 0.0
+        for I in np.ndindex(nx, ny, nz):
+            gmax = max(gmax, G[g + I[0], g + I[1], g + I[2]])
+        P[inner] = P[inner] / gmax
+        _bc3(P)
+    ext = max(nx * dx, ny * dy, nz * dz) if three else max(nx * dx, ny * dy)
+    timestop = 1.5 * ext if btn == 0 else 3.0 * dx
+    tol = 1.0e-5 if three else 1.0e-8
+    it = 0
+    time = 0.0
+    error = 0.0
+    while it < max_iter:
+        it += 1
+        time = time + rdt
+        tmp = P[inner].copy()
+        l1 = l2 = None
+        for stage in (1, 2, 3):
+            G = gradient(sign_tmp)
+            S1 = lam_s1(sign_tmp, G)
+            L = (sign_tmp[inner] - S1[inner]) * G[inner] - sign_tmp[inner]
+            if stage == 1:
+                l1 = L
+                src = L
+            elif stage == 2:
+                l2 = L
+                src = (-3.0 * l1 + L) / 4.0
+            else:
+                src = (-l1 - l2 + 8.0 * L) / 12.0
+            P[inner] = P[inner] - rdt * src
+            _bc3(P)
+        error = float(np.abs(tmp - P[inner]).max())
+        if time > timestop or error <= tol:
+            break
+    return np.ascontiguousarray(np.transpose(P[inner], (2, 1, 0))), it, error
