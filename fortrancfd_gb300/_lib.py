@@ -31,8 +31,8 @@ EXPORTS = (
     "gbmg_div_stats", "gbmg_level_coef", "gbmg_level_dims", "gbmg_kernel_launches",
     "gbmg_strerror", "gbmg_last_error", "gbmg_set_profiling", "gbmg_profile", "gbmg_adjoint",
     "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split",
-    "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_kernel_launches",
-    "gbmg_ls_last_error",
+    "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
+    "gbmg_ls_kernel_launches", "gbmg_ls_last_error",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -126,7 +126,9 @@ def load(build_if_missing: bool = True):
         L.gbmg_ls_kernel_launches.restype = C.c_int64
         L.gbmg_ls_last_error.argtypes = [H]
         L.gbmg_ls_last_error.restype = C.c_char_p
-        for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect"):
+        L.gbmg_ls_redistance.argtypes = [H, Field, C.c_double, C.c_double, C.c_double, C.c_int,
+                                         C.c_int, C.c_int, P(C.c_int32), P(C.c_double)]
+        for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance"):
             getattr(L, name).restype = C.c_int
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",

@@ -18,6 +18,7 @@
 // the FP64 oracle bit for bit.  GB300 runs FP64 at about 1/57 of its FP32
 // rate and a face costs two reconstructions of about 20 divisions each, so
 // these kernels are bound by the FP64 pipe, not by memory.
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -156,6 +157,183 @@ __global__ void __launch_bounds__(256) k_ls_stage(LsGrid g, int stage, double dt
   phi[q] = add(phi[q], mul(s, dt));
 }
 
+// ---- redistancing: level_set_rk3_redis ("Two phase flows/newOpenMP/2D/src/
+// interface_solver/level_set_rk3_redis.f90:1-361"; 3D "Two phase flows/
+// newOpenMP/3D+IBM/src/interface_solver/level_set_rk3_redis.f90") ----------
+constexpr double kPi = 3.141592653589793;  // acos(-1) in double
+
+// ls_funs ("Two phase flows/newOpenMP/3D+IBM/src/interface_solver/
+// others.f90:1-37"): smoothed Heaviside, its derivative and the sign 2H - 1
+__device__ __forceinline__ void ls_funs1(double phi, double ls_wid, double& heavy, double& delta,
+                                         double& sgn) {
+  const double eps = 1.0e-12;
+  const double x = dvd(phi, ls_wid);
+  double h, hp;
+  if (x > 1.0 - eps) {
+    h = 1.0;
+    hp = 0.0;
+  } else if (x < -1.0 + eps) {
+    h = 0.0;
+    hp = 0.0;
+  } else {
+    h = mul(0.5, add(add(1.0, x), dvd(sin(mul(kPi, x)), kPi)));
+    hp = dvd(mul(0.5, add(1.0, cos(mul(kPi, x)))), ls_wid);
+  }
+  h = h < 1.0 ? h : 1.0;
+  h = h > 0.0 ? h : 0.0;
+  heavy = h;
+  delta = hp;
+  sgn = sub(mul(2.0, h), 1.0);
+}
+
+// s = the sign held fixed through the call: 2H - 1, or phi itself for the
+// first redistancing (level_set_redis_stable, btn = 0)
+__global__ void __launch_bounds__(256) k_ls_sign(size_t n, const double* __restrict__ phi,
+                                                 double ls_wid, int btn, double* __restrict__ s) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (btn == 0) {
+    s[q] = phi[q];
+  } else {
+    double hv, dl, sg;
+    ls_funs1(phi[q], ls_wid, hv, dl, sg);
+    s[q] = sg;
+  }
+}
+
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+
+// |grad phi| by Godunov upwinding on the sign s (level_set_redis_gradient):
+// the WENO-JS one-sided values (EPS = 1e-10) of the backward differences
+// (phi_i - phi_{i-1})/h, zero-gradient ghosts by index clamping
+__global__ void __launch_bounds__(256) k_ls_grad(LsGrid g, const double* __restrict__ phi,
+                                                 const double* __restrict__ s,
+                                                 double* __restrict__ grad) {
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int i = (int)(q % g.nx);
+  const size_t r = q / g.nx;
+  const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+  const int naxes = g.nz > 1 ? 3 : 2;
+  const bool pos = s[q] >= 0.0;
+  double sum = 0.0;
+  for (int a = 0; a < naxes; ++a) {
+    const int n_a = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+    const int c = a == 0 ? i : (a == 1 ? j : k);
+    const size_t stride = a == 0 ? 1 : (a == 1 ? (size_t)g.nx : (size_t)g.nx * g.ny);
+    const double h = a == 0 ? g.dx : (a == 1 ? g.dy : g.dz);
+    const size_t base = q - (size_t)c * stride;
+    double f[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int cc = clampi(c - 2 + m, n_a);
+      const int cm = cc > 0 ? cc - 1 : 0;
+      f[m] = dvd(sub(phi[base + (size_t)cc * stride], phi[base + (size_t)cm * stride]), h);
+    }
+    const double s1 = weno_right(f[1], f[2], f[3], f[4], f[5], 1.0e-10);
+    const double s2 = weno_left(f[0], f[1], f[2], f[3], f[4], 1.0e-10);
+    const double pm = -dmin(s1, 0.0), pp = dmax(s1, 0.0);
+    const double mm = -dmin(s2, 0.0), mp = dmax(s2, 0.0);
+    const double t = pos ? dmax(pm, mp) : dmax(pp, mm);
+    sum = a == 0 ? mul(t, t) : add(sum, mul(t, t));
+  }
+  grad[q] = __dsqrt_rn(sum);
+}
+
+// s2 = lam s (|grad| - 1), s3 = |grad| delta lam (level_set_redis_lambda)
+__global__ void __launch_bounds__(256) k_ls_lambda(size_t n, int three, double ls_wid,
+                                                   double rho12, const double* __restrict__ phi,
+                                                   const double* __restrict__ s,
+                                                   const double* __restrict__ grad,
+                                                   double* __restrict__ s2,
+                                                   double* __restrict__ s3) {
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double hv, dl, sg;
+  ls_funs1(phi[q], ls_wid, hv, dl, sg);
+  const double lam = three ? mul(add(mul(mul(2.0, sub(1.0, rho12)), hv), rho12), dl) : dl;
+  s2[q] = mul(mul(lam, s[q]), sub(grad[q], 1.0));
+  s3[q] = mul(mul(grad[q], dl), lam);
+}
+
+// One pseudo-time stage: s1 = the correction (block sums of s2 and s3 with
+// weight 16 (2D) or 51 (3D) on the cell, btn = 1; 0 for btn = 0),
+// l = (s - s1)|grad| - s, phi -= rdt * (the stage's combination of l1..l3)
+__global__ void __launch_bounds__(256) k_ls_redis_stage(LsGrid g, int stage, int btn, double rdt,
+                                                        double ls_wid,
+                                                        const double* __restrict__ s,
+                                                        const double* __restrict__ grad,
+                                                        const double* __restrict__ s2,
+                                                        const double* __restrict__ s3,
+                                                        double* l1, double* l2, double* phi) {
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double s1 = 0.0;
+  if (btn != 0) {
+    const int i = (int)(q % g.nx);
+    const size_t r = q / g.nx;
+    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const bool three = g.nz > 1;
+    const double wgt = three ? 51.0 : 16.0;
+    double a = mul(wgt, s2[q]), b = mul(wgt, s3[q]);
+    const int k0 = three ? -1 : 0, k1 = three ? 1 : 0;
+    for (int kk = k0; kk <= k1; ++kk)
+      for (int jj = -1; jj <= 1; ++jj)
+        for (int ii = -1; ii <= 1; ++ii) {
+          const size_t rr = ((size_t)clampi(k + kk, g.nz) * g.ny + clampi(j + jj, g.ny)) * g.nx +
+                            clampi(i + ii, g.nx);
+          a = add(a, s2[rr]);
+          b = add(b, s3[rr]);
+        }
+    double hv, dl, sg;
+    ls_funs1(phi[q], ls_wid, hv, dl, sg);
+    s1 = fabs(b) > 1.0e-12 ? mul(dvd(a, b), dl) : 0.0;
+  }
+  const double l = sub(mul(sub(s[q], s1), grad[q]), s[q]);
+  double src;
+  if (stage == 1) {
+    l1[q] = l;
+    src = l;
+  } else if (stage == 2) {
+    l2[q] = l;
+    src = dvd(add(mul(-3.0, l1[q]), l), 4.0);
+  } else {
+    src = dvd(add(sub(-l1[q], l2[q]), mul(8.0, l)), 12.0);
+  }
+  phi[q] = sub(phi[q], mul(rdt, src));
+}
+
+// *out = max over cells of |a - b| (b == nullptr: max of a, a >= 0); the
+// maximum of non-negative doubles is the maximum of their bit patterns
+__global__ void __launch_bounds__(256) k_ls_maxabs(size_t n, const double* __restrict__ a,
+                                                   const double* __restrict__ b,
+                                                   unsigned long long* out) {
+  double m = 0.0;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const double v = b ? fabs(sub(a[q], b[q])) : a[q];
+    m = v > m ? v : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = dmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = dmax(m, ws[w]);
+    atomicMax(out, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+__global__ void k_ls_scale(size_t n, double* phi, const unsigned long long* gmax) {
+  const double gm = __longlong_as_double((long long)*gmax);
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) phi[q] = dvd(phi[q], gm);
+}
+
 inline unsigned blocks_for(size_t n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
@@ -171,6 +349,8 @@ struct gbmg_ls {
   bool own_stream = false;
   double *phi = nullptr, *u = nullptr, *v = nullptr, *w = nullptr, *l1 = nullptr, *l2 = nullptr;
   double* face[6] = {};
+  unsigned long long* red = nullptr;  // one max-reduction slot
+  unsigned long long* host_red = nullptr;
   int64_t launches = 0;
   std::string err;
 };
@@ -198,6 +378,10 @@ void ls_free(gbmg_ls* ls) {
       cudaFree(*p);
       *p = nullptr;
     }
+  if (ls->red) cudaFree(ls->red);
+  if (ls->host_red) cudaFreeHost(ls->host_red);
+  ls->red = nullptr;
+  ls->host_red = nullptr;
 }
 
 // host or device field (strided, x contiguous) -> dense device array
@@ -294,6 +478,14 @@ int gbmg_ls_create(const gbmg_grid* grid, int device, void* stream, gbmg_ls** ou
       return GBMG_OUT_OF_MEMORY;
     }
   }
+  if (cudaMalloc((void**)&ls->red, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost((void**)&ls->host_red, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    ls_free(ls);
+    if (ls->own_stream) cudaStreamDestroy(ls->stream);
+    delete ls;
+    return GBMG_OUT_OF_MEMORY;
+  }
   *out = ls;
   return GBMG_OK;
 }
@@ -351,6 +543,102 @@ int gbmg_ls_advect(gbmg_ls* ls, gbmg_field phi, gbmg_field u, gbmg_field v, gbmg
   LS_CUDA(ls, cudaGetLastError());
   if ((rc = ls_out(ls, ls->phi, mem, phi)) != GBMG_OK) return rc;
   LS_CUDA(ls, cudaStreamSynchronize(ls->stream));
+  return GBMG_OK;
+}
+
+namespace {
+// max over cells of |a - b| (or of a), read back to the host
+int ls_max(gbmg_ls* ls, const double* a, const double* b, double* out) {
+  const size_t n = ls_cells(ls->grid);
+  LS_CUDA(ls, cudaMemsetAsync(ls->red, 0, sizeof(unsigned long long), ls->stream));
+  unsigned blocks = blocks_for(n);
+  if (blocks > 1024) blocks = 1024;
+  k_ls_maxabs<<<blocks, 256, 0, ls->stream>>>(n, a, b, ls->red);
+  ls->launches += 1;
+  LS_CUDA(ls, cudaGetLastError());
+  LS_CUDA(ls, cudaMemcpyAsync(ls->host_red, ls->red, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, ls->stream));
+  LS_CUDA(ls, cudaStreamSynchronize(ls->stream));
+  long long bits = (long long)*ls->host_red;
+  std::memcpy(out, &bits, sizeof(double));
+  return GBMG_OK;
+}
+}  // namespace
+
+int gbmg_ls_redistance(gbmg_ls* ls, gbmg_field phi, double ls_wid, double rdt, double rho_12,
+                       int btn, int max_iter, int mem, int32_t* iters, double* last_change) {
+  if (!ls) return GBMG_INVALID_ARG;
+  ls->err.clear();
+  if (iters) *iters = 0;
+  if (last_change) *last_change = 0.0;
+  if (cudaSetDevice(ls->device) != cudaSuccess) {
+    ls->err = "cudaSetDevice failed";
+    return GBMG_CUDA_ERROR;
+  }
+  if (!(ls_wid > 0) || !(rdt > 0) || max_iter < 0 || (btn != 0 && btn != 1)) {
+    ls->err = "ls_wid and rdt must be > 0, max_iter >= 0, btn 0 or 1";
+    return GBMG_INVALID_ARG;
+  }
+  if (mem != GBMG_MEM_HOST && mem != GBMG_MEM_DEVICE) {
+    ls->err = "mem must be GBMG_MEM_HOST or GBMG_MEM_DEVICE";
+    return GBMG_INVALID_ARG;
+  }
+  const gbmg_grid& g = ls->grid;
+  const bool three = g.nz > 1;
+  const LsGrid G{g.nx, g.ny, g.nz, g.dx, g.dy, g.dz};
+  const size_t n = ls_cells(g);
+  const unsigned nb = blocks_for(n);
+  double* s = ls->face[0];
+  double* grad = ls->face[1];
+  double* s2 = ls->face[2];
+  double* s3 = ls->face[3];
+  double* tmp = ls->face[4];
+  int rc;
+  if ((rc = ls_in(ls, phi, mem, ls->phi)) != GBMG_OK) return rc;
+  // level_set_redis_init (+ level_set_redis_stable for btn = 0)
+  k_ls_sign<<<nb, 256, 0, ls->stream>>>(n, ls->phi, ls_wid, btn, s);
+  ls->launches += 1;
+  if (btn == 0) {
+    k_ls_grad<<<nb, 256, 0, ls->stream>>>(G, ls->phi, s, grad);
+    ls->launches += 1;
+    LS_CUDA(ls, cudaMemsetAsync(ls->red, 0, sizeof(unsigned long long), ls->stream));
+    unsigned blocks = nb > 1024 ? 1024 : nb;
+    k_ls_maxabs<<<blocks, 256, 0, ls->stream>>>(n, grad, nullptr, ls->red);
+    k_ls_scale<<<nb, 256, 0, ls->stream>>>(n, ls->phi, ls->red);
+    ls->launches += 2;
+  }
+  LS_CUDA(ls, cudaGetLastError());
+  const double ext = three ? std::max(std::max(g.nx * g.dx, g.ny * g.dy), g.nz * g.dz)
+                           : std::max(g.nx * g.dx, g.ny * g.dy);
+  const double timestop = btn == 0 ? 1.5 * ext : 3.0 * g.dx;
+  const double tol = three ? 1.0e-5 : 1.0e-8;
+  double time = 0.0, error = 0.0;
+  int iter = 0;
+  while (iter < max_iter) {
+    ++iter;
+    time = time + rdt;
+    LS_CUDA(ls, cudaMemcpyAsync(tmp, ls->phi, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                ls->stream));
+    for (int stage = 1; stage <= 3; ++stage) {
+      k_ls_grad<<<nb, 256, 0, ls->stream>>>(G, ls->phi, s, grad);
+      ls->launches += 1;
+      if (btn != 0) {
+        k_ls_lambda<<<nb, 256, 0, ls->stream>>>(n, three ? 1 : 0, ls_wid, rho_12, ls->phi, s,
+                                                grad, s2, s3);
+        ls->launches += 1;
+      }
+      k_ls_redis_stage<<<nb, 256, 0, ls->stream>>>(G, stage, btn, rdt, ls_wid, s, grad, s2, s3,
+                                                   ls->l1, ls->l2, ls->phi);
+      ls->launches += 1;
+    }
+    LS_CUDA(ls, cudaGetLastError());
+    if ((rc = ls_max(ls, tmp, ls->phi, &error)) != GBMG_OK) return rc;
+    if (time > timestop || error <= tol) break;
+  }
+  if ((rc = ls_out(ls, ls->phi, mem, phi)) != GBMG_OK) return rc;
+  LS_CUDA(ls, cudaStreamSynchronize(ls->stream));
+  if (iters) *iters = iter;
+  if (last_change) *last_change = error;
   return GBMG_OK;
 }
 

@@ -1,8 +1,9 @@
 """Level-set transport on the GPU: the advection step of the reference's
-interface solver, level_set_rk3_solver ("Two phase flows/newOpenMP/2D/src/
+interface solver and its redistancing, level_set_rk3_solver ("Two phase flows/newOpenMP/2D/src/
 interface_solver/level_set_rk3_solver.f90:1-186"; 3D "Two phase flows/
-newOpenMP/3D+IBM/src/interface_solver/level_set_rk3_solver.f90:1-215"),
-through the C ABI (gbmg_ls_*).  phi is advanced in place, as the reference
+newOpenMP/3D+IBM/src/interface_solver/level_set_rk3_solver.f90:1-215") and
+level_set_rk3_redis (".../level_set_rk3_redis.f90"), through the C ABI
+(gbmg_ls_*).  phi is advanced in place, as the reference
 advances p%loc%phi%now; u, v, w are the cell-centred velocities (the
 reference's nvel; node_velocity() forms them from MAC faces as node_vel
 does)."""
@@ -89,6 +90,21 @@ class LevelSet:
             msg = self._L.gbmg_ls_last_error(self._h).decode()
             raise GBMGError(f"ls_advect: {self._L.gbmg_strerror(rc).decode()} {msg}".strip())
         return phi
+
+    def redistance(self, phi, ls_wid, rdt, rho_12=1e-3, btn=1, max_iter=100000):
+        """level_set_rk3_redis(btn) on phi in place (see gbmg_ls_redistance).
+        Returns (phi, iterations, largest change of the last iteration)."""
+        fp, m = _field(phi, self.shape)
+        if torch is not None and _is_torch(phi) and phi.is_cuda:
+            torch.cuda.current_stream().synchronize()
+        it = C.c_int32(0)
+        ch = C.c_double(0.0)
+        rc = self._L.gbmg_ls_redistance(self._h, fp, float(ls_wid), float(rdt), float(rho_12),
+                                        int(btn), int(max_iter), m, C.byref(it), C.byref(ch))
+        if rc != _lib.GBMG_OK:
+            msg = self._L.gbmg_ls_last_error(self._h).decode()
+            raise GBMGError(f"ls_redistance: {self._L.gbmg_strerror(rc).decode()} {msg}".strip())
+        return phi, it.value, ch.value
 
     @property
     def kernel_launches(self):

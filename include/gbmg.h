@@ -267,6 +267,23 @@ int gbmg_ls_destroy(gbmg_ls* ls);
 int gbmg_ls_advect(gbmg_ls* ls, gbmg_field phi, gbmg_field u, gbmg_field v, gbmg_field w,
                    double dt, int steps, int mem);
 
+/* Redistancing, level_set_rk3_redis(btn) ("Two phase flows/newOpenMP/2D/src/
+ * interface_solver/level_set_rk3_redis.f90:1-361"; 3D "Two phase flows/
+ * newOpenMP/3D+IBM/src/interface_solver/level_set_rk3_redis.f90"), phi in
+ * place: phi_tau + S (|grad phi| - 1) = 0 in pseudo-time steps rdt with the
+ * Godunov gradient of WENO-JS one-sided derivatives and three SSP-RK3
+ * stages.  btn = 1 (every few time steps in the reference): S = 2H - 1 of the
+ * level set (H the smoothed Heaviside of half width ls_wid) and the
+ * mass-preserving correction (3D: weighted by the density ratio rho_12),
+ * for 3 dx of pseudo time.  btn = 0 (initialisation): S = phi, phi first
+ * divided by max |grad phi|, for 1.5 x the largest extent of the domain
+ * (n h per axis).  Both stop earlier when the largest change of an
+ * iteration is at most 1e-8 (2D) or 1e-5 (3D), or after max_iter
+ * iterations.  *iters and *last_change report the iterations done and that
+ * change.  The sign and the Heaviside use CUDA's sin and cos. */
+int gbmg_ls_redistance(gbmg_ls* ls, gbmg_field phi, double ls_wid, double rdt, double rho_12,
+                       int btn, int max_iter, int mem, int32_t* iters, double* last_change);
+
 /* Kernels launched by this handle since creation. */
 int64_t gbmg_ls_kernel_launches(gbmg_ls* ls);
 

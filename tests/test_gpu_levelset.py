@@ -86,3 +86,54 @@ def test_errors_and_no_op(cuda):
         np.testing.assert_array_equal(same, phi)
         with pytest.raises(ValueError):
             ls.advect(phi.copy(), u[:, :, :-1], v, w, dt=1e-3)
+
+
+def _stretched(shape, h, seed=4):
+    rng = np.random.default_rng(seed)
+    nz = shape[0]
+    z, y, x = np.meshgrid(*[(np.arange(n) + 0.5) * h for n in shape], indexing="ij")
+    r = np.sqrt((x - 0.5) ** 2 + (y - 0.45) ** 2 + ((z - 0.25) ** 2 if nz > 1 else 0))
+    return (r - 0.3) * 1.7 + 0.01 * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("shape", [(1, 40, 48), (16, 18, 20)])
+def test_redistance_initial_matches_oracle_bitwise(cuda, shape):
+    """btn = 0 (S = phi, no Heaviside): no transcendental function on the
+    path, so GPU and oracle agree bit for bit, iteration count included."""
+    h = 1.0 / shape[2]
+    phi = _stretched(shape, h)
+    want, it_w, ch_w = orc.ls_redistance(phi, 1.5 * h, 0.1 * h, (h, h, h), btn=0, max_iter=12)
+    got = phi.copy()
+    with LevelSet(shape, (h, h, h)) as ls:
+        _, it, ch = ls.redistance(got, 1.5 * h, 0.1 * h, btn=0, max_iter=12)
+    assert it == it_w and ch == ch_w
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("shape", [(1, 64, 64), (24, 24, 24)])
+def test_redistance_with_mass_correction_matches_oracle(cuda, shape):
+    """btn = 1: the sign and the mass correction use sin and cos (CUDA's on
+    the GPU, the C library's in the oracle), so the comparison is to 1e-12 of
+    max |phi|; the iteration count is the same."""
+    h = 1.0 / shape[2]
+    phi = _stretched(shape, h)
+    want, it_w, _ = orc.ls_redistance(phi, 1.5 * h, 0.1 * h, (h, h, h), btn=1)
+    got = phi.copy()
+    with LevelSet(shape, (h, h, h)) as ls:
+        _, it, _ = ls.redistance(got, 1.5 * h, 0.1 * h, btn=1)
+    assert it == it_w
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(phi).max())
+
+
+def test_redistance_device_tensor(cuda):
+    import torch
+    shape = (1, 32, 40)
+    h = 1.0 / 40
+    phi = _stretched(shape, h)
+    want, _, _ = orc.ls_redistance(phi, 1.5 * h, 0.1 * h, (h, h, h), btn=0, max_iter=5)
+    t = torch.from_numpy(phi).to(cuda)
+    with LevelSet(shape, (h, h, h)) as ls:
+        ls.redistance(t, 1.5 * h, 0.1 * h, btn=0, max_iter=5)
+        with pytest.raises(GBMGError):
+            ls.redistance(t, -1.0, 0.1 * h)
+    np.testing.assert_array_equal(t.cpu().numpy(), want)
