@@ -388,7 +388,8 @@ def levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h, steps=5):
         h = case.spacing[0]
         ls = LevelSet(case.shape, case.spacing, stream=stream)
         e0.record(stream)
-        _, iters, _ = ls.redistance(phi, case.eps, 0.1 * h, rho_12=case.rho_neg, btn=1)
+        rho_12 = min(case.rho_pos, case.rho_neg) / max(case.rho_pos, case.rho_neg)
+        _, iters, _ = ls.redistance(phi, case.eps, 0.1 * h, rho_12=rho_12, btn=1)
         e1.record(stream)
         torch.cuda.synchronize()
         redis_ms = e0.elapsed_time(e1)
@@ -398,7 +399,7 @@ def levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h, steps=5):
     ref = orc.ls_advect(phi_h, un_h, vn_h, wn_h, case.dt, case.spacing, steps=1)
     cpu_ms = (time.perf_counter() - t0) * 1e3
     t0 = time.perf_counter()
-    orc.ls_redistance(phi_h, case.eps, 0.1 * case.spacing[0], case.spacing, rho_12=case.rho_neg,
+    orc.ls_redistance(phi_h, case.eps, 0.1 * case.spacing[0], case.spacing, rho_12=rho_12,
                       btn=1, max_iter=2)
     cpu_redis_it_ms = (time.perf_counter() - t0) * 1e3 / 2
     nz, ny, nx = case.shape
