@@ -204,6 +204,50 @@ module gbmg
       integer(c_int32_t), value :: n
     end function
 
+    ! level-set transport (a separate handle, gbmg_ls)
+    integer(c_int) function gbmg_ls_create(grid, device, stream, ls) bind(c, name="gbmg_ls_create")
+      import :: c_int, c_ptr, gbmg_grid
+      type(gbmg_grid), intent(in) :: grid
+      integer(c_int), value   :: device
+      type(c_ptr), value      :: stream
+      type(c_ptr), intent(out) :: ls
+    end function
+
+    integer(c_int) function gbmg_ls_destroy(ls) bind(c, name="gbmg_ls_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ls
+    end function
+
+    integer(c_int) function gbmg_ls_advect(ls, phi, u, v, w, dt, steps, mem) &
+        bind(c, name="gbmg_ls_advect")
+      import :: c_int, c_ptr, c_double, gbmg_field
+      type(c_ptr), value      :: ls
+      type(gbmg_field), value :: phi, u, v, w
+      real(c_double), value   :: dt
+      integer(c_int), value   :: steps, mem
+    end function
+
+    integer(c_int) function gbmg_ls_redistance(ls, phi, ls_wid, rdt, rho_12, btn, max_iter, mem, &
+        iters, last_change) bind(c, name="gbmg_ls_redistance")
+      import :: c_int, c_int32_t, c_ptr, c_double, gbmg_field
+      type(c_ptr), value      :: ls
+      type(gbmg_field), value :: phi
+      real(c_double), value   :: ls_wid, rdt, rho_12
+      integer(c_int), value   :: btn, max_iter, mem
+      integer(c_int32_t), intent(out) :: iters
+      real(c_double), intent(out) :: last_change
+    end function
+
+    integer(c_int64_t) function gbmg_ls_kernel_launches(ls) bind(c, name="gbmg_ls_kernel_launches")
+      import :: c_int64_t, c_ptr
+      type(c_ptr), value :: ls
+    end function
+
+    type(c_ptr) function gbmg_ls_last_error_c(ls) bind(c, name="gbmg_ls_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: ls
+    end function
+
     type(c_ptr) function gbmg_strerror_c(status) bind(c, name="gbmg_strerror")
       import :: c_int, c_ptr
       integer(c_int), value :: status
