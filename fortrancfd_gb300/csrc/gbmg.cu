@@ -21,6 +21,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "gbmg.h"
 #include "gbmg_internal.h"
@@ -52,6 +53,8 @@ struct Level {
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
+constexpr int kGmresRestart = 30;   // flexible GMRES restart length
+constexpr int kGmresBlocks = 1024;  // blocks of its dot-product kernel
 
 }  // namespace
 
@@ -75,6 +78,9 @@ struct gbmg_handle {
   double* aux[2] = {nullptr, nullptr};  // adjoint outputs / staging, allocated on first use
   // flexible CG vectors (allocated when krylov = 1)
   double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
+  // flexible GMRES (krylov = 2): basis V (restart + 1 vectors), preconditioned
+  // vectors Z (restart), dot partials, device and pinned host coefficients
+  double *gmV = nullptr, *gmZ = nullptr, *gmPart = nullptr, *gmDev = nullptr, *gmHost = nullptr;
   // coarsest level
   int nc = 0;
   double *minv = nullptr, *adense = nullptr, *cwork = nullptr;
@@ -484,6 +490,8 @@ int free_all(gbmg_handle* h) {
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
   dfree(h->aux[0]); dfree(h->aux[1]);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
+  dfree(h->gmV); dfree(h->gmZ); dfree(h->gmPart); dfree(h->gmDev);
+  if (h->gmHost) cudaFreeHost(h->gmHost);
   dfree(h->minv); dfree(h->adense); dfree(h->cwork); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   dfree(h->bar);
   delete[] h->dmaps;
@@ -686,6 +694,13 @@ int allocate(gbmg_handle* h) {
     GB_TRY(dmalloc(h, &h->kzold, h->n0));
     GB_TRY(dmalloc(h, &h->kd, h->n0));
     GB_TRY(dmalloc(h, &h->kq, h->n0));
+    if (h->prm.krylov == 2) {
+      GB_TRY(dmalloc(h, &h->gmV, (size_t)(kGmresRestart + 1) * h->n0));
+      GB_TRY(dmalloc(h, &h->gmZ, (size_t)kGmresRestart * h->n0));
+      GB_TRY(dmalloc(h, &h->gmPart, (size_t)(kGmresRestart + 1) * kGmresBlocks));
+      GB_TRY(dmalloc(h, &h->gmDev, (size_t)kGmresRestart + 1));
+      GB_CUDA(h, cudaMallocHost((void**)&h->gmHost, (kGmresRestart + 1) * sizeof(double)));
+    }
   }
   GB_TRY(dmalloc(h, &h->minv, (size_t)nc * nc));
   GB_TRY(dmalloc(h, &h->adense, (size_t)nc * nc));
@@ -994,6 +1009,123 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
 }
 
 // The solve loop on the internal (b, p).  Leaves p mean-free.
+// z = M v: one V-cycle from zero on v (the flexible-CG preconditioner),
+// mean-free.  Leaves the finest level's sol/src pointing at p and b.
+int precondition(gbmg_handle* h, const double* v, double* z) {
+  const cudaStream_t s = h->stream;
+  Level& f = h->lv[0];
+  const size_t n = h->n0;
+  const int V = GBMG_PROF_VECTOR;
+  const bool zg = h->prm.nu1 > 0;
+  if (!h->mixed) {
+    if (!zg) GB_CUDA(h, cudaMemsetAsync(z, 0, n * sizeof(double), s));
+    f.sol = z; f.src = const_cast<double*>(v);
+    GB_TRY(enqueue_vcycle<double>(h, true, zg));
+  } else {
+    if (f.split) LAUNCH(h, V, launch_to_split(s, v, f.src32, f.nx, f.ny, f.nz, f.hstride));
+    else LAUNCH(h, V, launch_double_to_float(s, v, f.src32, n));
+    if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
+    GB_TRY(enqueue_vcycle<float>(h, true, zg));
+    if (f.split) LAUNCH(h, V, launch_from_split(s, f.sol32, z, f.nx, f.ny, f.nz, f.hstride));
+    else LAUNCH(h, V, launch_float_to_double(s, f.sol32, z, n));
+  }
+  LAUNCH(h, V, launch_sum(s, z, n, h->red, kSlotSum));
+  LAUNCH(h, V, launch_shift_by_mean(s, z, z, n, h->red, kSlotSum, -1));
+  f.sol = h->p; f.src = h->b;
+  return check_launch(h, "preconditioner");
+}
+
+// dots V_i . w, i < cnt, to the host (gmHost)
+int gm_dots(gbmg_handle* h, const double* V, int cnt, const double* w) {
+  const cudaStream_t s = h->stream;
+  LAUNCH(h, GBMG_PROF_VECTOR,
+         launch_mdot(s, V, h->n0, cnt, w, h->n0, h->gmPart, kGmresBlocks, h->gmDev));
+  h->launches += 1;  // the finishing kernel
+  GB_CUDA(h, cudaMemcpyAsync(h->gmHost, h->gmDev, cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(h, cudaStreamSynchronize(s));
+  return check_launch(h, "dots");
+}
+
+// Flexible GMRES(kGmresRestart) around the V-cycle (right preconditioning,
+// Saad's FGMRES): the residual norm falls monotonically, where conjugate
+// gradients can first raise it many-fold on a smooth right-hand side (the
+// adjoint of a smooth objective).  Classical Gram-Schmidt applied twice,
+// Givens rotations on the host; at each restart and at the end the true
+// FP64 residual b - A p is recomputed.  On entry kr holds r0 = b - A p and
+// host_res[kSlotNorm] its squared norm.
+int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles, int* status) {
+  const cudaStream_t s = h->stream;
+  Level& f = h->lv[0];
+  const size_t n = h->n0;
+  const int m = kGmresRestart;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), col(m + 1);
+  double r2 = h->host_res[kSlotNorm];
+  double rel = *rel_io;
+  int total = 0;
+  *status = GBMG_NOT_CONVERGED;
+  while (total < h->prm.max_cycles) {
+    const double beta = std::sqrt(r2);
+    if (!(beta > 0.0)) { *status = GBMG_OK; break; }
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_scale_copy(s, h->gmV, h->kr, 1.0 / beta, n));
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int j = 0;
+    for (; j < m && total < h->prm.max_cycles; ) {
+      double* vj = h->gmV + (size_t)j * n;
+      double* zj = h->gmZ + (size_t)j * n;
+      double* w = h->gmV + (size_t)(j + 1) * n;
+      GB_TRY(precondition(h, vj, zj));
+      LAUNCH(h, GBMG_PROF_RESIDUAL, launch_apply_dot(s, v64(f), zj, w, h->red, kSlotDot2));
+      std::fill(col.begin(), col.end(), 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        GB_TRY(gm_dots(h, h->gmV, j + 1, w));
+        for (int i = 0; i <= j; ++i) col[i] += h->gmHost[i];
+        LAUNCH(h, GBMG_PROF_VECTOR, launch_maxpy(s, w, h->gmV, n, h->gmDev, j + 1, -1.0, n));
+      }
+      GB_TRY(gm_dots(h, w, 1, w));
+      const double hn = std::sqrt(h->gmHost[0]);
+      col[j + 1] = hn;
+      if (hn > 0.0) LAUNCH(h, GBMG_PROF_VECTOR, launch_scale_copy(s, w, w, 1.0 / hn, n));
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+        col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+        col[i] = t;
+      }
+      const double d = std::hypot(col[j], col[j + 1]);
+      cs[j] = d > 0.0 ? col[j] / d : 1.0;
+      sn[j] = d > 0.0 ? col[j + 1] / d : 0.0;
+      col[j] = d;
+      col[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = col[i];
+      ++j;
+      ++total;
+      rel = std::fabs(g[j]) / scale;
+      if (!std::isfinite(rel) || rel < tol || !(hn > 0.0)) break;
+    }
+    // x += Z y with R y = g (R: the rotated Hessenberg, upper triangular)
+    for (int i = j - 1; i >= 0; --i) {
+      double t = g[i];
+      for (int k = i + 1; k < j; ++k) t -= H[(size_t)i * m + k] * y[k];
+      y[i] = H[(size_t)i * m + i] != 0.0 ? t / H[(size_t)i * m + i] : 0.0;
+    }
+    GB_CUDA(h, cudaMemcpyAsync(h->gmDev, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_maxpy(s, h->p, h->gmZ, n, h->gmDev, j, 1.0, n));
+    f.sol = h->p; f.src = h->b;
+    LAUNCH(h, GBMG_PROF_RESIDUAL,
+           launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
+    GB_TRY(check_launch(h, "fgmres residual"));
+    GB_TRY(read_result(h, kSlotNorm, &r2));
+    rel = std::sqrt(r2) / scale;
+    if (!std::isfinite(rel) || rel > 1e3) { *status = GBMG_DIVERGED; break; }
+    if (rel < tol) { *status = GBMG_OK; break; }
+  }
+  *rel_io = rel;
+  *cycles = total;
+  return GBMG_OK;
+}
+
 int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
@@ -1024,6 +1156,9 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   int cyc = 0;
   if (rel < tol) {
     status = GBMG_OK;
+  } else if (h->prm.krylov == 2) {
+    GB_TRY(fgmres(h, tol, scale, &rel, &cyc, &status));
+    r2 = rel * scale * rel * scale;
   } else {
     for (cyc = 1; cyc <= h->prm.max_cycles; ++cyc) {
       GB_TRY(run_iteration(h, kind, pcg && cyc == 1));

@@ -274,6 +274,14 @@ void launch_pcg_step(cudaStream_t s, double* x, const double* d, size_t n, const
 void launch_apply_dot(cudaStream_t s, const LevelView<double>& L, const double* d, double* q,
                       const ReduceScratch& R, int slot);
 void launch_float_to_double(cudaStream_t s, const float* a, double* b, size_t n);
+// flexible GMRES vector kernels (krylov.cu): out[i] = V_i . w for i < cnt
+// (basis V_i at V + i*ld; partials: cnt * max_blocks doubles), w += sign *
+// sum_i coef[i] V_i, out = alpha * in
+void launch_mdot(cudaStream_t s, const double* V, size_t ld, int cnt, const double* w, size_t n,
+                 double* partials, int max_blocks, double* out);
+void launch_maxpy(cudaStream_t s, double* w, const double* V, size_t ld, const double* coef,
+                  int cnt, double sign, size_t n);
+void launch_scale_copy(cudaStream_t s, double* out, const double* in, double alpha, size_t n);
 void launch_double_to_float(cudaStream_t s, const double* a, float* b, size_t n);
 
 int reduce_blocks_for(size_t n);

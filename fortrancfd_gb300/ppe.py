@@ -81,6 +81,17 @@ def _field(a, shape):
     return _lib.Field(a.ctypes.data, a.strides[1] // 8, a.strides[0] // 8), _lib.GBMG_MEM_HOST
 
 
+def _krylov_mode(krylov):
+    """0 / False: stationary V-cycles; 1 / True / "fcg": flexible CG;
+    2 / "fgmres": flexible GMRES(30), each with one V-cycle as preconditioner."""
+    if isinstance(krylov, str):
+        return {"none": 0, "fcg": 1, "fgmres": 2}[krylov]
+    k = int(krylov)
+    if k not in (0, 1, 2):
+        raise ValueError("krylov must be 0, 1 (flexible CG) or 2 (flexible GMRES)")
+    return k
+
+
 def _mem_of(*pairs):
     mems = {m for _, m in pairs if m is not None}
     if len(mems) != 1:
@@ -93,8 +104,10 @@ class PressurePoisson:
 
     shape: (nz, ny, nx) cells (nz = 1 for 2D); spacing: (dx, dy, dz).
     precision: "fp64" (FP64 V-cycles) or "mixed" (FP32 V-cycles inside FP64
-    defect correction).  krylov=True wraps one V-cycle per iteration in
-    flexible CG.
+    defect correction).  krylov=True (or "fcg") wraps one V-cycle per
+    iteration in flexible CG, krylov="fgmres" (or 2) in flexible GMRES(30),
+    whose residual falls monotonically (faster on smooth right-hand sides such
+    as adjoint solves).
     """
 
     def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
@@ -115,7 +128,7 @@ class PressurePoisson:
         prm.precision = {"fp64": _lib.GBMG_PREC_FP64, "mixed": _lib.GBMG_PREC_MIXED}[precision]
         prm.nu1, prm.nu2 = nu1, nu2
         prm.levels, prm.coarse_max, prm.max_cycles = levels, coarse_max, max_cycles
-        prm.krylov = int(bool(krylov))
+        prm.krylov = _krylov_mode(krylov)
         prm.use_graph = int(bool(use_graph))
         prm.remove_rhs_mean = int(bool(remove_rhs_mean))
         prm.certify = int(bool(certify))

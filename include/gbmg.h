@@ -68,7 +68,8 @@ typedef struct {
   int32_t levels;          /* 0 = automatic; else the reference's "Multigrid level" count */
   int32_t coarse_max;      /* automatic levels: coarsen until at most this many cells (<= 64) */
   int32_t max_cycles;      /* cycle (or Krylov iteration) limit */
-  int32_t krylov;          /* 0: stationary V-cycles; 1: flexible CG, one V-cycle as preconditioner */
+  int32_t krylov;          /* 0: stationary V-cycles; 1: flexible CG, 2: flexible GMRES(30)
+                              (residual falls monotonically), one V-cycle as preconditioner */
   int32_t use_graph;       /* 1: replay each cycle as a captured CUDA graph */
   int32_t remove_rhs_mean; /* 1: project the mean out of b before solving (compatibility) */
   int32_t certify;         /* mixed precision: 1 = recompute the final residual in native FP64
