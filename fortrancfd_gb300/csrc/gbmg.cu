@@ -112,6 +112,9 @@ struct gbmg_handle {
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
+  // flexible GMRES: kz = M kr and kq = A kz as one captured graph
+  cudaGraphExec_t gm_graph = nullptr;
+  int64_t gm_graph_kernels = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // host transfers of a solve that overlap its kernels: the H2D of the initial
   // p beside the right-hand side's preparation, the D2H of the result beside
@@ -452,6 +455,9 @@ int reset_graphs(gbmg_handle* h) {
       h->graph[k][par] = nullptr;
       h->graph_kernels[k][par] = 0;
     }
+  if (h->gm_graph) cudaGraphExecDestroy(h->gm_graph);
+  h->gm_graph = nullptr;
+  h->gm_graph_kernels = 0;
   return GBMG_OK;
 }
 
@@ -698,8 +704,8 @@ int allocate(gbmg_handle* h) {
       GB_TRY(dmalloc(h, &h->gmV, (size_t)(kGmresRestart + 1) * h->n0));
       GB_TRY(dmalloc(h, &h->gmZ, (size_t)kGmresRestart * h->n0));
       GB_TRY(dmalloc(h, &h->gmPart, (size_t)(kGmresRestart + 1) * kGmresBlocks));
-      GB_TRY(dmalloc(h, &h->gmDev, (size_t)kGmresRestart + 1));
-      GB_CUDA(h, cudaMallocHost((void**)&h->gmHost, (kGmresRestart + 1) * sizeof(double)));
+      GB_TRY(dmalloc(h, &h->gmDev, (size_t)3 * (kGmresRestart + 1)));
+      GB_CUDA(h, cudaMallocHost((void**)&h->gmHost, 3 * (kGmresRestart + 1) * sizeof(double)));
     }
   }
   GB_TRY(dmalloc(h, &h->minv, (size_t)nc * nc));
@@ -1035,29 +1041,63 @@ int precondition(gbmg_handle* h, const double* v, double* z) {
   return check_launch(h, "preconditioner");
 }
 
-// dots V_i . w, i < cnt, to the host (gmHost)
-int gm_dots(gbmg_handle* h, const double* V, int cnt, const double* w) {
+// kz = M kr, kq = A kz: enqueued, or replayed from a graph captured on first use
+int gm_apply(gbmg_handle* h) {
   const cudaStream_t s = h->stream;
-  LAUNCH(h, GBMG_PROF_VECTOR,
-         launch_mdot(s, V, h->n0, cnt, w, h->n0, h->gmPart, kGmresBlocks, h->gmDev));
-  h->launches += 1;  // the finishing kernel
-  GB_CUDA(h, cudaMemcpyAsync(h->gmHost, h->gmDev, cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
-  GB_CUDA(h, cudaStreamSynchronize(s));
-  return check_launch(h, "dots");
+  Level& f = h->lv[0];
+  const auto enqueue = [&]() -> int {
+    GB_TRY(precondition(h, h->kr, h->kz));
+    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_apply_dot(s, v64(f), h->kz, h->kq, h->red, kSlotDot2));
+    return check_launch(h, "preconditioned product");
+  };
+  if (!h->prm.use_graph || h->prof) return enqueue();
+  if (!h->gm_graph) {
+    cudaGraph_t g = nullptr;
+    const int64_t before = h->launches;
+    GB_CUDA(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    const cudaError_t ec = cudaStreamEndCapture(s, &g);
+    if (rc != GBMG_OK || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (rc != GBMG_OK) return rc;
+      h->err = std::string("graph capture: ") + cudaGetErrorString(ec);
+      return GBMG_CUDA_ERROR;
+    }
+    h->gm_graph_kernels = h->launches - before;
+    h->launches = before;
+    const cudaError_t ei = cudaGraphInstantiate(&h->gm_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      h->gm_graph = nullptr;
+      h->err = std::string("graph instantiate: ") + cudaGetErrorString(ei);
+      return GBMG_CUDA_ERROR;
+    }
+  }
+  GB_CUDA(h, cudaGraphLaunch(h->gm_graph, s));
+  h->launches += h->gm_graph_kernels;
+  return GBMG_OK;
 }
 
 // Flexible GMRES(kGmresRestart) around the V-cycle (right preconditioning,
 // Saad's FGMRES): the residual norm falls monotonically, where conjugate
 // gradients can first raise it many-fold on a smooth right-hand side (the
-// adjoint of a smooth objective).  Classical Gram-Schmidt applied twice,
-// Givens rotations on the host; at each restart and at the end the true
-// FP64 residual b - A p is recomputed.  On entry kr holds r0 = b - A p and
-// host_res[kSlotNorm] its squared norm.
+// adjoint of a smooth objective).  Per Arnoldi step: z_j = M v_j and
+// w = A z_j (one captured graph on fixed buffers: v_j is copied in, z_j and w
+// out), classical Gram-Schmidt applied twice and the normalisation on the
+// device, then one copy of the coefficients to the host for the Givens
+// rotations.  At each restart and at the end the true FP64 residual b - A p
+// is recomputed.  On entry kr holds r0 = b - A p and host_res[kSlotNorm] its
+// squared norm.
 int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles, int* status) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
   const size_t n = h->n0;
   const int m = kGmresRestart;
+  const int VC = GBMG_PROF_VECTOR;
+  const size_t bytes = n * sizeof(double);
+  double* h1 = h->gmDev;               // first Gram-Schmidt pass
+  double* h2 = h->gmDev + (m + 1);     // second pass
+  double* nrm = h->gmDev + 2 * (m + 1);  // |w|^2
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), col(m + 1);
   double r2 = h->host_res[kSlotNorm];
   double rel = *rel_io;
@@ -1066,26 +1106,31 @@ int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles
   while (total < h->prm.max_cycles) {
     const double beta = std::sqrt(r2);
     if (!(beta > 0.0)) { *status = GBMG_OK; break; }
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_scale_copy(s, h->gmV, h->kr, 1.0 / beta, n));
+    LAUNCH(h, VC, launch_scale_copy(s, h->gmV, h->kr, 1.0 / beta, n));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int j = 0;
-    for (; j < m && total < h->prm.max_cycles; ) {
+    for (; j < m && total < h->prm.max_cycles;) {
       double* vj = h->gmV + (size_t)j * n;
-      double* zj = h->gmZ + (size_t)j * n;
       double* w = h->gmV + (size_t)(j + 1) * n;
-      GB_TRY(precondition(h, vj, zj));
-      LAUNCH(h, GBMG_PROF_RESIDUAL, launch_apply_dot(s, v64(f), zj, w, h->red, kSlotDot2));
-      std::fill(col.begin(), col.end(), 0.0);
-      for (int pass = 0; pass < 2; ++pass) {
-        GB_TRY(gm_dots(h, h->gmV, j + 1, w));
-        for (int i = 0; i <= j; ++i) col[i] += h->gmHost[i];
-        LAUNCH(h, GBMG_PROF_VECTOR, launch_maxpy(s, w, h->gmV, n, h->gmDev, j + 1, -1.0, n));
-      }
-      GB_TRY(gm_dots(h, w, 1, w));
-      const double hn = std::sqrt(h->gmHost[0]);
+      GB_CUDA(h, cudaMemcpyAsync(h->kr, vj, bytes, cudaMemcpyDeviceToDevice, s));
+      GB_TRY(gm_apply(h));
+      GB_CUDA(h, cudaMemcpyAsync(h->gmZ + (size_t)j * n, h->kz, bytes, cudaMemcpyDeviceToDevice, s));
+      GB_CUDA(h, cudaMemcpyAsync(w, h->kq, bytes, cudaMemcpyDeviceToDevice, s));
+      LAUNCH(h, VC, launch_mdot(s, h->gmV, n, j + 1, w, n, h->gmPart, kGmresBlocks, h1));
+      LAUNCH(h, VC, launch_maxpy(s, w, h->gmV, n, h1, j + 1, -1.0, n));
+      LAUNCH(h, VC, launch_mdot(s, h->gmV, n, j + 1, w, n, h->gmPart, kGmresBlocks, h2));
+      LAUNCH(h, VC, launch_maxpy(s, w, h->gmV, n, h2, j + 1, -1.0, n));
+      LAUNCH(h, VC, launch_mdot(s, w, n, 1, w, n, h->gmPart, kGmresBlocks, nrm));
+      LAUNCH(h, VC, launch_scale_rsqrt(s, w, nrm, n));
+      h->launches += 3;  // the finishing kernels of the three dot launches
+      GB_CUDA(h, cudaMemcpyAsync(h->gmHost, h->gmDev, 3 * (m + 1) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+      GB_CUDA(h, cudaStreamSynchronize(s));
+      GB_TRY(check_launch(h, "arnoldi"));
+      for (int i = 0; i <= j; ++i) col[i] = h->gmHost[i] + h->gmHost[(m + 1) + i];
+      const double hn = std::sqrt(h->gmHost[2 * (m + 1)]);
       col[j + 1] = hn;
-      if (hn > 0.0) LAUNCH(h, GBMG_PROF_VECTOR, launch_scale_copy(s, w, w, 1.0 / hn, n));
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * col[i] + sn[i] * col[i + 1];
         col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
@@ -1110,8 +1155,9 @@ int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles
       for (int k = i + 1; k < j; ++k) t -= H[(size_t)i * m + k] * y[k];
       y[i] = H[(size_t)i * m + i] != 0.0 ? t / H[(size_t)i * m + i] : 0.0;
     }
-    GB_CUDA(h, cudaMemcpyAsync(h->gmDev, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_maxpy(s, h->p, h->gmZ, n, h->gmDev, j, 1.0, n));
+    std::copy(y.begin(), y.begin() + j, h->gmHost);
+    GB_CUDA(h, cudaMemcpyAsync(h->gmDev, h->gmHost, j * sizeof(double), cudaMemcpyHostToDevice, s));
+    LAUNCH(h, VC, launch_maxpy(s, h->p, h->gmZ, n, h->gmDev, j, 1.0, n));
     f.sol = h->p; f.src = h->b;
     LAUNCH(h, GBMG_PROF_RESIDUAL,
            launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));

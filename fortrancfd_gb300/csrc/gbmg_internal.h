@@ -282,6 +282,7 @@ void launch_mdot(cudaStream_t s, const double* V, size_t ld, int cnt, const doub
 void launch_maxpy(cudaStream_t s, double* w, const double* V, size_t ld, const double* coef,
                   int cnt, double sign, size_t n);
 void launch_scale_copy(cudaStream_t s, double* out, const double* in, double alpha, size_t n);
+void launch_scale_rsqrt(cudaStream_t s, double* w, const double* nrm2, size_t n);  // w /= |w|
 void launch_double_to_float(cudaStream_t s, const double* a, float* b, size_t n);
 
 int reduce_blocks_for(size_t n);

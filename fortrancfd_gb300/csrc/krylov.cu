@@ -75,6 +75,17 @@ __global__ void __launch_bounds__(kMThreads) k_scale_copy(double* out, const dou
     out[q] = alpha * in[q];
 }
 
+// w *= 1/sqrt(*nrm2) (w unchanged when the norm is 0)
+__global__ void __launch_bounds__(kMThreads) k_scale_rsqrt(double* w, const double* nrm2,
+                                                           size_t n) {
+  const double v = *nrm2;
+  if (!(v > 0.0)) return;
+  const double a = 1.0 / sqrt(v);
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    w[q] = a * w[q];
+}
+
 unsigned grid_for(size_t n, int max_blocks) {
   size_t b = (n + kMThreads - 1) / kMThreads;
   if (b > (size_t)max_blocks) b = (size_t)max_blocks;
@@ -97,6 +108,10 @@ void launch_maxpy(cudaStream_t s, double* w, const double* V, size_t ld, const d
 
 void launch_scale_copy(cudaStream_t s, double* out, const double* in, double alpha, size_t n) {
   k_scale_copy<<<grid_for(n, 4096), kMThreads, 0, s>>>(out, in, alpha, n);
+}
+
+void launch_scale_rsqrt(cudaStream_t s, double* w, const double* nrm2, size_t n) {
+  k_scale_rsqrt<<<grid_for(n, 4096), kMThreads, 0, s>>>(w, nrm2, n);
 }
 
 }  // namespace gbmg
