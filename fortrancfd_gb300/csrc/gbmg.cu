@@ -1082,10 +1082,10 @@ int gm_apply(gbmg_handle* h) {
 // Saad's FGMRES): the residual norm falls monotonically, where conjugate
 // gradients can first raise it many-fold on a smooth right-hand side (the
 // adjoint of a smooth objective).  Per Arnoldi step: z_j = M v_j and
-// w = A z_j (one captured graph on fixed buffers: v_j is copied in, z_j and w
-// out), classical Gram-Schmidt applied twice and the normalisation on the
-// device, then one copy of the coefficients to the host for the Givens
-// rotations.  At each restart and at the end the true FP64 residual b - A p
+// w = A z_j (one captured graph on fixed buffers: v_j is copied in, z_j out),
+// classical Gram-Schmidt on the device with a second pass only when the
+// first removed most of w, one copy of the coefficients to the host for the
+// Givens rotations, and w scaled into v_{j+1}.  At each restart and at the end the true FP64 residual b - A p
 // is recomputed.  On entry kr holds r0 = b - A p and host_res[kSlotNorm] its
 // squared norm.
 int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles, int* status) {
@@ -1097,7 +1097,7 @@ int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles
   const size_t bytes = n * sizeof(double);
   double* h1 = h->gmDev;               // first Gram-Schmidt pass
   double* h2 = h->gmDev + (m + 1);     // second pass
-  double* nrm = h->gmDev + 2 * (m + 1);  // |w|^2
+  double* nrm = h->gmDev + 2 * (m + 1);  // |w|^2 after, then before, the first pass
   std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m), col(m + 1);
   double r2 = h->host_res[kSlotNorm];
   double rel = *rel_io;
@@ -1112,25 +1112,39 @@ int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles
     int j = 0;
     for (; j < m && total < h->prm.max_cycles;) {
       double* vj = h->gmV + (size_t)j * n;
-      double* w = h->gmV + (size_t)(j + 1) * n;
+      double* w = h->kq;  // A z_j, orthogonalised in place, then scaled into V_{j+1}
       GB_CUDA(h, cudaMemcpyAsync(h->kr, vj, bytes, cudaMemcpyDeviceToDevice, s));
       GB_TRY(gm_apply(h));
       GB_CUDA(h, cudaMemcpyAsync(h->gmZ + (size_t)j * n, h->kz, bytes, cudaMemcpyDeviceToDevice, s));
-      GB_CUDA(h, cudaMemcpyAsync(w, h->kq, bytes, cudaMemcpyDeviceToDevice, s));
+      // classical Gram-Schmidt; a second pass only when the first removed most
+      // of w (|w| fell below 0.7 of its length: "twice is enough")
+      LAUNCH(h, VC, launch_mdot(s, w, n, 1, w, n, h->gmPart, kGmresBlocks, nrm + 1));
       LAUNCH(h, VC, launch_mdot(s, h->gmV, n, j + 1, w, n, h->gmPart, kGmresBlocks, h1));
       LAUNCH(h, VC, launch_maxpy(s, w, h->gmV, n, h1, j + 1, -1.0, n));
-      LAUNCH(h, VC, launch_mdot(s, h->gmV, n, j + 1, w, n, h->gmPart, kGmresBlocks, h2));
-      LAUNCH(h, VC, launch_maxpy(s, w, h->gmV, n, h2, j + 1, -1.0, n));
       LAUNCH(h, VC, launch_mdot(s, w, n, 1, w, n, h->gmPart, kGmresBlocks, nrm));
-      LAUNCH(h, VC, launch_scale_rsqrt(s, w, nrm, n));
-      h->launches += 3;  // the finishing kernels of the three dot launches
+      h->launches += 3;  // the finishing kernels of the dot launches
       GB_CUDA(h, cudaMemcpyAsync(h->gmHost, h->gmDev, 3 * (m + 1) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
       GB_CUDA(h, cudaStreamSynchronize(s));
       GB_TRY(check_launch(h, "arnoldi"));
-      for (int i = 0; i <= j; ++i) col[i] = h->gmHost[i] + h->gmHost[(m + 1) + i];
-      const double hn = std::sqrt(h->gmHost[2 * (m + 1)]);
+      for (int i = 0; i <= j; ++i) col[i] = h->gmHost[i];
+      double hn = std::sqrt(h->gmHost[2 * (m + 1)]);
+      const double before = std::sqrt(h->gmHost[2 * (m + 1) + 1]);
+      if (hn < 0.7 * before) {
+        LAUNCH(h, VC, launch_mdot(s, h->gmV, n, j + 1, w, n, h->gmPart, kGmresBlocks, h2));
+        LAUNCH(h, VC, launch_maxpy(s, w, h->gmV, n, h2, j + 1, -1.0, n));
+        LAUNCH(h, VC, launch_mdot(s, w, n, 1, w, n, h->gmPart, kGmresBlocks, nrm));
+        h->launches += 2;
+        GB_CUDA(h, cudaMemcpyAsync(h->gmHost, h->gmDev, 3 * (m + 1) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, s));
+        GB_CUDA(h, cudaStreamSynchronize(s));
+        GB_TRY(check_launch(h, "arnoldi"));
+        for (int i = 0; i <= j; ++i) col[i] += h->gmHost[(m + 1) + i];
+        hn = std::sqrt(h->gmHost[2 * (m + 1)]);
+      }
       col[j + 1] = hn;
+      LAUNCH(h, VC, launch_scale_copy(s, h->gmV + (size_t)(j + 1) * n, w, hn > 0.0 ? 1.0 / hn : 0.0,
+                                      n));
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * col[i] + sn[i] * col[i + 1];
         col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
