@@ -309,7 +309,7 @@ def _device_velocity(shape, seed, dev):
     return u, v, w
 
 
-def multi_bubble_section(dev, stream, scale=1, reps=2):
+def multi_bubble_section(dev, stream, scale=1, reps=2, krylov=True):
     """The 512³ sixteen-bubble case: mixed precision (flexible CG around the
     FP32 V-cycle, the mode these small light bubbles need) against the FP64
     GPU solve of the same system."""
@@ -327,7 +327,7 @@ def multi_bubble_section(dev, stream, scale=1, reps=2):
         out = {}
         ps = {}
         for prec in ("mixed", "fp64"):
-            s = PressurePoisson(case.shape, case.spacing, precision=prec, krylov=True,
+            s = PressurePoisson(case.shape, case.spacing, precision=prec, krylov=krylov,
                                 max_cycles=400, stream=stream)
             b = s.divergence(u, v, w, case.dt)
             p = torch.zeros_like(b)
@@ -415,7 +415,7 @@ def levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h, steps=5):
             "cpu_oracle_redistance_ms_per_iteration": cpu_redis_it_ms}
 
 
-def rollout_section(dev, stream, scale=1, steps=20):
+def rollout_section(dev, stream, scale=1, steps=20, krylov=True):
     """The 20-step differentiable projection rollout (128x128x256, 4 bubbles):
     forward (20 mixed solves) and backward (20 adjoint solves and the
     checkpointed level sets) device times, gradient w.r.t. centres and radii."""
