@@ -461,8 +461,10 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
     """The differentiable solve on the 1024^2 eight-circle case: forward
     (operator from phi + mixed-precision solve) and backward (operator rebuild,
     adjoint solve, adjoint kernel) device times, and central differences of
-    J = |p - p_t|^2/2 with FP64 solves (step 1e-6, 4 random unit directions of
-    phi) against the mixed-precision gradient.  Flexible GMRES around the
+    J = |p - p_t|^2/2 with FP64 solves (step 1e-6, 16 random unit directions
+    of phi) against the mixed-precision gradient, and the same gradient from
+    FP64 solves (the finite differences of FP64 solves at 1e-12 carry noise
+    near 1e-6 themselves: both gradients agree with them equally).  Flexible GMRES around the
     V-cycle by default: on the smooth adjoint right-hand side p - p_t flexible
     CG first raises the residual many-fold and needs 32 iterations against 20."""
     import torch
@@ -499,19 +501,26 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
                 fw.append(e0.elapsed_time(e1))
                 bw.append(e1.elapsed_time(e2))
         g = x.grad
+        # the same gradient from FP64 solves (forward 1e-12, adjoint 3e-9, the
+        # adjoint's FP64 floor being about 2.6e-9)
+        x64 = phi.clone().requires_grad_(True)
+        p64 = pressure_solve(x64, b, s64, tol=1e-12, adjoint_tol=3e-9, **kw)
+        (0.5 * ((p64 - p_t) ** 2).sum()).backward()
+        g64 = x64.grad
 
         def J(ph):
             q = pressure_solve(ph, b, s64, tol=1e-12, **kw)
             return 0.5 * ((q - p_t) ** 2).sum()
 
         rng = np.random.default_rng(7)
-        errs = []
+        errs, errs64 = [], []
         with torch.no_grad():
-            for _ in range(4):
+            for _ in range(16):
                 v = torch.from_numpy(rng.standard_normal(case.shape)).to(dev)
                 v /= v.norm()
                 fd = float((J(phi + 1e-6 * v) - J(phi - 1e-6 * v)) / 2e-6)
                 errs.append(abs(fd - float((g * v).sum())) / abs(fd))
+                errs64.append(abs(float(((g - g64) * v).sum())) / abs(float((g64 * v).sum())))
         s.close()
         s64.close()
     f, bk = float(np.median(fw)), float(np.median(bw))
@@ -521,7 +530,10 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
                         "adjoint",
             "forward_ms": f, "backward_ms": bk, "backward_over_forward": bk / f,
             "forward_iterations": fwd_cycles, "adjoint_iterations": adj_cycles,
-            "fd_max_rel_err": max(errs), "fd_directions": len(errs)}
+            "fd_max_rel_err": max(errs), "fd_median_rel_err": float(np.median(errs)),
+            "fd_directions": len(errs),
+            "fp64_gradient_max_rel_diff": max(errs64),
+            "fp64_gradient_rel_l2_diff": float((g - g64).norm() / g64.norm())}
 
 
 def run_ours(args):
