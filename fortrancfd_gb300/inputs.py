@@ -149,3 +149,118 @@ def custom(shape, extent=(1.0, 1.0, 1.0), centers=((0.5, 0.5, 0.5),), radii=(0.2
            seed=0, **kw) -> Case:
     return Case("custom", tuple(shape), tuple(extent), np.asarray(centers, float),
                 np.asarray(radii, float), seed=seed, **kw)
+
+
+def padded_shape(shape, ghost):
+    """The reference's ghost-padded box of an interior (nz, ny, nx):
+    (nz+2g, ny+2g, nx+2g), or (ny+2g, nx+2g) in 2D."""
+    nz, ny, nx = shape
+    if nz == 1:
+        return (ny + 2 * ghost, nx + 2 * ghost)
+    return (nz + 2 * ghost, ny + 2 * ghost, nx + 2 * ghost)
+
+
+def velbc_numpy(u, v, w, ghost, bc):
+    """velbc ("Two phase flows/newOpenMP/2D/src/others/bcs.f90:28-132",
+    3D "…/3D+IBM/src/others/bcs.f90:44-257") on padded numpy arrays, for
+    building consistent synthetic states: ghosts mirror the interior (negated
+    for bc 1, no-slip; copied for bc 2, slip), the wall-normal face is 0.
+    Passes x, y, z in order over the whole padded extent."""
+    g = ghost
+    comps = [u, v] + ([w] if w is not None else [])
+    ax_of = {0: -1, 1: -2, 2: -3}
+    for axis in range(len(comps)):
+        ax = ax_of[axis]
+        for side in (0, 1):
+            t = bc[2 * axis + side]
+            if t not in (1, 2):
+                continue
+            s = -1.0 if t == 1 else 1.0
+            for c, f in enumerate(comps):
+                n = f.shape[ax] - 2 * g
+                a = np.moveaxis(f, ax, -1)
+                stag = c == axis
+                for m in range(1, g + 1):
+                    if side == 0:  # ghost index 1-m <- 1-2+m (staggered) or m
+                        src = (m - 1) if stag else m
+                        a[..., g - m] = s * a[..., g + src - 1]
+                    else:          # ghost n+m <- n-m (staggered) or n+1-m
+                        src = (n - m) if stag else (n + 1 - m)
+                        a[..., g + n + m - 1] = s * a[..., g + src - 1]
+                if stag:
+                    a[..., g - 1 if side == 0 else g + n - 1] = 0.0
+    return u, v, w
+
+
+def momentum_state(case: Case, ghost=3, rho_12=1e-3, mu_12=1e-2, amplitude=0.1, seed=None):
+    """Seeded synthetic state of one Adams-Bashforth momentum step, every array
+    on the reference's ghost-padded box: the old level set phi (signed distance
+    to the case's bubbles) and from it heavy/delta (ls_funs with half width
+    eps), rho = H + rho_12 (1 - H), mu = H + mu_12 (1 - H), unit normals and
+    their divergence (curvature) by central differences; a smooth old
+    velocity (a few random Fourier modes, velbc no-slip applied) and a smooth
+    old source velsrc%old.  Returns a dict of float64 arrays plus 'rho_now'
+    (the interior density of the same phi, for the pressure operator)."""
+    rng = np.random.default_rng(case.seed + 17 if seed is None else seed)
+    nz, ny, nx = case.shape
+    dx, dy, dz = case.spacing
+    g = ghost
+    three = nz > 1
+    ps = padded_shape(case.shape, g)
+    xs = (np.arange(nx + 2 * g) - g + 0.5) * dx
+    ys = (np.arange(ny + 2 * g) - g + 0.5) * dy
+    if three:
+        zs = (np.arange(nz + 2 * g) - g + 0.5) * dz
+        Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    else:
+        Y, X = np.meshgrid(ys, xs, indexing="ij")
+        Z = np.full(X.shape, 0.5 * case.extent[2])
+    phi = np.full(Z.shape, np.inf)
+    for c, r in zip(case.centers, case.radii):
+        d2 = (X - c[0]) ** 2 + (Y - c[1]) ** 2
+        if three:
+            d2 = d2 + (Z - c[2]) ** 2
+        np.minimum(phi, np.sqrt(d2) - r, out=phi)
+    # negative inside the bubbles: phi > 0 is the heavy fluid 1 of the reference
+    eps = case.eps
+    x = phi / eps
+    heavy = np.where(x > 1 - 1e-12, 1.0, np.where(x < -1 + 1e-12, 0.0,
+                                                 0.5 * (1.0 + x + np.sin(np.pi * x) / np.pi)))
+    delta = np.where(np.abs(x) < 1 - 1e-12, 0.5 * (1.0 + np.cos(np.pi * x)) / eps, 0.0)
+    heavy = np.clip(heavy, 0.0, 1.0)
+    rho = heavy + rho_12 * (1.0 - heavy)
+    mu = heavy + mu_12 * (1.0 - heavy)
+    grads = np.gradient(phi, *((dz, dy, dx) if three else (dy, dx)))
+    mag = np.sqrt(sum(gr * gr for gr in grads)) + 1e-12
+    nrm = [gr / mag for gr in grads]  # (z, y, x) or (y, x) order
+    curv = sum(np.gradient(nrm[a], (dz, dy, dx)[a] if three else (dy, dx)[a], axis=a)
+               for a in range(len(nrm)))
+    nrm_x, nrm_y = nrm[-1], nrm[-2]
+    nrm_z = nrm[0] if three else None
+
+    def smooth():
+        f = np.zeros(Z.shape)
+        for _ in range(4):
+            kx, ky, kz = rng.integers(1, 4, size=3)
+            ph = rng.uniform(0, 2 * np.pi, size=3)
+            f += rng.standard_normal() * (np.sin(kx * np.pi * X + ph[0])
+                                          * np.sin(ky * np.pi * Y + ph[1])
+                                          * (np.sin(kz * np.pi * Z + ph[2]) if three else 1.0))
+        return amplitude * f
+
+    u, v = smooth(), smooth()
+    w = smooth() if three else None
+    bc = (1, 1, 1, 1, 1, 1)
+    velbc_numpy(u, v, w, g, bc)
+    su, sv = smooth(), smooth()
+    sw = smooth() if three else None
+    sl = (slice(g, g + nz),) if three else ()
+    rho_now = rho[sl + (slice(g, g + ny), slice(g, g + nx))].reshape(case.shape).copy()
+    out = dict(u=u, v=v, w=w, su_old=su, sv_old=sv, sw_old=sw, rho=rho, mu=mu, delta=delta,
+               phi=phi, nrm_x=nrm_x, nrm_y=nrm_y, nrm_z=nrm_z, curv=curv, rho_now=rho_now,
+               p=np.zeros(case.shape))
+    for k, a in out.items():
+        if a is not None:
+            out[k] = np.ascontiguousarray(a, np.float64)
+            assert k in ("rho_now", "p") or out[k].shape == ps, (k, out[k].shape, ps)
+    return out

@@ -1308,3 +1308,430 @@ int or_ls_redistance(const or_grid* g, double* phi, double ls_wid, double rdt, d
   free(s); free(grad); free(s1); free(s2); free(s3); free(l1); free(l2); free(tmp);
   return iter;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Momentum step of the Adams-Bashforth solver (NO2/NO3 src/ns_solver/        */
+/* admas_bashforth_solver.f90: ns_ab_solver_SOR, ns_ab_setup,                */
+/* ns_ab_predictor; ns_ab_adv.f90: ns_ab_adv_source_sec; ns_ab_diff.f90:     */
+/* sec_part1..3; ns_solvers.f90: ns_linearize, ns_check_convergence_vel;     */
+/* src/others/bcs.f90: velbc, find_stag_vel).                                 */
+/*                                                                           */
+/* These arrays keep the reference's ghost cells: every array is the padded  */
+/* box of the reference, (nx+2g)(ny+2g)(nz+2g) (2D: (nx+2g)(ny+2g)), C order  */
+/* (z, y, x), and element (i, j, k) in the reference's 1-based indices sits   */
+/* at ((k-1+gz)(ny+2g) + j-1+g)(nx+2g) + i-1+g with gz = g in 3D, 0 in 2D.    */
+/* u(i,j,k) is the x-face i+1/2 of cell (i,j,k), v and w likewise.  Every     */
+/* expression keeps the reference's operand order, and the file is built     */
+/* without contraction, so each result is the reference's double rounding.   */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int32_t ghost;       /* g, >= 2 */
+  int32_t bc[6];       /* velbc: ubc(1), ubc(2), vbc(1), vbc(2), wbc(1), wbc(2) */
+  int32_t iterations;  /* predictor-projection passes (the reference: 4) */
+  double dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf, p_tol;
+} or_ns_params;
+
+typedef struct {
+  int nx, ny, nz, g, gz;
+  size_t px, py;
+} ns_box;
+
+static ns_box ns_box_of(const or_grid* gr, int g) {
+  ns_box b;
+  b.nx = gr->nx; b.ny = gr->ny; b.nz = gr->nz; b.g = g;
+  b.gz = gr->nz > 1 ? g : 0;
+  b.px = (size_t)gr->nx + 2 * (size_t)g;
+  b.py = (size_t)gr->ny + 2 * (size_t)g;
+  return b;
+}
+
+static inline size_t NI(const ns_box* b, int i, int j, int k) {
+  return ((size_t)(k - 1 + b->gz) * b->py + (size_t)(j - 1 + b->g)) * b->px + (size_t)(i - 1 + b->g);
+}
+
+static size_t ns_span(const ns_box* b) {
+  return b->px * b->py * (b->nz > 1 ? (size_t)b->nz + 2 * (size_t)b->g : 1);
+}
+
+/* velsrc%tmp: the diffusion, interface-viscosity, gravity and surface-tension
+ * terms (sec_part1 + sec_part2 + sec_part3, NO2 ns_ab_diff.f90:10-135, NO3
+ * :10-199) from the old fields.  The surface-tension term is added only when
+ * btn_sf != 0 (the reference computes the curvature only then, ns_solvers.f90
+ * ns_init); nrm and curv may be NULL otherwise. */
+void or_ns_diffusion(const or_grid* gr, const or_ns_params* prm, const double* U, const double* V,
+                     const double* W, const double* R, const double* M, const double* D,
+                     const double* P, const double* N1, const double* N2, const double* N3,
+                     const double* CV, double* TU, double* TV, double* TW) {
+  const ns_box b = ns_box_of(gr, prm->ghost);
+  const int three = gr->nz > 1;
+  const double dx = gr->dx, dy = gr->dy, dz = gr->dz;
+  const double dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
+  const double re = prm->re, c1 = 1.0 - prm->mu_12;
+  const int sf = prm->btn_sf != 0.0;
+  const size_t sx = 1, sy = b.px, sz = b.px * b.py;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= gr->nz; ++k)
+    for (int j = 1; j <= gr->ny; ++j)
+      for (int i = 1; i <= gr->nx; ++i) {
+        const size_t q = NI(&b, i, j, k);
+        double rho, mu, delta, curv, xx, yy, zz, t;
+        double ux, uy, uz, vx, vy, vz, wx, wy, wz, phix, phiy, phiz, dxx, dyy, dzz;
+        /* ---- x: u at (i+1/2, j, k) ---- */
+        rho = 0.5 * (R[q] + R[q + sx]);
+        mu = 0.5 * (M[q] + M[q + sx]);
+        xx = ((U[q + sx] - 2.0 * U[q]) + U[q - sx]) / dx2;
+        yy = ((U[q + sy] - 2.0 * U[q]) + U[q - sy]) / dy2;
+        t = ((mu / rho) * xx) / re + ((mu / rho) * yy) / re;
+        if (three) {
+          zz = ((U[q + sz] - 2.0 * U[q]) + U[q - sz]) / dz2;
+          t = t + ((mu / rho) * zz) / re;
+        }
+        delta = 0.5 * (D[q] + D[q + sx]);
+        ux = 0.5 * (U[q + sx] - U[q - sx]) / dx;
+        uy = 0.5 * (U[q + sy] - U[q - sy]) / dy;
+        vx = 0.5 * (((V[q + sx] - V[q]) + V[q + sx - sy]) - V[q - sy]) / dx;
+        phix = (P[q + sx] - P[q]) / dx;
+        phiy = 0.25 * (((P[q + sx + sy] - P[q + sx - sy]) + P[q + sy]) - P[q - sy]) / dy;
+        dxx = c1 * delta * phix * 2.0 * ux / (rho * re);
+        dyy = c1 * delta * phiy * (uy + vx) / (rho * re);
+        t = (t + dxx) + dyy;
+        if (three) {
+          uz = 0.5 * (U[q + sz] - U[q - sz]) / dz;
+          wx = 0.5 * (((W[q + sx] - W[q]) + W[q + sx - sz]) - W[q - sz]) / dx;
+          phiz = 0.25 * (((P[q + sx + sz] - P[q + sx - sz]) + P[q + sz]) - P[q - sz]) / dz;
+          dzz = c1 * delta * phiz * (uz + wx) / (rho * re);
+          t = t + dzz;
+        }
+        t = t + prm->gx * prm->btn_g / prm->fr;
+        if (sf) {
+          curv = (CV[q] + CV[q + sx]) / 2.0;
+          phix = 0.5 * (N1[q] + N1[q + sx]);
+          t = t - prm->btn_sf * curv * delta * phix / (prm->we * rho);
+        }
+        TU[q] = t;
+        /* ---- y: v at (i, j+1/2, k) ---- */
+        rho = 0.5 * (R[q] + R[q + sy]);
+        mu = 0.5 * (M[q] + M[q + sy]);
+        xx = ((V[q + sx] - 2.0 * V[q]) + V[q - sx]) / dx2;
+        yy = ((V[q + sy] - 2.0 * V[q]) + V[q - sy]) / dy2;
+        t = ((mu / rho) * xx) / re + ((mu / rho) * yy) / re;
+        if (three) {
+          zz = ((V[q + sz] - 2.0 * V[q]) + V[q - sz]) / dz2;
+          t = t + ((mu / rho) * zz) / re;
+        }
+        delta = 0.5 * (D[q] + D[q + sy]);
+        vx = 0.5 * (V[q + sx] - V[q - sx]) / dx;
+        vy = 0.5 * (V[q + sy] - V[q - sy]) / dy;
+        uy = 0.5 * (((U[q + sy] - U[q]) + U[q - sx + sy]) - U[q - sx]) / dy;
+        phix = 0.25 * (((P[q + sx] - P[q - sx]) + P[q + sx + sy]) - P[q - sx + sy]) / dx;
+        phiy = (P[q + sy] - P[q]) / dy;
+        dxx = c1 * delta * phix * (uy + vx) / (rho * re);
+        dyy = c1 * delta * phiy * 2.0 * vy / (rho * re);
+        t = (t + dxx) + dyy;
+        if (three) {
+          vz = 0.5 * (V[q + sz] - V[q - sz]) / dz;
+          wy = 0.5 * (((W[q + sy] - W[q]) + W[q + sy - sz]) - W[q - sz]) / dy;
+          phiz = 0.25 * (((P[q + sy + sz] - P[q + sy - sz]) + P[q + sz]) - P[q - sz]) / dz;
+          dzz = c1 * delta * phiz * (wy + vz) / (rho * re);
+          t = t + dzz;
+        }
+        t = t + prm->gy * prm->btn_g / prm->fr;
+        if (sf) {
+          curv = (CV[q] + CV[q + sy]) / 2.0;
+          phiy = 0.5 * (N2[q] + N2[q + sy]);
+          t = t - prm->btn_sf * curv * delta * phiy / (prm->we * rho);
+        }
+        TV[q] = t;
+        if (!three) continue;
+        /* ---- z: w at (i, j, k+1/2) ---- */
+        rho = 0.5 * (R[q] + R[q + sz]);
+        mu = 0.5 * (M[q] + M[q + sz]);
+        xx = ((W[q + sx] - 2.0 * W[q]) + W[q - sx]) / dx2;
+        yy = ((W[q + sy] - 2.0 * W[q]) + W[q - sy]) / dy2;
+        zz = ((W[q + sz] - 2.0 * W[q]) + W[q - sz]) / dz2;
+        t = (((mu / rho) * xx) / re + ((mu / rho) * yy) / re) + ((mu / rho) * zz) / re;
+        delta = 0.5 * (D[q] + D[q + sz]);
+        wx = 0.5 * (W[q + sx] - W[q - sx]) / dx;
+        wy = 0.5 * (W[q + sy] - W[q - sy]) / dy;
+        wz = 0.5 * (W[q + sz] - W[q - sz]) / dz;
+        uz = 0.5 * (((U[q + sz] - U[q]) + U[q - sx + sz]) - U[q - sx]) / dz;
+        vz = 0.5 * (((V[q + sz] - V[q]) + V[q - sy + sz]) - V[q - sy]) / dz;
+        phix = 0.25 * (((P[q + sx + sz] - P[q - sx + sz]) + P[q + sx]) - P[q - sx]) / dx;
+        phiy = 0.25 * (((P[q + sy + sz] - P[q - sy + sz]) + P[q + sy]) - P[q - sy]) / dy;
+        phiz = (P[q + sz] - P[q]) / dz;
+        dxx = c1 * delta * phix * (uz + wx) / (rho * re);
+        dyy = c1 * delta * phiy * (vz + wy) / (rho * re);
+        dzz = c1 * delta * phiz * 2.0 * wz / (rho * re);
+        t = ((t + dxx) + dyy) + dzz;
+        t = t + prm->gz * prm->btn_g / prm->fr;
+        if (sf) {
+          curv = (CV[q] + CV[q + sz]) / 2.0;
+          phiz = 0.5 * (N3[q] + N3[q + sz]);
+          t = t - prm->btn_sf * curv * delta * phiz / (prm->we * rho);
+        }
+        TW[q] = t;
+      }
+}
+
+/* One predictor pass after ns_linearize (vel%tmp = the advecting velocity Ut,
+ * Vt, Wt): find_stag_vel's four-point averages of the other components at
+ * each face (bcs.f90), the second-order upwind advection of the old velocity
+ * (ns_ab_adv_source_sec, NO2 ns_ab_adv.f90:1-46, NO3 :1-73),
+ * velsrc%now = advection + velsrc%tmp (ns_ab_setup) and the AB2 predictor
+ * vel%now = vel%old + dt (1.5 velsrc%now - 0.5 velsrc%old) (ns_ab_predictor)
+ * over the reference's interior loops i = 1..nx etc. (which include the high
+ * wall face; velbc zeroes it).  Ghosts are not written. */
+static inline double ns_upwind(double a, double m, double p) {
+  return (a + fabs(a)) * m + (a - fabs(a)) * p;
+}
+
+void or_ns_advance(const or_grid* gr, const or_ns_params* prm, const double* U, const double* V,
+                   const double* W, const double* Ut, const double* Vt, const double* Wt,
+                   const double* TU, const double* TV, const double* TW, const double* SUo,
+                   const double* SVo, const double* SWo, double* SU, double* SV, double* SW,
+                   double* Un, double* Vn, double* Wn) {
+  const ns_box b = ns_box_of(gr, prm->ghost);
+  const int three = gr->nz > 1;
+  const double dx = gr->dx, dy = gr->dy, dz = gr->dz, dt = prm->dt;
+  const size_t sx = 1, sy = b.px, sz = b.px * b.py;
+  const double* F[3] = {U, V, W};
+  double* S[3] = {SU, SV, SW};
+  double* O[3] = {Un, Vn, Wn};
+  const double* T[3] = {TU, TV, TW};
+  const double* SO[3] = {SUo, SVo, SWo};
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= gr->nz; ++k)
+    for (int j = 1; j <= gr->ny; ++j)
+      for (int i = 1; i <= gr->nx; ++i) {
+        const size_t q = NI(&b, i, j, k);
+        for (int c = 0; c < (three ? 3 : 2); ++c) {
+          double a[3];
+          if (c == 0) {
+            a[0] = Ut[q];
+            a[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sx]) + Vt[q + sx - sy]);
+            if (three) a[2] = 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sx]) + Wt[q + sx - sz]);
+          } else if (c == 1) {
+            a[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sy]) + Ut[q - sx + sy]);
+            a[1] = Vt[q];
+            if (three) a[2] = 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sy]) + Wt[q + sy - sz]);
+          } else {
+            a[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sz]) + Ut[q - sx + sz]);
+            a[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sz]) + Vt[q - sy + sz]);
+            a[2] = Wt[q];
+          }
+          const double* f = F[c];
+          const size_t st[3] = {sx, sy, sz};
+          const double h[3] = {dx, dy, dz};
+          double src = 0.0;
+          for (int d = 0; d < (three ? 3 : 2); ++d) {
+            const size_t s = st[d];
+            const double fp = 0.5 * ((-f[q + 2 * s] + 4.0 * f[q + s]) - 3.0 * f[q]) / h[d];
+            const double fm = 0.5 * ((f[q - 2 * s] - 4.0 * f[q - s]) + 3.0 * f[q]) / h[d];
+            const double term = ns_upwind(a[d], fm, fp) / 2.0;
+            src = d == 0 ? -term : src - term;
+          }
+          src = src + T[c][q];
+          S[c][q] = src;
+          O[c][q] = F[c][q] + dt * (1.5 * src - 0.5 * SO[c][q]);
+        }
+      }
+}
+
+/* velbc (NO2 bcs.f90:28-132, NO3 :44-257): for each wall with bc 1 (no-slip)
+ * or 2 (slip) the g ghost layers mirror the interior, negated for no-slip;
+ * the normal component's wall face is set to 0.  Passes in the reference's
+ * order: x (low, high), then y, then z, each over the whole padded extent of
+ * the other axes.  Other bc values leave that wall's ghosts. */
+void or_velbc(const or_grid* gr, int g, const int32_t bc[6], double* U, double* V, double* W) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  const int nx = gr->nx, ny = gr->ny, nz = gr->nz;
+  const int k0 = three ? 1 - g : 1, k1 = three ? nz + g : 1;
+  double* F[3] = {U, V, W};
+  const int nc = three ? 3 : 2;
+  /* x */
+  for (int side = 0; side < 2; ++side) {
+    const int t = bc[side];
+    if (t != 1 && t != 2) continue;
+    for (int k = k0; k <= k1; ++k)
+      for (int j = 1 - g; j <= ny + g; ++j) {
+        for (int m = 1; m <= g; ++m)
+          for (int c = 0; c < nc; ++c) {
+            double* f = F[c];
+            if (side == 0) {
+              const int src = c == 0 ? 1 - 2 + m : 1 - 1 + m;
+              const double v = f[NI(&b, src, j, k)];
+              f[NI(&b, 1 - m, j, k)] = t == 1 ? -v : v;
+            } else {
+              const int src = c == 0 ? nx - m : nx + 1 - m;
+              const double v = f[NI(&b, src, j, k)];
+              f[NI(&b, nx + m, j, k)] = t == 1 ? -v : v;
+            }
+          }
+        U[NI(&b, side == 0 ? 0 : nx, j, k)] = 0.0;
+      }
+  }
+  /* y */
+  for (int side = 0; side < 2; ++side) {
+    const int t = bc[2 + side];
+    if (t != 1 && t != 2) continue;
+    for (int k = k0; k <= k1; ++k)
+      for (int i = 1 - g; i <= nx + g; ++i) {
+        for (int m = 1; m <= g; ++m)
+          for (int c = 0; c < nc; ++c) {
+            double* f = F[c];
+            if (side == 0) {
+              const int src = c == 1 ? 1 - 2 + m : 1 - 1 + m;
+              const double v = f[NI(&b, i, src, k)];
+              f[NI(&b, i, 1 - m, k)] = t == 1 ? -v : v;
+            } else {
+              const int src = c == 1 ? ny - m : ny + 1 - m;
+              const double v = f[NI(&b, i, src, k)];
+              f[NI(&b, i, ny + m, k)] = t == 1 ? -v : v;
+            }
+          }
+        V[NI(&b, i, side == 0 ? 0 : ny, k)] = 0.0;
+      }
+  }
+  if (!three) return;
+  /* z */
+  for (int side = 0; side < 2; ++side) {
+    const int t = bc[4 + side];
+    if (t != 1 && t != 2) continue;
+    for (int j = 1 - g; j <= ny + g; ++j)
+      for (int i = 1 - g; i <= nx + g; ++i) {
+        for (int m = 1; m <= g; ++m)
+          for (int c = 0; c < 3; ++c) {
+            double* f = F[c];
+            if (side == 0) {
+              const int src = c == 2 ? 1 - 2 + m : 1 - 1 + m;
+              const double v = f[NI(&b, i, j, src)];
+              f[NI(&b, i, j, 1 - m)] = t == 1 ? -v : v;
+            } else {
+              const int src = c == 2 ? nz - m : nz + 1 - m;
+              const double v = f[NI(&b, i, j, src)];
+              f[NI(&b, i, j, nz + m)] = t == 1 ? -v : v;
+            }
+          }
+        W[NI(&b, i, j, side == 0 ? 0 : nz)] = 0.0;
+      }
+  }
+}
+
+/* linf and l2f of vel%now - vel%tmp over the interior loops
+ * (ns_check_convergence_vel, NO2 ns_solvers.f90:85-116, NO3 :92-126):
+ * l2f = sqrt(sum / (2 nx ny)) in 2D, sqrt(sum / (3 nx ny nz)) in 3D. */
+void or_ns_vel_change(const or_grid* gr, int g, const double* Un, const double* Vn,
+                      const double* Wn, const double* Ut, const double* Vt, const double* Wt,
+                      double* linf, double* l2f) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  double mx = 0.0, s = 0.0;
+  for (int k = 1; k <= gr->nz; ++k)
+    for (int j = 1; j <= gr->ny; ++j)
+      for (int i = 1; i <= gr->nx; ++i) {
+        const size_t q = NI(&b, i, j, k);
+        const double du = Un[q] - Ut[q], dv = Vn[q] - Vt[q];
+        mx = fmax(mx, fabs(du));
+        mx = fmax(mx, fabs(dv));
+        if (three) mx = fmax(mx, fabs(Wn[q] - Wt[q]));
+        s = s + du * du;
+        s = s + dv * dv;
+        if (three) s = s + (Wn[q] - Wt[q]) * (Wn[q] - Wt[q]);
+      }
+  *linf = mx;
+  *l2f = three ? sqrt(s / (3.0 * gr->nx * gr->ny * gr->nz)) : sqrt(s / (2.0 * gr->nx * gr->ny));
+}
+
+/* The pressure step inside the loop: ppe_sor_solver + ns_momentum_correction
+ * on the padded velocity (faces 0..n of each axis), with the multigrid of this
+ * file in place of the point relaxation; then velbc. */
+static int ns_project(const or_grid* gr, const or_ns_params* prm, const double* rho,
+                      const double* cx, const double* cy, const double* cz, double* Un, double* Vn,
+                      double* Wn, double* p, const or_mg_params* mgp, or_mg_stats* st) {
+  const ns_box b = ns_box_of(gr, prm->ghost);
+  const int three = gr->nz > 1;
+  const int nx = gr->nx, ny = gr->ny, nz = gr->nz;
+  const size_t n = cells_of(nx, ny, nz);
+  double* u = dalloc((size_t)(nx + 1) * ny * nz);
+  double* v = dalloc((size_t)nx * (ny + 1) * nz);
+  double* w = three ? dalloc((size_t)nx * ny * (nz + 1)) : NULL;
+  double* rhs = dalloc(n);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int f = 0; f <= nx; ++f) u[((size_t)k * ny + j) * (nx + 1) + f] = Un[NI(&b, f, j + 1, k + 1)];
+  for (int k = 0; k < nz; ++k)
+    for (int f = 0; f <= ny; ++f)
+      for (int i = 0; i < nx; ++i) v[((size_t)k * (ny + 1) + f) * nx + i] = Vn[NI(&b, i + 1, f, k + 1)];
+  if (three)
+    for (int f = 0; f <= nz; ++f)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) w[((size_t)f * ny + j) * nx + i] = Wn[NI(&b, i + 1, j + 1, f)];
+  or_divergence(gr, u, v, w, prm->dt, 1, rhs);
+  const int rc = or_mg_solve(gr, cx, cy, cz, rhs, p, prm->p_tol, mgp, st);
+  or_correct(gr, rho, p, prm->dt, u, v, w);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int f = 1; f < nx; ++f) Un[NI(&b, f, j + 1, k + 1)] = u[((size_t)k * ny + j) * (nx + 1) + f];
+  for (int k = 0; k < nz; ++k)
+    for (int f = 1; f < ny; ++f)
+      for (int i = 0; i < nx; ++i) Vn[NI(&b, i + 1, f, k + 1)] = v[((size_t)k * (ny + 1) + f) * nx + i];
+  if (three)
+    for (int f = 1; f < nz; ++f)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) Wn[NI(&b, i + 1, j + 1, f)] = w[((size_t)f * ny + j) * nx + i];
+  free(u);
+  free(v);
+  free(w);
+  free(rhs);
+  or_velbc(gr, prm->ghost, prm->bc, Un, Vn, Wn);
+  return rc;
+}
+
+/* ns_ab_solver_SOR after ppe_sor_init (admas_bashforth_solver.f90:39-67):
+ * velsrc%tmp once (it depends on the old fields only), then `iterations`
+ * passes of ns_linearize, ns_ab_setup, ns_ab_predictor (+ velbc) and the
+ * pressure step, then ns_check_convergence_vel.  rho is the new cell density
+ * (compact) of the pressure operator; p the compact pressure (warm start in,
+ * result out); the velocity, source and old fields are padded.  Returns the
+ * worst solve status; cycles (may be NULL) receives the total cycles. */
+int or_ns_ab_step(const or_grid* gr, const or_ns_params* prm, const double* rho, double* Un,
+                  double* Vn, double* Wn, const double* U, const double* V, const double* W,
+                  double* SU, double* SV, double* SW, const double* SUo, const double* SVo,
+                  const double* SWo, const double* R, const double* M, const double* D,
+                  const double* P, const double* N1, const double* N2, const double* N3,
+                  const double* CV, double* p, const or_mg_params* mgp, double* linf,
+                  double* l2f, int32_t* cycles) {
+  const ns_box b = ns_box_of(gr, prm->ghost);
+  const int three = gr->nz > 1;
+  const size_t span = ns_span(&b), n = cells_of(gr->nx, gr->ny, gr->nz);
+  double* T[3] = {dalloc(span), dalloc(span), three ? dalloc(span) : NULL};
+  double* Tm[3] = {dalloc(span), dalloc(span), three ? dalloc(span) : NULL};
+  double* cx = dalloc(n);
+  double* cy = dalloc(n);
+  double* cz = dalloc(n);
+  or_face_coef(gr, rho, cx, cy, cz);
+  or_ns_diffusion(gr, prm, U, V, W, R, M, D, P, N1, N2, N3, CV, T[0], T[1], T[2]);
+  double* Nw[3] = {Un, Vn, Wn};
+  int worst = OR_OK, total = 0;
+  for (int it = 0; it < prm->iterations; ++it) {
+    for (int c = 0; c < (three ? 3 : 2); ++c) memcpy(Tm[c], Nw[c], span * sizeof(double));
+    or_ns_advance(gr, prm, U, V, W, Tm[0], Tm[1], Tm[2], T[0], T[1], T[2], SUo, SVo, SWo, SU, SV,
+                  SW, Un, Vn, Wn);
+    or_velbc(gr, prm->ghost, prm->bc, Un, Vn, Wn);
+    or_mg_stats st;
+    const int rc = ns_project(gr, prm, rho, cx, cy, cz, Un, Vn, Wn, p, mgp, &st);
+    total += st.cycles;
+    if (rc > worst) worst = rc;
+  }
+  or_ns_vel_change(gr, prm->ghost, Un, Vn, Wn, Tm[0], Tm[1], Tm[2], linf, l2f);
+  if (cycles) *cycles = total;
+  for (int c = 0; c < 3; ++c) {
+    free(T[c]);
+    free(Tm[c]);
+  }
+  free(cx);
+  free(cy);
+  free(cz);
+  return worst;
+}

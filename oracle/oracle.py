@@ -37,6 +37,14 @@ class MGStats(C.Structure):
                 ("rms_residual", C.c_double), ("history", C.c_double * 256)]
 
 
+class NSParams(C.Structure):
+    _fields_ = [("ghost", C.c_int32), ("bc", C.c_int32 * 6), ("iterations", C.c_int32),
+                ("dt", C.c_double), ("re", C.c_double), ("fr", C.c_double), ("we", C.c_double),
+                ("mu_12", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
+                ("gz", C.c_double), ("btn_g", C.c_double), ("btn_sf", C.c_double),
+                ("p_tol", C.c_double)]
+
+
 _D = C.POINTER(C.c_double)
 
 
@@ -80,6 +88,14 @@ def lib():
         L.or_ls_redistance.argtypes = [C.POINTER(Grid), _D, C.c_double, C.c_double, C.c_double,
                                        C.c_int, C.c_int, _D]
         L.or_ls_redistance.restype = C.c_int
+        _G, _N = C.POINTER(Grid), C.POINTER(NSParams)
+        L.or_ns_diffusion.argtypes = [_G, _N] + [_D] * 14
+        L.or_ns_advance.argtypes = [_G, _N] + [_D] * 18
+        L.or_velbc.argtypes = [_G, C.c_int, C.POINTER(C.c_int32), _D, _D, _D]
+        L.or_ns_vel_change.argtypes = [_G, C.c_int] + [_D] * 8
+        L.or_ns_ab_step.argtypes = ([_G, _N] + [_D] * 22
+                                    + [C.POINTER(MGParams), _D, _D, C.POINTER(C.c_int32)])
+        L.or_ns_ab_step.restype = C.c_int
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -299,3 +315,112 @@ def set_threads(n):
 
 def num_threads():
     return lib().or_num_threads()
+
+
+# --------------------------------------------------------------------------
+# Momentum step (admas_bashforth_solver.f90 and its callees).  These arrays
+# keep the reference's g ghost layers: padded shape (nz+2g, ny+2g, nx+2g) in 3D,
+# (ny+2g, nx+2g) in 2D; element (i, j, k) of the reference's 1-based indices
+# at [k-1+g, j-1+g, i-1+g]; u[.., .., i] is the face i+1/2.
+# --------------------------------------------------------------------------
+NS_OLD = ("u", "v", "w", "rho", "mu", "delta", "phi", "nrm_x", "nrm_y", "nrm_z", "curv")
+
+
+def ns_params(ghost=3, bc=(1, 1, 1, 1, 1, 1), iterations=4, dt=1e-3, re=1000.0, fr=1.0, we=1.0,
+              mu_12=1e-2, gravity=(0.0, -1.0, 0.0), btn_g=1.0, btn_sf=0.0, p_tol=1e-10):
+    return NSParams(int(ghost), (C.c_int32 * 6)(*[int(b) for b in bc]), int(iterations),
+                    float(dt), float(re), float(fr), float(we), float(mu_12),
+                    float(gravity[0]), float(gravity[1]), float(gravity[2]), float(btn_g),
+                    float(btn_sf), float(p_tol))
+
+
+def padded_shape(shape, ghost):
+    nz, ny, nx = shape
+    if nz == 1:
+        return (ny + 2 * ghost, nx + 2 * ghost)
+    return (nz + 2 * ghost, ny + 2 * ghost, nx + 2 * ghost)
+
+
+def _pad(a, shape, ghost, name):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, np.float64)
+    if a.shape != padded_shape(shape, ghost):
+        raise ValueError(f"{name}: expected {padded_shape(shape, ghost)}, got {a.shape}")
+    return a
+
+
+def _three(shape):
+    return shape[0] > 1
+
+
+def ns_diffusion(shape, spacing, prm, old):
+    """velsrc%tmp of sec_part1..3 from the old fields (dict with NS_OLD keys;
+    the normals and curv only needed when btn_sf != 0).  Returns (tu, tv, tw)."""
+    g = grid(shape, spacing)
+    G = prm.ghost
+    f = {k: _pad(old.get(k), shape, G, k) for k in NS_OLD}
+    if not _three(shape):
+        f["w"] = f["nrm_z"] = None
+    out = [np.zeros(padded_shape(shape, G)) for _ in range(3 if _three(shape) else 2)]
+    tw = out[2] if _three(shape) else None
+    lib().or_ns_diffusion(C.byref(g), C.byref(prm), *[_p(f[k]) for k in NS_OLD],
+                          _p(out[0]), _p(out[1]), _p(tw))
+    return out[0], out[1], tw
+
+
+def ns_advance(shape, spacing, prm, old_vel, tmp_vel, diff, src_old):
+    """One predictor pass: returns (src_now, vel_now) as tuples of padded arrays
+    (vel_now's ghosts are copies of the old velocity's; velbc is separate)."""
+    g = grid(shape, spacing)
+    G = prm.ghost
+    nc = 3 if _three(shape) else 2
+
+    def tri(t, name):
+        t = list(t) + [None] * (3 - len(t))
+        return [_pad(t[c], shape, G, name) if c < nc else None for c in range(3)]
+
+    o, t, d, so = tri(old_vel, "old"), tri(tmp_vel, "tmp"), tri(diff, "diff"), tri(src_old, "src")
+    src = [np.zeros(padded_shape(shape, G)) if c < nc else None for c in range(3)]
+    vel = [o[c].copy() if c < nc else None for c in range(3)]
+    lib().or_ns_advance(C.byref(g), C.byref(prm), *[_p(a) for a in o + t + d + so + src + vel])
+    return tuple(src[:nc]), tuple(vel[:nc])
+
+
+def velbc(shape, prm, u, v, w=None):
+    """velbc in place on padded arrays."""
+    g = grid(shape, (1.0, 1.0, 1.0))
+    for a in (u, v) + ((w,) if _three(shape) else ()):
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().or_velbc(C.byref(g), int(prm.ghost), prm.bc, _p(u), _p(v),
+                   _p(w) if _three(shape) else None)
+
+
+def ns_ab_step(shape, spacing, prm, rho_now, vel, old, src_old, p, **mg_kw):
+    """ns_ab_solver_SOR after ppe_sor_init.  vel: (u, v[, w]) padded vel%now
+    (start of the linearisation); old: dict of the old padded fields (NS_OLD);
+    src_old: velsrc%old; rho_now: compact new density (nz, ny, nx) of the
+    pressure operator; p: compact warm start.  Returns a dict with u, v, w,
+    su, sv, sw (padded), p, linf, l2f, cycles and status."""
+    g = grid(shape, spacing)
+    G = prm.ghost
+    nc = 3 if _three(shape) else 2
+    vel = [np.array(_pad(vel[c], shape, G, "vel"), copy=True) if c < nc else None
+           for c in range(3)]
+    f = {k: _pad(old.get(k), shape, G, k) for k in NS_OLD}
+    so = [_pad(src_old[c], shape, G, "src_old") if c < nc else None for c in range(3)]
+    if nc == 2:
+        f["w"] = f["nrm_z"] = None
+    src = [np.zeros(padded_shape(shape, G)) if c < nc else None for c in range(3)]
+    pp = np.array(np.asarray(p, np.float64).reshape(shape), copy=True, order="C")
+    rho = np.ascontiguousarray(np.asarray(rho_now, np.float64).reshape(shape))
+    mgp = mg_params(**mg_kw)
+    linf, l2f, cyc = C.c_double(), C.c_double(), C.c_int32()
+    st = lib().or_ns_ab_step(C.byref(g), C.byref(prm), _p(rho), *[_p(a) for a in vel],
+                             *[_p(f[k]) for k in ("u", "v", "w")], *[_p(a) for a in src],
+                             *[_p(a) for a in so],
+                             *[_p(f[k]) for k in ("rho", "mu", "delta", "phi", "nrm_x", "nrm_y",
+                                                  "nrm_z", "curv")],
+                             _p(pp), C.byref(mgp), C.byref(linf), C.byref(l2f), C.byref(cyc))
+    return {"u": vel[0], "v": vel[1], "w": vel[2], "su": src[0], "sv": src[1], "sw": src[2],
+            "p": pp, "linf": linf.value, "l2f": l2f.value, "cycles": cyc.value, "status": st}

@@ -750,3 +750,305 @@ def level_set_rk3_redis(phi, ls_wid, rdt, dx, dy, dz, rho_12=1e-3, btn=1, max_it
         if time > timestop or error <= tol:
             break
     return np.ascontiguousarray(np.transpose(P[inner], (2, 1, 0))), it, error
+
+
+# ---------------------------------------------------------------------------
+# Momentum step of the Adams-Bashforth solver, literally:
+#   ns_ab_adv_source_sec  "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ab_adv.f90:1-46"
+#                         (3D: ".../3D+IBM/src/ns_solver/ns_ab_adv.f90:1-73")
+#   sec_part1..3          ".../2D/src/ns_solver/ns_ab_diff.f90:10-135" (3D :10-199)
+#   ns_ab_setup, ns_ab_predictor
+#                         ".../2D/src/ns_solver/admas_bashforth_solver.f90:19-93"
+#   find_stag_vel, velbc  ".../2D/src/others/bcs.f90:28-132,265-287" (3D :44-257,464-495)
+# Arrays are the reference's ghost-padded boxes (numpy shape (ny+2g, nx+2g) or
+# (nz+2g, ny+2g, nx+2g)); R[i, j(, k)] reads them with the Fortran indices.
+# ---------------------------------------------------------------------------
+class R:
+    def __init__(self, a, g):
+        self.a, self.g, self.three = a, g, a.ndim == 3
+
+    def _ix(self, ijk):
+        g = self.g
+        if self.three:
+            i, j, k = ijk
+            return (k - 1 + g, j - 1 + g, i - 1 + g)
+        i, j = ijk
+        return (j - 1 + g, i - 1 + g)
+
+    def __getitem__(self, ijk):
+        return float(self.a[self._ix(ijk)])
+
+    def __setitem__(self, ijk, val):
+        self.a[self._ix(ijk)] = val
+
+
+def ns_ab_diff_sec_2d(uo, vo, rho, mu, delta, phi, nrm_x, nrm_y, curv, g, nx, ny, dx, dy, re,
+                      mu_12, gx, gy, btn_g, btn_sf, fr, we):
+    """velsrc%tmp (x, y) of sec_part1 + sec_part2 + sec_part3, 2D."""
+    U, V, RO, MU, DE, PH = (R(a, g) for a in (uo, vo, rho, mu, delta, phi))
+    NX, NY, CU = R(nrm_x, g), R(nrm_y, g), R(curv, g)
+    tx, ty = np.zeros_like(uo), np.zeros_like(vo)
+    TX, TY = R(tx, g), R(ty, g)
+    for j in range(1, ny + 1):
+        for i in range(1, nx + 1):
+            rho_ = 0.5 * (RO[i, j] + RO[i + 1, j])
+            mu_ = 0.5 * (MU[i, j] + MU[i + 1, j])
+            xx = (U[i + 1, j] - 2.0 * U[i, j] + U[i - 1, j]) / _sq(dx)
+            yy = (U[i, j + 1] - 2.0 * U[i, j] + U[i, j - 1]) / _sq(dy)
+            dif_x = mu_ / rho_ * xx / re
+            dif_y = mu_ / rho_ * yy / re
+            TX[i, j] = dif_x + dif_y
+            rho_ = 0.5 * (RO[i, j] + RO[i, j + 1])
+            mu_ = 0.5 * (MU[i, j] + MU[i, j + 1])
+            xx = (V[i + 1, j] - 2.0 * V[i, j] + V[i - 1, j]) / _sq(dx)
+            yy = (V[i, j + 1] - 2.0 * V[i, j] + V[i, j - 1]) / _sq(dy)
+            dif_x = mu_ / rho_ * xx / re
+            dif_y = mu_ / rho_ * yy / re
+            TY[i, j] = dif_x + dif_y
+    for j in range(1, ny + 1):
+        for i in range(1, nx + 1):
+            rho_ = 0.5 * (RO[i, j] + RO[i + 1, j])
+            delta_ = 0.5 * (DE[i, j] + DE[i + 1, j])
+            ux = 0.5 * (U[i + 1, j] - U[i - 1, j]) / dx
+            uy = 0.5 * (U[i, j + 1] - U[i, j - 1]) / dy
+            vx = 0.5 * (V[i + 1, j] - V[i, j] + V[i + 1, j - 1] - V[i, j - 1]) / dx
+            phix = (PH[i + 1, j] - PH[i, j]) / dx
+            phiy = 0.25 * (PH[i + 1, j + 1] - PH[i + 1, j - 1] + PH[i, j + 1] - PH[i, j - 1]) / dy
+            dif_x = (1.0 - mu_12) * delta_ * phix * 2.0 * ux / (rho_ * re)
+            dif_y = (1.0 - mu_12) * delta_ * phiy * (uy + vx) / (rho_ * re)
+            TX[i, j] = TX[i, j] + dif_x + dif_y
+            rho_ = 0.5 * (RO[i, j] + RO[i, j + 1])
+            delta_ = 0.5 * (DE[i, j] + DE[i, j + 1])
+            vx = 0.5 * (V[i + 1, j] - V[i - 1, j]) / dx
+            vy = 0.5 * (V[i, j + 1] - V[i, j - 1]) / dy
+            uy = 0.5 * (U[i, j + 1] - U[i, j] + U[i - 1, j + 1] - U[i - 1, j]) / dy
+            phix = 0.25 * (PH[i + 1, j] - PH[i - 1, j] + PH[i + 1, j + 1] - PH[i - 1, j + 1]) / dx
+            phiy = (PH[i, j + 1] - PH[i, j]) / dy
+            dif_x = (1.0 - mu_12) * delta_ * phix * (uy + vx) / (rho_ * re)
+            dif_y = (1.0 - mu_12) * delta_ * phiy * 2.0 * vy / (rho_ * re)
+            TY[i, j] = TY[i, j] + dif_x + dif_y
+    for j in range(1, ny + 1):
+        for i in range(1, nx + 1):
+            rho_ = 0.5 * (RO[i, j] + RO[i + 1, j])
+            delta_ = 0.5 * (DE[i, j] + DE[i + 1, j])
+            curv_ = (CU[i, j] + CU[i + 1, j]) / 2.0
+            phix = 0.5 * (NX[i, j] + NX[i + 1, j])
+            TX[i, j] = TX[i, j] + gx * btn_g / fr - btn_sf * curv_ * delta_ * phix / (we * rho_)
+            rho_ = 0.5 * (RO[i, j] + RO[i, j + 1])
+            delta_ = 0.5 * (DE[i, j] + DE[i, j + 1])
+            curv_ = (CU[i, j] + CU[i, j + 1]) / 2.0
+            phiy = 0.5 * (NY[i, j] + NY[i, j + 1])
+            TY[i, j] = TY[i, j] + gy * btn_g / fr - btn_sf * curv_ * delta_ * phiy / (we * rho_)
+    return tx, ty
+
+
+def ns_ab_diff_sec_3d(uo, vo, wo, rho, mu, delta, phi, nrm_x, nrm_y, nrm_z, curv, g, nx, ny, nz,
+                      dx, dy, dz, re, mu_12, gx, gy, gz, btn_g, btn_sf, fr, we):
+    """velsrc%tmp (x, y, z) of sec_part1 + sec_part2 + sec_part3, 3D."""
+    U, V, W, RO, MU, DE, PH = (R(a, g) for a in (uo, vo, wo, rho, mu, delta, phi))
+    NX, NY, NZ, CU = R(nrm_x, g), R(nrm_y, g), R(nrm_z, g), R(curv, g)
+    tx, ty, tz = np.zeros_like(uo), np.zeros_like(vo), np.zeros_like(wo)
+    TX, TY, TZ = R(tx, g), R(ty, g), R(tz, g)
+    rng = [(i, j, k) for k in range(1, nz + 1) for j in range(1, ny + 1) for i in range(1, nx + 1)]
+    for i, j, k in rng:
+        for (T, F, o) in ((TX, U, (1, 0, 0)), (TY, V, (0, 1, 0)), (TZ, W, (0, 0, 1))):
+            a, b, c = i + o[0], j + o[1], k + o[2]
+            rho_ = 0.5 * (RO[i, j, k] + RO[a, b, c])
+            mu_ = 0.5 * (MU[i, j, k] + MU[a, b, c])
+            xx = (F[i + 1, j, k] - 2.0 * F[i, j, k] + F[i - 1, j, k]) / _sq(dx)
+            yy = (F[i, j + 1, k] - 2.0 * F[i, j, k] + F[i, j - 1, k]) / _sq(dy)
+            zz = (F[i, j, k + 1] - 2.0 * F[i, j, k] + F[i, j, k - 1]) / _sq(dz)
+            dif_x = mu_ / rho_ * xx / re
+            dif_y = mu_ / rho_ * yy / re
+            dif_z = mu_ / rho_ * zz / re
+            T[i, j, k] = dif_x + dif_y + dif_z
+    for i, j, k in rng:
+        rho_ = 0.5 * (RO[i, j, k] + RO[i + 1, j, k])
+        delta_ = 0.5 * (DE[i, j, k] + DE[i + 1, j, k])
+        ux = 0.5 * (U[i + 1, j, k] - U[i - 1, j, k]) / dx
+        uy = 0.5 * (U[i, j + 1, k] - U[i, j - 1, k]) / dy
+        uz = 0.5 * (U[i, j, k + 1] - U[i, j, k - 1]) / dz
+        vx = 0.5 * (V[i + 1, j, k] - V[i, j, k] + V[i + 1, j - 1, k] - V[i, j - 1, k]) / dx
+        wx = 0.5 * (W[i + 1, j, k] - W[i, j, k] + W[i + 1, j, k - 1] - W[i, j, k - 1]) / dx
+        phix = (PH[i + 1, j, k] - PH[i, j, k]) / dx
+        phiy = 0.25 * (PH[i + 1, j + 1, k] - PH[i + 1, j - 1, k] + PH[i, j + 1, k] - PH[i, j - 1, k]) / dy
+        phiz = 0.25 * (PH[i + 1, j, k + 1] - PH[i + 1, j, k - 1] + PH[i, j, k + 1] - PH[i, j, k - 1]) / dz
+        dif_x = (1.0 - mu_12) * delta_ * phix * 2.0 * ux / (rho_ * re)
+        dif_y = (1.0 - mu_12) * delta_ * phiy * (uy + vx) / (rho_ * re)
+        dif_z = (1.0 - mu_12) * delta_ * phiz * (uz + wx) / (rho_ * re)
+        TX[i, j, k] = TX[i, j, k] + dif_x + dif_y + dif_z
+        rho_ = 0.5 * (RO[i, j, k] + RO[i, j + 1, k])
+        delta_ = 0.5 * (DE[i, j, k] + DE[i, j + 1, k])
+        vx = 0.5 * (V[i + 1, j, k] - V[i - 1, j, k]) / dx
+        vy = 0.5 * (V[i, j + 1, k] - V[i, j - 1, k]) / dy
+        vz = 0.5 * (V[i, j, k + 1] - V[i, j, k - 1]) / dz
+        uy = 0.5 * (U[i, j + 1, k] - U[i, j, k] + U[i - 1, j + 1, k] - U[i - 1, j, k]) / dy
+        wy = 0.5 * (W[i, j + 1, k] - W[i, j, k] + W[i, j + 1, k - 1] - W[i, j, k - 1]) / dy
+        phix = 0.25 * (PH[i + 1, j, k] - PH[i - 1, j, k] + PH[i + 1, j + 1, k] - PH[i - 1, j + 1, k]) / dx
+        phiy = (PH[i, j + 1, k] - PH[i, j, k]) / dy
+        phiz = 0.25 * (PH[i, j + 1, k + 1] - PH[i, j + 1, k - 1] + PH[i, j, k + 1] - PH[i, j, k - 1]) / dz
+        dif_x = (1.0 - mu_12) * delta_ * phix * (uy + vx) / (rho_ * re)
+        dif_y = (1.0 - mu_12) * delta_ * phiy * 2.0 * vy / (rho_ * re)
+        dif_z = (1.0 - mu_12) * delta_ * phiz * (wy + vz) / (rho_ * re)
+        TY[i, j, k] = TY[i, j, k] + dif_x + dif_y + dif_z
+        rho_ = 0.5 * (RO[i, j, k] + RO[i, j, k + 1])
+        delta_ = 0.5 * (DE[i, j, k] + DE[i, j, k + 1])
+        wx = 0.5 * (W[i + 1, j, k] - W[i - 1, j, k]) / dx
+        wy = 0.5 * (W[i, j + 1, k] - W[i, j - 1, k]) / dy
+        wz = 0.5 * (W[i, j, k + 1] - W[i, j, k - 1]) / dz
+        uz = 0.5 * (U[i, j, k + 1] - U[i, j, k] + U[i - 1, j, k + 1] - U[i - 1, j, k]) / dz
+        vz = 0.5 * (V[i, j, k + 1] - V[i, j, k] + V[i, j - 1, k + 1] - V[i, j - 1, k]) / dz
+        phix = 0.25 * (PH[i + 1, j, k + 1] - PH[i - 1, j, k + 1] + PH[i + 1, j, k] - PH[i - 1, j, k]) / dx
+        phiy = 0.25 * (PH[i, j + 1, k + 1] - PH[i, j - 1, k + 1] + PH[i, j + 1, k] - PH[i, j - 1, k]) / dy
+        phiz = (PH[i, j, k + 1] - PH[i, j, k]) / dz
+        dif_x = (1.0 - mu_12) * delta_ * phix * (uz + wx) / (rho_ * re)
+        dif_y = (1.0 - mu_12) * delta_ * phiy * (vz + wy) / (rho_ * re)
+        dif_z = (1.0 - mu_12) * delta_ * phiz * 2.0 * wz / (rho_ * re)
+        TZ[i, j, k] = TZ[i, j, k] + dif_x + dif_y + dif_z
+    for i, j, k in rng:
+        for (T, N, o, gg) in ((TX, NX, (1, 0, 0), gx), (TY, NY, (0, 1, 0), gy),
+                              (TZ, NZ, (0, 0, 1), gz)):
+            a, b, c = i + o[0], j + o[1], k + o[2]
+            rho_ = 0.5 * (RO[i, j, k] + RO[a, b, c])
+            delta_ = 0.5 * (DE[i, j, k] + DE[a, b, c])
+            curv_ = (CU[i, j, k] + CU[a, b, c]) / 2.0
+            phin = 0.5 * (N[i, j, k] + N[a, b, c])
+            T[i, j, k] = T[i, j, k] + gg * btn_g / fr - btn_sf * curv_ * delta_ * phin / (we * rho_)
+    return tx, ty, tz
+
+
+def find_stag_vel(us, vs, ws, g, nx, ny, nz):
+    """The interior averages of find_stag_vel: returns (V, W, U, WW, UU, VV) =
+    (y%s1, z%s1, x%s1, z%s2, x%s2, y%s2) as dicts keyed by (i, j[, k])."""
+    three = us.ndim == 3
+    Us, Vs = R(us, g), R(vs, g)
+    out = [dict() for _ in range(6)]
+    if not three:
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                out[0][i, j] = 0.25 * (Vs[i, j] + Vs[i, j - 1] + Vs[i + 1, j] + Vs[i + 1, j - 1])
+                out[2][i, j] = 0.25 * (Us[i, j] + Us[i - 1, j] + Us[i, j + 1] + Us[i - 1, j + 1])
+        return out
+    Ws = R(ws, g)
+    for k in range(1, nz + 1):
+        for j in range(1, ny + 1):
+            for i in range(1, nx + 1):
+                out[0][i, j, k] = 0.25 * (Vs[i, j, k] + Vs[i, j - 1, k] + Vs[i + 1, j, k] + Vs[i + 1, j - 1, k])
+                out[1][i, j, k] = 0.25 * (Ws[i, j, k] + Ws[i, j, k - 1] + Ws[i + 1, j, k] + Ws[i + 1, j, k - 1])
+                out[2][i, j, k] = 0.25 * (Us[i, j, k] + Us[i - 1, j, k] + Us[i, j + 1, k] + Us[i - 1, j + 1, k])
+                out[3][i, j, k] = 0.25 * (Ws[i, j, k] + Ws[i, j, k - 1] + Ws[i, j + 1, k] + Ws[i, j + 1, k - 1])
+                out[4][i, j, k] = 0.25 * (Us[i, j, k] + Us[i - 1, j, k] + Us[i, j, k + 1] + Us[i - 1, j, k + 1])
+                out[5][i, j, k] = 0.25 * (Vs[i, j, k] + Vs[i, j - 1, k] + Vs[i, j, k + 1] + Vs[i, j - 1, k + 1])
+    return out
+
+
+def ns_ab_adv_predictor(old, tmp, diff, src_old, g, n, h, dt):
+    """ns_linearize's find_stag_vel, ns_ab_adv_source_sec, ns_ab_setup and
+    ns_ab_predictor (without velbc).  old/tmp/diff/src_old: tuples of padded
+    arrays (u, v[, w]); n = (nx, ny[, nz]); h = (dx, dy[, dz]).  Returns
+    (velsrc%now, vel%now) tuples; vel%now starts as a copy of vel%old."""
+    three = len(old) == 3
+    nx, ny = n[0], n[1]
+    nz = n[2] if three else 1
+    st = find_stag_vel(tmp[0], tmp[1], tmp[2] if three else None, g, nx, ny, nz)
+    src = [np.zeros_like(a) for a in old]
+    vel = [a.copy() for a in old]
+    O = [R(a, g) for a in old]
+    T = [R(a, g) for a in tmp]
+    S = [R(a, g) for a in src]
+    D = [R(a, g) for a in diff]
+    SO = [R(a, g) for a in src_old]
+    VN = [R(a, g) for a in vel]
+
+    def d1(F, ix, ax, hh):
+        e = [0, 0, 0][:len(ix)]
+        e[ax] = 1
+        p1 = tuple(a + b for a, b in zip(ix, e))
+        p2 = tuple(a + 2 * b for a, b in zip(ix, e))
+        m1 = tuple(a - b for a, b in zip(ix, e))
+        m2 = tuple(a - 2 * b for a, b in zip(ix, e))
+        p = 0.5 * (-F[p2] + 4.0 * F[p1] - 3.0 * F[ix]) / hh
+        m = 0.5 * (F[m2] - 4.0 * F[m1] + 3.0 * F[ix]) / hh
+        return p, m
+
+    pts = ([(i, j, k) for k in range(1, nz + 1) for j in range(1, ny + 1) for i in range(1, nx + 1)]
+           if three else [(i, j) for j in range(1, ny + 1) for i in range(1, nx + 1)])
+    for ix in pts:
+        if three:
+            adv = [(T[0][ix], st[0][ix], st[1][ix]), (st[2][ix], T[1][ix], st[3][ix]),
+                   (st[4][ix], st[5][ix], T[2][ix])]
+        else:
+            adv = [(T[0][ix], st[0][ix]), (st[2][ix], T[1][ix])]
+        for c in range(len(old)):
+            a = adv[c]
+            xp, xm = d1(O[c], ix, 0, h[0])
+            yp, ym = d1(O[c], ix, 1, h[1])
+            u, v = a[0], a[1]
+            s = - ((u + abs(u)) * xm + (u - abs(u)) * xp) / 2.0 \
+                - ((v + abs(v)) * ym + (v - abs(v)) * yp) / 2.0
+            if three:
+                zp, zm = d1(O[c], ix, 2, h[2])
+                w = a[2]
+                s = s - ((w + abs(w)) * zm + (w - abs(w)) * zp) / 2.0
+            S[c][ix] = s
+            S[c][ix] = S[c][ix] + D[c][ix]
+            srcv = 1.50 * S[c][ix] - 0.5 * SO[c][ix]
+            VN[c][ix] = O[c][ix] + dt * srcv
+    return tuple(src), tuple(vel)
+
+
+def velbc(u, v, w, g, nx, ny, nz, ubc, vbc, wbc=(0, 0)):
+    """velbc in place (2D when w is None)."""
+    three = w is not None
+    U, V = R(u, g), R(v, g)
+    W = R(w, g) if three else None
+    ks = list(range(1 - g, nz + g + 1)) if three else [None]
+
+    def at(F, i, j, k):
+        return (i, j, k) if three else (i, j)
+
+    comps = [(U, 0), (V, 1)] + ([(W, 2)] if three else [])
+    for side, t in ((0, ubc[0]), (1, ubc[1])):
+        if t not in (1, 2):
+            continue
+        for k in ks:
+            for j in range(1 - g, ny + g + 1):
+                for m in range(1, g + 1):
+                    for F, c in comps:
+                        if side == 0:
+                            s_ = (1 - 2 + m) if c == 0 else (1 - 1 + m)
+                            F[at(F, 1 - m, j, k)] = F[at(F, s_, j, k)] if t == 2 else -F[at(F, s_, j, k)]
+                        else:
+                            s_ = (nx - m) if c == 0 else (nx + 1 - m)
+                            F[at(F, nx + m, j, k)] = F[at(F, s_, j, k)] if t == 2 else -F[at(F, s_, j, k)]
+                U[at(U, 0 if side == 0 else nx, j, k)] = 0.0
+    for side, t in ((0, vbc[0]), (1, vbc[1])):
+        if t not in (1, 2):
+            continue
+        for k in ks:
+            for i in range(1 - g, nx + g + 1):
+                for m in range(1, g + 1):
+                    for F, c in comps:
+                        if side == 0:
+                            s_ = (1 - 2 + m) if c == 1 else (1 - 1 + m)
+                            F[at(F, i, 1 - m, k)] = F[at(F, i, s_, k)] if t == 2 else -F[at(F, i, s_, k)]
+                        else:
+                            s_ = (ny - m) if c == 1 else (ny + 1 - m)
+                            F[at(F, i, ny + m, k)] = F[at(F, i, s_, k)] if t == 2 else -F[at(F, i, s_, k)]
+                V[at(V, i, 0 if side == 0 else ny, k)] = 0.0
+    if not three:
+        return
+    for side, t in ((0, wbc[0]), (1, wbc[1])):
+        if t not in (1, 2):
+            continue
+        for j in range(1 - g, ny + g + 1):
+            for i in range(1 - g, nx + g + 1):
+                for m in range(1, g + 1):
+                    for F, c in comps:
+                        if side == 0:
+                            s_ = (1 - 2 + m) if c == 2 else (1 - 1 + m)
+                            F[i, j, 1 - m] = F[i, j, s_] if t == 2 else -F[i, j, s_]
+                        else:
+                            s_ = (nz - m) if c == 2 else (nz + 1 - m)
+                            F[i, j, nz + m] = F[i, j, s_] if t == 2 else -F[i, j, s_]
+                W[i, j, 0 if side == 0 else nz] = 0.0
