@@ -6,15 +6,18 @@ include/gbmg.h).  This package holds its sources (csrc/), the in-tree build
 recipe (build.py), the ctypes binding (_lib.py), the host-side mirror of the
 reference's pressure routine (ppe.py), the differentiable solve (autograd.py),
 the registered operator torch.ops.gbmg.solve (ops.py), the level-set
-advection of the interface solver (levelset.py) and the seeded synthetic
-inputs (inputs.py).
+advection of the interface solver (levelset.py), the Adams-Bashforth momentum
+step around the projection (momentum.py) and the seeded synthetic inputs
+(inputs.py).
 """
 from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
 from .levelset import LevelSet, node_velocity  # noqa: F401
+from .momentum import NSParams, ns_ab_predictor, ns_ab_solver, velbc  # noqa: F401
 
 try:  # torch.ops.gbmg.solve (torch is optional for host-memory use)
     from . import ops  # noqa: F401
 except ImportError:  # pragma: no cover
     pass
 
-__all__ = ["PressurePoisson", "LevelSet", "node_velocity", "ConvergenceError", "GBMGError"]
+__all__ = ["PressurePoisson", "LevelSet", "node_velocity", "NSParams", "ns_ab_solver",
+           "ns_ab_predictor", "velbc", "ConvergenceError", "GBMGError"]

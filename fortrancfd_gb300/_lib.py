@@ -33,11 +33,12 @@ EXPORTS = (
     "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split",
     "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
     "gbmg_ls_kernel_launches", "gbmg_ls_last_error",
+    "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
                 "prolong_fine", "prolong_coarse", "coarse_solve", "residual", "vector", "setup",
-                "certify")
+                "certify", "momentum")
 
 
 class Grid(C.Structure):
@@ -64,6 +65,30 @@ class Stats(C.Structure):
 
 class Field(C.Structure):
     _fields_ = [("data", C.c_void_p), ("sy", C.c_int64), ("sz", C.c_int64)]
+
+
+class NSParams(C.Structure):
+    _fields_ = [("ghost", C.c_int32), ("bc", C.c_int32 * 6), ("iterations", C.c_int32),
+                ("dt", C.c_double), ("re", C.c_double), ("fr", C.c_double), ("we", C.c_double),
+                ("mu_12", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
+                ("gz", C.c_double), ("btn_g", C.c_double), ("btn_sf", C.c_double),
+                ("p_tol", C.c_double)]
+
+
+NS_FIELDS = ("u", "v", "w", "u_old", "v_old", "w_old", "su", "sv", "sw", "su_old", "sv_old",
+             "sw_old", "rho", "mu", "delta", "phi", "nrm_x", "nrm_y", "nrm_z", "curv", "p")
+
+
+class NSFields(C.Structure):
+    _fields_ = [(name, Field) for name in NS_FIELDS]
+
+
+class NSStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("cycles", C.c_int32), ("max_rel_residual", C.c_double),
+                ("linf", C.c_double), ("l2f", C.c_double), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 _lib = None
@@ -128,7 +153,11 @@ def load(build_if_missing: bool = True):
         L.gbmg_ls_last_error.restype = C.c_char_p
         L.gbmg_ls_redistance.argtypes = [H, Field, C.c_double, C.c_double, C.c_double, C.c_int,
                                          C.c_int, C.c_int, P(C.c_int32), P(C.c_double)]
-        for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance"):
+        L.gbmg_ns_ab_step.argtypes = [H, P(NSParams), P(NSFields), C.c_int, P(NSStats)]
+        L.gbmg_ns_ab_predict.argtypes = [H, P(NSParams), P(NSFields), C.c_int]
+        L.gbmg_ns_velbc.argtypes = [H, P(NSParams), Field, Field, Field, C.c_int]
+        for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
+                     "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc"):
             getattr(L, name).restype = C.c_int
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",

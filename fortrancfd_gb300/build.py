@@ -17,6 +17,9 @@ SO = os.path.join(BUILD, "libgbmg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", CSRC, "-I", INCLUDE]
+# Translation units whose FP64 results must equal the oracle's bit for bit are
+# compiled without multiply-add contraction.
+FILE_FLAGS = {"momentum.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -46,7 +49,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(pair):
         src, obj = pair
-        cmd = [nvcc(), *ARCH, *FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc(), *ARCH, *FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src,
+               "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

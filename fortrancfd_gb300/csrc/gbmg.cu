@@ -136,6 +136,10 @@ struct gbmg_handle {
   bool rho_ready = false;
   bool split_ready = false;  // gbmg_set_split: constant Laplacian + density for the split source
   double split_rho12 = 0.0;
+  // momentum step: padded-box buffers (vel%tmp, velsrc%tmp, and the host
+  // staging copies of the caller's arrays), allocated on first use
+  double* ns_buf[32] = {};
+  size_t ns_n[32] = {};
   std::string err;
 };
 
@@ -500,6 +504,7 @@ int free_all(gbmg_handle* h) {
   if (h->gmHost) cudaFreeHost(h->gmHost);
   dfree(h->minv); dfree(h->adense); dfree(h->cwork); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   dfree(h->bar);
+  for (int i = 0; i < 32; ++i) dfree(h->ns_buf[i]);
   delete[] h->dmaps;
   h->dmaps = nullptr;
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
@@ -1327,6 +1332,194 @@ int stage_velocity(gbmg_handle* h, const gbmg_field* const fv[3], bool has_w, in
   return GBMG_OK;
 }
 
+// The projection on device face velocities (fields addressed at their face
+// (0,0,0)) with the initial pressure already in h->p: b = div(u*)/dt, the
+// solve, then u -= dt beta grad p (ppe_sor_solver + ns_momentum_correction).
+int project_device(gbmg_handle* h, const gbmg_field dfield[3], bool has_w, double dt, double tol,
+                   gbmg_stats* st) {
+  const gbmg_grid& g = h->grid;
+  const cudaStream_t s = h->stream;
+  Strided su{dfield[0].data, dfield[0].sy, dfield[0].sz};
+  Strided sv{dfield[1].data, dfield[1].sy, dfield[1].sz};
+  Strided sw{has_w ? dfield[2].data : nullptr, has_w ? dfield[2].sy : 0,
+             has_w ? dfield[2].sz : 0};
+  launch_divergence(s, g.nx, g.ny, g.nz, su, sv, sw, g.dx, g.dy, g.dz, dt, h->b);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "divergence"));
+  // mean projection + norm of b in place
+  double bnorm = 0.0;
+  GB_TRY(finish_rhs(h, &bnorm));
+  const int status = solve_internal(h, tol, bnorm, st);
+  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
+  launch_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, g.dx, g.dy, g.dz, dt, dfield[0].data,
+                 dfield[0].sy, dfield[0].sz, dfield[1].data, dfield[1].sy, dfield[1].sz,
+                 has_w ? dfield[2].data : nullptr, has_w ? dfield[2].sy : 0,
+                 has_w ? dfield[2].sz : 0);
+  h->launches += 1;
+  GB_TRY(check_launch(h, "correct"));
+  return status;
+}
+
+// ---- Adams-Bashforth momentum step -------------------------------------------
+// Arrays of the step, in the order of gbmg_ns_fields.
+enum NsSlot {
+  kNsU, kNsV, kNsW, kNsUo, kNsVo, kNsWo, kNsSu, kNsSv, kNsSw, kNsSuo, kNsSvo, kNsSwo,
+  kNsRho, kNsMu, kNsDelta, kNsPhi, kNsNx, kNsNy, kNsNz, kNsCurv, kNsFields
+};
+// scratch buffers after the staging slots: vel%tmp (3), velsrc%tmp (3)
+constexpr int kNsTmp = kNsFields, kNsDiff = kNsFields + 3;
+
+const gbmg_field& ns_field(const gbmg_ns_fields* f, int slot) {
+  const gbmg_field* all[kNsFields] = {&f->u,      &f->v,      &f->w,      &f->u_old, &f->v_old,
+                                      &f->w_old,  &f->su,     &f->sv,     &f->sw,    &f->su_old,
+                                      &f->sv_old, &f->sw_old, &f->rho,    &f->mu,    &f->delta,
+                                      &f->phi,    &f->nrm_x,  &f->nrm_y,  &f->nrm_z, &f->curv};
+  return *all[slot];
+}
+
+// Offset of element (1,1,1) of the reference's indices from a field's
+// address: faces are addressed at their face 0 (u(0,1,1), v(1,0,1), w(1,1,0)).
+int64_t ns_origin(int slot, int64_t sy, int64_t sz) {
+  const int axis = slot < kNsRho ? slot % 3 : -1;
+  return axis == 0 ? 1 : axis == 1 ? sy : axis == 2 ? sz : 0;
+}
+
+struct NsPlan {
+  NsArgs a{};
+  NsBc bc{};
+  int64_t lo = 0, hi = 0;  // element offsets of the padded box from element (1,1,1)
+  double* base[kNsFields + 6] = {};
+  bool used[kNsFields] = {};
+};
+
+int ns_buffer(gbmg_handle* h, int slot, size_t n) {
+  if (h->ns_n[slot] < n) {
+    dfree(h->ns_buf[slot]);
+    h->ns_n[slot] = 0;
+    GB_TRY(dmalloc(h, &h->ns_buf[slot], n));
+    h->ns_n[slot] = n;
+  }
+  return GBMG_OK;
+}
+
+// Validate the arrays a call uses, fill the kernel arguments and make every
+// used array device-resident (host memory: staged copies of the padded box).
+int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
+               const bool (&used)[kNsFields], const bool (&copy_in)[kNsFields], NsPlan* P) {
+  const gbmg_grid& g = h->grid;
+  const bool three = g.nz > 1;
+  if (!prm || !f) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
+  const int gh = prm->ghost;
+  if (gh < 2 || g.nx < gh + 1 || g.ny < gh + 1 || (three && g.nz < gh + 1)) {
+    h->err = "the momentum step needs ghost >= 2 and at least ghost + 1 cells per axis";
+    return GBMG_INVALID_ARG;
+  }
+  if (!(prm->dt > 0) || !(prm->re > 0) || !(prm->fr > 0) || (prm->btn_sf != 0 && !(prm->we > 0))) {
+    h->err = "dt, re, fr (and we with surface tension) must be > 0";
+    return GBMG_INVALID_ARG;
+  }
+  int64_t sy = 0, sz = 0;
+  for (int i = 0; i < kNsFields; ++i) {
+    if (!used[i]) continue;
+    const gbmg_field& fi = ns_field(f, i);
+    if (!fi.data) { h->err = "a field the momentum step reads or writes is NULL"; return GBMG_INVALID_ARG; }
+    if (!sy) { sy = fi.sy; sz = fi.sz; }
+    if (fi.sy != sy || (three && fi.sz != sz)) {
+      h->err = "the arrays of the momentum step must share their strides";
+      return GBMG_INVALID_ARG;
+    }
+  }
+  if (sy < g.nx + 2 * gh || (three && sz < sy * (g.ny + 2 * gh))) {
+    h->err = "strides too small for the ghost-padded box";
+    return GBMG_INVALID_ARG;
+  }
+  NsArgs& a = P->a;
+  a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.g = gh;
+  a.sy = sy; a.sz = three ? sz : 0;
+  a.dx = g.dx; a.dy = g.dy; a.dz = g.dz;
+  a.dt = prm->dt; a.re = prm->re; a.fr = prm->fr; a.we = prm->we; a.mu_12 = prm->mu_12;
+  a.gx = prm->gx; a.gy = prm->gy; a.gz = prm->gz; a.btn_g = prm->btn_g; a.btn_sf = prm->btn_sf;
+  for (int i = 0; i < 6; ++i) P->bc.b[i] = prm->bc[i];
+  P->lo = -(int64_t)gh - gh * a.sy - (three ? gh * a.sz : 0);
+  P->hi = (int64_t)(g.nx + gh - 1) + (g.ny + gh - 1) * a.sy + (three ? (g.nz + gh - 1) * a.sz : 0);
+  const size_t span = (size_t)(P->hi - P->lo + 1);
+  for (int i = 0; i < kNsFields; ++i) {
+    P->used[i] = used[i];
+    if (!used[i]) continue;
+    double* b = ns_field(f, i).data + ns_origin(i, a.sy, a.sz);
+    if (mem == GBMG_MEM_DEVICE) {
+      P->base[i] = b;
+      continue;
+    }
+    GB_TRY(ns_buffer(h, i, span));
+    if (copy_in[i])
+      GB_CUDA(h, cudaMemcpyAsync(h->ns_buf[i], b + P->lo, span * sizeof(double),
+                                 cudaMemcpyHostToDevice, h->stream));
+    P->base[i] = h->ns_buf[i] - P->lo;
+  }
+  for (int c = 0; c < 6; ++c) {
+    if (!three && c % 3 == 2) continue;
+    GB_TRY(ns_buffer(h, kNsTmp + c, span));
+    P->base[kNsTmp + c] = h->ns_buf[kNsTmp + c] - P->lo;
+  }
+  return GBMG_OK;
+}
+
+int ns_finish(gbmg_handle* h, const gbmg_ns_fields* f, int mem, const NsPlan& P,
+              const bool (&copy_out)[kNsFields]) {
+  if (mem != GBMG_MEM_HOST) return GBMG_OK;
+  const size_t span = (size_t)(P.hi - P.lo + 1);
+  for (int i = 0; i < kNsFields; ++i) {
+    if (!P.used[i] || !copy_out[i]) continue;
+    double* b = ns_field(f, i).data + ns_origin(i, P.a.sy, P.a.sz);
+    GB_CUDA(h, cudaMemcpyAsync(b + P.lo, P.base[i] + P.lo, span * sizeof(double),
+                               cudaMemcpyDeviceToHost, h->stream));
+  }
+  return GBMG_OK;
+}
+
+// ns_linearize (vel%tmp = vel%now over the padded box), ns_ab_setup and
+// ns_ab_predictor, then velbc on vel%now.
+int ns_pass(gbmg_handle* h, const NsPlan& P) {
+  const cudaStream_t s = h->stream;
+  const bool three = P.a.nz > 1;
+  const size_t span = (size_t)(P.hi - P.lo + 1);
+  for (int c = 0; c < (three ? 3 : 2); ++c)
+    GB_CUDA(h, cudaMemcpyAsync(P.base[kNsTmp + c] + P.lo, P.base[kNsU + c] + P.lo,
+                               span * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  const double* old[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
+  const double* tmp[3] = {P.base[kNsTmp], P.base[kNsTmp + 1], P.base[kNsTmp + 2]};
+  const double* diff[3] = {P.base[kNsDiff], P.base[kNsDiff + 1], P.base[kNsDiff + 2]};
+  const double* so[3] = {P.base[kNsSuo], P.base[kNsSvo], P.base[kNsSwo]};
+  double* src[3] = {P.base[kNsSu], P.base[kNsSv], P.base[kNsSw]};
+  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_advance(s, P.a, old, tmp, diff, so, src, now));
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(s, P.a, P.bc, now));
+  return check_launch(h, "momentum predictor");
+}
+
+int ns_diffusion(gbmg_handle* h, const NsPlan& P) {
+  const double* vel[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
+  const double* nrm[3] = {P.base[kNsNx], P.base[kNsNy], P.base[kNsNz]};
+  double* out[3] = {P.base[kNsDiff], P.base[kNsDiff + 1], P.base[kNsDiff + 2]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM,
+         launch_ns_diffusion(h->stream, P.a, vel, P.base[kNsRho], P.base[kNsMu],
+                             P.base[kNsDelta], P.base[kNsPhi], nrm, P.base[kNsCurv], out));
+  return check_launch(h, "momentum sources");
+}
+
+void ns_used(const gbmg_grid& g, const gbmg_ns_params* prm, bool (&used)[kNsFields],
+             bool (&in)[kNsFields], bool (&out)[kNsFields]) {
+  const bool three = g.nz > 1, sf = prm && prm->btn_sf != 0.0;
+  for (int i = 0; i < kNsFields; ++i) {
+    const bool is_w = i < kNsRho && i % 3 == 2;
+    used[i] = !(is_w && !three) && !(i == kNsNz && !three) &&
+              !(i >= kNsNx && i <= kNsCurv && !sf);
+    in[i] = used[i];  // velsrc%now round-trips its ghosts
+    out[i] = used[i] && (i <= kNsW || (i >= kNsSu && i <= kNsSw));
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -1546,24 +1739,9 @@ int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_
   double* dv[3] = {nullptr, nullptr, nullptr};
   gbmg_field dfield[3];
   GB_TRY(stage_velocity(h, fv, has_w, mem, dv, dfield));
-  // b = div(u*)/dt into h->b (the RHS of ppe_sor_solver)
-  Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
-  Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
-  launch_divergence(s, g.nx, g.ny, g.nz, su, sv, sw, g.dx, g.dy, g.dz, dt, h->b);
-  h->launches += 1;
-  GB_TRY(check_launch(h, "divergence"));
-  // mean projection + norm of b in place
-  double bnorm = 0.0;
-  GB_TRY(finish_rhs(h, &bnorm));
   GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
-  const int status = solve_internal(h, tol, bnorm, st);
+  const int status = project_device(h, dfield, has_w, dt, tol, st);
   if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
-  // u -= dt beta grad p (ns_momentum_correction)
-  launch_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, g.dx, g.dy, g.dz, dt, dv[0], dfield[0].sy,
-                 dfield[0].sz, dv[1], dfield[1].sy, dfield[1].sz, has_w ? dv[2] : nullptr,
-                 has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0);
-  h->launches += 1;
-  GB_TRY(check_launch(h, "correct"));
   if (mem == GBMG_MEM_HOST)
     for (int a = 0; a < 3; ++a) {
       if (a == 2 && !has_w) continue;
@@ -1832,6 +2010,104 @@ int gbmg_set_profiling(gbmg_handle* h, int on) {
     h->prof_ms[c] = 0.0;
     h->prof_n[c] = 0;
   }
+  return GBMG_OK;
+}
+
+int gbmg_ns_ab_step(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
+                    gbmg_ns_stats* stats) {
+  GB_TRY(begin(h));
+  gbmg_ns_stats local{};
+  gbmg_ns_stats* st = stats ? stats : &local;
+  std::memset(st, 0, sizeof(*st));
+  if (!prm || !f) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
+  if (!h->coef_ready || !h->rho_ready) {
+    h->err = "the momentum step needs the new density: call gbmg_set_rho or gbmg_set_phi first";
+    return GBMG_STATE_ERROR;
+  }
+  const gbmg_grid& g = h->grid;
+  const bool three = g.nz > 1;
+  bool used[kNsFields], in[kNsFields], out[kNsFields];
+  ns_used(g, prm, used, in, out);
+  if (prm->iterations < 1 || !(prm->p_tol > 0)) {
+    h->err = "iterations must be >= 1 and p_tol > 0";
+    return GBMG_INVALID_ARG;
+  }
+  GB_TRY(validate_field(h, f->p, "p"));
+  const cudaStream_t s = h->stream;
+  GB_CUDA(h, cudaEventRecord(h->ev0, s));
+  NsPlan P;
+  GB_TRY(ns_prepare(h, prm, f, mem, used, in, &P));
+  GB_TRY(upload(h, f->p, g.nx, g.ny, g.nz, mem, h->p));
+  GB_TRY(ns_diffusion(h, P));
+  gbmg_field dfield[3] = {{P.base[kNsU] - 1, P.a.sy, P.a.sz},
+                          {P.base[kNsV] - P.a.sy, P.a.sy, P.a.sz},
+                          {three ? P.base[kNsW] - P.a.sz : nullptr, P.a.sy, P.a.sz}};
+  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
+  int worst = GBMG_OK;
+  for (int it = 0; it < prm->iterations; ++it) {
+    GB_TRY(ns_pass(h, P));
+    gbmg_stats ps{};
+    const int rc = project_device(h, dfield, three, prm->dt, prm->p_tol, &ps);
+    if (rc != GBMG_OK && rc != GBMG_NOT_CONVERGED && rc != GBMG_DIVERGED) return rc;
+    if (rc > worst) worst = rc;
+    st->cycles += ps.cycles;
+    st->max_rel_residual = std::max(st->max_rel_residual, ps.rel_residual);
+    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(s, P.a, P.bc, now));
+    GB_TRY(check_launch(h, "velbc"));
+  }
+  const double* tmp[3] = {P.base[kNsTmp], P.base[kNsTmp + 1], P.base[kNsTmp + 2]};
+  const double* nowc[3] = {now[0], now[1], now[2]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_change(s, P.a, nowc, tmp, h->red));
+  GB_TRY(check_launch(h, "velocity change"));
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  GB_TRY(ns_finish(h, f, mem, P, out));
+  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, f->p));
+  GB_CUDA(h, cudaEventRecord(h->ev1, s));
+  GB_CUDA(h, cudaEventSynchronize(h->ev1));
+  double mx = 0.0;
+  std::memcpy(&mx, &h->host_res[kSlotMax], sizeof(double));
+  const double cnt = (three ? 3.0 : 2.0) * g.nx * g.ny * g.nz;
+  st->linf = mx;
+  st->l2f = std::sqrt(h->host_res[kSlotSum] / cnt);
+  st->status = worst;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st->ms = ms;
+  return worst;
+}
+
+int gbmg_ns_ab_predict(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f,
+                       int mem) {
+  GB_TRY(begin(h));
+  bool used[kNsFields], in[kNsFields], out[kNsFields];
+  ns_used(h->grid, prm, used, in, out);
+  NsPlan P;
+  GB_TRY(ns_prepare(h, prm, f, mem, used, in, &P));
+  GB_TRY(ns_diffusion(h, P));
+  GB_TRY(ns_pass(h, P));
+  GB_TRY(ns_finish(h, f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_field v,
+                  gbmg_field w, int mem) {
+  GB_TRY(begin(h));
+  gbmg_ns_fields f{};
+  f.u = u; f.v = v; f.w = w;
+  bool used[kNsFields] = {}, in[kNsFields] = {}, out[kNsFields] = {};
+  const bool three = h->grid.nz > 1;
+  for (int c = 0; c < (three ? 3 : 2); ++c) used[c] = in[c] = out[c] = true;
+  NsPlan P;
+  gbmg_ns_params q = prm ? *prm : gbmg_ns_params{};
+  if (prm) { q.dt = q.re = q.fr = 1.0; q.btn_sf = 0.0; }  // velbc reads only ghost and bc
+  GB_TRY(ns_prepare(h, prm ? &q : nullptr, &f, mem, used, in, &P));
+  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(h->stream, P.a, P.bc, now));
+  GB_TRY(check_launch(h, "velbc"));
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
 }
 

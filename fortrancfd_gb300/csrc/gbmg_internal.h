@@ -318,4 +318,29 @@ void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratc
 void launch_dw_out(cudaStream_t s, const float2* p, double* out, size_t n, const ReduceScratch& R,
                    int slot);
 
+// ---- Adams-Bashforth momentum step (momentum.cu) ------------------------------
+// Geometry and constants of one step.  Arrays are ghost-padded boxes sharing
+// the strides sy, sz; kernels take the address of the reference's element
+// (1,1,1) of each.
+struct NsArgs {
+  int nx, ny, nz, g;
+  int64_t sy, sz;
+  double dx, dy, dz, dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf;
+};
+struct NsBc {
+  int b[6];  // velbc type of the walls x-, x+, y-, y+, z-, z+ (1 no-slip, 2 slip, else none)
+};
+void launch_ns_diffusion(cudaStream_t s, const NsArgs& a, const double* const vel[3],
+                         const double* rho, const double* mu, const double* delta,
+                         const double* phi, const double* const nrm[3], const double* curv,
+                         double* const out[3]);
+void launch_ns_advance(cudaStream_t s, const NsArgs& a, const double* const old[3],
+                       const double* const tmp[3], const double* const diff[3],
+                       const double* const src_old[3], double* const src[3],
+                       double* const now[3]);
+void launch_velbc(cudaStream_t s, const NsArgs& a, const NsBc& bc, double* const vel[3]);
+// max |now - tmp| -> R.result[kSlotMax] (bit pattern), sum (now - tmp)^2 -> R.result[kSlotSum]
+void launch_ns_change(cudaStream_t s, const NsArgs& a, const double* const now[3],
+                      const double* const tmp[3], const ReduceScratch& R);
+
 }  // namespace gbmg

@@ -1,0 +1,191 @@
+"""Host-side mirror of the reference's Adams-Bashforth momentum step, over
+libgbmg's C ABI.
+
+The reference's velocity step ("Two phase flows/newOpenMP/2D/src/ns_solver/
+admas_bashforth_solver.f90:40-67", 3D "Two phase flows/newOpenMP/3D+IBM/src/
+ns_solver/admas_bashforth_solver.f90:43-70") is
+
+    call ppe_sor_init
+    do iter = 1, 4
+        call ns_linearize      ! vel%tmp = vel%now, find_stag_vel
+        call ns_ab_setup       ! velsrc%now = advection + diffusion (+ gravity, tension)
+        call ns_ab_predictor   ! vel%now = vel%old + dt (1.5 velsrc%now - 0.5 velsrc%old); velbc
+        call ppe_sor_solver(p%glb%p_tol)   ! projection + ns_momentum_correction; velbc
+    end do
+    call ns_check_convergence_vel
+
+ns_ab_solver(pp, prm, state) runs that loop on the GPU after pp.ppe_init /
+pp.rho_mu (ppe_sor_init) with the new density; ns_ab_predictor runs one
+predictor pass without the projection and velbc fills the ghost layers.
+
+Arrays keep the reference's ghost cells: every field of `state` except p is
+the padded box, shape (nz+2g, ny+2g, nx+2g) (2D: (ny+2g, nx+2g)), with the
+reference's element (i, j, k) at [k-1+g, j-1+g, i-1+g] and u[.., .., i] the
+face i+1/2 (as the oracle's arrays).  numpy float64 arrays live in host memory,
+torch float64 CUDA tensors are used in place; x must be contiguous and all
+padded arrays must share their strides.  p is the interior pressure (nz, ny,
+nx) (2D (ny, nx)).  state keys: u, v, w (vel%now, in/out), u_old, v_old, w_old,
+su, sv, sw (velsrc%now, out), su_old, sv_old, sw_old, rho, mu, delta, phi
+(the old fields), nrm_x, nrm_y, nrm_z, curv (only with surface tension) and p.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .ppe import ConvergenceError, GBMGError, _field, _is_torch
+
+try:
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+
+@dataclass
+class NSParams:
+    """The reference's p%glb values the step reads (input/default.txt)."""
+    dt: float
+    re: float = 1000.0
+    fr: float = 1.0
+    we: float = 1.0
+    mu_12: float = 1e-2
+    gravity: tuple = (0.0, -1.0, 0.0)
+    btn_g: float = 1.0
+    btn_sf: float = 0.0
+    ghost: int = 3
+    bc: tuple = (1, 1, 1, 1, 1, 1)   # ubc(1:2), vbc(1:2), wbc(1:2): 1 no-slip, 2 slip
+    iterations: int = 4
+    p_tol: float = 1e-10
+
+    def c_struct(self):
+        return _lib.NSParams(int(self.ghost), (C.c_int32 * 6)(*[int(b) for b in self.bc]),
+                             int(self.iterations), float(self.dt), float(self.re), float(self.fr),
+                             float(self.we), float(self.mu_12), float(self.gravity[0]),
+                             float(self.gravity[1]), float(self.gravity[2]), float(self.btn_g),
+                             float(self.btn_sf), float(self.p_tol))
+
+
+def padded_shape(shape, ghost):
+    nz, ny, nx = shape
+    if nz == 1:
+        return (ny + 2 * ghost, nx + 2 * ghost)
+    return (nz + 2 * ghost, ny + 2 * ghost, nx + 2 * ghost)
+
+
+# face axis of each velocity-like field (0 = x, 1 = y, 2 = z), None for cells
+_AXIS = {"u": 0, "v": 1, "w": 2, "u_old": 0, "v_old": 1, "w_old": 2, "su": 0, "sv": 1, "sw": 2,
+         "su_old": 0, "sv_old": 1, "sw_old": 2}
+
+
+def _padded_field(a, name, shape, g):
+    """gbmg_field of a padded array at the address the ABI expects: interior
+    cell (1,1,1), or face 0 of its axis for the velocity-like arrays."""
+    if a is None:
+        return _lib.Field(None, 0, 0), None
+    want = padded_shape(shape, g)
+    if tuple(a.shape) != want:
+        raise ValueError(f"{name}: expected padded shape {want}, got {tuple(a.shape)}")
+    three = len(want) == 3
+    ix = [g] * len(want)       # numpy index of the reference's (1,1,1): [k, j, i]
+    ax = _AXIS.get(name)
+    if ax is not None:
+        ix[len(want) - 1 - ax] -= 1
+    if _is_torch(a):
+        if a.dtype != torch.float64 or not a.is_cuda:
+            raise TypeError(f"{name}: tensors must be float64 CUDA tensors")
+        st = a.stride()
+        if st[-1] != 1:
+            raise ValueError(f"{name}: x must be contiguous")
+        off = sum(i * s for i, s in zip(ix, st))
+        sy = st[-2]
+        sz = st[0] if three else sy * want[0]
+        return _lib.Field(a.data_ptr() + 8 * off, sy, sz), _lib.GBMG_MEM_DEVICE
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64:
+        raise TypeError(f"{name}: arrays must be float64 numpy arrays or torch tensors")
+    st = [s // 8 for s in a.strides]
+    if st[-1] != 1:
+        raise ValueError(f"{name}: x must be contiguous")
+    off = sum(i * s for i, s in zip(ix, st))
+    sy = st[-2]
+    sz = st[0] if three else sy * want[0]
+    return _lib.Field(a.ctypes.data + 8 * off, sy, sz), _lib.GBMG_MEM_HOST
+
+
+def _fields(pp, prm, state):
+    shape = pp.shape
+    three = shape[0] > 1
+    f = _lib.NSFields()
+    mems = set()
+    for name in _lib.NS_FIELDS:
+        a = state.get(name)
+        if name == "p":
+            fld, m = _field(a, shape)
+        elif not three and name in ("w", "w_old", "sw", "sw_old", "nrm_z"):
+            fld, m = _lib.Field(None, 0, 0), None
+        elif name in ("nrm_x", "nrm_y", "nrm_z", "curv") and not prm.btn_sf:
+            fld, m = _lib.Field(None, 0, 0), None
+        else:
+            if a is None:
+                raise ValueError(f"state['{name}'] is missing")
+            fld, m = _padded_field(a, name, shape, prm.ghost)
+        setattr(f, name, fld)
+        if m is not None:
+            mems.add(m)
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must be in the same memory (host or CUDA)")
+    return f, mems.pop()
+
+
+def _sync(state):
+    if torch is not None and any(_is_torch(a) and a.is_cuda for a in state.values()
+                                 if a is not None):
+        torch.cuda.current_stream().synchronize()
+
+
+def ns_ab_solver(pp, prm: NSParams, state, check=True):
+    """ns_ab_solver_SOR after ppe_sor_init (call pp.ppe_init(rho_now) or
+    pp.rho_mu(phi_now, ...) first): velsrc%tmp, then prm.iterations passes of
+    predictor + projection.  Updates u, v, w, su, sv, sw and p of `state` in
+    place; returns the statistics (linf, l2f of the last pass, solve cycles,
+    worst status).  Raises ConvergenceError where the reference would STOP."""
+    f, m = _fields(pp, prm, state)
+    _sync(state)
+    c = prm.c_struct()
+    st = _lib.NSStats()
+    rc = pp._L.gbmg_ns_ab_step(pp._h, C.byref(c), C.byref(f), m, C.byref(st))
+    stats = st.as_dict()
+    if rc in (_lib.GBMG_NOT_CONVERGED, _lib.GBMG_DIVERGED):
+        if check:
+            raise ConvergenceError(f"ns_ab_solver: pressure solve status {rc}, relative residual "
+                                   f"{stats['max_rel_residual']:.3e}", stats)
+    elif rc != _lib.GBMG_OK:
+        pp._check(rc, "ns_ab_solver")
+    return stats
+
+
+def ns_ab_predictor(pp, prm: NSParams, state):
+    """One pass of ns_linearize + ns_ab_setup + ns_ab_predictor + velbc with
+    vel%tmp = the given u, v, w (no projection)."""
+    f, m = _fields(pp, prm, state)
+    _sync(state)
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_ab_predict(pp._h, C.byref(c), C.byref(f), m), "ns_ab_predictor")
+
+
+def velbc(pp, prm: NSParams, u, v, w=None):
+    """velbc in place on padded u, v (, w)."""
+    three = pp.shape[0] > 1
+    fu, m1 = _padded_field(u, "u", pp.shape, prm.ghost)
+    fv, m2 = _padded_field(v, "v", pp.shape, prm.ghost)
+    fw, m3 = _padded_field(w if three else None, "w", pp.shape, prm.ghost)
+    mems = {m for m in (m1, m2, m3) if m is not None}
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must be in the same memory (host or CUDA)")
+    _sync({"u": u, "v": v, "w": w})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_velbc(pp._h, C.byref(c), fu, fv, fw, mems.pop()), "velbc")
+
+
+__all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "padded_shape",
+           "ConvergenceError", "GBMGError"]

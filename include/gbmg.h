@@ -212,6 +212,84 @@ int gbmg_div_stats_noalloc(const gbmg_grid* grid, gbmg_field u, gbmg_field v, gb
 int gbmg_adjoint(gbmg_handle* h, gbmg_field p, gbmg_field lam, gbmg_field phi, double eps,
                  double rho_pos, double rho_neg, gbmg_field grad_rho, gbmg_field grad_phi, int mem);
 
+/* ---- Adams-Bashforth momentum step ------------------------------------------
+ * The velocity step around the projection, ns_ab_solver_SOR after
+ * ppe_sor_init ("Two phase flows/newOpenMP/2D/src/ns_solver/
+ * admas_bashforth_solver.f90:40-67"; 3D "Two phase flows/newOpenMP/3D+IBM/
+ * src/ns_solver/admas_bashforth_solver.f90:43-70"): velsrc%tmp from the old
+ * fields (sec_part1..3 of ns_ab_diff.f90: viscous term mu/rho lap(u)/Re, the
+ * interface-viscosity term (1 - mu_12) delta grad(phi).grad(u)/(rho Re),
+ * gravity btn_g g/Fr and surface tension btn_sf curv delta n/(We rho)), then
+ * `iterations` passes (the reference: 4) of
+ *   ns_linearize     vel%tmp = vel%now (the advecting velocity), averaged to
+ *                    each face by find_stag_vel (bcs.f90),
+ *   ns_ab_setup      velsrc%now = second-order upwind advection of vel%old
+ *                    (ns_ab_adv_source_sec) + velsrc%tmp,
+ *   ns_ab_predictor  vel%now = vel%old + dt (1.5 velsrc%now - 0.5 velsrc%old),
+ *                    velbc,
+ *   the projection   gbmg_project's solve and correction with the handle's
+ *                    operator (set it from rho%now first: gbmg_set_rho /
+ *                    gbmg_set_phi, the reference's ppe_sor_init), velbc,
+ * and ns_check_convergence_vel (linf, l2f of vel%now - vel%tmp of the last
+ * pass).  All arithmetic of the explicit part is FP64 in the reference's
+ * operand order, so velsrc%now and the predicted velocity are the reference
+ * formulas' own doubles; the projection solves to p_tol.
+ *
+ * Arrays keep the reference's ghost cells: each is the padded box of `ghost`
+ * layers around the interior, and all of them (except p) share one pair of
+ * strides (a Fortran caller's arrays of one shape).  Addresses follow the
+ * layout above: a cell array at its interior cell (1,1,1) (c_loc(phi(1,1,1))),
+ * u at c_loc(u(0,1,1)), v at c_loc(v(1,0,1)), w at c_loc(w(1,1,0)).  velbc
+ * (bcs.f90:28-148, 3D :44-257) fills every ghost layer: per wall, bc 1
+ * (no-slip) mirrors the interior negated, 2 (slip) copies it, and the
+ * wall-normal face is set to 0; other values leave that wall's ghosts.  The
+ * surface-tension term is added only when btn_sf != 0 (the reference computes
+ * the curvature only then); nrm_* and curv may be NULL otherwise.  In 2D
+ * (nz = 1) the w arrays, nrm_z and gz are ignored.  p is an interior cell
+ * array with its own strides (ghosts untouched).  Needs ghost >= 2 and at
+ * least ghost + 1 cells per axis. */
+typedef struct {
+  int32_t ghost;       /* ghost layers of every array (the reference's ghc) */
+  int32_t bc[6];       /* velbc of the walls x-, x+, y-, y+, z-, z+: ubc(1:2), vbc(1:2), wbc(1:2) */
+  int32_t iterations;  /* predictor-projection passes */
+  double dt;
+  double re, fr, we;   /* Reynolds, Froude and Weber numbers */
+  double mu_12;        /* viscosity ratio */
+  double gx, gy, gz;   /* gravity direction */
+  double btn_g, btn_sf; /* gravity and surface-tension switches */
+  double p_tol;        /* relative residual of each pressure solve */
+} gbmg_ns_params;
+
+typedef struct {
+  gbmg_field u, v, w;                   /* vel%now: in, the first linearisation; out, the step */
+  gbmg_field u_old, v_old, w_old;       /* vel%old */
+  gbmg_field su, sv, sw;                /* velsrc%now (out: interior written) */
+  gbmg_field su_old, sv_old, sw_old;    /* velsrc%old */
+  gbmg_field rho, mu, delta, phi;       /* rho%old, mu%old, delta%old, phi%old */
+  gbmg_field nrm_x, nrm_y, nrm_z, curv; /* normals%{x,y,z,curv}%old */
+  gbmg_field p;                         /* p%now: warm start in, pressure out */
+} gbmg_ns_fields;
+
+typedef struct {
+  int32_t status;          /* worst gbmg_status of the pressure solves */
+  int32_t cycles;          /* cycles (or Krylov iterations) of all solves */
+  double max_rel_residual; /* largest final relative residual of the solves */
+  double linf, l2f;        /* ns_check_convergence_vel of the last pass */
+  double ms;               /* device time of the call */
+} gbmg_ns_stats;
+
+int gbmg_ns_ab_step(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
+                    gbmg_ns_stats* stats);
+
+/* One predictor pass without the projection: velsrc%tmp, ns_linearize,
+ * ns_ab_setup, ns_ab_predictor and velbc (su, sv, sw and u, v, w written). */
+int gbmg_ns_ab_predict(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f,
+                       int mem);
+
+/* velbc alone on u, v, w (uses prm->ghost and prm->bc). */
+int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_field v,
+                  gbmg_field w, int mem);
+
 /* Copies level `level`'s face coefficients (FP64) into cell-shaped arrays of
  * that level's size (gbmg_level_dims).  For tests of the coarsening rule. */
 int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,
@@ -240,7 +318,8 @@ enum {
   GBMG_PROF_VECTOR = 8,        /* mean projection, p += e, Krylov vector kernels */
   GBMG_PROF_SETUP = 9,         /* coefficients, coarse operators, coarse inverse */
   GBMG_PROF_CERTIFY = 10,      /* native FP64 residual after a mixed-precision solve */
-  GBMG_PROF_CLASSES = 11
+  GBMG_PROF_MOMENTUM = 11,     /* momentum step: sources, predictor, velbc, velocity change */
+  GBMG_PROF_CLASSES = 12
 };
 int gbmg_set_profiling(gbmg_handle* h, int on);
 /* ms[c] = summed device time, launches[c] = launch count of class c since

@@ -1476,7 +1476,7 @@ void or_ns_diffusion(const or_grid* gr, const or_ns_params* prm, const double* U
 /* One predictor pass after ns_linearize (vel%tmp = the advecting velocity Ut,
  * Vt, Wt): find_stag_vel's four-point averages of the other components at
  * each face (bcs.f90), the second-order upwind advection of the old velocity
- * (ns_ab_adv_source_sec, NO2 ns_ab_adv.f90:1-46, NO3 :1-73),
+ * (ns_ab_adv_source_sec, NO2 ns_ab_adv.f90:1-42, NO3 :1-73),
  * velsrc%now = advection + velsrc%tmp (ns_ab_setup) and the AB2 predictor
  * vel%now = vel%old + dt (1.5 velsrc%now - 0.5 velsrc%old) (ns_ab_predictor)
  * over the reference's interior loops i = 1..nx etc. (which include the high
@@ -1537,7 +1537,7 @@ void or_ns_advance(const or_grid* gr, const or_ns_params* prm, const double* U, 
       }
 }
 
-/* velbc (NO2 bcs.f90:28-132, NO3 :44-257): for each wall with bc 1 (no-slip)
+/* velbc (NO2 bcs.f90:28-148, NO3 :44-257): for each wall with bc 1 (no-slip)
  * or 2 (slip) the g ghost layers mirror the interior, negated for no-slip;
  * the normal component's wall face is set to 0.  Passes in the reference's
  * order: x (low, high), then y, then z, each over the whole padded extent of
@@ -1619,7 +1619,7 @@ void or_velbc(const or_grid* gr, int g, const int32_t bc[6], double* U, double* 
 }
 
 /* linf and l2f of vel%now - vel%tmp over the interior loops
- * (ns_check_convergence_vel, NO2 ns_solvers.f90:85-116, NO3 :92-126):
+ * (ns_check_convergence_vel, NO2 ns_solvers.f90:85-115, NO3 :92-126):
  * l2f = sqrt(sum / (2 nx ny)) in 2D, sqrt(sum / (3 nx ny nz)) in 3D. */
 void or_ns_vel_change(const or_grid* gr, int g, const double* Un, const double* Vn,
                       const double* Wn, const double* Ut, const double* Vt, const double* Wt,
@@ -1688,7 +1688,7 @@ static int ns_project(const or_grid* gr, const or_ns_params* prm, const double* 
   return rc;
 }
 
-/* ns_ab_solver_SOR after ppe_sor_init (admas_bashforth_solver.f90:39-67):
+/* ns_ab_solver_SOR after ppe_sor_init (NO2 admas_bashforth_solver.f90:40-67, NO3 :43-70):
  * velsrc%tmp once (it depends on the old fields only), then `iterations`
  * passes of ns_linearize, ns_ab_setup, ns_ab_predictor (+ velbc) and the
  * pressure step, then ns_check_convergence_vel.  rho is the new cell density

@@ -754,12 +754,12 @@ def level_set_rk3_redis(phi, ls_wid, rdt, dx, dy, dz, rho_12=1e-3, btn=1, max_it
 
 # ---------------------------------------------------------------------------
 # Momentum step of the Adams-Bashforth solver, literally:
-#   ns_ab_adv_source_sec  "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ab_adv.f90:1-46"
+#   ns_ab_adv_source_sec  "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ab_adv.f90:1-42"
 #                         (3D: ".../3D+IBM/src/ns_solver/ns_ab_adv.f90:1-73")
 #   sec_part1..3          ".../2D/src/ns_solver/ns_ab_diff.f90:10-135" (3D :10-199)
 #   ns_ab_setup, ns_ab_predictor
 #                         ".../2D/src/ns_solver/admas_bashforth_solver.f90:19-93"
-#   find_stag_vel, velbc  ".../2D/src/others/bcs.f90:28-132,265-287" (3D :44-257,464-495)
+#   find_stag_vel, velbc  ".../2D/src/others/bcs.f90:28-148,265-400" (3D :44-257,464-774)
 # Arrays are the reference's ghost-padded boxes (numpy shape (ny+2g, nx+2g) or
 # (nz+2g, ny+2g, nx+2g)); R[i, j(, k)] reads them with the Fortran indices.
 # ---------------------------------------------------------------------------

@@ -1,0 +1,196 @@
+"""The Adams-Bashforth momentum step on the GPU (gbmg_ns_*, momentum.py)
+against the CPU oracle's restatement (or_ns_*): the explicit part (sources,
+predictor, velbc) is FP64 in the reference's operand order on both sides and
+compared bit for bit; the whole step includes pressure solves to p_tol on both
+sides and is compared to a tolerance that follows from it."""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import GBMGError, NSParams, PressurePoisson, inputs
+from fortrancfd_gb300 import ns_ab_predictor, ns_ab_solver, velbc
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+G = 3
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def _setup(shape, seed=11, extent=None, sf=1.0, noise=0.01):
+    nz, ny, nx = shape
+    ext = extent or (1.0, ny / nx, (nz / nx) if nz > 1 else 1.0)
+    case = inputs.custom(shape, extent=ext, centers=((0.5 * ext[0], 0.45 * ext[1], 0.5 * ext[2]),),
+                         radii=(0.25 * min(ext[0], ext[1]),), seed=seed)
+    st = inputs.momentum_state(case, ghost=G, amplitude=0.3)
+    rng = np.random.default_rng(seed)
+    for k in ("u", "v", "w"):  # ghosts as arbitrary as the interior
+        if st[k] is not None:
+            st[k] = st[k] + noise * rng.standard_normal(st[k].shape)
+    st["p"] = 0.01 * rng.standard_normal(shape)
+    prm = NSParams(dt=2e-3, re=100.0, fr=0.5, we=2.0, mu_12=1e-2, gravity=(0.3, -0.8, -0.5),
+                   btn_g=1.0, btn_sf=sf, ghost=G, p_tol=1e-12)
+    return case, st, prm
+
+
+def _oprm(prm):
+    return orc.ns_params(ghost=prm.ghost, bc=prm.bc, iterations=prm.iterations, dt=prm.dt,
+                         re=prm.re, fr=prm.fr, we=prm.we, mu_12=prm.mu_12, gravity=prm.gravity,
+                         btn_g=prm.btn_g, btn_sf=prm.btn_sf, p_tol=prm.p_tol)
+
+
+def _state_for_lib(st, three):
+    s = {"u": st["u"].copy(), "v": st["v"].copy(), "w": st["w"].copy() if three else None,
+         "u_old": st["u"], "v_old": st["v"], "w_old": st["w"],
+         "su_old": st["su_old"], "sv_old": st["sv_old"], "sw_old": st["sw_old"],
+         "rho": st["rho"], "mu": st["mu"], "delta": st["delta"], "phi": st["phi"],
+         "nrm_x": st["nrm_x"], "nrm_y": st["nrm_y"], "nrm_z": st["nrm_z"], "curv": st["curv"],
+         "p": st["p"].copy()}
+    s["su"] = np.zeros_like(st["u"])
+    s["sv"] = np.zeros_like(st["v"])
+    s["sw"] = np.zeros_like(st["u"]) if three else None
+    return s
+
+
+def _oracle_predict(case, st, prm):
+    three = case.shape[0] > 1
+    nc = 3 if three else 2
+    op = _oprm(prm)
+    diff = orc.ns_diffusion(case.shape, case.spacing, op, st)[:nc]
+    old = tuple(st[k] for k in ("u", "v", "w")[:nc])
+    so = tuple(st[k] for k in ("su_old", "sv_old", "sw_old")[:nc])
+    src, vel = orc.ns_advance(case.shape, case.spacing, op, old, old, diff, so)
+    vel = [a.copy() for a in vel] + [None] * (3 - nc)
+    orc.velbc(case.shape, op, *vel[:nc])
+    return src, vel
+
+
+@pytest.mark.parametrize("shape", [(1, 24, 32), (6, 7, 9), (12, 10, 8)])
+@pytest.mark.parametrize("sf", [0.0, 1.0])
+def test_predictor_matches_oracle_bitwise(cuda, shape, sf):
+    case, st, prm = _setup(shape, sf=sf)
+    three = shape[0] > 1
+    src, vel = _oracle_predict(case, st, prm)
+    s = _state_for_lib(st, three)
+    with PressurePoisson(shape, case.spacing) as pp:
+        n0 = pp.kernel_launches
+        ns_ab_predictor(pp, prm, s)
+        assert pp.kernel_launches > n0
+    for c, (k, sk) in enumerate(zip(("u", "v", "w"), ("su", "sv", "sw"))):
+        if c == 2 and not three:
+            break
+        assert np.array_equal(_bits(s[k]), _bits(vel[c])), k
+        # velsrc%now: interior written, ghosts as given (zeros)
+        assert np.array_equal(_bits(s[sk]), _bits(src[c])), sk
+
+
+@pytest.mark.parametrize("shape", [(1, 8, 5), (4, 6, 5), (9, 8, 10)])
+@pytest.mark.parametrize("bc", [(1, 1, 1, 1, 1, 1), (2, 1, 1, 2, 2, 1), (0, 2, 1, 0, 1, 3)])
+def test_velbc_matches_oracle_bitwise(cuda, shape, bc):
+    import torch
+    rng = np.random.default_rng(4)
+    three = shape[0] > 1
+    ps = orc.padded_shape(shape, G)
+    f = [rng.standard_normal(ps) for _ in range(3 if three else 2)]
+    want = [a.copy() for a in f]
+    prm = NSParams(dt=1.0, ghost=G, bc=bc)
+    orc.velbc(shape, _oprm(prm), *want)
+    with PressurePoisson(shape, (0.1, 0.1, 0.1)) as pp:
+        t = [torch.from_numpy(a).to(cuda) for a in f]
+        velbc(pp, prm, *t)
+        got = [a.cpu().numpy() for a in t]
+        h = [a.copy() for a in f]
+        velbc(pp, prm, *h)
+    for c in range(len(f)):
+        assert np.array_equal(_bits(got[c]), _bits(want[c])), c
+        assert np.array_equal(_bits(h[c]), _bits(want[c])), c
+
+
+def _compare_step(out, s, three, tol):
+    for k in ("u", "v", "w")[: 3 if three else 2]:
+        scale = np.abs(out[k]).max()
+        np.testing.assert_allclose(s[k], out[k], rtol=0, atol=tol * scale, err_msg=k)
+    for k in ("su", "sv", "sw")[: 3 if three else 2]:
+        scale = np.abs(out[k]).max()
+        np.testing.assert_allclose(s[k], out[k], rtol=0, atol=tol * scale, err_msg=k)
+
+
+@pytest.mark.parametrize("shape", [(1, 32, 32), (16, 16, 16), (1, 48, 64)])
+def test_step_matches_oracle(cuda, shape):
+    """Whole step with FP64 solves to 1e-12 on both sides: velocities and
+    sources agree to 1e-8 of their largest value, the pressure to 1e-7 of
+    its, and the change statistics to 1e-6 (they measure a difference of
+    iterates, 1e-5 of the velocity)."""
+    case, st, prm = _setup(shape, sf=1.0)
+    three = shape[0] > 1
+    nc = 3 if three else 2
+    vel = tuple(st[k] for k in ("u", "v", "w")[:nc])
+    so = tuple(st[k] for k in ("su_old", "sv_old", "sw_old")[:nc])
+    out = orc.ns_ab_step(case.shape, case.spacing, _oprm(prm), st["rho_now"], vel, st, so,
+                         st["p"], krylov=1)
+    assert out["status"] == 0
+    s = _state_for_lib(st, three)
+    with PressurePoisson(shape, case.spacing, krylov=True) as pp:
+        pp.ppe_init(st["rho_now"])
+        stats = ns_ab_solver(pp, prm, s)
+    assert stats["status"] == 0 and stats["max_rel_residual"] < 1e-12
+    _compare_step(out, s, three, 1e-8)
+    p = s["p"].reshape(out["p"].shape)
+    np.testing.assert_allclose(p, out["p"], rtol=0, atol=1e-7 * np.abs(out["p"]).max())
+    assert stats["linf"] == pytest.approx(out["linf"], rel=1e-6)
+    assert stats["l2f"] == pytest.approx(out["l2f"], rel=1e-6)
+
+
+def test_step_on_device_tensors_mixed_precision(cuda):
+    """Device-resident state (CUDA tensors) with the mixed-precision solve."""
+    import torch
+    shape = (16, 16, 16)
+    case, st, prm = _setup(shape, sf=1.0)
+    out = orc.ns_ab_step(case.shape, case.spacing, _oprm(prm), st["rho_now"],
+                         (st["u"], st["v"], st["w"]), st, (st["su_old"], st["sv_old"],
+                                                         st["sw_old"]), st["p"], krylov=1)
+    s = _state_for_lib(st, True)
+    t = {k: (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) if a is not None else None)
+         for k, a in s.items()}
+    with PressurePoisson(shape, case.spacing, precision="mixed", krylov=True) as pp:
+        pp.ppe_init(torch.from_numpy(st["rho_now"]).to(cuda))
+        stats = ns_ab_solver(pp, prm, t)
+    assert stats["status"] == 0
+    got = {k: (a.cpu().numpy() if a is not None else None) for k, a in t.items()}
+    _compare_step(out, got, True, 1e-8)
+
+
+def test_step_two_iterations_and_slip_walls(cuda):
+    shape = (1, 40, 40)
+    case, st, prm = _setup(shape, sf=0.0)
+    prm.iterations = 2
+    prm.bc = (2, 2, 1, 2, 1, 1)
+    op = _oprm(prm)
+    out = orc.ns_ab_step(case.shape, case.spacing, op, st["rho_now"], (st["u"], st["v"]), st,
+                         (st["su_old"], st["sv_old"]), st["p"], krylov=1)
+    s = _state_for_lib(st, False)
+    s["nrm_x"] = s["nrm_y"] = s["curv"] = None
+    with PressurePoisson(shape, case.spacing, krylov=True) as pp:
+        pp.ppe_init(st["rho_now"])
+        ns_ab_solver(pp, prm, s)
+    _compare_step(out, s, False, 1e-8)
+
+
+def test_errors(cuda):
+    shape = (1, 16, 16)
+    case, st, prm = _setup(shape)
+    s = _state_for_lib(st, False)
+    with PressurePoisson(shape, case.spacing) as pp:
+        with pytest.raises(GBMGError, match="density"):
+            ns_ab_solver(pp, prm, s)   # no ppe_init yet
+        pp.ppe_init(st["rho_now"])
+        bad = NSParams(dt=prm.dt, ghost=1)
+        with pytest.raises((GBMGError, ValueError)):
+            ns_ab_solver(pp, bad, s)
+        s2 = dict(s)
+        big = np.zeros((s["mu"].shape[0], s["mu"].shape[1] + 4))
+        s2["mu"] = big[:, :s["mu"].shape[1]]  # other strides than the rest
+        with pytest.raises(GBMGError, match="strides"):
+            ns_ab_solver(pp, prm, s2)
