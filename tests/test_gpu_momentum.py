@@ -67,7 +67,7 @@ def _oracle_predict(case, st, prm):
     return src, vel
 
 
-@pytest.mark.parametrize("shape", [(1, 24, 32), (6, 7, 9), (12, 10, 8)])
+@pytest.mark.parametrize("shape", [(1, 24, 32), (6, 8, 8), (8, 12, 16)])
 @pytest.mark.parametrize("sf", [0.0, 1.0])
 def test_predictor_matches_oracle_bitwise(cuda, shape, sf):
     case, st, prm = _setup(shape, sf=sf)
@@ -86,7 +86,7 @@ def test_predictor_matches_oracle_bitwise(cuda, shape, sf):
         assert np.array_equal(_bits(s[sk]), _bits(src[c])), sk
 
 
-@pytest.mark.parametrize("shape", [(1, 8, 5), (4, 6, 5), (9, 8, 10)])
+@pytest.mark.parametrize("shape", [(1, 8, 5), (4, 8, 8), (6, 8, 10)])
 @pytest.mark.parametrize("bc", [(1, 1, 1, 1, 1, 1), (2, 1, 1, 2, 2, 1), (0, 2, 1, 0, 1, 3)])
 def test_velbc_matches_oracle_bitwise(cuda, shape, bc):
     import torch
