@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-multi", action="store_true", help="skip the 512^3 16-bubble section")
     ap.add_argument("--no-rollout", action="store_true", help="skip the 20-step rollout section")
     ap.add_argument("--no-levelset", action="store_true", help="skip the level-set advection section")
+    ap.add_argument("--no-momentum", action="store_true", help="skip the momentum-step section")
     return ap.parse_args()
 
 
@@ -417,6 +418,138 @@ def levelset_section(dev, stream, case, phi_h, u_h, v_h, w_h, steps=5):
             "cpu_oracle_redistance_ms_per_iteration": cpu_redis_it_ms}
 
 
+def momentum_section(dev, stream, case, iterations=4, reps=5):
+    """The Adams-Bashforth momentum step of the same case (ns_ab_solver_SOR:
+    velsrc%tmp, then `iterations` passes of predictor + mixed-precision
+    projection to TOL, velbc, ns_check_convergence_vel) on device-resident
+    ghost-padded arrays (g = 3), timed with CUDA events; a profiled step gives
+    the momentum kernels' share and roofline; the same step through the C ABI
+    with host arrays (e2e) and the CPU oracle's step beside it."""
+    import torch
+
+    from fortrancfd_gb300 import NSParams, PressurePoisson, inputs, ns_ab_predictor, ns_ab_solver
+    from oracle import oracle as orc
+
+    rho_12 = min(case.rho_pos, case.rho_neg) / max(case.rho_pos, case.rho_neg)
+    st = inputs.momentum_state(case, ghost=3, rho_12=rho_12, mu_12=1e-2, amplitude=0.1)
+    three = case.dim == 3
+    prm = NSParams(dt=case.dt, re=1000.0, fr=0.4096, we=1.0, mu_12=1e-2,
+                   gravity=(0.0, 0.0, -1.0) if three else (0.0, -1.0, 0.0), btn_g=1.0,
+                   btn_sf=1.0, ghost=3, iterations=iterations, p_tol=TOL)
+    names = ("u", "v", "w", "u_old", "v_old", "w_old", "su", "sv", "sw", "su_old", "sv_old",
+             "sw_old", "rho", "mu", "delta", "phi", "nrm_x", "nrm_y", "nrm_z", "curv", "p")
+    src = {"u": st["u"], "v": st["v"], "w": st["w"], "u_old": st["u"], "v_old": st["v"],
+           "w_old": st["w"], "su": np.zeros_like(st["u"]), "sv": np.zeros_like(st["v"]),
+           "sw": np.zeros_like(st["u"]) if three else None}
+    for k in names:
+        src.setdefault(k, st.get(k))
+    nz, ny, nx = case.shape
+    n = nx * ny * nz
+    with torch.cuda.stream(stream):
+        t = {k: (torch.from_numpy(np.ascontiguousarray(a)).to(dev) if a is not None else None)
+             for k, a in src.items()}
+        init = {k: t[k].clone() for k in ("u", "v", "w", "p") if t[k] is not None}
+        pp = PressurePoisson(case.shape, case.spacing, precision="mixed", stream=stream,
+                             nu1=NU1, nu2=NU2)
+        pp.ppe_init(torch.from_numpy(st["rho_now"]).to(dev))
+
+        def reset():
+            for k, a in init.items():
+                t[k].copy_(a)
+
+        ns_ab_solver(pp, prm, t)  # warm-up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        times = []
+        n0 = pp.kernel_launches
+        for _ in range(reps):
+            reset()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            stats = ns_ab_solver(pp, prm, t)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = statistics.median(times)
+        launches = (pp.kernel_launches - n0) // reps
+        gpu_u = {k: t[k].cpu().numpy() for k in ("u", "v", "w") if t[k] is not None}
+        # profiled step: the momentum kernels' time against the solves'
+        reset()
+        pp.set_profiling(True)
+        ns_ab_solver(pp, prm, t)
+        prof = pp.profile()
+        pp.set_profiling(False)
+        # one predictor pass without the projection, for the bitwise check
+        # against the oracle at full size below
+        reset()
+        ns_ab_predictor(pp, prm, t)
+        pred = {k: t[k].cpu().numpy() for k in ("u", "v", "w", "su", "sv", "sw")
+                if t[k] is not None}
+        # e2e: the same step through the C ABI on host arrays
+        host = {k: (np.array(a, copy=True) if a is not None else None) for k, a in src.items()}
+        t0 = time.perf_counter()
+        ns_ab_solver(pp, prm, host)
+        e2e_ms = (time.perf_counter() - t0) * 1e3
+        pp.close()
+    mom_ms, mom_cnt = prof.get("momentum", (0.0, 0))
+    prof_total = sum(v[0] for v in prof.values())
+    nc = 3 if three else 2
+    # algorithmic bytes (8-byte values per cell): sources once (3 velocities,
+    # rho, mu, delta, phi, 3 normals and curv in; 3 out), each pass's fused
+    # predictor (old, tmp, velsrc%tmp, velsrc%old in; velsrc%now, vel%now out)
+    # and the change statistics (2 x 3 in); velbc touches only the ghost shell
+    per_cell = 8 * ((nc + 4 + nc + 1) + nc + iterations * 6 * nc + 2 * nc)
+    alg = per_cell * n
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (mom_ms * 1e-3) / 1e9 if mom_ms else None
+    # FP64 divisions the reference writes, per cell (mu/rho counted once):
+    # sources about 20 per component in 3D (14 in 2D), each pass 2 per
+    # component and axis
+    divs = n * ((20 if three else 14) * nc + iterations * 2 * nc * nc)
+    # the CPU oracle's step on the host cores
+    vel = tuple(st[k] for k in ("u", "v", "w")[:nc])
+    so = tuple(st[k] for k in ("su_old", "sv_old", "sw_old")[:nc])
+    op = orc.ns_params(ghost=3, bc=prm.bc, iterations=iterations, dt=prm.dt, re=prm.re,
+                       fr=prm.fr, we=prm.we, mu_12=prm.mu_12, gravity=prm.gravity,
+                       btn_g=prm.btn_g, btn_sf=prm.btn_sf, p_tol=TOL)
+    # the predictor pass: oracle sources + advance + velbc, compared bit for bit
+    t0 = time.perf_counter()
+    dif = orc.ns_diffusion(case.shape, case.spacing, op, st)[:nc]
+    osrc, ovel = orc.ns_advance(case.shape, case.spacing, op, vel, vel, dif, so)
+    ovel = [a.copy() for a in ovel] + [None] * (3 - nc)
+    orc.velbc(case.shape, op, *ovel[:nc])
+    cpu_pred_ms = (time.perf_counter() - t0) * 1e3
+    pred_equal = all(np.array_equal(pred[k].view(np.int64), ovel[c].view(np.int64))
+                     for c, k in enumerate(("u", "v", "w")[:nc]))
+    pred_equal = pred_equal and all(
+        np.array_equal(pred[k].view(np.int64), osrc[c].view(np.int64))
+        for c, k in enumerate(("su", "sv", "sw")[:nc]))
+    t0 = time.perf_counter()
+    out = orc.ns_ab_step(case.shape, case.spacing, op, st["rho_now"], vel, st, so, st["p"],
+                         krylov=1)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    diff = max(float(np.abs(gpu_u[k] - out[k]).max() / np.abs(out[k]).max()) for k in gpu_u)
+    return {"workload": f"{case.name}: Adams-Bashforth momentum step on the {nx}x{ny}x{nz} grid "
+                        f"(3 ghost layers): sources (viscous, interface viscosity, gravity, "
+                        f"surface tension) + {iterations} passes of AB2 predictor, velbc and the "
+                        f"mixed-precision projection to {TOL}; FP64 explicit part",
+            "ms_per_step": ms, "ms_min": min(times), "cell_steps_per_s": n / (ms * 1e-3),
+            "kernels_per_step": launches, "solve_cycles_per_step": stats["cycles"], "linf": stats["linf"], "l2f": stats["l2f"],
+            "momentum_kernels_ms": mom_ms, "momentum_launches": mom_cnt,
+            "momentum_share": mom_ms / prof_total if prof_total else None,
+            "roofline_momentum": {"bound": "fp64 divisions (the reference's operand order kept)",
+                                  "achieved_gbs": achieved, "peak_gbs": peak,
+                                  "frac_hbm": achieved / peak if achieved else None,
+                                  "peak_source": peak_kind, "algorithmic_bytes": alg,
+                                  "fp64_divisions": divs,
+                                  "divisions_per_ns": divs / (mom_ms * 1e6) if mom_ms else None},
+            "e2e_host_arrays_ms": e2e_ms,
+            "cpu_oracle_ms_per_step": cpu_ms, "cpu_threads": orc.num_threads(),
+            "cpu_oracle_predictor_ms": cpu_pred_ms,
+            "predictor_gpu_equals_oracle_bitwise": bool(pred_equal),
+            "gpu_vs_oracle_max_rel_diff": diff}
+
+
+
 def rollout_section(dev, stream, scale=1, steps=20, krylov="fgmres"):
     """The 20-step differentiable projection rollout (128x128x256, 4 bubbles):
     forward (20 mixed solves) and backward (20 adjoint solves and the
@@ -705,6 +838,14 @@ def run_ours(args):
         except Exception as exc:
             lset = {"error": f"{type(exc).__name__}: {exc}"}
 
+    mom = None
+    if not args.no_momentum:
+        try:
+            mom = momentum_section(dev, stream, case)
+        except Exception as exc:
+            mom = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
@@ -727,7 +868,7 @@ def run_ours(args):
                            "parallelism": f"replicas x{world}"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "adjoint": adj, "multi_bubble": multi,
-                "rollout": roll, "levelset": lset}
+                "rollout": roll, "levelset": lset, "momentum": mom}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
         print(json.dumps(line), flush=True)

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "gbmg.h"
+#include "fdiv.cuh"
 #include "gbmg_internal.h"
 
 using namespace gbmg;
@@ -1439,6 +1440,20 @@ int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* 
   a.dx = g.dx; a.dy = g.dy; a.dz = g.dz;
   a.dt = prm->dt; a.re = prm->re; a.fr = prm->fr; a.we = prm->we; a.mu_12 = prm->mu_12;
   a.gx = prm->gx; a.gy = prm->gy; a.gz = prm->gz; a.btn_g = prm->btn_g; a.btn_sf = prm->btn_sf;
+  // reciprocals of the constant divisors (IEEE divisions, so RN(1/b)), and
+  // the gravity source (g_d btn_g)/fr as the reference evaluates it per cell
+  const double dvs[7] = {g.dx, g.dy, g.dz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz, prm->re};
+  double* rcp[7] = {&a.rdx, &a.rdy, &a.rdz, &a.rdx2, &a.rdy2, &a.rdz2, &a.rre};
+  a.fast = 1;
+  for (int i = 0; i < 7; ++i) {
+    *rcp[i] = 1.0 / dvs[i];
+    if (!fdiv_divisor_ok(dvs[i])) a.fast = 0;
+  }
+  // GBMG_NS_DIVIDE=1: IEEE divisions throughout (the same doubles, slower)
+  if (const char* e = std::getenv("GBMG_NS_DIVIDE")) a.fast = a.fast && std::atoi(e) == 0;
+  a.gterm[0] = prm->gx * prm->btn_g / prm->fr;
+  a.gterm[1] = prm->gy * prm->btn_g / prm->fr;
+  a.gterm[2] = prm->gz * prm->btn_g / prm->fr;
   for (int i = 0; i < 6; ++i) P->bc.b[i] = prm->bc[i];
   P->lo = -(int64_t)gh - gh * a.sy - (three ? gh * a.sz : 0);
   P->hi = (int64_t)(g.nx + gh - 1) + (g.ny + gh - 1) * a.sy + (three ? (g.nz + gh - 1) * a.sz : 0);

@@ -326,6 +326,12 @@ struct NsArgs {
   int nx, ny, nz, g;
   int64_t sy, sz;
   double dx, dy, dz, dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf;
+  // RN reciprocals of the constant divisors (dx, dy, dz, their squares, re)
+  // and fast = 1 when all of them allow the division-free quotient
+  // (fdiv.cuh); gterm = (g_d btn_g)/fr per axis, the gravity source
+  double rdx, rdy, rdz, rdx2, rdy2, rdz2, rre;
+  double gterm[3];
+  int fast;
 };
 struct NsBc {
   int b[6];  // velbc type of the walls x-, x+, y-, y+, z-, z+ (1 no-slip, 2 slip, else none)

@@ -27,11 +27,14 @@
 // Arithmetic: FP64, every expression in the reference's operand order, and
 // this translation unit is compiled with -fmad=false, so no multiply-add is
 // contracted: each value is the same double rounding as the reference's (and
-// the oracle's, built with -ffp-contract=off), bit for bit.  The kernels are
-// bound by the FP64 divisions the reference writes (by dx, dx^2, rho re, ...),
-// which have to stay divisions for that.
+// the oracle's, built with -ffp-contract=off), bit for bit.  The reference
+// divides a lot (by dx, dx^2, Re, rho Re, ...), and GB300's FP64 pipe is
+// narrow: quotients by a divisor used more than once come from its correctly
+// rounded reciprocal without a division (fdiv.cuh), which yields the same
+// doubles; the rest are IEEE divisions.
 #include <algorithm>
 
+#include "fdiv.cuh"
 #include "gbmg_internal.h"
 #include "reduce.cuh"
 
@@ -40,6 +43,11 @@ namespace gbmg {
 namespace {
 
 constexpr int kNsBx = 32, kNsBy = 8;
+
+// a / b for a constant divisor b with reciprocal y = RN(1/b)
+__device__ __forceinline__ double cdiv(const NsArgs& a, double x, double b, double y) {
+  return a.fast ? div_known(x, b, y) : x / b;
+}
 
 // signed: ghost elements lie before element (1,1,1)
 __device__ __forceinline__ int64_t ns_at(const NsArgs& a, int i, int j, int k) {
@@ -65,35 +73,41 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   const double dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
   const double re = a.re, c1 = 1.0 - a.mu_12;
   const bool sf = a.btn_sf != 0.0;
-  double rho, mu, delta, curv, xx, yy, zz, t;
+  double rho, mu, mr, rr, yr, delta, curv, xx, yy, zz, t;
   double ux, uy, uz, vx, vy, vz, wx, wy, wz, phix, phiy, phiz, dxx, dyy, dzz;
+  // x / (rho re): three quotients share the divisor, so one IEEE division
+  // gives its reciprocal and the quotients follow without dividing
+#define NS_DRR(x) (a.fast ? div_known_checked((x), rr, yr) : (x) / rr)
   // ---- x: u at (i+1/2, j, k) ----
   rho = 0.5 * (R[q] + R[q + sx]);
   mu = 0.5 * (M[q] + M[q + sx]);
-  xx = ((U[q + sx] - 2.0 * U[q]) + U[q - sx]) / dx2;
-  yy = ((U[q + sy] - 2.0 * U[q]) + U[q - sy]) / dy2;
-  t = ((mu / rho) * xx) / re + ((mu / rho) * yy) / re;
+  mr = mu / rho;
+  xx = cdiv(a, (U[q + sx] - 2.0 * U[q]) + U[q - sx], dx2, a.rdx2);
+  yy = cdiv(a, (U[q + sy] - 2.0 * U[q]) + U[q - sy], dy2, a.rdy2);
+  t = cdiv(a, mr * xx, re, a.rre) + cdiv(a, mr * yy, re, a.rre);
   if (kThree) {
-    zz = ((U[q + sz] - 2.0 * U[q]) + U[q - sz]) / dz2;
-    t = t + ((mu / rho) * zz) / re;
+    zz = cdiv(a, (U[q + sz] - 2.0 * U[q]) + U[q - sz], dz2, a.rdz2);
+    t = t + cdiv(a, mr * zz, re, a.rre);
   }
   delta = 0.5 * (D[q] + D[q + sx]);
-  ux = 0.5 * (U[q + sx] - U[q - sx]) / dx;
-  uy = 0.5 * (U[q + sy] - U[q - sy]) / dy;
-  vx = 0.5 * (((V[q + sx] - V[q]) + V[q + sx - sy]) - V[q - sy]) / dx;
-  phix = (P[q + sx] - P[q]) / dx;
-  phiy = 0.25 * (((P[q + sx + sy] - P[q + sx - sy]) + P[q + sy]) - P[q - sy]) / dy;
-  dxx = c1 * delta * phix * 2.0 * ux / (rho * re);
-  dyy = c1 * delta * phiy * (uy + vx) / (rho * re);
+  rr = rho * re;
+  yr = a.fast ? 1.0 / rr : 0.0;
+  ux = cdiv(a, 0.5 * (U[q + sx] - U[q - sx]), dx, a.rdx);
+  uy = cdiv(a, 0.5 * (U[q + sy] - U[q - sy]), dy, a.rdy);
+  vx = cdiv(a, 0.5 * (((V[q + sx] - V[q]) + V[q + sx - sy]) - V[q - sy]), dx, a.rdx);
+  phix = cdiv(a, P[q + sx] - P[q], dx, a.rdx);
+  phiy = cdiv(a, 0.25 * (((P[q + sx + sy] - P[q + sx - sy]) + P[q + sy]) - P[q - sy]), dy, a.rdy);
+  dxx = NS_DRR(c1 * delta * phix * 2.0 * ux);
+  dyy = NS_DRR(c1 * delta * phiy * (uy + vx));
   t = (t + dxx) + dyy;
   if (kThree) {
-    uz = 0.5 * (U[q + sz] - U[q - sz]) / dz;
-    wx = 0.5 * (((W[q + sx] - W[q]) + W[q + sx - sz]) - W[q - sz]) / dx;
-    phiz = 0.25 * (((P[q + sx + sz] - P[q + sx - sz]) + P[q + sz]) - P[q - sz]) / dz;
-    dzz = c1 * delta * phiz * (uz + wx) / (rho * re);
+    uz = cdiv(a, 0.5 * (U[q + sz] - U[q - sz]), dz, a.rdz);
+    wx = cdiv(a, 0.5 * (((W[q + sx] - W[q]) + W[q + sx - sz]) - W[q - sz]), dx, a.rdx);
+    phiz = cdiv(a, 0.25 * (((P[q + sx + sz] - P[q + sx - sz]) + P[q + sz]) - P[q - sz]), dz, a.rdz);
+    dzz = NS_DRR(c1 * delta * phiz * (uz + wx));
     t = t + dzz;
   }
-  t = t + a.gx * a.btn_g / a.fr;
+  t = t + a.gterm[0];
   if (sf) {
     curv = (CV[q] + CV[q + sx]) / 2.0;
     phix = 0.5 * (N1[q] + N1[q + sx]);
@@ -103,30 +117,33 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   // ---- y: v at (i, j+1/2, k) ----
   rho = 0.5 * (R[q] + R[q + sy]);
   mu = 0.5 * (M[q] + M[q + sy]);
-  xx = ((V[q + sx] - 2.0 * V[q]) + V[q - sx]) / dx2;
-  yy = ((V[q + sy] - 2.0 * V[q]) + V[q - sy]) / dy2;
-  t = ((mu / rho) * xx) / re + ((mu / rho) * yy) / re;
+  mr = mu / rho;
+  xx = cdiv(a, (V[q + sx] - 2.0 * V[q]) + V[q - sx], dx2, a.rdx2);
+  yy = cdiv(a, (V[q + sy] - 2.0 * V[q]) + V[q - sy], dy2, a.rdy2);
+  t = cdiv(a, mr * xx, re, a.rre) + cdiv(a, mr * yy, re, a.rre);
   if (kThree) {
-    zz = ((V[q + sz] - 2.0 * V[q]) + V[q - sz]) / dz2;
-    t = t + ((mu / rho) * zz) / re;
+    zz = cdiv(a, (V[q + sz] - 2.0 * V[q]) + V[q - sz], dz2, a.rdz2);
+    t = t + cdiv(a, mr * zz, re, a.rre);
   }
   delta = 0.5 * (D[q] + D[q + sy]);
-  vx = 0.5 * (V[q + sx] - V[q - sx]) / dx;
-  vy = 0.5 * (V[q + sy] - V[q - sy]) / dy;
-  uy = 0.5 * (((U[q + sy] - U[q]) + U[q - sx + sy]) - U[q - sx]) / dy;
-  phix = 0.25 * (((P[q + sx] - P[q - sx]) + P[q + sx + sy]) - P[q - sx + sy]) / dx;
-  phiy = (P[q + sy] - P[q]) / dy;
-  dxx = c1 * delta * phix * (uy + vx) / (rho * re);
-  dyy = c1 * delta * phiy * 2.0 * vy / (rho * re);
+  rr = rho * re;
+  yr = a.fast ? 1.0 / rr : 0.0;
+  vx = cdiv(a, 0.5 * (V[q + sx] - V[q - sx]), dx, a.rdx);
+  vy = cdiv(a, 0.5 * (V[q + sy] - V[q - sy]), dy, a.rdy);
+  uy = cdiv(a, 0.5 * (((U[q + sy] - U[q]) + U[q - sx + sy]) - U[q - sx]), dy, a.rdy);
+  phix = cdiv(a, 0.25 * (((P[q + sx] - P[q - sx]) + P[q + sx + sy]) - P[q - sx + sy]), dx, a.rdx);
+  phiy = cdiv(a, P[q + sy] - P[q], dy, a.rdy);
+  dxx = NS_DRR(c1 * delta * phix * (uy + vx));
+  dyy = NS_DRR(c1 * delta * phiy * 2.0 * vy);
   t = (t + dxx) + dyy;
   if (kThree) {
-    vz = 0.5 * (V[q + sz] - V[q - sz]) / dz;
-    wy = 0.5 * (((W[q + sy] - W[q]) + W[q + sy - sz]) - W[q - sz]) / dy;
-    phiz = 0.25 * (((P[q + sy + sz] - P[q + sy - sz]) + P[q + sz]) - P[q - sz]) / dz;
-    dzz = c1 * delta * phiz * (wy + vz) / (rho * re);
+    vz = cdiv(a, 0.5 * (V[q + sz] - V[q - sz]), dz, a.rdz);
+    wy = cdiv(a, 0.5 * (((W[q + sy] - W[q]) + W[q + sy - sz]) - W[q - sz]), dy, a.rdy);
+    phiz = cdiv(a, 0.25 * (((P[q + sy + sz] - P[q + sy - sz]) + P[q + sz]) - P[q - sz]), dz, a.rdz);
+    dzz = NS_DRR(c1 * delta * phiz * (wy + vz));
     t = t + dzz;
   }
-  t = t + a.gy * a.btn_g / a.fr;
+  t = t + a.gterm[1];
   if (sf) {
     curv = (CV[q] + CV[q + sy]) / 2.0;
     phiy = 0.5 * (N2[q] + N2[q + sy]);
@@ -137,30 +154,34 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   // ---- z: w at (i, j, k+1/2) ----
   rho = 0.5 * (R[q] + R[q + sz]);
   mu = 0.5 * (M[q] + M[q + sz]);
-  xx = ((W[q + sx] - 2.0 * W[q]) + W[q - sx]) / dx2;
-  yy = ((W[q + sy] - 2.0 * W[q]) + W[q - sy]) / dy2;
-  zz = ((W[q + sz] - 2.0 * W[q]) + W[q - sz]) / dz2;
-  t = (((mu / rho) * xx) / re + ((mu / rho) * yy) / re) + ((mu / rho) * zz) / re;
+  mr = mu / rho;
+  xx = cdiv(a, (W[q + sx] - 2.0 * W[q]) + W[q - sx], dx2, a.rdx2);
+  yy = cdiv(a, (W[q + sy] - 2.0 * W[q]) + W[q - sy], dy2, a.rdy2);
+  zz = cdiv(a, (W[q + sz] - 2.0 * W[q]) + W[q - sz], dz2, a.rdz2);
+  t = (cdiv(a, mr * xx, re, a.rre) + cdiv(a, mr * yy, re, a.rre)) + cdiv(a, mr * zz, re, a.rre);
   delta = 0.5 * (D[q] + D[q + sz]);
-  wx = 0.5 * (W[q + sx] - W[q - sx]) / dx;
-  wy = 0.5 * (W[q + sy] - W[q - sy]) / dy;
-  wz = 0.5 * (W[q + sz] - W[q - sz]) / dz;
-  uz = 0.5 * (((U[q + sz] - U[q]) + U[q - sx + sz]) - U[q - sx]) / dz;
-  vz = 0.5 * (((V[q + sz] - V[q]) + V[q - sy + sz]) - V[q - sy]) / dz;
-  phix = 0.25 * (((P[q + sx + sz] - P[q - sx + sz]) + P[q + sx]) - P[q - sx]) / dx;
-  phiy = 0.25 * (((P[q + sy + sz] - P[q - sy + sz]) + P[q + sy]) - P[q - sy]) / dy;
-  phiz = (P[q + sz] - P[q]) / dz;
-  dxx = c1 * delta * phix * (uz + wx) / (rho * re);
-  dyy = c1 * delta * phiy * (vz + wy) / (rho * re);
-  dzz = c1 * delta * phiz * 2.0 * wz / (rho * re);
+  rr = rho * re;
+  yr = a.fast ? 1.0 / rr : 0.0;
+  wx = cdiv(a, 0.5 * (W[q + sx] - W[q - sx]), dx, a.rdx);
+  wy = cdiv(a, 0.5 * (W[q + sy] - W[q - sy]), dy, a.rdy);
+  wz = cdiv(a, 0.5 * (W[q + sz] - W[q - sz]), dz, a.rdz);
+  uz = cdiv(a, 0.5 * (((U[q + sz] - U[q]) + U[q - sx + sz]) - U[q - sx]), dz, a.rdz);
+  vz = cdiv(a, 0.5 * (((V[q + sz] - V[q]) + V[q - sy + sz]) - V[q - sy]), dz, a.rdz);
+  phix = cdiv(a, 0.25 * (((P[q + sx + sz] - P[q - sx + sz]) + P[q + sx]) - P[q - sx]), dx, a.rdx);
+  phiy = cdiv(a, 0.25 * (((P[q + sy + sz] - P[q - sy + sz]) + P[q + sy]) - P[q - sy]), dy, a.rdy);
+  phiz = cdiv(a, P[q + sz] - P[q], dz, a.rdz);
+  dxx = NS_DRR(c1 * delta * phix * (uz + wx));
+  dyy = NS_DRR(c1 * delta * phiy * (vz + wy));
+  dzz = NS_DRR(c1 * delta * phiz * 2.0 * wz);
   t = ((t + dxx) + dyy) + dzz;
-  t = t + a.gz * a.btn_g / a.fr;
+  t = t + a.gterm[2];
   if (sf) {
     curv = (CV[q] + CV[q + sz]) / 2.0;
     phiz = 0.5 * (N3[q] + N3[q + sz]);
     t = t - a.btn_sf * curv * delta * phiz / (a.we * rho);
   }
   TW[q] = t;
+#undef NS_DRR
 }
 
 // (a + |a|) m + (a - |a|) p: the upwind choice of ns_ab_adv_source_sec
@@ -170,17 +191,17 @@ __device__ __forceinline__ double ns_upwind(double a, double m, double p) {
 
 // -(sum over axes of upwind(a_d, one-sided differences of f along d)/2)
 template <bool kThree>
-__device__ __forceinline__ double ns_adv(const double* __restrict__ f, int64_t q, int64_t sy,
-                                         int64_t sz, const double (&a)[3], double dx, double dy,
-                                         double dz) {
-  const int64_t st[3] = {1, sy, sz};
-  const double h[3] = {dx, dy, dz};
+__device__ __forceinline__ double ns_adv(const NsArgs& A, const double* __restrict__ f, int64_t q,
+                                         const double (&a)[3]) {
+  const int64_t st[3] = {1, A.sy, A.sz};
+  const double h[3] = {A.dx, A.dy, A.dz};
+  const double rh[3] = {A.rdx, A.rdy, A.rdz};
   double src = 0.0;
 #pragma unroll
   for (int d = 0; d < (kThree ? 3 : 2); ++d) {
     const int64_t s = st[d];
-    const double fp = 0.5 * ((-f[q + 2 * s] + 4.0 * f[q + s]) - 3.0 * f[q]) / h[d];
-    const double fm = 0.5 * ((f[q - 2 * s] - 4.0 * f[q - s]) + 3.0 * f[q]) / h[d];
+    const double fp = cdiv(A, 0.5 * ((-f[q + 2 * s] + 4.0 * f[q + s]) - 3.0 * f[q]), h[d], rh[d]);
+    const double fm = cdiv(A, 0.5 * ((f[q - 2 * s] - 4.0 * f[q - s]) + 3.0 * f[q]), h[d], rh[d]);
     const double term = ns_upwind(a[d], fm, fp) / 2.0;
     src = d == 0 ? -term : src - term;
   }
@@ -209,14 +230,14 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   c[0] = Ut[q];
   c[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sx]) + Vt[q + sx - sy]);
   c[2] = kThree ? 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sx]) + Wt[q + sx - sz]) : 0.0;
-  src = ns_adv<kThree>(U, q, sy, sz, c, a.dx, a.dy, a.dz) + TU[q];
+  src = ns_adv<kThree>(a, U, q, c) + TU[q];
   SU[q] = src;
   Un[q] = U[q] + dt * (1.5 * src - 0.5 * SUo[q]);
   // y: v at (i, j+1/2, k)
   c[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sy]) + Ut[q - sx + sy]);
   c[1] = Vt[q];
   c[2] = kThree ? 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sy]) + Wt[q + sy - sz]) : 0.0;
-  src = ns_adv<kThree>(V, q, sy, sz, c, a.dx, a.dy, a.dz) + TV[q];
+  src = ns_adv<kThree>(a, V, q, c) + TV[q];
   SV[q] = src;
   Vn[q] = V[q] + dt * (1.5 * src - 0.5 * SVo[q]);
   if (!kThree) return;
@@ -224,7 +245,7 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   c[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sz]) + Ut[q - sx + sz]);
   c[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sz]) + Vt[q - sy + sz]);
   c[2] = Wt[q];
-  src = ns_adv<kThree>(W, q, sy, sz, c, a.dx, a.dy, a.dz) + TW[q];
+  src = ns_adv<kThree>(a, W, q, c) + TW[q];
   SW[q] = src;
   Wn[q] = W[q] + dt * (1.5 * src - 0.5 * SWo[q]);
 }
