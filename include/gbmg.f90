@@ -17,7 +17,7 @@ module gbmg
   integer(c_int), parameter :: GBMG_OUT_OF_MEMORY = 6, GBMG_STATE_ERROR = 7
   integer(c_int), parameter :: GBMG_PREC_FP64 = 0, GBMG_PREC_MIXED = 1
   integer(c_int), parameter :: GBMG_MEM_HOST = 0, GBMG_MEM_DEVICE = 1
-  integer(c_int), parameter :: GBMG_PROF_CLASSES = 11
+  integer(c_int), parameter :: GBMG_PROF_CLASSES = 12
 
   type, bind(c) :: gbmg_grid
     integer(c_int32_t) :: nx, ny, nz
@@ -38,6 +38,24 @@ module gbmg
   type, bind(c) :: gbmg_field
     type(c_ptr)        :: data
     integer(c_int64_t) :: sy, sz
+  end type
+
+  ! the Adams-Bashforth momentum step (gbmg_ns_ab_step)
+  type, bind(c) :: gbmg_ns_params
+    integer(c_int32_t) :: ghost
+    integer(c_int32_t) :: bc(6)        ! ubc(1:2), vbc(1:2), wbc(1:2)
+    integer(c_int32_t) :: iterations
+    real(c_double)     :: dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf, p_tol
+  end type
+
+  type, bind(c) :: gbmg_ns_fields
+    type(gbmg_field) :: u, v, w, u_old, v_old, w_old, su, sv, sw, su_old, sv_old, sw_old
+    type(gbmg_field) :: rho, mu, delta, phi, nrm_x, nrm_y, nrm_z, curv, p
+  end type
+
+  type, bind(c) :: gbmg_ns_stats
+    integer(c_int32_t) :: status, cycles
+    real(c_double)     :: max_rel_residual, linf, l2f, ms
   end type
 
   interface
@@ -236,6 +254,31 @@ module gbmg
       integer(c_int), value   :: btn, max_iter, mem
       integer(c_int32_t), intent(out) :: iters
       real(c_double), intent(out) :: last_change
+    end function
+
+    integer(c_int) function gbmg_ns_ab_step(h, prm, f, mem, st) bind(c, name="gbmg_ns_ab_step")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_ns_fields, gbmg_ns_stats
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_ns_fields), intent(in) :: f
+      integer(c_int), value :: mem
+      type(gbmg_ns_stats), intent(out) :: st
+    end function
+
+    integer(c_int) function gbmg_ns_ab_predict(h, prm, f, mem) bind(c, name="gbmg_ns_ab_predict")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_ns_fields
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_ns_fields), intent(in) :: f
+      integer(c_int), value :: mem
+    end function
+
+    integer(c_int) function gbmg_ns_velbc(h, prm, u, v, w, mem) bind(c, name="gbmg_ns_velbc")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: u, v, w
+      integer(c_int), value :: mem
     end function
 
     integer(c_int64_t) function gbmg_ls_kernel_launches(ls) bind(c, name="gbmg_ls_kernel_launches")

@@ -67,3 +67,34 @@ def test_create_without_device_reports_no_device():
     g = _lib.Grid(8, 8, 8, 0.125, 0.125, 0.125)
     assert L.gbmg_create(C.byref(g), None, C.byref(h)) == _lib.GBMG_NO_DEVICE
     assert not h.value
+
+
+def test_fortran_module_binds_every_entry_point():
+    text = open(os.path.join(ROOT, "include", "gbmg.f90")).read()
+    bound = set(re.findall(r'bind\(c,\s*name="(gbmg_\w+)"\)', text))
+    assert bound == set(header_functions())
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """sizeof and field offsets of the ABI structs as a C compiler lays them
+    out from include/gbmg.h, against the ctypes mirrors."""
+    structs = {"gbmg_params": _lib.Params, "gbmg_stats": _lib.Stats, "gbmg_field": _lib.Field,
+               "gbmg_ns_params": _lib.NSParams, "gbmg_ns_fields": _lib.NSFields,
+               "gbmg_ns_stats": _lib.NSStats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbmg.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'  printf("{name} sizeof %zu\\n", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{name} {f} %zu\\n", offsetof({name}, {f}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    for line in out.splitlines():
+        name, field, val = line.split()
+        cls = structs[name]
+        want = C.sizeof(cls) if field == "sizeof" else getattr(cls, field).offset
+        assert int(val) == want, (name, field)
