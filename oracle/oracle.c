@@ -1735,3 +1735,204 @@ int or_ns_ab_step(const or_grid* gr, const or_ns_params* prm, const double* rho,
   free(cz);
   return worst;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Interface normals and curvature from combined compact differences          */
+/* (curv + surface_norms, NO2 src/interface_solver/others_normals.f90:1-103,   */
+/* NO3 :1-117; the "ccd" scheme of NO2 lib/solver/ccd_solvers.f90:76-159,     */
+/* 287-306, 379-399 with TWIN_DEC / TWIN_BKS of lib/solver/matrix_solver.f90). */
+/* Every line of the padded box (g ghosts each side, L = n + 2g points) is    */
+/* one 2x2-block tridiagonal system for (f', f''); the matrix depends only on */
+/* L and h, so it is decomposed once per axis.  dx**2.0d0 is dx*dx (a real    */
+/* exponent of integral value is an integer power in gfortran).               */
+/* ------------------------------------------------------------------------- */
+/* A, B, AA, BB: 3 x L each, row r (1..3 in the reference) at [(r-1)*L + i]. */
+void or_ccd_decompose(int L, double h, double* A, double* B, double* AA, double* BB) {
+#define M_(X, r, i) X[((r) - 1) * L + (i)]
+  const int is = 0, ie = L - 1;
+  /* working_matrix_bc */
+  M_(A, 2, is) = 1.0; M_(B, 2, is) = 0.0; M_(AA, 2, is) = 0.0; M_(BB, 2, is) = 1.0;
+  M_(A, 3, is) = 2.0; M_(B, 3, is) = -h; M_(AA, 3, is) = -(2.5 / h); M_(BB, 3, is) = 8.5;
+  M_(A, 2, ie) = 1.0; M_(B, 2, ie) = 0.0; M_(AA, 2, ie) = 0.0; M_(BB, 2, ie) = 1.0;
+  M_(A, 1, ie) = 2.0; M_(B, 1, ie) = h; M_(AA, 1, ie) = 2.5 / h; M_(BB, 1, ie) = 8.5;
+  /* working_matrix_init_ccd */
+  for (int i = is + 1; i <= ie - 1; ++i) {
+    M_(A, 1, i) = 7.0 / 16.0; M_(A, 2, i) = 1.0; M_(A, 3, i) = 7.0 / 16.0;
+    M_(B, 1, i) = h / 16.0; M_(B, 2, i) = 0.0; M_(B, 3, i) = -(h / 16.0);
+    M_(AA, 1, i) = -(9.0 / 8.0 / h); M_(AA, 2, i) = 0.0; M_(AA, 3, i) = 9.0 / 8.0 / h;
+    M_(BB, 1, i) = -(1.0 / 8.0); M_(BB, 2, i) = 1.0; M_(BB, 3, i) = -(1.0 / 8.0);
+  }
+  /* TWIN_DEC */
+  M_(A, 1, is) = 0.0; M_(AA, 1, is) = 0.0; M_(A, 3, ie) = 0.0; M_(AA, 3, ie) = 0.0;
+  M_(B, 1, is) = 0.0; M_(BB, 1, is) = 0.0; M_(B, 3, ie) = 0.0; M_(BB, 3, ie) = 0.0;
+  for (int i = is + 1; i <= ie; ++i) {
+    const double den = M_(A, 2, i - 1) * M_(BB, 2, i - 1) - M_(AA, 2, i - 1) * M_(B, 2, i - 1);
+    double sc1 = -((M_(AA, 2, i - 1) * M_(B, 1, i) - M_(A, 1, i) * M_(BB, 2, i - 1)) / den);
+    double sc2 = (M_(B, 1, i) * M_(A, 2, i - 1) - M_(B, 2, i - 1) * M_(A, 1, i)) / den;
+    M_(A, 1, i) = sc1;
+    M_(A, 2, i) = M_(A, 2, i) - (sc1 * M_(A, 3, i - 1) + sc2 * M_(AA, 3, i - 1));
+    M_(B, 1, i) = sc2;
+    M_(B, 2, i) = M_(B, 2, i) - (sc1 * M_(B, 3, i - 1) + sc2 * M_(BB, 3, i - 1));
+    sc1 = -((M_(AA, 2, i - 1) * M_(BB, 1, i) - M_(AA, 1, i) * M_(BB, 2, i - 1)) / den);
+    sc2 = (M_(BB, 1, i) * M_(A, 2, i - 1) - M_(B, 2, i - 1) * M_(AA, 1, i)) / den;
+    M_(AA, 1, i) = sc1;
+    M_(AA, 2, i) = M_(AA, 2, i) - (sc1 * M_(A, 3, i - 1) + sc2 * M_(AA, 3, i - 1));
+    M_(BB, 1, i) = sc2;
+    M_(BB, 2, i) = M_(BB, 2, i) - (sc1 * M_(B, 3, i - 1) + sc2 * M_(BB, 3, i - 1));
+  }
+#undef M_
+}
+
+/* One line: f at f[i*sf], i = 0..L-1, into fx, fxx at [i*so]
+ * (working_matrix_asgn_src_ccd, then TWIN_BKS). */
+void or_ccd_line(int L, double h, const double* A, const double* B, const double* AA,
+                 const double* BB, const double* f, int64_t sf, double* S, double* SS,
+                 int64_t so) {
+#define M_(X, r, i) X[((r) - 1) * L + (i)]
+#define F(i) f[(int64_t)(i) * sf]
+#define S_(i) S[(int64_t)(i) * so]
+#define SS_(i) SS[(int64_t)(i) * so]
+  const int is = 0, ie = L - 1;
+  const double h2 = h * h;
+  S_(is) = ((-3.5 * F(is) + 4.0 * F(is + 1)) - 0.5 * F(is + 2)) / h;
+  SS_(is) = (((34.0 / 3.0 * F(is) - 83.0 / 4.0 * F(is + 1)) + 10.0 * F(is + 2)) -
+             7.0 / 12.0 * F(is + 3)) / h2;
+  for (int i = is + 1; i <= ie - 1; ++i) {
+    S_(i) = 15.0 / 16.0 * (-F(i - 1) + F(i + 1)) / h;
+    SS_(i) = ((3.0 * F(i - 1) - 6.0 * F(i)) + 3.0 * F(i + 1)) / h2;
+  }
+  S_(ie) = -(((-3.5 * F(ie) + 4.0 * F(ie - 1)) - 0.5 * F(ie - 2)) / h);
+  SS_(ie) = (((34.0 / 3.0 * F(ie) - 83.0 / 4.0 * F(ie - 1)) + 10.0 * F(ie - 2)) -
+             7.0 / 12.0 * F(ie - 3)) / h2;
+  /* TWIN_BKS */
+  for (int i = is + 1; i <= ie; ++i) {
+    const double sp = S_(i - 1), ssp = SS_(i - 1);
+    S_(i) = S_(i) - (M_(A, 1, i) * sp + M_(B, 1, i) * ssp);
+    SS_(i) = SS_(i) - (M_(AA, 1, i) * sp + M_(BB, 1, i) * ssp);
+  }
+  double den = M_(A, 2, ie) * M_(BB, 2, ie) - M_(AA, 2, ie) * M_(B, 2, ie);
+  double sol = -((M_(B, 2, ie) * SS_(ie) - M_(BB, 2, ie) * S_(ie)) / den);
+  double sol2 = (M_(A, 2, ie) * SS_(ie) - M_(AA, 2, ie) * S_(ie)) / den;
+  S_(ie) = sol;
+  SS_(ie) = sol2;
+  for (int i = ie - 1; i >= is; --i) {
+    S_(i) = S_(i) - (M_(A, 3, i) * sol + M_(B, 3, i) * sol2);
+    SS_(i) = SS_(i) - (M_(AA, 3, i) * sol + M_(BB, 3, i) * sol2);
+    den = M_(A, 2, i) * M_(BB, 2, i) - M_(AA, 2, i) * M_(B, 2, i);
+    sol = -((M_(B, 2, i) * SS_(i) - M_(BB, 2, i) * S_(i)) / den);
+    sol2 = (M_(A, 2, i) * SS_(i) - M_(AA, 2, i) * S_(i)) / den;
+    S_(i) = sol;
+    SS_(i) = sol2;
+  }
+#undef M_
+#undef F
+#undef S_
+#undef SS_
+}
+
+/* all lines along one axis of the padded box */
+static void ccd_axis(const ns_box* b, int axis, double h, const double* f, double* fx,
+                     double* fxx) {
+  const int three = b->nz > 1;
+  const size_t px = b->px, py = b->py, pz = three ? (size_t)b->nz + 2 * (size_t)b->g : 1;
+  const size_t ext[3] = {px, py, pz};
+  const int64_t st[3] = {1, (int64_t)px, (int64_t)(px * py)};
+  const int L = (int)ext[axis];
+  double* A = dalloc(3 * (size_t)L);
+  double* B = dalloc(3 * (size_t)L);
+  double* AA = dalloc(3 * (size_t)L);
+  double* BB = dalloc(3 * (size_t)L);
+  or_ccd_decompose(L, h, A, B, AA, BB);
+  const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+  const size_t n1 = ext[a1], n2 = ext[a2];
+#pragma omp parallel for collapse(2) schedule(static)
+  for (size_t i2 = 0; i2 < n2; ++i2)
+    for (size_t i1 = 0; i1 < n1; ++i1) {
+      const size_t base = i1 * (size_t)st[a1] + i2 * (size_t)st[a2];
+      or_ccd_line(L, h, A, B, AA, BB, f + base, st[axis], fx + base, fxx + base, st[axis]);
+    }
+  free(A);
+  free(B);
+  free(AA);
+  free(BB);
+}
+
+/* bc (NO2 src/others/bcs.f90:1-26, NO3 :1-42): zero-gradient copies of the
+ * boundary values into the ghosts, x then y then z passes. */
+void or_ns_bc(const or_grid* gr, int g, double* a) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  const int k0 = three ? 1 - g : 1, k1 = three ? gr->nz + g : 1;
+  for (int k = k0; k <= k1; ++k)
+    for (int j = 1 - g; j <= gr->ny + g; ++j)
+      for (int m = 1; m <= g; ++m) {
+        a[NI(&b, 1 - m, j, k)] = a[NI(&b, 1, j, k)];
+        a[NI(&b, gr->nx + m, j, k)] = a[NI(&b, gr->nx, j, k)];
+      }
+  for (int k = k0; k <= k1; ++k)
+    for (int i = 1 - g; i <= gr->nx + g; ++i)
+      for (int m = 1; m <= g; ++m) {
+        a[NI(&b, i, 1 - m, k)] = a[NI(&b, i, 1, k)];
+        a[NI(&b, i, gr->ny + m, k)] = a[NI(&b, i, gr->ny, k)];
+      }
+  if (!three) return;
+  for (int j = 1 - g; j <= gr->ny + g; ++j)
+    for (int i = 1 - g; i <= gr->nx + g; ++i)
+      for (int m = 1; m <= g; ++m) {
+        a[NI(&b, i, j, 1 - m)] = a[NI(&b, i, j, 1)];
+        a[NI(&b, i, j, gr->nz + m)] = a[NI(&b, i, j, gr->nz)];
+      }
+}
+
+/* curv: the derivatives of phi by compact lines (x, y, z of phi; y of phi_x,
+ * z of phi_x and of phi_y), bc on each, then on the interior
+ *   2D  curv = (fyy fx^2 + fxx fy^2 - 2 fxy fx fy) / (fx^2 + fy^2 + 1e-12)^1.5
+ *   3D  curv = ((fyy+fzz) fx^2 + (fxx+fzz) fy^2 + (fxx+fyy) fz^2
+ *               - 2 (fxy fx fy + fxz fx fz + fyz fy fz)) / (|grad phi|^2 + 1e-12)^1.5
+ * and bc.  nx, ny, nz receive phi_x, phi_y, phi_z (the reference's normals%x..z,
+ * not normalised); d2 (may be NULL) receives fxx, fyy, fzz, fxy, fxz, fyz,
+ * six padded arrays one after another. */
+void or_ns_curvature(const or_grid* gr, int g, const double* phi, double* nx, double* ny,
+                     double* nz, double* curv, double* d2) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  const size_t span = ns_span(&b);
+  double* own = d2 ? NULL : dalloc(6 * span);
+  double* D = d2 ? d2 : own;
+  double *fxx = D, *fyy = D + span, *fzz = D + 2 * span, *fxy = D + 3 * span,
+         *fxz = D + 4 * span, *fyz = D + 5 * span;
+  double* dummy = dalloc(span);
+  ccd_axis(&b, 0, gr->dx, phi, nx, fxx);
+  ccd_axis(&b, 1, gr->dy, phi, ny, fyy);
+  if (three) ccd_axis(&b, 2, gr->dz, phi, nz, fzz);
+  ccd_axis(&b, 1, gr->dy, nx, fxy, dummy);
+  if (three) {
+    ccd_axis(&b, 2, gr->dz, nx, fxz, dummy);
+    ccd_axis(&b, 2, gr->dz, ny, fyz, dummy);
+  }
+  double* bcs[9] = {nx, fxx, ny, fyy, nz, fzz, fxy, fxz, fyz};
+  for (int a = 0; a < 9; ++a) {
+    if (!three && (a == 4 || a == 5 || a == 7 || a == 8)) continue;
+    or_ns_bc(gr, g, bcs[a]);
+  }
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 1; k <= gr->nz; ++k)
+    for (int j = 1; j <= gr->ny; ++j)
+      for (int i = 1; i <= gr->nx; ++i) {
+        const size_t q = NI(&b, i, j, k);
+        const double fx = nx[q], fy = ny[q];
+        if (!three) {
+          const double num = (fyy[q] * (fx * fx) + fxx[q] * (fy * fy)) - 2.0 * fxy[q] * fx * fy;
+          curv[q] = num / pow((fx * fx + fy * fy) + 1.0e-12, 1.5);
+        } else {
+          const double fz = nz[q];
+          const double num = (((fyy[q] + fzz[q]) * (fx * fx) + (fxx[q] + fzz[q]) * (fy * fy)) +
+                              (fxx[q] + fyy[q]) * (fz * fz)) -
+                             2.0 * ((fxy[q] * fx * fy + fxz[q] * fx * fz) + fyz[q] * fy * fz);
+          curv[q] = num / pow(((fx * fx + fy * fy) + fz * fz) + 1.0e-12, 1.5);
+        }
+      }
+  or_ns_bc(gr, g, curv);
+  free(own);
+  free(dummy);
+}

@@ -96,6 +96,11 @@ def lib():
         L.or_ns_ab_step.argtypes = ([_G, _N] + [_D] * 22
                                     + [C.POINTER(MGParams), _D, _D, C.POINTER(C.c_int32)])
         L.or_ns_ab_step.restype = C.c_int
+        L.or_ccd_decompose.argtypes = [C.c_int, C.c_double, _D, _D, _D, _D]
+        L.or_ccd_line.argtypes = [C.c_int, C.c_double, _D, _D, _D, _D, _D, C.c_int64, _D, _D,
+                                  C.c_int64]
+        L.or_ns_bc.argtypes = [_G, C.c_int, _D]
+        L.or_ns_curvature.argtypes = [_G, C.c_int, _D, _D, _D, _D, _D, _D]
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -424,3 +429,37 @@ def ns_ab_step(shape, spacing, prm, rho_now, vel, old, src_old, p, **mg_kw):
                              _p(pp), C.byref(mgp), C.byref(linf), C.byref(l2f), C.byref(cyc))
     return {"u": vel[0], "v": vel[1], "w": vel[2], "su": src[0], "sv": src[1], "sw": src[2],
             "p": pp, "linf": linf.value, "l2f": l2f.value, "cycles": cyc.value, "status": st}
+
+
+def ccd_line(f, h):
+    """root_solve("ccd") of one line: returns (f', f'')."""
+    f = np.ascontiguousarray(f, np.float64)
+    L = f.size
+    mats = [np.zeros(3 * L) for _ in range(4)]
+    lib().or_ccd_decompose(L, float(h), *[_p(m) for m in mats])
+    fx, fxx = np.empty(L), np.empty(L)
+    lib().or_ccd_line(L, float(h), *[_p(m) for m in mats], _p(f), 1, _p(fx), _p(fxx), 1)
+    return fx, fxx
+
+
+def ns_bc(shape, ghost, a):
+    """bc (zero-gradient ghost copies) in place on a padded array."""
+    g = grid(shape, (1.0, 1.0, 1.0))
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().or_ns_bc(C.byref(g), int(ghost), _p(a))
+
+
+def ns_curvature(shape, spacing, ghost, phi, want_d2=False):
+    """curv + surface_norms on a padded phi: returns (phi_x, phi_y, phi_z or
+    None, curv[, d2]) as padded arrays after bc; d2 = (fxx, fyy, fzz, fxy,
+    fxz, fyz)."""
+    g = grid(shape, spacing)
+    phi = _pad(phi, shape, ghost, "phi")
+    ps = padded_shape(shape, ghost)
+    nx, ny, cv = np.zeros(ps), np.zeros(ps), np.zeros(ps)
+    nz = np.zeros(ps) if _three(shape) else None
+    d2 = np.zeros((6,) + ps)
+    lib().or_ns_curvature(C.byref(g), int(ghost), _p(phi), _p(nx), _p(ny), _p(nz), _p(cv),
+                          _p(d2))
+    out = (nx, ny, nz, cv)
+    return out + (tuple(d2),) if want_d2 else out

@@ -1052,3 +1052,143 @@ def velbc(u, v, w, g, nx, ny, nz, ubc, vbc, wbc=(0, 0)):
                             s_ = (nz - m) if c == 2 else (nz + 1 - m)
                             F[i, j, nz + m] = F[i, j, s_] if t == 2 else -F[i, j, s_]
                 W[i, j, 0 if side == 0 else nz] = 0.0
+
+
+# ---------------------------------------------------------------------------
+# Compact-difference normals and curvature, literally:
+#   working_matrix_bc / init_ccd / asgn_src_ccd / root_solve("ccd")
+#       "Two phase flows/newOpenMP/2D/lib/solver/ccd_solvers.f90:76-159,287-306,379-399"
+#   TWIN_DEC, TWIN_BKS  ".../2D/lib/solver/matrix_solver.f90:6-78"
+#   surface_norms, curv ".../2D/src/interface_solver/others_normals.f90:1-103"
+#                       (3D ".../3D+IBM/src/interface_solver/others_normals.f90")
+#   bc                  ".../2D/src/others/bcs.f90:1-26"
+# Matrices are dicts keyed (row, i) with i the Fortran index is..ie.
+# ---------------------------------------------------------------------------
+def _twin_dec(A, B, AA, BB, IS, IE):
+    A[1, IS] = 0.0; AA[1, IS] = 0.0; A[3, IE] = 0.0; AA[3, IE] = 0.0
+    B[1, IS] = 0.0; BB[1, IS] = 0.0; B[3, IE] = 0.0; BB[3, IE] = 0.0
+    for i in range(IS + 1, IE + 1):
+        Den = A[2, i - 1] * BB[2, i - 1] - AA[2, i - 1] * B[2, i - 1]
+        SC1 = -(AA[2, i - 1] * B[1, i] - A[1, i] * BB[2, i - 1]) / Den
+        SC2 = (B[1, i] * A[2, i - 1] - B[2, i - 1] * A[1, i]) / Den
+        A[1, i] = SC1
+        A[2, i] = A[2, i] - (SC1 * A[3, i - 1] + SC2 * AA[3, i - 1])
+        B[1, i] = SC2
+        B[2, i] = B[2, i] - (SC1 * B[3, i - 1] + SC2 * BB[3, i - 1])
+        SC1 = -(AA[2, i - 1] * BB[1, i] - AA[1, i] * BB[2, i - 1]) / Den
+        SC2 = (BB[1, i] * A[2, i - 1] - B[2, i - 1] * AA[1, i]) / Den
+        AA[1, i] = SC1
+        AA[2, i] = AA[2, i] - (SC1 * A[3, i - 1] + SC2 * AA[3, i - 1])
+        BB[1, i] = SC2
+        BB[2, i] = BB[2, i] - (SC1 * B[3, i - 1] + SC2 * BB[3, i - 1])
+
+
+def _twin_bks(A, B, AA, BB, S, SS, IS, IE):
+    for i in range(IS + 1, IE + 1):
+        S[i] = S[i] - (A[1, i] * S[i - 1] + B[1, i] * SS[i - 1])
+        SS[i] = SS[i] - (AA[1, i] * S[i - 1] + BB[1, i] * SS[i - 1])
+    Den = A[2, IE] * BB[2, IE] - AA[2, IE] * B[2, IE]
+    SolS = -(B[2, IE] * SS[IE] - BB[2, IE] * S[IE]) / Den
+    SolSS = (A[2, IE] * SS[IE] - AA[2, IE] * S[IE]) / Den
+    S[IE] = SolS
+    SS[IE] = SolSS
+    for i in range(IE - 1, IS - 1, -1):
+        S[i] = S[i] - (A[3, i] * SolS + B[3, i] * SolSS)
+        SS[i] = SS[i] - (AA[3, i] * SolS + BB[3, i] * SolSS)
+        Den = A[2, i] * BB[2, i] - AA[2, i] * B[2, i]
+        SolS = -(B[2, i] * SS[i] - BB[2, i] * S[i]) / Den
+        SolSS = (A[2, i] * SS[i] - AA[2, i] * S[i]) / Den
+        S[i] = SolS
+        SS[i] = SolSS
+
+
+def ccd_solve(f, dx):
+    """root_solve("ccd"): f a list over is..ie (here 0..L-1); returns (fx, fxx)."""
+    IS, IE = 0, len(f) - 1
+    A, B, AA, BB = {}, {}, {}, {}
+    # working_matrix_bc
+    A[2, IS] = 1.0; B[2, IS] = 0.0; AA[2, IS] = 0.0; BB[2, IS] = 1.0
+    A[3, IS] = 2.0; B[3, IS] = - dx; AA[3, IS] = -2.5 / dx; BB[3, IS] = 8.5
+    A[2, IE] = 1.0; B[2, IE] = 0.0; AA[2, IE] = 0.0; BB[2, IE] = 1.0
+    A[1, IE] = 2.0; B[1, IE] = dx; AA[1, IE] = 2.5 / dx; BB[1, IE] = 8.5
+    # working_matrix_init_ccd
+    for i in range(IS + 1, IE):
+        A[1, i] = 7.0 / 16.0; A[2, i] = 1.0; A[3, i] = 7.0 / 16.0
+        B[1, i] = dx / 16.0; B[2, i] = 0.0; B[3, i] = - dx / 16.0
+        AA[1, i] = - 9.0 / 8.0 / dx; AA[2, i] = 0.0; AA[3, i] = 9.0 / 8.0 / dx
+        BB[1, i] = - 1.0 / 8.0; BB[2, i] = 1.0; BB[3, i] = - 1.0 / 8.0
+    _twin_dec(A, B, AA, BB, IS, IE)
+    S, SS = {}, {}
+    S[IS] = (-3.5 * f[IS] + 4.0 * f[IS + 1] - 0.5 * f[IS + 2]) / dx
+    SS[IS] = (34.0 / 3.0 * f[IS] - 83.0 / 4.0 * f[IS + 1] + 10.0 * f[IS + 2]
+              - 7.0 / 12.0 * f[IS + 3]) / _sq(dx)
+    for i in range(IS + 1, IE):
+        S[i] = 15.0 / 16.0 * (-f[i - 1] + f[i + 1]) / dx
+        SS[i] = (3.0 * f[i - 1] - 6.0 * f[i] + 3.0 * f[i + 1]) / _sq(dx)
+    S[IE] = -(-3.5 * f[IE] + 4.0 * f[IE - 1] - 0.5 * f[IE - 2]) / dx
+    SS[IE] = (34.0 / 3.0 * f[IE] - 83.0 / 4.0 * f[IE - 1] + 10.0 * f[IE - 2]
+              - 7.0 / 12.0 * f[IE - 3]) / _sq(dx)
+    _twin_bks(A, B, AA, BB, S, SS, IS, IE)
+    return [S[i] for i in range(IS, IE + 1)], [SS[i] for i in range(IS, IE + 1)]
+
+
+def _ccd_lines(a, axis, h):
+    """CCD along numpy axis `axis` (0 = slowest) of every line of a padded array."""
+    fx, fxx = np.empty_like(a), np.empty_like(a)
+    moved = np.moveaxis(a, axis, -1)
+    ox, oxx = np.moveaxis(fx, axis, -1), np.moveaxis(fxx, axis, -1)
+    for idx in np.ndindex(moved.shape[:-1]):
+        d1, d2 = ccd_solve([float(x) for x in moved[idx]], h)
+        ox[idx] = d1
+        oxx[idx] = d2
+    return fx, fxx
+
+
+def _bc_copy(a):
+    """bc: zero-gradient copies from the boundary interior, x then y (then z)."""
+    g = _bc_copy.g
+    for ax in range(a.ndim - 1, -1, -1):
+        m = np.moveaxis(a, ax, -1)
+        n = m.shape[-1] - 2 * g
+        for k in range(1, g + 1):
+            m[..., g - k] = m[..., g]
+            m[..., g + n - 1 + k] = m[..., g + n - 1]
+
+
+def curv(phi, g, dx, dy, dz=None):
+    """surface_norms + curv on a padded phi (2D (ny+2g, nx+2g) or 3D).  Returns
+    (fx, fy, fz or None, curv) after bc."""
+    _bc_copy.g = g
+    three = phi.ndim == 3
+    ax = {"x": phi.ndim - 1, "y": phi.ndim - 2, "z": 0}
+    fx, fxx = _ccd_lines(phi, ax["x"], dx)
+    fy, fyy = _ccd_lines(phi, ax["y"], dy)
+    fxy, _ = _ccd_lines(fx, ax["y"], dy)
+    if three:
+        fz, fzz = _ccd_lines(phi, ax["z"], dz)
+        fxz, _ = _ccd_lines(fx, ax["z"], dz)
+        fyz, _ = _ccd_lines(fy, ax["z"], dz)
+        arrs = (fx, fxx, fy, fyy, fz, fzz, fxy, fxz, fyz)
+    else:
+        fz = None
+        arrs = (fx, fxx, fy, fyy, fxy)
+    for a in arrs:
+        _bc_copy(a)
+    cv = np.zeros_like(phi)
+    inner = tuple(slice(g, s - g) for s in phi.shape)
+    it = np.ndindex(*[s - 2 * g for s in phi.shape])
+    for rel in it:
+        q = tuple(r + g for r in rel)
+        Fx, Fy = float(fx[q]), float(fy[q])
+        if not three:
+            cv[q] = (float(fyy[q]) * _sq(Fx) + float(fxx[q]) * _sq(Fy)
+                     - 2.0 * float(fxy[q]) * Fx * Fy) / (_sq(Fx) + _sq(Fy) + 1.0e-12) ** 1.5
+        else:
+            Fz = float(fz[q])
+            cv[q] = ((float(fyy[q]) + float(fzz[q])) * _sq(Fx) + (float(fxx[q]) + float(fzz[q])) * _sq(Fy)
+                     + (float(fxx[q]) + float(fyy[q])) * _sq(Fz)
+                     - 2.0 * (float(fxy[q]) * Fx * Fy + float(fxz[q]) * Fx * Fz + float(fyz[q]) * Fy * Fz)) \
+                / (_sq(Fx) + _sq(Fy) + _sq(Fz) + 1.0e-12) ** 1.5
+    del inner
+    _bc_copy(cv)
+    return fx, fy, fz, cv
