@@ -12,7 +12,7 @@ step around the projection (momentum.py) and the seeded synthetic inputs
 """
 from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
 from .levelset import LevelSet, node_velocity  # noqa: F401
-from .momentum import NSParams, ns_ab_predictor, ns_ab_solver, velbc  # noqa: F401
+from .momentum import NSParams, curv, ns_ab_predictor, ns_ab_solver, velbc  # noqa: F401
 
 try:  # torch.ops.gbmg.solve (torch is optional for host-memory use)
     from . import ops  # noqa: F401
@@ -20,4 +20,4 @@ except ImportError:  # pragma: no cover
     pass
 
 __all__ = ["PressurePoisson", "LevelSet", "node_velocity", "NSParams", "ns_ab_solver",
-           "ns_ab_predictor", "velbc", "ConvergenceError", "GBMGError"]
+           "ns_ab_predictor", "velbc", "curv", "ConvergenceError", "GBMGError"]

@@ -33,7 +33,7 @@ EXPORTS = (
     "gbmg_div_stats_noalloc", "gbmg_set_split", "gbmg_project_split",
     "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
     "gbmg_ls_kernel_launches", "gbmg_ls_last_error",
-    "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc",
+    "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc", "gbmg_ns_curvature",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -156,8 +156,10 @@ def load(build_if_missing: bool = True):
         L.gbmg_ns_ab_step.argtypes = [H, P(NSParams), P(NSFields), C.c_int, P(NSStats)]
         L.gbmg_ns_ab_predict.argtypes = [H, P(NSParams), P(NSFields), C.c_int]
         L.gbmg_ns_velbc.argtypes = [H, P(NSParams), Field, Field, Field, C.c_int]
+        L.gbmg_ns_curvature.argtypes = [H, P(NSParams), Field, Field, Field, Field, Field, C.c_int]
         for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
-                     "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc"):
+                     "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc",
+                     "gbmg_ns_curvature"):
             getattr(L, name).restype = C.c_int
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",

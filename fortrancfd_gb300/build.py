@@ -19,7 +19,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
          "-I", CSRC, "-I", INCLUDE]
 # Translation units whose FP64 results must equal the oracle's bit for bit are
 # compiled without multiply-add contraction.
-FILE_FLAGS = {"momentum.cu": ["-fmad=false"]}
+FILE_FLAGS = {"momentum.cu": ["-fmad=false"], "ccd.cu": ["-fmad=false"]}
 
 
 def nvcc():

@@ -139,8 +139,8 @@ struct gbmg_handle {
   double split_rho12 = 0.0;
   // momentum step: padded-box buffers (vel%tmp, velsrc%tmp, and the host
   // staging copies of the caller's arrays), allocated on first use
-  double* ns_buf[32] = {};
-  size_t ns_n[32] = {};
+  double* ns_buf[48] = {};
+  size_t ns_n[48] = {};
   std::string err;
 };
 
@@ -505,7 +505,7 @@ int free_all(gbmg_handle* h) {
   if (h->gmHost) cudaFreeHost(h->gmHost);
   dfree(h->minv); dfree(h->adense); dfree(h->cwork); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
   dfree(h->bar);
-  for (int i = 0; i < 32; ++i) dfree(h->ns_buf[i]);
+  for (int i = 0; i < 48; ++i) dfree(h->ns_buf[i]);
   delete[] h->dmaps;
   h->dmaps = nullptr;
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
@@ -1535,6 +1535,40 @@ void ns_used(const gbmg_grid& g, const gbmg_ns_params* prm, bool (&used)[kNsFiel
   }
 }
 
+// Compact-difference normals and curvature (curv + surface_norms): scratch
+// slots after the momentum step's: the six second derivatives and a dummy
+// second derivative, then a factor table per axis and the factoring work.
+constexpr int kCcdD2 = kNsDiff + 3, kCcdDummy = kCcdD2 + 6, kCcdTable = kCcdDummy + 1,
+              kCcdWork = kCcdTable + 3;
+
+int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double* S, double* SS) {
+  const NsArgs& a = P.a;
+  const bool three = a.nz > 1;
+  const int px = a.nx + 2 * a.g, py = a.ny + 2 * a.g, pz = three ? a.nz + 2 * a.g : 1;
+  const int ext[3] = {px, py, pz};
+  const int64_t str[3] = {1, a.sy, three ? a.sz : 0};
+  const double hs[3] = {a.dx, a.dy, a.dz};
+  CcdArgs c{};
+  c.L = ext[axis];
+  c.st = str[axis];
+  const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+  c.n1 = ext[a1]; c.s1 = str[a1];
+  c.n2 = ext[a2]; c.s2 = str[a2];
+  c.h = hs[axis];
+  c.h2 = c.h * c.h;
+  c.rh = 1.0 / c.h;
+  c.rh2 = 1.0 / c.h2;
+  c.fast = fdiv_divisor_ok(c.h) && fdiv_divisor_ok(c.h2);
+  // factor table of this axis (recomputed per call: L points, one thread)
+  GB_TRY(ns_buffer(h, kCcdTable + axis, (size_t)14 * c.L));
+  GB_TRY(ns_buffer(h, kCcdWork, (size_t)12 * c.L));
+  LAUNCH(h, GBMG_PROF_MOMENTUM,
+         launch_ccd_decompose(h->stream, c.L, c.h, h->ns_buf[kCcdWork], h->ns_buf[kCcdTable + axis]));
+  LAUNCH(h, GBMG_PROF_MOMENTUM,
+         launch_ccd_lines(h->stream, c, h->ns_buf[kCcdTable + axis], f + P.lo, S + P.lo, SS + P.lo));
+  return check_launch(h, "ccd lines");
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2121,6 +2155,58 @@ int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_
   double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
   LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(h->stream, P.a, P.bc, now));
   GB_TRY(check_launch(h, "velbc"));
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
+                      gbmg_field nrm_x, gbmg_field nrm_y, gbmg_field nrm_z, gbmg_field curv,
+                      int mem) {
+  GB_TRY(begin(h));
+  if (!prm) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
+  const bool three = h->grid.nz > 1;
+  gbmg_ns_fields f{};
+  f.phi = phi; f.nrm_x = nrm_x; f.nrm_y = nrm_y; f.nrm_z = nrm_z; f.curv = curv;
+  bool used[kNsFields] = {}, in[kNsFields] = {}, out[kNsFields] = {};
+  const int slots[5] = {kNsPhi, kNsNx, kNsNy, kNsNz, kNsCurv};
+  for (int i = 0; i < 5; ++i) {
+    if (slots[i] == kNsNz && !three) continue;
+    used[slots[i]] = in[slots[i]] = true;
+    out[slots[i]] = slots[i] != kNsPhi;
+  }
+  gbmg_ns_params q = *prm;
+  q.dt = q.re = q.fr = 1.0;  // only ghost is read
+  q.btn_sf = 0.0;
+  NsPlan P;
+  GB_TRY(ns_prepare(h, &q, &f, mem, used, in, &P));
+  const size_t span = (size_t)(P.hi - P.lo + 1);
+  double* d2[7];
+  for (int i = 0; i < 7; ++i) {
+    GB_TRY(ns_buffer(h, kCcdD2 + i, span));
+    d2[i] = h->ns_buf[kCcdD2 + i] - P.lo;
+  }
+  double* dummy = d2[6];
+  double* nx = P.base[kNsNx];
+  double* ny = P.base[kNsNy];
+  double* nz = three ? P.base[kNsNz] : nullptr;
+  const double* ph = P.base[kNsPhi];
+  // surface_norms: first derivatives of phi and their cross derivatives, in
+  // the reference's order (the cross derivatives read phi_x, phi_y before bc)
+  GB_TRY(ccd_axis(h, P, 0, ph, nx, d2[0]));
+  GB_TRY(ccd_axis(h, P, 1, ph, ny, d2[1]));
+  if (three) GB_TRY(ccd_axis(h, P, 2, ph, nz, d2[2]));
+  GB_TRY(ccd_axis(h, P, 1, nx, d2[3], dummy));
+  if (three) {
+    GB_TRY(ccd_axis(h, P, 2, nx, d2[4], dummy));
+    GB_TRY(ccd_axis(h, P, 2, ny, d2[5], dummy));
+  }
+  const double* d1c[3] = {nx, ny, nz};
+  const double* d2c[6] = {d2[0], d2[1], d2[2], d2[3], d2[4], d2[5]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_curvature(h->stream, P.a, d1c, d2c, P.base[kNsCurv]));
+  double* bcs[4] = {nx, ny, nz, P.base[kNsCurv]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, bcs));
+  GB_TRY(check_launch(h, "curvature"));
   GB_TRY(ns_finish(h, &f, mem, P, out));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;

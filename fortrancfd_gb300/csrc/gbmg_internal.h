@@ -349,4 +349,25 @@ void launch_velbc(cudaStream_t s, const NsArgs& a, const NsBc& bc, double* const
 void launch_ns_change(cudaStream_t s, const NsArgs& a, const double* const now[3],
                       const double* const tmp[3], const ReduceScratch& R);
 
+// ---- compact-difference normals and curvature (ccd.cu) ------------------------
+// One axis of CCD line solves over the padded box: L points per line, st
+// apart; lines i1 + n1 i2 start at i1 s1 + i2 s2 from the box origin.
+struct CcdArgs {
+  int L, n1, n2;
+  int64_t st, s1, s2;
+  double h, h2, rh, rh2;  // spacing, its square and their RN reciprocals
+  int fast;               // 1: quotients by h, h^2 from the reciprocals
+};
+// factor table of the CCD matrix for L points (14 doubles per point); work: 12 L doubles
+void launch_ccd_decompose(cudaStream_t s, int L, double h, double* work, double* table);
+// f' into S and f'' into SS along every line (box-origin pointers)
+void launch_ccd_lines(cudaStream_t s, const CcdArgs& c, const double* table, const double* f,
+                      double* S, double* SS);
+// zero-gradient ghosts (bc) of up to four arrays at element (1,1,1) (null = none)
+void launch_ccd_bc(cudaStream_t s, const NsArgs& a, double* const f[4]);
+// curvature on the interior from phi_x, phi_y, phi_z and the second derivatives
+// fxx, fyy, fzz, fxy, fxz, fyz (arrays at element (1,1,1))
+void launch_curvature(cudaStream_t s, const NsArgs& a, const double* const d1[3],
+                      const double* const d2[6], double* curv);
+
 }  // namespace gbmg

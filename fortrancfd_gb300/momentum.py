@@ -187,5 +187,24 @@ def velbc(pp, prm: NSParams, u, v, w=None):
     pp._check(pp._L.gbmg_ns_velbc(pp._h, C.byref(c), fu, fv, fw, mems.pop()), "velbc")
 
 
-__all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "padded_shape",
+def curv(pp, prm: NSParams, phi, nrm_x, nrm_y, nrm_z, curvature):
+    """curv + surface_norms: phi's gradient into nrm_x, nrm_y (nrm_z) and the
+    curvature, by compact-difference line solves; padded arrays, in place
+    (phi is read only).  nrm_z is ignored in 2D."""
+    three = pp.shape[0] > 1
+    fs, mems = [], set()
+    for name, a in (("phi", phi), ("nrm_x", nrm_x), ("nrm_y", nrm_y),
+                    ("nrm_z", nrm_z if three else None), ("curv", curvature)):
+        fld, m = _padded_field(a, name, pp.shape, prm.ghost)
+        fs.append(fld)
+        if m is not None:
+            mems.add(m)
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must be in the same memory (host or CUDA)")
+    _sync({"phi": phi, "x": nrm_x, "y": nrm_y, "z": nrm_z, "c": curvature})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_curvature(pp._h, C.byref(c), *fs, mems.pop()), "curv")
+
+
+__all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "padded_shape",
            "ConvergenceError", "GBMGError"]

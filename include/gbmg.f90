@@ -281,6 +281,15 @@ module gbmg
       integer(c_int), value :: mem
     end function
 
+    integer(c_int) function gbmg_ns_curvature(h, prm, phi, nrm_x, nrm_y, nrm_z, curv, mem) &
+        bind(c, name="gbmg_ns_curvature")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: phi, nrm_x, nrm_y, nrm_z, curv
+      integer(c_int), value :: mem
+    end function
+
     integer(c_int64_t) function gbmg_ls_kernel_launches(ls) bind(c, name="gbmg_ls_kernel_launches")
       import :: c_int64_t, c_ptr
       type(c_ptr), value :: ls

@@ -290,6 +290,24 @@ int gbmg_ns_ab_predict(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_
 int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_field v,
                   gbmg_field w, int mem);
 
+/* Interface normals and curvature, the reference's curv + surface_norms
+ * ("Two phase flows/newOpenMP/2D/src/interface_solver/others_normals.f90";
+ * 3D "…/3D+IBM/src/interface_solver/others_normals.f90") with the combined
+ * compact difference scheme "ccd" ("…/2D/lib/solver/ccd_solvers.f90",
+ * block tridiagonal solver "…/2D/lib/solver/matrix_solver.f90"): phi_x,
+ * phi_y (phi_z) and the second and cross derivatives of phi by compact line
+ * solves over the whole padded box, then on the interior
+ *   curv = (fyy fx^2 + fxx fy^2 - 2 fxy fx fy) / (fx^2 + fy^2 + 1e-12)^1.5
+ * (3D: the three-term form) and zero-gradient ghosts (bc) on nrm_x, nrm_y,
+ * nrm_z and curv.  nrm_* receive phi's gradient (the reference's
+ * normals%x..z, not normalised): the nrm_* and curv inputs of the momentum
+ * step at the next time step.  Padded arrays as gbmg_ns_fields (prm->ghost
+ * layers, one pair of strides); the derivatives equal the reference formulas'
+ * doubles, the curvature's power uses CUDA's pow. */
+int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
+                      gbmg_field nrm_x, gbmg_field nrm_y, gbmg_field nrm_z, gbmg_field curv,
+                      int mem);
+
 /* Copies level `level`'s face coefficients (FP64) into cell-shaped arrays of
  * that level's size (gbmg_level_dims).  For tests of the coarsening rule. */
 int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,
