@@ -427,7 +427,8 @@ def momentum_section(dev, stream, case, iterations=4, reps=5):
     with host arrays (e2e) and the CPU oracle's step beside it."""
     import torch
 
-    from fortrancfd_gb300 import NSParams, PressurePoisson, inputs, ns_ab_predictor, ns_ab_solver
+    from fortrancfd_gb300 import (NSParams, PressurePoisson, curv, inputs, ns_ab_predictor,
+                                  ns_ab_solver)
     from oracle import oracle as orc
 
     rho_12 = min(case.rho_pos, case.rho_neg) / max(case.rho_pos, case.rho_neg)
@@ -484,6 +485,21 @@ def momentum_section(dev, stream, case, iterations=4, reps=5):
         ns_ab_predictor(pp, prm, t)
         pred = {k: t[k].cpu().numpy() for k in ("u", "v", "w", "su", "sv", "sw")
                 if t[k] is not None}
+        # curv + surface_norms of the same level set (the step's normals and
+        # curvature inputs for the next time step), by compact differences
+        cv_out = [torch.zeros_like(t["phi"]) for _ in range(4)]
+        if not three:
+            cv_out[2] = None
+        curv(pp, prm, t["phi"], *cv_out)  # warm-up
+        ctimes = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            curv(pp, prm, t["phi"], *cv_out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ctimes.append(e0.elapsed_time(e1))
+        cv_gpu = [a.cpu().numpy() if a is not None else None for a in cv_out]
         # e2e: the same step through the C ABI on host arrays
         host = {k: (np.array(a, copy=True) if a is not None else None) for k, a in src.items()}
         t0 = time.perf_counter()
@@ -524,6 +540,12 @@ def momentum_section(dev, stream, case, iterations=4, reps=5):
         np.array_equal(pred[k].view(np.int64), osrc[c].view(np.int64))
         for c, k in enumerate(("su", "sv", "sw")[:nc]))
     t0 = time.perf_counter()
+    cv_or = orc.ns_curvature(case.shape, case.spacing, 3, st["phi"])
+    cpu_curv_ms = (time.perf_counter() - t0) * 1e3
+    curv_bitwise = all(np.array_equal(cv_gpu[c].view(np.int64), cv_or[c].view(np.int64))
+                       for c in range(nc))
+    curv_rel = float(np.abs(cv_gpu[3] - cv_or[3]).max() / np.abs(cv_or[3]).max())
+    t0 = time.perf_counter()
     out = orc.ns_ab_step(case.shape, case.spacing, op, st["rho_now"], vel, st, so, st["p"],
                          krylov=1)
     cpu_ms = (time.perf_counter() - t0) * 1e3
@@ -546,6 +568,11 @@ def momentum_section(dev, stream, case, iterations=4, reps=5):
             "cpu_oracle_ms_per_step": cpu_ms, "cpu_threads": orc.num_threads(),
             "cpu_oracle_predictor_ms": cpu_pred_ms,
             "predictor_gpu_equals_oracle_bitwise": bool(pred_equal),
+            "curvature": {"what": "curv + surface_norms (CCD line solves along every padded line, "
+                                  "curvature, zero-gradient ghosts)",
+                          "ms": statistics.median(ctimes), "cpu_oracle_ms": cpu_curv_ms,
+                          "gradient_equals_oracle_bitwise": bool(curv_bitwise),
+                          "curvature_max_rel_diff": curv_rel},
             "gpu_vs_oracle_max_rel_diff": diff}
 
 
