@@ -141,6 +141,9 @@ struct gbmg_handle {
   // staging copies of the caller's arrays), allocated on first use
   double* ns_buf[48] = {};
   size_t ns_n[48] = {};
+  // CCD factor table of each axis is valid for these line lengths and spacings
+  int ccd_L[3] = {0, 0, 0};
+  double ccd_h[3] = {0.0, 0.0, 0.0};
   std::string err;
 };
 
@@ -1559,11 +1562,19 @@ int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double*
   c.rh = 1.0 / c.h;
   c.rh2 = 1.0 / c.h2;
   c.fast = fdiv_divisor_ok(c.h) && fdiv_divisor_ok(c.h2);
-  // factor table of this axis (recomputed per call: L points, one thread)
-  GB_TRY(ns_buffer(h, kCcdTable + axis, (size_t)14 * c.L));
-  GB_TRY(ns_buffer(h, kCcdWork, (size_t)12 * c.L));
-  LAUNCH(h, GBMG_PROF_MOMENTUM,
-         launch_ccd_decompose(h->stream, c.L, c.h, h->ns_buf[kCcdWork], h->ns_buf[kCcdTable + axis]));
+  // factor table of this axis: one sequential thread, so it is made once
+  // and kept while the line length and spacing stay the same
+  if (h->ccd_L[axis] != c.L || h->ccd_h[axis] != c.h) {
+    h->ccd_L[axis] = 0;
+    GB_TRY(ns_buffer(h, kCcdTable + axis, (size_t)14 * c.L));
+    GB_TRY(ns_buffer(h, kCcdWork, (size_t)12 * c.L));
+    LAUNCH(h, GBMG_PROF_MOMENTUM,
+           launch_ccd_decompose(h->stream, c.L, c.h, h->ns_buf[kCcdWork],
+                                h->ns_buf[kCcdTable + axis]));
+    GB_TRY(check_launch(h, "ccd factors"));
+    h->ccd_L[axis] = c.L;
+    h->ccd_h[axis] = c.h;
+  }
   LAUNCH(h, GBMG_PROF_MOMENTUM,
          launch_ccd_lines(h->stream, c, h->ns_buf[kCcdTable + axis], f + P.lo, S + P.lo, SS + P.lo));
   return check_launch(h, "ccd lines");
