@@ -1739,7 +1739,7 @@ int or_ns_ab_step(const or_grid* gr, const or_ns_params* prm, const double* rho,
 /* ------------------------------------------------------------------------- */
 /* Interface normals and curvature from combined compact differences          */
 /* (curv + surface_norms, NO2 src/interface_solver/others_normals.f90:1-103,   */
-/* NO3 :1-117; the "ccd" scheme of NO2 lib/solver/ccd_solvers.f90:76-159,     */
+/* NO3 :1-166; the "ccd" scheme of NO2 lib/solver/ccd_solvers.f90:76-159,     */
 /* 287-306, 379-399 with TWIN_DEC / TWIN_BKS of lib/solver/matrix_solver.f90). */
 /* Every line of the padded box (g ghosts each side, L = n + 2g points) is    */
 /* one 2x2-block tridiagonal system for (f', f''); the matrix depends only on */
