@@ -7,12 +7,14 @@ recipe (build.py), the ctypes binding (_lib.py), the host-side mirror of the
 reference's pressure routine (ppe.py), the differentiable solve (autograd.py),
 the registered operator torch.ops.gbmg.solve (ops.py), the level-set
 advection of the interface solver (levelset.py), the Adams-Bashforth momentum
-step around the projection (momentum.py) and the seeded synthetic inputs
+step around the projection with the CCD curvature (momentum.py), the whole
+two-phase time step over those (timestep.py) and the seeded synthetic inputs
 (inputs.py).
 """
 from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
 from .levelset import LevelSet, node_velocity  # noqa: F401
-from .momentum import NSParams, curv, ns_ab_predictor, ns_ab_solver, velbc  # noqa: F401
+from .momentum import NSParams, bc, curv, ns_ab_predictor, ns_ab_solver, rho_mu, velbc  # noqa: F401
+from .timestep import InterfaceParams, TwoPhaseStep  # noqa: F401
 
 try:  # torch.ops.gbmg.solve (torch is optional for host-memory use)
     from . import ops  # noqa: F401
@@ -20,4 +22,5 @@ except ImportError:  # pragma: no cover
     pass
 
 __all__ = ["PressurePoisson", "LevelSet", "node_velocity", "NSParams", "ns_ab_solver",
-           "ns_ab_predictor", "velbc", "curv", "ConvergenceError", "GBMGError"]
+           "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc", "TwoPhaseStep", "InterfaceParams",
+           "ConvergenceError", "GBMGError"]

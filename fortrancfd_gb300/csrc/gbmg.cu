@@ -1580,6 +1580,23 @@ int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double*
   return check_launch(h, "ccd lines");
 }
 
+// Padded cell arrays of the momentum step's layout: the plan of ns_prepare
+// for the given slots (prm supplies the ghost count and mu_12).
+int ns_cells(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_ns_fields* f, int mem,
+             const int* slots, const bool* outs, int n, NsPlan* P, bool (&out)[kNsFields]) {
+  if (!prm) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
+  bool used[kNsFields] = {}, in[kNsFields] = {};
+  for (int i = 0; i < kNsFields; ++i) out[i] = false;
+  for (int i = 0; i < n; ++i) {
+    used[slots[i]] = in[slots[i]] = true;
+    out[slots[i]] = outs[i];
+  }
+  gbmg_ns_params q = *prm;
+  q.dt = q.re = q.fr = 1.0;
+  q.btn_sf = 0.0;
+  return ns_prepare(h, &q, f, mem, used, in, P);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -2218,6 +2235,48 @@ int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
   double* bcs[4] = {nx, ny, nz, P.base[kNsCurv]};
   LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, bcs));
   GB_TRY(check_launch(h, "curvature"));
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_ns_rho_mu(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi, double ls_wid,
+                   double rho_12, gbmg_field rho, gbmg_field mu, gbmg_field delta, int mem) {
+  GB_TRY(begin(h));
+  if (!(ls_wid > 0) || !(rho_12 > 0)) { h->err = "ls_wid and rho_12 must be > 0"; return GBMG_INVALID_ARG; }
+  gbmg_ns_fields f{};
+  f.phi = phi; f.rho = rho; f.mu = mu; f.delta = delta;
+  int slots[4] = {kNsPhi};
+  bool outs[4] = {false};
+  int n = 1;
+  const gbmg_field* o[3] = {&rho, &mu, &delta};
+  const int os[3] = {kNsRho, kNsMu, kNsDelta};
+  for (int i = 0; i < 3; ++i)
+    if (o[i]->data) { slots[n] = os[i]; outs[n++] = true; }
+  NsPlan P;
+  bool out[kNsFields];
+  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, n, &P, out));
+  LAUNCH(h, GBMG_PROF_MOMENTUM,
+         launch_ns_rho_mu(h->stream, P.a, P.base[kNsPhi], ls_wid, rho_12, P.base[kNsRho],
+                          P.base[kNsMu], P.base[kNsDelta]));
+  GB_TRY(check_launch(h, "rho_mu"));
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
+int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem) {
+  GB_TRY(begin(h));
+  gbmg_ns_fields f{};
+  f.phi = a;
+  const int slots[1] = {kNsPhi};
+  const bool outs[1] = {true};
+  NsPlan P;
+  bool out[kNsFields];
+  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, 1, &P, out));
+  double* arr[4] = {P.base[kNsPhi], nullptr, nullptr, nullptr};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));
+  GB_TRY(check_launch(h, "bc"));
   GB_TRY(ns_finish(h, &f, mem, P, out));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;

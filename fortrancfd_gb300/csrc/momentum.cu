@@ -359,6 +359,43 @@ __global__ void __launch_bounds__(kRedThreads) k_ns_change(NsArgs a, const doubl
   grid_sum_finish<1>(acc, R, kSlotSum);
 }
 
+// ls_funs + rho_mu over the whole padded box ("Two phase flows/newOpenMP/2D/
+// src/interface_solver/others.f90:1-61"): x = phi/ls_wid, heavy = 1 above
+// 1 - 1e-12, 0 below -1 + 1e-12, else (1 + x + sin(pi x)/pi)/2 clipped to
+// [0, 1]; delta = (1 + cos(pi x))/(2 ls_wid) inside the band, else 0;
+// rho = heavy + rho_12 (1 - heavy), mu = heavy + mu_12 (1 - heavy).
+// Arrays at element (1,1,1); CUDA's sin and cos.
+__global__ void __launch_bounds__(256) k_ns_rho_mu(NsArgs a, const double* __restrict__ phi,
+                                                   double ls_wid, double rho_12,
+                                                   double* __restrict__ rho,
+                                                   double* __restrict__ mu,
+                                                   double* __restrict__ delta) {
+  const int g = a.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1 - g;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1 - g;
+  const int k = (a.nz > 1 ? (int)blockIdx.z + 1 - g : 1);
+  if (i > a.nx + g || j > a.ny + g) return;
+  const int64_t q = ns_at(a, i, j, k);
+  const double pi = 3.141592653589793;
+  const double eps = 1.0e-12;
+  const double x = phi[q] / ls_wid;
+  double heavy, hp;
+  if (x > 1.0 - eps) {
+    heavy = 1.0;
+    hp = 0.0;
+  } else if (x < -1.0 + eps) {
+    heavy = 0.0;
+    hp = 0.0;
+  } else {
+    heavy = 0.5 * (1.0 + x + sin(pi * x) / pi);
+    hp = 0.5 * (1.0 + cos(pi * x)) / ls_wid;
+  }
+  heavy = fmax(fmin(heavy, 1.0), 0.0);
+  if (rho) rho[q] = heavy + rho_12 * (1.0 - heavy);
+  if (mu) mu[q] = heavy + a.mu_12 * (1.0 - heavy);
+  if (delta) delta[q] = hp;
+}
+
 dim3 ns_grid(const NsArgs& a) {
   return dim3((unsigned)((a.nx + kNsBx - 1) / kNsBx), (unsigned)((a.ny + kNsBy - 1) / kNsBy),
               (unsigned)a.nz);
@@ -416,6 +453,14 @@ void launch_ns_change(cudaStream_t s, const NsArgs& a, const double* const now[3
   else
     k_ns_change<false><<<blocks, kRedThreads, 0, s>>>(a, now[0], now[1], nullptr, tmp[0], tmp[1],
                                                       nullptr, R);
+}
+
+void launch_ns_rho_mu(cudaStream_t s, const NsArgs& a, const double* phi, double ls_wid,
+                      double rho_12, double* rho, double* mu, double* delta) {
+  const dim3 block(32, 8);
+  const dim3 grid((unsigned)((a.nx + 2 * a.g + 31) / 32), (unsigned)((a.ny + 2 * a.g + 7) / 8),
+                  (unsigned)(a.nz > 1 ? a.nz + 2 * a.g : 1));
+  k_ns_rho_mu<<<grid, block, 0, s>>>(a, phi, ls_wid, rho_12, rho, mu, delta);
 }
 
 }  // namespace gbmg

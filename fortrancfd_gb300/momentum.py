@@ -206,5 +206,34 @@ def curv(pp, prm: NSParams, phi, nrm_x, nrm_y, nrm_z, curvature):
     pp._check(pp._L.gbmg_ns_curvature(pp._h, C.byref(c), *fs, mems.pop()), "curv")
 
 
-__all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "padded_shape",
+def _one_memory(*pairs):
+    mems = {m for _, m in pairs if m is not None}
+    if len(mems) != 1:
+        raise ValueError("all arrays of one call must be in the same memory (host or CUDA)")
+    return mems.pop()
+
+
+def rho_mu(pp, prm: NSParams, phi, ls_wid, rho_12, rho=None, mu=None, delta=None):
+    """ls_funs + rho_mu over the padded box: rho, mu (viscosity ratio
+    prm.mu_12) and delta of phi, into the given padded arrays (None skipped)."""
+    fs = [_padded_field(a, n, pp.shape, prm.ghost)
+          for n, a in (("phi", phi), ("rho", rho), ("mu", mu), ("delta", delta))]
+    m = _one_memory(*fs)
+    _sync({"phi": phi, "rho": rho, "mu": mu, "delta": delta})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_rho_mu(pp._h, C.byref(c), fs[0][0], float(ls_wid), float(rho_12),
+                                   fs[1][0], fs[2][0], fs[3][0], m), "rho_mu")
+
+
+def bc(pp, prm: NSParams, a):
+    """bc: zero-gradient ghost layers of a padded cell array, in place."""
+    f = _padded_field(a, "phi", pp.shape, prm.ghost)
+    m = _one_memory(f)
+    _sync({"a": a})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_bc(pp._h, C.byref(c), f[0], m), "bc")
+
+
+__all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc",
+           "padded_shape",
            "ConvergenceError", "GBMGError"]

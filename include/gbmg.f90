@@ -290,6 +290,24 @@ module gbmg
       integer(c_int), value :: mem
     end function
 
+    integer(c_int) function gbmg_ns_rho_mu(h, prm, phi, ls_wid, rho_12, rho, mu, delta, mem) &
+        bind(c, name="gbmg_ns_rho_mu")
+      import :: c_int, c_ptr, c_double, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: phi, rho, mu, delta
+      real(c_double), value :: ls_wid, rho_12
+      integer(c_int), value :: mem
+    end function
+
+    integer(c_int) function gbmg_ns_bc(h, prm, a, mem) bind(c, name="gbmg_ns_bc")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: a
+      integer(c_int), value :: mem
+    end function
+
     integer(c_int64_t) function gbmg_ls_kernel_launches(ls) bind(c, name="gbmg_ls_kernel_launches")
       import :: c_int64_t, c_ptr
       type(c_ptr), value :: ls

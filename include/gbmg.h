@@ -308,6 +308,20 @@ int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
                       gbmg_field nrm_x, gbmg_field nrm_y, gbmg_field nrm_z, gbmg_field curv,
                       int mem);
 
+/* ls_funs + rho_mu over the whole padded box ("Two phase flows/newOpenMP/2D/
+ * src/interface_solver/others.f90:1-61"): with x = phi/ls_wid, heavy = 1 for
+ * x > 1 - 1e-12, 0 for x < -1 + 1e-12, else (1 + x + sin(pi x)/pi)/2 clipped
+ * to [0, 1]; delta = (1 + cos(pi x))/(2 ls_wid) inside the band, else 0;
+ * rho = heavy + rho_12 (1 - heavy), mu = heavy + prm->mu_12 (1 - heavy): the
+ * rho, mu and delta of the momentum step (as its old fields one step later).
+ * Padded arrays as gbmg_ns_fields; CUDA's sin and cos; NULL outputs skipped. */
+int gbmg_ns_rho_mu(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi, double ls_wid,
+                   double rho_12, gbmg_field rho, gbmg_field mu, gbmg_field delta, int mem);
+
+/* bc ("Two phase flows/newOpenMP/2D/src/others/bcs.f90:1-26"): zero-gradient
+ * ghost layers of one padded cell array, in place. */
+int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem);
+
 /* Copies level `level`'s face coefficients (FP64) into cell-shaped arrays of
  * that level's size (gbmg_level_dims).  For tests of the coarsening rule. */
 int gbmg_level_coef(gbmg_handle* h, int level, gbmg_field cx, gbmg_field cy, gbmg_field cz,

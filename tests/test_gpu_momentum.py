@@ -194,3 +194,64 @@ def test_errors(cuda):
         s2["mu"] = big[:, :s["mu"].shape[1]]  # other strides than the rest
         with pytest.raises(GBMGError, match="strides"):
             ns_ab_solver(pp, prm, s2)
+
+
+def test_two_ghost_layers_and_strided_views(cuda):
+    """ghost = 2 (the stencils' minimum) and arrays that are views into larger
+    allocations (strides wider than the padded box), on the device."""
+    import torch
+    g = 2
+    shape = (6, 8, 8)
+    case = inputs.custom(shape, extent=(1.0, 1.0, 0.75), centers=((0.5, 0.5, 0.4),),
+                         radii=(0.25,), seed=3)
+    st = inputs.momentum_state(case, ghost=g, amplitude=0.3)
+    prm = NSParams(dt=2e-3, re=50.0, fr=0.5, we=2.0, btn_sf=1.0, ghost=g,
+                   gravity=(0.0, 0.0, -1.0))
+    op = orc.ns_params(ghost=g, dt=prm.dt, re=prm.re, fr=prm.fr, we=prm.we, mu_12=prm.mu_12,
+                       gravity=prm.gravity, btn_g=prm.btn_g, btn_sf=prm.btn_sf)
+    old = (st["u"], st["v"], st["w"])
+    so = (st["su_old"], st["sv_old"], st["sw_old"])
+    dif = orc.ns_diffusion(shape, case.spacing, op, st)
+    src, vel = orc.ns_advance(shape, case.spacing, op, old, old, dif, so)
+    vel = [a.copy() for a in vel]
+    orc.velbc(shape, op, *vel)
+    ps = orc.padded_shape(shape, g)
+
+    def view(a):  # the padded box inside a wider allocation
+        big = torch.full((ps[0], ps[1] + 3, ps[2] + 5), float("nan"), dtype=torch.float64,
+                         device=cuda)
+        v = big[:, 1:1 + ps[1], 2:2 + ps[2]]
+        if a is not None:
+            v.copy_(torch.from_numpy(a))
+        else:
+            v.zero_()
+        return v
+
+    s = {k: view(st[k]) for k in ("u", "v", "w", "rho", "mu", "delta", "phi", "nrm_x", "nrm_y",
+                                   "nrm_z", "curv", "su_old", "sv_old", "sw_old")}
+    s.update(u_old=view(st["u"]), v_old=view(st["v"]), w_old=view(st["w"]),
+             su=view(None), sv=view(None), sw=view(None),
+             p=torch.zeros(shape, dtype=torch.float64, device=cuda))
+    with PressurePoisson(shape, case.spacing) as pp:
+        ns_ab_predictor(pp, prm, s)
+    for c, (k, sk) in enumerate(zip(("u", "v", "w"), ("su", "sv", "sw"))):
+        assert np.array_equal(_bits(s[k].cpu().numpy()), _bits(vel[c])), k
+        assert np.array_equal(_bits(s[sk].cpu().numpy()), _bits(src[c])), sk
+
+
+def test_host_and_device_steps_agree(cuda):
+    """The same step through host arrays (staged by the library) and through
+    device tensors gives the same doubles."""
+    import torch
+    shape = (1, 32, 48)
+    case, st, prm = _setup(shape, sf=1.0)
+    s_host = _state_for_lib(st, False)
+    s_dev = {k: (torch.from_numpy(np.ascontiguousarray(a)).to(cuda) if a is not None else None)
+             for k, a in _state_for_lib(st, False).items()}
+    with PressurePoisson(shape, case.spacing, krylov=True) as pp:
+        pp.ppe_init(st["rho_now"])
+        a = ns_ab_solver(pp, prm, s_host)
+        b = ns_ab_solver(pp, prm, s_dev)
+    for k in ("u", "v", "su", "sv", "p"):
+        assert np.array_equal(_bits(s_host[k]), _bits(s_dev[k].cpu().numpy())), k
+    assert a["linf"] == b["linf"] and a["cycles"] == b["cycles"]

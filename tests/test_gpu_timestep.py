@@ -1,0 +1,115 @@
+"""The whole two-phase time step on the GPU (TwoPhaseStep: switch, level-set
+advection, redistancing, rho_mu, CCD curvature, momentum step with four
+projections, divergence check, cell velocity) against the same sequence of
+the oracle's restatements, for a few steps.  The steps contain FP64 solves to
+1e-12 and CUDA's sin/cos/pow, so the comparison is to a tolerance."""
+import numpy as np
+import pytest
+
+from fortrancfd_gb300 import InterfaceParams, NSParams, TwoPhaseStep, inputs, node_velocity
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+G = 3
+
+
+def _faces(a, axis, shape):
+    nz, ny, nx = shape
+    g = G
+    three = nz > 1
+    sl = {0: (slice(g, g + nz), slice(g, g + ny), slice(g - 1, g + nx)),
+          1: (slice(g, g + nz), slice(g - 1, g + ny), slice(g, g + nx)),
+          2: (slice(g - 1, g + nz), slice(g, g + ny), slice(g, g + nx))}[axis]
+    return a[sl] if three else a[sl[1:]][None]
+
+
+def _inner(a, shape):
+    nz, ny, nx = shape
+    g = G
+    if nz > 1:
+        return a[g:g + nz, g:g + ny, g:g + nx]
+    return a[g:g + ny, g:g + nx][None]
+
+
+def _oracle_run(case, st, ns, itf, steps):
+    shape, sp = case.shape, case.spacing
+    three = shape[0] > 1
+    nc = 3 if three else 2
+    op = orc.ns_params(ghost=G, bc=ns.bc, iterations=ns.iterations, dt=ns.dt, re=ns.re,
+                       fr=ns.fr, we=ns.we, mu_12=ns.mu_12, gravity=ns.gravity, btn_g=ns.btn_g,
+                       btn_sf=ns.btn_sf, p_tol=ns.p_tol)
+    now = {k: (st[k].copy() if st.get(k) is not None else None)
+           for k in ("phi", "u", "v", "w")}
+    for k in ("su", "sv", "sw")[:nc]:
+        now[k] = np.zeros_like(st["phi"])
+    p = np.zeros(shape)
+
+    def derived(n):
+        H = orc.heaviside(n["phi"], itf.ls_wid)
+        n["rho"] = H + itf.rho_12 * (1.0 - H)
+        n["mu"] = H + ns.mu_12 * (1.0 - H)
+        n["delta"] = orc.heaviside_deriv(n["phi"], itf.ls_wid)
+        n["nrm_x"], n["nrm_y"], n["nrm_z"], n["curv"] = orc.ns_curvature(shape, sp, G, n["phi"])
+
+    def nvel(n):
+        f = [_faces(n[k], a, shape) for a, k in enumerate(("u", "v", "w")[:nc])]
+        un, vn, wn = node_velocity(f[0], f[1], f[2] if three else None)
+        return [np.ascontiguousarray(x) if x is not None else None for x in (un, vn, wn)]
+
+    derived(now)
+    vel = nvel(now)
+    for it in range(1, steps + 1):
+        old = {k: (a.copy() if a is not None else None) for k, a in now.items()}
+        phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
+        phi_in = orc.ls_advect(phi_in, vel[0], vel[1], vel[2], ns.dt, sp, steps=1)
+        _inner(now["phi"], shape)[...] = phi_in
+        orc.ns_bc(shape, G, now["phi"])
+        if itf.redis_every and it % itf.redis_every == 0:
+            phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
+            phi_in, _, _ = orc.ls_redistance(phi_in, itf.ls_wid, itf.rdt, sp, rho_12=itf.rho_12,
+                                             btn=1)
+            _inner(now["phi"], shape)[...] = phi_in
+            orc.ns_bc(shape, G, now["phi"])
+        derived(now)
+        rho_now = orc.rho_from_phi(np.ascontiguousarray(_inner(now["phi"], shape)),
+                                   itf.ls_wid, 1.0, itf.rho_12)
+        oldf = {k: old[k] for k in orc.NS_OLD}
+        out = orc.ns_ab_step(shape, sp, op, rho_now, tuple(now[k] for k in ("u", "v", "w")[:nc]),
+                             oldf, tuple(old[k] for k in ("su", "sv", "sw")[:nc]), p, krylov=1)
+        for k in ("u", "v", "w", "su", "sv", "sw")[:2 * nc] if three else ("u", "v", "su", "sv"):
+            now[k] = out[k]
+        p = out["p"]
+        vel = nvel(now)
+    return now, p
+
+
+@pytest.mark.parametrize("shape", [(1, 32, 32), (16, 16, 16)])
+def test_time_steps_match_the_oracle_sequence(cuda, shape):
+    nz, ny, nx = shape
+    ext = (1.0, ny / nx, (nz / nx) if nz > 1 else 1.0)
+    case = inputs.custom(shape, extent=ext, centers=((0.5, 0.45, 0.5 * ext[2]),), radii=(0.25,),
+                         seed=9)
+    st = inputs.momentum_state(case, ghost=G, amplitude=0.3)
+    h = case.spacing[0]
+    ns = NSParams(dt=2e-3, re=100.0, fr=0.5, we=2.0, mu_12=1e-2, btn_sf=1.0, ghost=G,
+                  gravity=(0.0, 0.0, -1.0) if nz > 1 else (0.0, -1.0, 0.0), p_tol=1e-12)
+    itf = InterfaceParams(ls_wid=1.5 * h, rho_12=1e-3, rdt=0.25 * h, redis_every=2)
+    steps = 3
+    want, p_or = _oracle_run(case, st, ns, itf, steps)
+    with TwoPhaseStep(shape, case.spacing, ns, itf, precision="fp64", krylov=True) as ts:
+        ts.load(st["phi"], st["u"], st["v"], st["w"])
+        for _ in range(steps):
+            stats = ts.step()
+        got = {k: (a.cpu().numpy() if a is not None else None) for k, a in ts.now.items()}
+        p = ts.p.cpu().numpy().reshape(p_or.shape)
+    assert stats["status"] == 0 and stats["iter"] == steps
+    assert stats["div_max"] < 1e-6
+    scale = np.abs(want["phi"]).max()
+    np.testing.assert_allclose(got["phi"], want["phi"], rtol=0, atol=1e-10 * scale)
+    for k in ("u", "v", "w") if nz > 1 else ("u", "v"):
+        np.testing.assert_allclose(got[k], want[k], rtol=0, atol=1e-7 * np.abs(want[k]).max(),
+                                   err_msg=k)
+    np.testing.assert_allclose(got["curv"], want["curv"], rtol=0,
+                               atol=1e-7 * np.abs(want["curv"]).max())
+    np.testing.assert_allclose(p, p_or, rtol=0, atol=1e-6 * np.abs(p_or).max())
