@@ -32,17 +32,17 @@ __device__ __forceinline__ int fdiv_exp(double x) {
 
 // y = RN(1/b), |b| in 2^-60..2^60 (checked by the caller)
 __device__ __forceinline__ double div_known(double a, double b, double y) {
-  const double q0 = a * y;
+  const double q0 = __dmul_rn(a, y);
   const int e = fdiv_exp(q0);
-  if (e < 1023 - 900 || e > 1023 + 900) return a / b;
-  const double q1 = fma(fma(-b, q0, a), y, q0);
-  return fma(fma(-b, q1, a), y, q1);
+  if (e < 1023 - 900 || e > 1023 + 900) return __ddiv_rn(a, b);
+  const double q1 = __fma_rn(__fma_rn(-b, q0, a), y, q0);
+  return __fma_rn(__fma_rn(-b, q1, a), y, q1);
 }
 
 // as div_known, with the range of b checked here (a divisor computed in the kernel)
 __device__ __forceinline__ double div_known_checked(double a, double b, double y) {
   const int eb = fdiv_exp(b);
-  if (eb < 1023 - 60 || eb > 1023 + 60) return a / b;
+  if (eb < 1023 - 60 || eb > 1023 + 60) return __ddiv_rn(a, b);
   return div_known(a, b, y);
 }
 
