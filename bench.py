@@ -600,7 +600,7 @@ def timestep_section(dev, stream, case, steps=5):
                   gravity=(0.0, 0.0, -1.0) if three else (0.0, -1.0, 0.0), btn_g=1.0,
                   btn_sf=1.0, ghost=3, iterations=4, p_tol=TOL)
     itf = InterfaceParams(ls_wid=case.eps, rho_12=rho_12, rdt=0.25 * case.spacing[0],
-                          redis_every=5)
+                          redis_every=5, method=2)
     with torch.cuda.stream(stream):
         ts = TwoPhaseStep(case.shape, case.spacing, ns, itf, precision="mixed", krylov=True,
                           stream=stream)
@@ -621,8 +621,9 @@ def timestep_section(dev, stream, case, steps=5):
     redis = [(t, s["redistance_iterations"]) for t, s in zip(times, stats)
              if s["redistance_iterations"]]
     return {"workload": f"{case.name}: whole two-phase time step on the {nx}x{ny}x{nz} grid "
-                        f"(dt={dt}; classical level set: advection every step, redistancing btn=1 "
-                        "every fifth step at rdt=0.25 dx; rho_mu, CCD curvature, AB2 momentum step "
+                        f"(dt={dt}; MPLS level set, the input default: advection every step, "
+                        "redistancing btn=1 every fifth step at rdt=0.25 dx, two mass-preserving "
+                        "corrections; rho_mu, CCD curvature, AB2 momentum step "
                         f"with 4 mixed flexible-CG projections to {TOL}, divergence check)",
             "steps_timed": [s["iter"] for s in stats], "ms_per_step": times,
             "ms_mean": sum(times) / len(times),
@@ -630,6 +631,7 @@ def timestep_section(dev, stream, case, steps=5):
             "ms_with_redistancing": redis[0][0] if redis else None,
             "redistancing_iterations": redis[0][1] if redis else None,
             "div_max": stats[-1]["div_max"], "solve_cycles_last": stats[-1]["cycles"],
+            "mass_last": stats[-1]["mass"],
             "velocity_change_linf_last": stats[-1]["linf"]}
 
 

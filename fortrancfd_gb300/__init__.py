@@ -13,7 +13,8 @@ two-phase time step over those (timestep.py) and the seeded synthetic inputs
 """
 from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
 from .levelset import LevelSet, node_velocity  # noqa: F401
-from .momentum import NSParams, bc, curv, ns_ab_predictor, ns_ab_solver, rho_mu, velbc  # noqa: F401
+from .momentum import (NSParams, bc, curv, ls_mv, mass_preserving_level_set,  # noqa: F401
+                       ns_ab_predictor, ns_ab_solver, rho_mu, velbc)
 from .timestep import InterfaceParams, TwoPhaseStep  # noqa: F401
 
 try:  # torch.ops.gbmg.solve (torch is optional for host-memory use)
@@ -22,5 +23,6 @@ except ImportError:  # pragma: no cover
     pass
 
 __all__ = ["PressurePoisson", "LevelSet", "node_velocity", "NSParams", "ns_ab_solver",
-           "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc", "TwoPhaseStep", "InterfaceParams",
+           "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc", "mass_preserving_level_set", "ls_mv",
+           "TwoPhaseStep", "InterfaceParams",
            "ConvergenceError", "GBMGError"]

@@ -26,6 +26,7 @@
 
 #include "fdiv.cuh"
 #include "gbmg_internal.h"
+#include "reduce.cuh"
 
 namespace gbmg {
 
@@ -231,6 +232,72 @@ __global__ void __launch_bounds__(256) k_curvature(NsArgs a, const double* __res
   }
 }
 
+
+// ls_funs at one value (others.f90:1-37): heavy and delta of x = phi/ls_wid
+__device__ __forceinline__ void mp_funs(double phi, double ls_wid, double* heavy, double* delta) {
+  const double pi = 3.141592653589793;
+  const double x = phi / ls_wid;
+  double h, hp;
+  if (x > 1.0 - 1.0e-12) {
+    h = 1.0;
+    hp = 0.0;
+  } else if (x < -1.0 + 1.0e-12) {
+    h = 0.0;
+    hp = 0.0;
+  } else {
+    h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+    hp = 0.5 * (1.0 + cos(pi * x)) / ls_wid;
+  }
+  *heavy = fmax(fmin(h, 1.0), 0.0);
+  *delta = hp;
+}
+
+// mass_preserving_level_set's sums over the interior (ls_mv's mass and the
+// lambda denominator): acc[0] = sum rho H dv, acc[1] = sum delta^2 |grad phi|
+// (2 (1 - rho_12) H + rho_12) dv; |grad phi| from the compact gradient.
+__global__ void __launch_bounds__(kRedThreads) k_mpls_sums(NsArgs a, const double* phi,
+                                                           const double* gx, const double* gy,
+                                                           const double* gz, double ls_wid,
+                                                           double rho_12, double dv,
+                                                           ReduceScratch R) {
+  double acc[2] = {0.0, 0.0};
+  const int rows = a.ny * a.nz;
+  for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int j = row % a.ny + 1, k = row / a.ny + 1;
+    for (int i = threadIdx.x + 1; i <= a.nx; i += blockDim.x) {
+      const int64_t q = (int64_t)(i - 1) + (int64_t)(j - 1) * a.sy + (int64_t)(k - 1) * a.sz;
+      double heavy, delta;
+      mp_funs(phi[q], ls_wid, &heavy, &delta);
+      const double rho = heavy + rho_12 * (1.0 - heavy);
+      acc[0] += rho * heavy * dv;
+      if (!gx) continue;  // the mass alone
+      const double g2 = gz ? (gx[q] * gx[q] + gy[q] * gy[q]) + gz[q] * gz[q]
+                           : gx[q] * gx[q] + gy[q] * gy[q];
+      const double grad = sqrt(g2);
+      double plam = delta * delta * grad;
+      plam = plam * (2.0 * (1.0 - rho_12) * heavy + rho_12) * a.dx * a.dy;
+      if (gz) plam = plam * a.dz;
+      acc[1] += plam;
+    }
+  }
+  grid_sum_finish<2>(acc, R, kSlotSum);
+}
+
+// phi += lam delta |grad phi| on the interior (delta of the phi before)
+__global__ void __launch_bounds__(256) k_mpls_update(NsArgs a, double* phi, const double* gx,
+                                                     const double* gy, const double* gz,
+                                                     double ls_wid, double lam) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > a.nx || j > a.ny) return;
+  const int64_t q = (int64_t)(i - 1) + (int64_t)(j - 1) * a.sy + (int64_t)(k - 1) * a.sz;
+  double heavy, delta;
+  mp_funs(phi[q], ls_wid, &heavy, &delta);
+  const double g2 = gz ? (gx[q] * gx[q] + gy[q] * gy[q]) + gz[q] * gz[q]
+                       : gx[q] * gx[q] + gy[q] * gy[q];
+  phi[q] = phi[q] + lam * delta * sqrt(g2);
+}
 }  // namespace
 
 void launch_ccd_decompose(cudaStream_t s, int L, double h, double* work, double* table) {
@@ -260,6 +327,19 @@ void launch_curvature(cudaStream_t s, const NsArgs& a, const double* const d1[3]
   else
     k_curvature<false><<<grid, block, 0, s>>>(a, d1[0], d1[1], nullptr, d2[0], d2[1], nullptr,
                                               d2[3], nullptr, nullptr, curv);
+}
+
+void launch_mpls_sums(cudaStream_t s, const NsArgs& a, const double* phi, const double* const g[3],
+                      double ls_wid, double rho_12, double dv, const ReduceScratch& R) {
+  const int blocks = std::min(reduce_blocks_for((size_t)a.ny * a.nz), R.max_blocks);
+  k_mpls_sums<<<blocks, kRedThreads, 0, s>>>(a, phi, g[0], g[1], g[2], ls_wid, rho_12, dv, R);
+}
+
+void launch_mpls_update(cudaStream_t s, const NsArgs& a, double* phi, const double* const g[3],
+                        double ls_wid, double lam) {
+  const dim3 block(32, 8);
+  const dim3 grid((unsigned)((a.nx + 31) / 32), (unsigned)((a.ny + 7) / 8), (unsigned)a.nz);
+  k_mpls_update<<<grid, block, 0, s>>>(a, phi, g[0], g[1], g[2], ls_wid, lam);
 }
 
 }  // namespace gbmg

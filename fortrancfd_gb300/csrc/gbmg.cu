@@ -2282,6 +2282,64 @@ int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem)
   return GBMG_OK;
 }
 
+int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
+                         double ls_wid, double rho_12, double imass, int iterations, int mem,
+                         double* mass) {
+  GB_TRY(begin(h));
+  if (!(ls_wid > 0) || !(rho_12 > 0) || iterations < 0) {
+    h->err = "ls_wid and rho_12 must be > 0 and iterations >= 0";
+    return GBMG_INVALID_ARG;
+  }
+  const bool three = h->grid.nz > 1;
+  gbmg_ns_fields f{};
+  f.phi = phi;
+  const int slots[1] = {kNsPhi};
+  const bool outs[1] = {iterations > 0};
+  NsPlan P;
+  bool out[kNsFields];
+  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, 1, &P, out));
+  const size_t span = (size_t)(P.hi - P.lo + 1);
+  double* gr[3] = {nullptr, nullptr, nullptr};
+  for (int c = 0; c < (three ? 3 : 2); ++c) {
+    GB_TRY(ns_buffer(h, kCcdD2 + c, span));
+    gr[c] = h->ns_buf[kCcdD2 + c] - P.lo;
+  }
+  GB_TRY(ns_buffer(h, kCcdD2 + 6, span));
+  double* dummy = h->ns_buf[kCcdD2 + 6] - P.lo;
+  double* ph = P.base[kNsPhi];
+  const gbmg_grid& g = h->grid;
+  const double dv = three ? g.dx * g.dy * g.dz : g.dx * g.dy;
+  const cudaStream_t s = h->stream;
+  double m = 0.0;
+  const int passes = iterations > 0 ? iterations : 1;
+  for (int it = 0; it < passes; ++it) {
+    // ls_mv, and before a correction surface_norms' gradient of phi
+    const bool correct = iterations > 0;
+    if (correct)
+      for (int c = 0; c < (three ? 3 : 2); ++c) GB_TRY(ccd_axis(h, P, c, ph, gr[c], dummy));
+    const double* gc[3] = {correct ? gr[0] : nullptr, gr[1], gr[2]};
+    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_sums(s, P.a, ph, gc, ls_wid, rho_12, dv, h->red));
+    GB_TRY(check_launch(h, "mass sums"));
+    GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    GB_CUDA(h, cudaStreamSynchronize(s));
+    m = h->host_res[kSlotSum];
+    if (!correct) break;
+    const double lam = (imass - m) / h->host_res[kSlotSum + 1];
+    const double* gcc[3] = {gr[0], gr[1], gr[2]};
+    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_update(s, P.a, ph, gcc, ls_wid, lam));
+    double* arr[4] = {ph, nullptr, nullptr, nullptr};
+    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(s, P.a, arr));
+    GB_TRY(check_launch(h, "mass correction"));
+  }
+  // the mass measured last: before the last correction, as the reference
+  // leaves p%glb%mass (or of phi itself when iterations = 0)
+  if (mass) *mass = m;
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(s));
+  return GBMG_OK;
+}
+
 int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n) {
   GB_TRY(begin(h));
   prof_flush(h);

@@ -372,5 +372,12 @@ void launch_ccd_bc(cudaStream_t s, const NsArgs& a, double* const f[4]);
 // fxx, fyy, fzz, fxy, fxz, fyz (arrays at element (1,1,1))
 void launch_curvature(cudaStream_t s, const NsArgs& a, const double* const d1[3],
                       const double* const d2[6], double* curv);
+// mass_preserving_level_set: result[kSlotSum] = ls_mv mass, [kSlotSum + 1] =
+// the lambda denominator; g = the compact gradient of phi (g[2] null in 2D)
+void launch_mpls_sums(cudaStream_t s, const NsArgs& a, const double* phi, const double* const g[3],
+                      double ls_wid, double rho_12, double dv, const ReduceScratch& R);
+// phi += lam delta |grad phi| on the interior
+void launch_mpls_update(cudaStream_t s, const NsArgs& a, double* phi, const double* const g[3],
+                        double ls_wid, double lam);
 
 }  // namespace gbmg

@@ -234,6 +234,26 @@ def bc(pp, prm: NSParams, a):
     pp._check(pp._L.gbmg_ns_bc(pp._h, C.byref(c), f[0], m), "bc")
 
 
+def mass_preserving_level_set(pp, prm: NSParams, phi, ls_wid, rho_12, imass, iterations=2):
+    """mass_preserving_level_set in place on the padded phi; returns the mass
+    measured last (iterations=0: ls_mv's mass of phi, no correction)."""
+    f = _padded_field(phi, "phi", pp.shape, prm.ghost)
+    m = _one_memory(f)
+    _sync({"phi": phi})
+    c = prm.c_struct()
+    mass = C.c_double(0.0)
+    pp._check(pp._L.gbmg_ns_mass_correct(pp._h, C.byref(c), f[0], float(ls_wid), float(rho_12),
+                                         float(imass), int(iterations), m, C.byref(mass)),
+              "mass_preserving_level_set")
+    return mass.value
+
+
+def ls_mv(pp, prm: NSParams, phi, ls_wid, rho_12):
+    """ls_mv's mass sum (H + rho_12 (1 - H)) H dv of a padded phi."""
+    return mass_preserving_level_set(pp, prm, phi, ls_wid, rho_12, 0.0, iterations=0)
+
+
 __all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc",
+           "mass_preserving_level_set", "ls_mv",
            "padded_shape",
            "ConvergenceError", "GBMGError"]

@@ -7,7 +7,8 @@ is, per step,
 
     call p%switch                       ! old <- now for every time-recorded field
     call interface_solver               ! level_set_rk3_solver; level_set_rk3_redis(1)
-                                        ! every fifth step
+                                        ! every fifth step; with MPLS (method 2, the
+                                        ! input default) mass_preserving_level_set
     call ns_solver                      ! ns_init (rho_mu, curv), ns_ab_solver_SOR,
                                         ! ns_check_convergence_div, node_vel
 
@@ -23,7 +24,8 @@ memory, the switch copies and the cell average of node_vel.
 from dataclasses import dataclass
 
 from .levelset import LevelSet, node_velocity
-from .momentum import NSParams, bc, curv, ns_ab_solver, padded_shape, rho_mu
+from .momentum import (NSParams, bc, curv, ls_mv, mass_preserving_level_set, ns_ab_solver,
+                       padded_shape, rho_mu)
 from .ppe import PressurePoisson
 
 try:
@@ -38,6 +40,7 @@ class InterfaceParams:
     rho_12: float = 1e-3     # density ratio of fluid 2 (phi < 0) to fluid 1
     rdt: float = 0.0         # redistancing pseudo-time step (0: 0.25 dx, the input default)
     redis_every: int = 5     # level_set_rk3_redis(1) every this many steps (0: never)
+    method: int = 1          # 1: classical level set, 2: MPLS (+ mass_preserving_level_set)
 
 
 class TwoPhaseStep:
@@ -114,6 +117,9 @@ class TwoPhaseStep:
         self._derived()
         self._node_vel()
         self.iter = 0
+        # problem_init's imass: ls_mv of the initial level set
+        self.imass = ls_mv(self.pp, self.ns, self.now["phi"], self.itf.ls_wid, self.itf.rho_12)
+        self.mass = self.imass
 
     def _derived(self):
         itf, ns, n = self.itf, self.ns, self.now
@@ -148,6 +154,9 @@ class TwoPhaseStep:
             rdt = itf.rdt or 0.25 * self.spacing[0]
             _, redis, _ = self.ls.redistance(self._inner(phi), itf.ls_wid, rdt, itf.rho_12, btn=1)
             bc(self.pp, ns, phi)
+        if itf.method == 2:
+            self.mass = mass_preserving_level_set(self.pp, ns, phi, itf.ls_wid, itf.rho_12,
+                                                  self.imass, iterations=2)
         # ns_init: rho_mu (and the pressure operator from the new level set), curv
         self._derived()
         self.pp.rho_mu(self._inner(phi), itf.ls_wid, 1.0, itf.rho_12)
@@ -165,7 +174,7 @@ class TwoPhaseStep:
         div_max, div_mean = self.pp.div_stats(u, v, w)
         self._node_vel()
         self.stats = dict(st, div_max=div_max, div_mean=div_mean, redistance_iterations=redis,
-                          iter=self.iter)
+                          iter=self.iter, mass=self.mass)
         return self.stats
 
     def close(self):

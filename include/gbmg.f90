@@ -300,6 +300,17 @@ module gbmg
       integer(c_int), value :: mem
     end function
 
+    integer(c_int) function gbmg_ns_mass_correct(h, prm, phi, ls_wid, rho_12, imass, iterations, &
+        mem, mass) bind(c, name="gbmg_ns_mass_correct")
+      import :: c_int, c_ptr, c_double, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: phi
+      real(c_double), value :: ls_wid, rho_12, imass
+      integer(c_int), value :: iterations, mem
+      real(c_double), intent(out) :: mass
+    end function
+
     integer(c_int) function gbmg_ns_bc(h, prm, a, mem) bind(c, name="gbmg_ns_bc")
       import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
       type(c_ptr), value :: h

@@ -318,6 +318,21 @@ int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
 int gbmg_ns_rho_mu(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi, double ls_wid,
                    double rho_12, gbmg_field rho, gbmg_field mu, gbmg_field delta, int mem);
 
+/* mass_preserving_level_set ("Two phase flows/newOpenMP/2D/src/interface_
+ * solver/mass_preserving_level_set.f90:1-48"; 3D "…/3D+IBM/…"), the correction
+ * of the MPLS interface method, in place on the padded phi: `iterations`
+ * times (the reference: 2) measure ls_mv's mass = sum (H + rho_12 (1 - H)) H dv
+ * and the compact gradient of phi (surface_norms), then
+ *     phi += lam delta |grad phi|,  lam = (imass - mass) /
+ *            sum delta^2 |grad phi| (2 (1 - rho_12) H + rho_12) dv
+ * on the interior, and bc.  *mass receives the mass measured last (before the
+ * last correction, as the reference leaves p%glb%mass); iterations = 0 only
+ * measures it (ls_mv, e.g. imass at the start).  H, delta from ls_funs with
+ * half width ls_wid (CUDA's sin and cos); sums in a fixed order. */
+int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
+                         double ls_wid, double rho_12, double imass, int iterations, int mem,
+                         double* mass);
+
 /* bc ("Two phase flows/newOpenMP/2D/src/others/bcs.f90:1-26"): zero-gradient
  * ghost layers of one padded cell array, in place. */
 int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem);

@@ -1936,3 +1936,74 @@ void or_ns_curvature(const or_grid* gr, int g, const double* phi, double* nx, do
   free(own);
   free(dummy);
 }
+
+/* mass_preserving_level_set (NO2 src/interface_solver/
+ * mass_preserving_level_set.f90:1-48, NO3 the same with dz): `iterations`
+ * times ls_mv's mass (ls_mv, NO2 others.f90:63-105: sum (H + rho_12 (1-H)) H dv)
+ * and surface_norms' compact gradient, then phi += lam delta |grad phi| with
+ * lam = (imass - mass) / sum delta^2 |grad phi| (2 (1 - rho_12) H + rho_12) dv,
+ * and bc.  Returns the mass measured last (iterations = 0: ls_mv only).  Sums
+ * in loop order (the reference's OpenMP reductions have no fixed order). */
+double or_ns_mass_correct(const or_grid* gr, int g, double* phi, double ls_wid, double rho_12,
+                          double imass, int iterations) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  const size_t span = ns_span(&b);
+  const double pi = acos(-1.0);
+  double* gx[3] = {dalloc(span), dalloc(span), three ? dalloc(span) : NULL};
+  double* dummy = dalloc(span);
+  const double dv = three ? gr->dx * gr->dy * gr->dz : gr->dx * gr->dy;
+  double mass = 0.0;
+  const int passes = iterations > 0 ? iterations : 1;
+  for (int it = 0; it < passes; ++it) {
+    const int correct = iterations > 0;
+    if (correct) {
+      ccd_axis(&b, 0, gr->dx, phi, gx[0], dummy);
+      ccd_axis(&b, 1, gr->dy, phi, gx[1], dummy);
+      if (three) ccd_axis(&b, 2, gr->dz, phi, gx[2], dummy);
+    }
+    double m = 0.0, den = 0.0;
+    for (int k = 1; k <= gr->nz; ++k)
+      for (int j = 1; j <= gr->ny; ++j)
+        for (int i = 1; i <= gr->nx; ++i) {
+          const size_t q = NI(&b, i, j, k);
+          const double x = phi[q] / ls_wid;
+          double heavy, delta;
+          if (x > 1.0 - 1e-12) { heavy = 1.0; delta = 0.0; }
+          else if (x < -1.0 + 1e-12) { heavy = 0.0; delta = 0.0; }
+          else {
+            heavy = 0.5 * (1.0 + x + sin(pi * x) / pi);
+            delta = 0.5 * (1.0 + cos(pi * x)) / ls_wid;
+          }
+          heavy = fmax(fmin(heavy, 1.0), 0.0);
+          const double rho = heavy + rho_12 * (1.0 - heavy);
+          m = m + rho * heavy * dv;
+          if (!correct) continue;
+          const double g2 = three ? (gx[0][q] * gx[0][q] + gx[1][q] * gx[1][q]) + gx[2][q] * gx[2][q]
+                                  : gx[0][q] * gx[0][q] + gx[1][q] * gx[1][q];
+          double plam = delta * delta * sqrt(g2);
+          plam = plam * (2.0 * (1.0 - rho_12) * heavy + rho_12) * gr->dx * gr->dy;
+          if (three) plam = plam * gr->dz;
+          den = den + plam;
+        }
+    mass = m;
+    if (!correct) break;
+    const double lam = (imass - m) / den;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 1; k <= gr->nz; ++k)
+      for (int j = 1; j <= gr->ny; ++j)
+        for (int i = 1; i <= gr->nx; ++i) {
+          const size_t q = NI(&b, i, j, k);
+          const double x = phi[q] / ls_wid;
+          double delta = 0.0;
+          if (!(x > 1.0 - 1e-12) && !(x < -1.0 + 1e-12)) delta = 0.5 * (1.0 + cos(pi * x)) / ls_wid;
+          const double g2 = three ? (gx[0][q] * gx[0][q] + gx[1][q] * gx[1][q]) + gx[2][q] * gx[2][q]
+                                  : gx[0][q] * gx[0][q] + gx[1][q] * gx[1][q];
+          phi[q] = phi[q] + lam * delta * sqrt(g2);
+        }
+    or_ns_bc(gr, g, phi);
+  }
+  for (int c = 0; c < 3; ++c) free(gx[c]);
+  free(dummy);
+  return mass;
+}

@@ -101,6 +101,9 @@ def lib():
                                   C.c_int64]
         L.or_ns_bc.argtypes = [_G, C.c_int, _D]
         L.or_ns_curvature.argtypes = [_G, C.c_int, _D, _D, _D, _D, _D, _D]
+        L.or_ns_mass_correct.argtypes = [_G, C.c_int, _D, C.c_double, C.c_double, C.c_double,
+                                         C.c_int]
+        L.or_ns_mass_correct.restype = C.c_double
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -463,3 +466,13 @@ def ns_curvature(shape, spacing, ghost, phi, want_d2=False):
                           _p(d2))
     out = (nx, ny, nz, cv)
     return out + (tuple(d2),) if want_d2 else out
+
+
+def ns_mass_correct(shape, spacing, ghost, phi, ls_wid, rho_12, imass, iterations=2):
+    """mass_preserving_level_set on a copy of the padded phi: returns
+    (phi, mass measured last); iterations = 0 gives ls_mv's mass only."""
+    g = grid(shape, spacing)
+    out = np.array(_pad(phi, shape, ghost, "phi"), copy=True)
+    m = lib().or_ns_mass_correct(C.byref(g), int(ghost), _p(out), float(ls_wid), float(rho_12),
+                                 float(imass), int(iterations))
+    return out, m

@@ -59,6 +59,7 @@ def _oracle_run(case, st, ns, itf, steps):
 
     derived(now)
     vel = nvel(now)
+    _, imass = orc.ns_mass_correct(shape, sp, G, now["phi"], itf.ls_wid, itf.rho_12, 0.0, 0)
     for it in range(1, steps + 1):
         old = {k: (a.copy() if a is not None else None) for k, a in now.items()}
         phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
@@ -71,6 +72,9 @@ def _oracle_run(case, st, ns, itf, steps):
                                              btn=1)
             _inner(now["phi"], shape)[...] = phi_in
             orc.ns_bc(shape, G, now["phi"])
+        if itf.method == 2:
+            now["phi"], _ = orc.ns_mass_correct(shape, sp, G, now["phi"], itf.ls_wid, itf.rho_12,
+                                                imass, 2)
         derived(now)
         rho_now = orc.rho_from_phi(np.ascontiguousarray(_inner(now["phi"], shape)),
                                    itf.ls_wid, 1.0, itf.rho_12)
@@ -84,8 +88,8 @@ def _oracle_run(case, st, ns, itf, steps):
     return now, p
 
 
-@pytest.mark.parametrize("shape", [(1, 32, 32), (16, 16, 16)])
-def test_time_steps_match_the_oracle_sequence(cuda, shape):
+@pytest.mark.parametrize("shape,method", [((1, 32, 32), 1), ((1, 32, 32), 2), ((16, 16, 16), 2)])
+def test_time_steps_match_the_oracle_sequence(cuda, shape, method):
     nz, ny, nx = shape
     ext = (1.0, ny / nx, (nz / nx) if nz > 1 else 1.0)
     case = inputs.custom(shape, extent=ext, centers=((0.5, 0.45, 0.5 * ext[2]),), radii=(0.25,),
@@ -94,7 +98,8 @@ def test_time_steps_match_the_oracle_sequence(cuda, shape):
     h = case.spacing[0]
     ns = NSParams(dt=2e-3, re=100.0, fr=0.5, we=2.0, mu_12=1e-2, btn_sf=1.0, ghost=G,
                   gravity=(0.0, 0.0, -1.0) if nz > 1 else (0.0, -1.0, 0.0), p_tol=1e-12)
-    itf = InterfaceParams(ls_wid=1.5 * h, rho_12=1e-3, rdt=0.25 * h, redis_every=2)
+    itf = InterfaceParams(ls_wid=1.5 * h, rho_12=1e-3, rdt=0.25 * h, redis_every=2,
+                          method=method)
     steps = 3
     want, p_or = _oracle_run(case, st, ns, itf, steps)
     with TwoPhaseStep(shape, case.spacing, ns, itf, precision="fp64", krylov=True) as ts:
@@ -113,3 +118,29 @@ def test_time_steps_match_the_oracle_sequence(cuda, shape):
     np.testing.assert_allclose(got["curv"], want["curv"], rtol=0,
                                atol=1e-7 * np.abs(want["curv"]).max())
     np.testing.assert_allclose(p, p_or, rtol=0, atol=1e-6 * np.abs(p_or).max())
+
+
+@pytest.mark.parametrize("shape", [(1, 40, 48), (16, 20, 24)])
+def test_mass_correction_matches_the_oracle(cuda, shape):
+    import torch
+    from fortrancfd_gb300 import PressurePoisson, ls_mv, mass_preserving_level_set
+    nz, ny, nx = shape
+    h = 1.0 / nx
+    ps = orc.padded_shape(shape, G)
+    grids = np.meshgrid(*[(np.arange(m) - G + 0.5) * h for m in ps], indexing="ij")
+    phi = 0.22 - np.sqrt(sum((a - 0.4) ** 2 for a in grids))
+    sp = (h, h, h)
+    prm = NSParams(dt=1.0, ghost=G)
+    _, m0 = orc.ns_mass_correct(shape, sp, G, phi, 1.5 * h, 1e-3, 0.0, 0)
+    shifted = phi + 0.3 * h
+    want, mw = orc.ns_mass_correct(shape, sp, G, shifted, 1.5 * h, 1e-3, m0, 2)
+    with PressurePoisson(shape, sp) as pp:
+        t = torch.from_numpy(shifted).to(cuda)
+        assert ls_mv(pp, prm, torch.from_numpy(phi).to(cuda), 1.5 * h, 1e-3) == \
+            pytest.approx(m0, rel=1e-13)
+        mg = mass_preserving_level_set(pp, prm, t, 1.5 * h, 1e-3, m0, iterations=2)
+        hostarr = shifted.copy()
+        mass_preserving_level_set(pp, prm, hostarr, 1.5 * h, 1e-3, m0, iterations=2)
+    assert mg == pytest.approx(mw, rel=1e-13)
+    np.testing.assert_allclose(t.cpu().numpy(), want, rtol=0, atol=1e-13 * np.abs(want).max())
+    np.testing.assert_array_equal(hostarr, t.cpu().numpy())
