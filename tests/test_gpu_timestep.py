@@ -120,7 +120,7 @@ def test_time_steps_match_the_oracle_sequence(cuda, shape, method):
     np.testing.assert_allclose(p, p_or, rtol=0, atol=1e-6 * np.abs(p_or).max())
 
 
-@pytest.mark.parametrize("shape", [(1, 40, 48), (16, 20, 24)])
+@pytest.mark.parametrize("shape", [(1, 40, 48), (16, 16, 24)])
 def test_mass_correction_matches_the_oracle(cuda, shape):
     import torch
     from fortrancfd_gb300 import PressurePoisson, ls_mv, mass_preserving_level_set
