@@ -1939,7 +1939,7 @@ void or_ns_curvature(const or_grid* gr, int g, const double* phi, double* nx, do
 
 /* mass_preserving_level_set (NO2 src/interface_solver/
  * mass_preserving_level_set.f90:1-48, NO3 the same with dz): `iterations`
- * times ls_mv's mass (ls_mv, NO2 others.f90:63-105: sum (H + rho_12 (1-H)) H dv)
+ * times ls_mv's mass (ls_mv, NO2 others.f90:63-113: sum (H + rho_12 (1-H)) H dv)
  * and surface_norms' compact gradient, then phi += lam delta |grad phi| with
  * lam = (imass - mass) / sum delta^2 |grad phi| (2 (1 - rho_12) H + rho_12) dv,
  * and bc.  Returns the mass measured last (iterations = 0: ls_mv only).  Sums
