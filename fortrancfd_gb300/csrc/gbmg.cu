@@ -1409,7 +1409,8 @@ int ns_buffer(gbmg_handle* h, int slot, size_t n) {
 // Validate the arrays a call uses, fill the kernel arguments and make every
 // used array device-resident (host memory: staged copies of the padded box).
 int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
-               const bool (&used)[kNsFields], const bool (&copy_in)[kNsFields], NsPlan* P) {
+               const bool (&used)[kNsFields], const bool (&copy_in)[kNsFields], NsPlan* P,
+               bool step_scratch = true) {
   const gbmg_grid& g = h->grid;
   const bool three = g.nz > 1;
   if (!prm || !f) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
@@ -1475,7 +1476,8 @@ int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* 
                                  cudaMemcpyHostToDevice, h->stream));
     P->base[i] = h->ns_buf[i] - P->lo;
   }
-  for (int c = 0; c < 6; ++c) {
+  // vel%tmp and velsrc%tmp of the momentum step (not for the other calls)
+  for (int c = 0; c < 6 && step_scratch; ++c) {
     if (!three && c % 3 == 2) continue;
     GB_TRY(ns_buffer(h, kNsTmp + c, span));
     P->base[kNsTmp + c] = h->ns_buf[kNsTmp + c] - P->lo;
@@ -1594,7 +1596,7 @@ int ns_cells(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_ns_fields* f, int m
   gbmg_ns_params q = *prm;
   q.dt = q.re = q.fr = 1.0;
   q.btn_sf = 0.0;
-  return ns_prepare(h, &q, f, mem, used, in, P);
+  return ns_prepare(h, &q, f, mem, used, in, P, false);
 }
 
 }  // namespace
@@ -2179,7 +2181,7 @@ int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_
   NsPlan P;
   gbmg_ns_params q = prm ? *prm : gbmg_ns_params{};
   if (prm) { q.dt = q.re = q.fr = 1.0; q.btn_sf = 0.0; }  // velbc reads only ghost and bc
-  GB_TRY(ns_prepare(h, prm ? &q : nullptr, &f, mem, used, in, &P));
+  GB_TRY(ns_prepare(h, prm ? &q : nullptr, &f, mem, used, in, &P, false));
   double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
   LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(h->stream, P.a, P.bc, now));
   GB_TRY(check_launch(h, "velbc"));
@@ -2207,7 +2209,7 @@ int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
   q.dt = q.re = q.fr = 1.0;  // only ghost is read
   q.btn_sf = 0.0;
   NsPlan P;
-  GB_TRY(ns_prepare(h, &q, &f, mem, used, in, &P));
+  GB_TRY(ns_prepare(h, &q, &f, mem, used, in, &P, false));
   const size_t span = (size_t)(P.hi - P.lo + 1);
   double* d2[7];
   for (int i = 0; i < 7; ++i) {
