@@ -298,6 +298,86 @@ __global__ void __launch_bounds__(256) k_mpls_update(NsArgs a, double* phi, cons
                        : gx[q] * gx[q] + gy[q] * gy[q];
   phi[q] = phi[q] + lam * delta * sqrt(g2);
 }
+
+// vof_wlic_solver's flux along axis ax at faces 0..n of that axis and rows
+// 0..n of the others (the reference's is-1..ie ranges): the WLIC blend of the
+// THINC flux (beta = 2.3) and the upwind flux by the normal's share, the
+// normal being surface_norms2's central difference of phi at the clamped
+// upwind cell (zero-gradient ghosts).  Arrays at element (1,1,1).
+__global__ void __launch_bounds__(256) k_wlic_flux(NsArgs a, int ax, const double* __restrict__ vof,
+                                                   const double* __restrict__ vel,
+                                                   const double* __restrict__ phi,
+                                                   double* __restrict__ flux) {
+  const bool three = a.nz > 1;
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  const int j = blockIdx.y * 8 + threadIdx.y;
+  const int k = three ? (int)blockIdx.z : 1;
+  if (i > a.nx || j > a.ny) return;
+  const double eps = 1.0e-12, beta = 2.3;
+  const double dt = a.dt;
+  const double hs[3] = {a.dx, a.dy, a.dz};
+  const int n[3] = {a.nx, a.ny, a.nz};
+  const int64_t st[3] = {1, a.sy, a.sz};
+  const int64_t q = (int64_t)(i - 1) + (int64_t)(j - 1) * a.sy + (int64_t)(k - 1) * a.sz;
+  const double u = vel[q];
+  int cc[3] = {i, j, k};
+  double isgn = 1.0;
+  if (!(u > 0.0)) {
+    cc[ax] += 1;
+    isgn = 0.0;
+  }
+  const int64_t qi = q + (cc[ax] - (ax == 0 ? i : (ax == 1 ? j : k))) * st[ax];
+  const double f = vof[qi];
+  double l;
+  if (f > 1.0 - eps || f < eps) {
+    l = f * u * dt;
+  } else {
+    const int cb = cc[ax] - 1 < 1 ? 1 : cc[ax] - 1;
+    const int64_t qb = qi + (cb - cc[ax]) * st[ax];
+    const double alpha = vof[qb] < vof[qi + st[ax]] ? 1.0 : -1.0;
+    const double h = hs[ax];
+    const double a1 = exp(beta * (2.0 * f - 1.0) / alpha);
+    const double a3 = exp(beta);
+    const double xc = 0.5 / beta * log((a3 * a3 - a1 * a3) / (a1 * a3 - 1.0));
+    const double a4 = cosh(beta * ((isgn - u * dt / h) - xc));
+    const double a5 = cosh(beta * (isgn - xc));
+    int c[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) c[d] = cc[d] < 1 ? 1 : (cc[d] > n[d] ? n[d] : cc[d]);
+    if (!three) c[2] = 1;
+    const int64_t qc = (int64_t)(c[0] - 1) + (int64_t)(c[1] - 1) * a.sy + (int64_t)(c[2] - 1) * a.sz;
+    double nrm[3];
+    nrm[0] = 0.5 * (phi[qc + 1] - phi[qc - 1]) / a.dx;
+    nrm[1] = 0.5 * (phi[qc + a.sy] - phi[qc - a.sy]) / a.dy;
+    nrm[2] = three ? 0.5 * (phi[qc + a.sz] - phi[qc - a.sz]) / a.dz : 0.0;
+    double w = three ? (fabs(nrm[0]) + fabs(nrm[1])) + fabs(nrm[2]) : fabs(nrm[0]) + fabs(nrm[1]);
+    w = fabs(nrm[ax]) / w;
+    l = 0.5 * (u * dt - alpha * h / beta * log(a4 / a5));
+    l = l * w + (1.0 - w) * f * u * dt;
+  }
+  flux[q] = l;
+}
+
+// the cell update of one sweep (clipped to [0, 1] after the last sweep)
+__global__ void __launch_bounds__(256) k_wlic_update(NsArgs a, int ax, int last, double* vof,
+                                                     const double* __restrict__ vof_old,
+                                                     const double* __restrict__ vel,
+                                                     const double* __restrict__ flux) {
+  const int i = blockIdx.x * 32 + threadIdx.x + 1;
+  const int j = blockIdx.y * 8 + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > a.nx || j > a.ny) return;
+  const double eps = 1.0e-12;
+  const int64_t st = ax == 0 ? 1 : (ax == 1 ? a.sy : a.sz);
+  const double h = ax == 0 ? a.dx : (ax == 1 ? a.dy : a.dz);
+  const int64_t q = (int64_t)(i - 1) + (int64_t)(j - 1) * a.sy + (int64_t)(k - 1) * a.sz;
+  double f = vof[q] - (flux[q] - flux[q - st]) / h + vof_old[q] * a.dt * (vel[q] - vel[q - st]) / h;
+  if (last) {
+    if (f < eps) f = 0.0;
+    if (f > 1.0 - eps) f = 1.0;
+  }
+  vof[q] = f;
+}
 }  // namespace
 
 void launch_ccd_decompose(cudaStream_t s, int L, double h, double* work, double* table) {
@@ -340,6 +420,17 @@ void launch_mpls_update(cudaStream_t s, const NsArgs& a, double* phi, const doub
   const dim3 block(32, 8);
   const dim3 grid((unsigned)((a.nx + 31) / 32), (unsigned)((a.ny + 7) / 8), (unsigned)a.nz);
   k_mpls_update<<<grid, block, 0, s>>>(a, phi, g[0], g[1], g[2], ls_wid, lam);
+}
+
+void launch_wlic(cudaStream_t s, const NsArgs& a, int ax, double* vof, const double* vof_old,
+                 const double* vel, const double* phi, double* flux) {
+  const dim3 block(32, 8);
+  const bool three = a.nz > 1;
+  const dim3 gf((unsigned)((a.nx + 1 + 31) / 32), (unsigned)((a.ny + 1 + 7) / 8),
+                (unsigned)(three ? a.nz + 1 : 1));
+  k_wlic_flux<<<gf, block, 0, s>>>(a, ax, vof, vel, phi, flux);
+  const dim3 gu((unsigned)((a.nx + 31) / 32), (unsigned)((a.ny + 7) / 8), (unsigned)a.nz);
+  k_wlic_update<<<gu, block, 0, s>>>(a, ax, ax == (three ? 2 : 1), vof, vof_old, vel, flux);
 }
 
 }  // namespace gbmg

@@ -2342,6 +2342,40 @@ int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field p
   return GBMG_OK;
 }
 
+int gbmg_ns_vof_advect(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field vof,
+                       gbmg_field vof_old, gbmg_field u_old, gbmg_field v_old, gbmg_field w_old,
+                       gbmg_field phi, int mem) {
+  GB_TRY(begin(h));
+  if (!prm || !(prm->dt > 0)) { h->err = "dt must be > 0"; return GBMG_INVALID_ARG; }
+  const bool three = h->grid.nz > 1;
+  // the cell arrays ride in the plan's cell slots (vof, vof_old, phi), the
+  // face velocities in the old-velocity slots
+  gbmg_ns_fields f{};
+  f.rho = vof; f.mu = vof_old; f.phi = phi;
+  f.u_old = u_old; f.v_old = v_old; f.w_old = w_old;
+  int slots[6] = {kNsRho, kNsMu, kNsPhi, kNsUo, kNsVo, kNsWo};
+  const bool outs[6] = {true, false, false, false, false, false};
+  NsPlan P;
+  bool out[kNsFields];
+  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, three ? 6 : 5, &P, out));
+  P.a.dt = prm->dt;
+  const size_t span = (size_t)(P.hi - P.lo + 1);
+  GB_TRY(ns_buffer(h, kCcdD2, span));
+  double* flux = h->ns_buf[kCcdD2] - P.lo;
+  double* vf = P.base[kNsRho];
+  const double* vel[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
+  for (int ax = 0; ax < (three ? 3 : 2); ++ax) {
+    LAUNCH(h, GBMG_PROF_MOMENTUM,
+           launch_wlic(h->stream, P.a, ax, vf, P.base[kNsMu], vel[ax], P.base[kNsPhi], flux));
+    double* arr[4] = {vf, nullptr, nullptr, nullptr};
+    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));
+    GB_TRY(check_launch(h, "vof sweep"));
+  }
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
 int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n) {
   GB_TRY(begin(h));
   prof_flush(h);

@@ -376,6 +376,10 @@ void launch_curvature(cudaStream_t s, const NsArgs& a, const double* const d1[3]
 // the lambda denominator; g = the compact gradient of phi (g[2] null in 2D)
 void launch_mpls_sums(cudaStream_t s, const NsArgs& a, const double* phi, const double* const g[3],
                       double ls_wid, double rho_12, double dv, const ReduceScratch& R);
+// one sweep of vof_wlic_solver along axis ax (flux, then the cell update;
+// the caller applies bc): arrays at element (1,1,1), flux a padded scratch
+void launch_wlic(cudaStream_t s, const NsArgs& a, int ax, double* vof, const double* vof_old,
+                 const double* vel, const double* phi, double* flux);
 // phi += lam delta |grad phi| on the interior
 void launch_mpls_update(cudaStream_t s, const NsArgs& a, double* phi, const double* const g[3],
                         double ls_wid, double lam);

@@ -248,12 +248,26 @@ def mass_preserving_level_set(pp, prm: NSParams, phi, ls_wid, rho_12, imass, ite
     return mass.value
 
 
+def vof_wlic_solver(pp, prm: NSParams, vof, vof_old, u_old, v_old, w_old, phi):
+    """vof_wlic_solver: the CLSVOF volume fraction advanced one step (prm.dt)
+    in place; padded arrays (u_old, v_old, w_old the face velocities)."""
+    three = pp.shape[0] > 1
+    fs = [_padded_field(a, n, pp.shape, prm.ghost)
+          for n, a in (("phi", vof), ("phi", vof_old), ("u", u_old), ("v", v_old),
+                       ("w", w_old if three else None), ("phi", phi))]
+    m = _one_memory(*fs)
+    _sync({"vof": vof, "old": vof_old, "u": u_old, "v": v_old, "w": w_old, "phi": phi})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_vof_advect(pp._h, C.byref(c), *[f[0] for f in fs], m),
+              "vof_wlic_solver")
+
+
 def ls_mv(pp, prm: NSParams, phi, ls_wid, rho_12):
     """ls_mv's mass sum (H + rho_12 (1 - H)) H dv of a padded phi."""
     return mass_preserving_level_set(pp, prm, phi, ls_wid, rho_12, 0.0, iterations=0)
 
 
 __all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc",
-           "mass_preserving_level_set", "ls_mv",
+           "mass_preserving_level_set", "ls_mv", "vof_wlic_solver",
            "padded_shape",
            "ConvergenceError", "GBMGError"]

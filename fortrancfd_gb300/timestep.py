@@ -25,7 +25,7 @@ from dataclasses import dataclass
 
 from .levelset import LevelSet, node_velocity
 from .momentum import (NSParams, bc, curv, ls_mv, mass_preserving_level_set, ns_ab_solver,
-                       padded_shape, rho_mu)
+                       padded_shape, rho_mu, vof_wlic_solver)
 from .ppe import PressurePoisson
 
 try:
@@ -40,7 +40,10 @@ class InterfaceParams:
     rho_12: float = 1e-3     # density ratio of fluid 2 (phi < 0) to fluid 1
     rdt: float = 0.0         # redistancing pseudo-time step (0: 0.25 dx, the input default)
     redis_every: int = 5     # level_set_rk3_redis(1) every this many steps (0: never)
-    method: int = 1          # 1: classical level set, 2: MPLS (+ mass_preserving_level_set)
+    method: int = 1          # 1: classical level set, 2: MPLS (+ mass_preserving_level_set),
+                             # 3: CLSVOF (VOF transport, rho and mu from the volume fraction)
+    recon_every: int = 10    # CLSVOF: clsvof_recon every this many steps (the reference: 10;
+                             # redistancing every redis_every = 3 otherwise)
 
 
 class TwoPhaseStep:
@@ -48,7 +51,7 @@ class TwoPhaseStep:
     step; itf: InterfaceParams.  precision / krylov as PressurePoisson."""
 
     _TIMED = ("phi", "u", "v", "w", "su", "sv", "sw", "rho", "mu", "delta", "nrm_x", "nrm_y",
-              "nrm_z", "curv")
+              "nrm_z", "curv", "vof")
 
     def __init__(self, shape, spacing, ns: NSParams, itf: InterfaceParams, precision="mixed",
                  krylov=False, device=None, stream=None):
@@ -97,7 +100,7 @@ class TwoPhaseStep:
         return a[sl[1:]].unsqueeze(0)
 
     # -- set-up ------------------------------------------------------------------
-    def load(self, phi, u, v, w=None, p=None):
+    def load(self, phi, u, v, w=None, p=None, vof=None):
         """Initial state (padded arrays, numpy or torch): phi and the face
         velocity; the derived fields (rho, mu, delta, normals, curvature, cell
         velocity) are formed as the reference's problem_init leaves them, and
@@ -114,6 +117,13 @@ class TwoPhaseStep:
         for k in ("su", "sv", "sw"):
             if self.now[k] is not None:
                 self.now[k].zero_()
+        if vof is not None:
+            put(self.now["vof"], vof)
+        elif self.itf.method == 3:  # the smoothed Heaviside of phi
+            x = self.now["phi"] / self.itf.ls_wid
+            hv = 0.5 * (1.0 + x + torch.sin(torch.pi * x) / torch.pi)
+            hv = torch.where(x > 1 - 1e-12, 1.0, torch.where(x < -1 + 1e-12, 0.0, hv))
+            self.now["vof"].copy_(hv.clamp(0.0, 1.0))
         self._derived()
         self._node_vel()
         self.iter = 0
@@ -123,7 +133,14 @@ class TwoPhaseStep:
 
     def _derived(self):
         itf, ns, n = self.itf, self.ns, self.now
-        rho_mu(self.pp, ns, n["phi"], itf.ls_wid, itf.rho_12, n["rho"], n["mu"], n["delta"])
+        if itf.method == 3:
+            # rho_mu with CLSVOF: heavy = vof (others.f90:50-52); delta from phi
+            rho_mu(self.pp, ns, n["phi"], itf.ls_wid, itf.rho_12, None, None, n["delta"])
+            hv = n["vof"]
+            n["rho"].copy_(hv + itf.rho_12 * (1.0 - hv))
+            n["mu"].copy_(hv + ns.mu_12 * (1.0 - hv))
+        else:
+            rho_mu(self.pp, ns, n["phi"], itf.ls_wid, itf.rho_12, n["rho"], n["mu"], n["delta"])
         if ns.btn_sf:
             curv(self.pp, ns, n["phi"], n["nrm_x"], n["nrm_y"], n["nrm_z"], n["curv"])
 
@@ -147,19 +164,28 @@ class TwoPhaseStep:
         # interface_solver: advection with the previous cell velocity, then
         # redistancing every redis_every steps
         phi = self.now["phi"]
+        rdt = itf.rdt or 0.25 * self.spacing[0]
+        if itf.method == 3:
+            o = self.old
+            vof_wlic_solver(self.pp, ns, self.now["vof"], o["vof"], o["u"], o["v"], o["w"], phi)
         self.ls.advect(self._inner(phi), *nvel_old, dt=ns.dt, steps=1)
         bc(self.pp, ns, phi)
         redis = 0
-        if itf.redis_every and self.iter % itf.redis_every == 0:
-            rdt = itf.rdt or 0.25 * self.spacing[0]
+        if itf.method == 3 and itf.recon_every and self.iter % itf.recon_every == 0:
+            redis = self._clsvof_recon(rdt)
+        elif itf.redis_every and self.iter % itf.redis_every == 0:
             _, redis, _ = self.ls.redistance(self._inner(phi), itf.ls_wid, rdt, itf.rho_12, btn=1)
             bc(self.pp, ns, phi)
         if itf.method == 2:
             self.mass = mass_preserving_level_set(self.pp, ns, phi, itf.ls_wid, itf.rho_12,
                                                   self.imass, iterations=2)
-        # ns_init: rho_mu (and the pressure operator from the new level set), curv
+        # ns_init: rho_mu (and the pressure operator from the new level set, or
+        # from the volume fraction with CLSVOF), curv
         self._derived()
-        self.pp.rho_mu(self._inner(phi), itf.ls_wid, 1.0, itf.rho_12)
+        if itf.method == 3:
+            self.pp.ppe_init(self._inner(self.now["rho"]).contiguous())
+        else:
+            self.pp.rho_mu(self._inner(phi), itf.ls_wid, 1.0, itf.rho_12)
         # ns_ab_solver_SOR: vel%now starts as vel%old (the switch left it)
         o, n = self.old, self.now
         state = {"u": n["u"], "v": n["v"], "w": n["w"], "u_old": o["u"], "v_old": o["v"],
@@ -176,6 +202,30 @@ class TwoPhaseStep:
         self.stats = dict(st, div_max=div_max, div_mean=div_mean, redistance_iterations=redis,
                           iter=self.iter, mass=self.mass)
         return self.stats
+
+    def _clsvof_recon(self, rdt):
+        """clsvof_recon (clsvof.f90:145-192): phi = 2 vof - 1 redistanced from
+        scratch (btn 0) for 3 dx of pseudo time, taken where the old |phi| <
+        ls_wid, then level_set_rk3_redis(1)."""
+        itf, ns = self.itf, self.ns
+        phi = self.now["phi"]
+        keep = phi.clone()
+        phi.copy_(2.0 * self.now["vof"] - 1.0)
+        n, t = 0, 0.0
+        while True:  # the reference's loop: time += rdt until time > 3 dx
+            n += 1
+            t += rdt
+            if t > 3.0 * self.spacing[0]:
+                break
+        _, it0, _ = self.ls.redistance(self._inner(phi), itf.ls_wid, rdt, itf.rho_12, btn=0,
+                                       max_iter=n)
+        bc(self.pp, ns, phi)
+        near = keep.abs() < itf.ls_wid
+        keep[near] = phi[near]
+        phi.copy_(keep)
+        _, it1, _ = self.ls.redistance(self._inner(phi), itf.ls_wid, rdt, itf.rho_12, btn=1)
+        bc(self.pp, ns, phi)
+        return it0 + it1
 
     def close(self):
         for x in (self.pp, self.ls):

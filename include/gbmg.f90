@@ -311,6 +311,15 @@ module gbmg
       real(c_double), intent(out) :: mass
     end function
 
+    integer(c_int) function gbmg_ns_vof_advect(h, prm, vof, vof_old, u_old, v_old, w_old, phi, &
+        mem) bind(c, name="gbmg_ns_vof_advect")
+      import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: vof, vof_old, u_old, v_old, w_old, phi
+      integer(c_int), value :: mem
+    end function
+
     integer(c_int) function gbmg_ns_bc(h, prm, a, mem) bind(c, name="gbmg_ns_bc")
       import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
       type(c_ptr), value :: h

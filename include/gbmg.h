@@ -333,6 +333,19 @@ int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field p
                          double ls_wid, double rho_12, double imass, int iterations, int mem,
                          double* mass);
 
+/* vof_wlic_solver ("Two phase flows/newOpenMP/2D/src/interface_solver/
+ * clsvof.f90:1-143"; 3D "…/3D+IBM/…"), the volume-fraction transport of the
+ * CLSVOF interface method, in place on the padded vof: sweeps along x, y (z),
+ * each the WLIC flux at every face (a THINC profile with beta = 2.3, weighted
+ * by |n_d|/|n|_1 of surface_norms2's central-difference normal of phi, against
+ * the upwind flux vof u dt), the update vof -= d(flux)/dx_d - vof_old dt du/dx_d
+ * and bc; vof is clipped to [0, 1] (1e-12 margins) after the last sweep.
+ * u_old, v_old, w_old are the face velocities (vel%old), prm->dt the step;
+ * padded arrays as gbmg_ns_fields.  CUDA's exp, log and cosh. */
+int gbmg_ns_vof_advect(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field vof,
+                       gbmg_field vof_old, gbmg_field u_old, gbmg_field v_old, gbmg_field w_old,
+                       gbmg_field phi, int mem);
+
 /* bc ("Two phase flows/newOpenMP/2D/src/others/bcs.f90:1-26"): zero-gradient
  * ghost layers of one padded cell array, in place. */
 int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem);

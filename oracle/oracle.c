@@ -2007,3 +2007,89 @@ double or_ns_mass_correct(const or_grid* gr, int g, double* phi, double ls_wid, 
   free(dummy);
   return mass;
 }
+
+/* ------------------------------------------------------------------------- */
+/* CLSVOF's volume-fraction transport, vof_wlic_solver (NO2 src/interface_     */
+/* solver/clsvof.f90:1-143; NO3 adds the z sweep): directional sweeps x, y(, z) */
+/* of the WLIC flux (a THINC profile of slope beta = 2.3 weighted by the       */
+/* normal's share |n_d|/|n|_1 against the upwind flux vof u dt), each followed */
+/* by the cell update with the divergence correction vof_old dt du/dx and bc; */
+/* after the last sweep vof is clipped to 0 below 1e-12 and 1 above 1 - 1e-12.  */
+/* The normals are surface_norms2's central differences of phi (others_       */
+/* normals.f90:47-74) with zero-gradient ghosts.  Padded arrays as the        */
+/* momentum step's; u, v, w are vel%old.                                      */
+/* ------------------------------------------------------------------------- */
+static inline int clampn(int x, int n) { return x < 1 ? 1 : (x > n ? n : x); }
+
+void or_vof_wlic(const or_grid* gr, int g, double* vof, const double* vof_old, const double* U,
+                 const double* V, const double* W, const double* phi, double dt) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  const int n[3] = {gr->nx, gr->ny, gr->nz};
+  const double h[3] = {gr->dx, gr->dy, gr->dz};
+  const double* vel[3] = {U, V, W};
+  const double eps = 1.0e-12, beta = 2.3;
+  const size_t span = ns_span(&b);
+  double* flux = dalloc(span);
+  for (int ax = 0; ax < (three ? 3 : 2); ++ax) {
+    const double* uu = vel[ax];
+    const int k0 = three ? 0 : 1;
+    /* fluxes at faces 0..n of the axis, rows js-1..je (ks-1..ke) of the others */
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = k0; k <= gr->nz; ++k)
+      for (int j = 0; j <= gr->ny; ++j)
+        for (int i = 0; i <= gr->nx; ++i) {
+          int ix[3] = {i, j, k};
+          const size_t q = NI(&b, i, j, k);
+          const double u = uu[q];
+          int cc[3] = {i, j, k};
+          double isgn;
+          if (u > 0.0) { isgn = 1.0; } else { cc[ax] = ix[ax] + 1; isgn = 0.0; }
+          const size_t qi = NI(&b, cc[0], cc[1], cc[2]);
+          const double f = vof[qi];
+          double l;
+          if (f > 1.0 - eps || f < eps) {
+            l = f * u * dt;
+          } else {
+            int cb[3] = {cc[0], cc[1], cc[2]}, cp[3] = {cc[0], cc[1], cc[2]};
+            cb[ax] = cc[ax] - 1 < 1 ? 1 : cc[ax] - 1;
+            cp[ax] = cc[ax] + 1;
+            const double alpha = vof[NI(&b, cb[0], cb[1], cb[2])] < vof[NI(&b, cp[0], cp[1], cp[2])] ? 1.0 : -1.0;
+            const double a1 = exp(beta * (2.0 * f - 1.0) / alpha);
+            const double a3 = exp(beta);
+            const double xc = 0.5 / beta * log((a3 * a3 - a1 * a3) / (a1 * a3 - 1.0));
+            const double a4 = cosh(beta * ((isgn - u * dt / h[ax]) - xc));
+            const double a5 = cosh(beta * (isgn - xc));
+            /* surface_norms2 at the (zero-gradient clamped) upwind cell */
+            const int c0 = clampn(cc[0], n[0]), c1 = clampn(cc[1], n[1]), c2 = three ? clampn(cc[2], n[2]) : 1;
+            const size_t qc = NI(&b, c0, c1, c2);
+            const size_t sy = b.px, sz = b.px * b.py;
+            double nrm[3];
+            nrm[0] = 0.5 * (phi[qc + 1] - phi[qc - 1]) / gr->dx;
+            nrm[1] = 0.5 * (phi[qc + sy] - phi[qc - sy]) / gr->dy;
+            nrm[2] = three ? 0.5 * (phi[qc + sz] - phi[qc - sz]) / gr->dz : 0.0;
+            double w = three ? (fabs(nrm[0]) + fabs(nrm[1])) + fabs(nrm[2]) : fabs(nrm[0]) + fabs(nrm[1]);
+            w = fabs(nrm[ax]) / w;
+            l = 0.5 * (u * dt - alpha * h[ax] / beta * log(a4 / a5));
+            l = l * w + (1.0 - w) * f * u * dt;
+          }
+          flux[q] = l;
+        }
+    const size_t st = ax == 0 ? 1 : (ax == 1 ? b.px : b.px * b.py);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 1; k <= gr->nz; ++k)
+      for (int j = 1; j <= gr->ny; ++j)
+        for (int i = 1; i <= gr->nx; ++i) {
+          const size_t q = NI(&b, i, j, k);
+          double f = vof[q] - (flux[q] - flux[q - st]) / h[ax] +
+                     vof_old[q] * dt * (uu[q] - uu[q - st]) / h[ax];
+          if (ax == (three ? 2 : 1)) {
+            if (f < eps) f = 0.0;
+            if (f > 1.0 - eps) f = 1.0;
+          }
+          vof[q] = f;
+        }
+    or_ns_bc(gr, g, vof);
+  }
+  free(flux);
+}

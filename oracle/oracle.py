@@ -104,6 +104,7 @@ def lib():
         L.or_ns_mass_correct.argtypes = [_G, C.c_int, _D, C.c_double, C.c_double, C.c_double,
                                          C.c_int]
         L.or_ns_mass_correct.restype = C.c_double
+        L.or_vof_wlic.argtypes = [_G, C.c_int, _D, _D, _D, _D, _D, _D, C.c_double]
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -476,3 +477,14 @@ def ns_mass_correct(shape, spacing, ghost, phi, ls_wid, rho_12, imass, iteration
     m = lib().or_ns_mass_correct(C.byref(g), int(ghost), _p(out), float(ls_wid), float(rho_12),
                                  float(imass), int(iterations))
     return out, m
+
+
+def vof_wlic(shape, spacing, ghost, vof, vof_old, u, v, w, phi, dt):
+    """vof_wlic_solver on a copy of the padded vof; returns it."""
+    g = grid(shape, spacing)
+    out = np.array(_pad(vof, shape, ghost, "vof"), copy=True)
+    args = [_pad(a, shape, ghost, n) if a is not None else None
+            for n, a in (("vof_old", vof_old), ("u", u), ("v", v),
+                         ("w", w if _three(shape) else None), ("phi", phi))]
+    lib().or_vof_wlic(C.byref(g), int(ghost), _p(out), *[_p(a) for a in args], float(dt))
+    return out

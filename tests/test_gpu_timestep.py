@@ -41,12 +41,13 @@ def _oracle_run(case, st, ns, itf, steps):
                        btn_sf=ns.btn_sf, p_tol=ns.p_tol)
     now = {k: (st[k].copy() if st.get(k) is not None else None)
            for k in ("phi", "u", "v", "w")}
+    now["vof"] = orc.heaviside(st["phi"], itf.ls_wid)
     for k in ("su", "sv", "sw")[:nc]:
         now[k] = np.zeros_like(st["phi"])
     p = np.zeros(shape)
 
     def derived(n):
-        H = orc.heaviside(n["phi"], itf.ls_wid)
+        H = n["vof"] if itf.method == 3 else orc.heaviside(n["phi"], itf.ls_wid)
         n["rho"] = H + itf.rho_12 * (1.0 - H)
         n["mu"] = H + ns.mu_12 * (1.0 - H)
         n["delta"] = orc.heaviside_deriv(n["phi"], itf.ls_wid)
@@ -62,11 +63,36 @@ def _oracle_run(case, st, ns, itf, steps):
     _, imass = orc.ns_mass_correct(shape, sp, G, now["phi"], itf.ls_wid, itf.rho_12, 0.0, 0)
     for it in range(1, steps + 1):
         old = {k: (a.copy() if a is not None else None) for k, a in now.items()}
+        if itf.method == 3:
+            now["vof"] = orc.vof_wlic(shape, sp, G, now["vof"], old["vof"], old["u"], old["v"],
+                                      old.get("w"), now["phi"], ns.dt)
         phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
         phi_in = orc.ls_advect(phi_in, vel[0], vel[1], vel[2], ns.dt, sp, steps=1)
         _inner(now["phi"], shape)[...] = phi_in
         orc.ns_bc(shape, G, now["phi"])
-        if itf.redis_every and it % itf.redis_every == 0:
+        if itf.method == 3 and it % itf.recon_every == 0:
+            keep = now["phi"].copy()
+            now["phi"] = 2.0 * now["vof"] - 1.0
+            n, t = 0, 0.0
+            while True:
+                n += 1
+                t += itf.rdt
+                if t > 3.0 * sp[0]:
+                    break
+            phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
+            phi_in, _, _ = orc.ls_redistance(phi_in, itf.ls_wid, itf.rdt, sp, rho_12=itf.rho_12,
+                                             btn=0, max_iter=n)
+            _inner(now["phi"], shape)[...] = phi_in
+            orc.ns_bc(shape, G, now["phi"])
+            near = np.abs(keep) < itf.ls_wid
+            keep[near] = now["phi"][near]
+            now["phi"] = keep
+            phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
+            phi_in, _, _ = orc.ls_redistance(phi_in, itf.ls_wid, itf.rdt, sp, rho_12=itf.rho_12,
+                                             btn=1)
+            _inner(now["phi"], shape)[...] = phi_in
+            orc.ns_bc(shape, G, now["phi"])
+        elif itf.redis_every and it % itf.redis_every == 0:
             phi_in = np.ascontiguousarray(_inner(now["phi"], shape))
             phi_in, _, _ = orc.ls_redistance(phi_in, itf.ls_wid, itf.rdt, sp, rho_12=itf.rho_12,
                                              btn=1)
@@ -76,8 +102,11 @@ def _oracle_run(case, st, ns, itf, steps):
             now["phi"], _ = orc.ns_mass_correct(shape, sp, G, now["phi"], itf.ls_wid, itf.rho_12,
                                                 imass, 2)
         derived(now)
-        rho_now = orc.rho_from_phi(np.ascontiguousarray(_inner(now["phi"], shape)),
-                                   itf.ls_wid, 1.0, itf.rho_12)
+        if itf.method == 3:
+            rho_now = np.ascontiguousarray(_inner(now["rho"], shape))
+        else:
+            rho_now = orc.rho_from_phi(np.ascontiguousarray(_inner(now["phi"], shape)),
+                                       itf.ls_wid, 1.0, itf.rho_12)
         oldf = {k: old[k] for k in orc.NS_OLD}
         out = orc.ns_ab_step(shape, sp, op, rho_now, tuple(now[k] for k in ("u", "v", "w")[:nc]),
                              oldf, tuple(old[k] for k in ("su", "sv", "sw")[:nc]), p, krylov=1)
@@ -88,7 +117,8 @@ def _oracle_run(case, st, ns, itf, steps):
     return now, p
 
 
-@pytest.mark.parametrize("shape,method", [((1, 32, 32), 1), ((1, 32, 32), 2), ((16, 16, 16), 2)])
+@pytest.mark.parametrize("shape,method", [((1, 32, 32), 1), ((1, 32, 32), 2), ((16, 16, 16), 2),
+                                          ((1, 32, 32), 3), ((16, 16, 16), 3)])
 def test_time_steps_match_the_oracle_sequence(cuda, shape, method):
     nz, ny, nx = shape
     ext = (1.0, ny / nx, (nz / nx) if nz > 1 else 1.0)
@@ -99,11 +129,12 @@ def test_time_steps_match_the_oracle_sequence(cuda, shape, method):
     ns = NSParams(dt=2e-3, re=100.0, fr=0.5, we=2.0, mu_12=1e-2, btn_sf=1.0, ghost=G,
                   gravity=(0.0, 0.0, -1.0) if nz > 1 else (0.0, -1.0, 0.0), p_tol=1e-12)
     itf = InterfaceParams(ls_wid=1.5 * h, rho_12=1e-3, rdt=0.25 * h, redis_every=2,
-                          method=method)
+                          method=method, recon_every=3)
     steps = 3
     want, p_or = _oracle_run(case, st, ns, itf, steps)
     with TwoPhaseStep(shape, case.spacing, ns, itf, precision="fp64", krylov=True) as ts:
-        ts.load(st["phi"], st["u"], st["v"], st["w"])
+        ts.load(st["phi"], st["u"], st["v"], st["w"],
+                vof=orc.heaviside(st["phi"], itf.ls_wid))
         for _ in range(steps):
             stats = ts.step()
         got = {k: (a.cpu().numpy() if a is not None else None) for k, a in ts.now.items()}
@@ -118,6 +149,8 @@ def test_time_steps_match_the_oracle_sequence(cuda, shape, method):
     np.testing.assert_allclose(got["curv"], want["curv"], rtol=0,
                                atol=1e-7 * np.abs(want["curv"]).max())
     np.testing.assert_allclose(p, p_or, rtol=0, atol=1e-6 * np.abs(p_or).max())
+    if method == 3:
+        np.testing.assert_allclose(got["vof"], want["vof"], rtol=0, atol=1e-10)
 
 
 @pytest.mark.parametrize("shape", [(1, 40, 48), (16, 16, 24)])
@@ -144,3 +177,30 @@ def test_mass_correction_matches_the_oracle(cuda, shape):
     assert mg == pytest.approx(mw, rel=1e-13)
     np.testing.assert_allclose(t.cpu().numpy(), want, rtol=0, atol=1e-13 * np.abs(want).max())
     np.testing.assert_array_equal(hostarr, t.cpu().numpy())
+
+
+@pytest.mark.parametrize("shape", [(1, 40, 48), (16, 16, 24)])
+def test_vof_transport_matches_the_oracle(cuda, shape):
+    import torch
+    from fortrancfd_gb300 import PressurePoisson, vof_wlic_solver
+    nz, ny, nx = shape
+    h = 1.0 / nx
+    ps = orc.padded_shape(shape, G)
+    grids = np.meshgrid(*[(np.arange(m) - G + 0.5) * h for m in ps], indexing="ij")
+    phi = 0.2 - np.sqrt(sum((a - 0.4) ** 2 for a in grids))
+    vof = orc.heaviside(phi, 1.5 * h)
+    rng = np.random.default_rng(4)
+    vel = [0.3 * rng.standard_normal(ps) for _ in range(3 if nz > 1 else 2)]
+    dt = 0.1 * h
+    want = orc.vof_wlic(shape, (h, h, h), G, vof, vof, *vel, *([None] if nz == 1 else []), phi, dt)
+    prm = NSParams(dt=dt, ghost=G)
+    with PressurePoisson(shape, (h, h, h)) as pp:
+        t = [torch.from_numpy(a).to(cuda) for a in [vof, vof] + vel + [phi]]
+        w = t[4] if nz > 1 else None
+        vof_wlic_solver(pp, prm, t[0], t[1], t[2], t[3], w, t[-1])
+        host = vof.copy()
+        vof_wlic_solver(pp, prm, host, vof, *vel, *([None] if nz == 1 else []), phi)
+    got = t[0].cpu().numpy()
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-13)
+    np.testing.assert_array_equal(host, got)
+    assert got.min() >= 0.0 and got.max() <= 1.0

@@ -97,3 +97,38 @@ def test_mass_correction_restores_the_initial_mass():
     _, m2 = orc.ns_mass_correct(shape, sp, g, fixed, 1.5 * h, 1e-3, 0.0, iterations=0)
     assert abs(m1 - m0) / m0 > 0.03
     assert abs(m2 - m0) / m0 < 2e-4
+
+
+def _disc(shape, g, h, c=(0.45, 0.5, 0.5), r=0.2):
+    ps = orc.padded_shape(shape, g)
+    grids = np.meshgrid(*[(np.arange(m) - g + 0.5) * h for m in ps], indexing="ij")
+    cen = c[:len(ps)][::-1]
+    phi = r - np.sqrt(sum((a - cc) ** 2 for a, cc in zip(grids, cen)))
+    vof = orc.heaviside(phi, 1.5 * h)
+    return phi, vof
+
+
+def test_vof_transport_conserves_and_moves_the_disc():
+    """vof_wlic_solver in a uniform x velocity (walls at rest, disc away from
+    them): the volume is conserved to round-off, vof stays in [0, 1] and the
+    centroid moves by u dt per step."""
+    g = 3
+    shape = (1, 48, 48)
+    h = 1 / 48
+    phi, vof = _disc(shape, g, h)
+    u = np.zeros_like(vof)
+    u[:, g:g + 47] = 0.5          # faces 1..47 of the reference (walls 0 and 48 at rest)
+    v = np.zeros_like(vof)
+    dt = 0.2 * h / 0.5
+    x = (np.arange(vof.shape[1]) - g + 0.5) * h
+    inner = (slice(g, g + 48), slice(g, g + 48))
+    vol0 = vof[inner].sum()
+    cx0 = (vof[inner] * x[None, g:g + 48]).sum() / vol0
+    cur = vof
+    for _ in range(10):
+        cur = orc.vof_wlic((1, 48, 48), (h, h, 1.0), g, cur, cur, u, v, None, phi, dt)
+    vol = cur[inner].sum()
+    cx = (cur[inner] * x[None, g:g + 48]).sum() / vol
+    assert abs(vol - vol0) / vol0 < 1e-12
+    assert cur.min() >= 0.0 and cur.max() <= 1.0
+    assert cx - cx0 == pytest.approx(10 * 0.5 * dt, rel=0.02)
