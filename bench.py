@@ -783,6 +783,11 @@ def run_ours(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        # replicas time the headline solve only: the single-GPU sections (and
+        # their CPU oracle legs, which would share the host cores) stay at N=1
+        for k in ("no_adjoint", "no_multi", "no_rollout", "no_levelset", "no_momentum",
+                  "no_timestep"):
+            setattr(args, k, True)
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     case = inputs.config(args.config, args.scale)
