@@ -14,7 +14,7 @@ two-phase time step over those (timestep.py) and the seeded synthetic inputs
 from .ppe import ConvergenceError, GBMGError, PressurePoisson  # noqa: F401
 from .levelset import LevelSet, node_velocity  # noqa: F401
 from .momentum import (NSParams, bc, curv, ls_mv, mass_preserving_level_set,  # noqa: F401
-                       ns_ab_predictor, ns_ab_solver, rho_mu, velbc, vof_wlic_solver)
+                       ns_ab_predictor, ns_ab_solver, rho_mu, velbc, vof_wlic_solver, ibm_bc)
 from .timestep import InterfaceParams, TwoPhaseStep  # noqa: F401
 
 try:  # torch.ops.gbmg.solve (torch is optional for host-memory use)
@@ -24,6 +24,6 @@ except ImportError:  # pragma: no cover
 
 __all__ = ["PressurePoisson", "LevelSet", "node_velocity", "NSParams", "ns_ab_solver",
            "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc", "mass_preserving_level_set", "ls_mv",
-           "vof_wlic_solver",
+           "vof_wlic_solver", "ibm_bc",
            "TwoPhaseStep", "InterfaceParams",
            "ConvergenceError", "GBMGError"]

@@ -34,7 +34,7 @@ EXPORTS = (
     "gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
     "gbmg_ls_kernel_launches", "gbmg_ls_last_error",
     "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc", "gbmg_ns_curvature",
-    "gbmg_ns_rho_mu", "gbmg_ns_bc", "gbmg_ns_mass_correct", "gbmg_ns_vof_advect",
+    "gbmg_ns_rho_mu", "gbmg_ns_bc", "gbmg_ns_mass_correct", "gbmg_ns_vof_advect", "gbmg_ns_ibm",
 )
 
 PROF_CLASSES = ("smooth_fine", "smooth_coarse", "restrict_fine", "restrict_coarse",
@@ -165,10 +165,11 @@ def load(build_if_missing: bool = True):
                                            C.c_double, C.c_int, C.c_int, P(C.c_double)]
         L.gbmg_ns_vof_advect.argtypes = [H, P(NSParams), Field, Field, Field, Field, Field, Field,
                                          C.c_int]
+        L.gbmg_ns_ibm.argtypes = [H, P(NSParams), Field, C.c_double, Field, Field, Field, C.c_int]
         for name in ("gbmg_ls_create", "gbmg_ls_destroy", "gbmg_ls_advect", "gbmg_ls_redistance",
                      "gbmg_ns_ab_step", "gbmg_ns_ab_predict", "gbmg_ns_velbc",
                      "gbmg_ns_curvature", "gbmg_ns_rho_mu", "gbmg_ns_bc",
-                     "gbmg_ns_mass_correct", "gbmg_ns_vof_advect"):
+                     "gbmg_ns_mass_correct", "gbmg_ns_vof_advect", "gbmg_ns_ibm"):
             getattr(L, name).restype = C.c_int
         for name in ("gbmg_create", "gbmg_destroy", "gbmg_set_rho", "gbmg_set_phi",
                      "gbmg_set_coef", "gbmg_solve", "gbmg_project", "gbmg_divergence",

@@ -2376,6 +2376,27 @@ int gbmg_ns_vof_advect(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field vof
   return GBMG_OK;
 }
 
+int gbmg_ns_ibm(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field solid, double w_body,
+                gbmg_field u, gbmg_field v, gbmg_field w, int mem) {
+  GB_TRY(begin(h));
+  const bool three = h->grid.nz > 1;
+  gbmg_ns_fields f{};
+  f.rho = solid; f.u = u; f.v = v; f.w = w;
+  const int slots[4] = {kNsRho, kNsU, kNsV, kNsW};
+  const bool outs[4] = {true, true, true, true};
+  NsPlan P;
+  bool out[kNsFields];
+  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, three ? 4 : 3, &P, out));
+  double* arr[4] = {P.base[kNsRho], nullptr, nullptr, nullptr};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));  // bc(solid)
+  double* vel[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_ibm(h->stream, P.a, P.base[kNsRho], w_body, vel));
+  GB_TRY(check_launch(h, "ibm"));
+  GB_TRY(ns_finish(h, &f, mem, P, out));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  return GBMG_OK;
+}
+
 int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n) {
   GB_TRY(begin(h));
   prof_flush(h);

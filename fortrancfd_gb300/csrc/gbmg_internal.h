@@ -345,6 +345,9 @@ void launch_ns_advance(cudaStream_t s, const NsArgs& a, const double* const old[
                        const double* const src_old[3], double* const src[3],
                        double* const now[3]);
 void launch_velbc(cudaStream_t s, const NsArgs& a, const NsBc& bc, double* const vel[3]);
+// ibm_bc's velocity forcing by the solid fraction (arrays at element (1,1,1))
+void launch_ns_ibm(cudaStream_t s, const NsArgs& a, const double* solid, double w_body,
+                   double* const vel[3]);
 // ls_funs + rho_mu over the padded box (null outputs skipped)
 void launch_ns_rho_mu(cudaStream_t s, const NsArgs& a, const double* phi, double ls_wid,
                       double rho_12, double* rho, double* mu, double* delta);

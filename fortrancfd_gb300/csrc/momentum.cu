@@ -396,6 +396,28 @@ __global__ void __launch_bounds__(256) k_ns_rho_mu(NsArgs a, const double* __res
   if (delta) delta[q] = hp;
 }
 
+// ibm_bc's forcing ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/
+// ns_solvers.f90:150-211") on the interior faces: with s the face average of
+// the cell solid fraction, u = (1 - s) u, v = (1 - s) v (2D: the last
+// component takes the body velocity), w = (1 - s) w + s w_body.
+template <bool kThree>
+__global__ void __launch_bounds__(kNsBx * kNsBy)
+    k_ns_ibm(NsArgs a, const double* __restrict__ S, double w_body, double* U, double* V,
+             double* W) {
+  const int i = blockIdx.x * kNsBx + threadIdx.x + 1;
+  const int j = blockIdx.y * kNsBy + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (i > a.nx || j > a.ny) return;
+  const int64_t q = ns_at(a, i, j, k);
+  double s = 0.5 * (S[q] + S[q + 1]);
+  U[q] = (1.0 - s) * U[q];
+  s = 0.5 * (S[q] + S[q + a.sy]);
+  V[q] = kThree ? (1.0 - s) * V[q] : (1.0 - s) * V[q] + s * w_body;
+  if (!kThree) return;
+  s = 0.5 * (S[q] + S[q + a.sz]);
+  W[q] = (1.0 - s) * W[q] + s * w_body;
+}
+
 dim3 ns_grid(const NsArgs& a) {
   return dim3((unsigned)((a.nx + kNsBx - 1) / kNsBx), (unsigned)((a.ny + kNsBy - 1) / kNsBy),
               (unsigned)a.nz);
@@ -461,6 +483,15 @@ void launch_ns_rho_mu(cudaStream_t s, const NsArgs& a, const double* phi, double
   const dim3 grid((unsigned)((a.nx + 2 * a.g + 31) / 32), (unsigned)((a.ny + 2 * a.g + 7) / 8),
                   (unsigned)(a.nz > 1 ? a.nz + 2 * a.g : 1));
   k_ns_rho_mu<<<grid, block, 0, s>>>(a, phi, ls_wid, rho_12, rho, mu, delta);
+}
+
+void launch_ns_ibm(cudaStream_t s, const NsArgs& a, const double* solid, double w_body,
+                   double* const vel[3]) {
+  const dim3 block(kNsBx, kNsBy);
+  if (a.nz > 1)
+    k_ns_ibm<true><<<ns_grid(a), block, 0, s>>>(a, solid, w_body, vel[0], vel[1], vel[2]);
+  else
+    k_ns_ibm<false><<<ns_grid(a), block, 0, s>>>(a, solid, w_body, vel[0], vel[1], nullptr);
 }
 
 }  // namespace gbmg

@@ -262,12 +262,25 @@ def vof_wlic_solver(pp, prm: NSParams, vof, vof_old, u_old, v_old, w_old, phi):
               "vof_wlic_solver")
 
 
+def ibm_bc(pp, prm: NSParams, solid, u, v, w=None, w_body=0.0):
+    """ibm_bc's forcing: bc on the padded solid fraction, then u, v (, w)
+    scaled by (1 - face solid fraction), w (2D: v) plus s w_body; in place."""
+    three = pp.shape[0] > 1
+    fs = [_padded_field(a, n, pp.shape, prm.ghost)
+          for n, a in (("phi", solid), ("u", u), ("v", v), ("w", w if three else None))]
+    m = _one_memory(*fs)
+    _sync({"s": solid, "u": u, "v": v, "w": w})
+    c = prm.c_struct()
+    pp._check(pp._L.gbmg_ns_ibm(pp._h, C.byref(c), fs[0][0], float(w_body), fs[1][0], fs[2][0],
+                                fs[3][0], m), "ibm_bc")
+
+
 def ls_mv(pp, prm: NSParams, phi, ls_wid, rho_12):
     """ls_mv's mass sum (H + rho_12 (1 - H)) H dv of a padded phi."""
     return mass_preserving_level_set(pp, prm, phi, ls_wid, rho_12, 0.0, iterations=0)
 
 
 __all__ = ["NSParams", "ns_ab_solver", "ns_ab_predictor", "velbc", "curv", "rho_mu", "bc",
-           "mass_preserving_level_set", "ls_mv", "vof_wlic_solver",
+           "mass_preserving_level_set", "ls_mv", "vof_wlic_solver", "ibm_bc",
            "padded_shape",
            "ConvergenceError", "GBMGError"]

@@ -320,6 +320,16 @@ module gbmg
       integer(c_int), value :: mem
     end function
 
+    integer(c_int) function gbmg_ns_ibm(h, prm, solid, w_body, u, v, w, mem) &
+        bind(c, name="gbmg_ns_ibm")
+      import :: c_int, c_ptr, c_double, gbmg_ns_params, gbmg_field
+      type(c_ptr), value :: h
+      type(gbmg_ns_params), intent(in) :: prm
+      type(gbmg_field), value :: solid, u, v, w
+      real(c_double), value :: w_body
+      integer(c_int), value :: mem
+    end function
+
     integer(c_int) function gbmg_ns_bc(h, prm, a, mem) bind(c, name="gbmg_ns_bc")
       import :: c_int, c_ptr, gbmg_ns_params, gbmg_field
       type(c_ptr), value :: h

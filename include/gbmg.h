@@ -346,6 +346,16 @@ int gbmg_ns_vof_advect(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field vof
                        gbmg_field vof_old, gbmg_field u_old, gbmg_field v_old, gbmg_field w_old,
                        gbmg_field phi, int mem);
 
+/* ibm_bc's forcing ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/
+ * ns_solvers.f90:150-211"), after ns_check_convergence_div: bc on the padded
+ * cell solid fraction (in place), then on the interior faces, with s the face
+ * average of the solid fraction, u = (1 - s) u, v = (1 - s) v and
+ * w = (1 - s) w + s w_body (the body's vertical speed; in 2D v takes it).
+ * The reference samples one gate geometry into the solid fraction; here the
+ * caller supplies the field.  Ghost faces are not touched, as there. */
+int gbmg_ns_ibm(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field solid, double w_body,
+                gbmg_field u, gbmg_field v, gbmg_field w, int mem);
+
 /* bc ("Two phase flows/newOpenMP/2D/src/others/bcs.f90:1-26"): zero-gradient
  * ghost layers of one padded cell array, in place. */
 int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem);

@@ -2093,3 +2093,27 @@ void or_vof_wlic(const or_grid* gr, int g, double* vof, const double* vof_old, c
   }
   free(flux);
 }
+
+/* ibm_bc's forcing (NO3 src/ns_solver/ns_solvers.f90:150-211) with a given
+ * solid fraction: bc(solid), then u = (1 - s) u, v = (1 - s) v,
+ * w = (1 - s) w + s w_body on the interior faces (s the face average; in 2D
+ * v takes the body velocity). */
+void or_ns_ibm(const or_grid* gr, int g, double* S, double w_body, double* U, double* V,
+               double* W) {
+  const ns_box b = ns_box_of(gr, g);
+  const int three = gr->nz > 1;
+  or_ns_bc(gr, g, S);
+  const size_t sy = b.px, sz = b.px * b.py;
+  for (int k = 1; k <= gr->nz; ++k)
+    for (int j = 1; j <= gr->ny; ++j)
+      for (int i = 1; i <= gr->nx; ++i) {
+        const size_t q = NI(&b, i, j, k);
+        double s = 0.5 * (S[q] + S[q + 1]);
+        U[q] = (1.0 - s) * U[q];
+        s = 0.5 * (S[q] + S[q + sy]);
+        V[q] = three ? (1.0 - s) * V[q] : (1.0 - s) * V[q] + s * w_body;
+        if (!three) continue;
+        s = 0.5 * (S[q] + S[q + sz]);
+        W[q] = (1.0 - s) * W[q] + s * w_body;
+      }
+}

@@ -105,6 +105,7 @@ def lib():
                                          C.c_int]
         L.or_ns_mass_correct.restype = C.c_double
         L.or_vof_wlic.argtypes = [_G, C.c_int, _D, _D, _D, _D, _D, _D, C.c_double]
+        L.or_ns_ibm.argtypes = [_G, C.c_int, _D, C.c_double, _D, _D, _D]
         L.or_num_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -488,3 +489,13 @@ def vof_wlic(shape, spacing, ghost, vof, vof_old, u, v, w, phi, dt):
                          ("w", w if _three(shape) else None), ("phi", phi))]
     lib().or_vof_wlic(C.byref(g), int(ghost), _p(out), *[_p(a) for a in args], float(dt))
     return out
+
+
+def ns_ibm(shape, ghost, solid, w_body, u, v, w=None):
+    """ibm_bc's forcing in place on padded arrays (solid gets its bc)."""
+    g = grid(shape, (1.0, 1.0, 1.0))
+    arrs = [solid, u, v] + ([w] if _three(shape) else [])
+    for a in arrs:
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+    lib().or_ns_ibm(C.byref(g), int(ghost), _p(solid), float(w_body), _p(u), _p(v),
+                    _p(w) if _three(shape) else None)

@@ -255,3 +255,25 @@ def test_host_and_device_steps_agree(cuda):
     for k in ("u", "v", "su", "sv", "p"):
         assert np.array_equal(_bits(s_host[k]), _bits(s_dev[k].cpu().numpy())), k
     assert a["linf"] == b["linf"] and a["cycles"] == b["cycles"]
+
+
+@pytest.mark.parametrize("shape", [(1, 16, 24), (8, 12, 16)])
+def test_ibm_forcing_matches_oracle_bitwise(cuda, shape):
+    import torch
+    from fortrancfd_gb300 import ibm_bc
+    rng = np.random.default_rng(6)
+    ps = orc.padded_shape(shape, G)
+    three = shape[0] > 1
+    solid = np.clip(rng.uniform(-0.5, 1.5, ps), 0.0, 1.0)
+    vel = [rng.standard_normal(ps) for _ in range(3 if three else 2)]
+    want_s, want = solid.copy(), [a.copy() for a in vel]
+    orc.ns_ibm(shape, G, want_s, 0.3, *want)
+    prm = NSParams(dt=1.0, ghost=G)
+    with PressurePoisson(shape, (0.1, 0.1, 0.1)) as pp:
+        t = [torch.from_numpy(a).to(cuda) for a in [solid] + vel]
+        ibm_bc(pp, prm, t[0], t[1], t[2], t[3] if three else None, w_body=0.3)
+        h = [a.copy() for a in [solid] + vel]
+        ibm_bc(pp, prm, h[0], h[1], h[2], h[3] if three else None, w_body=0.3)
+    for c, a in enumerate([want_s] + want):
+        assert np.array_equal(_bits(t[c].cpu().numpy()), _bits(a)), c
+        assert np.array_equal(_bits(h[c]), _bits(a)), c
