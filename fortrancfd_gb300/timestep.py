@@ -24,8 +24,8 @@ memory, the switch copies and the cell average of node_vel.
 from dataclasses import dataclass
 
 from .levelset import LevelSet, node_velocity
-from .momentum import (NSParams, bc, curv, ls_mv, mass_preserving_level_set, ns_ab_solver,
-                       padded_shape, rho_mu, vof_wlic_solver)
+from .momentum import (NSParams, bc, curv, ibm_bc, ls_mv, mass_preserving_level_set,
+                       ns_ab_solver, padded_shape, rho_mu, vof_wlic_solver)
 from .ppe import PressurePoisson
 
 try:
@@ -152,8 +152,10 @@ class TwoPhaseStep:
         self.nvel = tuple(x.contiguous() if x is not None else None for x in (un, vn, wn))
 
     # -- one time step -----------------------------------------------------------
-    def step(self):
-        """One time step; returns its statistics (momentum step, divergence)."""
+    def step(self, solid=None, w_body=0.0):
+        """One time step; returns its statistics (momentum step, divergence).
+        solid: a padded cell solid fraction for the 3D solver's immersed
+        boundary (ibm_bc after the divergence check), w_body its vertical speed."""
         self.iter += 1
         ns, itf = self.ns, self.itf
         # p%switch
@@ -198,6 +200,8 @@ class TwoPhaseStep:
         u, v = self._faces(n["u"], 0), self._faces(n["v"], 1)
         w = self._faces(n["w"], 2) if self.three else None
         div_max, div_mean = self.pp.div_stats(u, v, w)
+        if solid is not None:
+            ibm_bc(self.pp, ns, solid, n["u"], n["v"], n["w"], w_body=w_body)
         self._node_vel()
         self.stats = dict(st, div_max=div_max, div_mean=div_mean, redistance_iterations=redis,
                           iter=self.iter, mass=self.mass)
