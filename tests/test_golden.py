@@ -72,3 +72,41 @@ def test_gpu_reproduces_fixture(cuda, name, precision):
         assert rel_l2(p, fx["p"]) <= 1e-8
     for a, key in ((u, "u_abs"), (v, "v_abs"), (w, "w_abs")):
         assert np.abs(a).sum() == pytest.approx(float(fx[key]), rel=1e-8)
+
+
+def _momentum_fixture():
+    return np.load(os.path.join(HERE, "momentum2d_12x10.npz"))
+
+
+def _momentum_state(f):
+    st = {k[3:]: f[k] for k in f.files if k.startswith("in_")}
+    st["w"] = st["nrm_z"] = None
+    return st
+
+
+def test_momentum_oracle_equals_the_golden_loops():
+    """The oracle's predictor pass and CCD gradient equal the stored outputs
+    of the literal loop restatement bit for bit (curvature: its pow)."""
+    from oracle import oracle as orc
+    f = _momentum_fixture()
+    g = int(f["ghost"])
+    shape = tuple(int(x) for x in f["shape"])
+    sp = tuple(float(x) for x in f["spacing"])
+    st = _momentum_state(f)
+    prm = orc.ns_params(ghost=g, bc=tuple(int(b) for b in f["prm_bc"]) + (1, 1),
+                        dt=float(f["prm_dt"]), re=float(f["prm_re"]), fr=float(f["prm_fr"]),
+                        we=float(f["prm_we"]), mu_12=float(f["prm_mu_12"]),
+                        gravity=(float(f["prm_gx"]), float(f["prm_gy"]), 0.0),
+                        btn_g=float(f["prm_btn_g"]), btn_sf=float(f["prm_btn_sf"]))
+    dif = orc.ns_diffusion(shape, sp, prm, st)[:2]
+    old = (st["u"], st["v"])
+    src, vel = orc.ns_advance(shape, sp, prm, old, old, dif, (st["su_old"], st["sv_old"]))
+    u, v = vel[0].copy(), vel[1].copy()
+    orc.velbc(shape, prm, u, v)
+    bits = lambda a: np.ascontiguousarray(a).view(np.int64)  # noqa: E731
+    for got, key in ((src[0], "su"), (src[1], "sv"), (u, "u_new"), (v, "v_new")):
+        assert np.array_equal(bits(got), bits(f[key])), key
+    fx, fy, _, cv = orc.ns_curvature(shape, sp, g, st["phi"])
+    assert np.array_equal(bits(fx), bits(f["ccd_fx"]))
+    assert np.array_equal(bits(fy), bits(f["ccd_fy"]))
+    np.testing.assert_allclose(cv, f["ccd_curv"], rtol=1e-15, atol=0)
