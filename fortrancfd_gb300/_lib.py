@@ -70,6 +70,7 @@ class Field(C.Structure):
 
 class NSParams(C.Structure):
     _fields_ = [("ghost", C.c_int32), ("bc", C.c_int32 * 6), ("iterations", C.c_int32),
+                ("adv_scheme", C.c_int32),
                 ("dt", C.c_double), ("re", C.c_double), ("fr", C.c_double), ("we", C.c_double),
                 ("mu_12", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
                 ("gz", C.c_double), ("btn_g", C.c_double), ("btn_sf", C.c_double),

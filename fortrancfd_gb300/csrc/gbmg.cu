@@ -1455,6 +1455,11 @@ int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* 
   }
   // GBMG_NS_DIVIDE=1: IEEE divisions throughout (the same doubles, slower)
   if (const char* e = std::getenv("GBMG_NS_DIVIDE")) a.fast = a.fast && std::atoi(e) == 0;
+  a.scheme = prm->adv_scheme;
+  if (a.scheme != 0 && a.scheme != 1) {
+    h->err = "adv_scheme must be 0 (second-order upwind) or 1 (QUICK)";
+    return GBMG_INVALID_ARG;
+  }
   a.gterm[0] = prm->gx * prm->btn_g / prm->fr;
   a.gterm[1] = prm->gy * prm->btn_g / prm->fr;
   a.gterm[2] = prm->gz * prm->btn_g / prm->fr;

@@ -332,6 +332,7 @@ struct NsArgs {
   double rdx, rdy, rdz, rdx2, rdy2, rdz2, rre;
   double gterm[3];
   int fast;
+  int scheme;  // momentum advection: 0 second-order upwind, 1 QUICK
 };
 struct NsBc {
   int b[6];  // velbc type of the walls x-, x+, y-, y+, z-, z+ (1 no-slip, 2 slip, else none)

@@ -208,6 +208,35 @@ __device__ __forceinline__ double ns_adv(const NsArgs& A, const double* __restri
   return src;
 }
 
+// ns_ab_adv_source_quick: -(sum over axes d of ah_d (s_d(q) - s_d(q - e_d))/h_d),
+// s_d the QUICK face value along d from the old velocity f, chosen upwind by
+// ah_d = the average of the advecting velocity T_d over q and q + e_c.
+template <bool kThree>
+__device__ __forceinline__ double ns_adv_quick(const NsArgs& A, const double* __restrict__ f,
+                                               int64_t q, int64_t ec,
+                                               const double* const (&T)[3]) {
+  const int64_t st[3] = {1, A.sy, A.sz};
+  const double h[3] = {A.dx, A.dy, A.dz};
+  const double rh[3] = {A.rdx, A.rdy, A.rdz};
+  double src = 0.0;
+#pragma unroll
+  for (int d = 0; d < (kThree ? 3 : 2); ++d) {
+    const int64_t s = st[d];
+    double sv[2], ah = 0.0;
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      const int64_t pq = m == 0 ? q - s : q;
+      const double av = 0.5 * (T[d][pq] + T[d][pq + ec]);
+      sv[m] = av >= 0.0 ? ((-f[pq - s] + 6.0 * f[pq]) + 3.0 * f[pq + s]) / 8.0
+                        : ((-f[pq + 2 * s] + 6.0 * f[pq + s]) + 3.0 * f[pq]) / 8.0;
+      if (m == 1) ah = av;
+    }
+    const double term = cdiv(A, ah * (sv[1] - sv[0]), h[d], rh[d]);
+    src = d == 0 ? -term : src - term;
+  }
+  return src;
+}
+
 template <bool kThree>
 __global__ void __launch_bounds__(kNsBx * kNsBy)
     k_ns_advance(NsArgs a, const double* __restrict__ U, const double* __restrict__ V,
@@ -230,14 +259,17 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   c[0] = Ut[q];
   c[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sx]) + Vt[q + sx - sy]);
   c[2] = kThree ? 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sx]) + Wt[q + sx - sz]) : 0.0;
-  src = ns_adv<kThree>(a, U, q, c) + TU[q];
+  const double* const Tq[3] = {Ut, Vt, Wt};
+  src = (a.scheme == 1 ? ns_adv_quick<kThree>(a, U, q, sx, Tq) : ns_adv<kThree>(a, U, q, c)) +
+        TU[q];
   SU[q] = src;
   Un[q] = U[q] + dt * (1.5 * src - 0.5 * SUo[q]);
   // y: v at (i, j+1/2, k)
   c[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sy]) + Ut[q - sx + sy]);
   c[1] = Vt[q];
   c[2] = kThree ? 0.25 * (((Wt[q] + Wt[q - sz]) + Wt[q + sy]) + Wt[q + sy - sz]) : 0.0;
-  src = ns_adv<kThree>(a, V, q, c) + TV[q];
+  src = (a.scheme == 1 ? ns_adv_quick<kThree>(a, V, q, sy, Tq) : ns_adv<kThree>(a, V, q, c)) +
+        TV[q];
   SV[q] = src;
   Vn[q] = V[q] + dt * (1.5 * src - 0.5 * SVo[q]);
   if (!kThree) return;
@@ -245,7 +277,8 @@ __global__ void __launch_bounds__(kNsBx * kNsBy)
   c[0] = 0.25 * (((Ut[q] + Ut[q - sx]) + Ut[q + sz]) + Ut[q - sx + sz]);
   c[1] = 0.25 * (((Vt[q] + Vt[q - sy]) + Vt[q + sz]) + Vt[q - sy + sz]);
   c[2] = Wt[q];
-  src = ns_adv<kThree>(a, W, q, c) + TW[q];
+  src = (a.scheme == 1 ? ns_adv_quick<kThree>(a, W, q, sz, Tq) : ns_adv<kThree>(a, W, q, c)) +
+        TW[q];
   SW[q] = src;
   Wn[q] = W[q] + dt * (1.5 * src - 0.5 * SWo[q]);
 }

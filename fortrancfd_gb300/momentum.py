@@ -57,10 +57,12 @@ class NSParams:
     bc: tuple = (1, 1, 1, 1, 1, 1)   # ubc(1:2), vbc(1:2), wbc(1:2): 1 no-slip, 2 slip
     iterations: int = 4
     p_tol: float = 1e-10
+    adv_scheme: int = 0   # 0 second-order upwind (the reference's choice), 1 QUICK
 
     def c_struct(self):
         return _lib.NSParams(int(self.ghost), (C.c_int32 * 6)(*[int(b) for b in self.bc]),
-                             int(self.iterations), float(self.dt), float(self.re), float(self.fr),
+                             int(self.iterations), int(self.adv_scheme), float(self.dt),
+                             float(self.re), float(self.fr),
                              float(self.we), float(self.mu_12), float(self.gravity[0]),
                              float(self.gravity[1]), float(self.gravity[2]), float(self.btn_g),
                              float(self.btn_sf), float(self.p_tol))

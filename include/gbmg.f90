@@ -45,6 +45,7 @@ module gbmg
     integer(c_int32_t) :: ghost
     integer(c_int32_t) :: bc(6)        ! ubc(1:2), vbc(1:2), wbc(1:2)
     integer(c_int32_t) :: iterations
+    integer(c_int32_t) :: adv_scheme   ! 0 second-order upwind, 1 QUICK
     real(c_double)     :: dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf, p_tol
   end type
 

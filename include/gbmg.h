@@ -252,6 +252,8 @@ typedef struct {
   int32_t ghost;       /* ghost layers of every array (the reference's ghc) */
   int32_t bc[6];       /* velbc of the walls x-, x+, y-, y+, z-, z+: ubc(1:2), vbc(1:2), wbc(1:2) */
   int32_t iterations;  /* predictor-projection passes */
+  int32_t adv_scheme;  /* momentum advection: 0 second-order upwind (ns_ab_adv_source_sec, the
+                          reference's active choice), 1 QUICK (ns_ab_adv_source_quick) */
   double dt;
   double re, fr, we;   /* Reynolds, Froude and Weber numbers */
   double mu_12;        /* viscosity ratio */

@@ -1328,6 +1328,7 @@ typedef struct {
   int32_t ghost;       /* g, >= 2 */
   int32_t bc[6];       /* velbc: ubc(1), ubc(2), vbc(1), vbc(2), wbc(1), wbc(2) */
   int32_t iterations;  /* predictor-projection passes (the reference: 4) */
+  int32_t adv_scheme;  /* 0 second-order upwind (ns_ab_adv_source_sec), 1 QUICK */
   double dt, re, fr, we, mu_12, gx, gy, gz, btn_g, btn_sf, p_tol;
 } or_ns_params;
 
@@ -1523,12 +1524,31 @@ void or_ns_advance(const or_grid* gr, const or_ns_params* prm, const double* U, 
           const size_t st[3] = {sx, sy, sz};
           const double h[3] = {dx, dy, dz};
           double src = 0.0;
-          for (int d = 0; d < (three ? 3 : 2); ++d) {
-            const size_t s = st[d];
-            const double fp = 0.5 * ((-f[q + 2 * s] + 4.0 * f[q + s]) - 3.0 * f[q]) / h[d];
-            const double fm = 0.5 * ((f[q - 2 * s] - 4.0 * f[q - s]) + 3.0 * f[q]) / h[d];
-            const double term = ns_upwind(a[d], fm, fp) / 2.0;
-            src = d == 0 ? -term : src - term;
+          if (prm->adv_scheme == 1) {
+            /* ns_ab_adv_source_quick (NO2 ns_ab_adv.f90:44-114, NO3 :75-199) */
+            const double* Tv[3] = {Ut, Vt, Wt};
+            const size_t ec = st[c];
+            for (int d = 0; d < (three ? 3 : 2); ++d) {
+              const size_t s = st[d];
+              double sv[2], ah = 0.0;
+              for (int m = 0; m < 2; ++m) { /* positions q - e_d (m = 0) and q (m = 1) */
+                const size_t pq = m == 0 ? q - s : q;
+                const double av = 0.5 * (Tv[d][pq] + Tv[d][pq + ec]);
+                sv[m] = av >= 0.0 ? ((-f[pq - s] + 6.0 * f[pq]) + 3.0 * f[pq + s]) / 8.0
+                                  : ((-f[pq + 2 * s] + 6.0 * f[pq + s]) + 3.0 * f[pq]) / 8.0;
+                if (m == 1) ah = av;
+              }
+              const double term = ah * (sv[1] - sv[0]) / h[d];
+              src = d == 0 ? -term : src - term;
+            }
+          } else {
+            for (int d = 0; d < (three ? 3 : 2); ++d) {
+              const size_t s = st[d];
+              const double fp = 0.5 * ((-f[q + 2 * s] + 4.0 * f[q + s]) - 3.0 * f[q]) / h[d];
+              const double fm = 0.5 * ((f[q - 2 * s] - 4.0 * f[q - s]) + 3.0 * f[q]) / h[d];
+              const double term = ns_upwind(a[d], fm, fp) / 2.0;
+              src = d == 0 ? -term : src - term;
+            }
           }
           src = src + T[c][q];
           S[c][q] = src;

@@ -39,7 +39,7 @@ class MGStats(C.Structure):
 
 class NSParams(C.Structure):
     _fields_ = [("ghost", C.c_int32), ("bc", C.c_int32 * 6), ("iterations", C.c_int32),
-                ("dt", C.c_double), ("re", C.c_double), ("fr", C.c_double), ("we", C.c_double),
+                ("adv_scheme", C.c_int32), ("dt", C.c_double), ("re", C.c_double), ("fr", C.c_double), ("we", C.c_double),
                 ("mu_12", C.c_double), ("gx", C.c_double), ("gy", C.c_double),
                 ("gz", C.c_double), ("btn_g", C.c_double), ("btn_sf", C.c_double),
                 ("p_tol", C.c_double)]
@@ -337,9 +337,10 @@ NS_OLD = ("u", "v", "w", "rho", "mu", "delta", "phi", "nrm_x", "nrm_y", "nrm_z",
 
 
 def ns_params(ghost=3, bc=(1, 1, 1, 1, 1, 1), iterations=4, dt=1e-3, re=1000.0, fr=1.0, we=1.0,
-              mu_12=1e-2, gravity=(0.0, -1.0, 0.0), btn_g=1.0, btn_sf=0.0, p_tol=1e-10):
+              mu_12=1e-2, gravity=(0.0, -1.0, 0.0), btn_g=1.0, btn_sf=0.0, p_tol=1e-10,
+              adv_scheme=0):
     return NSParams(int(ghost), (C.c_int32 * 6)(*[int(b) for b in bc]), int(iterations),
-                    float(dt), float(re), float(fr), float(we), float(mu_12),
+                    int(adv_scheme), float(dt), float(re), float(fr), float(we), float(mu_12),
                     float(gravity[0]), float(gravity[1]), float(gravity[2]), float(btn_g),
                     float(btn_sf), float(p_tol))
 

@@ -1192,3 +1192,43 @@ def curv(phi, g, dx, dy, dz=None):
     del inner
     _bc_copy(cv)
     return fx, fy, fz, cv
+
+
+def ns_ab_adv_source_quick_2d(uo, vo, ut, vt, g, nx, ny, dx, dy):
+    """ns_ab_adv_source_quick, 2D ("Two phase flows/newOpenMP/2D/src/ns_solver/
+    ns_ab_adv.f90:44-114"), literally: returns velsrc%now (x, y)."""
+    U, V, UT, VT = R(uo, g), R(vo, g), R(ut, g), R(vt, g)
+    xs1, xs2, ys1, ys2 = {}, {}, {}, {}
+    for j in range(0, ny + 1):
+        for i in range(0, nx + 1):
+            uh = 0.5 * (UT[i, j] + UT[i + 1, j])
+            vh = 0.5 * (VT[i, j] + VT[i + 1, j])
+            if uh >= 0.0:
+                xs1[i, j] = (-U[i - 1, j] + 6.0 * U[i, j] + 3.0 * U[i + 1, j]) / 8.0
+            else:
+                xs1[i, j] = (-U[i + 2, j] + 6.0 * U[i + 1, j] + 3.0 * U[i, j]) / 8.0
+            if vh >= 0.0:
+                xs2[i, j] = (-U[i, j - 1] + 6.0 * U[i, j] + 3.0 * U[i, j + 1]) / 8.0
+            else:
+                xs2[i, j] = (-U[i, j + 2] + 6.0 * U[i, j + 1] + 3.0 * U[i, j]) / 8.0
+            uh = 0.5 * (UT[i, j] + UT[i, j + 1])
+            vh = 0.5 * (VT[i, j] + VT[i, j + 1])
+            if uh >= 0.0:
+                ys1[i, j] = (-V[i - 1, j] + 6.0 * V[i, j] + 3.0 * V[i + 1, j]) / 8.0
+            else:
+                ys1[i, j] = (-V[i + 2, j] + 6.0 * V[i + 1, j] + 3.0 * V[i, j]) / 8.0
+            if vh >= 0.0:
+                ys2[i, j] = (-V[i, j - 1] + 6.0 * V[i, j] + 3.0 * V[i, j + 1]) / 8.0
+            else:
+                ys2[i, j] = (-V[i, j + 2] + 6.0 * V[i, j + 1] + 3.0 * V[i, j]) / 8.0
+    sx, sy = np.zeros_like(uo), np.zeros_like(vo)
+    SX, SY = R(sx, g), R(sy, g)
+    for j in range(1, ny + 1):
+        for i in range(1, nx + 1):
+            uh = 0.5 * (UT[i, j] + UT[i + 1, j])
+            vh = 0.5 * (VT[i, j] + VT[i + 1, j])
+            SX[i, j] = - uh * (xs1[i, j] - xs1[i - 1, j]) / dx - vh * (xs2[i, j] - xs2[i, j - 1]) / dy
+            uh = 0.5 * (UT[i, j] + UT[i, j + 1])
+            vh = 0.5 * (VT[i, j] + VT[i, j + 1])
+            SY[i, j] = - uh * (ys1[i, j] - ys1[i - 1, j]) / dx - vh * (ys2[i, j] - ys2[i, j - 1]) / dy
+    return sx, sy

@@ -38,7 +38,8 @@ def _setup(shape, seed=11, extent=None, sf=1.0, noise=0.01):
 def _oprm(prm):
     return orc.ns_params(ghost=prm.ghost, bc=prm.bc, iterations=prm.iterations, dt=prm.dt,
                          re=prm.re, fr=prm.fr, we=prm.we, mu_12=prm.mu_12, gravity=prm.gravity,
-                         btn_g=prm.btn_g, btn_sf=prm.btn_sf, p_tol=prm.p_tol)
+                         btn_g=prm.btn_g, btn_sf=prm.btn_sf, p_tol=prm.p_tol,
+                         adv_scheme=prm.adv_scheme)
 
 
 def _state_for_lib(st, three):
@@ -308,3 +309,20 @@ def test_predictor_and_ccd_equal_the_golden_loops(cuda):
                      (out[0], "ccd_fx"), (out[1], "ccd_fy")):
         assert np.array_equal(_bits(got), _bits(f[key])), key
     np.testing.assert_allclose(out[2], f["ccd_curv"], rtol=1e-14, atol=1e-14)
+
+
+@pytest.mark.parametrize("shape", [(1, 24, 32), (8, 12, 16)])
+def test_quick_predictor_matches_oracle_bitwise(cuda, shape):
+    """The QUICK advection option (ns_ab_adv_source_quick)."""
+    case, st, prm = _setup(shape, sf=1.0)
+    prm.adv_scheme = 1
+    three = shape[0] > 1
+    src, vel = _oracle_predict(case, st, prm)
+    s = _state_for_lib(st, three)
+    with PressurePoisson(shape, case.spacing) as pp:
+        ns_ab_predictor(pp, prm, s)
+    for c, (k, sk) in enumerate(zip(("u", "v", "w"), ("su", "sv", "sw"))):
+        if c == 2 and not three:
+            break
+        assert np.array_equal(_bits(s[k]), _bits(vel[c])), k
+        assert np.array_equal(_bits(s[sk]), _bits(src[c])), sk
