@@ -2332,7 +2332,14 @@ int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field p
     GB_CUDA(h, cudaStreamSynchronize(s));
     m = h->host_res[kSlotSum];
     if (!correct) break;
-    const double lam = (imass - m) / h->host_res[kSlotSum + 1];
+    const double den = h->host_res[kSlotSum + 1];
+    if (!(den > 0.0) || !std::isfinite(den)) {
+      // no cell inside the interface band (or a non-finite field): the
+      // reference's lambda would be a division by zero
+      h->err = "mass correction: no interface cells (sum of delta^2 |grad phi| is not > 0)";
+      return GBMG_INVALID_ARG;
+    }
+    const double lam = (imass - m) / den;
     const double* gcc[3] = {gr[0], gr[1], gr[2]};
     LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_update(s, P.a, ph, gcc, ls_wid, lam));
     double* arr[4] = {ph, nullptr, nullptr, nullptr};

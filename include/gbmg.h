@@ -330,7 +330,9 @@ int gbmg_ns_rho_mu(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi, do
  * on the interior, and bc.  *mass receives the mass measured last (before the
  * last correction, as the reference leaves p%glb%mass); iterations = 0 only
  * measures it (ls_mv, e.g. imass at the start).  H, delta from ls_funs with
- * half width ls_wid (CUDA's sin and cos); sums in a fixed order. */
+ * half width ls_wid (CUDA's sin and cos); sums in a fixed order.  Returns
+ * GBMG_INVALID_ARG, phi unchanged by that pass, when no cell lies in the
+ * interface band (the reference would divide by zero). */
 int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
                          double ls_wid, double rho_12, double imass, int iterations, int mem,
                          double* mass);
