@@ -204,3 +204,14 @@ def test_vof_transport_matches_the_oracle(cuda, shape):
     np.testing.assert_allclose(got, want, rtol=0, atol=1e-13)
     np.testing.assert_array_equal(host, got)
     assert got.min() >= 0.0 and got.max() <= 1.0
+
+
+def test_mass_correction_without_an_interface_is_an_error(cuda):
+    from fortrancfd_gb300 import GBMGError, PressurePoisson, mass_preserving_level_set
+    shape = (1, 16, 16)
+    ps = orc.padded_shape(shape, G)
+    phi = np.ones(ps)  # no cell within ls_wid of the interface
+    with PressurePoisson(shape, (1 / 16, 1 / 16, 1.0)) as pp:
+        with pytest.raises(GBMGError, match="no interface cells"):
+            mass_preserving_level_set(pp, NSParams(dt=1.0, ghost=G), phi, 1.5 / 16, 1e-3, 1.0)
+    assert np.all(phi == 1.0)
