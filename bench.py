@@ -615,6 +615,24 @@ def timestep_section(dev, stream, case, steps=5):
             e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
+        # one profiled MPLS step (CUDA events per kernel class on the pressure
+        # handle: the solves' classes and "momentum" for the momentum, CCD,
+        # rho_mu, MPLS and bc kernels; the rest of the step is the level set)
+        ts.pp.set_profiling(True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ts.step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms = e0.elapsed_time(e1)
+        prof = ts.pp.profile()
+        ts.pp.set_profiling(False)
+        breakdown = {"step_ms": step_ms,
+                     "momentum_ccd_mpls_kernels_ms": prof.get("momentum", (0.0, 0))[0],
+                     "pressure_solve_kernels_ms": sum(v[0] for k, v in prof.items()
+                                                      if k != "momentum")}
+        breakdown["level_set_and_rest_ms"] = (step_ms - breakdown["momentum_ccd_mpls_kernels_ms"]
+                                              - breakdown["pressure_solve_kernels_ms"])
         ts.close()
         # the CLSVOF mode (volume-fraction transport; rho and mu from it):
         # steps 2 and 4 without redistancing, 3 with (every third step)
@@ -650,6 +668,7 @@ def timestep_section(dev, stream, case, steps=5):
             "div_max": stats[-1]["div_max"], "solve_cycles_last": stats[-1]["cycles"],
             "mass_last": stats[-1]["mass"],
             "clsvof_ms_steps_2_to_4": ctimes,
+            "profiled_step": breakdown,
             "velocity_change_linf_last": stats[-1]["linf"]}
 
 
