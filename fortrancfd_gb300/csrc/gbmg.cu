@@ -1223,12 +1223,15 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   st->res0 = rel;
   int status = GBMG_NOT_CONVERGED;
   int cyc = 0;
+  bool stalled = false;  // the mixed loop stopped on a flat tracked residual
   if (rel < tol) {
     status = GBMG_OK;
   } else if (h->prm.krylov == 2) {
     GB_TRY(fgmres(h, tol, scale, &rel, &cyc, &status));
     r2 = rel * scale * rel * scale;
   } else {
+    double best = rel;
+    int flat = 0;
     for (cyc = 1; cyc <= h->prm.max_cycles; ++cyc) {
       GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
       if (kind == kGraphMixed) h->pcur ^= 1;
@@ -1238,6 +1241,19 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
       rel = std::sqrt(r2) / scale;
       if (!std::isfinite(rel) || rel > 1e3) { status = GBMG_DIVERGED; break; }
       if (rel < tol) { status = GBMG_OK; break; }
+      // The mixed cycle tracks its residual in double-word FP32; near the
+      // tolerance that figure can level off while the FP64 residual is
+      // already below it.  Four cycles without any decrease end the loop and
+      // leave the verdict to the FP64 certification below.
+      if (kind == kGraphMixed && h->prm.certify) {
+        if (rel < best) {
+          best = rel;
+          flat = 0;
+        } else if (++flat >= 4) {
+          stalled = true;
+          break;
+        }
+      }
     }
     if (cyc > h->prm.max_cycles) cyc = h->prm.max_cycles;
   }
@@ -1267,6 +1283,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     GB_TRY(read_result(h, kSlotNorm, &r2));
     rel = std::sqrt(r2) / scale;
     if (status == GBMG_OK && !(rel < tol)) status = GBMG_NOT_CONVERGED;
+    if (status == GBMG_NOT_CONVERGED && stalled && rel < tol) status = GBMG_OK;
   }
   {
     int flags = 0;
