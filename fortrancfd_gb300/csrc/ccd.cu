@@ -92,10 +92,13 @@ __device__ __forceinline__ double qh(const CcdArgs& c, double x, double h, doubl
 
 // One line per thread.  Lines: line = i1 + n1 * i2, the line's first point
 // at i1 s1 + i2 s2 from the box origin, points st apart.
-__global__ void __launch_bounds__(128) k_ccd_lines(CcdArgs c, const double* __restrict__ table,
-                                                   const double* __restrict__ f,
-                                                   double* __restrict__ S,
-                                                   double* __restrict__ SS) {
+__global__ void __launch_bounds__(128) k_ccd_lines(CcdBatch batch) {
+  const int pass = blockIdx.y;
+  const CcdArgs& c = batch.c[pass];
+  const double* __restrict__ table = batch.table[pass];
+  const double* __restrict__ f = batch.f[pass];
+  double* __restrict__ S = batch.S[pass];
+  double* __restrict__ SS = batch.SS[pass];
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
   if (line >= c.n1 * c.n2) return;
   const int i1 = line % c.n1, i2 = line / c.n1;
@@ -384,10 +387,10 @@ void launch_ccd_decompose(cudaStream_t s, int L, double h, double* work, double*
   k_ccd_decompose<<<1, 1, 0, s>>>(L, h, work, table);
 }
 
-void launch_ccd_lines(cudaStream_t s, const CcdArgs& c, const double* table, const double* f,
-                      double* S, double* SS) {
-  const int lines = c.n1 * c.n2;
-  k_ccd_lines<<<(unsigned)((lines + 127) / 128), 128, 0, s>>>(c, table, f, S, SS);
+void launch_ccd_lines(cudaStream_t s, const CcdBatch& b) {
+  int lines = 0;
+  for (int i = 0; i < b.n; ++i) lines = std::max(lines, b.c[i].n1 * b.c[i].n2);
+  k_ccd_lines<<<dim3((unsigned)((lines + 127) / 128), (unsigned)b.n), 128, 0, s>>>(b);
 }
 
 void launch_ccd_bc(cudaStream_t s, const NsArgs& a, double* const f[4]) {

@@ -1566,9 +1566,12 @@ void ns_used(const gbmg_grid& g, const gbmg_ns_params* prm, bool (&used)[kNsFiel
 // slots after the momentum step's: the six second derivatives and a dummy
 // second derivative, then a factor table per axis and the factoring work.
 constexpr int kCcdD2 = kNsDiff + 3, kCcdDummy = kCcdD2 + 6, kCcdTable = kCcdDummy + 1,
-              kCcdWork = kCcdTable + 3;
+              kCcdWork = kCcdTable + 3, kCcdSpare = kCcdWork + 1;  // two spare fields
 
-int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double* S, double* SS) {
+// One CCD line pass: its arguments, and the axis's factor table (made by
+// one sequential thread, so once, and kept while the line length and spacing
+// stay the same).
+int ccd_pass(gbmg_handle* h, const NsPlan& P, int axis, CcdArgs* out) {
   const NsArgs& a = P.a;
   const bool three = a.nz > 1;
   const int px = a.nx + 2 * a.g, py = a.ny + 2 * a.g, pz = three ? a.nz + 2 * a.g : 1;
@@ -1586,8 +1589,6 @@ int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double*
   c.rh = 1.0 / c.h;
   c.rh2 = 1.0 / c.h2;
   c.fast = fdiv_divisor_ok(c.h) && fdiv_divisor_ok(c.h2);
-  // factor table of this axis: one sequential thread, so it is made once
-  // and kept while the line length and spacing stay the same
   if (h->ccd_L[axis] != c.L || h->ccd_h[axis] != c.h) {
     h->ccd_L[axis] = 0;
     GB_TRY(ns_buffer(h, kCcdTable + axis, (size_t)14 * c.L));
@@ -1599,8 +1600,24 @@ int ccd_axis(gbmg_handle* h, const NsPlan& P, int axis, const double* f, double*
     h->ccd_L[axis] = c.L;
     h->ccd_h[axis] = c.h;
   }
-  LAUNCH(h, GBMG_PROF_MOMENTUM,
-         launch_ccd_lines(h->stream, c, h->ns_buf[kCcdTable + axis], f + P.lo, S + P.lo, SS + P.lo));
+  *out = c;
+  return GBMG_OK;
+}
+
+// Independent line passes (axis, f -> f', f'') in one launch; arrays at
+// element (1,1,1), the second-derivative outputs distinct.
+int ccd_passes(gbmg_handle* h, const NsPlan& P, int n, const int* axes,
+               const double* const* f, double* const* S, double* const* SS) {
+  CcdBatch b{};
+  b.n = n;
+  for (int i = 0; i < n; ++i) {
+    GB_TRY(ccd_pass(h, P, axes[i], &b.c[i]));
+    b.table[i] = h->ns_buf[kCcdTable + axes[i]];
+    b.f[i] = f[i] + P.lo;
+    b.S[i] = S[i] + P.lo;
+    b.SS[i] = SS[i] + P.lo;
+  }
+  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_lines(h->stream, b));
   return check_launch(h, "ccd lines");
 }
 
@@ -2233,25 +2250,32 @@ int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
   NsPlan P;
   GB_TRY(ns_prepare(h, &q, &f, mem, used, in, &P, false));
   const size_t span = (size_t)(P.hi - P.lo + 1);
-  double* d2[7];
-  for (int i = 0; i < 7; ++i) {
-    GB_TRY(ns_buffer(h, kCcdD2 + i, span));
-    d2[i] = h->ns_buf[kCcdD2 + i] - P.lo;
+  double* d2[9];
+  for (int i = 0; i < 9; ++i) {
+    const int slot = i < 7 ? kCcdD2 + i : kCcdSpare + (i - 7);
+    GB_TRY(ns_buffer(h, slot, span));
+    d2[i] = h->ns_buf[slot] - P.lo;
   }
-  double* dummy = d2[6];
   double* nx = P.base[kNsNx];
   double* ny = P.base[kNsNy];
   double* nz = three ? P.base[kNsNz] : nullptr;
   const double* ph = P.base[kNsPhi];
-  // surface_norms: first derivatives of phi and their cross derivatives, in
-  // the reference's order (the cross derivatives read phi_x, phi_y before bc)
-  GB_TRY(ccd_axis(h, P, 0, ph, nx, d2[0]));
-  GB_TRY(ccd_axis(h, P, 1, ph, ny, d2[1]));
-  if (three) GB_TRY(ccd_axis(h, P, 2, ph, nz, d2[2]));
-  GB_TRY(ccd_axis(h, P, 1, nx, d2[3], dummy));
-  if (three) {
-    GB_TRY(ccd_axis(h, P, 2, nx, d2[4], dummy));
-    GB_TRY(ccd_axis(h, P, 2, ny, d2[5], dummy));
+  // surface_norms: first and second derivatives of phi along each axis (one
+  // launch), then the cross derivatives from phi_x and phi_y before any bc
+  // (one launch; their second derivatives are discarded, each its own buffer)
+  {
+    const int axes[3] = {0, 1, 2};
+    const double* src[3] = {ph, ph, ph};
+    double* S[3] = {nx, ny, nz};
+    double* SS[3] = {d2[0], d2[1], d2[2]};
+    GB_TRY(ccd_passes(h, P, three ? 3 : 2, axes, src, S, SS));
+  }
+  {
+    const int axes[3] = {1, 2, 2};
+    const double* src[3] = {nx, nx, ny};
+    double* S[3] = {d2[3], d2[4], d2[5]};
+    double* SS[3] = {d2[6], d2[7], d2[8]};
+    GB_TRY(ccd_passes(h, P, three ? 3 : 1, axes, src, S, SS));
   }
   const double* d1c[3] = {nx, ny, nz};
   const double* d2c[6] = {d2[0], d2[1], d2[2], d2[3], d2[4], d2[5]};
@@ -2329,7 +2353,11 @@ int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field p
     gr[c] = h->ns_buf[kCcdD2 + c] - P.lo;
   }
   GB_TRY(ns_buffer(h, kCcdD2 + 6, span));
+  GB_TRY(ns_buffer(h, kCcdSpare, span));
+  GB_TRY(ns_buffer(h, kCcdSpare + 1, span));
   double* dummy = h->ns_buf[kCcdD2 + 6] - P.lo;
+  double* dummy2 = h->ns_buf[kCcdSpare] - P.lo;
+  double* dummy3 = h->ns_buf[kCcdSpare + 1] - P.lo;
   double* ph = P.base[kNsPhi];
   const gbmg_grid& g = h->grid;
   const double dv = three ? g.dx * g.dy * g.dz : g.dx * g.dy;
@@ -2339,8 +2367,12 @@ int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field p
   for (int it = 0; it < passes; ++it) {
     // ls_mv, and before a correction surface_norms' gradient of phi
     const bool correct = iterations > 0;
-    if (correct)
-      for (int c = 0; c < (three ? 3 : 2); ++c) GB_TRY(ccd_axis(h, P, c, ph, gr[c], dummy));
+    if (correct) {
+      const int axes[3] = {0, 1, 2};
+      const double* src[3] = {ph, ph, ph};
+      double* SS[3] = {dummy, dummy2, dummy3};
+      GB_TRY(ccd_passes(h, P, three ? 3 : 2, axes, src, gr, SS));
+    }
     const double* gc[3] = {correct ? gr[0] : nullptr, gr[1], gr[2]};
     LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_sums(s, P.a, ph, gc, ls_wid, rho_12, dv, h->red));
     GB_TRY(check_launch(h, "mass sums"));

@@ -367,9 +367,18 @@ struct CcdArgs {
 };
 // factor table of the CCD matrix for L points (14 doubles per point); work: 12 L doubles
 void launch_ccd_decompose(cudaStream_t s, int L, double h, double* work, double* table);
-// f' into S and f'' into SS along every line (box-origin pointers)
-void launch_ccd_lines(cudaStream_t s, const CcdArgs& c, const double* table, const double* f,
-                      double* S, double* SS);
+// Up to three independent line passes in one launch (the grid's y index
+// picks the pass): f' into S and f'' into SS along every line of each pass
+// (box-origin pointers).
+struct CcdBatch {
+  int n;
+  CcdArgs c[3];
+  const double* table[3];
+  const double* f[3];
+  double* S[3];
+  double* SS[3];
+};
+void launch_ccd_lines(cudaStream_t s, const CcdBatch& b);
 // zero-gradient ghosts (bc) of up to four arrays at element (1,1,1) (null = none)
 void launch_ccd_bc(cudaStream_t s, const NsArgs& a, double* const f[4]);
 // curvature on the interior from phi_x, phi_y, phi_z and the second derivatives
