@@ -159,4 +159,4 @@ def test_rollout_gradient_matches_central_differences(cuda):
                     jm = rollout_loss(c0, r0 - d, case, s, steps=3, tol=1e-13)
                     ad = float(r.grad[i])
             fd = float((jp - jm) / (2 * h))
-            assert abs(fd - ad) <= 1e-5 * abs(fd) + 1e-9 * abs(float(J)), (kind, i, a, fd, ad)
+            assert abs(fd - ad) <= 1e-5 * abs(fd) + 1e-9 * abs(float(J.detach())), (kind, i, a, fd, ad)
