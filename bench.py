@@ -90,9 +90,8 @@ def max_over_ranks(value, device=None):
 
 def workload_desc(case):
     nz, ny, nx = case.shape
-    return (f"{case.name}: {nx}x{ny}x{nz} cells, {len(case.radii)} bubble(s), density ratio "
-            f"{case.rho_pos / case.rho_neg:g}, eps=1.5dx, u*~N(0,1) seed {case.seed}, dt={case.dt:g}, "
-            f"tol {TOL:g} relative residual, zero initial guess")
+    return (f"{nx}x{ny}x{nz}, {len(case.radii)} bubble(s), rho ratio "
+            f"{case.rho_pos / case.rho_neg:g}, phi->rho->solve to rel. res. {TOL:g} from p=0")
 
 
 class ClockSampler:
@@ -270,7 +269,8 @@ def _factor3(n):
 
 def cpu_baseline(case, phi, u, v, w, budget_s):
     """The oracle's FP64 multigrid (red-black, all host threads), full solves
-    until the sample budget is spent (at least one)."""
+    until the sample budget is spent (at least one).  Returns the baseline
+    record, the oracle's pressure (for the parity figures) and its (coef, b)."""
     from oracle import oracle as orc
 
     threads = os.cpu_count() or 1
@@ -282,13 +282,48 @@ def cpu_baseline(case, phi, u, v, w, budget_s):
         t0 = time.perf_counter()
         rho = orc.rho_from_phi(phi, case.eps, case.rho_pos, case.rho_neg)
         coef = orc.face_coef(rho, case.spacing)
-        _, st = orc.mg_solve(coef, b, tol=TOL)
+        p_or, st = orc.mg_solve(coef, b, tol=TOL)
         times.append((time.perf_counter() - t0) * 1e3)
         if time.perf_counter() - t_start > budget_s * 0.5:
             break
-    return {"value": float(np.mean(times)), "unit": "ms", "cores": threads, "kind": "port",
-            "sample": f"{len(times)} full FP64 red-black V(2,2) solve(s) of the same case on "
-                      f"{threads} threads, {st['cycles']} cycles each (oracle restatement)"}
+    rec = {"value": float(np.mean(times)), "unit": "ms", "cores": threads, "kind": "port",
+           "sample": f"{len(times)} full FP64 red-black V(2,2) solve(s) of the same case on "
+                     f"{threads} threads, {st['cycles']} cycles each (oracle restatement)"}
+    return rec, p_or, st, coef, b
+
+
+def rel_l2_mean_free(a, b):
+    """Relative L2 distance of two pressures after removing each one's mean."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    a = a - a.mean()
+    b = b - b.mean()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_parity(p_or, st_or, coef, b, p_mixed, p_fp64, threads):
+    """Full-size parity of the GPU pressures against the oracle: the red-black
+    FP64 multigrid (the same cycle as the GPU's) and the reference's own cycle
+    (lexicographic Gauss-Seidel in OpenMP subdomains, the reference arm's
+    algorithm), both solved to the same tolerance from zero."""
+    from oracle import oracle as orc
+
+    blocks = _factor3(threads)
+    t0 = time.perf_counter()
+    p_lex, st_lex = orc.mg_solve(coef, b, tol=TOL, smoother=1, blocks=blocks)
+    lex_ms = (time.perf_counter() - t0) * 1e3
+    out = {"cycles_oracle": st_or["cycles"],
+           "oracle_rel_residual": st_or["rel_residual"],
+           "p_rel_l2_mixed_vs_oracle": rel_l2_mean_free(p_mixed, p_or),
+           "cycles_lex": st_lex["cycles"],
+           "lex_rel_residual": st_lex["rel_residual"],
+           "p_rel_l2_mixed_vs_lex": rel_l2_mean_free(p_mixed, p_lex),
+           "p_rel_l2_oracle_vs_lex": rel_l2_mean_free(p_or, p_lex),
+           "lex_blocks": "x".join(str(x) for x in blocks), "lex_ms": lex_ms}
+    if p_fp64 is not None:
+        out["p_rel_l2_fp64_vs_oracle"] = rel_l2_mean_free(p_fp64, p_or)
+        out["p_rel_l2_fp64_vs_lex"] = rel_l2_mean_free(p_fp64, p_lex)
+    return out
 
 
 def _device_velocity(shape, seed, dev):
@@ -311,12 +346,14 @@ def _device_velocity(shape, seed, dev):
     return u, v, w
 
 
-def multi_bubble_section(dev, stream, scale=1, reps=2, krylov=True):
+def multi_bubble_section(dev, stream, scale=1, reps=2, krylov=True, oracle=True):
     """The 512³ sixteen-bubble case: mixed precision (flexible CG around the
     FP32 V-cycle, the mode these small light bubbles need) against the FP64
     GPU solve of the same system.  Flexible GMRES(30) needs 52 iterations
     against 67 here but its Gram-Schmidt over up to 30 vectors of 1 GB costs
-    more than it saves (1437 against 938 ms), so flexible CG stays."""
+    more than it saves (1437 against 938 ms), so flexible CG stays.  With
+    `oracle`, the oracle's flexible-CG FP64 solve of the same inputs on the
+    host cores gives the pressure error of both GPU solves."""
     import torch
 
     from fortrancfd_gb300 import PressurePoisson, inputs
@@ -353,6 +390,28 @@ def multi_bubble_section(dev, stream, scale=1, reps=2, krylov=True):
         out["p_rel_diff_mixed_vs_fp64"] = float((ps["mixed"] - ps["fp64"]).norm() /
                                                ps["fp64"].norm())
         out["mixed_over_fp64"] = out["mixed"]["ms_per_solve"] / out["fp64"]["ms_per_solve"]
+        if oracle:
+            host = [a.cpu().numpy() for a in (phi, u, v, w)]
+            ph = {k: a.cpu().numpy() for k, a in ps.items()}
+    del ps
+    if oracle:
+        # the oracle's flexible-CG FP64 solve of the same system on the host
+        # cores (inputs copied from the device, so both sides see the same bytes)
+        from oracle import oracle as orc
+        orc.set_threads(os.cpu_count() or 1)
+        phi_h, u_h, v_h, w_h = host
+        t0 = time.perf_counter()
+        rho = orc.rho_from_phi(phi_h, case.eps, case.rho_pos, case.rho_neg)
+        coef = orc.face_coef(rho, case.spacing)
+        b_h = orc.divergence(u_h, v_h, w_h, case.dt, case.spacing)
+        del rho, host, phi_h, u_h, v_h, w_h
+        p_or, st_or = orc.mg_solve(coef, b_h, tol=TOL, krylov=1, max_cycles=400)
+        out["oracle"] = {"ms": (time.perf_counter() - t0) * 1e3, "cycles": st_or["cycles"],
+                         "rel_residual": st_or["rel_residual"],
+                         "threads": orc.num_threads(),
+                         "p_rel_l2_mixed_vs_oracle": rel_l2_mean_free(ph["mixed"], p_or),
+                         "p_rel_l2_fp64_vs_oracle": rel_l2_mean_free(ph["fp64"], p_or)}
+        del coef, b_h, p_or, ph
     nz, ny, nx = case.shape
     out["workload"] = (f"{case.name}: {nx}x{ny}x{nz} cells, {len(case.radii)} bubbles, density "
                        "ratio 1000, flexible CG around one V(2,2) cycle, tol 1e-10; inputs drawn "
@@ -870,13 +929,14 @@ def run_ours(args):
     per_solve = ms_mixed / args.steps / world
     p_mixed = p.clone()
 
-    fp64 = None
+    fp64 = p_fp64 = None
     if not args.no_fp64:
         s64 = PressurePoisson(case.shape, case.spacing, precision="fp64", **kw)
         ms64, st64, _, _ = timed(s64, max(1, args.steps // 2), max(1, args.warmup // 2), b, p)
         fp64 = {"ms_per_solve": ms64 / max(1, args.steps // 2) / world, "cycles": st64["cycles"],
                 "rel_residual": st64["rel_residual"],
                 "p_rel_diff_vs_mixed": float((p - p_mixed).norm() / p.norm())}
+        p_fp64 = p.clone()
         s64.close()
 
     # per-kernel profile pass (eager launches bracketed by CUDA events)
@@ -949,7 +1009,8 @@ def run_ours(args):
     multi = roll = None
     if not args.no_multi:
         try:
-            multi = multi_bubble_section(dev, stream, scale=max(1, args.scale))
+            multi = multi_bubble_section(dev, stream, scale=max(1, args.scale),
+                                         oracle=not args.no_cpu and rank == 0)
         except Exception as exc:
             multi = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
@@ -982,9 +1043,14 @@ def run_ours(args):
             tstep = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(case, phi_h, u_h, v_h, w_h, args.cpu_seconds)
+        cpu, p_or, st_or, coef_or, b_or = cpu_baseline(case, phi_h, u_h, v_h, w_h,
+                                                       args.cpu_seconds)
+        parity = oracle_parity(p_or, st_or, coef_or, b_or, p_mixed.cpu().numpy(),
+                               p_fp64.cpu().numpy() if p_fp64 is not None else None,
+                               cpu["cores"])
+        del p_or, coef_or, b_or
 
     if rank == 0:
         ws_gb = n * 8 * 9 / 1e9
@@ -1002,16 +1068,65 @@ def run_ours(args):
                            "l2": f"inputs larger than L2: working set ~{ws_gb:.2f} GB vs 0.129 GB L2, "
                                  "each FP64 field alone exceeds it",
                            "parallelism": f"replicas x{world}"},
+                "parity": parity,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "adjoint": adj, "multi_bubble": multi,
                 "rollout": roll, "levelset": lset, "momentum": mom, "timestep": tstep}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}
+        line["config"].update(scalar_summary(fp64, parity, adj, multi, roll, tstep))
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def scalar_summary(fp64, parity, adj, multi, roll, tstep):
+    """The figures of the nested sections as flat scalar keys (a reader of the
+    line that keeps only scalars of `config` still sees them)."""
+    out = {}
+
+    def put(key, d, *path):
+        for k in path:
+            if not isinstance(d, dict) or k not in d:
+                return
+            d = d[k]
+        if isinstance(d, (int, float, str, bool)):
+            out[key] = d
+
+    put("ms_fp64", fp64, "ms_per_solve")
+    put("cycles_fp64", fp64, "cycles")
+    for k in ("p_rel_l2_mixed_vs_oracle", "p_rel_l2_fp64_vs_oracle", "cycles_oracle",
+              "p_rel_l2_fp64_vs_lex", "p_rel_l2_mixed_vs_lex", "p_rel_l2_oracle_vs_lex",
+              "cycles_lex", "lex_ms"):
+        put(k, parity, k)
+    put("ms_512_mixed", multi, "mixed", "ms_per_solve")
+    put("ms_512_fp64", multi, "fp64", "ms_per_solve")
+    put("mixed_over_fp64_512", multi, "mixed_over_fp64")
+    put("cycles_512_mixed", multi, "mixed", "cycles")
+    put("cycles_512_fp64", multi, "fp64", "cycles")
+    put("p_rel_l2_512_mixed_vs_fp64", multi, "p_rel_diff_mixed_vs_fp64")
+    put("p_rel_l2_512_mixed_vs_oracle", multi, "oracle", "p_rel_l2_mixed_vs_oracle")
+    put("p_rel_l2_512_fp64_vs_oracle", multi, "oracle", "p_rel_l2_fp64_vs_oracle")
+    put("cycles_512_oracle", multi, "oracle", "cycles")
+    put("error_512", multi, "error")
+    put("adj_forward_ms", adj, "forward_ms")
+    put("adj_backward_ms", adj, "backward_ms")
+    put("adj_backward_over_forward", adj, "backward_over_forward")
+    put("adj_fd_max_rel", adj, "fd_max_rel_err")
+    put("adj_fd_median_rel", adj, "fd_median_rel_err")
+    put("adj_fd_directions", adj, "fd_directions")
+    put("adj_vs_fp64_gradient_max_rel", adj, "fp64_gradient_max_rel_diff")
+    put("error_adjoint", adj, "error")
+    put("rollout_forward_ms", roll, "forward_ms")
+    put("rollout_backward_ms", roll, "backward_ms")
+    put("rollout_backward_over_forward", roll, "backward_over_forward")
+    put("error_rollout", roll, "error")
+    put("timestep_ms", tstep, "ms_without_redistancing")
+    put("timestep_redistancing_ms", tstep, "ms_with_redistancing")
+    put("error_timestep", tstep, "error")
+    return out
 
 
 class _Null:

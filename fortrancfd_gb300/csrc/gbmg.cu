@@ -77,6 +77,7 @@ struct gbmg_handle {
   double* vel[3] = {nullptr, nullptr, nullptr};
   size_t vel_n[3] = {0, 0, 0};
   double* aux[2] = {nullptr, nullptr};  // adjoint outputs / staging, allocated on first use
+  double* r0 = nullptr;  // initial FP64 residual of a warm-started mixed solve (first use)
   // flexible CG vectors (allocated when krylov = 1)
   double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
   // flexible GMRES (krylov = 2): basis V (restart + 1 vectors), preconditioned
@@ -502,7 +503,7 @@ int free_all(gbmg_handle* h) {
   dfree(h->b); dfree(h->p); dfree(h->rho); dfree(h->rho32);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
   for (int a = 0; a < 3; ++a) dfree(h->vel[a]);
-  dfree(h->aux[0]); dfree(h->aux[1]);
+  dfree(h->aux[0]); dfree(h->aux[1]); dfree(h->r0);
   dfree(h->kr); dfree(h->kz); dfree(h->kzold); dfree(h->kd); dfree(h->kq);
   dfree(h->gmV); dfree(h->gmZ); dfree(h->gmPart); dfree(h->gmDev);
   if (h->gmHost) cudaFreeHost(h->gmHost);
@@ -1195,6 +1196,59 @@ int fgmres(gbmg_handle* h, double tol, double scale, double* rel_io, int* cycles
   return GBMG_OK;
 }
 
+// Start of the stationary mixed loop.  A zero initial p goes straight into
+// the double-word pressure.  A warm start (p != 0) is solved as a correction:
+// r0 = b - A p in native FP64 becomes the loop's right-hand side and the loop
+// solves A d = r0 from d = 0; finish_mixed then adds d to p in FP64.  The
+// double-word operator rounds relative to |A||p|, and for a warm start |b| can
+// be far below |A||p| (a later pass of a time step), which would put the loop's
+// floor near the tolerance; in the correction form it rounds relative to
+// |A||d| instead.  *shifted tells finish_mixed which form ran.
+int start_mixed(gbmg_handle* h, bool* shifted) {
+  const cudaStream_t s = h->stream;
+  Level& f = h->lv[0];
+  const size_t n = h->n0;
+  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+  GB_TRY(check_launch(h, "initial guess"));
+  double pp = 0.0;
+  GB_TRY(read_result(h, kSlotSum + 1, &pp));
+  *shifted = pp != 0.0;
+  if (*shifted) {
+    if (!h->r0) GB_TRY(dmalloc(h, &h->r0, n));
+    f.sol = h->p; f.src = h->b;
+    LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<double>(s, v64(f), h->r0, h->red, kSlotNorm));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->r0, h->bw, n));
+    GB_CUDA(h, cudaMemsetAsync(h->pw[0], 0, n * sizeof(float2), s));
+  } else {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
+  }
+  // the first residual (no correction yet)
+  LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
+  h->pcur = 1;
+  return GBMG_OK;
+}
+
+// The mixed loop's result into h->p, mean-free (compatibility_sol on the
+// finest level); restores the double-word right-hand side after a correction
+// solve.
+int finish_mixed(gbmg_handle* h, bool shifted) {
+  const cudaStream_t s = h->stream;
+  const size_t n = h->n0;
+  if (shifted) {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_accumulate(s, h->pw[h->pcur], h->p, n));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->b, h->bw, n));
+  } else {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_sum(s, h->pw[h->pcur], n, h->red, kSlotSum));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_out(s, h->pw[h->pcur], h->p, n, h->red, kSlotSum));
+  }
+  return check_launch(h, "mean");
+}
+
+// Restarts of the stationary mixed loop after a failed FP64 certification.
+constexpr int kMixedRestarts = 2;
+
 int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
@@ -1202,16 +1256,14 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   const bool pcg = h->prm.krylov != 0;
   const int kind = pcg ? (h->mixed ? kGraphPcgMixed : kGraphPcg64) : (h->mixed ? kGraphMixed : kGraphFp64);
   const double scale = bnorm > 0.0 ? bnorm : 1.0;
+  bool shifted = false;
   // initial residual
   f.sol = h->p; f.src = h->b;
   if (pcg) {
     LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
     GB_CUDA(h, cudaMemsetAsync(h->kzold, 0, n * sizeof(double), s));
   } else if (h->mixed) {
-    // p into double-word, then the first residual (no correction yet)
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
-    LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
-    h->pcur = 1;
+    GB_TRY(start_mixed(h, &shifted));
   } else {
     LAUNCH(h, GBMG_PROF_RESIDUAL,
            launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
@@ -1223,58 +1275,63 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   st->res0 = rel;
   int status = GBMG_NOT_CONVERGED;
   int cyc = 0;
-  bool stalled = false;  // the mixed loop stopped on a flat tracked residual
   if (rel < tol) {
     status = GBMG_OK;
   } else if (h->prm.krylov == 2) {
     GB_TRY(fgmres(h, tol, scale, &rel, &cyc, &status));
     r2 = rel * scale * rel * scale;
-  } else {
-    double best = rel;
-    int flat = 0;
-    for (cyc = 1; cyc <= h->prm.max_cycles; ++cyc) {
-      GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
-      if (kind == kGraphMixed) h->pcur ^= 1;
-      GB_CUDA(h, cudaStreamSynchronize(s));
-      prof_flush(h);
-      r2 = h->host_res[kSlotNorm];
-      rel = std::sqrt(r2) / scale;
-      if (!std::isfinite(rel) || rel > 1e3) { status = GBMG_DIVERGED; break; }
-      if (rel < tol) { status = GBMG_OK; break; }
-      // The mixed cycle tracks its residual in double-word FP32; near the
-      // tolerance that figure can level off while the FP64 residual is
-      // already below it.  Four cycles without any decrease end the loop and
-      // leave the verdict to the FP64 certification below.
-      if (kind == kGraphMixed && h->prm.certify) {
-        if (rel < best) {
-          best = rel;
-          flat = 0;
-        } else if (++flat >= 4) {
-          stalled = true;
+  }
+  for (int restart = 0;; ++restart) {
+    bool stalled = false;  // the mixed loop stopped on a flat tracked residual
+    if (status == GBMG_NOT_CONVERGED && h->prm.krylov != 2) {
+      double best = rel;
+      int flat = 0;
+      while (cyc < h->prm.max_cycles) {
+        ++cyc;
+        GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
+        if (kind == kGraphMixed) h->pcur ^= 1;
+        GB_CUDA(h, cudaStreamSynchronize(s));
+        prof_flush(h);
+        r2 = h->host_res[kSlotNorm];
+        rel = std::sqrt(r2) / scale;
+        if (!std::isfinite(rel) || rel > 1e3 * std::max(1.0, st->res0)) {
+          status = GBMG_DIVERGED;
           break;
+        }
+        if (rel < tol) { status = GBMG_OK; break; }
+        // The mixed cycle tracks its residual in double-word FP32; near the
+        // tolerance that figure can level off while the FP64 residual is
+        // already below it.  Four cycles without any decrease end the loop and
+        // leave the verdict to the FP64 certification below.
+        if (kind == kGraphMixed && h->prm.certify) {
+          if (rel < best) {
+            best = rel;
+            flat = 0;
+          } else if (++flat >= 4) {
+            stalled = true;
+            break;
+          }
         }
       }
     }
-    if (cyc > h->prm.max_cycles) cyc = h->prm.max_cycles;
-  }
-  // mean projection of p (compatibility_sol on the finest level)
-  if (kind == kGraphMixed) {
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_sum(s, h->pw[h->pcur], n, h->red, kSlotSum));
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_out(s, h->pw[h->pcur], h->p, n, h->red, kSlotSum));
-  } else {
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
-  }
-  GB_TRY(check_launch(h, "mean"));
-  if (h->dl_field) {
-    // p is final: its copy to the host runs beside the certification
-    GB_CUDA(h, cudaEventRecord(h->cev[1], s));
-    GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[1], 0));
-    GB_TRY(download(h, h->p, h->grid.nx, h->grid.ny, h->grid.nz, GBMG_MEM_HOST, *h->dl_field,
-                    h->cstream));
-    h->dl_started = true;
-  }
-  if (kind == kGraphMixed && h->prm.certify) {
+    // mean projection of p (compatibility_sol on the finest level)
+    if (kind == kGraphMixed) {
+      GB_TRY(finish_mixed(h, shifted));
+    } else {
+      LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+      LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
+      GB_TRY(check_launch(h, "mean"));
+    }
+    if (h->dl_field) {
+      // p is final unless the certification below sends the loop round again:
+      // its copy to the host runs beside the certification
+      GB_CUDA(h, cudaEventRecord(h->cev[1], s));
+      GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[1], 0));
+      GB_TRY(download(h, h->p, h->grid.nx, h->grid.ny, h->grid.nz, GBMG_MEM_HOST, *h->dl_field,
+                      h->cstream));
+      h->dl_started = true;
+    }
+    if (!(kind == kGraphMixed && h->prm.certify)) break;
     // the loop tracked the residual in double-word; restate it in native FP64
     f.sol = h->p; f.src = h->b;
     LAUNCH(h, GBMG_PROF_CERTIFY,
@@ -1284,6 +1341,19 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     rel = std::sqrt(r2) / scale;
     if (status == GBMG_OK && !(rel < tol)) status = GBMG_NOT_CONVERGED;
     if (status == GBMG_NOT_CONVERGED && stalled && rel < tol) status = GBMG_OK;
+    if (status != GBMG_NOT_CONVERGED || cyc >= h->prm.max_cycles || restart >= kMixedRestarts)
+      break;
+    // Certified above the tolerance with cycles left: go round again from the
+    // certified p, as a correction solve (its residual is the FP64 one just
+    // computed).  The host copy started above must finish before p changes.
+    if (h->dl_field) {
+      GB_CUDA(h, cudaEventRecord(h->cev[0], h->cstream));
+      GB_CUDA(h, cudaStreamWaitEvent(s, h->cev[0], 0));
+    }
+    GB_TRY(start_mixed(h, &shifted));
+    GB_TRY(read_result(h, kSlotNorm, &r2));
+    rel = std::sqrt(r2) / scale;
+    if (rel < tol) status = GBMG_OK;
   }
   {
     int flags = 0;
@@ -2472,7 +2542,7 @@ const char* gbmg_strerror(int status) {
   switch (status) {
     case GBMG_OK: return "ok";
     case GBMG_NOT_CONVERGED: return "not converged within max_cycles";
-    case GBMG_DIVERGED: return "diverged (residual not finite or grew above 1e3)";
+    case GBMG_DIVERGED: return "diverged (residual not finite or grew 1e3-fold)";
     case GBMG_INVALID_ARG: return "invalid argument";
     case GBMG_CUDA_ERROR: return "CUDA error";
     case GBMG_NO_DEVICE: return "no CUDA device";

@@ -314,6 +314,8 @@ void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, i
                        size_t hstride);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
+// out += double(d)
+void launch_dw_accumulate(cudaStream_t s, const float2* d, double* out, size_t n);
 // out = double(p) - result[slot]/n
 void launch_dw_out(cudaStream_t s, const float2* p, double* out, size_t n, const ReduceScratch& R,
                    int slot);

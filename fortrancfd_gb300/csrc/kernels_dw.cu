@@ -287,6 +287,12 @@ __global__ void k_dw_out(const float2* __restrict__ p, double* __restrict__ out,
           [&](size_t q, dw v) { out[q] = dw_to_double_int(v) - m; });
 }
 
+// out += double(d): the correction of a warm-started solve added to its start
+__global__ void k_dw_accumulate(const float2* __restrict__ d, double* __restrict__ out, size_t n) {
+  stride4(n, [&](size_t q) { return dw_ldg(d + q); },
+          [&](size_t q, dw v) { out[q] += dw_to_double_int(v); });
+}
+
 inline unsigned stride_blocks(size_t n) {
   const size_t b = (n + kRedThreads - 1) / kRedThreads;
   return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 152 * 8));
@@ -354,6 +360,10 @@ void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratc
 void launch_dw_out(cudaStream_t s, const float2* p, double* out, size_t n, const ReduceScratch& R,
                    int slot) {
   k_dw_out<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(p, out, n, R, slot);
+}
+
+void launch_dw_accumulate(cudaStream_t s, const float2* d, double* out, size_t n) {
+  k_dw_accumulate<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(d, out, n);
 }
 
 }  // namespace gbmg

@@ -10,14 +10,19 @@
 //
 // Scratch layout (doubles): kRedValues x kStaticBlocks per-block partial sums,
 // then kRedSlots result slots, then one 8-byte slot holding the completion
-// counter.  Only the counter must start at zero: the block that finishes a
-// reduction last resets it, and the set-up below zeroes it once.  The
-// partials are written before they are read, and launch_div_stats zeroes the
-// max slot before every launch.
+// counter.  Only the counter must start at zero.  The block that finishes a
+// reduction last resets it, but a launch that fails part-way can leave it
+// non-zero, so every call zeroes it on the caller's stream before its launch
+// (an 8-byte cudaMemsetAsync, which allocates nothing).  The partials are
+// written before they are read, and launch_div_stats zeroes the max slot
+// before every launch.
 //
-// Set-up: the first call on a device (made with that device current) takes
-// the array's device address with cudaGetSymbolAddress and zeroes the counter
-// on the caller's stream, then synchronizes that stream.
+// Set-up: every call looks up the array's device address on the device it
+// runs on (cudaGetSymbolAddress with that device current; a host-side lookup
+// that allocates nothing).  The address is not cached: after a
+// cudaDeviceReset the module is loaded again and the array may move.  The
+// first call on a device may load the library's module there, so make it
+// before any stream capture on that device.
 //
 // Overlapping calls race: every call on a device uses the one scratch, so two
 // calls in flight at once (from two host threads, on any streams) corrupt each
@@ -25,7 +30,6 @@
 // calls from one host thread never overlap.
 #include <climits>
 #include <cstdio>
-#include <mutex>
 
 #include "gbmg.h"
 #include "gbmg_internal.h"
@@ -41,35 +45,27 @@ constexpr size_t kStaticDoubles = kStaticCounter + 1;  // 32,904 bytes
 
 static __device__ __align__(256) double g_noalloc_scratch[kStaticDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-double* g_scratch_of_device[kMaxDevices] = {};
-
 void set_err(char* err, size_t len, const char* fmt, long long a = 0, long long b = 0) {
   if (err && len > 0) std::snprintf(err, len, fmt, a, b);
 }
 
-// Device address of the scratch on the current device `dev`, set up on first use.
-int scratch_for(int dev, cudaStream_t s, double** out, char* err, size_t len) {
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_of_device[dev]) {
-    void* p = nullptr;
-    cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (rc != cudaSuccess || !p) {
-      set_err(err, len, "div_stats_noalloc: cudaGetSymbolAddress failed (CUDA error %lld)", rc);
-      return GBMG_CUDA_ERROR;
-    }
-    double* base = static_cast<double*>(p);
-    rc = cudaMemsetAsync(base + kStaticCounter, 0, sizeof(double), s);
-    if (rc == cudaSuccess) rc = cudaStreamSynchronize(s);
-    if (rc != cudaSuccess) {
-      set_err(err, len, "div_stats_noalloc: zeroing the static scratch failed (CUDA error %lld)",
-              rc);
-      return GBMG_CUDA_ERROR;
-    }
-    g_scratch_of_device[dev] = base;
+// Device address of the scratch on the current device, with its completion
+// counter zeroed on stream s (ordered before the caller's launch on s).
+int scratch_for(cudaStream_t s, double** out, char* err, size_t len) {
+  void* p = nullptr;
+  cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (rc != cudaSuccess || !p) {
+    set_err(err, len, "div_stats_noalloc: cudaGetSymbolAddress failed (CUDA error %lld)", rc);
+    return GBMG_CUDA_ERROR;
   }
-  *out = g_scratch_of_device[dev];
+  double* base = static_cast<double*>(p);
+  rc = cudaMemsetAsync(base + kStaticCounter, 0, sizeof(double), s);
+  if (rc != cudaSuccess) {
+    set_err(err, len, "div_stats_noalloc: zeroing the completion counter failed (CUDA error %lld)",
+            rc);
+    return GBMG_CUDA_ERROR;
+  }
+  *out = base;
   return GBMG_OK;
 }
 
@@ -110,7 +106,7 @@ extern "C" int gbmg_div_stats_noalloc(const gbmg_grid* grid, gbmg_field u, gbmg_
   int prev = 0;
   cudaGetDevice(&prev);
   const int dev = device >= 0 ? device : prev;
-  if (dev >= ndev || dev >= kMaxDevices) {
+  if (dev >= ndev) {
     set_err(err, err_len, "div_stats_noalloc: device %lld out of range (%lld devices)", dev,
             ndev);
     return GBMG_INVALID_ARG;
@@ -130,7 +126,7 @@ extern "C" int gbmg_div_stats_noalloc(const gbmg_grid* grid, gbmg_field u, gbmg_
   }
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
   double* base = nullptr;
-  if (st == GBMG_OK) st = scratch_for(dev, s, &base, err, err_len);
+  if (st == GBMG_OK) st = scratch_for(s, &base, err, err_len);
   if (st == GBMG_OK) {
     const ReduceScratch R{base, reinterpret_cast<unsigned int*>(base + kStaticCounter),
                           base + kStaticResult, kStaticBlocks};

@@ -192,9 +192,12 @@ int gbmg_div_stats(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, dou
  * blocks (the call needs 8 per SM) plus result slots; grids whose rows of
  * cells (ny*nz) exceed 2^31 - 1, or a device whose reduction needs more than
  * 2048 blocks, are rejected with GBMG_INVALID_ARG and a message in err.
- * The first call on each device does a one-time set-up (takes the scratch's
- * address, zeroes its counter, synchronizes the stream); make it before any
- * stream capture.  Calls share the one scratch of their device: two calls in
+ * Every call looks up the scratch's address on its device (no cached address,
+ * so a cudaDeviceReset in between is safe) and zeroes the scratch's completion
+ * counter on the stream before its launch, so a launch that failed earlier
+ * leaves nothing behind.  The first call on a device may load the library's
+ * module there: make it before any stream capture on that device.  Calls
+ * share the one scratch of their device: two calls in
  * flight at once (from two host threads) race and corrupt each other's sums.
  * Every call returns after its stream has finished it. */
 int gbmg_div_stats_noalloc(const gbmg_grid* grid, gbmg_field u, gbmg_field v, gbmg_field w,

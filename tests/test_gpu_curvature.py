@@ -1,8 +1,10 @@
 """Interface normals and curvature on the GPU (gbmg_ns_curvature, momentum.curv)
 against the oracle's compact-difference restatement: the derivatives are FP64
 in the reference's operand order on both sides and compared bit for bit; the
-curvature divides by (|grad phi|^2 + 1e-12)^1.5 with CUDA's pow on the GPU and
-glibc's on the host, so it is compared to 1e-14 relative."""
+curvature divides by s^1.5, s = |grad phi|^2 + 1e-12, which the GPU forms as
+s*sqrt(s) (correctly rounded sqrt, so within about two roundings of exact)
+and the oracle with glibc's pow (within about one), so it is compared to
+1e-14 relative."""
 import numpy as np
 import pytest
 

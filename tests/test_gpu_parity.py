@@ -9,8 +9,13 @@ Tolerances (floating point):
   * plain FP64 solve: mean-free pressure within 1e-9 relative L2 of the
     oracle's and the same cycle count +/- 1;
   * mixed precision (FP32 cycles inside FP64 defect correction): the same
-    1e-10 relative residual in FP64, pressure within 1e-8 relative L2 of the
-    FP64 oracle solution.
+    1e-10 relative residual in FP64, pressure within 1e-9 relative L2 of the
+    FP64 oracle solution;
+  * the FP64 iterate after k = 1, 2, 3 cycles: within 1e-12 relative L2 of the
+    oracle's iterate after the same cycles (restriction, prolongation and the
+    coarse solve each enter every cycle, so a slip in any shows here);
+  * against the reference's own cycle (lexicographic Gauss-Seidel in
+    subdomains): pressure within 1e-9 relative L2, cycles within one in 3D.
 """
 import numpy as np
 import pytest
@@ -102,6 +107,75 @@ def test_fp64_solve_matches_oracle(cuda, idx, scale):
     assert abs(p.mean()) <= 1e-12 * np.abs(p).max()
 
 
+@pytest.mark.parametrize("idx,scale", [(0, 1), (1, 4)])
+def test_fp64_iterates_after_each_cycle_match_oracle(cuda, idx, scale):
+    """The FP64 iterate after k = 1, 2, 3 V(2,2) cycles from zero against the
+    oracle's after the same cycles (tol too small to stop).  Every cycle goes
+    through restriction, the coarse solve and prolongation on every level, so
+    a slip in any of them that still converges within a cycle shows here."""
+    c = cases.config(idx, scale)
+    scale_b = np.linalg.norm(c.b)
+    for k in (1, 2, 3):
+        p_or, st_or = orc.mg_solve(c.coef, c.b, tol=1e-300, max_cycles=k)
+        assert st_or["cycles"] == k
+        with solver(c, max_cycles=k) as s:
+            s.ppe_init(c.rho)
+            p, st = s.solve(c.b, tol=1e-300, check=False)
+        assert st["cycles"] == k and st["status"] == 1, st
+        # the iterate is far from converged: compare it and its residual
+        assert rel_l2(p - p.mean(), p_or - p_or.mean()) <= 1e-12, k
+        assert st["rel_residual"] == pytest.approx(st_or["rel_residual"], rel=1e-9), k
+        _, r2 = orc.residual(c.coef, p, c.b)
+        assert np.sqrt(r2) / scale_b == pytest.approx(st_or["rel_residual"], rel=1e-9)
+
+
+@pytest.mark.parametrize("idx,scale,blocks,max_gap", [
+    (1, 4, (2, 2, 2), 1), (1, 4, (1, 2, 4), 1), (1, 2, (2, 2, 2), 1), (0, 1, (1, 2, 2), 2)])
+def test_fp64_solve_matches_reference_lexicographic_cycle(cuda, idx, scale, blocks, max_gap):
+    """The GPU's red-black FP64 cycle against the reference's own cycle: V(2,2)
+    with lexicographic Gauss-Seidel inside OpenMP subdomains (the oracle's
+    restatement of multigrid_relax over DomainDecomposition's blocks), both
+    solved from zero to 1e-10.  The pressures agree to 1e-9 relative L2
+    (measured: 2e-11 to 2e-10); the cycle counts differ by at most one in 3D.
+    On the 2D bubble the lexicographic cycle converges in two fewer cycles
+    (14 against 16): the red-black colouring smooths a little less per sweep
+    there."""
+    c = cases.config(idx, scale)
+    p_lex, st_lex = orc.mg_solve(c.coef, c.b, tol=1e-10, smoother=1, blocks=blocks)
+    assert st_lex["status"] == 0
+    with solver(c) as s:
+        s.ppe_init(c.rho)
+        p, st = s.solve(c.b, tol=1e-10)
+    assert st["status"] == 0
+    gap = rel_l2(p - p.mean(), p_lex - p_lex.mean())
+    print(f"lexicographic {blocks}: cycles GPU {st['cycles']} / lex {st_lex['cycles']}, "
+          f"relative L2 gap {gap:.2e}")
+    assert gap <= 1e-9
+    assert abs(st["cycles"] - st_lex["cycles"]) <= max_gap, (st["cycles"], st_lex["cycles"])
+
+
+@pytest.mark.parametrize("idx,scale", [(1, 4), (0, 1)])
+def test_mixed_warm_start_far_from_the_solution(cuda, idx, scale):
+    """A warm start whose A p is 10^4 times the right-hand side (as in the later
+    passes of a time step, where the predicted velocity is nearly
+    divergence-free but the pressure is not small): the mixed solve works on
+    the correction from the FP64 initial residual, so the double-word
+    operator's rounding scales with the correction, not with p, and the solve
+    still certifies 1e-10 in FP64 and meets the oracle's pressure."""
+    c = cases.config(idx, scale)
+    p_big, _ = orc.mg_solve(c.coef, c.b, tol=1e-12, max_cycles=200)
+    b_small = c.b * 1e-4
+    want, _ = orc.mg_solve(c.coef, b_small, tol=1e-12, max_cycles=200)
+    with solver(c, precision="mixed", max_cycles=100) as s:
+        s.ppe_init(c.rho)
+        p0 = p_big.copy()
+        p, st = s.solve(b_small, p0, tol=1e-10)
+    assert st["status"] == 0 and st["rel_residual"] < 1e-10, st
+    _, r2 = orc.residual(c.coef, p, b_small)
+    assert np.sqrt(r2) / np.linalg.norm(b_small) < 1e-10
+    assert rel_l2(p, want) <= 1e-9
+
+
 @pytest.mark.parametrize("idx,scale", [(0, 1), (1, 4), (1, 2)])
 def test_mixed_solve_reaches_fp64_accuracy(cuda, idx, scale):
     c = cases.config(idx, scale)
@@ -113,7 +187,7 @@ def test_mixed_solve_reaches_fp64_accuracy(cuda, idx, scale):
     # the true FP64 residual, recomputed by the oracle
     _, r2 = orc.residual(c.coef, p, c.b)
     assert np.sqrt(r2) / np.linalg.norm(c.b) < 1e-10
-    assert rel_l2(p, p_or) <= 1e-8
+    assert rel_l2(p, p_or) <= 1e-9
     assert st["cycles"] <= st_or["cycles"] + 2
 
 
@@ -130,7 +204,7 @@ def test_krylov_matches_oracle(cuda, precision):
         assert abs(st["cycles"] - st_or["cycles"]) <= 1, (st["cycles"], st_or["cycles"])
     else:
         assert st["cycles"] <= st_or["cycles"] + 3
-    assert rel_l2(p, p_or) <= 1e-8
+    assert rel_l2(p, p_or) <= 1e-9
 
 
 @pytest.mark.parametrize("precision,idx,scale", [("fp64", 2, 8), ("mixed", 2, 8), ("mixed", 1, 4),
@@ -147,7 +221,7 @@ def test_fgmres_matches_oracle(cuda, precision, idx, scale):
     assert st["status"] == 0 and st["rel_residual"] < 1e-10
     _, r2 = orc.residual(c.coef, p, c.b)
     assert np.sqrt(r2) / np.linalg.norm(c.b) < 1e-10
-    assert rel_l2(p, p_or) <= 1e-8
+    assert rel_l2(p, p_or) <= 1e-9
     assert st["cycles"] <= st_or["cycles"] + 3
 
 
@@ -503,4 +577,4 @@ def test_mixed_small_and_ragged_grids(cuda, shape):
     assert st["status"] == st_or["status"] == 0
     assert st["rel_residual"] < 1e-10
     assert st["cycles"] <= st_or["cycles"] + 2
-    assert rel_l2(p, p_or) <= 1e-8
+    assert rel_l2(p, p_or) <= 1e-9
