@@ -193,10 +193,23 @@ def rho_form():
     return os.environ.get("GBMG_RHO_COEF", "1") != "0"
 
 
-def algorithmic_bytes_per_cell(cls, w=4):
+def one_launch_sweep(shape):
+    """Whether the finest FP32 level sweeps with one launch per sweep
+    (k_sweep_split: colour-split density form, nx % 8 == 0, nx/2 <= 256;
+    GBMG_SWEEP=0 keeps one launch per colour)."""
+    nx = shape[2]
+    return (rho_form() and os.environ.get("GBMG_SPLIT", "1") != "0"
+            and os.environ.get("GBMG_SWEEP", "1") != "0" and nx % 8 == 0 and nx // 2 <= 256)
+
+
+def algorithmic_bytes_per_cell(cls, w=4, shape=None):
     c = w if rho_form() else 3.0 * w
+    # one sweep reads p, b and the coefficients and writes p; the one-launch
+    # sweep reads only the second colour's half of p (the first colour's old
+    # values never enter a Gauss-Seidel update)
+    p_read = 0.5 * w if shape is not None and one_launch_sweep(shape) else w
     return {
-        "smooth_fine": 3.0 * w + c,              # one sweep: p, b, coefficients read, p' write
+        "smooth_fine": p_read + 2.0 * w + c,     # one sweep: p, b, coefficients read, p' write
         "restrict_fine": 2.0 * w + c + 2.0 * w / 8,  # p, b, coefficients -> coarse b, sol
         "prolong_fine": 2.0 * w + w / 8,         # p r/w + coarse e
         "residual": 56.0,                        # defect: p(8) + e(4) + b(8) + 3 coefs(24) in,
@@ -951,7 +964,8 @@ def run_ours(args):
             prof = mixed.profile()
             mixed.set_profiling(False)
         total = sum(v[0] for v in prof.values())
-        ranked = sorted(((k, v) for k, v in prof.items() if algorithmic_bytes_per_cell(k, 4)),
+        ranked = sorted(((k, v) for k, v in prof.items()
+                         if algorithmic_bytes_per_cell(k, 4, case.shape)),
                         key=lambda kv: -kv[1][0])
         cls, (ms_cls, cnt) = ranked[0]
         per_launch_ms = ms_cls / max(cnt, 1)
@@ -960,7 +974,7 @@ def run_ours(args):
         units = n
         if cls == "smooth_fine":
             units = n * st_prof["cycles"] * (NU1 + NU2) / max(cnt, 1)
-        alg = algorithmic_bytes_per_cell(cls, 4) * units
+        alg = algorithmic_bytes_per_cell(cls, 4, case.shape) * units
         peak, peak_kind = measured_peaks()
         achieved = alg / (per_launch_ms * 1e-3) / 1e9
         tr = traffic_per_cell().get(cls)
@@ -969,6 +983,8 @@ def run_ours(args):
                     "traffic": (tr * units if tr else None), "launch_ms": per_launch_ms,
                     "share": ms_cls / total if total else None,
                     "algorithmic_bytes_per_launch": alg, "cells_per_launch": units,
+                    "bytes_per_cell": algorithmic_bytes_per_cell(cls, 4, case.shape),
+                    "one_launch_sweep": one_launch_sweep(case.shape),
                     "coefficients": "density form" if rho_form() else "stored FP32"}
 
     e2e = None

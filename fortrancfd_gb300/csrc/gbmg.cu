@@ -51,6 +51,7 @@ struct Level {
   int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
   int zmarch = 0, zc = 16;  // z-marching colour sweep of the split level (LevelView)
   int minb = 0;             // register bound of the split level's colour sweep (LevelView)
+  int fsweep = 0;  // the split level sweeps with one launch per sweep (k_sweep_split)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -322,7 +323,13 @@ void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   const bool fused = h->fused_levels > l || (l >= h->fused_lo && l < h->fused_hi);
   if (zero_guess && (lv.tmaps || fused))  // out-of-place sweeps read p
     cudaMemsetAsync(lv.sol32, 0, lv.n * sizeof(float), h->stream);
-  if (lv.tmaps) {
+  if (lv.fsweep) {
+    // the colour-split finest level: a whole sweep per launch, out of place
+    // (from a zero guess it reads no p at all)
+    LAUNCH(h, cs, launch_sweep_split(h->stream, v32(lv), lv.sol32, lv.alt32, first_color,
+                                     zero_guess, h->derr));
+    std::swap(lv.sol32, lv.alt32);
+  } else if (lv.tmaps) {
     const SweepMaps& m = lv.tmaps[lv.sol32 == lv.buf_a ? 0 : 1];
     LAUNCH(h, cs, launch_smooth_tma(h->stream, m, lv.nx, lv.ny, lv.nz, lv.alt32, first_color, h->derr));
     std::swap(lv.sol32, lv.alt32);
@@ -686,7 +693,7 @@ int allocate(gbmg_handle* h) {
       GB_TRY(dmalloc(h, &v.cy32, v.n));
       GB_TRY(dmalloc(h, &v.cz32, v.n));
       GB_TRY(dmalloc(h, &v.sol32, nv));
-      GB_TRY(dmalloc(h, &v.alt32, v.n));
+      GB_TRY(dmalloc(h, &v.alt32, nv));
       GB_TRY(dmalloc(h, &v.src32, nv));
     }
   }
@@ -877,6 +884,15 @@ void set_rho_form(gbmg_handle* h, bool on) {
   f.zmarch = zm;
   f.zc = zc;
   f.minb = minb;
+  // one launch per sweep on the split level: even sweep counts (so that the
+  // level's unknown is back in its first buffer wherever the cycle reads it),
+  // rows of at most 256 half cells; GBMG_SWEEP=0 keeps the two colour launches
+  bool fs = split && zm == 0 && h->prm.nu1 % 2 == 0 && h->prm.nu2 % 2 == 0 &&
+            sweep_split_supported(f.nx, f.ny, f.nz, hs) && sweep_split_init() == 0;
+  if (const char* e = std::getenv("GBMG_SWEEP"))
+    if (std::atoi(e) == 0) fs = false;
+  if ((int)fs != f.fsweep) reset_graphs(h);
+  f.fsweep = fs ? 1 : 0;
   f.rho32 = r;
   f.split = split ? 1 : 0;
   f.hstride = hs;

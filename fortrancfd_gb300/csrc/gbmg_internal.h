@@ -221,12 +221,26 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
+// The roundings of the density-form FP32 arithmetic are pinned with explicit
+// _rn intrinsics (no contraction left to the compiler), so that every kernel
+// that relaxes a cell -- natural layout, colour-split layout, one colour per
+// launch or a whole sweep per launch -- gives the same bits.
 // face coefficient k/(rho_a + rho_b), k = 2/h^2
 __device__ __forceinline__ float rho_face32(float k, float ra, float rb) {
-  return k * rcp_approx(ra + rb);
+  return __fmul_rn(k, rcp_approx(__fadd_rn(ra, rb)));
+}
+// one face of the smoother's sums: s += c p_nb, d += c
+__device__ __forceinline__ void rho_acc32(float c, float pn, float& s, float& d) {
+  s = __fmaf_rn(c, pn, s);
+  d = __fadd_rn(d, c);
 }
 // the smoother's update (s - b)/d
-__device__ __forceinline__ float rho_update32(float v, float d) { return v * rcp_approx(d); }
+__device__ __forceinline__ float rho_update32(float v, float d) {
+  return __fmul_rn(v, rcp_approx(d));
+}
+__device__ __forceinline__ float rho_relax32(float s, float b, float d) {
+  return rho_update32(__fsub_rn(s, b), d);
+}
 
 // ---- colour-split FP32 finest level (kernels_split.cu) ----
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess);
@@ -237,6 +251,13 @@ void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny
                      size_t hstride);
 void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz,
                        size_t hstride);
+// One whole red-black sweep of the colour-split finest level, out of place
+// (kernels_sweep.cu): first_color relaxes first; zero_guess: p_in is taken as
+// zero and not read.  *err |= 1 on a bulk-copy wait timeout.
+bool sweep_split_supported(int nx, int ny, int nz, size_t hstride);
+int sweep_split_init();
+void launch_sweep_split(cudaStream_t s, const LevelView<float>& L, const float* pin, float* pout,
+                        int first_color, bool zero_guess, int* err);
 // elements reserved past n in each split FP32 finest-level array for the pad
 constexpr size_t kSplitPadMax = 65536;
 

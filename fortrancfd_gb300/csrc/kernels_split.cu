@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(256) k_smooth_split(LevelView<float> L, int co
   if (cond) {                                   \
     const size_t tt = (t);                      \
     c = face(kk, rc, ro[tt]);                   \
-    if (!kZero) s += c * po[tt];                \
-    d += c;                                     \
+    if (!kZero) rho_acc32(c, po[tt], s, d);     \
+    else d = __fadd_rn(d, c);                   \
   }
   SPLIT_TERM(i > 0, L.kx, h - 1 + par)
   SPLIT_TERM(i < L.nx - 1, L.kx, h + par)
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_smooth_split(LevelView<float> L, int co
   SPLIT_TERM(k > 0, L.kz, h - sz)
   SPLIT_TERM(k < L.nz - 1, L.kz, h + sz)
 #undef SPLIT_TERM
-  L.sol[own] = rho_update(s - L.src[own], d);
+  L.sol[own] = rho_relax32(s, L.src[own], d);
 }
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
@@ -130,13 +130,13 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_smooth_split4(LevelView<flo
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float s = 0.f, d = 0.f, cc;
-    cc = face(L.kx, rc[c], rxm[c]); if (!kZero) s += cc * pxm[c]; d += cc;
-    cc = face(L.kx, rc[c], rxp[c]); if (!kZero) s += cc * pxp[c]; d += cc;
-    cc = face(L.ky, rc[c], rym[c]); if (!kZero) s += cc * pym[c]; d += cc;
-    cc = face(L.ky, rc[c], ryp[c]); if (!kZero) s += cc * pyp[c]; d += cc;
-    cc = face(L.kz, rc[c], rzm[c]); if (!kZero) s += cc * pzm[c]; d += cc;
-    cc = face(L.kz, rc[c], rzp[c]); if (!kZero) s += cc * pzp[c]; d += cc;
-    out[c] = rho_update(s - b[c], d);
+    cc = face(L.kx, rc[c], rxm[c]); if (!kZero) rho_acc32(cc, pxm[c], s, d); else d = __fadd_rn(d, cc);
+    cc = face(L.kx, rc[c], rxp[c]); if (!kZero) rho_acc32(cc, pxp[c], s, d); else d = __fadd_rn(d, cc);
+    cc = face(L.ky, rc[c], rym[c]); if (!kZero) rho_acc32(cc, pym[c], s, d); else d = __fadd_rn(d, cc);
+    cc = face(L.ky, rc[c], ryp[c]); if (!kZero) rho_acc32(cc, pyp[c], s, d); else d = __fadd_rn(d, cc);
+    cc = face(L.kz, rc[c], rzm[c]); if (!kZero) rho_acc32(cc, pzm[c], s, d); else d = __fadd_rn(d, cc);
+    cc = face(L.kz, rc[c], rzp[c]); if (!kZero) rho_acc32(cc, pzp[c], s, d); else d = __fadd_rn(d, cc);
+    out[c] = rho_relax32(s, b[c], d);
   }
   st4(L.sol + own, make_float4(out[0], out[1], out[2], out[3]));
 }
@@ -272,13 +272,13 @@ __global__ void __launch_bounds__(32 * BY) k_smooth_split4z(LevelView<float> L, 
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       float s = 0.f, d = 0.f, cc;
-      cc = face(L.kx, rc[c], rxm[c]); if (!kZero) s += cc * pxm[c]; d += cc;
-      cc = face(L.kx, rc[c], rxp[c]); if (!kZero) s += cc * pxp[c]; d += cc;
-      cc = face(L.ky, rc[c], rym_[c]); if (!kZero) s += cc * pym_[c]; d += cc;
-      cc = face(L.ky, rc[c], ryp_[c]); if (!kZero) s += cc * pyp_[c]; d += cc;
-      cc = face(L.kz, rc[c], rzm[c]); if (!kZero) s += cc * pzm[c]; d += cc;
-      cc = face(L.kz, rc[c], rzp[c]); if (!kZero) s += cc * pzp[c]; d += cc;
-      out[c] = rho_update(s - b[c], d);
+      cc = face(L.kx, rc[c], rxm[c]); if (!kZero) rho_acc32(cc, pxm[c], s, d); else d = __fadd_rn(d, cc);
+      cc = face(L.kx, rc[c], rxp[c]); if (!kZero) rho_acc32(cc, pxp[c], s, d); else d = __fadd_rn(d, cc);
+      cc = face(L.ky, rc[c], rym_[c]); if (!kZero) rho_acc32(cc, pym_[c], s, d); else d = __fadd_rn(d, cc);
+      cc = face(L.ky, rc[c], ryp_[c]); if (!kZero) rho_acc32(cc, pyp_[c], s, d); else d = __fadd_rn(d, cc);
+      cc = face(L.kz, rc[c], rzm[c]); if (!kZero) rho_acc32(cc, pzm[c], s, d); else d = __fadd_rn(d, cc);
+      cc = face(L.kz, rc[c], rzp[c]); if (!kZero) rho_acc32(cc, pzp[c], s, d); else d = __fadd_rn(d, cc);
+      out[c] = rho_relax32(s, b[c], d);
     }
     if (act) st4(pown + hk, make_float4(out[0], out[1], out[2], out[3]));
     rm = rc4; pm = pc4;

@@ -71,12 +71,20 @@ __device__ __forceinline__ void stencil_rho(const LevelView<T>& L, const T* __re
   T c;
   s = T(0);
   d = T(0);
-  if (i > 0) { c = rho_face(L.kx, rc, r[q - 1]); s += c * p[q - 1]; d += c; }
-  if (i < L.nx - 1) { c = rho_face(L.kx, rc, r[q + 1]); s += c * p[q + 1]; d += c; }
-  if (j > 0) { c = rho_face(L.ky, rc, r[q - sy]); s += c * p[q - sy]; d += c; }
-  if (j < L.ny - 1) { c = rho_face(L.ky, rc, r[q + sy]); s += c * p[q + sy]; d += c; }
-  if (k > 0) { c = rho_face(L.kz, rc, r[q - sz]); s += c * p[q - sz]; d += c; }
-  if (k < L.nz - 1) { c = rho_face(L.kz, rc, r[q + sz]); s += c * p[q + sz]; d += c; }
+  const auto acc = [&](T cc, T pn) {
+    if constexpr (std::is_same<T, float>::value) {
+      rho_acc32(cc, pn, s, d);
+    } else {
+      s += cc * pn;
+      d += cc;
+    }
+  };
+  if (i > 0) { c = rho_face(L.kx, rc, r[q - 1]); acc(c, p[q - 1]); }
+  if (i < L.nx - 1) { c = rho_face(L.kx, rc, r[q + 1]); acc(c, p[q + 1]); }
+  if (j > 0) { c = rho_face(L.ky, rc, r[q - sy]); acc(c, p[q - sy]); }
+  if (j < L.ny - 1) { c = rho_face(L.ky, rc, r[q + sy]); acc(c, p[q + sy]); }
+  if (k > 0) { c = rho_face(L.kz, rc, r[q - sz]); acc(c, p[q - sz]); }
+  if (k < L.nz - 1) { c = rho_face(L.kz, rc, r[q + sz]); acc(c, p[q + sz]); }
 }
 
 // The diagonal sum_f coe_f alone (same order as stencil_rho).
@@ -86,12 +94,16 @@ __device__ __forceinline__ T diag_rho(const LevelView<T>& L, int i, int j, int k
   const T* __restrict__ r = L.rho;
   const T rc = r[q];
   T d = T(0);
-  if (i > 0) d += rho_face(L.kx, rc, r[q - 1]);
-  if (i < L.nx - 1) d += rho_face(L.kx, rc, r[q + 1]);
-  if (j > 0) d += rho_face(L.ky, rc, r[q - sy]);
-  if (j < L.ny - 1) d += rho_face(L.ky, rc, r[q + sy]);
-  if (k > 0) d += rho_face(L.kz, rc, r[q - sz]);
-  if (k < L.nz - 1) d += rho_face(L.kz, rc, r[q + sz]);
+  const auto add = [&](T cc) {
+    if constexpr (std::is_same<T, float>::value) d = __fadd_rn(d, cc);
+    else d += cc;
+  };
+  if (i > 0) add(rho_face(L.kx, rc, r[q - 1]));
+  if (i < L.nx - 1) add(rho_face(L.kx, rc, r[q + 1]));
+  if (j > 0) add(rho_face(L.ky, rc, r[q - sy]));
+  if (j < L.ny - 1) add(rho_face(L.ky, rc, r[q + sy]));
+  if (k > 0) add(rho_face(L.kz, rc, r[q - sz]));
+  if (k < L.nz - 1) add(rho_face(L.kz, rc, r[q + sz]));
   return d;
 }
 
@@ -145,10 +157,14 @@ __device__ __forceinline__ void smooth_cell(const LevelView<T>& L, int i, int j,
   } else {
     stencil<T, kCg>(L, L.sol, i, j, k, q, s, d);
   }
-  const T v = s - ldc<kCg>(L.src + q);
-  if (kIdiag) L.sol[q] = v * L.idiag[q];
-  else if (kRho) L.sol[q] = rho_update(v, d);
-  else L.sol[q] = v / d;
+  if constexpr (kRho && std::is_same<T, float>::value) {
+    L.sol[q] = rho_relax32(s, ldc<kCg>(L.src + q), d);
+  } else {
+    const T v = s - ldc<kCg>(L.src + q);
+    if (kIdiag) L.sol[q] = v * L.idiag[q];
+    else if (kRho) L.sol[q] = rho_update(v, d);
+    else L.sol[q] = v / d;
+  }
 }
 
 
