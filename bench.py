@@ -792,13 +792,17 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
     J = |p - p_t|^2/2 with FP64 solves (step 1e-6, 16 random unit directions
     of phi) against the mixed-precision gradient, and the same gradient from
     FP64 solves (the finite differences of FP64 solves at 1e-12 carry noise
-    near 1e-6 themselves: both gradients agree with them equally).  Flexible GMRES around the
+    near 1e-6 themselves: both gradients agree with them equally).  The same
+    central differences are also formed from their parts (gradcheck:
+    p(phi - h v) and the solve for p(phi + h v) - p(phi - h v)), which removes
+    that cancellation noise.  Flexible GMRES around the
     V-cycle by default: on the smooth adjoint right-hand side p - p_t flexible
     CG first raises the residual many-fold and needs 32 iterations against 20."""
     import torch
 
     from fortrancfd_gb300 import PressurePoisson, inputs
     from fortrancfd_gb300.autograd import pressure_solve
+    from fortrancfd_gb300.gradcheck import central_difference
 
     case = inputs.config(3, scale)
     kw = dict(eps=case.eps, rho_pos=case.rho_pos, rho_neg=case.rho_neg)
@@ -841,7 +845,7 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
             return 0.5 * ((q - p_t) ** 2).sum()
 
         rng = np.random.default_rng(7)
-        errs, errs64 = [], []
+        errs, errs64, errs_x = [], [], []
         with torch.no_grad():
             for _ in range(16):
                 v = torch.from_numpy(rng.standard_normal(case.shape)).to(dev)
@@ -849,6 +853,9 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
                 fd = float((J(phi + 1e-6 * v) - J(phi - 1e-6 * v)) / 2e-6)
                 errs.append(abs(fd - float((g * v).sum())) / abs(fd))
                 errs64.append(abs(float(((g - g64) * v).sum())) / abs(float((g64 * v).sum())))
+                # the same central difference from its parts (no cancellation)
+                fdx = central_difference(s64, phi, b, p_t, v, 1e-6, **kw)
+                errs_x.append(abs(fdx - float((g * v).sum())) / abs(fdx))
         s.close()
         s64.close()
     f, bk = float(np.median(fw)), float(np.median(bw))
@@ -860,6 +867,8 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
             "forward_iterations": fwd_cycles, "adjoint_iterations": adj_cycles,
             "fd_max_rel_err": max(errs), "fd_median_rel_err": float(np.median(errs)),
             "fd_directions": len(errs),
+            "fd_exact_max_rel_err": max(errs_x),
+            "fd_exact_median_rel_err": float(np.median(errs_x)),
             "fp64_gradient_max_rel_diff": max(errs64),
             "fp64_gradient_rel_l2_diff": float((g - g64).norm() / g64.norm())}
 
@@ -1133,6 +1142,8 @@ def scalar_summary(fp64, parity, adj, multi, roll, tstep):
     put("adj_fd_max_rel", adj, "fd_max_rel_err")
     put("adj_fd_median_rel", adj, "fd_median_rel_err")
     put("adj_fd_directions", adj, "fd_directions")
+    put("adj_fd_exact_max_rel", adj, "fd_exact_max_rel_err")
+    put("adj_fd_exact_median_rel", adj, "fd_exact_median_rel_err")
     put("adj_vs_fp64_gradient_max_rel", adj, "fp64_gradient_max_rel_diff")
     put("error_adjoint", adj, "error")
     put("rollout_forward_ms", roll, "forward_ms")

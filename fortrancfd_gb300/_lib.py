@@ -21,6 +21,9 @@ GBMG_STATE_ERROR = 7
 
 GBMG_PREC_FP64 = 0
 GBMG_PREC_MIXED = 1
+GBMG_STOP_RELATIVE = 0
+GBMG_STOP_RMS = 1
+GBMG_STOP_INCREMENT = 2
 GBMG_MEM_HOST = 0
 GBMG_MEM_DEVICE = 1
 
@@ -51,14 +54,15 @@ class Params(C.Structure):
     _fields_ = [("precision", C.c_int32), ("nu1", C.c_int32), ("nu2", C.c_int32),
                 ("levels", C.c_int32), ("coarse_max", C.c_int32), ("max_cycles", C.c_int32),
                 ("krylov", C.c_int32), ("use_graph", C.c_int32), ("remove_rhs_mean", C.c_int32),
-                ("certify", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p)]
+                ("certify", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
+                ("stop_rule", C.c_int32), ("zero_wall_faces", C.c_int32)]
 
 
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int32), ("cycles", C.c_int32), ("levels", C.c_int32),
                 ("coarse_n", C.c_int32), ("rel_residual", C.c_double),
                 ("rms_residual", C.c_double), ("res0", C.c_double), ("ms", C.c_double),
-                ("bytes", C.c_double)]
+                ("bytes", C.c_double), ("increment", C.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

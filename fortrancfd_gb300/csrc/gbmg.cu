@@ -41,7 +41,6 @@ struct Level {
   float *sol32 = nullptr, *src32 = nullptr;
   float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
   float* buf_a = nullptr;  // the buffer sol32 pointed to at allocation
-  SweepMaps* tmaps = nullptr;  // TMA maps with p = buffer A and p = buffer B (host memory)
   // FP32 kernels take the coefficients from this density instead of cx32..cz32
   // (finest level of a mixed solve whose operator came from rho or phi)
   const float* rho32 = nullptr;
@@ -49,8 +48,6 @@ struct Level {
   int split = 0;  // sol32, src32 and rho32 in the colour-split layout
   size_t hstride = 0;  // distance between the colour halves (elements)
   int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
-  int zmarch = 0, zc = 16;  // z-marching colour sweep of the split level (LevelView)
-  int minb = 0;             // register bound of the split level's colour sweep (LevelView)
   int fsweep = 0;  // the split level sweeps with one launch per sweep (k_sweep_split)
 };
 
@@ -96,19 +93,8 @@ struct gbmg_handle {
   float2* bw = nullptr;
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
-  int fused_levels = 0;  // FP32 levels [0, fused_levels) sweep with the fused kernel
-  // FP32 levels [fused_lo, fused_hi) above the bottom block sweep with the
-  // fused kernel, fused_kz z planes per block (GBMG_FUSED_COARSE = number of
-  // levels from level 1, GBMG_FUSED_KZ)
-  int fused_lo = 0, fused_hi = 0, fused_kz = 4;
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
-  bool sub_cluster = false;  // ... on a thread-block cluster (k_cluster_cycle)
-  int cl_ranks = 8;          // blocks of that cluster
-  int cl_single = 4096;      // its levels of at most this many cells run whole in block 0
-  int* derr = nullptr;   // device error flags (TMA wait and grid barrier timeouts)
-  unsigned* bar = nullptr;  // grid barrier of the mid-cycle kernel: arrivals, generation
-  bool mid_ok = false;      // middle levels in one cooperative launch
-  int mid_grid = 0;         // its block count (all resident)
+  int* derr = nullptr;   // device error flags (bulk-copy wait timeouts)
   DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B],
                                 // then [p buffer] with a colour-split e (buffer A)
   bool dmaps_split = false;     // whether the colour-split entries were made
@@ -261,9 +247,6 @@ LevelView<float> v32(const Level& l) {
   LevelView<float> v{l.nx, l.ny, l.nz, l.fx, l.fy, l.fz, l.cx32, l.cy32, l.cz32, nullptr,
                      l.sol32, l.src32, l.rho32, l.k32[0], l.k32[1], l.k32[2], l.split,
                      l.hstride};
-  v.zmarch = l.zmarch;
-  v.zc = l.zc;
-  v.minb = l.minb;
   return v;
 }
 template <typename T>
@@ -297,10 +280,11 @@ template <typename T> const T* adense_of(const gbmg_handle* h);
 template <> const double* adense_of<double>(const gbmg_handle* h) { return h->adense; }
 template <> const float* adense_of<float>(const gbmg_handle* h) { return h->adense32; }
 
-// One red-black sweep of level l.  FP64: two colour launches in place.
-// FP32: one fused launch out of place, after which the level's solution lives
-// in the other buffer (the host swaps the pointers; graph capture records the
-// resulting sequence, which replays identically).
+// One red-black sweep of level l: two colour launches in place, except on the
+// colour-split FP32 finest level, which sweeps in one launch out of place
+// (after which its solution lives in the other buffer: the host swaps the
+// pointers, and graph capture records the resulting sequence, which replays
+// identically).
 // zero_guess: the level's values are taken as zero (its first sweep after the
 // coarse unknown was started at zero, or the finest level of a correction
 // cycle), so no memset is needed and the first colour does not read p.
@@ -318,24 +302,11 @@ void sweep<double>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
 template <>
 void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   Level& lv = h->lv[l];
-  const LevelView<float> V = v32(lv);
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-  const bool fused = h->fused_levels > l || (l >= h->fused_lo && l < h->fused_hi);
-  if (zero_guess && (lv.tmaps || fused))  // out-of-place sweeps read p
-    cudaMemsetAsync(lv.sol32, 0, lv.n * sizeof(float), h->stream);
   if (lv.fsweep) {
-    // the colour-split finest level: a whole sweep per launch, out of place
-    // (from a zero guess it reads no p at all)
+    // from a zero guess the one-launch sweep reads no p at all
     LAUNCH(h, cs, launch_sweep_split(h->stream, v32(lv), lv.sol32, lv.alt32, first_color,
                                      zero_guess, h->derr));
-    std::swap(lv.sol32, lv.alt32);
-  } else if (lv.tmaps) {
-    const SweepMaps& m = lv.tmaps[lv.sol32 == lv.buf_a ? 0 : 1];
-    LAUNCH(h, cs, launch_smooth_tma(h->stream, m, lv.nx, lv.ny, lv.nz, lv.alt32, first_color, h->derr));
-    std::swap(lv.sol32, lv.alt32);
-  } else if (fused) {
-    LAUNCH(h, cs, launch_smooth_fused<float>(h->stream, V, lv.sol32, lv.alt32, first_color,
-                                             l == 0 ? 0 : h->fused_kz));
     std::swap(lv.sol32, lv.alt32);
   } else {
     LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), first_color, zero_guess));
@@ -376,22 +347,6 @@ SubCycle<T> make_subcycle(gbmg_handle* h, bool reverse) {
   return S;
 }
 
-// Levels 1 .. top-1 and the bottom block as one cooperative launch.
-template <typename T>
-MidCycle<T> make_midcycle(gbmg_handle* h, bool reverse) {
-  MidCycle<T> M{};
-  const int top = h->sub_lc;
-  M.nmid = top - 1;
-  for (int i = 0; i <= M.nmid; ++i) M.lv[i] = view<T>(h->lv[1 + i]);
-  M.bottom = make_subcycle<T>(h, reverse);
-  M.nu1 = h->prm.nu1;
-  M.nu2 = h->prm.nu2;
-  M.reverse = reverse ? 1 : 0;
-  M.bar = h->bar;
-  M.err = h->derr;
-  return M;
-}
-
 // One V-cycle on the current level-0 (sol, src) of type T.  reverse_post runs
 // the post-smoothing colours black-first (symmetric preconditioner for CG).
 // zero_fine: the level-0 unknown starts at zero (correction and Krylov
@@ -402,39 +357,13 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
   const cudaStream_t s = h->stream;
   const bool pre = h->prm.nu1 > 0;
   const int top = std::min(h->sub_lc, L - 1);  // levels above the bottom block
-  if (h->mid_ok) {
-    // finest level by its own kernels, the rest in one cooperative launch
-    for (int it = 0; it < h->prm.nu1; ++it) sweep<T>(h, 0, 0, it == 0 && zero_fine);
-    LAUNCH(h, GBMG_PROF_RESTRICT_FINE,
-           launch_restrict<T>(s, view_next<T>(h->lv[0]), view<T>(h->lv[1]), !pre));
-    cudaError_t e = cudaSuccess;
-    LAUNCH(h, GBMG_PROF_SMOOTH_COARSE,
-           e = launch_midcycle<T>(s, make_midcycle<T>(h, reverse_post), h->mid_grid));
-    if (e != cudaSuccess) {
-      h->err = std::string("mid-cycle launch: ") + cudaGetErrorString(e);
-      return GBMG_CUDA_ERROR;
-    }
-    LAUNCH(h, GBMG_PROF_PROLONG_FINE,
-           launch_prolong<T>(s, view_next<T>(h->lv[0]), view<T>(h->lv[1])));
-    for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, 0, reverse_post ? 1 : 0, false);
-    return check_launch(h, "v-cycle");
-  }
   for (int l = 0; l < top; ++l) {
     for (int it = 0; it < h->prm.nu1; ++it)
       sweep<T>(h, l, 0, it == 0 && (l > 0 || zero_fine));
     LAUNCH(h, l == 0 ? GBMG_PROF_RESTRICT_FINE : GBMG_PROF_RESTRICT_COARSE,
            launch_restrict<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1]), !pre));
   }
-  if (h->sub_lc < L && h->sub_cluster) {
-    cudaError_t e = cudaSuccess;
-    LAUNCH(h, GBMG_PROF_COARSE_SOLVE,
-           e = launch_cluster_cycle<T>(s, make_cluster_cycle(make_subcycle<T>(h, reverse_post),
-                                                              h->cl_ranks, h->cl_single)));
-    if (e != cudaSuccess) {
-      h->err = std::string("cluster bottom-cycle launch: ") + cudaGetErrorString(e);
-      return GBMG_CUDA_ERROR;
-    }
-  } else if (h->sub_lc < L) {
+  if (h->sub_lc < L) {
     LAUNCH(h, GBMG_PROF_COARSE_SOLVE, launch_subcycle<T>(s, make_subcycle<T>(h, reverse_post)));
   } else {
     const LevelView<T> C = view<T>(h->lv[L - 1]);
@@ -504,8 +433,6 @@ int free_all(gbmg_handle* h) {
     dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
     if (l > 0) { dfree(v.sol); dfree(v.src); }
     dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.alt32); dfree(v.src32);
-    delete[] v.tmaps;
-    v.tmaps = nullptr;
   }
   dfree(h->b); dfree(h->p); dfree(h->rho); dfree(h->rho32);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
@@ -515,7 +442,6 @@ int free_all(gbmg_handle* h) {
   dfree(h->gmV); dfree(h->gmZ); dfree(h->gmPart); dfree(h->gmDev);
   if (h->gmHost) cudaFreeHost(h->gmHost);
   dfree(h->minv); dfree(h->adense); dfree(h->cwork); dfree(h->minv32); dfree(h->adense32); dfree(h->derr);
-  dfree(h->bar);
   for (int i = 0; i < 48; ++i) dfree(h->ns_buf[i]);
   delete[] h->dmaps;
   h->dmaps = nullptr;
@@ -535,46 +461,14 @@ int free_all(gbmg_handle* h) {
   return GBMG_OK;
 }
 
-// TMA-fed sweeps on the FP32 levels with at least 2^15 cells and rows a
-// multiple of 16 bytes (GBMG_TMA_LEVELS overrides how many finest levels).
 // The one-block bottom of the cycle: the first level >= 1 with at most
-// kSubMaxCells cells and at least one coarser level below it.
-//
-// The bottom runs on a thread-block cluster instead (GBMG_CLUSTER=1; the
-// opt-in cooperative mid-cycle needs the one-block bottom), from the first
-// level >= 1 with at most kClusterMaxCells cells, when that level has at
-// least as many z planes as the cluster has blocks and the cluster fits:
-// GBMG_CLUSTER_RANKS blocks (default 8, at most 16), levels of at most
-// GBMG_CLUSTER_SINGLE cells (default 4096) whole in block 0.
+// kSubMaxCells cells and at least one coarser level below it
+// (GBMG_SUBCYCLE=0 runs those levels as separate launches instead).
 template <typename T>
 void setup_subcycle(gbmg_handle* h) {
   h->sub_lc = h->L;
-  h->sub_cluster = false;
   if (const char* e = std::getenv("GBMG_SUBCYCLE"))
     if (std::atoi(e) == 0) return;
-  bool cluster = false;
-  if (const char* e = std::getenv("GBMG_CLUSTER")) cluster = std::atoi(e) != 0;
-  if (const char* e = std::getenv("GBMG_MIDCYCLE")) cluster = cluster && std::atoi(e) == 0;
-  if (const char* e = std::getenv("GBMG_CLUSTER_RANKS"))
-    h->cl_ranks = std::min(kClusterMaxRanks, std::max(1, std::atoi(e)));
-  if (const char* e = std::getenv("GBMG_CLUSTER_SINGLE")) h->cl_single = std::max(0, std::atoi(e));
-  if (cluster) {
-    for (int l = 1; l + 1 < h->L; ++l)
-      if (h->lv[l].n <= (size_t)kClusterMaxCells && h->L - l <= kSubMaxLevels) {
-        if (h->lv[l].nz >= h->cl_ranks) {
-          h->sub_lc = l;
-          const ClusterCycle<T> P =
-              make_cluster_cycle(make_subcycle<T>(h, false), h->cl_ranks, h->cl_single);
-          const size_t smem = cluster_smem<T>(P);
-          if (smem <= 200 * 1024 && cluster_init<T>(smem, h->cl_ranks) == 0) {
-            h->sub_cluster = true;
-            return;
-          }
-          h->sub_lc = h->L;
-        }
-        break;
-      }
-  }
   for (int l = 1; l + 1 < h->L; ++l)
     if (h->lv[l].n <= (size_t)kSubMaxCells && h->L - l <= kSubMaxLevels) {
       h->sub_lc = l;
@@ -586,39 +480,9 @@ void setup_subcycle(gbmg_handle* h) {
   if (smem > 200 * 1024 || subcycle_init<T>(smem) != 0) h->sub_lc = h->L;
 }
 
-// The cooperative mid-cycle: levels strictly between the finest and the
-// bottom block (at least one of them).  Opt-in (GBMG_MIDCYCLE=1): on the 256^3
-// benchmark it measured 263 us per cycle against about 150 us for the same
-// levels as separate launches overlapped by programmatic dependent launch in
-// the captured graph (its bottom phase runs on one block while the others
-// wait, and each of its ~36 phases ends in a grid barrier).
-template <typename T>
-int setup_midcycle(gbmg_handle* h) {
-  h->mid_ok = false;
-  const char* ev = std::getenv("GBMG_MIDCYCLE");
-  if (!ev || std::atoi(ev) == 0) return GBMG_OK;
-  const int nmid = h->sub_lc - 1;
-  if (h->sub_lc >= h->L || nmid < 1 || nmid > kMidMaxLevels) return GBMG_OK;
-  const size_t smem = subcycle_smem<T>(make_subcycle<T>(h, false));
-  int grid = 0;
-  if (midcycle_init<T>(smem, &grid) != 0 || grid < 1) {
-    cudaGetLastError();
-    return GBMG_OK;  // keep the separate launches
-  }
-  if (!h->bar) {
-    GB_TRY(dmalloc(h, &h->bar, 2));
-    GB_CUDA(h, cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), h->stream));
-  }
-  h->mid_grid = grid;
-  h->mid_ok = true;
-  return GBMG_OK;
-}
-
+// TMA maps of the double-word defect kernel (finest level with nx % 4 == 0;
+// GBMG_TMA_DEFECT=0 keeps the plain-load defect kernel).
 int setup_tma(gbmg_handle* h) {
-  // the two-colour FP32 sweep measured faster than the TMA-fed one on GB300
-  // (132 vs 143 us per 256^3 sweep), so the TMA sweep is opt-in
-  int want = 0;
-  if (const char* e = std::getenv("GBMG_TMA_LEVELS")) want = std::atoi(e);
   Level& f = h->lv[0];
   f.buf_a = f.sol32;
   const char* ed = std::getenv("GBMG_TMA_DEFECT");
@@ -633,21 +497,6 @@ int setup_tma(gbmg_handle* h) {
       }
     if (ok) h->dmaps = m;  // the colour-split entries 6, 7 are made by set_rho_form
     else delete[] m;
-  }
-  if (smooth_tma_init() != 0) return GBMG_OK;  // keep the two-colour sweeps
-  for (int l = 0; l < h->L && l < want; ++l) {
-    Level& v = h->lv[l];
-    if (v.nx % 4 != 0 || v.n < (size_t(1) << 15)) continue;
-    SweepMaps* m = new SweepMaps[2];
-    v.buf_a = v.sol32;
-    const bool ok =
-        make_sweep_maps(&m[0], v.sol32, v.src32, v.cx32, v.cy32, v.cz32, v.nx, v.ny, v.nz) &&
-        make_sweep_maps(&m[1], v.alt32, v.src32, v.cx32, v.cy32, v.cz32, v.nx, v.ny, v.nz);
-    if (!ok) {
-      delete[] m;
-      continue;
-    }
-    v.tmaps = m;
   }
   return GBMG_OK;
 }
@@ -711,6 +560,8 @@ int allocate(gbmg_handle* h) {
     GB_TRY(dmalloc(h, &h->cyw, h->n0));
     GB_TRY(dmalloc(h, &h->czw, h->n0));
   }
+  // the FP64 increment rule keeps the previous cycle's p
+  if (h->prm.stop_rule == GBMG_STOP_INCREMENT && !h->mixed) GB_TRY(dmalloc(h, &h->r0, h->n0));
   if (h->prm.krylov) {
     GB_TRY(dmalloc(h, &h->kr, h->n0));
     GB_TRY(dmalloc(h, &h->kz, h->n0));
@@ -746,15 +597,6 @@ int allocate(gbmg_handle* h) {
   if (h->mixed) GB_TRY(setup_tma(h));
   if (h->mixed) setup_subcycle<float>(h);
   else setup_subcycle<double>(h);
-  if (h->mixed) GB_TRY(setup_midcycle<float>(h));
-  else GB_TRY(setup_midcycle<double>(h));
-  if (h->mixed && !h->mid_ok) {
-    if (const char* e = std::getenv("GBMG_FUSED_COARSE")) {
-      h->fused_lo = 1;
-      h->fused_hi = std::max(1, std::min(1 + std::atoi(e), h->sub_lc));
-    }
-    if (const char* e = std::getenv("GBMG_FUSED_KZ")) h->fused_kz = std::max(1, std::atoi(e));
-  }
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
   for (int i = 0; i < 2; ++i) GB_CUDA(h, cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
@@ -850,17 +692,16 @@ void set_rho_form(gbmg_handle* h, bool on) {
   Level& f = h->lv[0];
   // (with the finest level inside the single-block bottom, sub_lc == 0, that
   // block reads stored coefficients and the density form has no user)
-  bool want = on && h->mixed && !f.tmaps && h->fused_levels == 0 && h->sub_lc > 0;
+  bool want = on && h->mixed && h->sub_lc > 0;
   if (const char* e = std::getenv("GBMG_RHO_COEF"))
     if (std::atoi(e) == 0) want = false;
   bool split = want && f.nx % 2 == 0 && h->L > 1 && f.fx == 2 && h->sub_lc > 0;
   if (const char* e = std::getenv("GBMG_SPLIT"))
     if (std::atoi(e) == 0) split = false;
   // the halves sit n/2 + pad apart (pad a multiple of 4 floats: 16-byte
-  // aligned halves for the TMA maps); GBMG_SPLIT_PAD overrides the pad
-  size_t pad = 4128;
-  if (const char* e = std::getenv("GBMG_SPLIT_PAD")) pad = (size_t)std::max(0, std::atoi(e));
-  pad = std::min(pad, kSplitPadMax) & ~size_t(3);
+  // aligned halves for the bulk copies and TMA maps; not a power of two, so
+  // same-offset accesses to both halves fall on different DRAM channels)
+  const size_t pad = 4128;
   const size_t hs = split ? f.n / 2 + pad : 0;
   const float* r = want ? h->rho32 : nullptr;
   if (r != f.rho32 || (int)split != f.split || hs != f.hstride) reset_graphs(h);
@@ -872,22 +713,10 @@ void set_rho_form(gbmg_handle* h, bool on) {
                              f.nx, f.ny, f.nz, hs);
     h->dmaps_split = oks;
   }
-  // z-marching colour sweep of the split level: GBMG_SMOOTH_Z=1 (blocks of
-  // 8 rows) or 2 (16 rows), GBMG_SMOOTH_ZC planes per thread (default 16)
-  int zm = 0, zc = 16;
-  if (const char* e = std::getenv("GBMG_SMOOTH_Z")) zm = std::min(2, std::max(0, std::atoi(e)));
-  if (const char* e = std::getenv("GBMG_SMOOTH_ZC")) zc = std::max(1, std::atoi(e));
-  if (!split) zm = 0;
-  int minb = 0;
-  if (const char* e = std::getenv("GBMG_SMOOTH_MINB")) minb = std::atoi(e);
-  if (zm != f.zmarch || zc != f.zc || minb != f.minb) reset_graphs(h);
-  f.zmarch = zm;
-  f.zc = zc;
-  f.minb = minb;
   // one launch per sweep on the split level: even sweep counts (so that the
   // level's unknown is back in its first buffer wherever the cycle reads it),
   // rows of at most 256 half cells; GBMG_SWEEP=0 keeps the two colour launches
-  bool fs = split && zm == 0 && h->prm.nu1 % 2 == 0 && h->prm.nu2 % 2 == 0 &&
+  bool fs = split && h->prm.nu1 % 2 == 0 && h->prm.nu2 % 2 == 0 &&
             sweep_split_supported(f.nx, f.ny, f.nz, hs) && sweep_split_init() == 0;
   if (const char* e = std::getenv("GBMG_SWEEP"))
     if (std::atoi(e) == 0) fs = false;
@@ -964,14 +793,22 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
   const size_t n = h->n0;
   const int V = GBMG_PROF_VECTOR, R = GBMG_PROF_RESIDUAL;
   const bool zg = h->prm.nu1 > 0;  // zero initial guess handled by the first sweep
+  const bool inc = h->prm.stop_rule == GBMG_STOP_INCREMENT;
   if (kind == kGraphFp64) {
     f.sol = h->p; f.src = h->b;
+    // the increment rule compares p after the cycle with p before it
+    if (inc) GB_CUDA(h, cudaMemcpyAsync(h->r0, h->p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     GB_TRY(enqueue_vcycle<double>(h, false, false));
+    if (inc) LAUNCH(h, V, launch_increment<double>(s, h->p, h->r0, n, 0, h->red, kSlotIncSum, kSlotInc));
     LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
   } else if (kind == kGraphMixed) {
     // e = V-cycle(r) in FP32; p += e and r = b - A p in double-word
     if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
     GB_TRY(enqueue_vcycle<float>(h, false, zg));
+    // the increment rule: the cycle's correction e is p_k - p_(k-1)
+    if (inc)
+      LAUNCH(h, V, launch_increment<float>(s, f.sol32, (const float*)nullptr, n,
+                                           f.split ? f.hstride : 0, h->red, kSlotIncSum, kSlotInc));
     LAUNCH(h, R, enqueue_defect(h, h->pcur, f.sol32, f.src32, kSlotNorm));
   } else {
     // flexible CG: z = M r (one V-cycle from zero), mean-free
@@ -1272,6 +1109,12 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   const bool pcg = h->prm.krylov != 0;
   const int kind = pcg ? (h->mixed ? kGraphPcgMixed : kGraphPcg64) : (h->mixed ? kGraphMixed : kGraphFp64);
   const double scale = bnorm > 0.0 ? bnorm : 1.0;
+  // Stopping rules.  RMS: sqrt(|r|^2/n) < tol is |r|/|b| < tol sqrt(n)/|b|, so
+  // the relative test below runs with that threshold.  INCREMENT: the loop
+  // stops on max |p_k - p_(k-1)| < tol; the residual is only reported.
+  const bool by_inc = h->prm.stop_rule == GBMG_STOP_INCREMENT;
+  if (h->prm.stop_rule == GBMG_STOP_RMS) tol = tol * std::sqrt((double)n) / scale;
+  const double rtol = by_inc ? 0.0 : tol;  // threshold of the residual tests
   bool shifted = false;
   // initial residual
   f.sol = h->p; f.src = h->b;
@@ -1291,7 +1134,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   st->res0 = rel;
   int status = GBMG_NOT_CONVERGED;
   int cyc = 0;
-  if (rel < tol) {
+  if (rel < rtol || r2 == 0.0) {
     status = GBMG_OK;
   } else if (h->prm.krylov == 2) {
     GB_TRY(fgmres(h, tol, scale, &rel, &cyc, &status));
@@ -1313,6 +1156,13 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
         if (!std::isfinite(rel) || rel > 1e3 * std::max(1.0, st->res0)) {
           status = GBMG_DIVERGED;
           break;
+        }
+        if (by_inc) {
+          double dp = 0.0;
+          std::memcpy(&dp, &h->host_res[kSlotInc], sizeof(double));
+          st->increment = dp;
+          if (dp < tol) { status = GBMG_OK; break; }
+          continue;
         }
         if (rel < tol) { status = GBMG_OK; break; }
         // The mixed cycle tracks its residual in double-word FP32; near the
@@ -1348,6 +1198,16 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
       h->dl_started = true;
     }
     if (!(kind == kGraphMixed && h->prm.certify)) break;
+    if (by_inc) {
+      // reported only: the increment decided
+      f.sol = h->p; f.src = h->b;
+      LAUNCH(h, GBMG_PROF_CERTIFY,
+             launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
+      GB_TRY(check_launch(h, "certify"));
+      GB_TRY(read_result(h, kSlotNorm, &r2));
+      rel = std::sqrt(r2) / scale;
+      break;
+    }
     // the loop tracked the residual in double-word; restate it in native FP64
     f.sol = h->p; f.src = h->b;
     LAUNCH(h, GBMG_PROF_CERTIFY,
@@ -1376,10 +1236,8 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     GB_CUDA(h, cudaMemcpyAsync(&flags, h->derr, sizeof(int), cudaMemcpyDeviceToHost, s));
     GB_CUDA(h, cudaStreamSynchronize(s));
     if (flags) {
-      h->err = (flags & 2) ? "the grid barrier of the mid-cycle kernel timed out"
-                           : "a TMA wait timed out inside the sweep kernel";
+      h->err = "a bulk-copy wait timed out inside a kernel of the cycle";
       cudaMemsetAsync(h->derr, 0, sizeof(int), s);
-      if (h->bar) cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), s);  // arrivals left over
       return GBMG_CUDA_ERROR;
     }
   }
@@ -1439,6 +1297,19 @@ int stage_velocity(gbmg_handle* h, const gbmg_field* const fv[3], bool has_w, in
   return GBMG_OK;
 }
 
+// RHSP's wall-normal faces set to zero on the device copies of u, v, w
+// (gbmg_params.zero_wall_faces; nothing otherwise).
+int zero_walls(gbmg_handle* h, const gbmg_field dfield[3], bool has_w) {
+  if (!h->prm.zero_wall_faces) return GBMG_OK;
+  const gbmg_grid& g = h->grid;
+  launch_zero_wall_faces(h->stream, g.nx, g.ny, g.nz, dfield[0].data, dfield[0].sy, dfield[0].sz,
+                         dfield[1].data, dfield[1].sy, dfield[1].sz,
+                         has_w ? dfield[2].data : nullptr, has_w ? dfield[2].sy : 0,
+                         has_w ? dfield[2].sz : 0);
+  h->launches += 1;
+  return check_launch(h, "zero_wall_faces");
+}
+
 // The projection on device face velocities (fields addressed at their face
 // (0,0,0)) with the initial pressure already in h->p: b = div(u*)/dt, the
 // solve, then u -= dt beta grad p (ppe_sor_solver + ns_momentum_correction).
@@ -1450,6 +1321,7 @@ int project_device(gbmg_handle* h, const gbmg_field dfield[3], bool has_w, doubl
   Strided sv{dfield[1].data, dfield[1].sy, dfield[1].sz};
   Strided sw{has_w ? dfield[2].data : nullptr, has_w ? dfield[2].sy : 0,
              has_w ? dfield[2].sz : 0};
+  GB_TRY(zero_walls(h, dfield, has_w));
   launch_divergence(s, g.nx, g.ny, g.nz, su, sv, sw, g.dx, g.dy, g.dz, dt, h->b);
   h->launches += 1;
   GB_TRY(check_launch(h, "divergence"));
@@ -1556,8 +1428,6 @@ int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* 
     *rcp[i] = 1.0 / dvs[i];
     if (!fdiv_divisor_ok(dvs[i])) a.fast = 0;
   }
-  // GBMG_NS_DIVIDE=1: IEEE divisions throughout (the same doubles, slower)
-  if (const char* e = std::getenv("GBMG_NS_DIVIDE")) a.fast = a.fast && std::atoi(e) == 0;
   a.scheme = prm->adv_scheme;
   if (a.scheme != 0 && a.scheme != 1) {
     h->err = "adv_scheme must be 0 (second-order upwind) or 1 (QUICK)";
@@ -1765,7 +1635,10 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
   if (prm) h->prm = *prm; else gbmg_default_params(&h->prm);
   if (h->prm.nu1 < 0 || h->prm.nu2 < 0 || h->prm.max_cycles < 1 || h->prm.coarse_max < 1 ||
       h->prm.coarse_max > kMaxCoarse || (h->prm.precision != GBMG_PREC_FP64 &&
-                                         h->prm.precision != GBMG_PREC_MIXED)) {
+                                         h->prm.precision != GBMG_PREC_MIXED) ||
+      h->prm.stop_rule < GBMG_STOP_RELATIVE || h->prm.stop_rule > GBMG_STOP_INCREMENT ||
+      (h->prm.stop_rule == GBMG_STOP_INCREMENT && h->prm.krylov != 0) ||
+      (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1)) {
     delete h;
     return GBMG_INVALID_ARG;
   }
@@ -2013,6 +1886,7 @@ int gbmg_project_split(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w,
   GB_TRY(upload(h, p_hat, g.nx, g.ny, g.nz, mem, h->aux[0]));
   Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
   Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
+  GB_TRY(zero_walls(h, dfield, has_w));
   launch_psplit_rhs(s, g.nx, g.ny, g.nz, h->rho, su, sv, sw, h->aux[0], h->split_rho12, g.dx,
                     g.dy, g.dz, dt, h->b);
   h->launches += 1;
@@ -2069,6 +1943,17 @@ int gbmg_divergence(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, do
       GB_TRY(upload(h, *fv[a], ext[a][0], ext[a][1], ext[a][2], mem, h->vel[a]));
       sd[a] = Strided{h->vel[a], ext[a][0], (int64_t)ext[a][0] * ext[a][1]};
     }
+  }
+  if (h->prm.zero_wall_faces) {
+    const gbmg_field df[3] = {{const_cast<double*>(sd[0].data), sd[0].sy, sd[0].sz},
+                              {const_cast<double*>(sd[1].data), sd[1].sy, sd[1].sz},
+                              {const_cast<double*>(sd[2].data), sd[2].sy, sd[2].sz}};
+    GB_TRY(zero_walls(h, df, has_w));
+    if (mem != GBMG_MEM_DEVICE)  // the caller's host arrays get the zeros too
+      for (int a = 0; a < 3; ++a) {
+        if (a == 2 && !has_w) continue;
+        GB_TRY(download(h, sd[a].data, ext[a][0], ext[a][1], ext[a][2], mem, *fv[a]));
+      }
   }
   launch_divergence(h->stream, g.nx, g.ny, g.nz, sd[0], sd[1], sd[2], g.dx, g.dy, g.dz, dt, h->b);
   h->launches += 1;

@@ -43,12 +43,6 @@ struct LevelView {
   // on the finest level alternate direction, so each starts on the planes the
   // previous one touched last, which are still in L2
   int zrev = 0;
-  // finest-level sweep marching over chunks of zc z planes per thread
-  // (k_smooth_split4z): 0 off, 1 blocks of 8 rows, 2 blocks of 16 rows
-  int zmarch = 0, zc = 16;
-  // resident blocks per SM requested from the compiler for the finest-level
-  // colour sweep (0: its own register choice)
-  int minb = 0;
 };
 
 // Deterministic single-pass grid reduction scratch: per-block partial sums,
@@ -71,6 +65,8 @@ enum : int {
   kSlotMax = 6,      // max |div| (bit pattern, atomicMax)
   kSlotDot = 8,      // Krylov dot products (2 values)
   kSlotDot2 = 10,
+  kSlotInc = 12,     // max |p_k - p_(k-1)| of the last cycle (bit pattern, atomicMax)
+  kSlotIncSum = 14,  // sum of p_k - p_(k-1) (its mean is removed first)
 };
 
 // ---- the bottom of the cycle in one block (subcycle.cu) ----------------------
@@ -95,50 +91,6 @@ struct SubCycle {
   const T* minv;
   const T* adense;
 };
-// The bottom of the cycle from a level of up to kClusterMaxCells cells on one
-// thread-block cluster of `ranks` blocks (subcycle.cu): the finer levels split
-// by z planes over the blocks, the coarsest ones ("single" levels, at most
-// `single_cells` cells) whole in block 0.
-constexpr int kClusterMaxRanks = 16;
-constexpr int kClusterMaxCells = 32768;
-template <typename T>
-struct ClusterCycle {
-  SubCycle<T> S;               // levels, global arrays, coarse inverse (S.off unused)
-  int ranks;                   // blocks of the cluster
-  int nsplit;                  // levels [0, nsplit) split by planes, the rest in block 0
-  int pz[kSubMaxLevels];       // z planes per block of each level (nz for a single level)
-  int lpz[kSubMaxLevels];      // log2(pz), or -1 when pz is not a power of two
-  int off[kSubMaxLevels + 1];  // shared-memory offset (elements) of each level's
-                               // sol, src, cx, cy, cz; off[nlev]: coarse scratch
-};
-template <typename T>
-ClusterCycle<T> make_cluster_cycle(const SubCycle<T>& S, int ranks, int single_cells);
-template <typename T>
-size_t cluster_smem(const ClusterCycle<T>& P);
-template <typename T>
-int cluster_init(size_t smem, int ranks);
-template <typename T>
-cudaError_t launch_cluster_cycle(cudaStream_t s, const ClusterCycle<T>& P);
-// The middle levels (between the finest and the bottom block) in one
-// cooperative launch (subcycle.cu).
-constexpr int kMidMaxLevels = 8;
-constexpr int kMidThreads = 512;
-template <typename T>
-struct MidCycle {
-  int nmid;                          // middle levels, lv[0 .. nmid-1], finest first
-  LevelView<T> lv[kMidMaxLevels + 1];  // ... and lv[nmid], the bottom's top level
-  SubCycle<T> bottom;                // the single-block bottom, from lv[nmid] down
-  int nu1, nu2, reverse;
-  unsigned* bar;                     // grid barrier: arrivals, generation
-  int* err;                          // device error flags
-};
-template <typename T>
-size_t midcycle_smem(const MidCycle<T>& M);
-template <typename T>
-int midcycle_init(size_t smem, int* grid_blocks);
-template <typename T>
-cudaError_t launch_midcycle(cudaStream_t s, const MidCycle<T>& M, int grid_blocks);
-
 template <typename T>
 size_t subcycle_smem(const SubCycle<T>& S);
 template <typename T>
@@ -151,22 +103,6 @@ void launch_subcycle(cudaStream_t s, const SubCycle<T>& S);
 // the first sweep after the coarse unknown was started at zero)
 template <typename T>
 void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_guess = false);
-// TMA descriptors of one FP32 level for the TMA-fed sweep (smooth_tma.cu).
-struct SweepMaps {
-  CUtensorMap p, b, cx, cy, cz;
-};
-bool make_sweep_maps(SweepMaps* m, const float* p, const float* b, const float* cx,
-                     const float* cy, const float* cz, int nx, int ny, int nz);
-int smooth_tma_init();
-// One whole red-black sweep, p (from maps.p) -> pout; *err |= 1 on a TMA wait timeout.
-void launch_smooth_tma(cudaStream_t s, const SweepMaps& maps, int nx, int ny, int nz, float* pout,
-                       int first_color, int* err);
-
-// One whole red-black sweep, out of place (smooth_fused.cu); first_color 0 =
-// red first.  Instantiated for float.
-template <typename T>
-void launch_smooth_fused(cudaStream_t s, const LevelView<T>& L, const T* pin, T* pout,
-                         int first_color, int planes = 0);  // planes per block, 0 = 32
 // zero_sol: also set the coarse unknown to zero (not needed when its first
 // sweep starts from a zero guess)
 template <typename T>
@@ -278,6 +214,16 @@ void launch_adjoint(cudaStream_t s, int nx, int ny, int nz, double dx2, double d
                     double eps, double rpos, double rneg, double* grad_rho, double* grad_phi);
 void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                       double dx, double dy, double dz, const ReduceScratch& R);
+// The mean-free increment of a cycle: d = x - y (y null: d = x) over the
+// cells (colour-split when hstride > 0); R.result[slot_sum] <- sum d,
+// R.result[slot_out] <- max |d - mean d| (bit pattern of a non-negative double)
+template <typename T>
+void launch_increment(cudaStream_t s, const T* x, const T* y, size_t n, size_t hstride,
+                      const ReduceScratch& R, int slot_sum, int slot_out);
+// u at f = 0 and nx, v at 0 and ny, w (if not null) at 0 and nz set to zero
+void launch_zero_wall_faces(cudaStream_t s, int nx, int ny, int nz, double* u, int64_t usy,
+                            int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w,
+                            int64_t wsy, int64_t wsz);
 // slot <- sum x, slot+1 <- sum x^2
 void launch_sum(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot);
 // y = x - result[slot]/n ; result[slot2] <- sum y^2 (slot2 < 0: no norm)

@@ -16,6 +16,8 @@
 // coefficients of ppe_sor_init ("Two phase flows/newOpenMP/3D+IBM/src/
 // ns_solver/ns_ppe_solver.f90:1-65"): differences first, so each term's
 // rounding is relative to a flux, not to |p|.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 #include "dword.cuh"
@@ -309,6 +311,30 @@ void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float
                    const float* e, float* r32, const ReduceScratch& R, int slot, size_t hstride) {
   launch_pdl(k_defect, defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s, A, pin, pout, e,
              r32, R, slot, hstride);
+}
+
+// A 3D tiled map over a dense (nx, ny, nz) array (cuTensorMapEncodeTiled via
+// the runtime's driver entry point, so the library links no libcuda).
+bool make_tensor_map_3d(CUtensorMap* map, const void* base, CUtensorMapDataType type, int elem,
+                        int nx, int ny, int nz, int bx, int by) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (((size_t)nx * elem) % 16 != 0 || ((size_t)bx * elem) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * elem, (cuuint64_t)nx * ny * elem};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  return encode(map, type, 3, const_cast<void*>(base), dims, strides, box, estride,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 bool make_defect_maps(DefectMaps* m, const float2* p, const float* e, const float2* b,

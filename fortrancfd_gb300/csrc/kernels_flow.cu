@@ -277,6 +277,79 @@ __global__ void __launch_bounds__(kRedThreads) k_div_stats(int nx, int ny, int n
   grid_sum_finish<1>(acc, R, kSlotSum);
 }
 
+// The increment of one cycle for GBMG_STOP_INCREMENT: d = x - y (y may be
+// null) over the cells (colour-split when hstride > 0: cells [0, n/2) of each
+// half, the pad between the halves skipped).  The reference removes the mean
+// of p before it measures the change (ppe_sor_solver, PRESS_POISSON), so the
+// increment is max |d - mean(d)|: k_delta_sum sums d, k_delta_absmax takes
+// the maximum of |d - mean| as a bit pattern (non-negative doubles order as
+// unsigned integers) by atomicMax into R.result[slot_out].
+template <typename T>
+__device__ __forceinline__ size_t cell_index(size_t i, size_t n, size_t hstride) {
+  return hstride ? (i < n / 2 ? i : hstride + (i - n / 2)) : i;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_delta_sum(const T* __restrict__ x,
+                                                           const T* __restrict__ y, size_t n,
+                                                           size_t hstride, ReduceScratch R,
+                                                           int slot) {
+  double acc[1] = {0.0};
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t q = cell_index<T>(i, n, hstride);
+    acc[0] += y ? (double)x[q] - (double)y[q] : (double)x[q];
+  }
+  grid_sum_finish<1>(acc, R, slot);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_delta_absmax(const T* __restrict__ x,
+                                                              const T* __restrict__ y, size_t n,
+                                                              size_t hstride, ReduceScratch R,
+                                                              int slot_sum, int slot_out) {
+  const double m = R.result[slot_sum] / (double)n;
+  double mx = 0.0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t q = cell_index<T>(i, n, hstride);
+    const double d = y ? (double)x[q] - (double)y[q] : (double)x[q];
+    mx = fmax(mx, fabs(d - m));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0)
+    atomicMax(reinterpret_cast<unsigned long long*>(R.result + slot_out),
+              (unsigned long long)__double_as_longlong(mx));
+}
+
+// RHSP's wall-normal faces set to zero: u at f = 0 and nx, v at 0 and ny, w at
+// 0 and nz (arrays at face (0,0,0)); one thread per face of each wall pair.
+__global__ void k_zero_wall_faces(int nx, int ny, int nz, double* u, int64_t usy, int64_t usz,
+                                  double* v, int64_t vsy, int64_t vsz, double* w, int64_t wsy,
+                                  int64_t wsz) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nu = (int64_t)ny * nz, nv = (int64_t)nx * nz, nw = w ? (int64_t)nx * ny : 0;
+  if (t < nu) {
+    const int j = (int)(t % ny), k = (int)(t / ny);
+    const int64_t q = j * usy + k * usz;
+    u[q] = 0.0;
+    u[q + nx] = 0.0;
+  } else if (t < nu + nv) {
+    const int64_t r = t - nu;
+    const int i = (int)(r % nx), k = (int)(r / nx);
+    const int64_t q = i + k * vsz;
+    v[q] = 0.0;
+    v[q + (int64_t)ny * vsy] = 0.0;
+  } else if (t < nu + nv + nw) {
+    const int64_t r = t - nu - nv;
+    const int i = (int)(r % nx), j = (int)(r / nx);
+    const int64_t q = i + j * wsy;
+    w[q] = 0.0;
+    w[q + (int64_t)nz * wsz] = 0.0;
+  }
+}
+
 __global__ void __launch_bounds__(kRedThreads) k_sum(const double* __restrict__ x, size_t n,
                                                      ReduceScratch R, int slot) {
   double acc[2] = {0.0, 0.0};
@@ -443,6 +516,28 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
   cudaMemsetAsync(R.result + kSlotMax, 0, sizeof(double), s);
   const int blocks = std::min(reduce_blocks_for((size_t)ny * nz), R.max_blocks);
   k_div_stats<<<blocks, kRedThreads, 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, R);
+}
+
+template <typename T>
+void launch_increment(cudaStream_t s, const T* x, const T* y, size_t n, size_t hstride,
+                      const ReduceScratch& R, int slot_sum, int slot_out) {
+  const unsigned b = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_delta_sum<T><<<b, kRedThreads, 0, s>>>(x, y, n, hstride, R, slot_sum);
+  cudaMemsetAsync(R.result + slot_out, 0, sizeof(double), s);
+  k_delta_absmax<T><<<stride_blocks(n), kRedThreads, 0, s>>>(x, y, n, hstride, R, slot_sum,
+                                                             slot_out);
+}
+template void launch_increment<float>(cudaStream_t, const float*, const float*, size_t, size_t,
+                                      const ReduceScratch&, int, int);
+template void launch_increment<double>(cudaStream_t, const double*, const double*, size_t,
+                                       size_t, const ReduceScratch&, int, int);
+
+void launch_zero_wall_faces(cudaStream_t s, int nx, int ny, int nz, double* u, int64_t usy,
+                            int64_t usz, double* v, int64_t vsy, int64_t vsz, double* w,
+                            int64_t wsy, int64_t wsz) {
+  const int64_t total = (int64_t)ny * nz + (int64_t)nx * nz + (w ? (int64_t)nx * ny : 0);
+  k_zero_wall_faces<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(nx, ny, nz, u, usy, usz, v,
+                                                                   vsy, vsz, w, wsy, wsz);
 }
 
 void launch_sum(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot) {

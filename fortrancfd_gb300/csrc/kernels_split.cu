@@ -78,8 +78,8 @@ __device__ __forceinline__ void unpack(float4 v, float (&a)[4]) { a[0] = v.x; a[
 // nx % 8 == 0): every load is a float4 except the one-element x edge of the
 // window, and the index and bounds work is shared by the four cells.  The
 // per-cell arithmetic is k_smooth_split's, in the same order.
-template <bool kZero, int kMinBlocks = 1>
-__global__ void __launch_bounds__(256, kMinBlocks) k_smooth_split4(LevelView<float> L, int color) {
+template <bool kZero>
+__global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int color) {
   pdl_enter();
   const int hx = L.nx >> 1;
   const int m0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
@@ -139,153 +139,6 @@ __global__ void __launch_bounds__(256, kMinBlocks) k_smooth_split4(LevelView<flo
     out[c] = rho_relax32(s, b[c], d);
   }
   st4(L.sol + own, make_float4(out[0], out[1], out[2], out[3]));
-}
-
-// k_smooth_split4 marching over a chunk of kc z planes per thread.  The
-// other colour's rows of planes k-1, k and k+1 (rho and p, one float4 each)
-// stay in registers from plane to plane, the rows j-1 and j+1 of plane k come
-// from the neighbouring threads of the block through shared memory (loaded
-// only at the block's y edges), the x-window edge element from the
-// neighbouring lane by a shuffle, and the next plane's rows are loaded before
-// the current plane is computed.  A colour launch thus loads each row about
-// once instead of five times; the per-cell arithmetic is k_smooth_split4's,
-// in the same order, so the results are the same bits.
-template <bool kZero, int BY>
-__global__ void __launch_bounds__(32 * BY) k_smooth_split4z(LevelView<float> L, int color, int kc) {
-  pdl_enter();
-  __shared__ float4 sR[2][BY][32], sP[2][BY][32];
-  const int lane = threadIdx.x, ty = threadIdx.y;
-  const int hx = L.nx >> 1;
-  const int m0 = 4 * (blockIdx.x * 32 + lane);
-  const int j = blockIdx.y * BY + ty;
-  const bool act = m0 < hx && j < L.ny;
-  const int nch = (L.nz + kc - 1) / kc;
-  const int ch = L.zrev ? nch - 1 - (int)blockIdx.z : (int)blockIdx.z;
-  const int kb = ch * kc, ke = min(L.nz, kb + kc);
-  const size_t sy = (size_t)hx, sz = (size_t)hx * L.ny;
-  const size_t hrow = (size_t)j * sy + m0;
-  const float* __restrict__ ro = L.rho + (size_t)(1 - color) * L.hstride;
-  const float* __restrict__ po = L.sol + (size_t)(1 - color) * L.hstride;
-  const float* __restrict__ rown = L.rho + (size_t)color * L.hstride;
-  const float* __restrict__ bown = L.src + (size_t)color * L.hstride;
-  float* __restrict__ pown = L.sol + (size_t)color * L.hstride;
-  const float inf = __int_as_float(0x7f800000);
-  const float4 winf = make_float4(inf, inf, inf, inf), zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  // other-colour rows of plane k (walls: density +inf, p 0)
-  const auto ldr = [&](int k) {
-    return (act && k >= 0 && k < L.nz) ? ld4(ro + (size_t)k * sz + hrow) : winf;
-  };
-  const auto ldp = [&](int k) {
-    return (!kZero && act && k >= 0 && k < L.nz) ? ld4(po + (size_t)k * sz + hrow) : zero4;
-  };
-  float4 rm = ldr(kb - 1), pm = ldp(kb - 1);
-  float4 rc4 = ldr(kb), pc4 = ldp(kb);
-  float4 rp = ldr(kb + 1), pp = ldp(kb + 1);
-  float4 orh = act ? ld4(rown + (size_t)kb * sz + hrow) : winf;
-  float4 obh = act ? ld4(bown + (size_t)kb * sz + hrow) : zero4;
-  for (int k = kb; k < ke; ++k) {
-    const int buf = k & 1;
-    sR[buf][ty][lane] = rc4;
-    sP[buf][ty][lane] = pc4;
-    __syncthreads();
-    // the next plane's rows, in flight while this plane is computed
-    float4 nr = winf, np = zero4, nor = winf, nob = zero4;
-    if (k + 1 < ke) {
-      nr = ldr(k + 2);
-      np = ldp(k + 2);
-      if (act) {
-        nor = ld4(rown + (size_t)(k + 1) * sz + hrow);
-        nob = ld4(bown + (size_t)(k + 1) * sz + hrow);
-      }
-    }
-    const size_t hk = (size_t)k * sz + hrow;
-    float4 rym = winf, pym = zero4, ryp = winf, pyp = zero4;
-    if (ty > 0) {
-      rym = sR[buf][ty - 1][lane];
-      pym = sP[buf][ty - 1][lane];
-    } else if (act && j > 0) {
-      rym = ld4(ro + hk - sy);
-      if (!kZero) pym = ld4(po + hk - sy);
-    }
-    if (j + 1 < L.ny) {
-      if (ty < BY - 1) {
-        ryp = sR[buf][ty + 1][lane];
-        pyp = sP[buf][ty + 1][lane];
-      } else if (act) {
-        ryp = ld4(ro + hk + sy);
-        if (!kZero) pyp = ld4(po + hk + sy);
-      }
-    }
-    // x window: the other colour's half indices m0-1+par .. m0+3+par; the
-    // edge element from the neighbouring lane (or memory at a warp edge)
-    const int par = (j + k + color) & 1;
-    const float nxr = __shfl_down_sync(0xffffffffu, rc4.x, 1);
-    const float nxp = __shfl_down_sync(0xffffffffu, pc4.x, 1);
-    const float pvr = __shfl_up_sync(0xffffffffu, rc4.w, 1);
-    const float pvp = __shfl_up_sync(0xffffffffu, pc4.w, 1);
-    float rv[4], pv[4];
-    unpack(rc4, rv);
-    unpack(pc4, pv);
-    float re = inf, pe = 0.f;
-    float rxm[4], rxp[4], pxm[4], pxp[4];
-    if (par) {
-      if (m0 + 4 < hx) {
-        if (lane < 31) {
-          re = nxr;
-          if (!kZero) pe = nxp;
-        } else if (act) {
-          re = ro[hk + 4];
-          if (!kZero) pe = po[hk + 4];
-        }
-      }
-      rxm[0] = rv[0]; rxm[1] = rv[1]; rxm[2] = rv[2]; rxm[3] = rv[3];
-      rxp[0] = rv[1]; rxp[1] = rv[2]; rxp[2] = rv[3]; rxp[3] = re;
-      pxm[0] = pv[0]; pxm[1] = pv[1]; pxm[2] = pv[2]; pxm[3] = pv[3];
-      pxp[0] = pv[1]; pxp[1] = pv[2]; pxp[2] = pv[3]; pxp[3] = pe;
-    } else {
-      if (m0 > 0) {
-        if (lane > 0) {
-          re = pvr;
-          if (!kZero) pe = pvp;
-        } else if (act) {
-          re = ro[hk - 1];
-          if (!kZero) pe = po[hk - 1];
-        }
-      }
-      rxm[0] = re; rxm[1] = rv[0]; rxm[2] = rv[1]; rxm[3] = rv[2];
-      rxp[0] = rv[0]; rxp[1] = rv[1]; rxp[2] = rv[2]; rxp[3] = rv[3];
-      pxm[0] = pe; pxm[1] = pv[0]; pxm[2] = pv[1]; pxm[3] = pv[2];
-      pxp[0] = pv[0]; pxp[1] = pv[1]; pxp[2] = pv[2]; pxp[3] = pv[3];
-    }
-    float rc[4], b[4], rym_[4], ryp_[4], rzm[4], rzp[4], pym_[4], pyp_[4], pzm[4], pzp[4];
-    unpack(orh, rc);
-    unpack(obh, b);
-    unpack(rym, rym_);
-    unpack(ryp, ryp_);
-    unpack(rm, rzm);
-    unpack(rp, rzp);
-    unpack(pym, pym_);
-    unpack(pyp, pyp_);
-    unpack(pm, pzm);
-    unpack(pp, pzp);
-    float out[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      float s = 0.f, d = 0.f, cc;
-      cc = face(L.kx, rc[c], rxm[c]); if (!kZero) rho_acc32(cc, pxm[c], s, d); else d = __fadd_rn(d, cc);
-      cc = face(L.kx, rc[c], rxp[c]); if (!kZero) rho_acc32(cc, pxp[c], s, d); else d = __fadd_rn(d, cc);
-      cc = face(L.ky, rc[c], rym_[c]); if (!kZero) rho_acc32(cc, pym_[c], s, d); else d = __fadd_rn(d, cc);
-      cc = face(L.ky, rc[c], ryp_[c]); if (!kZero) rho_acc32(cc, pyp_[c], s, d); else d = __fadd_rn(d, cc);
-      cc = face(L.kz, rc[c], rzm[c]); if (!kZero) rho_acc32(cc, pzm[c], s, d); else d = __fadd_rn(d, cc);
-      cc = face(L.kz, rc[c], rzp[c]); if (!kZero) rho_acc32(cc, pzp[c], s, d); else d = __fadd_rn(d, cc);
-      out[c] = rho_relax32(s, b[c], d);
-    }
-    if (act) st4(pown + hk, make_float4(out[0], out[1], out[2], out[3]));
-    rm = rc4; pm = pc4;
-    rc4 = rp; pc4 = pp;
-    rp = nr; pp = np;
-    orh = nor; obh = nob;
-  }
 }
 
 // Fused residual + restriction out of the split finest level (fx = 2): one
@@ -597,28 +450,9 @@ inline bool vec4_ok(const LevelView<float>& F) {
 
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess) {
   const dim3 blk(32, 8, 1);
-  const int zmode = L.zmarch, zc = std::max(1, L.zc);
-  if (zmode > 0 && vec4_ok(L)) {
-    const int by = zmode == 2 ? 16 : 8;
-    const dim3 gz(cdiv((size_t)(L.nx / 2), 128), cdiv((size_t)L.ny, by),
-                  cdiv((size_t)L.nz, (unsigned)zc));
-    if (by == 16) {
-      if (zero_guess) launch_pdl(k_smooth_split4z<true, 16>, gz, dim3(32, 16), 0, s, L, color, zc);
-      else launch_pdl(k_smooth_split4z<false, 16>, gz, dim3(32, 16), 0, s, L, color, zc);
-    } else {
-      if (zero_guess) launch_pdl(k_smooth_split4z<true, 8>, gz, dim3(32, 8), 0, s, L, color, zc);
-      else launch_pdl(k_smooth_split4z<false, 8>, gz, dim3(32, 8), 0, s, L, color, zc);
-    }
-    return;
-  }
   if (vec4_ok(L)) {
     const dim3 g4(cdiv((size_t)(L.nx / 8), 32), cdiv((size_t)L.ny, 8), (unsigned)L.nz);
-    // L.minb: resident blocks per SM the compiler is asked to allow for
-    // (fewer registers per thread), 0 = its own choice
     if (zero_guess) launch_pdl(k_smooth_split4<true>, g4, blk, 0, s, L, color);
-    else if (L.minb == 5) launch_pdl(k_smooth_split4<false, 5>, g4, blk, 0, s, L, color);
-    else if (L.minb == 6) launch_pdl(k_smooth_split4<false, 6>, g4, blk, 0, s, L, color);
-    else if (L.minb == 8) launch_pdl(k_smooth_split4<false, 8>, g4, blk, 0, s, L, color);
     else launch_pdl(k_smooth_split4<false>, g4, blk, 0, s, L, color);
     return;
   }
@@ -631,15 +465,9 @@ void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const Leve
                            bool zero_sol) {
   const dim3 blk(32, 8, 1);
   if (vec4_ok(F) && C.nx % 4 == 0) {
-    // two coarse cells per thread unless GBMG_RESTRICT_VEC=4
-    static int vec = 0;
-    if (vec == 0) {
-      const char* e = std::getenv("GBMG_RESTRICT_VEC");
-      vec = (e && std::atoi(e) == 4) ? 4 : 2;
-    }
-    const dim3 gv(cdiv((size_t)(C.nx / vec), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-    if (vec == 4) launch_pdl(k_restrict_splitv<4>, gv, blk, 0, s, F, C, zero_sol ? 1 : 0);
-    else launch_pdl(k_restrict_splitv<2>, gv, blk, 0, s, F, C, zero_sol ? 1 : 0);
+    // two coarse cells per thread
+    const dim3 gv(cdiv((size_t)(C.nx / 2), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
+    launch_pdl(k_restrict_splitv<2>, gv, blk, 0, s, F, C, zero_sol ? 1 : 0);
     return;
   }
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);

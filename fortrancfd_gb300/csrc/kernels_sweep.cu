@@ -70,24 +70,6 @@ __device__ __forceinline__ void unpack4(float4 v, float (&a)[4]) {
   a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
 }
 
-// Copy rows [j_lo, j_hi) of plane k of one colour half into shared memory at
-// dst + (j_lo - j_base) * hx (one bulk copy; completion counted on bar).
-__device__ __forceinline__ uint32_t stage_rows(float* dst, const float* half, const SweepArgs& A,
-                                               int k, int j_base, int j_lo, int j_hi,
-                                               uint64_t* bar) {
-  j_lo = max(j_lo, 0);
-  j_hi = min(j_hi, A.ny);
-  if (j_hi <= j_lo) return 0;
-  const uint32_t bytes = (uint32_t)(j_hi - j_lo) * (uint32_t)A.hx * 4u;
-  const float* src = half + ((size_t)k * A.ny + j_lo) * A.hx;
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_u32(dst + (size_t)(j_lo - j_base) * A.hx)), "l"(src), "r"(bytes),
-      "r"(smem_u32(bar))
-      : "memory");
-  return bytes;
-}
-
 // The x window of a cell quad m0..m0+3 of colour parity `par` in a row of the
 // other colour: x- neighbours at half index m-1+par, x+ at m+par (walls: +inf
 // density, zero pressure), as k_smooth_split4 forms them.
@@ -154,144 +136,158 @@ __device__ __forceinline__ float4 relax4(const SweepArgs& A, const float (&rc)[4
   return make_float4(out[0], out[1], out[2], out[3]);
 }
 
+// Pointers to one plane's staged rows of each array, and to its new colour-A
+// rows, offset to this thread's quad.
+struct PlaneRows {
+  const float* pB;  // row jj of p_in colour B (by+4-row array)
+  const float* rB;  // row jj of rho colour B
+  const float* rA;  // row jj of rho colour A (by+2-row array)
+  float* nA;        // row jj of the new colour A
+};
+
 // kZero: the first colour relaxes from p = 0 (the first sweep after a zero
 // initial guess), so p_in is not read at all.
 template <bool kZero>
 __global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
   pdl_enter();
-  extern __shared__ unsigned char sw_raw[];
-  float* sm = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sw_raw) + 127) &
-                                       ~uintptr_t(127));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + (size_t)A.o_new + (size_t)kSwNew * (A.by + 2) * A.hx);
-  const int tq = A.hx >> 2;                 // threads per row
-  const int q = threadIdx.x % tq, ra = threadIdx.x / tq;  // ra: row 0 .. by+1 (j0-1 .. j0+by)
+  extern __shared__ float4 sw_smem[];
+  float* const sm = reinterpret_cast<float*>(sw_smem);
+  const int hx = A.hx;
+  const int rowsA = A.by + 2;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A.o_new + kSwNew * rowsA * hx);
+  const int tq = hx >> 2;                                 // threads per row
+  const int q = threadIdx.x % tq, ra = threadIdx.x / tq;  // ra: row j0-1 .. j0+by
   const int m0 = 4 * q;
   const int rg = blockIdx.x % A.nrg, ch = blockIdx.x / A.nrg;
   const int j0 = rg * A.by;
   const int z0 = ch * A.zc, z1 = min(A.nz, z0 + A.zc);
   const int jj = j0 - 1 + ra;
   const bool row_in = jj >= 0 && jj < A.ny;
+  const bool own_row = row_in && ra >= 1 && ra <= A.by;
+  const bool ym_ok = jj > 0, yp_ok = jj < A.ny - 1;
   const int c1 = 1 - A.c0;
-  const size_t sz = (size_t)A.hx * A.ny;
-  const float* pB_g = A.pin + (size_t)c1 * A.hstride;
-  const float* rB_g = A.rho + (size_t)c1 * A.hstride;
-  const float* rA_g = A.rho + (size_t)A.c0 * A.hstride;
-  const float* bA_g = A.src + (size_t)A.c0 * A.hstride;
-  const float* bB_g = A.src + (size_t)c1 * A.hstride;
-  float* pA_o = A.pout + (size_t)A.c0 * A.hstride;
-  float* pB_o = A.pout + (size_t)c1 * A.hstride;
+  const size_t sz = (size_t)hx * A.ny;
+  const int offB = (ra + 1) * hx + m0;  // this thread's row in the by+4-row arrays
+  const int offA = ra * hx + m0;        // ... and in the by+2-row arrays
   // planes staged: [qlo, qhi]
   const int qlo = max(0, z0 - 2), qhi = min(A.nz - 1, z1 + 1);
-  const int rowsB = A.by + 4, rowsA = A.by + 2;
-  const auto slot_of = [&](int k) { return (k - qlo) % kSwStages; };
-  const auto stage_pB = [&](int k) { return sm + (size_t)slot_of(k) * A.stage; };
-  const auto stage_rB = [&](int k) { return sm + (size_t)slot_of(k) * A.stage + A.o_rB; };
-  const auto stage_rA = [&](int k) { return sm + (size_t)slot_of(k) * A.stage + A.o_rA; };
-  const auto new_row = [&](int k, int r) {
-    return sm + A.o_new + ((size_t)(k % kSwNew) * rowsA + r) * A.hx;
-  };
+  const auto stage_base = [&](int slot) { return sm + slot * A.stage; };
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSwStages; ++s) mbar_init(&bar[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
+  // the block's row ranges of the staged arrays, clamped to the grid
+  const int loB = max(j0 - 2, 0), hiB = min(j0 + A.by + 2, A.ny);
+  const int loA = max(j0 - 1, 0), hiA = min(j0 + A.by + 1, A.ny);
+  const uint32_t bytesB = (uint32_t)(hiB - loB) * hx * 4u, bytesA = (uint32_t)(hiA - loA) * hx * 4u;
+  const float* pB_g = A.pin + (size_t)c1 * A.hstride + (size_t)loB * hx;
+  const float* rB_g = A.rho + (size_t)c1 * A.hstride + (size_t)loB * hx;
+  const float* rA_g = A.rho + (size_t)A.c0 * A.hstride + (size_t)loA * hx;
+  const int dstB = (loB - (j0 - 2)) * hx, dstA = (loA - (j0 - 1)) * hx;
   const auto issue = [&](int k) {  // one thread
-    const int s = slot_of(k);
+    const int slot = (k - qlo) % kSwStages;
+    float* base = stage_base(slot);
+    uint64_t* b = &bar[slot];
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    // expected bytes first, then the copies
-    uint32_t bytes = 0;
-    const int lo = max(j0 - 2, 0), hi = min(j0 + A.by + 2, A.ny);
-    const int loA = max(j0 - 1, 0), hiA = min(j0 + A.by + 1, A.ny);
-    bytes += (uint32_t)(hi - lo) * A.hx * 4u * (kZero ? 1u : 2u);
-    bytes += (uint32_t)(hiA - loA) * A.hx * 4u;
-    mbar_arrive_expect_tx(&bar[s], bytes);
-    if (!kZero) stage_rows(stage_pB(k), pB_g, A, k, j0 - 2, j0 - 2, j0 + A.by + 2, &bar[s]);
-    stage_rows(stage_rB(k), rB_g, A, k, j0 - 2, j0 - 2, j0 + A.by + 2, &bar[s]);
-    stage_rows(stage_rA(k), rA_g, A, k, j0 - 1, j0 - 1, j0 + A.by + 1, &bar[s]);
+    mbar_arrive_expect_tx(b, (kZero ? 1u : 2u) * bytesB + bytesA);
+    const size_t pk = (size_t)k * sz;
+    const auto copy = [&](float* dst, const float* src, uint32_t bytes) {
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b))
+          : "memory");
+    };
+    if (!kZero) copy(base + dstB, pB_g + pk, bytesB);
+    copy(base + A.o_rB + dstB, rB_g + pk, bytesB);
+    copy(base + A.o_rA + dstA, rA_g + pk, bytesA);
   };
-  int issued = qlo - 1, waited = qlo - 1;
   const int t0 = max(z0 - 1, 0);
+  int issued = min(qhi, t0 + 2);
   if (threadIdx.x == 0)
-    for (int k = qlo; k <= min(qhi, t0 + 2); ++k) issue(k);
-  issued = min(qhi, t0 + 2);
-  const float inf = __int_as_float(0x7f800000);
+    for (int k = qlo; k <= issued; ++k) issue(k);
+  int waited = qlo - 1;
+  // this thread's right-hand sides and outputs, advanced one plane per step
+  // (offsets in signed arithmetic: plane t0 - 1 may be -1, never dereferenced)
+  const ptrdiff_t off0 = (ptrdiff_t)t0 * (ptrdiff_t)sz + (ptrdiff_t)jj * hx + m0;
+  const float* bA_p = A.src + (ptrdiff_t)A.c0 * (ptrdiff_t)A.hstride + off0;
+  const float* bB_p = A.src + (ptrdiff_t)c1 * (ptrdiff_t)A.hstride + off0 - (ptrdiff_t)sz;
+  float* oA_p = A.pout + (ptrdiff_t)A.c0 * (ptrdiff_t)A.hstride + off0;
+  float* oB_p = A.pout + (ptrdiff_t)c1 * (ptrdiff_t)A.hstride + off0 - (ptrdiff_t)sz;
+  // ring positions of planes t-2 .. t+1 (stages) and t-2 .. t (new colour A)
+  int sl = (t0 - qlo) % kSwStages;  // slot of plane t
+  int nl = t0 % kSwNew;             // new-ring slot of plane t
+  const auto wrap5 = [](int v) { return v >= kSwStages ? v - kSwStages : (v < 0 ? v + kSwStages : v); };
+  const auto wrap3 = [](int v) { return v >= kSwNew ? v - kSwNew : (v < 0 ? v + kSwNew : v); };
+  const auto rows_of = [&](int slot, int nslot) {
+    const float* base = stage_base(slot);
+    return PlaneRows{base + offB, base + A.o_rB + offB, base + A.o_rA + offA,
+                     sm + A.o_new + nslot * rowsA * hx + offA};
+  };
+  const int rowB = hx, rowA = hx;  // row pitch of the staged arrays
   for (int t = t0; t <= z1; ++t) {
     if (t + 2 <= qhi && t + 2 > issued) {
       if (threadIdx.x == 0) issue(t + 2);
       issued = t + 2;
     }
-    // this step's right-hand sides straight into registers
-    const bool doA = row_in && t < A.nz;
     const int u = t - 1;
-    const bool doB = row_in && ra >= 1 && ra <= A.by && u >= z0 && u < z1;
+    const bool doA = row_in && t < A.nz;
+    const bool doB = own_row && u >= z0 && u < z1;
     float bA[4] = {0.f, 0.f, 0.f, 0.f}, bB[4] = {0.f, 0.f, 0.f, 0.f};
-    if (doA) unpack4(__ldg(reinterpret_cast<const float4*>(bA_g + t * sz + (size_t)jj * A.hx + m0)), bA);
-    if (doB) unpack4(__ldg(reinterpret_cast<const float4*>(bB_g + u * sz + (size_t)jj * A.hx + m0)), bB);
+    if (doA) unpack4(__ldg(reinterpret_cast<const float4*>(bA_p)), bA);
+    if (doB) unpack4(__ldg(reinterpret_cast<const float4*>(bB_p)), bB);
     const int need = min(t + 1, qhi);
     while (waited < need) {
       ++waited;
-      const int s = slot_of(waited);
-      mbar_wait(&bar[s], (uint32_t)(((waited - qlo) / kSwStages) & 1), A.err);
+      const int slot = (waited - qlo) % kSwStages;
+      mbar_wait(&bar[slot], (uint32_t)(((waited - qlo) / kSwStages) & 1), A.err);
     }
+    const PlaneRows Pm = rows_of(wrap5(sl - 1), wrap3(nl - 1));  // plane t-1
+    const PlaneRows P0 = rows_of(sl, nl);                          // plane t
     // colour A of plane t on rows j0-1 .. j0+by
     if (doA) {
+      const PlaneRows Pp = rows_of(wrap5(sl + 1), nl);  // plane t+1 (stages only)
       const int par = (jj + t + A.c0) & 1;
-      const int rb_ = ra + 1;  // row jj in the by+4 row arrays
-      const float* rB = stage_rB(t);
-      const float* pB = stage_pB(t);
       float rc[4];
-      unpack4(lds4(stage_rA(t) + (size_t)ra * A.hx + m0), rc);
+      unpack4(lds4(P0.rA), rc);
       float rxm[4], rxp[4], pxm[4], pxp[4];
-      x_window(rB + (size_t)rb_ * A.hx, pB + (size_t)rb_ * A.hx, m0, A.hx, par, kZero, rxm, rxp,
-               pxm, pxp);
+      x_window(P0.rB - m0, P0.pB - m0, m0, hx, par, kZero, rxm, rxp, pxm, pxp);
       float rym[4], pym[4], ryp[4], pyp[4], rzm[4], pzm[4], rzp[4], pzp[4];
-      nb_row(rB + (size_t)(rb_ - 1) * A.hx, pB + (size_t)(rb_ - 1) * A.hx, m0, jj > 0, kZero,
-             rym, pym);
-      nb_row(rB + (size_t)(rb_ + 1) * A.hx, pB + (size_t)(rb_ + 1) * A.hx, m0, jj < A.ny - 1,
-             kZero, ryp, pyp);
-      if (t > 0)
-        nb_row(stage_rB(t - 1) + (size_t)rb_ * A.hx, stage_pB(t - 1) + (size_t)rb_ * A.hx, m0,
-               true, kZero, rzm, pzm);
-      else
-        nb_row(rB, pB, m0, false, kZero, rzm, pzm);
-      if (t < A.nz - 1)
-        nb_row(stage_rB(t + 1) + (size_t)rb_ * A.hx, stage_pB(t + 1) + (size_t)rb_ * A.hx, m0,
-               true, kZero, rzp, pzp);
-      else
-        nb_row(rB, pB, m0, false, kZero, rzp, pzp);
+      nb_row(P0.rB - rowB - m0, P0.pB - rowB - m0, m0, ym_ok, kZero, rym, pym);
+      nb_row(P0.rB + rowB - m0, P0.pB + rowB - m0, m0, yp_ok, kZero, ryp, pyp);
+      nb_row(Pm.rB - m0, Pm.pB - m0, m0, t > 0, kZero, rzm, pzm);
+      nb_row(Pp.rB - m0, Pp.pB - m0, m0, t < A.nz - 1, kZero, rzp, pzp);
       const float4 v = relax4<kZero>(A, rc, bA, rxm, rxp, pxm, pxp, rym, pym, ryp, pyp, rzm, pzm,
                                      rzp, pzp);
-      sts4(new_row(t, ra) + m0, v);
-      if (ra >= 1 && ra <= A.by && t >= z0 && t < z1)
-        *reinterpret_cast<float4*>(pA_o + t * sz + (size_t)jj * A.hx + m0) = v;
+      sts4(P0.nA, v);
+      if (own_row && t >= z0 && t < z1) *reinterpret_cast<float4*>(oA_p) = v;
     }
     __syncthreads();
     // colour B of plane u = t-1 on the block's rows, from the new colour A
     if (doB) {
+      const PlaneRows Pmm = rows_of(wrap5(sl - 2), wrap3(nl - 2));  // plane u-1
       const int par = (jj + u + c1) & 1;
       float rc[4];
-      unpack4(lds4(stage_rB(u) + (size_t)(ra + 1) * A.hx + m0), rc);
-      const float* rA = stage_rA(u);
+      unpack4(lds4(Pm.rB), rc);
       float rxm[4], rxp[4], pxm[4], pxp[4];
-      x_window(rA + (size_t)ra * A.hx, new_row(u, ra), m0, A.hx, par, false, rxm, rxp, pxm, pxp);
+      x_window(Pm.rA - m0, Pm.nA - m0, m0, hx, par, false, rxm, rxp, pxm, pxp);
       float rym[4], pym[4], ryp[4], pyp[4], rzm[4], pzm[4], rzp[4], pzp[4];
-      nb_row(rA + (size_t)(ra - 1) * A.hx, new_row(u, ra - 1), m0, jj > 0, false, rym, pym);
-      nb_row(rA + (size_t)(ra + 1) * A.hx, new_row(u, ra + 1), m0, jj < A.ny - 1, false, ryp, pyp);
-      if (u > 0)
-        nb_row(stage_rA(u - 1) + (size_t)ra * A.hx, new_row(u - 1, ra), m0, true, false, rzm, pzm);
-      else
-        nb_row(rA, rA, m0, false, false, rzm, pzm);
-      if (u < A.nz - 1)
-        nb_row(stage_rA(u + 1) + (size_t)ra * A.hx, new_row(u + 1, ra), m0, true, false, rzp, pzp);
-      else
-        nb_row(rA, rA, m0, false, false, rzp, pzp);
+      nb_row(Pm.rA - rowA - m0, Pm.nA - rowA - m0, m0, ym_ok, false, rym, pym);
+      nb_row(Pm.rA + rowA - m0, Pm.nA + rowA - m0, m0, yp_ok, false, ryp, pyp);
+      nb_row(Pmm.rA - m0, Pmm.nA - m0, m0, u > 0, false, rzm, pzm);
+      nb_row(P0.rA - m0, P0.nA - m0, m0, u < A.nz - 1, false, rzp, pzp);
       const float4 v = relax4<false>(A, rc, bB, rxm, rxp, pxm, pxp, rym, pym, ryp, pyp, rzm, pzm,
                                      rzp, pzp);
-      *reinterpret_cast<float4*>(pB_o + u * sz + (size_t)jj * A.hx + m0) = v;
+      *reinterpret_cast<float4*>(oB_p) = v;
     }
     __syncthreads();
+    sl = wrap5(sl + 1);
+    nl = wrap3(nl + 1);
+    bA_p += sz;
+    bB_p += sz;
+    oA_p += sz;
+    oB_p += sz;
   }
-  (void)inf;
 }
 
 struct SweepShape {
@@ -310,7 +306,7 @@ SweepShape sweep_shape(int hx) {
   S.o_rA = 2 * hx * (S.by + 4);
   S.o_new = kSwStages * S.stage;
   const size_t floats = (size_t)S.o_new + (size_t)kSwNew * (S.by + 2) * hx;
-  S.smem = (int)(floats * sizeof(float) + kSwStages * sizeof(uint64_t) + 128);
+  S.smem = (int)(floats * sizeof(float) + kSwStages * sizeof(uint64_t));
   return S;
 }
 

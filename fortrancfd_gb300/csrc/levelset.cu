@@ -97,8 +97,6 @@ struct LsGrid {
 LsGrid ls_grid(const gbmg_grid& g) {
   LsGrid G{g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, 1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz, 1};
   G.fast = fdiv_divisor_ok(g.dx) && fdiv_divisor_ok(g.dy) && fdiv_divisor_ok(g.dz);
-  // GBMG_NS_DIVIDE=1: IEEE divisions throughout (the same doubles, for comparison)
-  if (const char* e = std::getenv("GBMG_NS_DIVIDE")) G.fast = G.fast && std::atoi(e) == 0;
   return G;
 }
 

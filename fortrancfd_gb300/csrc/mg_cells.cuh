@@ -1,6 +1,6 @@
 // Per-cell bodies of the multigrid kernels (sm_103a), shared by the
-// one-launch-per-step kernels of kernels_mg.cu and the cooperative mid-cycle
-// kernel of midcycle.cu, so both do the same arithmetic in the same order.
+// one-launch-per-step kernels of kernels_mg.cu and the one-block bottom of the
+// cycle (subcycle.cu), so both do the same arithmetic in the same order.
 // The cycle restated is the reference's ("DomainDecomposition/3D/src/
 // others/multigrid_solver.f90": multigrid_relax :1-49, multigrid_restriction
 // :51-90, multigrid_prolongation :106-160, multigrid_residual :162-222) on the

@@ -107,12 +107,17 @@ class PressurePoisson:
     defect correction).  krylov=True (or "fcg") wraps one V-cycle per
     iteration in flexible CG, krylov="fgmres" (or 2) in flexible GMRES(30),
     whose residual falls monotonically (faster on smooth right-hand sides such
-    as adjoint solves).
+    as adjoint solves).  stop_rule: "relative" (|b - A p|/|b| < tol),
+    "rms" (the DomainDecomposition driver's absolute RMS residual < tol; pass
+    p_tol*1e-3) or "increment" (max |p_k - p_(k-1)| < tol between cycles, the
+    rule of ppe_sor_solver and PRESS_POISSON; pass p_tol).  zero_wall_faces:
+    set the wall-normal faces of u, v, w to zero before the divergence, as
+    MPLS_RisingBubble's RHSP does.
     """
 
     def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
                  max_cycles=100, krylov=False, use_graph=True, remove_rhs_mean=True, certify=True,
-                 device=None, stream=None):
+                 device=None, stream=None, stop_rule="relative", zero_wall_faces=False):
         if len(shape) == 2:
             shape = (1,) + tuple(shape)
         self.shape = tuple(int(s) for s in shape)
@@ -132,6 +137,9 @@ class PressurePoisson:
         prm.use_graph = int(bool(use_graph))
         prm.remove_rhs_mean = int(bool(remove_rhs_mean))
         prm.certify = int(bool(certify))
+        prm.stop_rule = {"relative": _lib.GBMG_STOP_RELATIVE, "rms": _lib.GBMG_STOP_RMS,
+                         "increment": _lib.GBMG_STOP_INCREMENT}[stop_rule]
+        prm.zero_wall_faces = int(bool(zero_wall_faces))
         prm.device = -1 if device is None else int(device)
         # a torch.cuda.Stream, or a raw cudaStream_t handle; None = the handle's own stream
         prm.stream = getattr(stream, "cuda_stream", stream) or None

@@ -16,6 +16,7 @@ module gbmg
   integer(c_int), parameter :: GBMG_INVALID_ARG = 3, GBMG_CUDA_ERROR = 4, GBMG_NO_DEVICE = 5
   integer(c_int), parameter :: GBMG_OUT_OF_MEMORY = 6, GBMG_STATE_ERROR = 7
   integer(c_int), parameter :: GBMG_PREC_FP64 = 0, GBMG_PREC_MIXED = 1
+  integer(c_int), parameter :: GBMG_STOP_RELATIVE = 0, GBMG_STOP_RMS = 1, GBMG_STOP_INCREMENT = 2
   integer(c_int), parameter :: GBMG_MEM_HOST = 0, GBMG_MEM_DEVICE = 1
   integer(c_int), parameter :: GBMG_PROF_CLASSES = 12
 
@@ -28,11 +29,12 @@ module gbmg
     integer(c_int32_t) :: precision, nu1, nu2, levels, coarse_max, max_cycles
     integer(c_int32_t) :: krylov, use_graph, remove_rhs_mean, certify, device
     type(c_ptr)        :: stream
+    integer(c_int32_t) :: stop_rule, zero_wall_faces
   end type
 
   type, bind(c) :: gbmg_stats
     integer(c_int32_t) :: status, cycles, levels, coarse_n
-    real(c_double)     :: rel_residual, rms_residual, res0, ms, bytes
+    real(c_double)     :: rel_residual, rms_residual, res0, ms, bytes, increment
   end type
 
   type, bind(c) :: gbmg_field

@@ -24,7 +24,8 @@
  * Operator: (A p)_i = sum over faces f of coe_f (p_nb - p_i), coe_f =
  * 2/(rho_i + rho_nb)/h^2, zero on walls (homogeneous Neumann, folded as in
  * ppe_sor_init).  The solve finds the mean-free p with A p = b to a relative
- * residual ||b - A p||_2/||b||_2 < tol.
+ * residual ||b - A p||_2/||b||_2 < tol (or the reference's own stopping rules,
+ * gbmg_params.stop_rule).
  *
  * Errors never abort: every call returns a gbmg_status.  A solve that reaches
  * max_cycles returns GBMG_NOT_CONVERGED with the best iterate in p (the
@@ -54,6 +55,22 @@ typedef enum {
 } gbmg_status;
 
 enum { GBMG_PREC_FP64 = 0, GBMG_PREC_MIXED = 1 };
+/* When a solve stops (gbmg_params.stop_rule):
+ *   GBMG_STOP_RELATIVE   ||b - A p||_2 / ||b||_2 < tol (the default);
+ *   GBMG_STOP_RMS        sqrt(sum r^2 / n) < tol, the absolute RMS residual of
+ *                        the reference's multigrid driver ppe_mg_solver, which
+ *                        stops at l2norm < p_tol*0.001 ("DomainDecomposition/3D/
+ *                        src/ns_solver/ns_ppe_mg_solver.f90:42-43"): pass
+ *                        tol = p_tol*1e-3;
+ *   GBMG_STOP_INCREMENT  max over the cells of |p_k - p_(k-1)| < tol between
+ *                        successive V-cycles, the increment max-norm with which
+ *                        ppe_sor_solver ("Two phase flows/newOpenMP/3D+IBM/src/
+ *                        ns_solver/ns_ppe_solver.f90:143,152") and PRESS_POISSON
+ *                        ("MPLS_RisingBubble/20190612/SOLVE_PRESSURE_POISSON.F90:
+ *                        158-164") stop their sweeps: pass tol = p_tol.  The
+ *                        reference measures it per SOR sweep, this library per
+ *                        V-cycle.  Stationary cycles only (krylov = 0). */
+enum { GBMG_STOP_RELATIVE = 0, GBMG_STOP_RMS = 1, GBMG_STOP_INCREMENT = 2 };
 enum { GBMG_MEM_HOST = 0, GBMG_MEM_DEVICE = 1 };
 
 typedef struct {
@@ -76,6 +93,13 @@ typedef struct {
                               (the cycle loop tracks it in double-word FP32 pairs) */
   int32_t device;          /* CUDA device ordinal; -1 = the current device */
   void* stream;            /* cudaStream_t to run on; NULL = the handle creates its own */
+  int32_t stop_rule;       /* GBMG_STOP_* (default GBMG_STOP_RELATIVE) */
+  int32_t zero_wall_faces; /* 1: gbmg_project and gbmg_divergence first set the wall-normal
+                              faces of u, v, w to zero in the caller's arrays (u at f = 0
+                              and nx, v at 0 and ny, w at 0 and nz), as RHSP does before
+                              its divergence ("MPLS_RisingBubble/20190612/
+                              SOLVE_PRESSURE_POISSON.F90:16-41"); 0 (default): the faces
+                              are read as given */
 } gbmg_params;
 
 typedef struct {
@@ -87,7 +111,9 @@ typedef struct {
   double rms_residual;  /* sqrt(sum r^2 / n): the reference's multigrid norm */
   double res0;          /* relative residual of the initial guess */
   double ms;            /* device time of the call (CUDA events on the handle's stream) */
-  double bytes;         /* algorithmic HBM bytes of the call (model in the design doc) */
+  double bytes;         /* algorithmic HBM bytes of the call */
+  double increment;     /* GBMG_STOP_INCREMENT: max |p_k - p_(k-1)| of the last cycle (the
+                           reference's ppe_linf); 0 under the other rules */
 } gbmg_stats;
 
 typedef struct {
@@ -100,7 +126,7 @@ typedef struct gbmg_handle gbmg_handle;
 
 /* Defaults: FP64, V(2,2), automatic levels, coarse_max 64, 100 cycles,
  * stationary cycles, graphs on, mean projection of b on, FP64 certification
- * on, current device. */
+ * on, current device, relative-residual stopping rule, wall faces as given. */
 void gbmg_default_params(gbmg_params* prm);
 
 /* Allocates the device hierarchy for one grid.  Replaces the level set-up of
