@@ -43,6 +43,7 @@ namespace {
 
 constexpr int kSwStages = 5;  // plane stages of the ring
 constexpr int kSwNew = 3;     // planes of new colour-A values kept
+constexpr int kSwGuard = 4;   // guard floats before and after every staged row
 
 struct SweepArgs {
   const float* rho;  // colour-split density, pressure and right-hand side
@@ -57,57 +58,48 @@ struct SweepArgs {
   float kx, ky, kz;
   int c0;   // first colour
   int* err;
-  // shared memory (floats): per stage pB (by+4 rows), rB (by+4), rA (by+2);
-  // then the new colour-A ring (kSwNew planes of by+2 rows)
-  int stage, o_rB, o_rA, o_new;
+  // shared memory (floats): rows of rp = hx + 2*kSwGuard floats (the row's
+  // cells start at kSwGuard; the guards hold the wall values).  Per stage:
+  // pB (by+4 rows), rB (by+4), rA (by+2); then the new colour-A ring (kSwNew
+  // planes of by+2 rows), a wall density row (+inf) and a wall pressure row (0).
+  int rp, stage, o_rB, o_rA, o_new, o_wall;
 };
 
 __device__ __forceinline__ float4 lds4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
-__device__ __forceinline__ void sts4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ void unpack4(float4 v, float (&a)[4]) {
   a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w;
 }
 
-// The x window of a cell quad m0..m0+3 of colour parity `par` in a row of the
-// other colour: x- neighbours at half index m-1+par, x+ at m+par (walls: +inf
-// density, zero pressure), as k_smooth_split4 forms them.
-__device__ __forceinline__ void x_window(const float* row_r, const float* row_p, int m0, int hx,
-                                         int par, bool zero, float (&rxm)[4], float (&rxp)[4],
-                                         float (&pxm)[4], float (&pxp)[4]) {
-  const float inf = __int_as_float(0x7f800000);
-  float rv[4], pv[4] = {0.f, 0.f, 0.f, 0.f};
-  unpack4(lds4(row_r + m0), rv);
-  if (!zero) unpack4(lds4(row_p + m0), pv);
-  float re = inf, pe = 0.f;
-  if (par) {
-    if (m0 + 4 < hx) { re = row_r[m0 + 4]; if (!zero) pe = row_p[m0 + 4]; }
-    rxm[0] = rv[0]; rxm[1] = rv[1]; rxm[2] = rv[2]; rxm[3] = rv[3];
-    rxp[0] = rv[1]; rxp[1] = rv[2]; rxp[2] = rv[3]; rxp[3] = re;
-    pxm[0] = pv[0]; pxm[1] = pv[1]; pxm[2] = pv[2]; pxm[3] = pv[3];
-    pxp[0] = pv[1]; pxp[1] = pv[2]; pxp[2] = pv[3]; pxp[3] = pe;
-  } else {
-    if (m0 > 0) { re = row_r[m0 - 1]; if (!zero) pe = row_p[m0 - 1]; }
-    rxm[0] = re; rxm[1] = rv[0]; rxm[2] = rv[1]; rxm[3] = rv[2];
-    rxp[0] = rv[0]; rxp[1] = rv[1]; rxp[2] = rv[2]; rxp[3] = rv[3];
-    pxm[0] = pe; pxm[1] = pv[0]; pxm[2] = pv[1]; pxm[3] = pv[2];
-    pxp[0] = pv[0]; pxp[1] = pv[1]; pxp[2] = pv[2]; pxp[3] = pv[3];
+// The x window of a cell quad m0..m0+3 of colour parity par in a row of the
+// other colour: x- neighbours at half index m-1+par, x+ at m+par.  rowc points
+// at the row's cell m0 - 1 + par; a wall is a guard value (+inf density, zero
+// pressure), as k_smooth_split4 substitutes them.
+__device__ __forceinline__ void x_window(const float* rowr, const float* rowp, bool zero,
+                                         float (&rxm)[4], float (&rxp)[4], float (&pxm)[4],
+                                         float (&pxp)[4]) {
+  float w[5], v[5];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) {
+    w[c] = rowr[c];
+    v[c] = zero ? 0.f : rowp[c];
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    rxm[c] = w[c];
+    rxp[c] = w[c + 1];
+    pxm[c] = v[c];
+    pxp[c] = v[c + 1];
   }
 }
 
-// A neighbour row (y or z) of the other colour, or a wall.
-__device__ __forceinline__ void nb_row(const float* row_r, const float* row_p, int m0, bool valid,
-                                       bool zero, float (&r)[4], float (&p)[4]) {
-  const float inf = __int_as_float(0x7f800000);
-  if (valid) {
-    unpack4(lds4(row_r + m0), r);
-    if (!zero) unpack4(lds4(row_p + m0), p);
-    else p[0] = p[1] = p[2] = p[3] = 0.f;
-  } else {
-    r[0] = r[1] = r[2] = r[3] = inf;
-    p[0] = p[1] = p[2] = p[3] = 0.f;
-  }
+// A neighbour row (y or z) of the other colour (a wall row when outside).
+__device__ __forceinline__ void nb_row(const float* rowr, const float* rowp, bool zero,
+                                       float (&r)[4], float (&p)[4]) {
+  unpack4(lds4(rowr), r);
+  if (!zero) unpack4(lds4(rowp), p);
+  else p[0] = p[1] = p[2] = p[3] = 0.f;
 }
 
 // The four cells' updates from their six neighbours (k_smooth_split4's
@@ -136,25 +128,16 @@ __device__ __forceinline__ float4 relax4(const SweepArgs& A, const float (&rc)[4
   return make_float4(out[0], out[1], out[2], out[3]);
 }
 
-// Pointers to one plane's staged rows of each array, and to its new colour-A
-// rows, offset to this thread's quad.
-struct PlaneRows {
-  const float* pB;  // row jj of p_in colour B (by+4-row array)
-  const float* rB;  // row jj of rho colour B
-  const float* rA;  // row jj of rho colour A (by+2-row array)
-  float* nA;        // row jj of the new colour A
-};
-
 // kZero: the first colour relaxes from p = 0 (the first sweep after a zero
 // initial guess), so p_in is not read at all.
 template <bool kZero>
-__global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
+__global__ void __launch_bounds__(640, 1) k_sweep_split(SweepArgs A) {
   pdl_enter();
   extern __shared__ float4 sw_smem[];
   float* const sm = reinterpret_cast<float*>(sw_smem);
-  const int hx = A.hx;
-  const int rowsA = A.by + 2;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A.o_new + kSwNew * rowsA * hx);
+  const int hx = A.hx, rp = A.rp;
+  const int rowsA = A.by + 2, rowsB = A.by + 4;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A.o_wall + 2 * rp);
   const int tq = hx >> 2;                                 // threads per row
   const int q = threadIdx.x % tq, ra = threadIdx.x / tq;  // ra: row j0-1 .. j0+by
   const int m0 = 4 * q;
@@ -167,11 +150,34 @@ __global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
   const bool ym_ok = jj > 0, yp_ok = jj < A.ny - 1;
   const int c1 = 1 - A.c0;
   const size_t sz = (size_t)hx * A.ny;
-  const int offB = (ra + 1) * hx + m0;  // this thread's row in the by+4-row arrays
-  const int offA = ra * hx + m0;        // ... and in the by+2-row arrays
+  const float* wall_r = sm + A.o_wall + kSwGuard;       // +inf row
+  const float* wall_p = sm + A.o_wall + rp + kSwGuard;  // zero row
+  // guards and wall rows: +inf for densities, 0 for pressures, written once
+  {
+    const float inf = __int_as_float(0x7f800000);
+    const int nrows = kSwStages * (2 * rowsB + rowsA) + kSwNew * rowsA;
+    for (int e = threadIdx.x; e < nrows * 2 * kSwGuard; e += blockDim.x) {
+      const int row = e / (2 * kSwGuard), g = e % (2 * kSwGuard);
+      const int col = g < kSwGuard ? g : hx + g;  // 0..3 and hx+4..hx+7
+      float* base;
+      bool dens;
+      if (row < kSwStages * (2 * rowsB + rowsA)) {
+        const int st = row / (2 * rowsB + rowsA), r = row % (2 * rowsB + rowsA);
+        base = sm + st * A.stage + r * rp;  // pB rows, then rB, then rA
+        dens = r >= rowsB;
+      } else {
+        base = sm + A.o_new + (row - kSwStages * (2 * rowsB + rowsA)) * rp;
+        dens = false;
+      }
+      base[col] = dens ? inf : 0.f;
+    }
+    for (int e = threadIdx.x; e < rp; e += blockDim.x) {
+      sm[A.o_wall + e] = inf;
+      sm[A.o_wall + rp + e] = 0.f;
+    }
+  }
   // planes staged: [qlo, qhi]
   const int qlo = max(0, z0 - 2), qhi = min(A.nz - 1, z1 + 1);
-  const auto stage_base = [&](int slot) { return sm + slot * A.stage; };
   if (threadIdx.x == 0) {
     for (int s = 0; s < kSwStages; ++s) mbar_init(&bar[s], 1);
     fence_barrier_init();
@@ -180,54 +186,70 @@ __global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
   // the block's row ranges of the staged arrays, clamped to the grid
   const int loB = max(j0 - 2, 0), hiB = min(j0 + A.by + 2, A.ny);
   const int loA = max(j0 - 1, 0), hiA = min(j0 + A.by + 1, A.ny);
-  const uint32_t bytesB = (uint32_t)(hiB - loB) * hx * 4u, bytesA = (uint32_t)(hiA - loA) * hx * 4u;
+  const int nB = hiB - loB, nA = hiA - loA;
+  const uint32_t row_bytes = (uint32_t)hx * 4u;
   const float* pB_g = A.pin + (size_t)c1 * A.hstride + (size_t)loB * hx;
   const float* rB_g = A.rho + (size_t)c1 * A.hstride + (size_t)loB * hx;
   const float* rA_g = A.rho + (size_t)A.c0 * A.hstride + (size_t)loA * hx;
-  const int dstB = (loB - (j0 - 2)) * hx, dstA = (loA - (j0 - 1)) * hx;
-  const auto issue = [&](int k) {  // one thread
+  const int dB = loB - (j0 - 2), dA = loA - (j0 - 1);  // first staged row's index
+  // one plane's rows into its stage, a row per copy (rows are padded in shared
+  // memory), issued by the lanes of warp 0
+  const auto issue = [&](int k) {
     const int slot = (k - qlo) % kSwStages;
-    float* base = stage_base(slot);
+    float* base = sm + slot * A.stage;
     uint64_t* b = &bar[slot];
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive_expect_tx(b, (kZero ? 1u : 2u) * bytesB + bytesA);
+    const int lane = threadIdx.x;  // warp 0
+    if (lane == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive_expect_tx(b, ((kZero ? 1u : 2u) * nB + nA) * row_bytes);
+    }
+    __syncwarp();
     const size_t pk = (size_t)k * sz;
-    const auto copy = [&](float* dst, const float* src, uint32_t bytes) {
+    const int ncopy = (kZero ? 0 : nB) + nB + nA;
+    for (int c = lane; c < ncopy; c += 32) {
+      float* dst;
+      const float* src;
+      if (!kZero && c < nB) {
+        dst = base + (dB + c) * rp + kSwGuard;
+        src = pB_g + pk + (size_t)c * hx;
+      } else {
+        const int cc = kZero ? c : c - nB;
+        if (cc < nB) {
+          dst = base + A.o_rB + (dB + cc) * rp + kSwGuard;
+          src = rB_g + pk + (size_t)cc * hx;
+        } else {
+          dst = base + A.o_rA + (dA + cc - nB) * rp + kSwGuard;
+          src = rA_g + pk + (size_t)(cc - nB) * hx;
+        }
+      }
       asm volatile(
           "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-          ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(b))
+          ::"r"(smem_u32(dst)), "l"(src), "r"(row_bytes), "r"(smem_u32(b))
           : "memory");
-    };
-    if (!kZero) copy(base + dstB, pB_g + pk, bytesB);
-    copy(base + A.o_rB + dstB, rB_g + pk, bytesB);
-    copy(base + A.o_rA + dstA, rA_g + pk, bytesA);
+    }
   };
   const int t0 = max(z0 - 1, 0);
   int issued = min(qhi, t0 + 2);
-  if (threadIdx.x == 0)
+  if (threadIdx.x < 32)
     for (int k = qlo; k <= issued; ++k) issue(k);
   int waited = qlo - 1;
   // this thread's right-hand sides and outputs, advanced one plane per step
-  // (offsets in signed arithmetic: plane t0 - 1 may be -1, never dereferenced)
+  // (signed offsets: plane t0 - 1 may be -1, never dereferenced)
   const ptrdiff_t off0 = (ptrdiff_t)t0 * (ptrdiff_t)sz + (ptrdiff_t)jj * hx + m0;
   const float* bA_p = A.src + (ptrdiff_t)A.c0 * (ptrdiff_t)A.hstride + off0;
   const float* bB_p = A.src + (ptrdiff_t)c1 * (ptrdiff_t)A.hstride + off0 - (ptrdiff_t)sz;
   float* oA_p = A.pout + (ptrdiff_t)A.c0 * (ptrdiff_t)A.hstride + off0;
   float* oB_p = A.pout + (ptrdiff_t)c1 * (ptrdiff_t)A.hstride + off0 - (ptrdiff_t)sz;
-  // ring positions of planes t-2 .. t+1 (stages) and t-2 .. t (new colour A)
-  int sl = (t0 - qlo) % kSwStages;  // slot of plane t
+  // this thread's offsets inside a stage and the new ring (cell m0 of its row)
+  const int offB = (ra + 1) * rp + kSwGuard + m0;
+  const int offA = ra * rp + kSwGuard + m0;
+  int sl = (t0 - qlo) % kSwStages;  // stage slot of plane t
   int nl = t0 % kSwNew;             // new-ring slot of plane t
   const auto wrap5 = [](int v) { return v >= kSwStages ? v - kSwStages : (v < 0 ? v + kSwStages : v); };
   const auto wrap3 = [](int v) { return v >= kSwNew ? v - kSwNew : (v < 0 ? v + kSwNew : v); };
-  const auto rows_of = [&](int slot, int nslot) {
-    const float* base = stage_base(slot);
-    return PlaneRows{base + offB, base + A.o_rB + offB, base + A.o_rA + offA,
-                     sm + A.o_new + nslot * rowsA * hx + offA};
-  };
-  const int rowB = hx, rowA = hx;  // row pitch of the staged arrays
   for (int t = t0; t <= z1; ++t) {
     if (t + 2 <= qhi && t + 2 > issued) {
-      if (threadIdx.x == 0) issue(t + 2);
+      if (threadIdx.x < 32) issue(t + 2);
       issued = t + 2;
     }
     const int u = t - 1;
@@ -242,40 +264,50 @@ __global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
       const int slot = (waited - qlo) % kSwStages;
       mbar_wait(&bar[slot], (uint32_t)(((waited - qlo) / kSwStages) & 1), A.err);
     }
-    const PlaneRows Pm = rows_of(wrap5(sl - 1), wrap3(nl - 1));  // plane t-1
-    const PlaneRows P0 = rows_of(sl, nl);                          // plane t
+    const float* S0 = sm + sl * A.stage;
+    const float* Sm = sm + wrap5(sl - 1) * A.stage;
+    const float* Sp = sm + wrap5(sl + 1) * A.stage;
+    float* N0 = sm + A.o_new + nl * rowsA * rp;
+    const float* Nm = sm + A.o_new + wrap3(nl - 1) * rowsA * rp;
     // colour A of plane t on rows j0-1 .. j0+by
     if (doA) {
-      const PlaneRows Pp = rows_of(wrap5(sl + 1), nl);  // plane t+1 (stages only)
       const int par = (jj + t + A.c0) & 1;
+      const float* rB0 = S0 + A.o_rB + offB;  // row jj of rho colour B, cell m0
+      const float* pB0 = S0 + offB;
       float rc[4];
-      unpack4(lds4(P0.rA), rc);
+      unpack4(lds4(S0 + A.o_rA + offA), rc);
       float rxm[4], rxp[4], pxm[4], pxp[4];
-      x_window(P0.rB - m0, P0.pB - m0, m0, hx, par, kZero, rxm, rxp, pxm, pxp);
+      x_window(rB0 - 1 + par, pB0 - 1 + par, kZero, rxm, rxp, pxm, pxp);
       float rym[4], pym[4], ryp[4], pyp[4], rzm[4], pzm[4], rzp[4], pzp[4];
-      nb_row(P0.rB - rowB - m0, P0.pB - rowB - m0, m0, ym_ok, kZero, rym, pym);
-      nb_row(P0.rB + rowB - m0, P0.pB + rowB - m0, m0, yp_ok, kZero, ryp, pyp);
-      nb_row(Pm.rB - m0, Pm.pB - m0, m0, t > 0, kZero, rzm, pzm);
-      nb_row(Pp.rB - m0, Pp.pB - m0, m0, t < A.nz - 1, kZero, rzp, pzp);
+      nb_row(ym_ok ? rB0 - rp : wall_r + m0, ym_ok ? pB0 - rp : wall_p + m0, kZero, rym, pym);
+      nb_row(yp_ok ? rB0 + rp : wall_r + m0, yp_ok ? pB0 + rp : wall_p + m0, kZero, ryp, pyp);
+      const bool zm = t > 0, zp = t < A.nz - 1;
+      nb_row(zm ? Sm + A.o_rB + offB : wall_r + m0, zm ? Sm + offB : wall_p + m0, kZero, rzm, pzm);
+      nb_row(zp ? Sp + A.o_rB + offB : wall_r + m0, zp ? Sp + offB : wall_p + m0, kZero, rzp, pzp);
       const float4 v = relax4<kZero>(A, rc, bA, rxm, rxp, pxm, pxp, rym, pym, ryp, pyp, rzm, pzm,
                                      rzp, pzp);
-      sts4(P0.nA, v);
+      *reinterpret_cast<float4*>(N0 + offA) = v;
       if (own_row && t >= z0 && t < z1) *reinterpret_cast<float4*>(oA_p) = v;
     }
     __syncthreads();
     // colour B of plane u = t-1 on the block's rows, from the new colour A
     if (doB) {
-      const PlaneRows Pmm = rows_of(wrap5(sl - 2), wrap3(nl - 2));  // plane u-1
+      const float* Smm = sm + wrap5(sl - 2) * A.stage;
+      const float* Nmm = sm + A.o_new + wrap3(nl - 2) * rowsA * rp;
       const int par = (jj + u + c1) & 1;
       float rc[4];
-      unpack4(lds4(Pm.rB), rc);
+      unpack4(lds4(Sm + A.o_rB + offB), rc);
+      const float* rA0 = Sm + A.o_rA + offA;  // row jj of rho colour A, plane u, cell m0
+      const float* nA0 = Nm + offA;           // row jj of the new colour A, plane u
       float rxm[4], rxp[4], pxm[4], pxp[4];
-      x_window(Pm.rA - m0, Pm.nA - m0, m0, hx, par, false, rxm, rxp, pxm, pxp);
+      x_window(rA0 - 1 + par, nA0 - 1 + par, false, rxm, rxp, pxm, pxp);
       float rym[4], pym[4], ryp[4], pyp[4], rzm[4], pzm[4], rzp[4], pzp[4];
-      nb_row(Pm.rA - rowA - m0, Pm.nA - rowA - m0, m0, ym_ok, false, rym, pym);
-      nb_row(Pm.rA + rowA - m0, Pm.nA + rowA - m0, m0, yp_ok, false, ryp, pyp);
-      nb_row(Pmm.rA - m0, Pmm.nA - m0, m0, u > 0, false, rzm, pzm);
-      nb_row(P0.rA - m0, P0.nA - m0, m0, u < A.nz - 1, false, rzp, pzp);
+      nb_row(ym_ok ? rA0 - rp : wall_r + m0, ym_ok ? nA0 - rp : wall_p + m0, false, rym, pym);
+      nb_row(yp_ok ? rA0 + rp : wall_r + m0, yp_ok ? nA0 + rp : wall_p + m0, false, ryp, pyp);
+      const bool zm = u > 0, zp = u < A.nz - 1;
+      nb_row(zm ? Smm + A.o_rA + offA : wall_r + m0, zm ? Nmm + offA : wall_p + m0, false, rzm,
+             pzm);
+      nb_row(zp ? S0 + A.o_rA + offA : wall_r + m0, zp ? N0 + offA : wall_p + m0, false, rzp, pzp);
       const float4 v = relax4<false>(A, rc, bB, rxm, rxp, pxm, pxp, rym, pym, ryp, pyp, rzm, pzm,
                                      rzp, pzp);
       *reinterpret_cast<float4*>(oB_p) = v;
@@ -291,21 +323,24 @@ __global__ void __launch_bounds__(384) k_sweep_split(SweepArgs A) {
 }
 
 struct SweepShape {
-  int by, threads, smem, stage, o_rB, o_rA, o_new;
+  int by, threads, smem, rp, stage, o_rB, o_rA, o_new, o_wall;
 };
 
-// Rows per block for a row of hx half cells: about 256-384 threads.
+// Rows per block for a row of hx half cells (hx <= 256): 16 rows up to 128
+// half cells (576 threads at 128), 8 at 256 (640 threads).
 SweepShape sweep_shape(int hx) {
   SweepShape S{};
   const int tq = hx / 4;
-  S.by = hx <= 64 ? 16 : (hx <= 128 ? 8 : 4);
+  S.by = hx <= 128 ? 16 : 8;
   S.threads = tq * (S.by + 2);
-  S.stage = hx * (2 * (S.by + 4) + (S.by + 2));
+  S.rp = hx + 2 * kSwGuard;
+  S.stage = S.rp * (2 * (S.by + 4) + (S.by + 2));
   S.stage = (S.stage + 31) & ~31;  // 128-byte aligned stages
-  S.o_rB = hx * (S.by + 4);
-  S.o_rA = 2 * hx * (S.by + 4);
+  S.o_rB = S.rp * (S.by + 4);
+  S.o_rA = 2 * S.rp * (S.by + 4);
   S.o_new = kSwStages * S.stage;
-  const size_t floats = (size_t)S.o_new + (size_t)kSwNew * (S.by + 2) * hx;
+  S.o_wall = S.o_new + kSwNew * (S.by + 2) * S.rp;
+  const size_t floats = (size_t)S.o_wall + 2 * (size_t)S.rp;
   S.smem = (int)(floats * sizeof(float) + kSwStages * sizeof(uint64_t));
   return S;
 }
@@ -318,7 +353,7 @@ bool sweep_split_supported(int nx, int ny, int nz, size_t hstride) {
   const int hx = nx / 2;
   if (nx % 8 != 0 || hx > 256 || hstride % 4 != 0) return false;
   const SweepShape S = sweep_shape(hx);
-  return S.threads <= 384 && S.smem <= 227 * 1024;
+  return S.threads <= 640 && S.smem <= 227 * 1024;
 }
 
 // Both variants may use up to 227 KB of dynamic shared memory (each launch
@@ -350,7 +385,8 @@ void launch_sweep_split(cudaStream_t s, const LevelView<float>& L, const float* 
   A.kx = L.kx; A.ky = L.ky; A.kz = L.kz;
   A.c0 = first_color;
   A.err = err;
-  A.stage = S.stage; A.o_rB = S.o_rB; A.o_rA = S.o_rA; A.o_new = S.o_new;
+  A.rp = S.rp; A.stage = S.stage; A.o_rB = S.o_rB; A.o_rA = S.o_rA; A.o_new = S.o_new;
+  A.o_wall = S.o_wall;
   // z chunks: as many as fill the resident blocks of the device in one wave
   static int sms = 0;
   if (!sms) {
