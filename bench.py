@@ -193,23 +193,10 @@ def rho_form():
     return os.environ.get("GBMG_RHO_COEF", "1") != "0"
 
 
-def one_launch_sweep(shape):
-    """Whether the finest FP32 level sweeps with one launch per sweep
-    (k_sweep_split: colour-split density form, nx % 8 == 0, nx/2 <= 256;
-    GBMG_SWEEP=0 keeps one launch per colour)."""
-    nx = shape[2]
-    return (rho_form() and os.environ.get("GBMG_SPLIT", "1") != "0"
-            and os.environ.get("GBMG_SWEEP", "1") != "0" and nx % 8 == 0 and nx // 2 <= 256)
-
-
 def algorithmic_bytes_per_cell(cls, w=4, shape=None):
     c = w if rho_form() else 3.0 * w
-    # one sweep reads p, b and the coefficients and writes p; the one-launch
-    # sweep reads only the second colour's half of p (the first colour's old
-    # values never enter a Gauss-Seidel update)
-    p_read = 0.5 * w if shape is not None and one_launch_sweep(shape) else w
     return {
-        "smooth_fine": p_read + 2.0 * w + c,     # one sweep: p, b, coefficients read, p' write
+        "smooth_fine": 3.0 * w + c,              # one sweep: p, b, coefficients read, p' write
         "restrict_fine": 2.0 * w + c + 2.0 * w / 8,  # p, b, coefficients -> coarse b, sol
         "prolong_fine": 2.0 * w + w / 8,         # p r/w + coarse e
         "residual": 56.0,                        # defect: p(8) + e(4) + b(8) + 3 coefs(24) in,
@@ -993,7 +980,6 @@ def run_ours(args):
                     "share": ms_cls / total if total else None,
                     "algorithmic_bytes_per_launch": alg, "cells_per_launch": units,
                     "bytes_per_cell": algorithmic_bytes_per_cell(cls, 4, case.shape),
-                    "one_launch_sweep": one_launch_sweep(case.shape),
                     "coefficients": "density form" if rho_form() else "stored FP32"}
 
     e2e = None

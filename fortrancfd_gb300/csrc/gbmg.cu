@@ -48,7 +48,6 @@ struct Level {
   int split = 0;  // sol32, src32 and rho32 in the colour-split layout
   size_t hstride = 0;  // distance between the colour halves (elements)
   int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
-  int fsweep = 0;  // the split level sweeps with one launch per sweep (k_sweep_split)
 };
 
 enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
@@ -280,11 +279,7 @@ template <typename T> const T* adense_of(const gbmg_handle* h);
 template <> const double* adense_of<double>(const gbmg_handle* h) { return h->adense; }
 template <> const float* adense_of<float>(const gbmg_handle* h) { return h->adense32; }
 
-// One red-black sweep of level l: two colour launches in place, except on the
-// colour-split FP32 finest level, which sweeps in one launch out of place
-// (after which its solution lives in the other buffer: the host swaps the
-// pointers, and graph capture records the resulting sequence, which replays
-// identically).
+// One red-black sweep of level l: two colour launches in place.
 // zero_guess: the level's values are taken as zero (its first sweep after the
 // coarse unknown was started at zero, or the finest level of a correction
 // cycle), so no memset is needed and the first colour does not read p.
@@ -303,15 +298,8 @@ template <>
 void sweep<float>(gbmg_handle* h, int l, int first_color, bool zero_guess) {
   Level& lv = h->lv[l];
   const int cs = l == 0 ? GBMG_PROF_SMOOTH_FINE : GBMG_PROF_SMOOTH_COARSE;
-  if (lv.fsweep) {
-    // from a zero guess the one-launch sweep reads no p at all
-    LAUNCH(h, cs, launch_sweep_split(h->stream, v32(lv), lv.sol32, lv.alt32, first_color,
-                                     zero_guess, h->derr));
-    std::swap(lv.sol32, lv.alt32);
-  } else {
-    LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), first_color, zero_guess));
-    LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), 1 - first_color));
-  }
+  LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), first_color, zero_guess));
+  LAUNCH(h, cs, launch_smooth<float>(h->stream, view_next<float>(lv), 1 - first_color));
 }
 
 // Levels [h->sub_lc, L) as one single-block launch.
@@ -713,15 +701,6 @@ void set_rho_form(gbmg_handle* h, bool on) {
                              f.nx, f.ny, f.nz, hs);
     h->dmaps_split = oks;
   }
-  // one launch per sweep on the split level: even sweep counts (so that the
-  // level's unknown is back in its first buffer wherever the cycle reads it),
-  // rows of at most 256 half cells; GBMG_SWEEP=0 keeps the two colour launches
-  bool fs = split && h->prm.nu1 % 2 == 0 && h->prm.nu2 % 2 == 0 &&
-            sweep_split_supported(f.nx, f.ny, f.nz, hs) && sweep_split_init() == 0;
-  if (const char* e = std::getenv("GBMG_SWEEP"))
-    if (std::atoi(e) == 0) fs = false;
-  if ((int)fs != f.fsweep) reset_graphs(h);
-  f.fsweep = fs ? 1 : 0;
   f.rho32 = r;
   f.split = split ? 1 : 0;
   f.hstride = hs;

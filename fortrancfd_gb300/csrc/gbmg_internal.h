@@ -187,13 +187,6 @@ void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny
                      size_t hstride);
 void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz,
                        size_t hstride);
-// One whole red-black sweep of the colour-split finest level, out of place
-// (kernels_sweep.cu): first_color relaxes first; zero_guess: p_in is taken as
-// zero and not read.  *err |= 1 on a bulk-copy wait timeout.
-bool sweep_split_supported(int nx, int ny, int nz, size_t hstride);
-int sweep_split_init();
-void launch_sweep_split(cudaStream_t s, const LevelView<float>& L, const float* pin, float* pout,
-                        int first_color, bool zero_guess, int* err);
 // elements reserved past n in each split FP32 finest-level array for the pad
 constexpr size_t kSplitPadMax = 65536;
 

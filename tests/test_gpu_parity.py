@@ -430,12 +430,9 @@ def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     (None, None, False, (16, 16, 12))])
 def test_colour_split_layout_is_bit_identical(cuda, monkeypatch, idx, scale, krylov, shape):
     """The colour-split FP32 finest level (the default, with the density
-    form) does the natural-layout kernels' arithmetic in the same order, with
-    its sweeps either as one launch per sweep (k_sweep_split, the default) or
-    as one launch per colour (GBMG_SWEEP=0); GBMG_SPLIT=0 keeps the natural
-    layout.  All three: same cycles, same bits.  The shapes cover rows of 16
-    to 256 half cells (the sweep's 16-, 8- and 4-row blocks; 48 half cells
-    gives 12 threads per row), a 2D grid, and
+    form) does the natural-layout kernels' arithmetic in the same order
+    (GBMG_SPLIT=0 keeps the natural layout): same cycles, same bits.  The
+    shapes cover rows of 16 to 256 half cells, a 2D grid, and
     the 16 x 16 x 12 grid with nx % 8 != 0, whose split level keeps the
     colour launches and whose defect runs without TMA."""
     if shape is None:
@@ -448,19 +445,14 @@ def test_colour_split_layout_is_bit_identical(cuda, monkeypatch, idx, scale, kry
                                       radii=(0.3 * min(ext),), seed=3))
     out = {}
     monkeypatch.setenv("GBMG_RHO_COEF", "1")
-    for name, split, sweep in (("natural", "0", "1"), ("colour launches", "1", "0"),
-                               ("one-launch sweep", "1", "1")):
+    for name, split in (("natural", "0"), ("colour-split", "1")):
         monkeypatch.setenv("GBMG_SPLIT", split)
-        monkeypatch.setenv("GBMG_SWEEP", sweep)
         with solver(c, precision="mixed", krylov=krylov, max_cycles=400) as s:
             s.ppe_init(c.rho)
             out[name] = s.solve(c.b, tol=1e-10)
-    p0, s0 = out["natural"]
-    assert s0["status"] == 0
-    for name in ("colour launches", "one-launch sweep"):
-        p1, s1 = out[name]
-        assert s1["cycles"] == s0["cycles"], name
-        np.testing.assert_array_equal(p1, p0, err_msg=name)
+    (p0, s0), (p1, s1) = out["natural"], out["colour-split"]
+    assert s0["status"] == 0 and s1["cycles"] == s0["cycles"]
+    np.testing.assert_array_equal(p1, p0)
 
 
 
