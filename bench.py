@@ -44,6 +44,7 @@ NU1, NU2 = 2, 2  # V(2,2), the library's default
 # adjoint solves: the right-hand side p - p_t is smooth, so A^+ of it is large
 # and the attainable relative residual is higher than the forward's
 ADJ_TOL = 1e-8
+ADJ_TOL_LOOSE = 1e-7
 
 
 def parse():
@@ -820,6 +821,22 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
                 fw.append(e0.elapsed_time(e1))
                 bw.append(e1.elapsed_time(e2))
         g = x.grad
+        # the same timing with the adjoint solved to 1e-7 (the gradient still
+        # meets the differences below to well under 1e-6)
+        bw_loose = []
+        for it in range(reps + 1):
+            xl = phi.clone().requires_grad_(True)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            pl = pressure_solve(xl, b, s, tol=1e-10, adjoint_tol=ADJ_TOL_LOOSE, **kw)
+            e1.record(stream)
+            (0.5 * ((pl - p_t) ** 2).sum()).backward()
+            e2.record(stream)
+            torch.cuda.synchronize()
+            adj_cycles_loose = s.last_stats["cycles"]
+            if it:
+                bw_loose.append(e1.elapsed_time(e2))
+        g_loose = xl.grad
         # the same gradient from FP64 solves (forward 1e-12, adjoint 3e-9, the
         # adjoint's FP64 floor being about 2.6e-9)
         x64 = phi.clone().requires_grad_(True)
@@ -832,7 +849,7 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
             return 0.5 * ((q - p_t) ** 2).sum()
 
         rng = np.random.default_rng(7)
-        errs, errs64, errs_x = [], [], []
+        errs, errs64, errs_x, errs_xl = [], [], [], []
         with torch.no_grad():
             for _ in range(16):
                 v = torch.from_numpy(rng.standard_normal(case.shape)).to(dev)
@@ -843,6 +860,7 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
                 # the same central difference from its parts (no cancellation)
                 fdx = central_difference(s64, phi, b, p_t, v, 1e-6, **kw)
                 errs_x.append(abs(fdx - float((g * v).sum())) / abs(fdx))
+                errs_xl.append(abs(fdx - float((g_loose * v).sum())) / abs(fdx))
         s.close()
         s64.close()
     f, bk = float(np.median(fw)), float(np.median(bw))
@@ -856,6 +874,12 @@ def adjoint_section(dev, stream, reps=5, scale=1, krylov="fgmres"):
             "fd_directions": len(errs),
             "fd_exact_max_rel_err": max(errs_x),
             "fd_exact_median_rel_err": float(np.median(errs_x)),
+            "adjoint_tol": ADJ_TOL,
+            "loose_adjoint_tol": ADJ_TOL_LOOSE,
+            "loose_backward_ms": float(np.median(bw_loose)),
+            "loose_backward_over_forward": float(np.median(bw_loose)) / f,
+            "loose_adjoint_iterations": adj_cycles_loose,
+            "loose_fd_exact_max_rel_err": max(errs_xl),
             "fp64_gradient_max_rel_diff": max(errs64),
             "fp64_gradient_rel_l2_diff": float((g - g64).norm() / g64.norm())}
 
@@ -1130,6 +1154,9 @@ def scalar_summary(fp64, parity, adj, multi, roll, tstep):
     put("adj_fd_directions", adj, "fd_directions")
     put("adj_fd_exact_max_rel", adj, "fd_exact_max_rel_err")
     put("adj_fd_exact_median_rel", adj, "fd_exact_median_rel_err")
+    put("adj_loose_tol", adj, "loose_adjoint_tol")
+    put("adj_loose_backward_over_forward", adj, "loose_backward_over_forward")
+    put("adj_loose_fd_exact_max_rel", adj, "loose_fd_exact_max_rel_err")
     put("adj_vs_fp64_gradient_max_rel", adj, "fp64_gradient_max_rel_diff")
     put("error_adjoint", adj, "error")
     put("rollout_forward_ms", roll, "forward_ms")

@@ -1046,23 +1046,27 @@ int start_mixed(gbmg_handle* h, bool* shifted) {
   GB_TRY(read_result(h, kSlotSum + 1, &pp));
   *shifted = pp != 0.0;
   if (*shifted) {
+    // the correction starts at d = 0, so its first residual is r0 itself:
+    // the loop's right-hand side in double-word and the FP32 cycle's input
     if (!h->r0) GB_TRY(dmalloc(h, &h->r0, n));
     f.sol = h->p; f.src = h->b;
     LAUNCH(h, GBMG_PROF_RESIDUAL, launch_residual_norm<double>(s, v64(f), h->r0, h->red, kSlotNorm));
     LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->r0, h->bw, n));
-    GB_CUDA(h, cudaMemsetAsync(h->pw[0], 0, n * sizeof(float2), s));
+    if (f.split) LAUNCH(h, GBMG_PROF_VECTOR, launch_to_split(s, h->r0, f.src32, f.nx, f.ny, f.nz, f.hstride));
+    else LAUNCH(h, GBMG_PROF_VECTOR, launch_double_to_float(s, h->r0, f.src32, n));
+    GB_CUDA(h, cudaMemsetAsync(h->pw[1], 0, n * sizeof(float2), s));
   } else {
     LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
+    // the first residual (no correction yet)
+    LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
   }
-  // the first residual (no correction yet)
-  LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
   h->pcur = 1;
   return GBMG_OK;
 }
 
 // The mixed loop's result into h->p, mean-free (compatibility_sol on the
-// finest level); restores the double-word right-hand side after a correction
-// solve.
+// finest level).  After a correction solve the double-word right-hand side
+// still holds r0; every solve writes it afresh before its loop.
 int finish_mixed(gbmg_handle* h, bool shifted) {
   const cudaStream_t s = h->stream;
   const size_t n = h->n0;
@@ -1070,7 +1074,6 @@ int finish_mixed(gbmg_handle* h, bool shifted) {
     LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_accumulate(s, h->pw[h->pcur], h->p, n));
     LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
     LAUNCH(h, GBMG_PROF_VECTOR, launch_shift_by_mean(s, h->p, h->p, n, h->red, kSlotSum, -1));
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->b, h->bw, n));
   } else {
     LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_sum(s, h->pw[h->pcur], n, h->red, kSlotSum));
     LAUNCH(h, GBMG_PROF_VECTOR, launch_dw_out(s, h->pw[h->pcur], h->p, n, h->red, kSlotSum));
