@@ -662,7 +662,7 @@ def timestep_section(dev, stream, case, steps=5):
     itf = InterfaceParams(ls_wid=case.eps, rho_12=rho_12, rdt=0.25 * case.spacing[0],
                           redis_every=5, method=2)
     with torch.cuda.stream(stream):
-        ts = TwoPhaseStep(case.shape, case.spacing, ns, itf, precision="mixed", krylov=True,
+        ts = TwoPhaseStep(case.shape, case.spacing, ns, itf, precision="mixed", krylov=False,
                           stream=stream)
         ts.load(st["phi"], st["u"], st["v"], st["w"])
         ts.step()  # warm-up (step 1)
@@ -698,7 +698,7 @@ def timestep_section(dev, stream, case, steps=5):
         # steps 2 and 4 without redistancing, 3 with (every third step)
         itf3 = InterfaceParams(ls_wid=case.eps, rho_12=rho_12, rdt=0.25 * case.spacing[0],
                                redis_every=3, method=3, recon_every=10)
-        ts = TwoPhaseStep(case.shape, case.spacing, ns, itf3, precision="mixed", krylov=True,
+        ts = TwoPhaseStep(case.shape, case.spacing, ns, itf3, precision="mixed", krylov=False,
                           stream=stream)
         ts.load(st["phi"], st["u"], st["v"], st["w"])
         ts.step()
@@ -719,7 +719,7 @@ def timestep_section(dev, stream, case, steps=5):
                         f"(dt={dt}; MPLS level set, the input default: advection every step, "
                         "redistancing btn=1 every fifth step at rdt=0.25 dx, two mass-preserving "
                         "corrections; rho_mu, CCD curvature, AB2 momentum step "
-                        f"with 4 mixed flexible-CG projections to {TOL}, divergence check)",
+                        f"with 4 mixed stationary-cycle projections to {TOL}, divergence check)",
             "steps_timed": [s["iter"] for s in stats], "ms_per_step": times,
             "ms_mean": sum(times) / len(times),
             "ms_without_redistancing": statistics.median(plain) if plain else None,
