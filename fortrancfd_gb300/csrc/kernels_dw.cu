@@ -179,6 +179,22 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       tma_load_3d(qtile_e(base, s), &maps.e, x0 - 4, yq, k, &bar[s]);
     }
   };
+  // this thread's box cells for the p + e update (at most two: the box has
+  // kQTile cells for kDTX * kDTY threads), with their e offsets worked out
+  // once: the split e box holds a cell of parity c at c * kQSEOff + its row's
+  // offset, and the parity of box cell (x, y) flips with every plane
+  constexpr int kBoxPer = (kQTile + kDTX * kDTY - 1) / (kDTX * kDTY);
+  static_assert(kBoxPer == 2, "two box cells per thread");
+  int boff[kBoxPer], eoff[kBoxPer], bpar[kBoxPer];
+#pragma unroll
+  for (int u = 0; u < kBoxPer; ++u) {
+    const int t = tid + u * kDTX * kDTY;
+    boff[u] = t < kQTile ? t : -1;
+    const int row = t / kQBX, col = t % kQBX;
+    const int xx = x0 - 2 + col, yy = y0 - 1 + row;
+    eoff[u] = split ? row * kQSEX + ((xx >> 1) - (x0 >> 1) + 4) : row * kQEX + col + 2;
+    bpar[u] = (xx + yy) & 1;
+  }
   uint32_t parity = 0;
   const int pre_end = min(z0 + 1, phi);
   if (tid == 0)
@@ -200,18 +216,14 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       if (use_e) {  // p + e on the whole box
         float2* P = qtile(base, s, 0);
         const float* E = qtile_e(base, s);
-        for (int t = tid; t < kQTile; t += kDTX * kDTY) {
-          const int row = t / kQBX, col = t % kQBX;
-          float ev;
-          if (split) {
-            // box cell (row, col) is x = x0-2+col, y = y0-1+row of plane `waited`
-            const int xx = x0 - 2 + col, yy = y0 - 1 + row;
-            const int c = (xx + yy + waited) & 1;
-            ev = E[c * kQSEOff + row * kQSEX + ((xx >> 1) - (x0 >> 1) + 4)];
-          } else {
-            ev = E[row * kQEX + col + 2];
-          }
-          const dw a = dw_add_f(dw{P[t].x, P[t].y}, ev);
+#pragma unroll
+        for (int u = 0; u < kBoxPer; ++u) {
+          const int t = boff[u];
+          if (t < 0) continue;
+          // box cell (row, col) is x = x0-2+col, y = y0-1+row of plane `waited`
+          const float ev = E[split ? ((bpar[u] + waited) & 1) * kQSEOff + eoff[u] : eoff[u]];
+          const float2 pv = P[t];
+          const dw a = dw_add_f(dw{pv.x, pv.y}, ev);
           P[t] = make_float2(a.hi, a.lo);
         }
       }
