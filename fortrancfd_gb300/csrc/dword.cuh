@@ -115,11 +115,6 @@ __device__ __forceinline__ double dw_to_double_int(dw a) {
   return float_to_double_int(a.hi) + float_to_double_int(a.lo);
 }
 
-// Accumulator of sum_f c_f (p_nb - p_c) with cascaded summation: the high
-// parts are added error-free with TwoSum, everything of order u|term| goes
-// into one float.  Absolute error O(u^2 sum |c_f (p_nb - p_c)|), the bound the
-// residual needs; about 19 FP32 operations per term instead of ~30 with the
-// normalised double-word operations.
 // One flux term t = c (nb - pc), unnormalised (th + tl).  Every operation is
 // sign-symmetric, so flux_term(c, pc, nb) is exactly -flux_term(c, nb, pc):
 // a face's term can be computed once and used, negated, by its other cell.
@@ -135,16 +130,21 @@ __device__ __forceinline__ dw flux_term(dw c, dw nb, dw pc) {
   return dw{th, tl};
 }
 
-struct flux_acc {
-  float hi = 0.f, lo = 0.f;
-  // acc += t
-  __device__ __forceinline__ void add(dw t) {
-    const dw a = two_sum(hi, t.hi);
+// The residual b - sum_f t_f with cascaded summation started from b: the high
+// parts are subtracted error-free with TwoSum, everything of order u|term|
+// goes into one float.  Absolute error O(u^2 (|b| + sum |t_f|)), the bound
+// the residual needs; the residual is needed only as a float (hi + lo), so
+// no normalisation and no double-word subtraction follow.
+struct residual_acc {
+  float hi, lo;
+  __device__ __forceinline__ explicit residual_acc(dw b) : hi(b.hi), lo(b.lo) {}
+  // acc -= t
+  __device__ __forceinline__ void sub(dw t) {
+    const dw a = two_sum(hi, -t.hi);
     hi = a.hi;
-    lo += a.lo + t.lo;
+    lo += a.lo - t.lo;
   }
-  __device__ __forceinline__ void add_term(dw c, dw nb, dw pc) { add(flux_term(c, nb, pc)); }
-  __device__ __forceinline__ dw value() const { return fast_two_sum(hi, lo); }
+  __device__ __forceinline__ float value_f() const { return hi + lo; }
 };
 
 __device__ __forceinline__ dw dw_load(const float2* p) {

@@ -88,11 +88,11 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
       const size_t q = (size_t)k * sz + (size_t)y * sy + x;
       const float2 c2 = ring.p[s0][ty + 1][tx + 1];
       const dw pc{c2.x, c2.y};
-      flux_acc acc;
+      residual_acc acc(dw_ldg(A.b + q));
 #define DW_TERM(cond, cptr, nbv)                                   \
       if (cond) {                                                  \
         const float2 nb = nbv;                                     \
-        acc.add_term(dw_ldg(cptr), dw{nb.x, nb.y}, pc);            \
+        acc.sub(flux_term(dw_ldg(cptr), dw{nb.x, nb.y}, pc));      \
       }
       DW_TERM(x > 0, A.cx + q, ring.p[s0][ty + 1][tx])
       DW_TERM(x < A.nx - 1, A.cx + q + 1, ring.p[s0][ty + 1][tx + 2])
@@ -101,8 +101,7 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
       DW_TERM(k > 0, A.cz + q, ring.p[sm][ty + 1][tx + 1])
       DW_TERM(k < A.nz - 1, A.cz + q + sz, ring.p[sp][ty + 1][tx + 1])
 #undef DW_TERM
-      const dw r = dw_sub(dw_ldg(A.b + q), acc.value());
-      const float rf = dw_to_float(r);
+      const float rf = acc.value_f();
       r32[fine_index(q, x, y, k, hstride)] = rf;
       s2 = fmaf(rf, rf, s2);
     }
@@ -255,17 +254,16 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
       if (k < nz - 1) fzp = flux_term(ld(qtile(base, sp, 4), t), ld(qtile(base, sp, 0), t), pc);
       fz_carry = fzp;
       if (x < nx && y < ny) {
-        flux_acc acc;
-        acc.add(fxm);
-        acc.add(fxp);
-        acc.add(fym);
-        acc.add(fyp);
-        if (k > 0) acc.add(fzm);
-        if (k < nz - 1) acc.add(fzp);
         const float2 b2 = qtile(base, s0, 1)[t];
-        const dw r = dw_sub(dw{b2.x, b2.y}, acc.value());
+        residual_acc acc(dw{b2.x, b2.y});
+        acc.sub(fxm);
+        acc.sub(fxp);
+        acc.sub(fym);
+        acc.sub(fyp);
+        if (k > 0) acc.sub(fzm);
+        if (k < nz - 1) acc.sub(fzp);
         const size_t q = ((size_t)k * ny + y) * nx + x;
-        const float rf = dw_to_float(r);
+        const float rf = acc.value_f();
         r32[fine_index(q, x, y, k, hstride)] = rf;
         pout[q] = pc2;
         s2 = fmaf(rf, rf, s2);
