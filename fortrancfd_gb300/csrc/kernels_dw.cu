@@ -201,12 +201,11 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
   int issued = pre_end, waited = plo - 1;
   float s2 = 0.f;
   dw fz_carry{0.f, 0.f};  // z flux between planes k-1 and k, computed at plane k-1
-  // One block barrier per plane: the one after the p + e update of the newly
-  // arrived plane k+1.  Plane k+2 is issued after it, into the slot of plane
-  // k-2, which only the compute of plane k-1 read (before that barrier); the
-  // update of plane k+1 and the compute of plane k touch four distinct slots
-  // (k-1 .. k+2), so no barrier is needed at the end of the step.
   for (int k = z0; k < z1; ++k) {
+    if (k + 2 <= phi && k + 2 > issued) {
+      if (tid == 0) issue(k + 2);
+      issued = k + 2;
+    }
     const int need = min(k + 1, phi);
     while (waited < need) {
       ++waited;
@@ -228,10 +227,6 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
         }
       }
       __syncthreads();
-    }
-    if (k + 2 <= phi && k + 2 > issued) {
-      if (tid == 0) issue(k + 2);
-      issued = k + 2;
     }
     // Face terms in the order x-, x+, y-, y+, z-, z+; the z- term is the
     // previous plane's z+ term negated (flux_term is sign-symmetric, so this
@@ -274,6 +269,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
         s2 = fmaf(rf, rf, s2);
       }
     }
+    __syncthreads();
   }
   double v[1] = {(double)s2};
   grid_sum_finish<1>(v, R, slot);
