@@ -19,7 +19,6 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
-#include <cmath>
 
 #include "dword.cuh"
 #include "gbmg_internal.h"
@@ -69,12 +68,12 @@ __global__ void __launch_bounds__(kDTX * kDTY) k_defect(DwOperator A, const floa
                                                         float2* __restrict__ pout,
                                                         const float* __restrict__ e,
                                                         float* __restrict__ r32, ReduceScratch R,
-                                                        int slot, size_t hstride, int zc) {
+                                                        int slot, size_t hstride) {
   pdl_enter();
   __shared__ DefectRing ring;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
   const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
-  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, A.nz);
+  const int z0 = blockIdx.z * kDZ, z1 = min(z0 + kDZ, A.nz);
   const int x = x0 + tx, y = y0 + ty;
   const bool mine = x < A.nx && y < A.ny;
   const size_t sy = (size_t)A.nx, sz = (size_t)A.nx * A.ny;
@@ -145,7 +144,7 @@ __device__ __forceinline__ float* qtile_e(unsigned char* base, int slot) {
 __global__ void __launch_bounds__(kDTX * kDTY, 3)
     k_defect_tma(const __grid_constant__ DefectMaps maps, int nx, int ny, int nz, int use_e,
                  float2* __restrict__ pout, float* __restrict__ r32, ReduceScratch R, int slot,
-                 int* err, size_t hstride, int zc) {
+                 int* err, size_t hstride) {
   pdl_enter();
   const bool split = hstride != 0;
   extern __shared__ unsigned char dsm_raw[];
@@ -154,7 +153,7 @@ __global__ void __launch_bounds__(kDTX * kDTY, 3)
   uint64_t* bar = reinterpret_cast<uint64_t*>(base + (size_t)kQSlots * kQSlotBytes);
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDTX + tx;
   const int x0 = blockIdx.x * kDTX, y0 = blockIdx.y * kDTY;
-  const int z0 = blockIdx.z * zc, z1 = min(z0 + zc, nz);
+  const int z0 = blockIdx.z * kDZ, z1 = min(z0 + kDZ, nz);
   const int plo = max(z0 - 1, 0), phi = min(z1, nz - 1);
   if (tid == 0) {
     for (int s = 0; s < kQSlots; ++s) mbar_init(&bar[s], 1);
@@ -313,50 +312,15 @@ inline unsigned stride_blocks(size_t n) {
 
 }  // namespace
 
-// z planes per block of the defect kernels.  A block marches over a chunk of
-// planes and loads two halo planes besides, so long chunks waste less; but
-// the last wave of blocks is partly empty unless the block count fills the
-// resident slots (3 blocks per SM for the TMA kernel).  The chunk length
-// maximises the useful planes over the slot time spent, tiles * nz /
-// (slots * whole waves * (zc + 2)): 37 planes (7 chunks, 3.93 waves on 152
-// SMs) for a 256^3 grid instead of 32 (8 chunks, 4.49 waves).
-int defect_zchunk(int nx, int ny, int nz) {
-  static int slots = 0;
-  if (!slots) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_defect_tma, kDTX * kDTY,
-                                                      kQSmem) != cudaSuccess)
-      cudaGetLastError();
-    slots = std::max(1, sms) * std::max(1, per_sm);
-  }
-  if (nz <= 8) return nz;
-  const double tiles = (double)((nx + kDTX - 1) / kDTX) * ((ny + kDTY - 1) / kDTY);
-  int best_zc = kDZ;
-  double best = -1.0;
-  for (int zc = 8; zc <= std::min(nz, 128); ++zc) {
-    const int ch = (nz + zc - 1) / zc;
-    const double waves = std::ceil(tiles * ch / slots);
-    const double eff = tiles * nz / (slots * waves * (zc + 2.0));
-    if (eff > best + 1e-12) {
-      best = eff;
-      best_zc = zc;
-    }
-  }
-  return best_zc;
-}
-
 dim3 defect_grid(int nx, int ny, int nz) {
-  const int zc = defect_zchunk(nx, ny, nz);
   return dim3((unsigned)((nx + kDTX - 1) / kDTX), (unsigned)((ny + kDTY - 1) / kDTY),
-              (unsigned)((nz + zc - 1) / zc));
+              (unsigned)((nz + kDZ - 1) / kDZ));
 }
 
 void launch_defect(cudaStream_t s, const DwOperator& A, const float2* pin, float2* pout,
                    const float* e, float* r32, const ReduceScratch& R, int slot, size_t hstride) {
   launch_pdl(k_defect, defect_grid(A.nx, A.ny, A.nz), dim3(kDTX, kDTY), 0, s, A, pin, pout, e,
-             r32, R, slot, hstride, defect_zchunk(A.nx, A.ny, A.nz));
+             r32, R, slot, hstride);
 }
 
 // A 3D tiled map over a dense (nx, ny, nz) array (cuTensorMapEncodeTiled via
@@ -417,7 +381,7 @@ void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, i
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
                        size_t hstride) {
   launch_pdl(k_defect_tma, defect_grid(nx, ny, nz), dim3(kDTX, kDTY), kQSmem, s, maps, nx, ny, nz,
-             use_e ? 1 : 0, pout, r32, R, slot, err, hstride, defect_zchunk(nx, ny, nz));
+             use_e ? 1 : 0, pout, r32, R, slot, err, hstride);
 }
 
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {
