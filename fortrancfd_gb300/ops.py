@@ -12,7 +12,10 @@ counterpart; the reference's solvers are Fortran subroutines with no tensor
 interface).  precision: "fp64" or "mixed".
 
 Handles (the multigrid hierarchy on the device) are cached per shape,
-spacing, precision and device, so repeated calls allocate nothing new.
+spacing, precision and device, so repeated calls allocate nothing new.  A
+handle is not re-entrant, so every call holds its handle's lock from setting
+the operator to the end of the solve (and of the adjoint in backward): calls
+from several host threads on the same shape take turns.
 """
 import threading
 
@@ -25,21 +28,24 @@ _lock = threading.Lock()
 
 
 def _handle(shape, spacing, precision, device):
+    """(handle, its lock) for this shape, spacing, precision and device."""
     key = (tuple(shape), tuple(spacing), precision, device.index)
     with _lock:
-        s = _handles.get(key)
-        if s is None:
+        entry = _handles.get(key)
+        if entry is None:
             s = PressurePoisson(shape, spacing, precision=precision, krylov=True,
                                 max_cycles=400, device=device.index)
-            _handles[key] = s
-        return s
+            entry = (s, threading.Lock())
+            _handles[key] = entry
+        return entry
 
 
 def clear_cache():
     """Destroy the cached handles (frees their device memory)."""
     with _lock:
-        for s in _handles.values():
-            s.close()
+        for s, lock in _handles.values():
+            with lock:
+                s.close()
         _handles.clear()
 
 
@@ -54,10 +60,11 @@ def _check(rho, b):
 def solve(rho: torch.Tensor, b: torch.Tensor, dx: float, dy: float, dz: float, tol: float,
           adjoint_tol: float, precision: str) -> torch.Tensor:
     _check(rho, b)
-    s = _handle(b.shape, (dx, dy, dz), precision, b.device)
-    s.ppe_init(rho.contiguous())
+    s, lock = _handle(b.shape, (dx, dy, dz), precision, b.device)
     p = torch.zeros_like(b, memory_format=torch.contiguous_format)
-    s.solve(b.contiguous(), p, tol=tol)
+    with lock:
+        s.ppe_init(rho.contiguous())
+        s.solve(b.contiguous(), p, tol=tol)
     return p
 
 
@@ -75,11 +82,12 @@ def _setup_context(ctx, inputs, output):
 def _backward(ctx, grad_p):
     rho, p = ctx.saved_tensors
     dx, dy, dz, adjoint_tol, precision = ctx.cfg
-    s = _handle(p.shape, (dx, dy, dz), precision, p.device)
-    s.ppe_init(rho.contiguous())
+    s, lock = _handle(p.shape, (dx, dy, dz), precision, p.device)
     lam = torch.zeros_like(p)
-    s.solve(grad_p.contiguous(), lam, tol=adjoint_tol)
-    grad_rho = s.adjoint(p, lam)[0] if ctx.needs_input_grad[0] else None
+    with lock:
+        s.ppe_init(rho.contiguous())
+        s.solve(grad_p.contiguous(), lam, tol=adjoint_tol)
+        grad_rho = s.adjoint(p, lam)[0] if ctx.needs_input_grad[0] else None
     grad_b = lam if ctx.needs_input_grad[1] else None
     return grad_rho, grad_b, None, None, None, None, None, None
 

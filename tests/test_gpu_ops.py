@@ -75,3 +75,36 @@ def test_rho_gradient_matches_central_differences(cuda):
     fd = float((jp - jm) / (2 * h))
     # as the autograd Function's rho test: 2e-6 (the adjoint's FP64 floor)
     assert abs(fd - float((rho.grad * v).sum())) <= 2e-6 * abs(fd)
+
+
+@pytest.mark.gpu
+def test_concurrent_calls_from_two_threads(cuda):
+    """Two host threads call the operator on the same shape (one cached
+    handle) with different densities: each result equals the one computed
+    alone, because every call holds its handle's lock for the whole solve."""
+    import threading
+
+    c = cases.config(1, 8)
+    rhos = [torch.from_numpy(c.rho).to(cuda), torch.from_numpy(c.rho[::-1].copy()).to(cuda)]
+    b = torch.from_numpy(c.b).to(cuda)
+    want = [torch.ops.gbmg.solve(r, b, *c.spacing, 1e-10, 1e-10, "fp64") for r in rhos]
+    got = [[None] * 4 for _ in rhos]
+    errors = []
+
+    def run(i):
+        try:
+            torch.cuda.set_device(cuda)
+            for k in range(4):
+                got[i][k] = torch.ops.gbmg.solve(rhos[i], b, *c.spacing, 1e-10, 1e-10, "fp64")
+        except Exception as exc:  # reported below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for i in range(2):
+        for k in range(4):
+            assert torch.equal(got[i][k], want[i]), (i, k)
