@@ -24,193 +24,14 @@
 #include <vector>
 
 #include "gbmg.h"
-#include "fdiv.cuh"
 #include "gbmg_internal.h"
+#include "handle.h"
 
 using namespace gbmg;
+using namespace gbmg::host;
+
 
 namespace {
-
-struct Level {
-  int nx = 0, ny = 0, nz = 0;
-  int fx = 1, fy = 1, fz = 1;
-  size_t n = 0;
-  double *cx = nullptr, *cy = nullptr, *cz = nullptr, *idiag = nullptr;
-  double *sol = nullptr, *src = nullptr;  // owned on levels >= 1
-  float *cx32 = nullptr, *cy32 = nullptr, *cz32 = nullptr;
-  float *sol32 = nullptr, *src32 = nullptr;
-  float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
-  float* buf_a = nullptr;  // the buffer sol32 pointed to at allocation
-  // FP32 kernels take the coefficients from this density instead of cx32..cz32
-  // (finest level of a mixed solve whose operator came from rho or phi)
-  const float* rho32 = nullptr;
-  float k32[3] = {0.f, 0.f, 0.f};  // 2/h^2 per axis
-  int split = 0;  // sol32, src32 and rho32 in the colour-split layout
-  size_t hstride = 0;  // distance between the colour halves (elements)
-  int zrev = 0;   // direction of the next split-kernel launch (toggles per launch)
-};
-
-enum GraphKind { kGraphNone = -1, kGraphFp64 = 0, kGraphMixed = 1, kGraphPcg64 = 2, kGraphPcgMixed = 3 };
-constexpr int kGmresRestart = 30;   // flexible GMRES restart length
-constexpr int kGmresBlocks = 1024;  // blocks of its dot-product kernel
-
-}  // namespace
-
-struct gbmg_handle {
-  gbmg_grid grid{};
-  gbmg_params prm{};
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  int L = 0;
-  Level lv[kMaxLevels];
-  size_t n0 = 0;
-  bool mixed = false;
-  // fine-level buffers
-  double* b = nullptr;    // mean-free right-hand side
-  double* p = nullptr;    // pressure being solved for
-  double* rho = nullptr;  // cell density of the current operator
-  float* rho32 = nullptr; // its FP32 copy (mixed precision)
-  double* vel[3] = {nullptr, nullptr, nullptr};
-  size_t vel_n[3] = {0, 0, 0};
-  double* aux[2] = {nullptr, nullptr};  // adjoint outputs / staging, allocated on first use
-  double* r0 = nullptr;  // initial FP64 residual of a warm-started mixed solve (first use)
-  // flexible CG vectors (allocated when krylov = 1)
-  double *kr = nullptr, *kz = nullptr, *kzold = nullptr, *kd = nullptr, *kq = nullptr;
-  // flexible GMRES (krylov = 2): basis V (restart + 1 vectors), preconditioned
-  // vectors Z (restart), dot partials, device and pinned host coefficients
-  double *gmV = nullptr, *gmZ = nullptr, *gmPart = nullptr, *gmDev = nullptr, *gmHost = nullptr;
-  // coarsest level
-  int nc = 0;
-  double *minv = nullptr, *adense = nullptr, *cwork = nullptr;
-  float *minv32 = nullptr, *adense32 = nullptr;
-  // reductions
-  ReduceScratch red{};
-  double* host_res = nullptr;  // pinned mirror of red.result
-  // double-word finest level of the mixed solve: p (ping-pong), b, coefficients
-  float2* pw[2] = {nullptr, nullptr};
-  float2* bw = nullptr;
-  float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
-  int pcur = 0;  // which pw holds the current pressure
-  int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
-  int* derr = nullptr;   // device error flags (bulk-copy wait timeouts)
-  DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B],
-                                // then [p buffer] with a colour-split e (buffer A)
-  bool dmaps_split = false;     // whether the colour-split entries were made
-  // captured iterations, per kind and per parity of pcur
-  cudaGraphExec_t graph[4][2] = {};
-  int64_t graph_kernels[4][2] = {};
-  // flexible GMRES: kz = M kr and kq = A kz as one captured graph
-  cudaGraphExec_t gm_graph = nullptr;
-  int64_t gm_graph_kernels = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // host transfers of a solve that overlap its kernels: the H2D of the initial
-  // p beside the right-hand side's preparation, the D2H of the result beside
-  // the FP64 certification
-  cudaStream_t cstream = nullptr;
-  cudaEvent_t cev[2] = {nullptr, nullptr};
-  const gbmg_field* dl_field = nullptr;  // set by gbmg_solve for solve_internal
-  bool dl_started = false;
-  int64_t launches = 0;
-  // profiling: event pairs around launches, summed per kernel class
-  bool prof = false;
-  cudaEvent_t pev[2 * 512] = {};
-  int pcls[512] = {};
-  int pused = 0;
-  double prof_ms[GBMG_PROF_CLASSES] = {};
-  int64_t prof_n[GBMG_PROF_CLASSES] = {};
-  bool coef_ready = false;
-  bool fine_copies = false;  // finest FP32 / double-word coefficients already written
-  bool rho_ready = false;
-  bool split_ready = false;  // gbmg_set_split: constant Laplacian + density for the split source
-  double split_rho12 = 0.0;
-  // momentum step: padded-box buffers (vel%tmp, velsrc%tmp, and the host
-  // staging copies of the caller's arrays), allocated on first use
-  double* ns_buf[48] = {};
-  size_t ns_n[48] = {};
-  // CCD factor table of each axis is valid for these line lengths and spacings
-  int ccd_L[3] = {0, 0, 0};
-  double ccd_h[3] = {0.0, 0.0, 0.0};
-  std::string err;
-};
-
-namespace {
-
-#define GB_CUDA(h, call)                                                        \
-  do {                                                                          \
-    cudaError_t e_ = (call);                                                    \
-    if (e_ != cudaSuccess) {                                                    \
-      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
-      return e_ == cudaErrorMemoryAllocation ? GBMG_OUT_OF_MEMORY : GBMG_CUDA_ERROR; \
-    }                                                                           \
-  } while (0)
-
-#define GB_TRY(expr)            \
-  do {                          \
-    int rc_ = (expr);           \
-    if (rc_ != GBMG_OK) return rc_; \
-  } while (0)
-
-int check_launch(gbmg_handle* h, const char* what) {
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    h->err = std::string(what) + ": " + cudaGetErrorString(e);
-    return GBMG_CUDA_ERROR;
-  }
-  return GBMG_OK;
-}
-
-// Sum the recorded event pairs into the per-class totals (syncs the stream).
-void prof_flush(gbmg_handle* h) {
-  if (!h->pused) return;
-  cudaStreamSynchronize(h->stream);
-  for (int i = 0; i < h->pused; ++i) {
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, h->pev[2 * i], h->pev[2 * i + 1]) == cudaSuccess) {
-      h->prof_ms[h->pcls[i]] += ms;
-      h->prof_n[h->pcls[i]] += 1;
-    }
-  }
-  h->pused = 0;
-}
-
-void prof_begin(gbmg_handle* h) {
-  if (!h->prof) return;
-  if (h->pused == 512) prof_flush(h);
-  cudaEvent_t& e = h->pev[2 * h->pused];
-  if (!e) cudaEventCreate(&e);
-  cudaEventRecord(e, h->stream);
-}
-
-void prof_end(gbmg_handle* h, int cls) {
-  h->launches += 1;
-  if (!h->prof) return;
-  cudaEvent_t& e = h->pev[2 * h->pused + 1];
-  if (!e) cudaEventCreate(&e);
-  cudaEventRecord(e, h->stream);
-  h->pcls[h->pused++] = cls;
-}
-
-// One kernel launch, counted and (when profiling) timed as class `cls`.
-#define LAUNCH(h, cls, stmt) \
-  do {                       \
-    prof_begin(h);           \
-    stmt;                    \
-    prof_end(h, cls);        \
-  } while (0)
-
-template <typename T>
-int dmalloc(gbmg_handle* h, T** ptr, size_t n) {
-  *ptr = nullptr;
-  GB_CUDA(h, cudaMalloc((void**)ptr, (n ? n : 1) * sizeof(T)));
-  return GBMG_OK;
-}
-
-template <typename T>
-void dfree(T*& ptr) {
-  if (ptr) cudaFree((void*)ptr);
-  ptr = nullptr;
-}
 
 // Level plan, the same rule as the oracle: every axis with more than one cell
 // halves per level; auto mode stops at <= coarse_max cells or when an axis is
@@ -593,52 +414,6 @@ int allocate(gbmg_handle* h) {
   return GBMG_OK;
 }
 
-bool dense_cells(const gbmg_field& f, int nx, int ny) {
-  return f.sy == nx && f.sz == (int64_t)nx * ny;
-}
-
-// Copy a field of extent (ex, ey, ez) into a dense device buffer.
-int upload(gbmg_handle* h, const gbmg_field& f, int ex, int ey, int ez, int mem, double* dst,
-           cudaStream_t s = nullptr) {
-  if (!s) s = h->stream;
-  if (!f.data) {
-    h->err = "null field";
-    return GBMG_INVALID_ARG;
-  }
-  const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  if (dense_cells(f, ex, ey)) {
-    GB_CUDA(h, cudaMemcpyAsync(dst, f.data, (size_t)ex * ey * ez * sizeof(double), kind, s));
-  } else if (mem == GBMG_MEM_DEVICE) {
-    launch_copy_in(s, ex, ey, ez, Strided{f.data, f.sy, f.sz}, dst);
-    h->launches += 1;
-    GB_TRY(check_launch(h, "copy_in"));
-  } else {
-    for (int k = 0; k < ez; ++k)
-      GB_CUDA(h, cudaMemcpy2DAsync(dst + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
-                                   f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
-                                   (size_t)ex * sizeof(double), (size_t)ey, kind, s));
-  }
-  return GBMG_OK;
-}
-
-int download(gbmg_handle* h, const double* src, int ex, int ey, int ez, int mem,
-             const gbmg_field& f, cudaStream_t s = nullptr) {
-  if (!s) s = h->stream;
-  const cudaMemcpyKind kind = mem == GBMG_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  if (dense_cells(f, ex, ey)) {
-    GB_CUDA(h, cudaMemcpyAsync(f.data, src, (size_t)ex * ey * ez * sizeof(double), kind, s));
-  } else if (mem == GBMG_MEM_DEVICE) {
-    launch_copy_out(s, ex, ey, ez, src, f.data, f.sy, f.sz);
-    h->launches += 1;
-    GB_TRY(check_launch(h, "copy_out"));
-  } else {
-    for (int k = 0; k < ez; ++k)
-      GB_CUDA(h, cudaMemcpy2DAsync(f.data + (int64_t)k * f.sz, (size_t)f.sy * sizeof(double),
-                                   src + (size_t)k * ex * ey, (size_t)ex * sizeof(double),
-                                   (size_t)ex * sizeof(double), (size_t)ey, kind, s));
-  }
-  return GBMG_OK;
-}
 
 // Coarse levels, 1/diagonal, FP32 copies and the coarse inverse from the
 // level-0 FP64 coefficients.
@@ -1238,20 +1013,6 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   return status;
 }
 
-int validate_field(gbmg_handle* h, const gbmg_field& f, const char* name) {
-  if (!f.data || f.sy < 1 || f.sz < 1) {
-    h->err = std::string("invalid field ") + name;
-    return GBMG_INVALID_ARG;
-  }
-  return GBMG_OK;
-}
-
-int begin(gbmg_handle* h) {
-  if (!h) return GBMG_INVALID_ARG;
-  h->err.clear();
-  GB_CUDA(h, cudaSetDevice(h->device));
-  return GBMG_OK;
-}
 
 // Face velocities on the device: the caller's arrays (device memory) or
 // staging copies of them (host memory).
@@ -1292,6 +1053,11 @@ int zero_walls(gbmg_handle* h, const gbmg_field dfield[3], bool has_w) {
   return check_launch(h, "zero_wall_faces");
 }
 
+}  // namespace
+
+namespace gbmg {
+namespace host {
+
 // The projection on device face velocities (fields addressed at their face
 // (0,0,0)) with the initial pressure already in h->p: b = div(u*)/dt, the
 // solve, then u -= dt beta grad p (ppe_sor_solver + ns_momentum_correction).
@@ -1321,262 +1087,9 @@ int project_device(gbmg_handle* h, const gbmg_field dfield[3], bool has_w, doubl
   return status;
 }
 
-// ---- Adams-Bashforth momentum step -------------------------------------------
-// Arrays of the step, in the order of gbmg_ns_fields.
-enum NsSlot {
-  kNsU, kNsV, kNsW, kNsUo, kNsVo, kNsWo, kNsSu, kNsSv, kNsSw, kNsSuo, kNsSvo, kNsSwo,
-  kNsRho, kNsMu, kNsDelta, kNsPhi, kNsNx, kNsNy, kNsNz, kNsCurv, kNsFields
-};
-// scratch buffers after the staging slots: vel%tmp (3), velsrc%tmp (3)
-constexpr int kNsTmp = kNsFields, kNsDiff = kNsFields + 3;
+}  // namespace host
+}  // namespace gbmg
 
-const gbmg_field& ns_field(const gbmg_ns_fields* f, int slot) {
-  const gbmg_field* all[kNsFields] = {&f->u,      &f->v,      &f->w,      &f->u_old, &f->v_old,
-                                      &f->w_old,  &f->su,     &f->sv,     &f->sw,    &f->su_old,
-                                      &f->sv_old, &f->sw_old, &f->rho,    &f->mu,    &f->delta,
-                                      &f->phi,    &f->nrm_x,  &f->nrm_y,  &f->nrm_z, &f->curv};
-  return *all[slot];
-}
-
-// Offset of element (1,1,1) of the reference's indices from a field's
-// address: faces are addressed at their face 0 (u(0,1,1), v(1,0,1), w(1,1,0)).
-int64_t ns_origin(int slot, int64_t sy, int64_t sz) {
-  const int axis = slot < kNsRho ? slot % 3 : -1;
-  return axis == 0 ? 1 : axis == 1 ? sy : axis == 2 ? sz : 0;
-}
-
-struct NsPlan {
-  NsArgs a{};
-  NsBc bc{};
-  int64_t lo = 0, hi = 0;  // element offsets of the padded box from element (1,1,1)
-  double* base[kNsFields + 6] = {};
-  bool used[kNsFields] = {};
-};
-
-int ns_buffer(gbmg_handle* h, int slot, size_t n) {
-  if (h->ns_n[slot] < n) {
-    dfree(h->ns_buf[slot]);
-    h->ns_n[slot] = 0;
-    GB_TRY(dmalloc(h, &h->ns_buf[slot], n));
-    h->ns_n[slot] = n;
-  }
-  return GBMG_OK;
-}
-
-// Validate the arrays a call uses, fill the kernel arguments and make every
-// used array device-resident (host memory: staged copies of the padded box).
-int ns_prepare(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
-               const bool (&used)[kNsFields], const bool (&copy_in)[kNsFields], NsPlan* P,
-               bool step_scratch = true) {
-  const gbmg_grid& g = h->grid;
-  const bool three = g.nz > 1;
-  if (!prm || !f) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
-  const int gh = prm->ghost;
-  if (gh < 2 || g.nx < gh + 1 || g.ny < gh + 1 || (three && g.nz < gh + 1)) {
-    h->err = "the momentum step needs ghost >= 2 and at least ghost + 1 cells per axis";
-    return GBMG_INVALID_ARG;
-  }
-  if (!(prm->dt > 0) || !(prm->re > 0) || !(prm->fr > 0) || (prm->btn_sf != 0 && !(prm->we > 0))) {
-    h->err = "dt, re, fr (and we with surface tension) must be > 0";
-    return GBMG_INVALID_ARG;
-  }
-  int64_t sy = 0, sz = 0;
-  for (int i = 0; i < kNsFields; ++i) {
-    if (!used[i]) continue;
-    const gbmg_field& fi = ns_field(f, i);
-    if (!fi.data) { h->err = "a field the momentum step reads or writes is NULL"; return GBMG_INVALID_ARG; }
-    if (!sy) { sy = fi.sy; sz = fi.sz; }
-    if (fi.sy != sy || (three && fi.sz != sz)) {
-      h->err = "the arrays of the momentum step must share their strides";
-      return GBMG_INVALID_ARG;
-    }
-  }
-  if (sy < g.nx + 2 * gh || (three && sz < sy * (g.ny + 2 * gh))) {
-    h->err = "strides too small for the ghost-padded box";
-    return GBMG_INVALID_ARG;
-  }
-  NsArgs& a = P->a;
-  a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.g = gh;
-  a.sy = sy; a.sz = three ? sz : 0;
-  a.dx = g.dx; a.dy = g.dy; a.dz = g.dz;
-  a.dt = prm->dt; a.re = prm->re; a.fr = prm->fr; a.we = prm->we; a.mu_12 = prm->mu_12;
-  a.gx = prm->gx; a.gy = prm->gy; a.gz = prm->gz; a.btn_g = prm->btn_g; a.btn_sf = prm->btn_sf;
-  // reciprocals of the constant divisors (IEEE divisions, so RN(1/b)), and
-  // the gravity source (g_d btn_g)/fr as the reference evaluates it per cell
-  const double dvs[7] = {g.dx, g.dy, g.dz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz, prm->re};
-  double* rcp[7] = {&a.rdx, &a.rdy, &a.rdz, &a.rdx2, &a.rdy2, &a.rdz2, &a.rre};
-  a.fast = 1;
-  for (int i = 0; i < 7; ++i) {
-    *rcp[i] = 1.0 / dvs[i];
-    if (!fdiv_divisor_ok(dvs[i])) a.fast = 0;
-  }
-  a.scheme = prm->adv_scheme;
-  if (a.scheme != 0 && a.scheme != 1) {
-    h->err = "adv_scheme must be 0 (second-order upwind) or 1 (QUICK)";
-    return GBMG_INVALID_ARG;
-  }
-  a.gterm[0] = prm->gx * prm->btn_g / prm->fr;
-  a.gterm[1] = prm->gy * prm->btn_g / prm->fr;
-  a.gterm[2] = prm->gz * prm->btn_g / prm->fr;
-  for (int i = 0; i < 6; ++i) P->bc.b[i] = prm->bc[i];
-  P->lo = -(int64_t)gh - gh * a.sy - (three ? gh * a.sz : 0);
-  P->hi = (int64_t)(g.nx + gh - 1) + (g.ny + gh - 1) * a.sy + (three ? (g.nz + gh - 1) * a.sz : 0);
-  const size_t span = (size_t)(P->hi - P->lo + 1);
-  for (int i = 0; i < kNsFields; ++i) {
-    P->used[i] = used[i];
-    if (!used[i]) continue;
-    double* b = ns_field(f, i).data + ns_origin(i, a.sy, a.sz);
-    if (mem == GBMG_MEM_DEVICE) {
-      P->base[i] = b;
-      continue;
-    }
-    GB_TRY(ns_buffer(h, i, span));
-    if (copy_in[i])
-      GB_CUDA(h, cudaMemcpyAsync(h->ns_buf[i], b + P->lo, span * sizeof(double),
-                                 cudaMemcpyHostToDevice, h->stream));
-    P->base[i] = h->ns_buf[i] - P->lo;
-  }
-  // vel%tmp and velsrc%tmp of the momentum step (not for the other calls)
-  for (int c = 0; c < 6 && step_scratch; ++c) {
-    if (!three && c % 3 == 2) continue;
-    GB_TRY(ns_buffer(h, kNsTmp + c, span));
-    P->base[kNsTmp + c] = h->ns_buf[kNsTmp + c] - P->lo;
-  }
-  return GBMG_OK;
-}
-
-int ns_finish(gbmg_handle* h, const gbmg_ns_fields* f, int mem, const NsPlan& P,
-              const bool (&copy_out)[kNsFields]) {
-  if (mem != GBMG_MEM_HOST) return GBMG_OK;
-  const size_t span = (size_t)(P.hi - P.lo + 1);
-  for (int i = 0; i < kNsFields; ++i) {
-    if (!P.used[i] || !copy_out[i]) continue;
-    double* b = ns_field(f, i).data + ns_origin(i, P.a.sy, P.a.sz);
-    GB_CUDA(h, cudaMemcpyAsync(b + P.lo, P.base[i] + P.lo, span * sizeof(double),
-                               cudaMemcpyDeviceToHost, h->stream));
-  }
-  return GBMG_OK;
-}
-
-// ns_linearize (vel%tmp = vel%now over the padded box), ns_ab_setup and
-// ns_ab_predictor, then velbc on vel%now.
-int ns_pass(gbmg_handle* h, const NsPlan& P) {
-  const cudaStream_t s = h->stream;
-  const bool three = P.a.nz > 1;
-  const size_t span = (size_t)(P.hi - P.lo + 1);
-  for (int c = 0; c < (three ? 3 : 2); ++c)
-    GB_CUDA(h, cudaMemcpyAsync(P.base[kNsTmp + c] + P.lo, P.base[kNsU + c] + P.lo,
-                               span * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  const double* old[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
-  const double* tmp[3] = {P.base[kNsTmp], P.base[kNsTmp + 1], P.base[kNsTmp + 2]};
-  const double* diff[3] = {P.base[kNsDiff], P.base[kNsDiff + 1], P.base[kNsDiff + 2]};
-  const double* so[3] = {P.base[kNsSuo], P.base[kNsSvo], P.base[kNsSwo]};
-  double* src[3] = {P.base[kNsSu], P.base[kNsSv], P.base[kNsSw]};
-  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_advance(s, P.a, old, tmp, diff, so, src, now));
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(s, P.a, P.bc, now));
-  return check_launch(h, "momentum predictor");
-}
-
-int ns_diffusion(gbmg_handle* h, const NsPlan& P) {
-  const double* vel[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
-  const double* nrm[3] = {P.base[kNsNx], P.base[kNsNy], P.base[kNsNz]};
-  double* out[3] = {P.base[kNsDiff], P.base[kNsDiff + 1], P.base[kNsDiff + 2]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM,
-         launch_ns_diffusion(h->stream, P.a, vel, P.base[kNsRho], P.base[kNsMu],
-                             P.base[kNsDelta], P.base[kNsPhi], nrm, P.base[kNsCurv], out));
-  return check_launch(h, "momentum sources");
-}
-
-void ns_used(const gbmg_grid& g, const gbmg_ns_params* prm, bool (&used)[kNsFields],
-             bool (&in)[kNsFields], bool (&out)[kNsFields]) {
-  const bool three = g.nz > 1, sf = prm && prm->btn_sf != 0.0;
-  for (int i = 0; i < kNsFields; ++i) {
-    const bool is_w = i < kNsRho && i % 3 == 2;
-    used[i] = !(is_w && !three) && !(i == kNsNz && !three) &&
-              !(i >= kNsNx && i <= kNsCurv && !sf);
-    in[i] = used[i];  // velsrc%now round-trips its ghosts
-    out[i] = used[i] && (i <= kNsW || (i >= kNsSu && i <= kNsSw));
-  }
-}
-
-// Compact-difference normals and curvature (curv + surface_norms): scratch
-// slots after the momentum step's: the six second derivatives and a dummy
-// second derivative, then a factor table per axis and the factoring work.
-constexpr int kCcdD2 = kNsDiff + 3, kCcdDummy = kCcdD2 + 6, kCcdTable = kCcdDummy + 1,
-              kCcdWork = kCcdTable + 3, kCcdSpare = kCcdWork + 1;  // two spare fields
-
-// One CCD line pass: its arguments, and the axis's factor table (made by
-// one sequential thread, so once, and kept while the line length and spacing
-// stay the same).
-int ccd_pass(gbmg_handle* h, const NsPlan& P, int axis, CcdArgs* out) {
-  const NsArgs& a = P.a;
-  const bool three = a.nz > 1;
-  const int px = a.nx + 2 * a.g, py = a.ny + 2 * a.g, pz = three ? a.nz + 2 * a.g : 1;
-  const int ext[3] = {px, py, pz};
-  const int64_t str[3] = {1, a.sy, three ? a.sz : 0};
-  const double hs[3] = {a.dx, a.dy, a.dz};
-  CcdArgs c{};
-  c.L = ext[axis];
-  c.st = str[axis];
-  const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
-  c.n1 = ext[a1]; c.s1 = str[a1];
-  c.n2 = ext[a2]; c.s2 = str[a2];
-  c.h = hs[axis];
-  c.h2 = c.h * c.h;
-  c.rh = 1.0 / c.h;
-  c.rh2 = 1.0 / c.h2;
-  c.fast = fdiv_divisor_ok(c.h) && fdiv_divisor_ok(c.h2);
-  if (h->ccd_L[axis] != c.L || h->ccd_h[axis] != c.h) {
-    h->ccd_L[axis] = 0;
-    GB_TRY(ns_buffer(h, kCcdTable + axis, (size_t)14 * c.L));
-    GB_TRY(ns_buffer(h, kCcdWork, (size_t)12 * c.L));
-    LAUNCH(h, GBMG_PROF_MOMENTUM,
-           launch_ccd_decompose(h->stream, c.L, c.h, h->ns_buf[kCcdWork],
-                                h->ns_buf[kCcdTable + axis]));
-    GB_TRY(check_launch(h, "ccd factors"));
-    h->ccd_L[axis] = c.L;
-    h->ccd_h[axis] = c.h;
-  }
-  *out = c;
-  return GBMG_OK;
-}
-
-// Independent line passes (axis, f -> f', f'') in one launch; arrays at
-// element (1,1,1), the second-derivative outputs distinct.
-int ccd_passes(gbmg_handle* h, const NsPlan& P, int n, const int* axes,
-               const double* const* f, double* const* S, double* const* SS) {
-  CcdBatch b{};
-  b.n = n;
-  for (int i = 0; i < n; ++i) {
-    GB_TRY(ccd_pass(h, P, axes[i], &b.c[i]));
-    b.table[i] = h->ns_buf[kCcdTable + axes[i]];
-    b.f[i] = f[i] + P.lo;
-    b.S[i] = S[i] + P.lo;
-    b.SS[i] = SS[i] + P.lo;
-  }
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_lines(h->stream, b));
-  return check_launch(h, "ccd lines");
-}
-
-// Padded cell arrays of the momentum step's layout: the plan of ns_prepare
-// for the given slots (prm supplies the ghost count and mu_12).
-int ns_cells(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_ns_fields* f, int mem,
-             const int* slots, const bool* outs, int n, NsPlan* P, bool (&out)[kNsFields]) {
-  if (!prm) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
-  bool used[kNsFields] = {}, in[kNsFields] = {};
-  for (int i = 0; i < kNsFields; ++i) out[i] = false;
-  for (int i = 0; i < n; ++i) {
-    used[slots[i]] = in[slots[i]] = true;
-    out[slots[i]] = outs[i];
-  }
-  gbmg_ns_params q = *prm;
-  q.dt = q.re = q.fr = 1.0;
-  q.btn_sf = 0.0;
-  return ns_prepare(h, &q, f, mem, used, in, P, false);
-}
-
-}  // namespace
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -2084,332 +1597,6 @@ int gbmg_set_profiling(gbmg_handle* h, int on) {
   return GBMG_OK;
 }
 
-int gbmg_ns_ab_step(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f, int mem,
-                    gbmg_ns_stats* stats) {
-  GB_TRY(begin(h));
-  gbmg_ns_stats local{};
-  gbmg_ns_stats* st = stats ? stats : &local;
-  std::memset(st, 0, sizeof(*st));
-  if (!prm || !f) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
-  if (!h->coef_ready || !h->rho_ready) {
-    h->err = "the momentum step needs the new density: call gbmg_set_rho or gbmg_set_phi first";
-    return GBMG_STATE_ERROR;
-  }
-  const gbmg_grid& g = h->grid;
-  const bool three = g.nz > 1;
-  bool used[kNsFields], in[kNsFields], out[kNsFields];
-  ns_used(g, prm, used, in, out);
-  if (prm->iterations < 1 || !(prm->p_tol > 0)) {
-    h->err = "iterations must be >= 1 and p_tol > 0";
-    return GBMG_INVALID_ARG;
-  }
-  GB_TRY(validate_field(h, f->p, "p"));
-  const cudaStream_t s = h->stream;
-  GB_CUDA(h, cudaEventRecord(h->ev0, s));
-  NsPlan P;
-  GB_TRY(ns_prepare(h, prm, f, mem, used, in, &P));
-  GB_TRY(upload(h, f->p, g.nx, g.ny, g.nz, mem, h->p));
-  GB_TRY(ns_diffusion(h, P));
-  gbmg_field dfield[3] = {{P.base[kNsU] - 1, P.a.sy, P.a.sz},
-                          {P.base[kNsV] - P.a.sy, P.a.sy, P.a.sz},
-                          {three ? P.base[kNsW] - P.a.sz : nullptr, P.a.sy, P.a.sz}};
-  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
-  int worst = GBMG_OK;
-  for (int it = 0; it < prm->iterations; ++it) {
-    GB_TRY(ns_pass(h, P));
-    gbmg_stats ps{};
-    const int rc = project_device(h, dfield, three, prm->dt, prm->p_tol, &ps);
-    if (rc != GBMG_OK && rc != GBMG_NOT_CONVERGED && rc != GBMG_DIVERGED) return rc;
-    if (rc > worst) worst = rc;
-    st->cycles += ps.cycles;
-    st->max_rel_residual = std::max(st->max_rel_residual, ps.rel_residual);
-    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(s, P.a, P.bc, now));
-    GB_TRY(check_launch(h, "velbc"));
-  }
-  const double* tmp[3] = {P.base[kNsTmp], P.base[kNsTmp + 1], P.base[kNsTmp + 2]};
-  const double* nowc[3] = {now[0], now[1], now[2]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_change(s, P.a, nowc, tmp, h->red));
-  GB_TRY(check_launch(h, "velocity change"));
-  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
-                             cudaMemcpyDeviceToHost, s));
-  GB_TRY(ns_finish(h, f, mem, P, out));
-  GB_TRY(download(h, h->p, g.nx, g.ny, g.nz, mem, f->p));
-  GB_CUDA(h, cudaEventRecord(h->ev1, s));
-  GB_CUDA(h, cudaEventSynchronize(h->ev1));
-  double mx = 0.0;
-  std::memcpy(&mx, &h->host_res[kSlotMax], sizeof(double));
-  const double cnt = (three ? 3.0 : 2.0) * g.nx * g.ny * g.nz;
-  st->linf = mx;
-  st->l2f = std::sqrt(h->host_res[kSlotSum] / cnt);
-  st->status = worst;
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-  st->ms = ms;
-  return worst;
-}
-
-int gbmg_ns_ab_predict(gbmg_handle* h, const gbmg_ns_params* prm, const gbmg_ns_fields* f,
-                       int mem) {
-  GB_TRY(begin(h));
-  bool used[kNsFields], in[kNsFields], out[kNsFields];
-  ns_used(h->grid, prm, used, in, out);
-  NsPlan P;
-  GB_TRY(ns_prepare(h, prm, f, mem, used, in, &P));
-  GB_TRY(ns_diffusion(h, P));
-  GB_TRY(ns_pass(h, P));
-  GB_TRY(ns_finish(h, f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_velbc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field u, gbmg_field v,
-                  gbmg_field w, int mem) {
-  GB_TRY(begin(h));
-  gbmg_ns_fields f{};
-  f.u = u; f.v = v; f.w = w;
-  bool used[kNsFields] = {}, in[kNsFields] = {}, out[kNsFields] = {};
-  const bool three = h->grid.nz > 1;
-  for (int c = 0; c < (three ? 3 : 2); ++c) used[c] = in[c] = out[c] = true;
-  NsPlan P;
-  gbmg_ns_params q = prm ? *prm : gbmg_ns_params{};
-  if (prm) { q.dt = q.re = q.fr = 1.0; q.btn_sf = 0.0; }  // velbc reads only ghost and bc
-  GB_TRY(ns_prepare(h, prm ? &q : nullptr, &f, mem, used, in, &P, false));
-  double* now[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_velbc(h->stream, P.a, P.bc, now));
-  GB_TRY(check_launch(h, "velbc"));
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_curvature(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
-                      gbmg_field nrm_x, gbmg_field nrm_y, gbmg_field nrm_z, gbmg_field curv,
-                      int mem) {
-  GB_TRY(begin(h));
-  if (!prm) { h->err = "null parameters"; return GBMG_INVALID_ARG; }
-  const bool three = h->grid.nz > 1;
-  gbmg_ns_fields f{};
-  f.phi = phi; f.nrm_x = nrm_x; f.nrm_y = nrm_y; f.nrm_z = nrm_z; f.curv = curv;
-  bool used[kNsFields] = {}, in[kNsFields] = {}, out[kNsFields] = {};
-  const int slots[5] = {kNsPhi, kNsNx, kNsNy, kNsNz, kNsCurv};
-  for (int i = 0; i < 5; ++i) {
-    if (slots[i] == kNsNz && !three) continue;
-    used[slots[i]] = in[slots[i]] = true;
-    out[slots[i]] = slots[i] != kNsPhi;
-  }
-  gbmg_ns_params q = *prm;
-  q.dt = q.re = q.fr = 1.0;  // only ghost is read
-  q.btn_sf = 0.0;
-  NsPlan P;
-  GB_TRY(ns_prepare(h, &q, &f, mem, used, in, &P, false));
-  const size_t span = (size_t)(P.hi - P.lo + 1);
-  double* d2[9];
-  for (int i = 0; i < 9; ++i) {
-    const int slot = i < 7 ? kCcdD2 + i : kCcdSpare + (i - 7);
-    GB_TRY(ns_buffer(h, slot, span));
-    d2[i] = h->ns_buf[slot] - P.lo;
-  }
-  double* nx = P.base[kNsNx];
-  double* ny = P.base[kNsNy];
-  double* nz = three ? P.base[kNsNz] : nullptr;
-  const double* ph = P.base[kNsPhi];
-  // surface_norms: first and second derivatives of phi along each axis (one
-  // launch), then the cross derivatives from phi_x and phi_y before any bc
-  // (one launch; their second derivatives are discarded, each its own buffer)
-  {
-    const int axes[3] = {0, 1, 2};
-    const double* src[3] = {ph, ph, ph};
-    double* S[3] = {nx, ny, nz};
-    double* SS[3] = {d2[0], d2[1], d2[2]};
-    GB_TRY(ccd_passes(h, P, three ? 3 : 2, axes, src, S, SS));
-  }
-  {
-    const int axes[3] = {1, 2, 2};
-    const double* src[3] = {nx, nx, ny};
-    double* S[3] = {d2[3], d2[4], d2[5]};
-    double* SS[3] = {d2[6], d2[7], d2[8]};
-    GB_TRY(ccd_passes(h, P, three ? 3 : 1, axes, src, S, SS));
-  }
-  const double* d1c[3] = {nx, ny, nz};
-  const double* d2c[6] = {d2[0], d2[1], d2[2], d2[3], d2[4], d2[5]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_curvature(h->stream, P.a, d1c, d2c, P.base[kNsCurv]));
-  double* bcs[4] = {nx, ny, nz, P.base[kNsCurv]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, bcs));
-  GB_TRY(check_launch(h, "curvature"));
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_rho_mu(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi, double ls_wid,
-                   double rho_12, gbmg_field rho, gbmg_field mu, gbmg_field delta, int mem) {
-  GB_TRY(begin(h));
-  if (!(ls_wid > 0) || !(rho_12 > 0)) { h->err = "ls_wid and rho_12 must be > 0"; return GBMG_INVALID_ARG; }
-  gbmg_ns_fields f{};
-  f.phi = phi; f.rho = rho; f.mu = mu; f.delta = delta;
-  int slots[4] = {kNsPhi};
-  bool outs[4] = {false};
-  int n = 1;
-  const gbmg_field* o[3] = {&rho, &mu, &delta};
-  const int os[3] = {kNsRho, kNsMu, kNsDelta};
-  for (int i = 0; i < 3; ++i)
-    if (o[i]->data) { slots[n] = os[i]; outs[n++] = true; }
-  NsPlan P;
-  bool out[kNsFields];
-  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, n, &P, out));
-  LAUNCH(h, GBMG_PROF_MOMENTUM,
-         launch_ns_rho_mu(h->stream, P.a, P.base[kNsPhi], ls_wid, rho_12, P.base[kNsRho],
-                          P.base[kNsMu], P.base[kNsDelta]));
-  GB_TRY(check_launch(h, "rho_mu"));
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_bc(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field a, int mem) {
-  GB_TRY(begin(h));
-  gbmg_ns_fields f{};
-  f.phi = a;
-  const int slots[1] = {kNsPhi};
-  const bool outs[1] = {true};
-  NsPlan P;
-  bool out[kNsFields];
-  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, 1, &P, out));
-  double* arr[4] = {P.base[kNsPhi], nullptr, nullptr, nullptr};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));
-  GB_TRY(check_launch(h, "bc"));
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_mass_correct(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field phi,
-                         double ls_wid, double rho_12, double imass, int iterations, int mem,
-                         double* mass) {
-  GB_TRY(begin(h));
-  if (!(ls_wid > 0) || !(rho_12 > 0) || iterations < 0) {
-    h->err = "ls_wid and rho_12 must be > 0 and iterations >= 0";
-    return GBMG_INVALID_ARG;
-  }
-  const bool three = h->grid.nz > 1;
-  gbmg_ns_fields f{};
-  f.phi = phi;
-  const int slots[1] = {kNsPhi};
-  const bool outs[1] = {iterations > 0};
-  NsPlan P;
-  bool out[kNsFields];
-  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, 1, &P, out));
-  const size_t span = (size_t)(P.hi - P.lo + 1);
-  double* gr[3] = {nullptr, nullptr, nullptr};
-  for (int c = 0; c < (three ? 3 : 2); ++c) {
-    GB_TRY(ns_buffer(h, kCcdD2 + c, span));
-    gr[c] = h->ns_buf[kCcdD2 + c] - P.lo;
-  }
-  GB_TRY(ns_buffer(h, kCcdD2 + 6, span));
-  GB_TRY(ns_buffer(h, kCcdSpare, span));
-  GB_TRY(ns_buffer(h, kCcdSpare + 1, span));
-  double* dummy = h->ns_buf[kCcdD2 + 6] - P.lo;
-  double* dummy2 = h->ns_buf[kCcdSpare] - P.lo;
-  double* dummy3 = h->ns_buf[kCcdSpare + 1] - P.lo;
-  double* ph = P.base[kNsPhi];
-  const gbmg_grid& g = h->grid;
-  const double dv = three ? g.dx * g.dy * g.dz : g.dx * g.dy;
-  const cudaStream_t s = h->stream;
-  double m = 0.0;
-  const int passes = iterations > 0 ? iterations : 1;
-  for (int it = 0; it < passes; ++it) {
-    // ls_mv, and before a correction surface_norms' gradient of phi
-    const bool correct = iterations > 0;
-    if (correct) {
-      const int axes[3] = {0, 1, 2};
-      const double* src[3] = {ph, ph, ph};
-      double* SS[3] = {dummy, dummy2, dummy3};
-      GB_TRY(ccd_passes(h, P, three ? 3 : 2, axes, src, gr, SS));
-    }
-    const double* gc[3] = {correct ? gr[0] : nullptr, gr[1], gr[2]};
-    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_sums(s, P.a, ph, gc, ls_wid, rho_12, dv, h->red));
-    GB_TRY(check_launch(h, "mass sums"));
-    GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
-                               cudaMemcpyDeviceToHost, s));
-    GB_CUDA(h, cudaStreamSynchronize(s));
-    m = h->host_res[kSlotSum];
-    if (!correct) break;
-    const double den = h->host_res[kSlotSum + 1];
-    if (!(den > 0.0) || !std::isfinite(den)) {
-      // no cell inside the interface band (or a non-finite field): the
-      // reference's lambda would be a division by zero
-      h->err = "mass correction: no interface cells (sum of delta^2 |grad phi| is not > 0)";
-      return GBMG_INVALID_ARG;
-    }
-    const double lam = (imass - m) / den;
-    const double* gcc[3] = {gr[0], gr[1], gr[2]};
-    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_mpls_update(s, P.a, ph, gcc, ls_wid, lam));
-    double* arr[4] = {ph, nullptr, nullptr, nullptr};
-    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(s, P.a, arr));
-    GB_TRY(check_launch(h, "mass correction"));
-  }
-  // the mass measured last: before the last correction, as the reference
-  // leaves p%glb%mass (or of phi itself when iterations = 0)
-  if (mass) *mass = m;
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(s));
-  return GBMG_OK;
-}
-
-int gbmg_ns_vof_advect(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field vof,
-                       gbmg_field vof_old, gbmg_field u_old, gbmg_field v_old, gbmg_field w_old,
-                       gbmg_field phi, int mem) {
-  GB_TRY(begin(h));
-  if (!prm || !(prm->dt > 0)) { h->err = "dt must be > 0"; return GBMG_INVALID_ARG; }
-  const bool three = h->grid.nz > 1;
-  // the cell arrays ride in the plan's cell slots (vof, vof_old, phi), the
-  // face velocities in the old-velocity slots
-  gbmg_ns_fields f{};
-  f.rho = vof; f.mu = vof_old; f.phi = phi;
-  f.u_old = u_old; f.v_old = v_old; f.w_old = w_old;
-  int slots[6] = {kNsRho, kNsMu, kNsPhi, kNsUo, kNsVo, kNsWo};
-  const bool outs[6] = {true, false, false, false, false, false};
-  NsPlan P;
-  bool out[kNsFields];
-  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, three ? 6 : 5, &P, out));
-  P.a.dt = prm->dt;
-  const size_t span = (size_t)(P.hi - P.lo + 1);
-  GB_TRY(ns_buffer(h, kCcdD2, span));
-  double* flux = h->ns_buf[kCcdD2] - P.lo;
-  double* vf = P.base[kNsRho];
-  const double* vel[3] = {P.base[kNsUo], P.base[kNsVo], P.base[kNsWo]};
-  for (int ax = 0; ax < (three ? 3 : 2); ++ax) {
-    LAUNCH(h, GBMG_PROF_MOMENTUM,
-           launch_wlic(h->stream, P.a, ax, vf, P.base[kNsMu], vel[ax], P.base[kNsPhi], flux));
-    double* arr[4] = {vf, nullptr, nullptr, nullptr};
-    LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));
-    GB_TRY(check_launch(h, "vof sweep"));
-  }
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
-
-int gbmg_ns_ibm(gbmg_handle* h, const gbmg_ns_params* prm, gbmg_field solid, double w_body,
-                gbmg_field u, gbmg_field v, gbmg_field w, int mem) {
-  GB_TRY(begin(h));
-  const bool three = h->grid.nz > 1;
-  gbmg_ns_fields f{};
-  f.rho = solid; f.u = u; f.v = v; f.w = w;
-  const int slots[4] = {kNsRho, kNsU, kNsV, kNsW};
-  const bool outs[4] = {true, true, true, true};
-  NsPlan P;
-  bool out[kNsFields];
-  GB_TRY(ns_cells(h, prm, &f, mem, slots, outs, three ? 4 : 3, &P, out));
-  double* arr[4] = {P.base[kNsRho], nullptr, nullptr, nullptr};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ccd_bc(h->stream, P.a, arr));  // bc(solid)
-  double* vel[3] = {P.base[kNsU], P.base[kNsV], P.base[kNsW]};
-  LAUNCH(h, GBMG_PROF_MOMENTUM, launch_ns_ibm(h->stream, P.a, P.base[kNsRho], w_body, vel));
-  GB_TRY(check_launch(h, "ibm"));
-  GB_TRY(ns_finish(h, &f, mem, P, out));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
-  return GBMG_OK;
-}
 
 int gbmg_profile(gbmg_handle* h, double* ms, int64_t* launches, int32_t n) {
   GB_TRY(begin(h));
