@@ -226,8 +226,7 @@ void enqueue_defect(gbmg_handle* h, int pc, const float* e, float* r32, int slot
   const bool split = f.split != 0;
   const size_t hs = split ? f.hstride : 0;
   if (h->dmaps && (!split || h->dmaps_split)) {
-    const int ei = e == nullptr ? 0 : (e == f.buf_a ? 1 : 2);
-    const int mi = split && e ? 6 + pc : pc * 3 + ei;
+    const int mi = split && e ? 4 + pc : pc * 2 + (e ? 1 : 0);
     launch_defect_tma(h->stream, h->dmaps[mi], f.nx, f.ny, f.nz, e != nullptr, h->pw[1 - pc], r32,
                       h->red, slot, h->derr, hs);
   } else {
@@ -241,7 +240,7 @@ int free_all(gbmg_handle* h) {
     Level& v = h->lv[l];
     dfree(v.cx); dfree(v.cy); dfree(v.cz); dfree(v.idiag);
     if (l > 0) { dfree(v.sol); dfree(v.src); }
-    dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.alt32); dfree(v.src32);
+    dfree(v.cx32); dfree(v.cy32); dfree(v.cz32); dfree(v.sol32); dfree(v.src32);
   }
   dfree(h->b); dfree(h->p); dfree(h->rho); dfree(h->rho32);
   dfree(h->pw[0]); dfree(h->pw[1]); dfree(h->bw); dfree(h->cxw); dfree(h->cyw); dfree(h->czw);
@@ -293,18 +292,17 @@ void setup_subcycle(gbmg_handle* h) {
 // GBMG_TMA_DEFECT=0 keeps the plain-load defect kernel).
 int setup_tma(gbmg_handle* h) {
   Level& f = h->lv[0];
-  f.buf_a = f.sol32;
   const char* ed = std::getenv("GBMG_TMA_DEFECT");
   if (f.nx % 4 == 0 && !(ed && std::atoi(ed) == 0) && defect_tma_init() == 0) {
-    DefectMaps* m = new DefectMaps[8];
+    // [p buffer][e: none, the level's unknown]; then, per p buffer, the
+    // colour-split e (entries 4, 5, made by set_rho_form)
+    DefectMaps* m = new DefectMaps[6];
     bool ok = true;
     for (int pc = 0; pc < 2; ++pc)
-      for (int ei = 0; ei < 3; ++ei) {
-        const float* e = ei == 0 ? nullptr : (ei == 1 ? f.sol32 : f.alt32);
-        ok = ok && make_defect_maps(&m[pc * 3 + ei], h->pw[pc], e, h->bw, h->cxw, h->cyw, h->czw,
-                                    f.nx, f.ny, f.nz, 0);
-      }
-    if (ok) h->dmaps = m;  // the colour-split entries 6, 7 are made by set_rho_form
+      for (int ei = 0; ei < 2; ++ei)
+        ok = ok && make_defect_maps(&m[pc * 2 + ei], h->pw[pc], ei ? f.sol32 : nullptr, h->bw,
+                                    h->cxw, h->cyw, h->czw, f.nx, f.ny, f.nz, 0);
+    if (ok) h->dmaps = m;
     else delete[] m;
   }
   return GBMG_OK;
@@ -351,7 +349,6 @@ int allocate(gbmg_handle* h) {
       GB_TRY(dmalloc(h, &v.cy32, v.n));
       GB_TRY(dmalloc(h, &v.cz32, v.n));
       GB_TRY(dmalloc(h, &v.sol32, nv));
-      GB_TRY(dmalloc(h, &v.alt32, nv));
       GB_TRY(dmalloc(h, &v.src32, nv));
     }
   }
@@ -446,8 +443,8 @@ int build_hierarchy(gbmg_handle* h) {
 }
 
 // Whether the FP32 finest-level kernels compute their coefficients from the
-// density (an operator from rho/phi; GBMG_RHO_COEF=0 turns it off; the TMA
-// and fused sweeps read stored coefficients), and whether that level
+// density (an operator from rho/phi; GBMG_RHO_COEF=0 turns it off), and
+// whether that level
 // is stored colour-split (density form, nx even, x halved by the first
 // coarsening, the level outside the single-block bottom; GBMG_SPLIT=0 turns
 // it off).  Captured graphs hold the level views, so a change drops them.
@@ -472,7 +469,7 @@ void set_rho_form(gbmg_handle* h, bool on) {
     // colour-split e maps (rows of nx/2 floats must be 16-byte multiples)
     bool oks = f.nx % 8 == 0;
     for (int pc = 0; pc < 2 && oks; ++pc)
-      oks = make_defect_maps(&h->dmaps[6 + pc], h->pw[pc], f.sol32, h->bw, h->cxw, h->cyw, h->czw,
+      oks = make_defect_maps(&h->dmaps[4 + pc], h->pw[pc], f.sol32, h->bw, h->cxw, h->cyw, h->czw,
                              f.nx, f.ny, f.nz, hs);
     h->dmaps_split = oks;
   }

@@ -22,8 +22,6 @@ struct Level {
   double *sol = nullptr, *src = nullptr;  // owned on levels >= 1
   float *cx32 = nullptr, *cy32 = nullptr, *cz32 = nullptr;
   float *sol32 = nullptr, *src32 = nullptr;
-  float* alt32 = nullptr;  // second FP32 solution buffer: fused sweeps run out of place
-  float* buf_a = nullptr;  // the buffer sol32 pointed to at allocation
   // FP32 kernels take the coefficients from this density instead of cx32..cz32
   // (finest level of a mixed solve whose operator came from rho or phi)
   const float* rho32 = nullptr;
@@ -78,8 +76,8 @@ struct gbmg_handle {
   int pcur = 0;  // which pw holds the current pressure
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   int* derr = nullptr;   // device error flags (bulk-copy wait timeouts)
-  gbmg::DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none, A, B],
-                                // then [p buffer] with a colour-split e (buffer A)
+  gbmg::DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none,
+                                      // the unknown], then [p buffer] with a colour-split e
   bool dmaps_split = false;     // whether the colour-split entries were made
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
