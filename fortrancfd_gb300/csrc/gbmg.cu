@@ -180,8 +180,13 @@ int enqueue_vcycle(gbmg_handle* h, bool reverse_post, bool zero_fine) {
            launch_coarse_solve<T>(s, h->nc, minv_of<T>(h), adense_of<T>(h), C.src, C.sol));
   }
   for (int l = top - 1; l >= 0; --l) {
+    // A colour launch does not read its own colour's values (Gauss-Seidel
+    // overwrites them), so the colour that the first post-smoothing launch
+    // updates needs no correction: the split finest level corrects only the
+    // other one.  Results are unchanged bit for bit.
+    const int live = (l == 0 && h->prm.nu2 > 0) ? (reverse_post ? 0 : 1) : -1;
     LAUNCH(h, l == 0 ? GBMG_PROF_PROLONG_FINE : GBMG_PROF_PROLONG_COARSE,
-           launch_prolong<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1])));
+           launch_prolong<T>(s, view_next<T>(h->lv[l]), view<T>(h->lv[l + 1]), live));
     for (int it = 0; it < h->prm.nu2; ++it) sweep<T>(h, l, reverse_post ? 1 : 0, false);
   }
   return check_launch(h, "v-cycle");

@@ -107,8 +107,10 @@ void launch_smooth(cudaStream_t s, const LevelView<T>& L, int color, bool zero_g
 // sweep starts from a zero guess)
 template <typename T>
 void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, bool zero_sol);
+// live >= 0 (split finest level only): correct only the cells of colour live,
+// when the next sweep's first colour launch overwrites the other colour unread
 template <typename T>
-void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C);
+void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, int live = -1);
 // r = src - A sol on a level; writes r (type TO, may be null) and sum r^2 into slot.
 template <typename TO>
 void launch_residual_norm(cudaStream_t s, const LevelView<double>& L, TO* r,
@@ -182,7 +184,8 @@ __device__ __forceinline__ float rho_relax32(float s, float b, float d) {
 void launch_smooth_split(cudaStream_t s, const LevelView<float>& L, int color, bool zero_guess);
 void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
                            bool zero_sol);
-void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C);
+void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
+                          int live);
 void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz,
                      size_t hstride);
 void launch_from_split(cudaStream_t s, const float* a, double* out, int nx, int ny, int nz,

@@ -401,12 +401,12 @@ void launch_restrict(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& 
 }
 
 template <typename T>
-void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C) {
+void launch_prolong(cudaStream_t s, const LevelView<T>& F, const LevelView<T>& C, int live) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
   if constexpr (std::is_same<T, float>::value) {
     if (F.split) {
-      launch_prolong_split(s, F, C);
+      launch_prolong_split(s, F, C, live);
       return;
     }
   }
@@ -480,9 +480,9 @@ template void launch_restrict<double>(cudaStream_t, const LevelView<double>&,
 template void launch_restrict<float>(cudaStream_t, const LevelView<float>&,
                                      const LevelView<float>&, bool);
 template void launch_prolong<double>(cudaStream_t, const LevelView<double>&,
-                                     const LevelView<double>&);
+                                     const LevelView<double>&, int);
 template void launch_prolong<float>(cudaStream_t, const LevelView<float>&,
-                                    const LevelView<float>&);
+                                    const LevelView<float>&, int);
 template void launch_residual_norm<double>(cudaStream_t, const LevelView<double>&, double*,
                                            const ReduceScratch&, int);
 template void launch_residual_norm<float>(cudaStream_t, const LevelView<double>&, float*,

@@ -329,7 +329,10 @@ __global__ void __launch_bounds__(256) k_restrict_splitv(LevelView<float> F, Lev
 }
 
 // k_prolong_split for four coarse cells per thread (C.nx % 4 == 0).
-__global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, LevelView<float> C) {
+// live >= 0: only the cells of that colour are corrected (the other colour is
+// overwritten, unread, by the next sweep's first colour launch).
+__global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, LevelView<float> C,
+                                                        int live) {
   pdl_enter();
   const int I0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -370,9 +373,10 @@ __global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, Leve
       const size_t h = ((size_t)k * F.ny + j) * hx + I0;
       float* A = F.sol + (size_t)ca * half + h;
       float* B = F.sol + (size_t)(1 - ca) * half + h;
+      const bool da = live < 0 || live == ca, db = live < 0 || live != ca;
       float a[4], b[4];
-      unpack(ld4(A), a);
-      unpack(ld4(B), b);
+      if (da) unpack(ld4(A), a);
+      if (db) unpack(ld4(B), b);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const float ty = dy ? 0.25f * my[c] : -(0.25f * my[c]);
@@ -383,13 +387,15 @@ __global__ void __launch_bounds__(256) k_prolong_split4(LevelView<float> F, Leve
         a[c] += v0;
         b[c] += v1;
       }
-      st4(A, make_float4(a[0], a[1], a[2], a[3]));
-      st4(B, make_float4(b[0], b[1], b[2], b[3]));
+      if (da) st4(A, make_float4(a[0], a[1], a[2], a[3]));
+      if (db) st4(B, make_float4(b[0], b[1], b[2], b[3]));
     }
 }
 
-// Prolongation + correction into the split finest level (fx = 2), as k_prolong.
-__global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, LevelView<float> C) {
+// Prolongation + correction into the split finest level (fx = 2), as k_prolong
+// (live: as in k_prolong_split4).
+__global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, LevelView<float> C,
+                                                       int live) {
   pdl_enter();
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
@@ -415,8 +421,8 @@ __global__ void __launch_bounds__(256) k_prolong_split(LevelView<float> F, Level
       float v0 = ec + -(0.25f * mx), v1 = ec + 0.25f * mx;
       if (F.fy == 2) { v0 += ty; v1 += ty; }
       if (F.fz == 2) { v0 += tz; v1 += tz; }
-      F.sol[(size_t)ca * half + h] += v0;
-      F.sol[(size_t)(1 - ca) * half + h] += v1;
+      if (live < 0 || live == ca) F.sol[(size_t)ca * half + h] += v0;
+      if (live < 0 || live != ca) F.sol[(size_t)(1 - ca) * half + h] += v1;
     }
 }
 
@@ -474,15 +480,16 @@ void launch_restrict_split(cudaStream_t s, const LevelView<float>& F, const Leve
   launch_pdl(k_restrict_split, grd, blk, 0, s, F, C, zero_sol ? 1 : 0);
 }
 
-void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C) {
+void launch_prolong_split(cudaStream_t s, const LevelView<float>& F, const LevelView<float>& C,
+                          int live) {
   const dim3 blk(32, 8, 1);
   if (vec4_ok(F) && C.nx % 4 == 0) {
     const dim3 g4(cdiv((size_t)(C.nx / 4), 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-    launch_pdl(k_prolong_split4, g4, blk, 0, s, F, C);
+    launch_pdl(k_prolong_split4, g4, blk, 0, s, F, C, live);
     return;
   }
   const dim3 grd(cdiv((size_t)C.nx, 32), cdiv((size_t)C.ny, 8), (unsigned)C.nz);
-  launch_pdl(k_prolong_split, grd, blk, 0, s, F, C);
+  launch_pdl(k_prolong_split, grd, blk, 0, s, F, C, live);
 }
 
 void launch_to_split(cudaStream_t s, const double* a, float* out, int nx, int ny, int nz,
