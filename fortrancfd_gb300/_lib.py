@@ -62,7 +62,7 @@ class Stats(C.Structure):
     _fields_ = [("status", C.c_int32), ("cycles", C.c_int32), ("levels", C.c_int32),
                 ("coarse_n", C.c_int32), ("rel_residual", C.c_double),
                 ("rms_residual", C.c_double), ("res0", C.c_double), ("ms", C.c_double),
-                ("bytes", C.c_double), ("increment", C.c_double)]
+                ("bytes", C.c_double), ("increment", C.c_double), ("device_loop", C.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -214,6 +214,12 @@ int reset_graphs(gbmg_handle* h) {
       h->graph[k][par] = nullptr;
       h->graph_kernels[k][par] = 0;
     }
+  for (int k = 0; k < 4; ++k)
+    for (int par = 0; par < 2; ++par) {
+      if (h->loop_graph[k][par]) cudaGraphExecDestroy(h->loop_graph[k][par]);
+      h->loop_graph[k][par] = nullptr;
+      h->loop_kernels[k][par] = 0;
+    }
   if (h->gm_graph) cudaGraphExecDestroy(h->gm_graph);
   h->gm_graph = nullptr;
   h->gm_graph_kernels = 0;
@@ -261,6 +267,9 @@ int free_all(gbmg_handle* h) {
   dfree(h->red.partials); dfree(h->red.counter); dfree(h->red.result);
   if (h->host_res) cudaFreeHost(h->host_res);
   h->host_res = nullptr;
+  dfree(h->ctl);
+  if (h->ctl_host) cudaFreeHost(h->ctl_host);
+  h->ctl_host = nullptr;
   for (int i = 0; i < 2 * 512; ++i)
     if (h->pev[i]) cudaEventDestroy(h->pev[i]);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -403,6 +412,8 @@ int allocate(gbmg_handle* h) {
   GB_CUDA(h, cudaMemsetAsync(h->red.counter, 0, sizeof(unsigned int), h->stream));
   GB_CUDA(h, cudaMemsetAsync(h->red.result, 0, kRedSlots * sizeof(double), h->stream));
   GB_CUDA(h, cudaMallocHost((void**)&h->host_res, kRedSlots * sizeof(double)));
+  GB_TRY(dmalloc(h, &h->ctl, 1));
+  GB_CUDA(h, cudaMallocHost((void**)&h->ctl_host, sizeof(CycleCtl)));
   GB_TRY(dmalloc(h, &h->derr, 4));
   GB_CUDA(h, cudaMemsetAsync(h->derr, 0, 4 * sizeof(int), h->stream));
   if (h->mixed) GB_TRY(setup_tma(h));
@@ -543,7 +554,7 @@ int read_result(gbmg_handle* h, int slot, double* v) {
 }
 
 // Enqueue the body of one solver iteration for the given kind.
-int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
+int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
   const size_t n = h->n0;
@@ -591,8 +602,9 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first) {
     LAUNCH(h, V, launch_pcg_step(s, h->p, h->kd, n, h->red));
     LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), h->kr, h->red, kSlotNorm));
   }
-  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
-                             cudaMemcpyDeviceToHost, s));
+  if (to_host)
+    GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
   return check_launch(h, "iteration");
 }
 
@@ -630,6 +642,115 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
   }
   GB_CUDA(h, cudaGraphLaunch(gx, h->stream));
   h->launches += h->graph_kernels[kind][par];
+  return GBMG_OK;
+}
+
+// The cycle loop as one graph: a WHILE node whose body is the iteration of
+// `kind` followed by k_cycle_ctl, which applies the stopping tests on the
+// device and ends the loop, so the host waits once per solve instead of once
+// per cycle.  The mixed iteration alternates its two p buffers, so its body is
+// the iteration from buffer par, the controller, then (an IF node on that
+// controller's verdict) the iteration from the other buffer and the
+// controller again.  Leaves h->loop_graph[kind][par] null, and sets
+// h->loop_off, when the graph cannot be built (the host loop then runs).
+int build_loop(gbmg_handle* h, int kind, int par) {
+  const cudaStream_t s = h->stream;
+  const bool two = kind == kGraphMixed;
+  cudaGraph_t g = nullptr;
+  GB_CUDA(h, cudaGraphCreate(&g, 0));
+  const int64_t before = h->launches;
+  const int pcur = h->pcur;
+  int rc = GBMG_OK;
+  bool capturing = false;
+  cudaError_t e = cudaSuccess;
+  cudaGraph_t done = nullptr;
+  do {
+    cudaGraphConditionalHandle hw{}, hi{};
+    if ((e = cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault))) break;
+    cudaGraphNodeParams wp{};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    if ((e = cudaGraphAddNode(&wn, g, nullptr, nullptr, 0, &wp))) break;
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    if (two && (e = cudaGraphConditionalHandleCreate(&hi, body, 0, 0))) break;
+    if ((e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal)))
+      break;
+    capturing = true;
+    h->pcur = par;
+    if ((rc = enqueue_iteration(h, kind, false, false)) != GBMG_OK) break;
+    launch_cycle_ctl(s, h->ctl, h->red.result, hw, hi, two ? 1 : 0);
+    h->launches += 1;
+    if (two) {
+      cudaStreamCaptureStatus cs;
+      const cudaGraphNode_t* d = nullptr;
+      size_t nd = 0;
+      if ((e = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &d, nullptr, &nd))) break;
+      std::vector<cudaGraphNode_t> deps(d, d + nd);
+      capturing = false;
+      if ((e = cudaStreamEndCapture(s, &done))) break;
+      cudaGraphNodeParams ip{};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = hi;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      cudaGraphNode_t in = nullptr;
+      if ((e = cudaGraphAddNode(&in, body, deps.data(), nullptr, deps.size(), &ip))) break;
+      if ((e = cudaStreamBeginCaptureToGraph(s, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal)))
+        break;
+      capturing = true;
+      h->pcur = 1 - par;
+      if ((rc = enqueue_iteration(h, kind, false, false)) != GBMG_OK) break;
+      launch_cycle_ctl(s, h->ctl, h->red.result, hw, hi, 0);
+      h->launches += 1;
+    }
+    capturing = false;
+    if ((e = cudaStreamEndCapture(s, &done))) break;
+    if ((e = cudaGraphInstantiate(&h->loop_graph[kind][par], g, 0))) {
+      h->loop_graph[kind][par] = nullptr;
+      break;
+    }
+  } while (false);
+  if (capturing) cudaStreamEndCapture(s, &done);
+  h->pcur = pcur;
+  h->loop_kernels[kind][par] = (h->launches - before) / (two ? 2 : 1);
+  h->launches = before;
+  cudaGraphDestroy(g);
+  if (rc != GBMG_OK) return rc;
+  if (e != cudaSuccess || !h->loop_graph[kind][par]) {
+    cudaGetLastError();
+    h->loop_off = true;
+  }
+  return GBMG_OK;
+}
+
+// Runs cycles on the device from the state *c until the stopping tests end
+// them; *c receives the final state.  *used = false: the device loop is not
+// available and nothing ran.
+int run_loop(gbmg_handle* h, int kind, CycleCtl* c, bool* used) {
+  *used = false;
+  if (h->loop_off || h->prm.use_graph != 1 || h->prof) return GBMG_OK;
+  const int par = kind == kGraphMixed ? h->pcur : 0;
+  if (!h->loop_graph[kind][par]) {
+    GB_TRY(build_loop(h, kind, par));
+    if (!h->loop_graph[kind][par]) return GBMG_OK;
+  }
+  const cudaStream_t s = h->stream;
+  const int cyc0 = c->cyc;
+  *h->ctl_host = *c;
+  GB_CUDA(h, cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(CycleCtl), cudaMemcpyHostToDevice, s));
+  GB_CUDA(h, cudaGraphLaunch(h->loop_graph[kind][par], s));
+  GB_CUDA(h, cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(CycleCtl), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  GB_CUDA(h, cudaStreamSynchronize(s));
+  *c = *h->ctl_host;
+  h->launches += h->loop_kernels[kind][par] * (int64_t)(c->cyc - cyc0);
+  *used = true;
   return GBMG_OK;
 }
 
@@ -905,6 +1026,33 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
       double best = rel;
       int flat = 0;
       while (cyc < h->prm.max_cycles) {
+        // every iteration but the first flexible-CG one: the loop on the device
+        if (!(pcg && cyc == 0)) {
+          CycleCtl c{};
+          c.scale = scale;
+          c.tol = tol;
+          c.guard = 1e3 * std::max(1.0, st->res0);
+          c.best = best;
+          c.max_cycles = h->prm.max_cycles;
+          c.by_inc = by_inc ? 1 : 0;
+          c.flat_stop = (kind == kGraphMixed && h->prm.certify) ? 1 : 0;
+          c.cyc = cyc;
+          c.flat = flat;
+          bool used = false;
+          GB_TRY(run_loop(h, kind, &c, &used));
+          if (used) {
+            if (kind == kGraphMixed) h->pcur ^= (c.cyc - cyc) & 1;
+            cyc = c.cyc;
+            r2 = c.r2;
+            rel = c.rel;
+            if (by_inc) st->increment = c.inc;
+            if (c.status == kCtlDiverged) status = GBMG_DIVERGED;
+            else if (c.status == kCtlConverged) status = GBMG_OK;
+            stalled = c.stalled != 0;
+            st->device_loop = 1;
+            break;
+          }
+        }
         ++cyc;
         GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
         if (kind == kGraphMixed) h->pcur ^= 1;
@@ -1135,7 +1283,8 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
                                          h->prm.precision != GBMG_PREC_MIXED) ||
       h->prm.stop_rule < GBMG_STOP_RELATIVE || h->prm.stop_rule > GBMG_STOP_INCREMENT ||
       (h->prm.stop_rule == GBMG_STOP_INCREMENT && h->prm.krylov != 0) ||
-      (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1)) {
+      (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1) || h->prm.use_graph < 0 ||
+      h->prm.use_graph > 2) {
     delete h;
     return GBMG_INVALID_ARG;
   }

@@ -57,6 +57,25 @@ struct ReduceScratch {
 constexpr int kRedValues = 2;   // values reduced together per launch
 constexpr int kRedSlots = 16;   // result slots
 
+// State of the cycle loop run on the device (k_cycle_ctl after each cycle):
+// the host's stopping tests, in the same order and arithmetic.
+struct CycleCtl {
+  double scale;      // ||b|| (1 when b = 0)
+  double tol;        // threshold of the residual test (or of the increment)
+  double guard;      // divergence bound on the relative residual
+  double best;       // lowest relative residual so far (the flat test)
+  double r2, rel;    // last cycle: sum r^2 and ||r|| / scale
+  double inc;        // last cycle: max |p_k - p_(k-1)| (increment rule)
+  int max_cycles;
+  int by_inc;        // stop on the increment instead of the residual
+  int flat_stop;     // stop after four cycles without a lower residual
+  int cyc;           // cycles done
+  int flat;          // cycles since the last new lowest residual
+  int status;        // kCtlRunning / kCtlConverged / kCtlDiverged
+  int stalled;       // the flat test ended the loop
+};
+enum : int { kCtlRunning = 0, kCtlConverged = 1, kCtlDiverged = 2 };
+
 // Result slot assignment.
 enum : int {
   kSlotNorm = 0,     // sum r^2 of the last residual
@@ -213,6 +232,12 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
 // The mean-free increment of a cycle: d = x - y (y null: d = x) over the
 // cells (colour-split when hstride > 0); R.result[slot_sum] <- sum d,
 // R.result[slot_out] <- max |d - mean d| (bit pattern of a non-negative double)
+// One thread: applies the stopping tests to the cycle just finished and
+// sets the graph conditionals `loop` (and `next` when has_next) to 1 to go on
+// or 0 to stop.  Only inside a graph that owns these handles.
+void launch_cycle_ctl(cudaStream_t s, CycleCtl* c, const double* result,
+                      cudaGraphConditionalHandle loop, cudaGraphConditionalHandle next,
+                      int has_next);
 template <typename T>
 void launch_increment(cudaStream_t s, const T* x, const T* y, size_t n, size_t hstride,
                       const ReduceScratch& R, int slot_sum, int slot_out);

@@ -82,6 +82,13 @@ struct gbmg_handle {
   // captured iterations, per kind and per parity of pcur
   cudaGraphExec_t graph[4][2] = {};
   int64_t graph_kernels[4][2] = {};
+  // the whole cycle loop as one graph (a device-side WHILE node), per kind and
+  // per starting parity of pcur; loop_kernels: kernels per cycle
+  cudaGraphExec_t loop_graph[4][2] = {};
+  int64_t loop_kernels[4][2] = {};
+  bool loop_off = false;          // the device loop could not be built: host loop
+  gbmg::CycleCtl* ctl = nullptr;  // its state on the device, and a pinned mirror
+  gbmg::CycleCtl* ctl_host = nullptr;
   // flexible GMRES: kz = M kr and kq = A kz as one captured graph
   cudaGraphExec_t gm_graph = nullptr;
   int64_t gm_graph_kernels = 0;

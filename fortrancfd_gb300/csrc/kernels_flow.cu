@@ -518,6 +518,48 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
   k_div_stats<<<blocks, kRedThreads, 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, R);
 }
 
+__global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
+                            cudaGraphConditionalHandle loop, cudaGraphConditionalHandle next,
+                            int has_next) {
+  c->cyc += 1;
+  const double r2 = result[kSlotNorm];
+  const double rel = sqrt(r2) / c->scale;
+  c->r2 = r2;
+  c->rel = rel;
+  int stop = 0;
+  if (!isfinite(rel) || rel > c->guard) {
+    c->status = kCtlDiverged;
+    stop = 1;
+  } else if (c->by_inc) {
+    const double dp = result[kSlotInc];  // a non-negative double kept as its bit pattern
+    c->inc = dp;
+    if (dp < c->tol) {
+      c->status = kCtlConverged;
+      stop = 1;
+    }
+  } else if (rel < c->tol) {
+    c->status = kCtlConverged;
+    stop = 1;
+  } else if (c->flat_stop) {
+    if (rel < c->best) {
+      c->best = rel;
+      c->flat = 0;
+    } else if (++c->flat >= 4) {
+      c->stalled = 1;
+      stop = 1;
+    }
+  }
+  if (!stop && c->cyc >= c->max_cycles) stop = 1;
+  cudaGraphSetConditional(loop, stop ? 0u : 1u);
+  if (has_next) cudaGraphSetConditional(next, stop ? 0u : 1u);
+}
+
+void launch_cycle_ctl(cudaStream_t s, CycleCtl* c, const double* result,
+                      cudaGraphConditionalHandle loop, cudaGraphConditionalHandle next,
+                      int has_next) {
+  k_cycle_ctl<<<1, 1, 0, s>>>(c, result, loop, next, has_next);
+}
+
 template <typename T>
 void launch_increment(cudaStream_t s, const T* x, const T* y, size_t n, size_t hstride,
                       const ReduceScratch& R, int slot_sum, int slot_out) {

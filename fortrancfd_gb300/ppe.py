@@ -112,7 +112,10 @@ class PressurePoisson:
     p_tol*1e-3) or "increment" (max |p_k - p_(k-1)| < tol between cycles, the
     rule of ppe_sor_solver and PRESS_POISSON; pass p_tol).  zero_wall_faces:
     set the wall-normal faces of u, v, w to zero before the divergence, as
-    MPLS_RisingBubble's RHSP does.
+    MPLS_RisingBubble's RHSP does.  use_graph: True (or "loop") runs the
+    cycle loop as one CUDA graph with the stopping tests on the device,
+    "cycle" replays one graph per cycle and tests on the host, False launches
+    each kernel.
     """
 
     def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
@@ -134,7 +137,7 @@ class PressurePoisson:
         prm.nu1, prm.nu2 = nu1, nu2
         prm.levels, prm.coarse_max, prm.max_cycles = levels, coarse_max, max_cycles
         prm.krylov = _krylov_mode(krylov)
-        prm.use_graph = int(bool(use_graph))
+        prm.use_graph = {True: 1, False: 0, "loop": 1, "cycle": 2}.get(use_graph, use_graph)
         prm.remove_rhs_mean = int(bool(remove_rhs_mean))
         prm.certify = int(bool(certify))
         prm.stop_rule = {"relative": _lib.GBMG_STOP_RELATIVE, "rms": _lib.GBMG_STOP_RMS,

@@ -35,6 +35,7 @@ module gbmg
   type, bind(c) :: gbmg_stats
     integer(c_int32_t) :: status, cycles, levels, coarse_n
     real(c_double)     :: rel_residual, rms_residual, res0, ms, bytes, increment
+    integer(c_int32_t) :: device_loop
   end type
 
   type, bind(c) :: gbmg_field

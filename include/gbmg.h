@@ -87,7 +87,9 @@ typedef struct {
   int32_t max_cycles;      /* cycle (or Krylov iteration) limit */
   int32_t krylov;          /* 0: stationary V-cycles; 1: flexible CG, 2: flexible GMRES(30)
                               (residual falls monotonically), one V-cycle as preconditioner */
-  int32_t use_graph;       /* 1: replay each cycle as a captured CUDA graph */
+  int32_t use_graph;       /* 1 (default): the cycle loop as one CUDA graph whose stopping tests
+                              run on the device (one host wait per solve); 2: one captured graph
+                              per cycle, tested on the host; 0: no graphs */
   int32_t remove_rhs_mean; /* 1: project the mean out of b before solving (compatibility) */
   int32_t certify;         /* mixed precision: 1 = recompute the final residual in native FP64
                               (the cycle loop tracks it in double-word FP32 pairs) */
@@ -114,6 +116,7 @@ typedef struct {
   double bytes;         /* algorithmic HBM bytes of the call */
   double increment;     /* GBMG_STOP_INCREMENT: max |p_k - p_(k-1)| of the last cycle (the
                            reference's ppe_linf); 0 under the other rules */
+  int32_t device_loop;  /* 1: the cycles ran as one graph with the stopping tests on the device */
 } gbmg_stats;
 
 typedef struct {
