@@ -324,6 +324,17 @@ def oracle_parity(p_or, st_or, coef, b, p_mixed, p_fp64, threads):
     if p_fp64 is not None:
         out["p_rel_l2_fp64_vs_oracle"] = rel_l2_mean_free(p_fp64, p_or)
         out["p_rel_l2_fp64_vs_lex"] = rel_l2_mean_free(p_fp64, p_lex)
+    # The error of each solution: against the oracle continued from its own
+    # solution to a relative residual of 1e-13 (the solves above stop at
+    # 1e-10 after different cycle counts, so they differ from one another by
+    # about their own errors).
+    p_conv, st_conv = orc.mg_solve(coef, b, p0=p_or, tol=1e-13, max_cycles=60)
+    out["converged_rel_residual"] = st_conv["rel_residual"]
+    out["p_err_oracle"] = rel_l2_mean_free(p_or, p_conv)
+    out["p_err_lex"] = rel_l2_mean_free(p_lex, p_conv)
+    out["p_err_mixed"] = rel_l2_mean_free(p_mixed, p_conv)
+    if p_fp64 is not None:
+        out["p_err_fp64"] = rel_l2_mean_free(p_fp64, p_conv)
     return out
 
 
@@ -1134,7 +1145,7 @@ def scalar_summary(fp64, parity, adj, multi, roll, tstep):
     put("cycles_fp64", fp64, "cycles")
     for k in ("p_rel_l2_mixed_vs_oracle", "p_rel_l2_fp64_vs_oracle", "cycles_oracle",
               "p_rel_l2_fp64_vs_lex", "p_rel_l2_mixed_vs_lex", "p_rel_l2_oracle_vs_lex",
-              "cycles_lex", "lex_ms"):
+              "cycles_lex", "lex_ms", "p_err_mixed", "p_err_fp64", "p_err_oracle", "p_err_lex"):
         put(k, parity, k)
     put("ms_512_mixed", multi, "mixed", "ms_per_solve")
     put("ms_512_fp64", multi, "fp64", "ms_per_solve")

@@ -55,7 +55,8 @@ class Params(C.Structure):
                 ("levels", C.c_int32), ("coarse_max", C.c_int32), ("max_cycles", C.c_int32),
                 ("krylov", C.c_int32), ("use_graph", C.c_int32), ("remove_rhs_mean", C.c_int32),
                 ("certify", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
-                ("stop_rule", C.c_int32), ("zero_wall_faces", C.c_int32)]
+                ("stop_rule", C.c_int32), ("zero_wall_faces", C.c_int32),
+                ("inner_cycles", C.c_int32)]
 
 
 class Stats(C.Structure):

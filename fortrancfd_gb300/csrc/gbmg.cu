@@ -554,7 +554,8 @@ int read_result(gbmg_handle* h, int slot, double* v) {
 }
 
 // Enqueue the body of one solver iteration for the given kind.
-int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true) {
+// cycles: FP32 V-cycles of a mixed iteration (one defect correction)
+int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true, int cycles = 1) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
   const size_t n = h->n0;
@@ -569,9 +570,11 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true)
     if (inc) LAUNCH(h, V, launch_increment<double>(s, h->p, h->r0, n, 0, h->red, kSlotIncSum, kSlotInc));
     LAUNCH(h, R, launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
   } else if (kind == kGraphMixed) {
-    // e = V-cycle(r) in FP32; p += e and r = b - A p in double-word
+    // e = V-cycles(r) in FP32 (the first from zero, the others continuing
+    // from e); p += e and r = b - A p in double-word
     if (!zg) GB_CUDA(h, cudaMemsetAsync(f.sol32, 0, n * sizeof(float), s));
     GB_TRY(enqueue_vcycle<float>(h, false, zg));
+    for (int c = 1; c < cycles; ++c) GB_TRY(enqueue_vcycle<float>(h, false, false));
     // the increment rule: the cycle's correction e is p_k - p_(k-1)
     if (inc)
       LAUNCH(h, V, launch_increment<float>(s, f.sol32, (const float*)nullptr, n,
@@ -608,9 +611,9 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true)
   return check_launch(h, "iteration");
 }
 
-int run_iteration(gbmg_handle* h, int kind, bool first) {
-  if (!h->prm.use_graph || first || h->prof) {
-    GB_TRY(enqueue_iteration(h, kind, first));
+int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
+  if (!h->prm.use_graph || first || h->prof || (kind == kGraphMixed && cycles != h->inner)) {
+    GB_TRY(enqueue_iteration(h, kind, first, true, cycles));
     return GBMG_OK;
   }
   const int par = kind == kGraphMixed ? h->pcur : 0;
@@ -619,7 +622,7 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
     cudaGraph_t g = nullptr;
     const int64_t before = h->launches;
     GB_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    const int rc = enqueue_iteration(h, kind, false);
+    const int rc = enqueue_iteration(h, kind, false, true, cycles);
     const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     if (rc != GBMG_OK) {
       if (g) cudaGraphDestroy(g);
@@ -656,6 +659,7 @@ int run_iteration(gbmg_handle* h, int kind, bool first) {
 int build_loop(gbmg_handle* h, int kind, int par) {
   const cudaStream_t s = h->stream;
   const bool two = kind == kGraphMixed;
+  const int step = two ? h->inner : 1;
   cudaGraph_t g = nullptr;
   GB_CUDA(h, cudaGraphCreate(&g, 0));
   const int64_t before = h->launches;
@@ -681,7 +685,7 @@ int build_loop(gbmg_handle* h, int kind, int par) {
       break;
     capturing = true;
     h->pcur = par;
-    if ((rc = enqueue_iteration(h, kind, false, false)) != GBMG_OK) break;
+    if ((rc = enqueue_iteration(h, kind, false, false, step)) != GBMG_OK) break;
     launch_cycle_ctl(s, h->ctl, h->red.result, hw, hi, two ? 1 : 0);
     h->launches += 1;
     if (two) {
@@ -704,7 +708,7 @@ int build_loop(gbmg_handle* h, int kind, int par) {
         break;
       capturing = true;
       h->pcur = 1 - par;
-      if ((rc = enqueue_iteration(h, kind, false, false)) != GBMG_OK) break;
+      if ((rc = enqueue_iteration(h, kind, false, false, step)) != GBMG_OK) break;
       launch_cycle_ctl(s, h->ctl, h->red.result, hw, hi, 0);
       h->launches += 1;
     }
@@ -740,7 +744,7 @@ int run_loop(gbmg_handle* h, int kind, CycleCtl* c, bool* used) {
     if (!h->loop_graph[kind][par]) return GBMG_OK;
   }
   const cudaStream_t s = h->stream;
-  const int cyc0 = c->cyc;
+  const int it0 = c->iters;
   *h->ctl_host = *c;
   GB_CUDA(h, cudaMemcpyAsync(h->ctl, h->ctl_host, sizeof(CycleCtl), cudaMemcpyHostToDevice, s));
   GB_CUDA(h, cudaGraphLaunch(h->loop_graph[kind][par], s));
@@ -749,7 +753,7 @@ int run_loop(gbmg_handle* h, int kind, CycleCtl* c, bool* used) {
                              cudaMemcpyDeviceToHost, s));
   GB_CUDA(h, cudaStreamSynchronize(s));
   *c = *h->ctl_host;
-  h->launches += h->loop_kernels[kind][par] * (int64_t)(c->cyc - cyc0);
+  h->launches += h->loop_kernels[kind][par] * (int64_t)(c->iters - it0);
   *used = true;
   return GBMG_OK;
 }
@@ -1034,6 +1038,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
           c.guard = 1e3 * std::max(1.0, st->res0);
           c.best = best;
           c.max_cycles = h->prm.max_cycles;
+          c.step = kind == kGraphMixed ? h->inner : 1;
           c.by_inc = by_inc ? 1 : 0;
           c.flat_stop = (kind == kGraphMixed && h->prm.certify) ? 1 : 0;
           c.cyc = cyc;
@@ -1041,20 +1046,27 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
           bool used = false;
           GB_TRY(run_loop(h, kind, &c, &used));
           if (used) {
-            if (kind == kGraphMixed) h->pcur ^= (c.cyc - cyc) & 1;
-            cyc = c.cyc;
-            r2 = c.r2;
-            rel = c.rel;
-            if (by_inc) st->increment = c.inc;
-            if (c.status == kCtlDiverged) status = GBMG_DIVERGED;
-            else if (c.status == kCtlConverged) status = GBMG_OK;
-            stalled = c.stalled != 0;
+            if (kind == kGraphMixed) h->pcur ^= c.iters & 1;
             st->device_loop = 1;
-            break;
+            if (c.iters > 0) {
+              cyc = c.cyc;
+              r2 = c.r2;
+              rel = c.rel;
+              best = c.best;
+              flat = c.flat;
+              if (by_inc) st->increment = c.inc;
+              if (c.status == kCtlDiverged) status = GBMG_DIVERGED;
+              else if (c.status == kCtlConverged) status = GBMG_OK;
+              stalled = c.stalled != 0;
+            }
+            // ended by a test, or too few cycles left for a whole iteration:
+            // those run below, one cycle at a time
+            if (status != GBMG_NOT_CONVERGED || stalled || cyc >= h->prm.max_cycles) break;
           }
         }
-        ++cyc;
-        GB_TRY(run_iteration(h, kind, pcg && cyc == 1));
+        const int step = kind == kGraphMixed ? std::min(h->inner, h->prm.max_cycles - cyc) : 1;
+        cyc += step;
+        GB_TRY(run_iteration(h, kind, pcg && cyc == 1, step));
         if (kind == kGraphMixed) h->pcur ^= 1;
         GB_CUDA(h, cudaStreamSynchronize(s));
         prof_flush(h);
@@ -1154,10 +1166,13 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
   st->coarse_n = h->nc;
   st->rel_residual = rel;
   st->rms_residual = std::sqrt(r2 / (double)n);
-  // algorithmic bytes: per cycle V-cycle + FP64 residual (p, b, cx, cy, cz)
+  // algorithmic bytes per cycle: the V-cycle, plus the residual of each
+  // iteration (FP64: p, b, cx, cy, cz; or the defect with its e read, p write,
+  // r32 write and zeroed e)
   const int w = h->mixed ? 4 : 8;
-  double per = vcycle_bytes(h, w) + 40.0 * n;
-  if (h->mixed) per += 16.0 * n + 4.0 * n;  // defect: + e read, p write, r32 write; zero e
+  double per = vcycle_bytes(h, w);
+  if (kind == kGraphMixed) per += (40.0 * n + 16.0 * n + 4.0 * n) / h->inner;
+  else per += 40.0 * n + (h->mixed ? 20.0 * n : 0.0);
   if (pcg) per += (h->mixed ? 24.0 : 8.0) * n + 16.0 * n + 32.0 * n + 48.0 * n + 24.0 * n + 8.0 * n;
   st->bytes = per * cyc + 40.0 * n + 32.0 * n;
   return status;
@@ -1284,11 +1299,19 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
       h->prm.stop_rule < GBMG_STOP_RELATIVE || h->prm.stop_rule > GBMG_STOP_INCREMENT ||
       (h->prm.stop_rule == GBMG_STOP_INCREMENT && h->prm.krylov != 0) ||
       (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1) || h->prm.use_graph < 0 ||
-      h->prm.use_graph > 2) {
+      h->prm.use_graph > 2 || h->prm.inner_cycles < 0 || h->prm.inner_cycles > 8 ||
+      (h->prm.inner_cycles > 1 && h->prm.stop_rule == GBMG_STOP_INCREMENT)) {
     delete h;
     return GBMG_INVALID_ARG;
   }
   h->mixed = h->prm.precision == GBMG_PREC_MIXED;
+  // Two FP32 cycles per defect correction: the FP32 correction is good to
+  // about 1e-6 of its size, so a second cycle still gains its full factor,
+  // and one defect kernel in two is saved; the residual is tested every two
+  // cycles, so the count can exceed the per-cycle one by one.  The
+  // increment rule measures one cycle.
+  h->inner = h->prm.inner_cycles > 0 ? h->prm.inner_cycles
+                                     : (h->prm.stop_rule == GBMG_STOP_INCREMENT ? 1 : 2);
   if (h->prm.device >= 0) {
     if (h->prm.device >= ndev) { delete h; return GBMG_INVALID_ARG; }
     h->device = h->prm.device;

@@ -67,6 +67,8 @@ struct CycleCtl {
   double r2, rel;    // last cycle: sum r^2 and ||r|| / scale
   double inc;        // last cycle: max |p_k - p_(k-1)| (increment rule)
   int max_cycles;
+  int step;          // cycles per iteration (FP32 cycles per defect correction)
+  int iters;         // iterations done
   int by_inc;        // stop on the increment instead of the residual
   int flat_stop;     // stop after four cycles without a lower residual
   int cyc;           // cycles done

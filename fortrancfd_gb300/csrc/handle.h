@@ -74,6 +74,7 @@ struct gbmg_handle {
   float2* bw = nullptr;
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
+  int inner = 1;  // FP32 V-cycles per defect correction of the stationary mixed loop
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   int* derr = nullptr;   // device error flags (bulk-copy wait timeouts)
   gbmg::DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none,

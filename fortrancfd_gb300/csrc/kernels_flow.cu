@@ -521,7 +521,8 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
 __global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
                             cudaGraphConditionalHandle loop, cudaGraphConditionalHandle next,
                             int has_next) {
-  c->cyc += 1;
+  c->cyc += c->step;
+  c->iters += 1;
   const double r2 = result[kSlotNorm];
   const double rel = sqrt(r2) / c->scale;
   c->r2 = r2;
@@ -549,7 +550,9 @@ __global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
       stop = 1;
     }
   }
-  if (!stop && c->cyc >= c->max_cycles) stop = 1;
+  // stop before an iteration would pass the cycle limit (the host runs the
+  // remaining cycles one at a time)
+  if (!stop && c->cyc + c->step > c->max_cycles) stop = 1;
   cudaGraphSetConditional(loop, stop ? 0u : 1u);
   if (has_next) cudaGraphSetConditional(next, stop ? 0u : 1u);
 }

@@ -94,7 +94,9 @@ __global__ void __launch_bounds__(256) k_smooth_split4(LevelView<float> L, int c
   const size_t own = (size_t)color * L.hstride + h;
   float rc[4], b[4];
   unpack(ld4(L.rho + own), rc);
-  unpack(ld4(L.src + own), b);
+  // b is read once per launch and not by the next one (the other colour):
+  // streaming loads, so that the L2 keeps rho and p for the next launch
+  unpack(__ldcs(reinterpret_cast<const float4*>(L.src + own)), b);
   // A wall face gets neighbour density +inf, so its coefficient k/(rho + inf)
   // is exactly 0 and the term adds nothing: the faces need no branches.
   const float inf = __int_as_float(0x7f800000);
@@ -217,12 +219,13 @@ __global__ void __launch_bounds__(256) k_restrict_split(LevelView<float> F, Leve
 // float4 (W = 4) or float2 (W = 2) loads of each child row, the same per-cell
 // arithmetic and order.  W = 2 keeps half the loads live (fewer registers,
 // more resident warps).
-template <int W>
+template <int W, bool kStream = false>
 __device__ __forceinline__ void ldw(const float* p, float (&a)[W]) {
   if constexpr (W == 4) {
-    unpack(ld4(p), a);
+    unpack(kStream ? __ldcs(reinterpret_cast<const float4*>(p)) : ld4(p), a);
   } else {
-    const float2 v = *reinterpret_cast<const float2*>(p);
+    const float2 v = kStream ? __ldcs(reinterpret_cast<const float2*>(p))
+                             : *reinterpret_cast<const float2*>(p);
     a[0] = v.x;
     a[1] = v.y;
   }
@@ -261,8 +264,9 @@ __global__ void __launch_bounds__(256) k_restrict_splitv(LevelView<float> F, Lev
       ldw<W>(Pb, pb);
       ldw<W>(Ra, ra);
       ldw<W>(Rb, rb);
-      ldw<W>(F.src + (size_t)ca * half + h, ba);
-      ldw<W>(F.src + (size_t)(1 - ca) * half + h, bb);
+      // b is not read again in this cycle: streaming loads
+      ldw<W, true>(F.src + (size_t)ca * half + h, ba);
+      ldw<W, true>(F.src + (size_t)(1 - ca) * half + h, bb);
       // x-: cell 2I-1 (b's colour, index I-1); x+ of b: cell 2I+2 (a's colour, I+1)
       float pl_e = 0.f, rl_e = inf, pr_e = 0.f, rr_e = inf;
       if (I0 > 0) { pl_e = Pb[-1]; rl_e = Rb[-1]; }

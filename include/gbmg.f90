@@ -29,7 +29,7 @@ module gbmg
     integer(c_int32_t) :: precision, nu1, nu2, levels, coarse_max, max_cycles
     integer(c_int32_t) :: krylov, use_graph, remove_rhs_mean, certify, device
     type(c_ptr)        :: stream
-    integer(c_int32_t) :: stop_rule, zero_wall_faces
+    integer(c_int32_t) :: stop_rule, zero_wall_faces, inner_cycles
   end type
 
   type, bind(c) :: gbmg_stats

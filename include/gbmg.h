@@ -102,6 +102,9 @@ typedef struct {
                               its divergence ("MPLS_RisingBubble/20190612/
                               SOLVE_PRESSURE_POISSON.F90:16-41"); 0 (default): the faces
                               are read as given */
+  int32_t inner_cycles;    /* mixed precision, stationary loop: FP32 V-cycles per double-word
+                              defect correction (the residual is tested after each correction);
+                              0 (default) = 2, or 1 under GBMG_STOP_INCREMENT; at most 8 */
 } gbmg_params;
 
 typedef struct {

@@ -409,7 +409,8 @@ def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     against the stored FP32 coefficients (GBMG_RHO_COEF=0): the FP32 values
     differ by a few ulp, so the preconditioner changes slightly; both solves
     reach the tolerance, agree with the FP64 oracle to tol-scaled accuracy and
-    take the same number of cycles to within one."""
+    take the same number of cycles to within one iteration (the stationary
+    loop tests its residual every two cycles, one per defect correction)."""
     c = cases.config(idx, scale)
     out = {}
     for flag in ("0", "1"):
@@ -421,7 +422,7 @@ def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     for flag, (p, st) in out.items():
         assert st["rel_residual"] < 1e-10, flag
         assert rel_l2(p, want) <= 1e-6, flag
-    assert abs(out["0"][1]["cycles"] - out["1"][1]["cycles"]) <= 1
+    assert abs(out["0"][1]["cycles"] - out["1"][1]["cycles"]) <= (1 if krylov else 2)
 
 
 @pytest.mark.parametrize("idx,scale,krylov,shape", [
