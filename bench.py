@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--no-levelset", action="store_true", help="skip the level-set advection section")
     ap.add_argument("--no-momentum", action="store_true", help="skip the momentum-step section")
     ap.add_argument("--no-timestep", action="store_true", help="skip the whole-time-step section")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="headline solves with one graph per cycle, tested on the host")
     return ap.parse_args()
 
 
@@ -923,7 +925,8 @@ def run_ours(args):
 
     phi = dev_t(phi_h)
     u, v, w = dev_t(u_h), dev_t(v_h), dev_t(w_h)
-    kw = dict(krylov=args.krylov, stream=stream, nu1=NU1, nu2=NU2)
+    kw = dict(krylov=args.krylov, stream=stream, nu1=NU1, nu2=NU2,
+              use_graph="cycle" if args.host_loop else True)
 
     def barrier():
         if world > 1:
