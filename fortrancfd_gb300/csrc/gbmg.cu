@@ -273,7 +273,7 @@ int free_all(gbmg_handle* h) {
   for (int i = 0; i < 2 * 512; ++i)
     if (h->pev[i]) cudaEventDestroy(h->pev[i]);
   if (h->ev0) cudaEventDestroy(h->ev0);
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 5; ++i)
     if (h->cev[i]) cudaEventDestroy(h->cev[i]);
   if (h->cstream) cudaStreamDestroy(h->cstream);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -421,7 +421,8 @@ int allocate(gbmg_handle* h) {
   else setup_subcycle<double>(h);
   GB_CUDA(h, cudaEventCreate(&h->ev0));
   GB_CUDA(h, cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking));
-  for (int i = 0; i < 2; ++i) GB_CUDA(h, cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
+  for (int i = 0; i < 5; ++i) GB_CUDA(h, cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
+  GB_CUDA(h, cudaEventRecord(h->cev[3], h->stream));
   GB_CUDA(h, cudaEventCreate(&h->ev1));
   GB_CUDA(h, cudaStreamSynchronize(h->stream));
   return GBMG_OK;
@@ -1354,8 +1355,12 @@ int gbmg_set_rho(gbmg_handle* h, gbmg_field rho, int mem) {
   GB_TRY(validate_field(h, rho, "rho"));
   const gbmg_grid& g = h->grid;
   GB_TRY(upload(h, rho, g.nx, g.ny, g.nz, mem, h->rho));
+  GB_CUDA(h, cudaEventRecord(h->cev[4], h->stream));
   GB_TRY(set_rho_device(h, nullptr));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  // The set-up kernels run on after the call returns (the next call on the
+  // handle is ordered after them on its stream); the caller's rho has been
+  // read once the copy is done.
+  GB_CUDA(h, cudaEventSynchronize(h->cev[4]));
   return GBMG_OK;
 }
 
@@ -1375,10 +1380,15 @@ int gbmg_set_phi(gbmg_handle* h, gbmg_field phi, double eps, double rho_pos, dou
   launch_rho_from_phi(h->stream, g.nx, g.ny, g.nz, sp, eps, rho_pos, rho_neg, h->rho);
   h->launches += 1;
   GB_TRY(check_launch(h, "rho_from_phi"));
+  // phi (and the staging copy in p) has been read by here
+  GB_CUDA(h, cudaEventRecord(h->cev[3], h->stream));
   // away from the interface rho is exactly rho_pos*1 + rho_neg*0 or rho_pos*0 + rho_neg*1
   const double bulk[2] = {rho_pos * 1.0 + rho_neg * (1.0 - 1.0), rho_pos * 0.0 + rho_neg * (1.0 - 0.0)};
   GB_TRY(set_rho_device(h, bulk));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  // The remaining set-up kernels run on after the call returns (the next call
+  // on the handle is ordered after them on its stream; a solve from host
+  // arrays uploads b and p beside them).
+  GB_CUDA(h, cudaEventSynchronize(h->cev[3]));
   return GBMG_OK;
 }
 
@@ -1425,17 +1435,27 @@ int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
   double bnorm = 0.0;
   const bool host = mem == GBMG_MEM_HOST;
   if (host) {
-    // host memory: the initial p crosses to the device beside the right-hand
-    // side's upload and preparation, and the result crosses back beside the
-    // certification (the copies run on the handle's second stream)
-    GB_CUDA(h, cudaEventRecord(h->cev[0], h->stream));
-    GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[0], 0));
+    // host memory: b and the initial p cross to the device on the handle's
+    // second stream, beside the operator set-up still running from
+    // gbmg_set_phi / gbmg_set_rho (which reads neither b nor p once the
+    // staging copy in p has been consumed: cev[3]) and beside the right-hand
+    // side's preparation; the result crosses back beside the certification
+    GB_CUDA(h, cudaStreamWaitEvent(h->cstream, h->cev[3], 0));
+    GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b, h->cstream));
+    GB_CUDA(h, cudaEventRecord(h->cev[2], h->cstream));
     GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p, h->cstream));
     GB_CUDA(h, cudaEventRecord(h->cev[0], h->cstream));
+    GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[2], 0));
+    const int rc = finish_rhs(h, &bnorm);
+    if (rc != GBMG_OK) {
+      cudaStreamSynchronize(h->cstream);  // the caller's p may be freed on return
+      return rc;
+    }
+    GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[0], 0));
+  } else {
+    GB_TRY(prepare_rhs(h, b, mem, &bnorm));
+    GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
   }
-  GB_TRY(prepare_rhs(h, b, mem, &bnorm));
-  if (host) GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[0], 0));
-  else GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
   h->dl_field = host ? &p : nullptr;
   h->dl_started = false;
   const int status = solve_internal(h, tol, bnorm, st);

@@ -98,7 +98,12 @@ struct gbmg_handle {
   // p beside the right-hand side's preparation, the D2H of the result beside
   // the FP64 certification
   cudaStream_t cstream = nullptr;
-  cudaEvent_t cev[2] = {nullptr, nullptr};
+  // cev[0], cev[1]: ordering of the copy stream; cev[2]: the right-hand
+  // side's upload; cev[3]: the staging buffer p free again (the operator
+  // set-up from a host or device cell field leaves its later kernels running
+  // after the call returns, once its input has been read); cev[4]: an input
+  // field consumed
+  cudaEvent_t cev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   const gbmg_field* dl_field = nullptr;  // set by gbmg_solve for solve_internal
   bool dl_started = false;
   int64_t launches = 0;

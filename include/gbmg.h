@@ -145,13 +145,17 @@ int gbmg_destroy(gbmg_handle* h);
 /* Face coefficients from the cell density rho: ppe_sor_init
  * ("Two phase flows/newOpenMP/3D+IBM/src/ns_solver/ns_ppe_solver.f90:1-65";
  * 2D "Two phase flows/newOpenMP/2D/src/ns_solver/ns_ppe_solver.f90:1-48").
- * Also builds every coarse level and the coarse-level inverse. */
+ * Also builds every coarse level and the coarse-level inverse.  Returns once
+ * rho has been read (the caller may then reuse it); the set-up kernels run on
+ * on the handle's stream, and every later call on the handle is ordered after
+ * them (a kernel failure there is reported by the next call). */
 int gbmg_set_rho(gbmg_handle* h, gbmg_field rho, int mem);
 
 /* Density from the level set, then as gbmg_set_rho: rho_mu + ls_funs
  * ("Two phase flows/newOpenMP/2D/src/interface_solver/others.f90:1-61"):
  * rho = rho_pos*H + rho_neg*(1-H), H the smoothed Heaviside of half width eps.
- * The reference is rho_pos = 1, rho_neg = rho_12. */
+ * The reference is rho_pos = 1, rho_neg = rho_12.  Returns once phi has been
+ * read, as gbmg_set_rho. */
 int gbmg_set_phi(gbmg_handle* h, gbmg_field phi, double eps, double rho_pos, double rho_neg,
                  int mem);
 
