@@ -943,11 +943,13 @@ int start_mixed(gbmg_handle* h, bool* shifted) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
   const size_t n = h->n0;
-  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(s, h->p, n, h->red, kSlotSum));
+  LAUNCH(h, GBMG_PROF_VECTOR, launch_nonzero(s, h->p, n, h->red.result + kSlotSum + 1));
   GB_TRY(check_launch(h, "initial guess"));
   double pp = 0.0;
   GB_TRY(read_result(h, kSlotSum + 1, &pp));
-  *shifted = pp != 0.0;
+  unsigned long long nz = 0ull;
+  std::memcpy(&nz, &pp, sizeof(nz));
+  *shifted = nz != 0ull;
   if (*shifted) {
     // the correction starts at d = 0, so its first residual is r0 itself:
     // the loop's right-hand side in double-word and the FP32 cycle's input
@@ -959,9 +961,16 @@ int start_mixed(gbmg_handle* h, bool* shifted) {
     else LAUNCH(h, GBMG_PROF_VECTOR, launch_double_to_float(s, h->r0, f.src32, n));
     GB_CUDA(h, cudaMemsetAsync(h->pw[1], 0, n * sizeof(float2), s));
   } else {
-    LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(s, h->p, h->pw[0], n));
-    // the first residual (no correction yet)
-    LAUNCH(h, GBMG_PROF_RESIDUAL, enqueue_defect(h, 0, nullptr, f.src32, kSlotNorm));
+    // p = 0: the first residual is b.  Its FP32 copy is b rounded to float
+    // (what the defect kernel would store: the double-word b's hi is b
+    // rounded to nearest, and hi + lo rounds back to it), its norm is the
+    // right-hand side's from its preparation, and the double-word p is zero.
+    GB_CUDA(h, cudaMemsetAsync(h->pw[1], 0, n * sizeof(float2), s));
+    if (f.split)
+      LAUNCH(h, GBMG_PROF_VECTOR, launch_to_split(s, h->b, f.src32, f.nx, f.ny, f.nz, f.hstride));
+    else LAUNCH(h, GBMG_PROF_VECTOR, launch_double_to_float(s, h->b, f.src32, n));
+    GB_CUDA(h, cudaMemcpyAsync(h->red.result + kSlotNorm, h->red.result + kSlotSumB + 1,
+                               sizeof(double), cudaMemcpyDeviceToDevice, s));
   }
   h->pcur = 1;
   return GBMG_OK;

@@ -234,6 +234,8 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
 // The mean-free increment of a cycle: d = x - y (y null: d = x) over the
 // cells (colour-split when hstride > 0); R.result[slot_sum] <- sum d,
 // R.result[slot_out] <- max |d - mean d| (bit pattern of a non-negative double)
+// *flag (a result slot, as bits) = nonzero when any x[q] is nonzero
+void launch_nonzero(cudaStream_t s, const double* x, size_t n, double* flag);
 // One thread: applies the stopping tests to the cycle just finished and
 // sets the graph conditionals `loop` (and `next` when has_next) to 1 to go on
 // or 0 to stop.  Only inside a graph that owns these handles.

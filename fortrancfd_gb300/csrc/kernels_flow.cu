@@ -518,6 +518,16 @@ void launch_div_stats(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided
   k_div_stats<<<blocks, kRedThreads, 0, s>>>(nx, ny, nz, u, v, w, dx, dy, dz, R);
 }
 
+// *flag |= 1 when any x[q] is nonzero (-0 counts as zero): bit tests only,
+// so the pass runs at the memory rate whatever the FP64 rate
+__global__ void __launch_bounds__(kRedThreads) k_nonzero(const double* __restrict__ x, size_t n,
+                                                         unsigned long long* flag) {
+  unsigned long long acc = 0ull;
+  stride4(n, [&](size_t q) { return (unsigned long long)__double_as_longlong(x[q]); },
+          [&](size_t, unsigned long long b) { acc |= b << 1; });
+  if (__any_sync(0xffffffffu, acc != 0ull) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
 __global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
                             cudaGraphConditionalHandle loop, cudaGraphConditionalHandle next,
                             int has_next) {
@@ -583,6 +593,12 @@ void launch_zero_wall_faces(cudaStream_t s, int nx, int ny, int nz, double* u, i
   const int64_t total = (int64_t)ny * nz + (int64_t)nx * nz + (w ? (int64_t)nx * ny : 0);
   k_zero_wall_faces<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(nx, ny, nz, u, usy, usz, v,
                                                                    vsy, vsz, w, wsy, wsz);
+}
+
+void launch_nonzero(cudaStream_t s, const double* x, size_t n, double* flag) {
+  cudaMemsetAsync(flag, 0, sizeof(double), s);
+  k_nonzero<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(
+      x, n, reinterpret_cast<unsigned long long*>(flag));
 }
 
 void launch_sum(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot) {
