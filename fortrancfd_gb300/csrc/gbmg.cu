@@ -433,14 +433,17 @@ int allocate(gbmg_handle* h) {
 // level-0 FP64 coefficients.
 int build_hierarchy(gbmg_handle* h) {
   const cudaStream_t s = h->stream;
+  // the coarse levels' FP32 copies come out of the coarsening
   for (int l = 1; l < h->L; ++l) {
     Level& c = h->lv[l];
-    LAUNCH(h, GBMG_PROF_SETUP, launch_coarsen(s, v64(h->lv[l - 1]), c.cx, c.cy, c.cz, c.nx, c.ny, c.nz));
+    LAUNCH(h, GBMG_PROF_SETUP,
+           launch_coarsen(s, v64(h->lv[l - 1]), c.cx, c.cy, c.cz, c.nx, c.ny, c.nz,
+                          Float3Out{{c.cx32, c.cy32, c.cz32}}));
   }
   for (int l = 0; l < h->L; ++l) {
     Level& v = h->lv[l];
     if (v.idiag) LAUNCH(h, GBMG_PROF_SETUP, launch_idiag(s, v64(v), v.idiag));
-    if (v.cx32 && !(l == 0 && h->fine_copies)) {
+    if (l == 0 && v.cx32 && !h->fine_copies) {
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cx, v.cx32, v.n));
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cy, v.cy32, v.n));
       LAUNCH(h, GBMG_PROF_SETUP, launch_to_float(s, v.cz, v.cz32, v.n));
@@ -527,11 +530,15 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
 // h->b holds the right-hand side: project its mean out (when asked), make the
 // double-word copy of the mixed solve, and return |b|.
 int finish_rhs(gbmg_handle* h, double* bnorm) {
-  LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
-  if (h->prm.remove_rhs_mean)
-    LAUNCH(h, GBMG_PROF_VECTOR,
-           launch_shift_by_mean(h->stream, h->b, h->b, h->n0, h->red, kSlotSumB, kSlotSumB + 1));
-  if (h->mixed) LAUNCH(h, GBMG_PROF_VECTOR, launch_to_dw(h->stream, h->b, h->bw, h->n0));
+  const bool rm = h->prm.remove_rhs_mean != 0;
+  if (rm) LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
+  // one pass: the shift, |b|^2, the double-word copy and (stationary mixed
+  // loop) the first FP32 residual of a solve from p = 0
+  const Level& f = h->lv[0];
+  float* r32 = h->mixed && h->prm.krylov == 0 ? f.src32 : nullptr;
+  LAUNCH(h, GBMG_PROF_VECTOR,
+         launch_rhs_prep(h->stream, h->b, h->n0, h->red, rm ? kSlotSumB : -1, kSlotSumB + 1,
+                         h->mixed ? h->bw : nullptr, r32, f.nx, f.ny, f.split ? f.hstride : 0));
   GB_TRY(check_launch(h, "rhs"));
   GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
                              cudaMemcpyDeviceToHost, h->stream));
@@ -961,14 +968,11 @@ int start_mixed(gbmg_handle* h, bool* shifted) {
     else LAUNCH(h, GBMG_PROF_VECTOR, launch_double_to_float(s, h->r0, f.src32, n));
     GB_CUDA(h, cudaMemsetAsync(h->pw[1], 0, n * sizeof(float2), s));
   } else {
-    // p = 0: the first residual is b.  Its FP32 copy is b rounded to float
-    // (what the defect kernel would store: the double-word b's hi is b
-    // rounded to nearest, and hi + lo rounds back to it), its norm is the
-    // right-hand side's from its preparation, and the double-word p is zero.
+    // p = 0: the first residual is b.  The right-hand side's preparation
+    // already wrote its FP32 copy, b rounded to float (what the defect kernel
+    // would store: the double-word b's hi is b rounded to nearest, and
+    // hi + lo rounds back to it), and its norm; the double-word p is zero.
     GB_CUDA(h, cudaMemsetAsync(h->pw[1], 0, n * sizeof(float2), s));
-    if (f.split)
-      LAUNCH(h, GBMG_PROF_VECTOR, launch_to_split(s, h->b, f.src32, f.nx, f.ny, f.nz, f.hstride));
-    else LAUNCH(h, GBMG_PROF_VECTOR, launch_double_to_float(s, h->b, f.src32, n));
     GB_CUDA(h, cudaMemcpyAsync(h->red.result + kSlotNorm, h->red.result + kSlotSumB + 1,
                                sizeof(double), cudaMemcpyDeviceToDevice, s));
   }

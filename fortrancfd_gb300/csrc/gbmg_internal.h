@@ -141,8 +141,12 @@ void launch_coarse_solve(cudaStream_t s, int n, const T* minv, const T* adense, 
 // work: 2 n^2 + n doubles of scratch (n = cells of the coarsest level)
 void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* minv,
                           double* adense, float* minv32, float* adense32, double* work);
+// three optional float outputs
+struct Float3Out {
+  float* p[3];
+};
 void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,
-                    double* cz, int cnx, int cny, int cnz);
+                    double* cz, int cnx, int cny, int cnz, Float3Out c32 = Float3Out{});
 void launch_idiag(cudaStream_t s, const LevelView<double>& L, double* idiag);
 void launch_to_float(cudaStream_t s, const double* a, float* b, size_t n);
 
@@ -305,6 +309,11 @@ void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, i
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
                        size_t hstride);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
+// b -= result[mslot]/n (mslot < 0: unchanged), sum b^2 -> result[slot2], and
+// when given the double-word copy bw and float(b) into r32 (colour-split when
+// hstride != 0): one pass
+void launch_rhs_prep(cudaStream_t s, double* b, size_t n, const ReduceScratch& R, int mslot,
+                     int slot2, float2* bw, float* r32, int nx, int ny, size_t hstride);
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot);
 // out += double(d)
 void launch_dw_accumulate(cudaStream_t s, const float2* d, double* out, size_t n);

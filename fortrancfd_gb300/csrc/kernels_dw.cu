@@ -305,12 +305,60 @@ __global__ void k_dw_accumulate(const float2* __restrict__ d, double* __restrict
           [&](size_t q, dw v) { out[q] += dw_to_double_int(v); });
 }
 
+// The right-hand side's preparation in one pass: b -= m (m = result[mslot]/n;
+// mslot < 0: no shift, b not written), sum (b - m)^2 -> result[slot2] (the
+// order of k_shift_by_mean / k_sum, so the same bits), and, when given, the
+// double-word copy bw and b rounded to float into r32 (the mixed solve's
+// first residual for p = 0), colour-split when hstride != 0.
+template <typename I>
+__device__ __forceinline__ size_t split_index(size_t q, int nx, int ny, size_t hstride) {
+  const I qq = (I)q;
+  const I r = qq / (I)nx;
+  const int i = (int)(qq - r * (I)nx);
+  const I k = r / (I)ny;
+  const int j = (int)(r - k * (I)ny);
+  return (size_t)((i + j + (int)(k & 1)) & 1) * hstride + (q >> 1);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_rhs_prep(double* __restrict__ b, size_t n,
+                                                          ReduceScratch R, int mslot, int slot2,
+                                                          float2* __restrict__ bw,
+                                                          float* __restrict__ r32, int nx, int ny,
+                                                          size_t hstride) {
+  const double m = mslot >= 0 ? R.result[mslot] / (double)n : 0.0;
+  const bool small = n < (size_t(1) << 32);
+  double acc[1] = {0.0};
+  stride4(n, [&](size_t q) { return b[q]; }, [&](size_t q, double x) {
+    const double a = mslot >= 0 ? x - m : x;
+    if (mslot >= 0) b[q] = a;
+    acc[0] += a * a;
+    if (bw) {
+      const dw v = dw_from_double_int(a);
+      bw[q] = make_float2(v.hi, v.lo);
+      // v.hi is a rounded to nearest float
+      if (r32) {
+        const size_t o = hstride == 0 ? q
+                         : small    ? split_index<unsigned>(q, nx, ny, hstride)
+                                    : split_index<size_t>(q, nx, ny, hstride);
+        r32[o] = v.hi;
+      }
+    }
+  });
+  grid_sum_finish<1>(acc, R, slot2);
+}
+
 inline unsigned stride_blocks(size_t n) {
   const size_t b = (n + kRedThreads - 1) / kRedThreads;
   return (unsigned)std::max<size_t>(1, std::min<size_t>(b, 152 * 8));
 }
 
 }  // namespace
+
+void launch_rhs_prep(cudaStream_t s, double* b, size_t n, const ReduceScratch& R, int mslot,
+                     int slot2, float2* bw, float* r32, int nx, int ny, size_t hstride) {
+  const unsigned blocks = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_rhs_prep<<<blocks, kRedThreads, 0, s>>>(b, n, R, mslot, slot2, bw, r32, nx, ny, hstride);
+}
 
 dim3 defect_grid(int nx, int ny, int nz) {
   return dim3((unsigned)((nx + kDTX - 1) / kDTX), (unsigned)((ny + kDTY - 1) / kDTY),

@@ -38,31 +38,42 @@ inline unsigned stride_blocks(size_t n) {
 // NaN stays on the full branch), and outside cells store the two bulk values
 // rho_pos*1 + rho_neg*0 and rho_pos*0 + rho_neg*1 computed by the host: the
 // full formula's result for H = 1 and 0, without FP64 work.
+constexpr int kRhoPlanes = 4;
+
 __global__ void __launch_bounds__(256) k_rho_from_phi(int nx, int ny, int nz, Strided phi,
                                                       double eps, long long eps_out_bits,
                                                       double rho_pos, double rho_neg,
                                                       double bulk_pos, double bulk_neg,
                                                       double* rho) {
+  // four z planes per thread, their loads issued together
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  const int k0 = blockIdx.z * kRhoPlanes;
   if (i >= nx || j >= ny) return;
   const double pi = 3.141592653589793;
-  const double ph = phi.data[i + j * phi.sy + k * phi.sz];
-  const long long pb = __double_as_longlong(ph);
-  const long long mag = pb & 0x7fffffffffffffffll;
-  double* out = rho + ((size_t)k * ny + j) * nx + i;
-  if (mag > eps_out_bits && mag <= 0x7ff0000000000000ll) {
-    *out = pb < 0 ? bulk_neg : bulk_pos;
-    return;
+  double ph[kRhoPlanes];
+#pragma unroll
+  for (int u = 0; u < kRhoPlanes; ++u)
+    ph[u] = k0 + u < nz ? phi.data[i + j * phi.sy + (int64_t)(k0 + u) * phi.sz] : 0.0;
+#pragma unroll
+  for (int u = 0; u < kRhoPlanes; ++u) {
+    const int k = k0 + u;
+    if (k >= nz) break;
+    const long long pb = __double_as_longlong(ph[u]);
+    const long long mag = pb & 0x7fffffffffffffffll;
+    double* out = rho + ((size_t)k * ny + j) * nx + i;
+    if (mag > eps_out_bits && mag <= 0x7ff0000000000000ll) {
+      *out = pb < 0 ? bulk_neg : bulk_pos;
+      continue;
+    }
+    double h;
+    const double x = ph[u] / eps;
+    if (x > 1.0 - 1e-12) h = 1.0;
+    else if (x < -1.0 + 1e-12) h = 0.0;
+    else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
+    h = fmax(fmin(h, 1.0), 0.0);
+    *out = rho_pos * h + rho_neg * (1.0 - h);
   }
-  double h;
-  const double x = ph / eps;
-  if (x > 1.0 - 1e-12) h = 1.0;
-  else if (x < -1.0 + 1e-12) h = 0.0;
-  else h = 0.5 * (1.0 + x + sin(pi * x) / pi);
-  h = fmax(fmin(h, 1.0), 0.0);
-  *out = rho_pos * h + rho_neg * (1.0 - h);
 }
 
 __global__ void __launch_bounds__(256) k_copy_in(int nx, int ny, int nz, Strided src, double* dst) {
@@ -438,7 +449,8 @@ void launch_rho_from_phi(cudaStream_t s, int nx, int ny, int nz, Strided phi, do
   std::memcpy(&eps_bits, &eps_out, sizeof eps_bits);
   const double bulk_pos = rho_pos * 1.0 + rho_neg * (1.0 - 1.0);
   const double bulk_neg = rho_pos * 0.0 + rho_neg * (1.0 - 0.0);
-  k_rho_from_phi<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
+  const dim3 g(cdiv((size_t)nx, 32), cdiv((size_t)ny, 8), cdiv((size_t)nz, kRhoPlanes));
+  k_rho_from_phi<<<g, dim3(32, 8), 0, s>>>(
       nx, ny, nz, phi, eps, eps_bits, rho_pos, rho_neg, bulk_pos, bulk_neg, rho);
 }
 

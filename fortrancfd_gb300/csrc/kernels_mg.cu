@@ -267,8 +267,10 @@ __global__ void __launch_bounds__(kMaxCoarse) k_coarse_gram(int n, const double*
 // fine face coefficients covering each coarse face: coe_c = mean(coe_f)/f^2
 // along a coarsened axis (beta_c = mean beta_f).  The reference multigrid is
 // constant-coefficient and has no counterpart.
+// With c32: the coefficients rounded to float into c32[0..2] as well.
 __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx, double* cy,
-                                                 double* cz, int cnx, int cny, int cnz) {
+                                                 double* cz, int cnx, int cny, int cnz,
+                                                 Float3Out c32) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
   const int J = blockIdx.y * blockDim.y + threadIdx.y;
   const int K = blockIdx.z;
@@ -305,13 +307,17 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
       double* cc = a == 0 ? cx : (a == 1 ? cy : cz);
       const int idx = a == 0 ? I : (a == 1 ? J : K);
       const int fa = a == 0 ? F.fx : (a == 1 ? F.fy : F.fz);
-      if (idx == 0 || fa == 1) { cc[cq] = 0.0; continue; }
-      double acc = 0.0;
+      double v = 0.0;
+      if (!(idx == 0 || fa == 1)) {
+        double acc = 0.0;
 #pragma unroll
-      for (int m = 0; m < 4; ++m)
-        if (use[a][m]) acc += t[a][m];
-      acc *= tang * fa;
-      cc[cq] = acc * (fa == 2 ? 0.25 : 1.0);
+        for (int m = 0; m < 4; ++m)
+          if (use[a][m]) acc += t[a][m];
+        acc *= tang * fa;
+        v = acc * (fa == 2 ? 0.25 : 1.0);
+      }
+      cc[cq] = v;
+      if (c32.p[a]) c32.p[a][cq] = (float)v;
     }
     return;
   }
@@ -322,16 +328,20 @@ __global__ void __launch_bounds__(256) k_coarsen(LevelView<double> F, double* cx
     double* cc = a == 0 ? cx : (a == 1 ? cy : cz);
     const int idx = a == 0 ? I : (a == 1 ? J : K);
     const int fa = a == 0 ? F.fx : (a == 1 ? F.fy : F.fz);
-    if (idx == 0 || fa == 1) { cc[cq] = 0.0; continue; }
-    double acc = 0.0;
-    for (int dz = 0; dz < F.fz; ++dz)
-      for (int dy = 0; dy < F.fy; ++dy)
-        for (int dx = 0; dx < F.fx; ++dx) {
-          if ((a == 0 && dx) || (a == 1 && dy) || (a == 2 && dz)) continue;
-          acc += fc[q0 + dz * sz + dy * sy + dx];
-        }
-    acc *= tang * fa;
-    cc[cq] = acc / (double)(fa * fa);
+    double v = 0.0;
+    if (!(idx == 0 || fa == 1)) {
+      double acc = 0.0;
+      for (int dz = 0; dz < F.fz; ++dz)
+        for (int dy = 0; dy < F.fy; ++dy)
+          for (int dx = 0; dx < F.fx; ++dx) {
+            if ((a == 0 && dx) || (a == 1 && dy) || (a == 2 && dz)) continue;
+            acc += fc[q0 + dz * sz + dy * sy + dx];
+          }
+      acc *= tang * fa;
+      v = acc / (double)(fa * fa);
+    }
+    cc[cq] = v;
+    if (c32.p[a]) c32.p[a][cq] = (float)v;
   }
 }
 
@@ -456,10 +466,10 @@ void launch_coarse_invert(cudaStream_t s, const LevelView<double>& C, double* mi
 }
 
 void launch_coarsen(cudaStream_t s, const LevelView<double>& F, double* cx, double* cy,
-                    double* cz, int cnx, int cny, int cnz) {
+                    double* cz, int cnx, int cny, int cnz, Float3Out c32) {
   const dim3 blk(32, 8, 1);
   const dim3 grd(cdiv((size_t)cnx, 32), cdiv((size_t)cny, 8), (unsigned)cnz);
-  k_coarsen<<<grd, blk, 0, s>>>(F, cx, cy, cz, cnx, cny, cnz);
+  k_coarsen<<<grd, blk, 0, s>>>(F, cx, cy, cz, cnx, cny, cnz, c32);
 }
 
 void launch_idiag(cudaStream_t s, const LevelView<double>& L, double* idiag) {
