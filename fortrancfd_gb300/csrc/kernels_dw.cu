@@ -282,21 +282,26 @@ __global__ void k_to_dw(const double* __restrict__ a, float2* __restrict__ out, 
   });
 }
 
-// slot <- sum of the double values of p (for the final mean projection)
+// slot <- sum of the values of p (for the final mean projection): each
+// thread sums its elements in double-word on the FP32 pipes (error about
+// 2u^2 of the partial sums, u = 2^-24), the threads' sums are added in FP64
 __global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict__ p, size_t n,
                                                         ReduceScratch R, int slot) {
-  double acc[1] = {0.0};
-  stride4(n, [&](size_t q) { return dw_ldg(p + q); },
-          [&](size_t, dw v) { acc[0] += dw_to_double_int(v); });
+  dw a{0.f, 0.f};
+  stride4(n, [&](size_t q) { return dw_ldg(p + q); }, [&](size_t, dw v) { a = dw_add(a, v); });
+  double acc[1] = {dw_to_double_int(a)};
   grid_sum_finish<1>(acc, R, slot);
 }
 
-// out = double(p) - result[slot]/n
+// out = p - result[slot]/n: the difference in double-word (error about
+// 2u^2 (|p| + |m|)), then converted exactly and summed in FP64 (one FP64
+// addition per element)
 __global__ void k_dw_out(const float2* __restrict__ p, double* __restrict__ out, size_t n,
                          ReduceScratch R, int slot) {
   const double m = R.result[slot] / (double)n;
+  const dw mneg = dw_neg(dw_from_double(m));
   stride4(n, [&](size_t q) { return dw_ldg(p + q); },
-          [&](size_t q, dw v) { out[q] = dw_to_double_int(v) - m; });
+          [&](size_t q, dw v) { out[q] = dw_to_double_int(dw_add(v, mneg)); });
 }
 
 // out += double(d): the correction of a warm-started solve added to its start
