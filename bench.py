@@ -933,6 +933,8 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    step_spread = {}
+
     def timed(solver, steps, warmup, b, p, sample_clocks=False):
         def step():
             p.zero_()
@@ -950,16 +952,23 @@ def run_ours(args):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            # an event after every step as well: the spread of the steps
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
             launches0 = solver.kernel_launches
             t0 = time.monotonic()
             e0.record(stream)
-            for _ in range(steps):
+            for i in range(steps):
                 st = step()
+                ev[i].record(stream)
             e1.record(stream)
             torch.cuda.synchronize()
             t1 = time.monotonic()
             barrier()
         ms = e0.elapsed_time(e1)
+        per = sorted([e0.elapsed_time(ev[0])] +
+                     [ev[i - 1].elapsed_time(ev[i]) for i in range(1, steps)])
+        if sample_clocks:  # the headline solve
+            step_spread.update(min=per[0], median=per[len(per) // 2], max=per[-1])
         launches = solver.kernel_launches - launches0
         if sample_clocks:
             sampler.window(t0, t1)
@@ -1119,7 +1128,8 @@ def run_ours(args):
                            "parallelism": f"replicas x{world}"},
                 "parity": parity,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "adjoint": adj, "multi_bubble": multi,
+                "gpu_launches": launches, "step_ms_spread": step_spread,
+                "adjoint": adj, "multi_bubble": multi,
                 "rollout": roll, "levelset": lset, "momentum": mom, "timestep": tstep}
         if prof:
             line["profile_ms"] = {k: round(v[0], 4) for k, v in prof.items()}

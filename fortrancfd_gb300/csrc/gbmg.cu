@@ -411,7 +411,7 @@ int allocate(gbmg_handle* h) {
   GB_TRY(dmalloc(h, &h->red.result, kRedSlots));
   GB_CUDA(h, cudaMemsetAsync(h->red.counter, 0, sizeof(unsigned int), h->stream));
   GB_CUDA(h, cudaMemsetAsync(h->red.result, 0, kRedSlots * sizeof(double), h->stream));
-  GB_CUDA(h, cudaMallocHost((void**)&h->host_res, kRedSlots * sizeof(double)));
+  GB_CUDA(h, cudaMallocHost((void**)&h->host_res, (kRedSlots + 1) * sizeof(double)));
   GB_TRY(dmalloc(h, &h->ctl, 1));
   GB_CUDA(h, cudaMallocHost((void**)&h->ctl_host, sizeof(CycleCtl)));
   GB_TRY(dmalloc(h, &h->derr, 4));
@@ -526,10 +526,24 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   return build_hierarchy(h);
 }
 
+// The result slots and the device error flag to the host, one wait.
+int read_results(gbmg_handle* h) {
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res + kRedSlots, h->derr, sizeof(int),
+                             cudaMemcpyDeviceToHost, h->stream));
+  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->flags_at = h->launches;
+  return GBMG_OK;
+}
+
 // b -> h->b with the mean removed (when asked); result[kSlotSumB+1] = |b|^2.
 // h->b holds the right-hand side: project its mean out (when asked), make the
 // double-word copy of the mixed solve, and return |b|.
-int finish_rhs(gbmg_handle* h, double* bnorm) {
+// check_p: also test whether the initial p is zero (the stationary mixed
+// loop's start), after p_ready, in the same wait as |b|.
+int finish_rhs(gbmg_handle* h, double* bnorm, bool check_p = false,
+               cudaEvent_t p_ready = nullptr) {
   const bool rm = h->prm.remove_rhs_mean != 0;
   if (rm) LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
   // one pass: the shift, |b|^2, the double-word copy and (stationary mixed
@@ -540,23 +554,25 @@ int finish_rhs(gbmg_handle* h, double* bnorm) {
          launch_rhs_prep(h->stream, h->b, h->n0, h->red, rm ? kSlotSumB : -1, kSlotSumB + 1,
                          h->mixed ? h->bw : nullptr, r32, f.nx, f.ny, f.split ? f.hstride : 0));
   GB_TRY(check_launch(h, "rhs"));
-  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
-                             cudaMemcpyDeviceToHost, h->stream));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  const bool test_p = check_p && h->mixed && h->prm.krylov == 0;
+  if (test_p) {
+    if (p_ready) GB_CUDA(h, cudaStreamWaitEvent(h->stream, p_ready, 0));
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_nonzero(h->stream, h->p, h->n0, h->red.result + kSlotSum + 1));
+    GB_TRY(check_launch(h, "initial guess"));
+  }
+  GB_TRY(read_results(h));
   *bnorm = std::sqrt(h->host_res[kSlotSumB + 1]);
+  h->p_nonzero = -1;
+  if (test_p) {
+    unsigned long long nz = 0ull;
+    std::memcpy(&nz, &h->host_res[kSlotSum + 1], sizeof(nz));
+    h->p_nonzero = nz != 0ull ? 1 : 0;
+  }
   return GBMG_OK;
 }
 
-int prepare_rhs(gbmg_handle* h, const gbmg_field& b, int mem, double* bnorm) {
-  const gbmg_grid& g = h->grid;
-  GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
-  return finish_rhs(h, bnorm);
-}
-
 int read_result(gbmg_handle* h, int slot, double* v) {
-  GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
-                             cudaMemcpyDeviceToHost, h->stream));
-  GB_CUDA(h, cudaStreamSynchronize(h->stream));
+  GB_TRY(read_results(h));
   *v = h->host_res[slot];
   return GBMG_OK;
 }
@@ -759,9 +775,12 @@ int run_loop(gbmg_handle* h, int kind, CycleCtl* c, bool* used) {
   GB_CUDA(h, cudaMemcpyAsync(h->ctl_host, h->ctl, sizeof(CycleCtl), cudaMemcpyDeviceToHost, s));
   GB_CUDA(h, cudaMemcpyAsync(h->host_res, h->red.result, kRedSlots * sizeof(double),
                              cudaMemcpyDeviceToHost, s));
+  GB_CUDA(h, cudaMemcpyAsync(h->host_res + kRedSlots, h->derr, sizeof(int),
+                             cudaMemcpyDeviceToHost, s));
   GB_CUDA(h, cudaStreamSynchronize(s));
   *c = *h->ctl_host;
   h->launches += h->loop_kernels[kind][par] * (int64_t)(c->iters - it0);
+  h->flags_at = h->launches;
   *used = true;
   return GBMG_OK;
 }
@@ -950,13 +969,19 @@ int start_mixed(gbmg_handle* h, bool* shifted) {
   const cudaStream_t s = h->stream;
   Level& f = h->lv[0];
   const size_t n = h->n0;
-  LAUNCH(h, GBMG_PROF_VECTOR, launch_nonzero(s, h->p, n, h->red.result + kSlotSum + 1));
-  GB_TRY(check_launch(h, "initial guess"));
-  double pp = 0.0;
-  GB_TRY(read_result(h, kSlotSum + 1, &pp));
-  unsigned long long nz = 0ull;
-  std::memcpy(&nz, &pp, sizeof(nz));
-  *shifted = nz != 0ull;
+  if (h->p_nonzero >= 0) {
+    // tested with the right-hand side
+    *shifted = h->p_nonzero != 0;
+    h->p_nonzero = -1;
+  } else {
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_nonzero(s, h->p, n, h->red.result + kSlotSum + 1));
+    GB_TRY(check_launch(h, "initial guess"));
+    double pp = 0.0;
+    GB_TRY(read_result(h, kSlotSum + 1, &pp));
+    unsigned long long nz = 0ull;
+    std::memcpy(&nz, &pp, sizeof(nz));
+    *shifted = nz != 0ull;
+  }
   if (*shifted) {
     // the correction starts at d = 0, so its first residual is r0 itself:
     // the loop's right-hand side in double-word and the FP32 cycle's input
@@ -1165,9 +1190,14 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     if (rel < tol) status = GBMG_OK;
   }
   {
+    // the flag came back with the last results when no kernel ran since
     int flags = 0;
-    GB_CUDA(h, cudaMemcpyAsync(&flags, h->derr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GB_CUDA(h, cudaStreamSynchronize(s));
+    if (h->flags_at == h->launches) {
+      std::memcpy(&flags, h->host_res + kRedSlots, sizeof(int));
+    } else {
+      GB_CUDA(h, cudaMemcpyAsync(&flags, h->derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GB_CUDA(h, cudaStreamSynchronize(s));
+    }
     if (flags) {
       h->err = "a bulk-copy wait timed out inside a kernel of the cycle";
       cudaMemsetAsync(h->derr, 0, sizeof(int), s);
@@ -1459,15 +1489,16 @@ int gbmg_solve(gbmg_handle* h, gbmg_field b, gbmg_field p, double tol, int mem,
     GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p, h->cstream));
     GB_CUDA(h, cudaEventRecord(h->cev[0], h->cstream));
     GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[2], 0));
-    const int rc = finish_rhs(h, &bnorm);
+    const int rc = finish_rhs(h, &bnorm, true, h->cev[0]);
     if (rc != GBMG_OK) {
       cudaStreamSynchronize(h->cstream);  // the caller's p may be freed on return
       return rc;
     }
     GB_CUDA(h, cudaStreamWaitEvent(h->stream, h->cev[0], 0));
   } else {
-    GB_TRY(prepare_rhs(h, b, mem, &bnorm));
+    GB_TRY(upload(h, b, g.nx, g.ny, g.nz, mem, h->b));
     GB_TRY(upload(h, p, g.nx, g.ny, g.nz, mem, h->p));
+    GB_TRY(finish_rhs(h, &bnorm, true));
   }
   h->dl_field = host ? &p : nullptr;
   h->dl_started = false;

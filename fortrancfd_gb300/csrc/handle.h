@@ -68,7 +68,9 @@ struct gbmg_handle {
   float *minv32 = nullptr, *adense32 = nullptr;
   // reductions
   gbmg::ReduceScratch red{};
-  double* host_res = nullptr;  // pinned mirror of red.result
+  double* host_res = nullptr;  // pinned mirror of red.result, then a copy of derr[0]
+  int64_t flags_at = -1;       // launch count when derr[0] was last copied with the results
+  int p_nonzero = -1;          // the initial p tested with the right-hand side (-1: not tested)
   // double-word finest level of the mixed solve: p (ping-pong), b, coefficients
   float2* pw[2] = {nullptr, nullptr};
   float2* bw = nullptr;
