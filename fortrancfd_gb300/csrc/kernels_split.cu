@@ -14,8 +14,10 @@
 // All six neighbours of a cell are of the other colour, at half-index offsets
 // -1/0 or 0/+1 (x, by the cell's parity), -+nx/2 (y) and -+nx*ny/2 (z), so a
 // colour launch reads the other half of p and rho and its own half of b and
-// rho and writes its own half of p, all coalesced: 20 bytes per cell per
-// sweep.  The kernels here do the arithmetic of the natural-layout kernels
+// rho and writes its own half of p, all coalesced.  A sweep's algorithmic
+// traffic is 16 bytes per cell (p read and written, b and rho read once); the
+// two colour launches read rho twice, 20 bytes per cell, unless the second
+// finds the first's rho still in L2.  The kernels here do the arithmetic of the natural-layout kernels
 // (k_smooth, k_restrict, k_prolong with the density form) in the same order,
 // so both layouts give bit-identical results.
 #include <algorithm>
