@@ -203,35 +203,29 @@ __global__ void __launch_bounds__(256) k_coarse_factor(LevelView<double> C, doub
     M[e] = sn - a;
   }
   __syncthreads();
-  // Right-looking Cholesky, one barrier per step: the column L_ij = M_ij /
-  // L_jj goes straight to work (M keeps column j unscaled while the trailing
-  // update reads it, each L_ij formed as the same rounded product), and
-  // thread 0, which updates the next diagonal element first, takes its
-  // square root and reciprocal before the barrier.  The trailing update is
-  // walked as a 16 x 16 thread grid over (row, column) without divisions.
+  // right-looking Cholesky, lower triangle in place; the trailing update is
+  // walked as a 16 x 16 thread grid over (row, column) without divisions
   double* rdiag = work + (size_t)n * n;  // 1/L_jj
-  __shared__ double rd_sh[2];
+  __shared__ double rd_sh;
   const int tx = t % 16, ty = t / 16;
-  const auto pivot = [&](int j) {  // thread 0
-    const double d = sqrt(M[j * n + j]);
-    work[j * n + j] = d;
-    rd_sh[j & 1] = 1.0 / d;
-    rdiag[j] = rd_sh[j & 1];
-  };
-  if (t == 0 && n > 0) pivot(0);
-  __syncthreads();
   for (int j = 0; j < n; ++j) {
-    const double rjj = rd_sh[j & 1];
-    for (int i = j + 1 + t; i < n; i += nt) work[i * n + j] = M[i * n + j] * rjj;
+    if (t == 0) {
+      const double d = sqrt(M[j * n + j]);
+      M[j * n + j] = d;
+      rd_sh = 1.0 / d;
+      rdiag[j] = rd_sh;
+    }
+    __syncthreads();
+    const double rjj = rd_sh;
+    for (int i = j + 1 + t; i < n; i += nt) M[i * n + j] *= rjj;
+    __syncthreads();
     for (int i = j + 1 + ty; i < n; i += 16) {
-      const double lij = M[i * n + j] * rjj;
-      for (int k = j + 1 + tx; k <= i; k += 16) {
-        M[i * n + k] -= lij * (M[k * n + j] * rjj);
-        if (t == 0 && i == j + 1 && k == j + 1) pivot(j + 1);
-      }
+      const double lij = M[i * n + j];
+      for (int k = j + 1 + tx; k <= i; k += 16) M[i * n + k] -= lij * M[k * n + j];
     }
     __syncthreads();
   }
+  for (int e = t; e < n * n; e += nt) work[e] = M[e];
 }
 
 // W = L^{-1}, column c in block c (one warp): row by row forward
