@@ -66,6 +66,25 @@ __device__ __forceinline__ dw dw_from_double(double x) {
 
 __device__ __forceinline__ double dw_to_double(dw a) { return (double)a.hi + (double)a.lo; }
 
+// The conversion-instruction paths of the two integer conversions below, for
+// their rare inputs, as calls: an inlined fallback would be if-converted and
+// its FP64-pipe instructions issued for every element.
+static __device__ __noinline__ dw dw_from_double_rare(double x) { return dw_from_double(x); }
+static __device__ __noinline__ double float_to_double_rare(float f) { return (double)f; }
+
+// float(r) rounded to nearest even, for |r| <= 2^28, without a conversion
+// instruction (GB300 runs those on its FP64 pipe): r = a 2^14 + c with
+// |a| <= 2^14 and 0 <= c < 2^14; each part is exact as a float by the
+// 1.5 * 2^23 bit-pattern offset, and a 2^14 + c is rounded once by the
+// fused multiply-add.
+__device__ __forceinline__ float int29_to_float(int r) {
+  const int a = r >> 14;
+  const int c = r & 0x3fff;
+  const float fa = __int_as_float(0x4B400000 + a) - 12582912.0f;
+  const float fc = __int_as_float(0x4B400000 + c) - 12582912.0f;
+  return __fmaf_rn(fa, 16384.0f, fc);
+}
+
 // The same conversions with integer operations in place of the FP64
 // conversion instructions, which GB300 runs at its FP64 rate (1/57 of FP32):
 // results are bit-identical to dw_from_double / dw_to_double.
@@ -87,13 +106,13 @@ __device__ __forceinline__ dw dw_from_double_int(double x) {
   top += (rb > (1ll << 28) || (rb == (1ll << 28) && (top & 1))) ? 1 : 0;
   const int carry = top == (1ll << 24) ? 1 : 0;
   const int fe = e - 896 + carry;
-  if (e < 949 || fe > 254) return dw_from_double(x);
+  if (e < 949 || fe > 254) return dw_from_double_rare(x);
   const unsigned hb =
       (s << 31) | ((unsigned)fe << 23) | ((unsigned)(carry ? (top >> 1) : top) & 0x7fffffu);
   const int r = (int)((long long)m - (top << 29));
   float lo = 0.f;
   if (r != 0) {
-    lo = __int_as_float(__float_as_int(__int2float_rn(r)) + (e - 1075) * (1 << 23));
+    lo = __int_as_float(__float_as_int(int29_to_float(r)) + (e - 1075) * (1 << 23));
     if (s) lo = -lo;
   }
   return dw{__uint_as_float(hb), lo};
@@ -106,7 +125,7 @@ __device__ __forceinline__ double float_to_double_int(float f) {
   const unsigned e = (u >> 23) & 0xffu;
   const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
   if ((u << 1) == 0u) return __longlong_as_double((long long)sgn);
-  if (e == 0u || e == 255u) return (double)f;
+  if (e == 0u || e == 255u) return float_to_double_rare(f);
   return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
                                           ((unsigned long long)(u & 0x7fffffu) << 29)));
 }

@@ -545,7 +545,7 @@ int read_results(gbmg_handle* h) {
 int finish_rhs(gbmg_handle* h, double* bnorm, bool check_p = false,
                cudaEvent_t p_ready = nullptr) {
   const bool rm = h->prm.remove_rhs_mean != 0;
-  if (rm) LAUNCH(h, GBMG_PROF_VECTOR, launch_sum(h->stream, h->b, h->n0, h->red, kSlotSumB));
+  if (rm) LAUNCH(h, GBMG_PROF_VECTOR, launch_sum_dw(h->stream, h->b, h->n0, h->red, kSlotSumB));
   // one pass: the shift, |b|^2, the double-word copy and (stationary mixed
   // loop) the first FP32 residual of a solve from p = 0
   const Level& f = h->lv[0];

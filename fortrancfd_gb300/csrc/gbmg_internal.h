@@ -309,6 +309,8 @@ void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, i
                        float2* pout, float* r32, const ReduceScratch& R, int slot, int* err,
                        size_t hstride);
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n);
+// result[slot] = sum of x, summed in double-word per thread (FP32 pipes)
+void launch_sum_dw(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot);
 // b -= result[mslot]/n (mslot < 0: unchanged), sum b^2 -> result[slot2], and
 // when given the double-word copy bw and float(b) into r32 (colour-split when
 // hstride != 0): one pass

@@ -293,6 +293,18 @@ __global__ void __launch_bounds__(kRedThreads) k_dw_sum(const float2* __restrict
   grid_sum_finish<1>(acc, R, slot);
 }
 
+// slot <- sum of x (FP64 values): each thread sums its elements in
+// double-word on the FP32 pipes (each value to 48 bits, the sum to about
+// 2u^2 of the partial sums), the threads' sums are added in FP64
+__global__ void __launch_bounds__(kRedThreads) k_sum_dw(const double* __restrict__ x, size_t n,
+                                                        ReduceScratch R, int slot) {
+  dw a{0.f, 0.f};
+  stride4(n, [&](size_t q) { return x[q]; },
+          [&](size_t, double v) { a = dw_add(a, dw_from_double_int(v)); });
+  double acc[1] = {dw_to_double_int(a)};
+  grid_sum_finish<1>(acc, R, slot);
+}
+
 // out = p - result[slot]/n: the difference in double-word (error about
 // 2u^2 (|p| + |m|)), then converted exactly and summed in FP64 (one FP64
 // addition per element)
@@ -315,15 +327,37 @@ __global__ void k_dw_accumulate(const float2* __restrict__ d, double* __restrict
 // order of k_shift_by_mean / k_sum, so the same bits), and, when given, the
 // double-word copy bw and b rounded to float into r32 (the mixed solve's
 // first residual for p = 0), colour-split when hstride != 0.
-template <typename I>
-__device__ __forceinline__ size_t split_index(size_t q, int nx, int ny, size_t hstride) {
-  const I qq = (I)q;
-  const I r = qq / (I)nx;
-  const int i = (int)(qq - r * (I)nx);
-  const I k = r / (I)ny;
-  const int j = (int)(r - k * (I)ny);
-  return (size_t)((i + j + (int)(k & 1)) & 1) * hstride + (q >> 1);
-}
+// The colour (i + j + k) & 1 of the cells a grid-stride loop visits, kept
+// up to date by additions (integer division runs its conversions on GB300's
+// FP64 pipe): set at the thread's first cell, advanced by the stride.
+struct ColourWalk {
+  int i, j, kp;     // x, y and the parity of z of the current cell
+  int si, sj, skp;  // the stride split the same way
+  int nx, ny;
+  __device__ ColourWalk(size_t q, size_t s, int nx_, int ny_) : nx(nx_), ny(ny_) {
+    const size_t row = q / (size_t)nx, srow = s / (size_t)nx;
+    i = (int)(q - row * nx);
+    j = (int)(row % (size_t)ny);
+    kp = (int)((row / (size_t)ny) & 1);
+    si = (int)(s - srow * nx);
+    sj = (int)(srow % (size_t)ny);
+    skp = (int)((srow / (size_t)ny) & 1);
+  }
+  __device__ __forceinline__ int colour() const { return (i + j + kp) & 1; }
+  __device__ __forceinline__ void advance() {
+    i += si;
+    int carry = i >= nx;
+    if (carry) i -= nx;
+    j += sj + carry;
+    carry = j >= ny;
+    if (carry) j -= ny;
+    kp = (kp + skp + carry) & 1;
+  }
+};
+
+// (a call, so that the FP64 fused multiply-add is not if-converted and
+// issued for every element)
+__device__ __noinline__ double add_square_rare(double acc, double a) { return acc + a * a; }
 
 __global__ void __launch_bounds__(kRedThreads) k_rhs_prep(double* __restrict__ b, size_t n,
                                                           ReduceScratch R, int mslot, int slot2,
@@ -331,24 +365,37 @@ __global__ void __launch_bounds__(kRedThreads) k_rhs_prep(double* __restrict__ b
                                                           float* __restrict__ r32, int nx, int ny,
                                                           size_t hstride) {
   const double m = mslot >= 0 ? R.result[mslot] / (double)n : 0.0;
-  const bool small = n < (size_t(1) << 32);
-  double acc[1] = {0.0};
+  const size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ColourWalk cw(q0, (size_t)gridDim.x * blockDim.x, nx, ny);
+  // |b - m|^2 (it only sets the scale of the relative tolerance) summed per
+  // thread in double-word on the FP32 pipes: a^2 = hi^2 + 2 hi lo to about
+  // 2^-47; the shift itself is the one FP64 operation per element
+  // (values outside 2^-60 <= |a| <= 2^60, whose squares would leave the
+  // float range, go to an FP64 sum instead)
+  dw sq{0.f, 0.f};
+  double sq64 = 0.0;
+  // stride4 calls use() for q0, q0 + s, q0 + 2s, ... in this order
   stride4(n, [&](size_t q) { return b[q]; }, [&](size_t q, double x) {
     const double a = mslot >= 0 ? x - m : x;
     if (mslot >= 0) b[q] = a;
-    acc[0] += a * a;
+    const dw v = dw_from_double_int(a);
+    const float ah = fabsf(v.hi);
+    if (ah == 0.f || (ah >= 0x1p-60f && ah <= 0x1p60f)) {
+      const float p = v.hi * v.hi;
+      float e = __fmaf_rn(v.hi, v.hi, -p);
+      e = __fmaf_rn(2.f * v.hi, v.lo, e);
+      sq = dw_add(sq, dw{p, e});
+    } else {
+      sq64 = add_square_rare(sq64, a);
+    }
     if (bw) {
-      const dw v = dw_from_double_int(a);
       bw[q] = make_float2(v.hi, v.lo);
       // v.hi is a rounded to nearest float
-      if (r32) {
-        const size_t o = hstride == 0 ? q
-                         : small    ? split_index<unsigned>(q, nx, ny, hstride)
-                                    : split_index<size_t>(q, nx, ny, hstride);
-        r32[o] = v.hi;
-      }
+      if (r32) r32[hstride == 0 ? q : (size_t)cw.colour() * hstride + (q >> 1)] = v.hi;
+      cw.advance();
     }
   });
+  double acc[1] = {dw_to_double_int(sq) + sq64};
   grid_sum_finish<1>(acc, R, slot2);
 }
 
@@ -439,6 +486,11 @@ void launch_defect_tma(cudaStream_t s, const DefectMaps& maps, int nx, int ny, i
 
 void launch_to_dw(cudaStream_t s, const double* a, float2* out, size_t n) {
   k_to_dw<<<stride_blocks(n) * 2, kRedThreads, 0, s>>>(a, out, n);
+}
+
+void launch_sum_dw(cudaStream_t s, const double* x, size_t n, const ReduceScratch& R, int slot) {
+  const unsigned b = std::min<unsigned>(stride_blocks(n), (unsigned)R.max_blocks);
+  k_sum_dw<<<b, kRedThreads, 0, s>>>(x, n, R, slot);
 }
 
 void launch_dw_sum(cudaStream_t s, const float2* p, size_t n, const ReduceScratch& R, int slot) {
