@@ -511,16 +511,13 @@ int set_rho_device(gbmg_handle* h, const double* bulk_rho) {
   float* c32[3] = {f.cx32, f.cy32, f.cz32};
   float2* cw[3] = {h->cxw, h->cyw, h->czw};
   const bool want32 = h->mixed && !f.rho32;
+  // (the mixed cycle's FP32 density comes out of the same pass)
   LAUNCH(h, GBMG_PROF_SETUP,
          launch_face_coef(h->stream, g.nx, g.ny, g.nz, g.dx * g.dx, g.dy * g.dy, g.dz * g.dz,
                           h->rho, f.cx, f.cy, f.cz, want32 ? c32 : nullptr,
-                          h->mixed ? cw : nullptr, bulk_rho));
+                          h->mixed ? cw : nullptr, bulk_rho, h->mixed ? h->rho32 : nullptr,
+                          f.split ? f.hstride : 0));
   h->fine_copies = h->mixed;
-  if (h->mixed && f.split)
-    LAUNCH(h, GBMG_PROF_SETUP,
-           launch_to_split(h->stream, h->rho, h->rho32, f.nx, f.ny, f.nz, f.hstride));
-  else if (h->mixed)
-    LAUNCH(h, GBMG_PROF_SETUP, launch_double_to_float(h->stream, h->rho, h->rho32, h->n0));
   GB_TRY(check_launch(h, "face_coef"));
   h->rho_ready = true;
   return build_hierarchy(h);

@@ -222,7 +222,8 @@ constexpr size_t kSplitPadMax = 65536;
 // null; faces between two bulk cells use host-computed values.
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
                       const double* rho, double* cx, double* cy, double* cz, float* const* c32,
-                      float2* const* cw, const double* bulk_rho);
+                      float2* const* cw, const double* bulk_rho, float* rho32 = nullptr,
+                      size_t hstride = 0);
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
                        double dx, double dy, double dz, double dt, double* b);
 void launch_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho, const double* p,

@@ -145,13 +145,18 @@ __device__ __forceinline__ void face_value(const BulkFaces& B, int a, double ra,
 __global__ void __launch_bounds__(256) k_face_coef(int nx, int ny, int nz, double3 h2, double3 ih2,
                                                    int pow2, BulkFaces B,
                                                    const double* __restrict__ rho, FaceOut ox,
-                                                   FaceOut oy, FaceOut oz) {
+                                                   FaceOut oy, FaceOut oz, float* rho32,
+                                                   size_t hstride) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (i >= nx || j >= ny) return;
   const size_t q = ((size_t)k * ny + j) * nx + i;
   const double r = rho[q];
+  // the FP32 density of the mixed cycle (rounded to nearest; colour-split
+  // when hstride != 0)
+  if (rho32) rho32[hstride ? (size_t)((i + j + k) & 1) * hstride + (q >> 1) : q] =
+      dw_from_double_int(r).hi;
   if (i > 0) face_value(B, 0, r, rho[q - 1], h2.x, ih2.x, pow2 & 1, ox, q);
   else face_store(ox, q, 0.0);
   if (j > 0) face_value(B, 1, r, rho[q - nx], h2.y, ih2.y, pow2 & 2, oy, q);
@@ -470,7 +475,7 @@ static bool is_pow2(double v) {
 
 void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double dy2, double dz2,
                       const double* rho, double* cx, double* cy, double* cz, float* const* c32,
-                      float2* const* cw, const double* bulk_rho) {
+                      float2* const* cw, const double* bulk_rho, float* rho32, size_t hstride) {
   const int pow2 = (is_pow2(dx2) ? 1 : 0) | (is_pow2(dy2) ? 2 : 0) | (is_pow2(dz2) ? 4 : 0);
   const double h2[3] = {dx2, dy2, dz2};
   BulkFaces B;
@@ -494,7 +499,7 @@ void launch_face_coef(cudaStream_t s, int nx, int ny, int nz, double dx2, double
   const FaceOut oz{cz, c32 ? c32[2] : nullptr, cw ? cw[2] : nullptr};
   k_face_coef<<<grid3(nx, ny, nz), dim3(32, 8), 0, s>>>(
       nx, ny, nz, make_double3(dx2, dy2, dz2), make_double3(1.0 / dx2, 1.0 / dy2, 1.0 / dz2), pow2,
-      B, rho, ox, oy, oz);
+      B, rho, ox, oy, oz, rho32, hstride);
 }
 
 void launch_divergence(cudaStream_t s, int nx, int ny, int nz, Strided u, Strided v, Strided w,
