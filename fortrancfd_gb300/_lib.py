@@ -56,14 +56,15 @@ class Params(C.Structure):
                 ("krylov", C.c_int32), ("use_graph", C.c_int32), ("remove_rhs_mean", C.c_int32),
                 ("certify", C.c_int32), ("device", C.c_int32), ("stream", C.c_void_p),
                 ("stop_rule", C.c_int32), ("zero_wall_faces", C.c_int32),
-                ("inner_cycles", C.c_int32)]
+                ("inner_cycles", C.c_int32), ("split_restarts", C.c_int32)]
 
 
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int32), ("cycles", C.c_int32), ("levels", C.c_int32),
                 ("coarse_n", C.c_int32), ("rel_residual", C.c_double),
                 ("rms_residual", C.c_double), ("res0", C.c_double), ("ms", C.c_double),
-                ("bytes", C.c_double), ("increment", C.c_double), ("device_loop", C.c_int32)]
+                ("bytes", C.c_double), ("increment", C.c_double), ("device_loop", C.c_int32),
+                ("restarts", C.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

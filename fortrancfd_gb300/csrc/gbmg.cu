@@ -758,7 +758,7 @@ int build_loop(gbmg_handle* h, int kind, int par) {
 // available and nothing ran.
 int run_loop(gbmg_handle* h, int kind, CycleCtl* c, bool* used) {
   *used = false;
-  if (h->loop_off || h->prm.use_graph != 1 || h->prof) return GBMG_OK;
+  if (h->loop_off || h->prm.use_graph != 1 || h->prof || h->stag_mode) return GBMG_OK;
   const int par = kind == kGraphMixed ? h->pcur : 0;
   if (!h->loop_graph[kind][par]) {
     GB_TRY(build_loop(h, kind, par));
@@ -1100,7 +1100,9 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
             if (status != GBMG_NOT_CONVERGED || stalled || cyc >= h->prm.max_cycles) break;
           }
         }
-        const int step = kind == kGraphMixed ? std::min(h->inner, h->prm.max_cycles - cyc) : 1;
+        const int inner = h->stag_mode ? 1 : h->inner;
+        const int step = kind == kGraphMixed ? std::min(inner, h->prm.max_cycles - cyc) : 1;
+        const double prev = rel;
         cyc += step;
         GB_TRY(run_iteration(h, kind, pcg && cyc == 1, step));
         if (kind == kGraphMixed) h->pcur ^= 1;
@@ -1111,6 +1113,22 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
         if (!std::isfinite(rel) || rel > 1e3 * std::max(1.0, st->res0)) {
           status = GBMG_DIVERGED;
           break;
+        }
+        if (h->stag_mode) {
+          // the split driver's test: a cycle that does not cut the residual
+          // by 1% (or raises it) stagnates
+          const double grow = rel / prev;
+          if (grow > 1.0 || std::fabs(grow - 1.0) < 0.01) {
+            if (h->stag_mode == 1) {
+              h->stagnated = true;
+              break;
+            }
+            if (rel < 1000.0 * tol) { status = GBMG_OK; break; }
+          } else if (rel < tol) {
+            status = GBMG_OK;
+            break;
+          }
+          continue;
         }
         if (by_inc) {
           double dp = 0.0;
@@ -1153,6 +1171,15 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
       h->dl_started = true;
     }
     if (!(kind == kGraphMixed && h->prm.certify)) break;
+    if (h->stagnated) {  // the caller restarts; report the FP64 residual
+      f.sol = h->p; f.src = h->b;
+      LAUNCH(h, GBMG_PROF_CERTIFY,
+             launch_residual_norm<double>(s, v64(f), (double*)nullptr, h->red, kSlotNorm));
+      GB_TRY(check_launch(h, "certify"));
+      GB_TRY(read_result(h, kSlotNorm, &r2));
+      rel = std::sqrt(r2) / scale;
+      break;
+    }
     if (by_inc) {
       // reported only: the increment decided
       f.sol = h->p; f.src = h->b;
@@ -1341,6 +1368,8 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
       (h->prm.stop_rule == GBMG_STOP_INCREMENT && h->prm.krylov != 0) ||
       (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1) || h->prm.use_graph < 0 ||
       h->prm.use_graph > 2 || h->prm.inner_cycles < 0 || h->prm.inner_cycles > 8 ||
+      h->prm.split_restarts < 0 || h->prm.split_restarts > 100 ||
+      (h->prm.split_restarts > 0 && h->prm.krylov != 0) ||
       (h->prm.inner_cycles > 1 && h->prm.stop_rule == GBMG_STOP_INCREMENT)) {
     delete h;
     return GBMG_INVALID_ARG;
@@ -1617,16 +1646,34 @@ int gbmg_project_split(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w,
   Strided su{dv[0], dfield[0].sy, dfield[0].sz}, sv{dv[1], dfield[1].sy, dfield[1].sz};
   Strided sw{has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0, has_w ? dfield[2].sz : 0};
   GB_TRY(zero_walls(h, dfield, has_w));
-  launch_psplit_rhs(s, g.nx, g.ny, g.nz, h->rho, su, sv, sw, h->aux[0], h->split_rho12, g.dx,
-                    g.dy, g.dz, dt, h->b);
-  h->launches += 1;
-  GB_TRY(check_launch(h, "split source"));
-  double bnorm = 0.0;
-  GB_TRY(finish_rhs(h, &bnorm));
-  GB_CUDA(h, cudaMemcpyAsync(h->p, h->aux[0], h->n0 * sizeof(double), cudaMemcpyDeviceToDevice,
-                             s));
-  const int status = solve_internal(h, tol, bnorm, st);
-  if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED) return status;
+  // The driver's restarts: a stagnating cycle ends the solve, p^ becomes
+  // 1.5 p - 0.5 p^ and the source is rebuilt from it
+  // ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90:29-44").
+  const int nres = h->prm.split_restarts;
+  int status = GBMG_OK, cycles = 0, restart = 0;
+  for (;; ++restart) {
+    launch_psplit_rhs(s, g.nx, g.ny, g.nz, h->rho, su, sv, sw, h->aux[0], h->split_rho12, g.dx,
+                      g.dy, g.dz, dt, h->b);
+    h->launches += 1;
+    GB_TRY(check_launch(h, "split source"));
+    double bnorm = 0.0;
+    GB_TRY(finish_rhs(h, &bnorm));
+    GB_CUDA(h, cudaMemcpyAsync(h->p, h->aux[0], h->n0 * sizeof(double),
+                               cudaMemcpyDeviceToDevice, s));
+    h->stag_mode = nres > 0 ? (restart < nres ? 1 : 2) : 0;
+    h->stagnated = false;
+    status = solve_internal(h, tol, bnorm, st);
+    h->stag_mode = 0;
+    cycles += st->cycles;
+    if (status != GBMG_OK && status != GBMG_NOT_CONVERGED && status != GBMG_DIVERGED)
+      return status;
+    if (!h->stagnated) break;
+    LAUNCH(h, GBMG_PROF_VECTOR, launch_guess_update(s, h->p, h->aux[0], h->n0, 1.5));
+    GB_TRY(check_launch(h, "split restart"));
+  }
+  h->stagnated = false;
+  st->cycles = cycles;
+  st->restarts = restart;
   launch_psplit_correct(s, g.nx, g.ny, g.nz, h->rho, h->p, h->aux[0], h->split_rho12, g.dx, g.dy,
                         g.dz, dt, dv[0], dfield[0].sy, dfield[0].sz, dv[1], dfield[1].sy,
                         dfield[1].sz, has_w ? dv[2] : nullptr, has_w ? dfield[2].sy : 0,

@@ -168,6 +168,8 @@ void launch_psplit_rhs(cudaStream_t s, int nx, int ny, int nz, const double* rho
                        Strided v, Strided w, const double* ph, double rho12, double dx, double dy,
                        double dz, double dt, double* src);
 // u_f -= dt ((1/rho_12) dp/h + (beta_f - 1/rho_12) dp^/h) (ppe_mg_correction)
+// ph = w p + (1 - w) ph
+void launch_guess_update(cudaStream_t s, const double* p, double* ph, size_t n, double w);
 void launch_psplit_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho,
                            const double* p, const double* ph, double rho12, double dx, double dy,
                            double dz, double dt, double* u, int64_t usy, int64_t usz, double* v,

@@ -77,6 +77,12 @@ struct gbmg_handle {
   float2 *cxw = nullptr, *cyw = nullptr, *czw = nullptr;
   int pcur = 0;  // which pw holds the current pressure
   int inner = 1;  // FP32 V-cycles per defect correction of the stationary mixed loop
+  // the split driver's stagnation test (set by gbmg_project_split): 0 off; 1 a
+  // cycle that cuts the residual by under 1% (or raises it) ends the loop
+  // (stagnated = true); 2 after the last restart: such a cycle ends it once
+  // the residual is under 1000 tol
+  int stag_mode = 0;
+  bool stagnated = false;
   int sub_lc = 0;         // first level run by the one-block bottom of the cycle (L = none)
   int* derr = nullptr;   // device error flags (bulk-copy wait timeouts)
   gbmg::DefectMaps* dmaps = nullptr;  // TMA maps of the defect kernel: [p buffer][e: none,

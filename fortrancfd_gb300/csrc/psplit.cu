@@ -16,6 +16,8 @@
 #include <cmath>
 
 #include "dword.cuh"
+#include <algorithm>
+
 #include "gbmg_internal.h"
 
 namespace gbmg {
@@ -166,6 +168,16 @@ int pow2_mask(double dx, double dy, double dz) {
 
 dim3 grid3(int nx, int ny, int nz) { return dim3(cdiv((size_t)nx, 32), cdiv((size_t)ny, 8), (unsigned)nz); }
 
+// ph = w p + (1 - w) ph, the driver's new p^ after a stagnating cycle
+// ("DomainDecomposition/3D/src/ns_solver/ns_ppe_mg_solver.f90:136-150"), in
+// that operation order (products rounded, then the sum)
+__global__ void k_guess_update(const double* __restrict__ p, double* __restrict__ ph, size_t n,
+                               double w) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    ph[q] = __dadd_rn(__dmul_rn(w, p[q]), __dmul_rn(1.0 - w, ph[q]));
+}
+
 }  // namespace
 
 void launch_psplit_rhs(cudaStream_t s, int nx, int ny, int nz, const double* rho, Strided u,
@@ -175,6 +187,10 @@ void launch_psplit_rhs(cudaStream_t s, int nx, int ny, int nz, const double* rho
       nx, ny, nz, rho, u, v, w, ph, rho12, make_double3(dx, dy, dz),
       make_double3(1.0 / dx, 1.0 / dy, 1.0 / dz), make_double3(dx * dx, dy * dy, dz * dz),
       pow2_mask(dx, dy, dz), dt, src);
+}
+
+void launch_guess_update(cudaStream_t s, const double* p, double* ph, size_t n, double w) {
+  k_guess_update<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(p, ph, n, w);
 }
 
 void launch_psplit_correct(cudaStream_t s, int nx, int ny, int nz, const double* rho,

@@ -117,13 +117,14 @@ class PressurePoisson:
     "cycle" replays one graph per cycle and tests on the host, False launches
     each kernel.  inner_cycles: FP32 V-cycles per double-word defect
     correction of the stationary mixed loop (0: two, one under the increment
-    rule).
+    rule).  split_restarts: the DomainDecomposition driver's restarts of a
+    stagnating cycle in ppe_mg_solver (at most that many; 0: none).
     """
 
     def __init__(self, shape, spacing, precision="fp64", nu1=2, nu2=2, levels=0, coarse_max=64,
                  max_cycles=100, krylov=False, use_graph=True, remove_rhs_mean=True, certify=True,
                  device=None, stream=None, stop_rule="relative", zero_wall_faces=False,
-                 inner_cycles=0):
+                 inner_cycles=0, split_restarts=0):
         if len(shape) == 2:
             shape = (1,) + tuple(shape)
         self.shape = tuple(int(s) for s in shape)
@@ -142,6 +143,7 @@ class PressurePoisson:
         prm.krylov = _krylov_mode(krylov)
         prm.use_graph = {True: 1, False: 0, "loop": 1, "cycle": 2}.get(use_graph, use_graph)
         prm.inner_cycles = int(inner_cycles)
+        prm.split_restarts = int(split_restarts)
         prm.remove_rhs_mean = int(bool(remove_rhs_mean))
         prm.certify = int(bool(certify))
         prm.stop_rule = {"relative": _lib.GBMG_STOP_RELATIVE, "rms": _lib.GBMG_STOP_RMS,

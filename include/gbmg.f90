@@ -29,13 +29,13 @@ module gbmg
     integer(c_int32_t) :: precision, nu1, nu2, levels, coarse_max, max_cycles
     integer(c_int32_t) :: krylov, use_graph, remove_rhs_mean, certify, device
     type(c_ptr)        :: stream
-    integer(c_int32_t) :: stop_rule, zero_wall_faces, inner_cycles
+    integer(c_int32_t) :: stop_rule, zero_wall_faces, inner_cycles, split_restarts
   end type
 
   type, bind(c) :: gbmg_stats
     integer(c_int32_t) :: status, cycles, levels, coarse_n
     real(c_double)     :: rel_residual, rms_residual, res0, ms, bytes, increment
-    integer(c_int32_t) :: device_loop
+    integer(c_int32_t) :: device_loop, restarts
   end type
 
   type, bind(c) :: gbmg_field

@@ -105,6 +105,15 @@ typedef struct {
   int32_t inner_cycles;    /* mixed precision, stationary loop: FP32 V-cycles per double-word
                               defect correction (the residual is tested after each correction);
                               0 (default) = 2, or 1 under GBMG_STOP_INCREMENT; at most 8 */
+  int32_t split_restarts;  /* gbmg_project_split, stationary cycle: the DomainDecomposition
+                              driver's restarts ("DomainDecomposition/3D/src/ns_solver/
+                              ns_ppe_mg_solver.f90:29-44"): a cycle that does not cut the
+                              residual by 1% (or raises it) ends the solve, p^ becomes
+                              1.5 p - 0.5 p^, the source is rebuilt and the solve starts again
+                              from the new p^, at most split_restarts times; after the last one
+                              a stagnating cycle stops once the residual is under 1000 tol.
+                              One V-cycle per iteration (also in mixed precision); 0 (default):
+                              no restarts; at most 100 */
 } gbmg_params;
 
 typedef struct {
@@ -120,6 +129,8 @@ typedef struct {
   double increment;     /* GBMG_STOP_INCREMENT: max |p_k - p_(k-1)| of the last cycle (the
                            reference's ppe_linf); 0 under the other rules */
   int32_t device_loop;  /* 1: the cycles ran as one graph with the stopping tests on the device */
+  int32_t restarts;     /* gbmg_project_split with split_restarts: restarts made (cycles counts
+                           all of them) */
 } gbmg_stats;
 
 typedef struct {
@@ -190,9 +201,11 @@ int gbmg_project(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w, gbmg_
  * folded); gbmg_set_rho/phi/coef switch back.  gbmg_project_split starts the
  * solve from p_hat (the reference extrapolates p_hat = 2 p^n - p^{n-1} after
  * its third step and uses p^n before) and writes the mean-free pressure to
- * p; wall faces of u, v, w are left as given.  The reference's restarts of a
- * stagnating stationary cycle (ns_ppe_mg_solver.f90:29-44) are not needed:
- * the solve runs to the relative residual tol. */
+ * p; wall faces of u, v, w are left as given.  By default the solve runs to
+ * tol under the handle's stop rule; with gbmg_params.split_restarts > 0 it
+ * follows the reference driver's restarts of a stagnating cycle
+ * (ns_ppe_mg_solver.f90:29-44: p_hat <- 1.5 p - 0.5 p_hat and the source
+ * rebuilt), and the correction uses the last p_hat. */
 int gbmg_set_split(gbmg_handle* h, gbmg_field rho, double rho_12, int mem);
 int gbmg_project_split(gbmg_handle* h, gbmg_field u, gbmg_field v, gbmg_field w,
                        gbmg_field p_hat, gbmg_field p, double dt, double tol, int mem,
