@@ -214,6 +214,12 @@ int reset_graphs(gbmg_handle* h) {
       h->graph[k][par] = nullptr;
       h->graph_kernels[k][par] = 0;
     }
+  for (int k = 0; k < 3; ++k)
+    for (int par = 0; par < 2; ++par) {
+      if (h->tail_graph[k][par]) cudaGraphExecDestroy(h->tail_graph[k][par]);
+      h->tail_graph[k][par] = nullptr;
+      h->tail_kernels[k][par] = 0;
+    }
   for (int k = 0; k < 4; ++k)
     for (int par = 0; par < 2; ++par) {
       if (h->loop_graph[k][par]) cudaGraphExecDestroy(h->loop_graph[k][par]);
@@ -633,12 +639,16 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true,
 }
 
 int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
-  if (!h->prm.use_graph || first || h->prof || (kind == kGraphMixed && cycles != h->inner)) {
+  // (mixed iterations of another length than inner: graphs for 1 and 2
+  // cycles, the adaptive tail; eager otherwise)
+  const bool tail = kind == kGraphMixed && cycles != h->inner;
+  if (!h->prm.use_graph || first || h->prof || (tail && cycles > 2)) {
     GB_TRY(enqueue_iteration(h, kind, first, true, cycles));
     return GBMG_OK;
   }
   const int par = kind == kGraphMixed ? h->pcur : 0;
-  cudaGraphExec_t& gx = h->graph[kind][par];
+  cudaGraphExec_t& gx = tail ? h->tail_graph[cycles][par] : h->graph[kind][par];
+  int64_t& gk = tail ? h->tail_kernels[cycles][par] : h->graph_kernels[kind][par];
   if (!gx) {
     cudaGraph_t g = nullptr;
     const int64_t before = h->launches;
@@ -654,7 +664,7 @@ int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
       if (g) cudaGraphDestroy(g);
       return GBMG_CUDA_ERROR;
     }
-    h->graph_kernels[kind][par] = h->launches - before;
+    gk = h->launches - before;
     h->launches = before;
     const cudaError_t ei = cudaGraphInstantiate(&gx, g, 0);
     cudaGraphDestroy(g);
@@ -665,7 +675,7 @@ int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
     }
   }
   GB_CUDA(h, cudaGraphLaunch(gx, h->stream));
-  h->launches += h->graph_kernels[kind][par];
+  h->launches += gk;
   return GBMG_OK;
 }
 
@@ -1065,9 +1075,14 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
     if (status == GBMG_NOT_CONVERGED && h->prm.krylov != 2) {
       double best = rel;
       int flat = 0;
+      // cycles of the next iteration (the adaptive mixed loop shortens the
+      // last correction to what tail_cycles predicts)
+      const bool adapt = kind == kGraphMixed && h->adaptive && !h->stag_mode;
+      int next = kind == kGraphMixed ? (h->stag_mode ? 1 : h->inner) : 1;
       while (cyc < h->prm.max_cycles) {
-        // every iteration but the first flexible-CG one: the loop on the device
-        if (!(pcg && cyc == 0)) {
+        // every iteration of full length but the first flexible-CG one: the
+        // loop on the device
+        if (!(pcg && cyc == 0) && next == (kind == kGraphMixed ? h->inner : 1)) {
           CycleCtl c{};
           c.scale = scale;
           c.tol = tol;
@@ -1079,6 +1094,8 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
           c.flat_stop = (kind == kGraphMixed && h->prm.certify) ? 1 : 0;
           c.cyc = cyc;
           c.flat = flat;
+          c.rel = rel;
+          c.adaptive = adapt ? 1 : 0;
           bool used = false;
           GB_TRY(run_loop(h, kind, &c, &used));
           if (used) {
@@ -1095,13 +1112,13 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
               else if (c.status == kCtlConverged) status = GBMG_OK;
               stalled = c.stalled != 0;
             }
-            // ended by a test, or too few cycles left for a whole iteration:
-            // those run below, one cycle at a time
+            // ended by a test, by the predicted last correction (run below),
+            // or with too few cycles left for a whole iteration (run below)
             if (status != GBMG_NOT_CONVERGED || stalled || cyc >= h->prm.max_cycles) break;
+            if (c.tail > 0) next = c.tail;
           }
         }
-        const int inner = h->stag_mode ? 1 : h->inner;
-        const int step = kind == kGraphMixed ? std::min(inner, h->prm.max_cycles - cyc) : 1;
+        const int step = kind == kGraphMixed ? std::min(next, h->prm.max_cycles - cyc) : 1;
         const double prev = rel;
         cyc += step;
         GB_TRY(run_iteration(h, kind, pcg && cyc == 1, step));
@@ -1138,6 +1155,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
           continue;
         }
         if (rel < tol) { status = GBMG_OK; break; }
+        if (adapt) next = tail_cycles(rel, prev, tol, step, h->inner);
         // The mixed cycle tracks its residual in double-word FP32; near the
         // tolerance that figure can level off while the FP64 residual is
         // already below it.  Four cycles without any decrease end the loop and
@@ -1375,13 +1393,14 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
     return GBMG_INVALID_ARG;
   }
   h->mixed = h->prm.precision == GBMG_PREC_MIXED;
-  // Two FP32 cycles per defect correction: the FP32 correction is good to
-  // about 1e-6 of its size, so a second cycle still gains its full factor,
-  // and one defect kernel in two is saved; the residual is tested every two
-  // cycles, so the count can exceed the per-cycle one by one.  The
+  // Several FP32 cycles per defect correction: the FP32 correction is good to
+  // about 1e-6 of its size, so later cycles still gain their full factor,
+  // and defect kernels are saved.  By default three per correction while
+  // the residual is far from the tolerance, then as many as tail_cycles
+  // predicts, so that the cycle count stays the per-cycle test's.  The
   // increment rule measures one cycle.
-  h->inner = h->prm.inner_cycles > 0 ? h->prm.inner_cycles
-                                     : (h->prm.stop_rule == GBMG_STOP_INCREMENT ? 1 : 2);
+  h->adaptive = h->prm.inner_cycles == 0 && h->prm.stop_rule != GBMG_STOP_INCREMENT;
+  h->inner = h->prm.inner_cycles > 0 ? h->prm.inner_cycles : (h->adaptive ? 3 : 1);
   if (h->prm.device >= 0) {
     if (h->prm.device >= ndev) { delete h; return GBMG_INVALID_ARG; }
     h->device = h->prm.device;

@@ -75,7 +75,29 @@ struct CycleCtl {
   int flat;          // cycles since the last new lowest residual
   int status;        // kCtlRunning / kCtlConverged / kCtlDiverged
   int stalled;       // the flat test ended the loop
+  int adaptive;      // end the loop when fewer than `step` cycles will do (tail_cycles)
+  int tail;          // ... and the cycles of that last correction
 };
+
+// Cycles the next correction needs, predicted from the last one: it took the
+// relative residual from prev to rel in s cycles, so a cycle multiplies it by
+// r = (rel/prev)^(1/s); the answer is the smallest k < step_max with
+// rel r^k < tol, i.e. rel^s (rel/prev)^k < tol^s (products only, so the host
+// and the device decide alike), else step_max.
+__host__ __device__ inline int tail_cycles(double rel, double prev, double tol, int s,
+                                           int step_max) {
+  const double ratio = rel / prev;
+  double q = 1.0, t = 1.0;
+  for (int i = 0; i < s; ++i) {
+    q *= rel;
+    t *= tol;
+  }
+  for (int k = 1; k < step_max; ++k) {
+    q *= ratio;
+    if (q < t) return k;
+  }
+  return step_max;
+}
 enum : int { kCtlRunning = 0, kCtlConverged = 1, kCtlDiverged = 2 };
 
 // Result slot assignment.

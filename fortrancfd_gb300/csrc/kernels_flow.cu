@@ -550,6 +550,7 @@ __global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
                             int has_next) {
   c->cyc += c->step;
   c->iters += 1;
+  const double prev = c->rel;
   const double r2 = result[kSlotNorm];
   const double rel = sqrt(r2) / c->scale;
   c->r2 = r2;
@@ -579,6 +580,13 @@ __global__ void k_cycle_ctl(CycleCtl* c, const double* __restrict__ result,
   }
   // stop before an iteration would pass the cycle limit (the host runs the
   // remaining cycles one at a time)
+  if (!stop && c->adaptive) {
+    const int k = tail_cycles(rel, prev, c->tol, c->step, c->step);
+    if (k < c->step) {
+      c->tail = k;
+      stop = 1;
+    }
+  }
   if (!stop && c->cyc + c->step > c->max_cycles) stop = 1;
   cudaGraphSetConditional(loop, stop ? 0u : 1u);
   if (has_next) cudaGraphSetConditional(next, stop ? 0u : 1u);
