@@ -214,7 +214,7 @@ int reset_graphs(gbmg_handle* h) {
       h->graph[k][par] = nullptr;
       h->graph_kernels[k][par] = 0;
     }
-  for (int k = 0; k < 3; ++k)
+  for (int k = 0; k < 4; ++k)
     for (int par = 0; par < 2; ++par) {
       if (h->tail_graph[k][par]) cudaGraphExecDestroy(h->tail_graph[k][par]);
       h->tail_graph[k][par] = nullptr;
@@ -639,10 +639,10 @@ int enqueue_iteration(gbmg_handle* h, int kind, bool first, bool to_host = true,
 }
 
 int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
-  // (mixed iterations of another length than inner: graphs for 1 and 2
+  // (mixed iterations of another length than inner: graphs for 1 to 3
   // cycles, the adaptive tail; eager otherwise)
   const bool tail = kind == kGraphMixed && cycles != h->inner;
-  if (!h->prm.use_graph || first || h->prof || (tail && cycles > 2)) {
+  if (!h->prm.use_graph || first || h->prof || (tail && cycles > 3)) {
     GB_TRY(enqueue_iteration(h, kind, first, true, cycles));
     return GBMG_OK;
   }
@@ -1395,12 +1395,13 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
   h->mixed = h->prm.precision == GBMG_PREC_MIXED;
   // Several FP32 cycles per defect correction: the FP32 correction is good to
   // about 1e-6 of its size, so later cycles still gain their full factor,
-  // and defect kernels are saved.  By default three per correction while
-  // the residual is far from the tolerance, then as many as tail_cycles
-  // predicts, so that the cycle count stays the per-cycle test's.  The
-  // increment rule measures one cycle.
+  // and defect kernels are saved.  By default four per correction while the
+  // residual is far from the tolerance (five left a warm start far from its
+  // solution above 1e-10), then as many as tail_cycles predicts, so that the
+  // cycle count stays the per-cycle test's.  The increment rule measures one
+  // cycle.
   h->adaptive = h->prm.inner_cycles == 0 && h->prm.stop_rule != GBMG_STOP_INCREMENT;
-  h->inner = h->prm.inner_cycles > 0 ? h->prm.inner_cycles : (h->adaptive ? 3 : 1);
+  h->inner = h->prm.inner_cycles > 0 ? h->prm.inner_cycles : (h->adaptive ? 4 : 1);
   if (h->prm.device >= 0) {
     if (h->prm.device >= ndev) { delete h; return GBMG_INVALID_ARG; }
     h->device = h->prm.device;

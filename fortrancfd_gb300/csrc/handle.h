@@ -78,8 +78,8 @@ struct gbmg_handle {
   int pcur = 0;  // which pw holds the current pressure
   int inner = 1;  // FP32 V-cycles per defect correction of the stationary mixed loop
   bool adaptive = false;  // ... the last correction as long as tail_cycles predicts
-  cudaGraphExec_t tail_graph[3][2] = {};  // mixed iterations of 1 and 2 cycles (adaptive tail)
-  int64_t tail_kernels[3][2] = {};
+  cudaGraphExec_t tail_graph[4][2] = {};  // mixed iterations of 1 to 3 cycles (adaptive tail)
+  int64_t tail_kernels[4][2] = {};
   // the split driver's stagnation test (set by gbmg_project_split): 0 off; 1 a
   // cycle that cuts the residual by under 1% (or raises it) ends the loop
   // (stagnated = true); 2 after the last restart: such a cycle ends it once

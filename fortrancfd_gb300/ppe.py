@@ -116,7 +116,7 @@ class PressurePoisson:
     cycle loop as one CUDA graph with the stopping tests on the device,
     "cycle" replays one graph per cycle and tests on the host, False launches
     each kernel.  inner_cycles: FP32 V-cycles per double-word defect
-    correction of the stationary mixed loop (0: three, the last correction
+    correction of the stationary mixed loop (0: four, the last correction
     as many as predicted to reach tol; one under the increment rule).  split_restarts: the DomainDecomposition driver's restarts of a
     stagnating cycle in ppe_mg_solver (at most that many; 0: none).
     """

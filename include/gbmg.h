@@ -104,7 +104,7 @@ typedef struct {
                               are read as given */
   int32_t inner_cycles;    /* mixed precision, stationary loop: FP32 V-cycles per double-word
                               defect correction (the residual is tested after each correction);
-                              0 (default): three, and for the last correction the number the
+                              0 (default): four, and for the last correction the number the
                               last reduction predicts will reach tol (one under
                               GBMG_STOP_INCREMENT); 1..8: that many; at most 8 */
   int32_t split_restarts;  /* gbmg_project_split, stationary cycle: the DomainDecomposition

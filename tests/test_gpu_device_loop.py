@@ -81,7 +81,7 @@ def test_device_loop_warm_start_mixed(cuda):
 def test_fp32_cycles_per_defect_correction(cuda):
     """inner_cycles: FP32 V-cycles per double-word defect correction.  Every
     setting reaches the tolerance in FP64 (certified) with the same solution
-    to 1e-9; a fixed count tests every that many cycles; the default (three,
+    to 1e-9; a fixed count tests every that many cycles; the default (four,
     the last correction as many as the last reduction predicts) takes at most
     one cycle more than one cycle per correction."""
     from fortrancfd_gb300 import GBMGError
