@@ -409,8 +409,9 @@ def test_density_form_coefficients(cuda, monkeypatch, idx, scale, krylov):
     against the stored FP32 coefficients (GBMG_RHO_COEF=0): the FP32 values
     differ by a few ulp, so the preconditioner changes slightly; both solves
     reach the tolerance, agree with the FP64 oracle to tol-scaled accuracy and
-    take the same number of cycles to within one iteration (the stationary
-    loop tests its residual every two cycles, one per defect correction)."""
+    take the same number of cycles to within two (the stationary loop tests
+    its residual once per defect correction, whose length it predicts from
+    the last one)."""
     c = cases.config(idx, scale)
     out = {}
     for flag in ("0", "1"):
