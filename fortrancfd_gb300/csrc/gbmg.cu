@@ -684,7 +684,7 @@ int run_iteration(gbmg_handle* h, int kind, bool first, int cycles = 1) {
 // device and ends the loop, so the host waits once per solve instead of once
 // per cycle.  The mixed iteration alternates its two p buffers, so its body is
 // the iteration from buffer par, the controller, then (an IF node on that
-// controller's verdict) the iteration from the other buffer and the
+// controller's decision) the iteration from the other buffer and the
 // controller again.  Leaves h->loop_graph[kind][par] null, and sets
 // h->loop_off, when the graph cannot be built (the host loop then runs).
 int build_loop(gbmg_handle* h, int kind, int par) {
@@ -1159,7 +1159,7 @@ int solve_internal(gbmg_handle* h, double tol, double bnorm, gbmg_stats* st) {
         // The mixed cycle tracks its residual in double-word FP32; near the
         // tolerance that figure can level off while the FP64 residual is
         // already below it.  Four cycles without any decrease end the loop and
-        // leave the verdict to the FP64 certification below.
+        // leave the decision to the FP64 certification below.
         if (kind == kGraphMixed && h->prm.certify) {
           if (rel < best) {
             best = rel;
