@@ -7,6 +7,7 @@
 // has the same index map and alignment.
 #pragma once
 
+#include "schedule.h"
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -79,25 +80,7 @@ struct CycleCtl {
   int tail;          // ... and the cycles of that last correction
 };
 
-// Cycles the next correction needs, predicted from the last one: it took the
-// relative residual from prev to rel in s cycles, so a cycle multiplies it by
-// r = (rel/prev)^(1/s); the answer is the smallest k < step_max with
-// rel r^k < tol, i.e. rel^s (rel/prev)^k < tol^s (products only, so the host
-// and the device decide alike), else step_max.
-__host__ __device__ inline int tail_cycles(double rel, double prev, double tol, int s,
-                                           int step_max) {
-  const double ratio = rel / prev;
-  double q = 1.0, t = 1.0;
-  for (int i = 0; i < s; ++i) {
-    q *= rel;
-    t *= tol;
-  }
-  for (int k = 1; k < step_max; ++k) {
-    q *= ratio;
-    if (q < t) return k;
-  }
-  return step_max;
-}
+// tail_cycles (the adaptive mixed loop's schedule): schedule.h
 enum : int { kCtlRunning = 0, kCtlConverged = 1, kCtlDiverged = 2 };
 
 // Result slot assignment.
