@@ -1370,6 +1370,19 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
   if (grid->nx < 1 || grid->ny < 1 || grid->nz < 1 || !(grid->dx > 0) || !(grid->dy > 0) ||
       (grid->nz > 1 && !(grid->dz > 0)))
     return GBMG_INVALID_ARG;
+  // the parameters are checked before any CUDA call
+  gbmg_params P;
+  if (prm) P = *prm; else gbmg_default_params(&P);
+  if (P.nu1 < 0 || P.nu2 < 0 || P.max_cycles < 1 || P.coarse_max < 1 ||
+      P.coarse_max > kMaxCoarse ||
+      (P.precision != GBMG_PREC_FP64 && P.precision != GBMG_PREC_MIXED) ||
+      P.stop_rule < GBMG_STOP_RELATIVE || P.stop_rule > GBMG_STOP_INCREMENT ||
+      (P.stop_rule == GBMG_STOP_INCREMENT && P.krylov != 0) ||
+      (P.zero_wall_faces != 0 && P.zero_wall_faces != 1) || P.use_graph < 0 ||
+      P.use_graph > 2 || P.inner_cycles < 0 || P.inner_cycles > 8 || P.split_restarts < 0 ||
+      P.split_restarts > 100 || (P.split_restarts > 0 && P.krylov != 0) ||
+      (P.inner_cycles > 1 && P.stop_rule == GBMG_STOP_INCREMENT))
+    return GBMG_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
     cudaGetLastError();
@@ -1378,20 +1391,7 @@ int gbmg_create(const gbmg_grid* grid, const gbmg_params* prm, gbmg_handle** out
   gbmg_handle* h = new gbmg_handle();
   h->grid = *grid;
   if (h->grid.nz == 1 && !(h->grid.dz > 0)) h->grid.dz = 1.0;
-  if (prm) h->prm = *prm; else gbmg_default_params(&h->prm);
-  if (h->prm.nu1 < 0 || h->prm.nu2 < 0 || h->prm.max_cycles < 1 || h->prm.coarse_max < 1 ||
-      h->prm.coarse_max > kMaxCoarse || (h->prm.precision != GBMG_PREC_FP64 &&
-                                         h->prm.precision != GBMG_PREC_MIXED) ||
-      h->prm.stop_rule < GBMG_STOP_RELATIVE || h->prm.stop_rule > GBMG_STOP_INCREMENT ||
-      (h->prm.stop_rule == GBMG_STOP_INCREMENT && h->prm.krylov != 0) ||
-      (h->prm.zero_wall_faces != 0 && h->prm.zero_wall_faces != 1) || h->prm.use_graph < 0 ||
-      h->prm.use_graph > 2 || h->prm.inner_cycles < 0 || h->prm.inner_cycles > 8 ||
-      h->prm.split_restarts < 0 || h->prm.split_restarts > 100 ||
-      (h->prm.split_restarts > 0 && h->prm.krylov != 0) ||
-      (h->prm.inner_cycles > 1 && h->prm.stop_rule == GBMG_STOP_INCREMENT)) {
-    delete h;
-    return GBMG_INVALID_ARG;
-  }
+  h->prm = P;
   h->mixed = h->prm.precision == GBMG_PREC_MIXED;
   // Several FP32 cycles per defect correction: the FP32 correction is good to
   // about 1e-6 of its size, so later cycles still gain their full factor,

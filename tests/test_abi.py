@@ -55,6 +55,38 @@ def test_null_and_invalid_arguments_return_codes():
     assert L.gbmg_kernel_launches(None) == 0
 
 
+@pytest.mark.parametrize("field,value", [
+    ("nu1", -1), ("max_cycles", 0), ("coarse_max", 65), ("precision", 7), ("stop_rule", 3),
+    ("zero_wall_faces", 2), ("use_graph", 3), ("inner_cycles", 9), ("split_restarts", -1),
+    ("split_restarts", 101)])
+def test_invalid_parameters_are_rejected_before_any_device_call(field, value):
+    """gbmg_create checks its parameters before it asks for a device, so these
+    run without a GPU (and give the same code with one)."""
+    L = _lib.load()
+    prm = _lib.Params()
+    L.gbmg_default_params(C.byref(prm))
+    setattr(prm, field, value)
+    h = C.c_void_p()
+    g = _lib.Grid(8, 8, 8, 0.125, 0.125, 0.125)
+    assert L.gbmg_create(C.byref(g), C.byref(prm), C.byref(h)) == _lib.GBMG_INVALID_ARG
+    assert not h.value
+
+
+@pytest.mark.parametrize("combo", [
+    {"stop_rule": 2, "krylov": 1},          # the increment rule with a Krylov iteration
+    {"stop_rule": 2, "inner_cycles": 2},    # ... or with several FP32 cycles per correction
+    {"split_restarts": 5, "krylov": 2}])    # the split driver's restarts with a Krylov iteration
+def test_invalid_parameter_combinations_are_rejected(combo):
+    L = _lib.load()
+    prm = _lib.Params()
+    L.gbmg_default_params(C.byref(prm))
+    for k, v in combo.items():
+        setattr(prm, k, v)
+    h = C.c_void_p()
+    g = _lib.Grid(8, 8, 8, 0.125, 0.125, 0.125)
+    assert L.gbmg_create(C.byref(g), C.byref(prm), C.byref(h)) == _lib.GBMG_INVALID_ARG
+
+
 def test_create_without_device_reports_no_device():
     try:
         import torch
